@@ -1,0 +1,231 @@
+/*
+ * sdm_capi.h -- C ABI of the GB300 (sm_103a) SDM two-state force.
+ *
+ * One call evaluates, for every replica (lambda state) of every registered
+ * system, what one step of the reference's SDM integrator computes on the
+ * nonbonded force group:
+ *
+ *   U0, F0   at the original coordinates x
+ *            (reference: calcForcesAndEnergy(true,true,4) followed by SaveState1,
+ *             openmmapi/src/LangevinIntegratorSDM.cpp:159-162)
+ *   U1, F1   at the displaced coordinates x+d
+ *            (MakeState2 + calcForcesAndEnergy + SaveState2 + RestoreState1,
+ *             LangevinIntegratorSDM.cpp:165-173; displacement
+ *             platforms/reference/src/ReferenceSDMKernels.cpp:192-199)
+ *   u = U1-U0, u' = SoftCoreF(u), W(u'), W'(u'), E_pot = U0 + W
+ *            (LangevinIntegratorSDM.cpp:125-149; ReferenceSDMKernels.cpp:247-287)
+ *   F = (1-s) F0 + s F1 with s = W' * du'/du
+ *            (ReferenceSDMKernels.cpp:309-318; OpenCL sdmForce, langevin.cl:72-87)
+ *   dW/dlambda of the non-equilibrium schedule
+ *            (ReferenceSDMKernels.cpp:231-245,289-302)
+ *
+ * The Langevin update and the group-1 (bonded/restraint) forces stay with the
+ * caller: the caller adds its own group-1 energy to E_pot and its group-1
+ * forces to F, exactly as the reference adds them at
+ * ReferenceSDMKernels.cpp:283 and :315-317.
+ *
+ * Nonbonded model (the part of OpenMM's NonbondedForce the reference calls
+ * with CutoffPeriodic + reaction field, example/desmonddmsfile75.py:424-438):
+ * Lennard-Jones (Lorentz-Berthelot mixing, truncated, unshifted) plus
+ * reaction-field Coulomb, orthorhombic periodic box, excluded pairs skipped,
+ * no dispersion correction.
+ *
+ * Conventions: nm, kJ/mol, e.  Coordinates, energies and forces are FP64 at
+ * the ABI.  Pair arithmetic is FP32 on the GPU, forces accumulate in 64-bit
+ * fixed point (scale 2^32, the OpenMM-CUDA convention), energies in FP64.
+ * Replicas are numbered system by system: system 0's replicas first.
+ * No function throws; every function returns an sdm_status.  One host
+ * thread per handle at a time.
+ */
+#ifndef SDM_CAPI_H
+#define SDM_CAPI_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int sdm_status;
+enum {
+    SDM_OK = 0,
+    SDM_ERR_INVALID_ARGUMENT = 1,  /* bad pointer, size, index or parameter */
+    SDM_ERR_CUDA = 2,              /* a CUDA runtime call failed; see sdm_last_error */
+    SDM_ERR_NO_DEVICE = 3,         /* no usable sm_103 device */
+    SDM_ERR_OVERFLOW = 4,          /* fixed-point force overflow or non-finite pair term */
+    SDM_ERR_CAPACITY = 5,          /* a diagnostic buffer was too small */
+    SDM_ERR_UNKNOWN_METHOD = 6,    /* bias or soft-core method id not 0,1,2 */
+    SDM_ERR_TIMEOUT = 7            /* a bounded device wait expired */
+};
+
+/* Bias and soft-core method ids: the reference's integer constants
+ * (openmmapi/include/LangevinIntegratorSDM.h:120-122 and :143-145). */
+enum { SDM_LINEAR = 0, SDM_QUADRATIC = 1, SDM_ILOGISTIC = 2 };
+enum { SDM_NO_SOFTCORE = 0, SDM_TANH_SOFTCORE = 1, SDM_RATIONAL_SOFTCORE = 2 };
+
+/* Per-replica SDM parameters, SDM_NPARAMS doubles in this order.  Each field
+ * is the value of the reference integrator setter named beside it
+ * (openmmapi/include/LangevinIntegratorSDM.h). */
+enum {
+    SDM_P_BIAS_METHOD = 0,      /* setBiasMethod        :127 */
+    SDM_P_SOFTCORE_METHOD = 1,  /* setSoftCoreMethod    :146 */
+    SDM_P_LAMBDA = 2,           /* setLambda            :75  (Linear slope; t/Ntmax when non-equilibrium) */
+    SDM_P_LAMBDA1 = 3,          /* setLambda1           :212 */
+    SDM_P_LAMBDA2 = 4,          /* setLambda2           :218 */
+    SDM_P_ALPHA = 5,            /* setAlpha             :224 (1/(kJ/mol)) */
+    SDM_P_U0 = 6,               /* setU0                :230 */
+    SDM_P_W0 = 7,               /* setW0coeff           :196 */
+    SDM_P_GAMMA = 8,            /* setGamma             :161 */
+    SDM_P_WB = 9,               /* setWBcoeff           :178 */
+    SDM_P_UMAX = 10,            /* setUmax              :350 */
+    SDM_P_ACORE = 11,           /* setAcore             :359 */
+    SDM_P_UBCORE = 12,          /* setUbcore            :369 */
+    SDM_P_NONEQ = 13,           /* setNonEquilibrium    :393 */
+    SDM_P_M_LAMBDA1 = 14,       /* setlambda1Slope      :403 */
+    SDM_P_M_LAMBDA2 = 15,       /* setlambda2Slope      :409 */
+    SDM_P_M_U0 = 16,            /* setu0Slope           :415 */
+    SDM_P_M_W0 = 17,            /* setw0Slope           :421 */
+    SDM_P_B_LAMBDA1 = 18,       /* setlambda1intercept  :427 */
+    SDM_P_B_LAMBDA2 = 19,       /* setlambda2intercept  :433 */
+    SDM_P_B_U0 = 20,            /* setu0intercept       :439 */
+    SDM_P_B_W0 = 21,            /* setw0intercept       :445 */
+    SDM_NPARAMS = 22
+};
+
+/* Per-replica results, SDM_NRESULTS doubles in this order. */
+enum {
+    SDM_R_U0 = 0,        /* state-1 (original coordinates) nonbonded energy */
+    SDM_R_U1 = 1,        /* state-2 (displaced coordinates) nonbonded energy = U0 + u */
+    SDM_R_U = 2,         /* perturbation energy u = U1 - U0, accumulated directly */
+    SDM_R_BINDE = 3,     /* u' = SoftCoreF(u): the reference's getBindE() */
+    SDM_R_FP = 4,        /* du'/du */
+    SDM_R_W = 5,         /* bias energy W(u') ("ebias") */
+    SDM_R_DW = 6,        /* W'(u') ("bfp") */
+    SDM_R_S = 7,         /* force mixing weight s = W' * du'/du ("sp") */
+    SDM_R_EPOT = 8,      /* U0 + W: the reference's getPotEnergy() without group 1 */
+    SDM_R_DWDLAMBDA = 9, /* non-equilibrium dW/dlambda (0 unless SDM_P_NONEQ == 1) */
+    SDM_R_LAMBDA1 = 10,  /* parameters actually used (after the non-equilibrium schedule) */
+    SDM_R_LAMBDA2 = 11,
+    SDM_R_U0PARAM = 12,
+    SDM_R_W0PARAM = 13,
+    SDM_R_STATUS = 14,   /* device status bits of this call (0 = clean) */
+    SDM_R_RESERVED = 15,
+    SDM_NRESULTS = 16
+};
+
+typedef struct sdm_handle sdm_handle;
+
+/* Topology of one system.  All arrays are read during sdm_create only. */
+typedef struct {
+    int num_particles;
+    const double* charge;        /* [num_particles] e */
+    const double* sigma;         /* [num_particles] nm */
+    const double* epsilon;       /* [num_particles] kJ/mol */
+    int num_exclusions;          /* excluded pairs (each unordered pair once) */
+    const int* exclusions;       /* [2*num_exclusions] particle indices */
+    const double* displacement;  /* [3*num_particles] nm, NULL = all zero */
+    double box[3];               /* orthorhombic periodic box edges, nm */
+    double cutoff;               /* nm; must satisfy cutoff < box/2 in every axis */
+    double reaction_field_dielectric;
+    int num_replicas;            /* coordinate sets (lambda states) per call, >= 1 */
+} sdm_system_desc;
+
+/* Creates a handle for num_systems systems on CUDA device `device`, owning all
+ * device memory and one CUDA stream.  Replaces the reference's kernel
+ * construction and initialize(): ReferenceSDMKernelFactory.cpp:58-63,
+ * ReferenceSDMKernels.cpp:144-159, OpenCLSDMKernels.cpp:73-133. */
+sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int device,
+                      sdm_handle** out);
+
+/* Releases every resource of the handle.  NULL is accepted. */
+sdm_status sdm_destroy(sdm_handle* h);
+
+/* Message of the last failing call on this handle ("" if none).  With a NULL
+ * handle: the message of the last failing sdm_create on this thread. */
+const char* sdm_last_error(const sdm_handle* h);
+
+/* Number of replicas over all systems. */
+sdm_status sdm_num_replicas(const sdm_handle* h, int* out);
+
+/* Replaces the displacement map of one system ([3*num_particles] nm).
+ * Reference: LangevinIntegratorSDM::setDisplacement
+ * (openmmapi/include/LangevinIntegratorSDM.h:467) with the upload of
+ * OpenCLSDMKernels.cpp:86-97. */
+sdm_status sdm_set_displacement(sdm_handle* h, int system, const double* displacement);
+
+/* Sets the SDM parameters of one replica (SDM_NPARAMS doubles, see above).
+ * Rejects unknown bias/soft-core method ids with SDM_ERR_UNKNOWN_METHOD (the
+ * reference throws "Unknown soft core method", LangevinIntegratorSDM.cpp:147). */
+sdm_status sdm_set_params(sdm_handle* h, int replica, const double* params);
+
+/* Host-buffer evaluation of all replicas.
+ *   x        [sum over replicas of 3*num_particles] FP64 coordinates
+ *   results  [num_replicas * SDM_NRESULTS] (may be NULL)
+ *   forces   [sum over replicas of 3*num_particles] mixed force F (may be NULL)
+ * Copies in, evaluates, copies out and synchronises.  Replaces one SDM step's
+ * force part: LangevinIntegratorSDM.cpp:158-176 with
+ * ReferenceSDMKernels.cpp:202-318 (minus the Langevin update). */
+sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double* forces);
+
+/* Device-buffer evaluation, asynchronous on `stream` (a cudaStream_t, NULL =
+ * the handle's own stream).  x/results/forces are device pointers with the
+ * sizes of sdm_evaluate.  With graph mode on (default), the launch sequence is
+ * captured once per distinct (x, results, forces, stream) tuple and replayed
+ * as a CUDA graph. */
+sdm_status sdm_evaluate_device(sdm_handle* h, const double* x, double* results, double* forces,
+                               void* stream);
+
+/* Per-state forces of the last evaluation (device pointers or host pointers
+ * selected by `on_device`): F0 and F1 = F0 + dF, [sum 3*num_particles] each. */
+sdm_status sdm_get_state_forces(sdm_handle* h, double* F0, double* F1, int on_device);
+
+/* Reads and clears the device status word (SDM_DEV_* bits).  Synchronises. */
+sdm_status sdm_check_status(sdm_handle* h, int* device_status);
+
+/* Options. */
+enum {
+    SDM_OPT_GRAPH = 0,        /* 1 = capture/replay CUDA graphs in sdm_evaluate_device (default 1) */
+    SDM_OPT_PROFILE = 1,      /* 1 = time every kernel with CUDA events (disables graphs) */
+    SDM_OPT_SPLIT = 2,        /* work items per i-cluster in the pair kernel (1,2,4) */
+    SDM_OPT_CTAS_PER_SM = 3,  /* persistent pair-kernel CTAs per SM (1..8) */
+    SDM_OPT_VERIFY = 4        /* 1 = sdm_evaluate checks the device status word after each call */
+};
+sdm_status sdm_set_option(sdm_handle* h, int option, int value);
+sdm_status sdm_get_option(const sdm_handle* h, int option, int* value);
+
+/* Kernel timings of the last profiled evaluation: names[i] (static strings)
+ * and ms[i] for i < *count (in: capacity, out: entries). */
+sdm_status sdm_get_kernel_times(const sdm_handle* h, const char** names, float* ms, int* count);
+
+/* Tries every schedule candidate (split x CTAs per SM) on coordinates x
+ * (device pointer) and keeps the fastest; writes the choice to split/ctas. */
+sdm_status sdm_autotune(sdm_handle* h, const double* x_device, int* split, int* ctas_per_sm);
+
+/* Interaction counts of coordinates x (host pointer) under the kernels' own
+ * pair rule: counts[2*r] = P0 (pairs within the cutoff at x), counts[2*r+1] =
+ * P1delta (pairs within the cutoff at x+d whose displacements differ). */
+sdm_status sdm_count_pairs(sdm_handle* h, const double* x, long long* counts);
+
+/* Cell grid of one system: M[0..2] cells per axis (columns are M[0]*M[1]). */
+sdm_status sdm_get_grid(const sdm_handle* h, int system, int* M);
+
+/* Diagnostic export of the clustering and neighbour lists of replica
+ * `replica` for coordinates x (host pointer, that replica's 3*num_particles):
+ *   perm[cap_slots]                slot -> particle (-1 = padding)
+ *   ncl                            clusters
+ *   cnt[cap_clusters]              list entries per i-cluster
+ *   ent_slot/ent_mask[cap_clusters*cap_per_cluster]  (j slot, allowed-i bits)
+ * Returns SDM_ERR_CAPACITY if a capacity is too small. */
+sdm_status sdm_export_lists(sdm_handle* h, int replica, const double* x, int cap_slots,
+                            int cap_clusters, int cap_per_cluster, int* perm, int* ncl, int* cnt,
+                            int* ent_slot, unsigned char* ent_mask);
+
+/* Device status bits (sdm_check_status, SDM_R_STATUS). */
+enum {
+    SDM_DEV_FORCE_OVERFLOW = 1,   /* |force term| >= 2^31 kJ/mol/nm or NaN */
+    SDM_DEV_ENERGY_NONFINITE = 2, /* NaN/Inf energy */
+    SDM_DEV_EXCL_OVERFLOW = 4     /* internal exclusion table overflow (should not happen) */
+};
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDM_CAPI_H */

@@ -1,0 +1,13 @@
+"""GB300-native (sm_103a) Single-Decoupling (SDM) two-state force.
+
+Public surface:
+  * :mod:`.capi`     ctypes binding of the C ABI (include/sdm_capi.h)
+  * :class:`SDMForce` host mirror of the reference's SDM parameter API
+  * :mod:`.systems`  seeded synthetic systems
+  * :mod:`.build`    in-tree build of the CUDA library
+"""
+from . import systems  # noqa: F401
+from .capi import Handle, SdmError, load_library  # noqa: F401
+from .force import SDMForce, force_from_system  # noqa: F401
+
+__all__ = ["systems", "Handle", "SdmError", "load_library", "SDMForce", "force_from_system"]

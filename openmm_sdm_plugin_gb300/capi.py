@@ -1,0 +1,257 @@
+"""ctypes binding of the C ABI in ``include/sdm_capi.h``.
+
+The shared library is the in-tree ``libsdm_gb300.so`` built by
+``openmm_sdm_plugin_gb300.build``.  There is no fallback: if the library is
+missing or cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsdm_gb300.so")
+
+# status codes
+SDM_OK = 0
+SDM_ERR_INVALID_ARGUMENT = 1
+SDM_ERR_CUDA = 2
+SDM_ERR_NO_DEVICE = 3
+SDM_ERR_OVERFLOW = 4
+SDM_ERR_CAPACITY = 5
+SDM_ERR_UNKNOWN_METHOD = 6
+SDM_ERR_TIMEOUT = 7
+
+NPARAMS = 22
+NRESULTS = 16
+RESULT_FIELDS = ("U0", "U1", "u", "BindE", "fp", "W", "dW", "s", "E_pot", "dWdlambda",
+                 "lambda1", "lambda2", "u0", "w0", "status", "nclusters")
+(R_U0, R_U1, R_U, R_BINDE, R_FP, R_W, R_DW, R_S, R_EPOT, R_DWDL, R_L1, R_L2, R_U0P, R_W0P,
+ R_STATUS, R_NCL) = range(16)
+
+OPT_GRAPH, OPT_PROFILE, OPT_SPLIT, OPT_CTAS_PER_SM, OPT_VERIFY = range(5)
+
+EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
+            "sdm_set_displacement", "sdm_set_params", "sdm_evaluate", "sdm_evaluate_device",
+            "sdm_get_state_forces", "sdm_check_status", "sdm_set_option", "sdm_get_option",
+            "sdm_get_kernel_times", "sdm_autotune", "sdm_count_pairs", "sdm_get_grid",
+            "sdm_export_lists")
+
+
+class SdmError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"sdm status {status}: {message}")
+        self.status = status
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [
+        ("num_particles", C.c_int),
+        ("charge", C.POINTER(C.c_double)),
+        ("sigma", C.POINTER(C.c_double)),
+        ("epsilon", C.POINTER(C.c_double)),
+        ("num_exclusions", C.c_int),
+        ("exclusions", C.POINTER(C.c_int)),
+        ("displacement", C.POINTER(C.c_double)),
+        ("box", C.c_double * 3),
+        ("cutoff", C.c_double),
+        ("reaction_field_dielectric", C.c_double),
+        ("num_replicas", C.c_int),
+    ]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads (once) and returns the CDLL with argument types declared."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise RuntimeError(f"CUDA library {path} is missing: run openmm_sdm_plugin_gb300.build.build()")
+        L = C.CDLL(path)
+        vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+        L.sdm_create.argtypes = [C.POINTER(SystemDesc), C.c_int, C.c_int, C.POINTER(vp)]
+        L.sdm_destroy.argtypes = [vp]
+        L.sdm_last_error.argtypes = [vp]
+        L.sdm_last_error.restype = C.c_char_p
+        L.sdm_num_replicas.argtypes = [vp, ip]
+        L.sdm_set_displacement.argtypes = [vp, C.c_int, vp]
+        L.sdm_set_params.argtypes = [vp, C.c_int, vp]
+        L.sdm_evaluate.argtypes = [vp, vp, vp, vp]
+        L.sdm_evaluate_device.argtypes = [vp, vp, vp, vp, vp]
+        L.sdm_get_state_forces.argtypes = [vp, vp, vp, C.c_int]
+        L.sdm_check_status.argtypes = [vp, ip]
+        L.sdm_set_option.argtypes = [vp, C.c_int, C.c_int]
+        L.sdm_get_option.argtypes = [vp, C.c_int, ip]
+        L.sdm_get_kernel_times.argtypes = [vp, C.POINTER(C.c_char_p), C.POINTER(C.c_float), ip]
+        L.sdm_autotune.argtypes = [vp, vp, ip, ip]
+        L.sdm_count_pairs.argtypes = [vp, vp, vp]
+        L.sdm_get_grid.argtypes = [vp, C.c_int, ip]
+        L.sdm_export_lists.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, ip, vp, vp, vp]
+        for name in EXPORTED:
+            if name != "sdm_last_error":
+                getattr(L, name).restype = C.c_int
+        _lib = L
+        return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class Handle:
+    """Owning wrapper of one ``sdm_handle``.
+
+    ``systems`` is a list of :class:`openmm_sdm_plugin_gb300.systems.SDMSystem`
+    (or duck-typed objects with the same fields).
+    """
+
+    def __init__(self, systems, device: int = 0):
+        self.lib = load_library()
+        self.systems = list(systems)
+        self._keep = []
+        descs = (SystemDesc * len(self.systems))()
+        for k, s in enumerate(self.systems):
+            q = np.ascontiguousarray(s.charge, np.float64)
+            sg = np.ascontiguousarray(s.sigma, np.float64)
+            ep = np.ascontiguousarray(s.epsilon, np.float64)
+            ex = np.ascontiguousarray(np.asarray(s.exclusions, np.int32).reshape(-1))
+            dd = np.ascontiguousarray(np.asarray(s.displacement, np.float64).reshape(-1))
+            self._keep += [q, sg, ep, ex, dd]
+            d = descs[k]
+            d.num_particles = int(q.shape[0])
+            d.charge = q.ctypes.data_as(C.POINTER(C.c_double))
+            d.sigma = sg.ctypes.data_as(C.POINTER(C.c_double))
+            d.epsilon = ep.ctypes.data_as(C.POINTER(C.c_double))
+            d.num_exclusions = int(ex.shape[0] // 2)
+            d.exclusions = ex.ctypes.data_as(C.POINTER(C.c_int)) if ex.size else None
+            d.displacement = dd.ctypes.data_as(C.POINTER(C.c_double))
+            d.box[:] = [float(v) for v in s.box]
+            d.cutoff = float(s.cutoff)
+            d.reaction_field_dielectric = float(s.eps_rf)
+            d.num_replicas = int(s.positions.shape[0]) if getattr(s, "positions", None) is not None else 1
+        h = C.c_void_p()
+        st = self.lib.sdm_create(descs, len(self.systems), int(device), C.byref(h))
+        if st != SDM_OK:
+            raise SdmError(st, self.lib.sdm_last_error(None).decode())
+        self.h = h
+        n = C.c_int(0)
+        self.lib.sdm_num_replicas(self.h, C.byref(n))
+        self.nrep = n.value
+        self.rep_sys = []
+        self.rep_n = []
+        for k, s in enumerate(self.systems):
+            r = int(s.positions.shape[0]) if getattr(s, "positions", None) is not None else 1
+            self.rep_sys += [k] * r
+            self.rep_n += [int(s.charge.shape[0])] * r
+        self.total_particles = int(sum(self.rep_n))
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.sdm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != SDM_OK:
+            raise SdmError(st, self.lib.sdm_last_error(self.h).decode())
+
+    # -- configuration ----------------------------------------------------
+    def set_params(self, replica: int, params):
+        p = np.ascontiguousarray(np.asarray(params, np.float64).reshape(-1))
+        if p.size != NPARAMS:
+            raise ValueError(f"need {NPARAMS} parameters")
+        self._check(self.lib.sdm_set_params(self.h, int(replica), p.ctypes.data))
+
+    def set_displacement(self, system: int, d):
+        dd = np.ascontiguousarray(np.asarray(d, np.float64).reshape(-1))
+        self._check(self.lib.sdm_set_displacement(self.h, int(system), dd.ctypes.data))
+
+    def set_option(self, opt: int, value: int):
+        self._check(self.lib.sdm_set_option(self.h, int(opt), int(value)))
+
+    def get_option(self, opt: int) -> int:
+        v = C.c_int(0)
+        self._check(self.lib.sdm_get_option(self.h, int(opt), C.byref(v)))
+        return v.value
+
+    def grid(self, system: int = 0):
+        M = (C.c_int * 3)()
+        self._check(self.lib.sdm_get_grid(self.h, int(system), M))
+        return np.array(list(M), np.int32)
+
+    # -- evaluation -------------------------------------------------------
+    def evaluate(self, x, forces: bool = True):
+        """Host evaluation of all replicas. x: (total_particles, 3) float64."""
+        x = np.ascontiguousarray(np.asarray(x, np.float64).reshape(-1))
+        if x.size != 3 * self.total_particles:
+            raise ValueError("coordinate array has the wrong size")
+        res = np.zeros((self.nrep, NRESULTS))
+        f = np.zeros(3 * self.total_particles) if forces else None
+        self._check(self.lib.sdm_evaluate(self.h, x.ctypes.data, res.ctypes.data, _ptr(f)))
+        return res, (f.reshape(-1, 3) if forces else None)
+
+    def evaluate_device(self, x_ptr: int, res_ptr: int, f_ptr: int = 0, stream: int = 0):
+        self._check(self.lib.sdm_evaluate_device(self.h, C.c_void_p(x_ptr), C.c_void_p(res_ptr),
+                                                 C.c_void_p(f_ptr) if f_ptr else None,
+                                                 C.c_void_p(stream) if stream else None))
+
+    def state_forces(self):
+        F0 = np.zeros(3 * self.total_particles)
+        F1 = np.zeros(3 * self.total_particles)
+        self._check(self.lib.sdm_get_state_forces(self.h, F0.ctypes.data, F1.ctypes.data, 0))
+        return F0.reshape(-1, 3), F1.reshape(-1, 3)
+
+    def check_status(self) -> int:
+        v = C.c_int(0)
+        self._check(self.lib.sdm_check_status(self.h, C.byref(v)))
+        return v.value
+
+    def kernel_times(self):
+        names = (C.c_char_p * 16)()
+        ms = (C.c_float * 16)()
+        n = C.c_int(16)
+        self._check(self.lib.sdm_get_kernel_times(self.h, names, ms, C.byref(n)))
+        return {names[k].decode(): float(ms[k]) for k in range(n.value)}
+
+    def autotune(self, x_ptr: int):
+        sp, ct = C.c_int(0), C.c_int(0)
+        self._check(self.lib.sdm_autotune(self.h, C.c_void_p(x_ptr), C.byref(sp), C.byref(ct)))
+        return sp.value, ct.value
+
+    def count_pairs(self, x):
+        x = np.ascontiguousarray(np.asarray(x, np.float64).reshape(-1))
+        c = np.zeros(2 * self.nrep, np.int64)
+        self._check(self.lib.sdm_count_pairs(self.h, x.ctypes.data, c.ctypes.data))
+        return c.reshape(-1, 2)
+
+    def export_lists(self, replica: int, x, cap_per_cluster: int = 2048):
+        x = np.ascontiguousarray(np.asarray(x, np.float64).reshape(-1))
+        n = self.rep_n[replica]
+        M = self.grid(self.rep_sys[replica])
+        cap_slots = n + 8 * int(M[0] * M[1]) + 16
+        capcl = cap_slots // 8 + 1
+        perm = np.zeros(cap_slots, np.int32)
+        cnt = np.zeros(capcl, np.int32)
+        es = np.zeros(capcl * cap_per_cluster, np.int32)
+        em = np.zeros(capcl * cap_per_cluster, np.uint8)
+        ncl = C.c_int(0)
+        self._check(self.lib.sdm_export_lists(self.h, int(replica), x.ctypes.data, cap_slots, capcl,
+                                              cap_per_cluster, perm.ctypes.data, C.byref(ncl),
+                                              cnt.ctypes.data, es.ctypes.data, em.ctypes.data))
+        k = ncl.value
+        return dict(ncl=k, perm=perm[:8 * k], cnt=cnt[:k], slot=es.reshape(capcl, -1)[:k],
+                    mask=em.reshape(capcl, -1)[:k])

@@ -1,0 +1,857 @@
+// sdm_capi.cpp -- host side of the C ABI declared in include/sdm_capi.h.
+//
+// The handle owns one device arena (a single cudaMalloc sized at creation),
+// one CUDA stream, pinned staging for parameters, and a small cache of CUDA
+// graphs (one per distinct set of input/output pointers).  Nothing here throws
+// across the ABI: every entry point catches and converts to an sdm_status.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/sdm_capi.h"
+#include "sdm_types.h"
+
+cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* done, cudaStream_t st,
+                            cudaEvent_t* ev, int nev);
+cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
+                            cudaStream_t st);
+cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
+cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
+cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st);
+
+namespace {
+
+const double kCoulomb = 138.935456;  // kJ nm / (mol e^2), OpenMM's ONE_4PI_EPS0
+thread_local std::string g_create_error;
+
+struct SysHost {
+    int n;
+    std::vector<float> q, hs, se;
+    std::vector<int> grp;
+    std::vector<double> d;      // 3n
+    std::vector<int> excl_off;  // n+1 (local)
+    std::vector<int> excl_idx;
+    std::vector<int> D;         // displaced particles
+    std::vector<int> cx_off;    // nD+1 (local)
+    std::vector<int> cx_idx;
+    SdmSys dev;
+    int replicas;
+};
+
+struct Arena {
+    size_t off = 0;
+    template <class T>
+    size_t take(size_t count) {
+        off = (off + 255) & ~size_t(255);
+        size_t o = off;
+        off += count * sizeof(T) + 16;
+        return o;
+    }
+};
+
+struct GraphKey {
+    const void* x;
+    const void* res;
+    const void* f;
+    const void* stream;
+    int split, ctas;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(x, res, f, stream, split, ctas) <
+               std::tie(o.x, o.res, o.f, o.stream, o.split, o.ctas);
+    }
+};
+
+}  // namespace
+
+struct sdm_handle {
+    int device = 0;
+    std::vector<SysHost> sys;
+    std::vector<SdmRep> rep;
+    int nrep = 0;
+    long long total_particles = 0;  // over replicas (coordinate count / 3)
+    // device
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    cudaStream_t stream = nullptr;
+    SdmArgs args{};
+    int* item_prefix = nullptr;
+    int* done = nullptr;
+    void* counters = nullptr;  // memset block
+    size_t counters_bytes = 0;
+    double* x_in = nullptr;
+    double* res_in = nullptr;
+    double* f_in = nullptr;
+    double* params_dev = nullptr;
+    // host
+    double* params_pinned = nullptr;
+    std::vector<double> params;
+    bool params_dirty = true;
+    // options
+    int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 4, opt_verify = 1;
+    // graphs
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    // profiling
+    cudaEvent_t ev[12] = {};
+    float last_ms[12] = {};
+    int last_nk = 0;
+    std::string err;
+    // last evaluation pointers (for state forces)
+    bool have_eval = false;
+};
+
+namespace {
+
+const char* const kKernelNames[] = {"k_cells", "k_scan", "k_bucket", "k_colsort",
+                                    "k_clusters", "k_pair", "k_perturb", "k_finalize+k_mix"};
+
+sdm_status fail(sdm_handle* h, sdm_status code, const std::string& msg) {
+    if (h) h->err = msg; else g_create_error = msg;
+    return code;
+}
+
+sdm_status cuda_fail(sdm_handle* h, cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return fail(h, SDM_ERR_CUDA, m);
+}
+
+#define SDM_CUDA(h, call)                                   \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+    } while (0)
+
+void default_params(double* p) {
+    // reference integrator defaults, openmmapi/src/LangevinIntegratorSDM.cpp:48-85
+    for (int k = 0; k < SDM_NPARAMS; ++k) p[k] = 0.0;
+    p[SDM_P_BIAS_METHOD] = SDM_LINEAR;
+    p[SDM_P_SOFTCORE_METHOD] = SDM_NO_SOFTCORE;
+    p[SDM_P_LAMBDA] = 1.0;
+    p[SDM_P_LAMBDA1] = 1.0;
+    p[SDM_P_LAMBDA2] = 1.0;
+    p[SDM_P_ALPHA] = 1.0;
+    p[SDM_P_U0] = 0.0;
+    p[SDM_P_W0] = 0.0;
+    p[SDM_P_GAMMA] = 0.0;
+    p[SDM_P_WB] = 1.0;
+    p[SDM_P_UMAX] = 200.0;
+    p[SDM_P_ACORE] = 0.25;
+    p[SDM_P_UBCORE] = 0.0;
+}
+
+int round8(long long v) { return (int)((v + 7) / 8 * 8); }
+
+std::string setup_system(const sdm_system_desc& d, SysHost& s) {
+    char buf[256];
+    if (d.num_particles < 1) return "num_particles must be >= 1";
+    if (!d.charge || !d.sigma || !d.epsilon) return "charge/sigma/epsilon must not be NULL";
+    if (d.num_exclusions < 0 || (d.num_exclusions > 0 && !d.exclusions))
+        return "invalid exclusion list";
+    if (d.num_replicas < 1) return "num_replicas must be >= 1";
+    if (!(d.cutoff > 0.0)) return "cutoff must be > 0";
+    for (int k = 0; k < 3; ++k) {
+        if (!(d.box[k] > 0.0) || !std::isfinite(d.box[k])) return "box edges must be finite and > 0";
+        if (!(d.cutoff < 0.5 * d.box[k])) {
+            snprintf(buf, sizeof buf, "cutoff %.6g must be below half the box edge %.6g", d.cutoff, d.box[k]);
+            return buf;
+        }
+    }
+    if (!(d.reaction_field_dielectric > 0.0)) return "reaction_field_dielectric must be > 0";
+    const int n = d.num_particles;
+    s.n = n;
+    s.replicas = d.num_replicas;
+    s.q.resize(n); s.hs.resize(n); s.se.resize(n); s.grp.assign(n, 0); s.d.assign(3 * (size_t)n, 0.0);
+    const double sk = std::sqrt(kCoulomb);
+    for (int i = 0; i < n; ++i) {
+        if (!(d.sigma[i] >= 0.0) || !(d.epsilon[i] >= 0.0) || !std::isfinite(d.charge[i]))
+            return "sigma/epsilon must be >= 0 and charges finite";
+        s.q[i] = (float)(d.charge[i] * sk);
+        s.hs[i] = (float)(0.5 * d.sigma[i]);
+        s.se[i] = (float)(2.0 * std::sqrt(d.epsilon[i]));
+    }
+    // exclusions: symmetric CSR, sorted, de-duplicated
+    std::vector<std::vector<int>> adj(n);
+    for (int e = 0; e < d.num_exclusions; ++e) {
+        const int a = d.exclusions[2 * e], b = d.exclusions[2 * e + 1];
+        if (a < 0 || b < 0 || a >= n || b >= n || a == b) return "exclusion index out of range or self pair";
+        adj[a].push_back(b);
+        adj[b].push_back(a);
+    }
+    s.excl_off.assign(n + 1, 0);
+    s.excl_idx.clear();
+    for (int i = 0; i < n; ++i) {
+        auto& v = adj[i];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        s.excl_idx.insert(s.excl_idx.end(), v.begin(), v.end());
+        s.excl_off[i + 1] = (int)s.excl_idx.size();
+    }
+    // grid
+    SdmSys& g = s.dev;
+    std::memset(&g, 0, sizeof g);
+    g.n = n;
+    const double vol = d.box[0] * d.box[1] * d.box[2];
+    const double side = std::cbrt(8.0 * vol / n);
+    for (int k = 0; k < 3; ++k) {
+        int M = (int)std::floor(d.box[k] / side + 0.5);
+        M = std::max(1, std::min(M, 1024));
+        g.M[k] = M;
+        g.box[k] = d.box[k];
+        g.invL[k] = 1.0 / d.box[k];
+        g.g[k] = d.box[k] / (double)M;
+        g.invg[k] = (double)M / d.box[k];
+        g.Lf[k] = (float)d.box[k];
+        g.invLf[k] = (float)(1.0 / d.box[k]);
+        g.gf[k] = (float)g.g[k];
+    }
+    g.ncol = g.M[0] * g.M[1];
+    g.rc = d.cutoff;
+    g.img_static = 0;
+    for (int k = 0; k < 2; ++k) {
+        const int K = (int)std::floor((d.cutoff + 2.0e-4) / g.g[k]) + 1;
+        if (2 * K + 1 <= g.M[k]) { g.stlo[k] = -K; g.sthi[k] = K; }
+        else { g.stlo[k] = -((g.M[k] - 1) / 2); g.sthi[k] = g.M[k] / 2; }
+        if (!(0.5 * d.box[k] - d.cutoff - g.g[k] > 1.0e-3)) g.img_static = 1;
+    }
+    const double e = d.reaction_field_dielectric, rc = d.cutoff;
+    g.krf = (float)((e - 1.0) / ((2.0 * e + 1.0) * rc * rc * rc));
+    g.crf = (float)(3.0 * e / ((2.0 * e + 1.0) * rc));
+    g.rc2f = (float)(rc * rc);
+    g.rcl = (float)(rc + SDM_LIST_MARGIN);
+    g.rcl2f = g.rcl * g.rcl;
+    return "";
+}
+
+// displacement groups: distinct displacement vectors (exact), 0 = zero vector
+void setup_displacement(SysHost& s, const double* disp) {
+    const int n = s.n;
+    s.grp.assign(n, 0);
+    if (disp) std::copy(disp, disp + 3 * (size_t)n, s.d.begin());
+    else std::fill(s.d.begin(), s.d.end(), 0.0);
+    std::map<std::tuple<double, double, double>, int> ids;
+    s.D.clear();
+    for (int i = 0; i < n; ++i) {
+        const double x = s.d[3 * i], y = s.d[3 * i + 1], z = s.d[3 * i + 2];
+        if (x == 0.0 && y == 0.0 && z == 0.0) continue;
+        auto key = std::make_tuple(x, y, z);
+        auto it = ids.find(key);
+        int id;
+        if (it == ids.end()) { id = (int)ids.size() + 1; ids[key] = id; }
+        else id = it->second;
+        s.grp[i] = id;
+        s.D.push_back(i);
+    }
+    s.cx_off.assign(s.D.size() + 1, 0);
+    s.cx_idx.clear();
+    for (size_t k = 0; k < s.D.size(); ++k) {
+        const int p = s.D[k];
+        for (int e = s.excl_off[p]; e < s.excl_off[p + 1]; ++e) {
+            const int j = s.excl_idx[e];
+            if (s.grp[j] != s.grp[p]) s.cx_idx.push_back(j);
+        }
+        s.cx_off[k + 1] = (int)s.cx_idx.size();
+    }
+}
+
+template <class T>
+T* at(char* base, size_t off) { return reinterpret_cast<T*>(base + off); }
+
+sdm_status upload_topology(sdm_handle* h) {
+    // rebuilds the per-particle topology arrays of every system (after a
+    // displacement change) in the arena
+    std::vector<float> q, hs, se;
+    std::vector<int> grp, eoff, eidx, D, cxo, cxi;
+    std::vector<double> dd;
+    std::vector<float> tab;
+    std::vector<SdmSys> sd;
+    int atom = 0, excl = 0, dbase = 0, cxbase = 0, tabbase = 0;
+    for (auto& s : h->sys) {
+        SdmSys g = s.dev;
+        g.atom_base = atom;
+        g.excl_base = excl;
+        g.D_base = dbase;
+        g.nD = (int)s.D.size();
+        g.cx_base = cxbase;
+        g.shift_base = tabbase;
+        q.insert(q.end(), s.q.begin(), s.q.end());
+        hs.insert(hs.end(), s.hs.begin(), s.hs.end());
+        se.insert(se.end(), s.se.begin(), s.se.end());
+        grp.insert(grp.end(), s.grp.begin(), s.grp.end());
+        dd.insert(dd.end(), s.d.begin(), s.d.end());
+        for (int i = 0; i < s.n; ++i) eoff.push_back(excl + s.excl_off[i]);
+        eidx.insert(eidx.end(), s.excl_idx.begin(), s.excl_idx.end());
+        D.insert(D.end(), s.D.begin(), s.D.end());
+        for (size_t k = 0; k < s.D.size(); ++k) cxo.push_back((int)cxi.size() + s.cx_off[k]);
+        const int cx_total = (int)cxi.size() + s.cx_off[s.D.size()];
+        cxi.insert(cxi.end(), s.cx_idx.begin(), s.cx_idx.end());
+        cxo.push_back(cx_total);
+        for (int k = 0; k < 3; ++k)
+            for (int m = -g.M[k]; m <= g.M[k]; ++m) tab.push_back((float)((double)m * g.g[k]));
+        atom += s.n;
+        excl += (int)s.excl_idx.size();
+        dbase += (int)s.D.size();
+        cxbase += (int)s.D.size() + 1;
+        tabbase += 2 * (g.M[0] + g.M[1] + g.M[2]) + 3;
+        s.dev = g;
+        sd.push_back(g);
+    }
+    eoff.push_back(excl);
+    if (eidx.empty()) eidx.push_back(0);
+    if (D.empty()) D.push_back(0);
+    if (cxi.empty()) cxi.push_back(0);
+    SdmArgs& a = h->args;
+    auto put = [&](const void* dst, const void* src, size_t bytes) -> sdm_status {
+        SDM_CUDA(h, cudaMemcpyAsync(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice, h->stream));
+        return SDM_OK;
+    };
+    sdm_status st;
+    if ((st = put(a.sys, sd.data(), sd.size() * sizeof(SdmSys)))) return st;
+    if ((st = put(a.topo_q, q.data(), q.size() * 4))) return st;
+    if ((st = put(a.topo_hs, hs.data(), hs.size() * 4))) return st;
+    if ((st = put(a.topo_se, se.data(), se.size() * 4))) return st;
+    if ((st = put(a.topo_grp, grp.data(), grp.size() * 4))) return st;
+    if ((st = put(a.topo_d, dd.data(), dd.size() * 8))) return st;
+    if ((st = put(a.excl_off, eoff.data(), eoff.size() * 4))) return st;
+    if ((st = put(a.excl_idx, eidx.data(), eidx.size() * 4))) return st;
+    if ((st = put(a.D_idx, D.data(), D.size() * 4))) return st;
+    if ((st = put(a.cx_off, cxo.data(), cxo.size() * 4))) return st;
+    if ((st = put(a.cx_idx, cxi.data(), cxi.size() * 4))) return st;
+    if ((st = put(a.shift_tab, tab.data(), tab.size() * 4))) return st;
+    // perturbation windows depend on nD
+    int pw = 0;
+    for (auto& r : h->rep) { r.pert_win = pw; pw += 2 * h->sys[r.sys].dev.nD; }
+    a.total_pert = pw;
+    if ((st = put(a.rep, h->rep.data(), h->rep.size() * sizeof(SdmRep)))) return st;
+    SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    return SDM_OK;
+}
+
+sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, bool profile) {
+    SDM_CUDA(h, cudaMemsetAsync(h->counters, 0, h->counters_bytes, st));
+    cudaEvent_t* ev = profile ? h->ev : nullptr;
+    SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->done, st, ev, 6));
+    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, st));
+    if (profile) SDM_CUDA(h, cudaEventRecord(h->ev[6], st));
+    if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
+    if (profile) SDM_CUDA(h, cudaEventRecord(h->ev[7], st));
+    if (mode == 0) SDM_CUDA(h, sdm_launch_finalize(a, st));
+    if (profile) SDM_CUDA(h, cudaEventRecord(h->ev[8], st));
+    return SDM_OK;
+}
+
+sdm_status flush_params(sdm_handle* h, cudaStream_t st) {
+    if (!h->params_dirty) return SDM_OK;
+    std::memcpy(h->params_pinned, h->params.data(), h->params.size() * sizeof(double));
+    SDM_CUDA(h, cudaMemcpyAsync(h->params_dev, h->params_pinned, h->params.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+    // the pinned staging must not be overwritten before the copy ran
+    SDM_CUDA(h, cudaStreamSynchronize(st));
+    h->params_dirty = false;
+    return SDM_OK;
+}
+
+sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStream_t st, int mode,
+               bool allow_graph) {
+    SdmArgs a = h->args;
+    a.x = x;
+    a.results = res;
+    a.forces = f;
+    a.F0out = nullptr;
+    a.F1out = nullptr;
+    a.split = mode == 2 ? 1 : h->opt_split;
+    sdm_status s = flush_params(h, st);
+    if (s) return s;
+    const bool profile = h->opt_profile != 0;
+    if (profile || !h->opt_graph || !allow_graph || mode != 0) {
+        s = enqueue(h, a, mode, st, profile);
+        if (s) return s;
+        if (profile) {
+            SDM_CUDA(h, cudaEventSynchronize(h->ev[8]));
+            for (int k = 0; k < 8; ++k) SDM_CUDA(h, cudaEventElapsedTime(&h->last_ms[k], h->ev[k], h->ev[k + 1]));
+            h->last_nk = 8;
+        }
+        h->have_eval = (mode == 0);
+        return SDM_OK;
+    }
+    GraphKey key{x, res, f, st, a.split, h->opt_ctas};
+    auto it = h->graphs.find(key);
+    if (it == h->graphs.end()) {
+        cudaGraph_t g = nullptr;
+        SDM_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        s = enqueue(h, a, mode, st, false);
+        cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (s) { if (g) cudaGraphDestroy(g); return s; }
+        if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaStreamEndCapture");
+        cudaGraphExec_t ex = nullptr;
+        ce = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaGraphInstantiate");
+        if (h->graphs.size() > 16) {
+            for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+            h->graphs.clear();
+        }
+        it = h->graphs.emplace(key, ex).first;
+    }
+    SDM_CUDA(h, cudaGraphLaunch(it->second, st));
+    h->have_eval = true;
+    return SDM_OK;
+}
+
+sdm_status check_dev_status(sdm_handle* h, int* out, bool clear) {
+    int v = 0;
+    SDM_CUDA(h, cudaMemcpy(&v, h->args.status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (clear && v) SDM_CUDA(h, cudaMemset(h->args.status, 0, sizeof(int)));
+    if (out) *out = v;
+    return SDM_OK;
+}
+
+}  // namespace
+
+// --------------------------------------------------------------------------- //
+extern "C" {
+
+sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int device, sdm_handle** out) {
+    if (!out) return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "out must not be NULL");
+    *out = nullptr;
+    if (!systems || num_systems < 1) return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "need >= 1 system");
+    sdm_handle* h = new (std::nothrow) sdm_handle();
+    if (!h) return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "out of host memory");
+    auto bail = [&](sdm_status s) {
+        g_create_error = h->err.empty() ? g_create_error : h->err;
+        sdm_destroy(h);
+        return s;
+    };
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        delete h;
+        return fail(nullptr, SDM_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= ndev) {
+        delete h;
+        return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "device index out of range");
+    }
+    h->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) { delete h; return fail(nullptr, SDM_ERR_CUDA, "cudaSetDevice failed"); }
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, device);
+    if (prop.major < 10) {
+        delete h;
+        return fail(nullptr, SDM_ERR_NO_DEVICE, "the library is built for sm_103a (Blackwell Ultra)");
+    }
+    h->sys.resize(num_systems);
+    for (int s = 0; s < num_systems; ++s) {
+        std::string e = setup_system(systems[s], h->sys[s]);
+        if (!e.empty()) {
+            delete h;
+            return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "system " + std::to_string(s) + ": " + e);
+        }
+        setup_displacement(h->sys[s], systems[s].displacement);
+    }
+    // replica windows
+    long long xo = 0;
+    int aw = 0, cw = 0, sw = 0;
+    for (int s = 0; s < num_systems; ++s) {
+        const SysHost& S = h->sys[s];
+        for (int k = 0; k < S.replicas; ++k) {
+            SdmRep r{};
+            r.sys = s;
+            r.n = S.n;
+            r.x_off = xo;
+            r.atom_win = aw;
+            r.col_win = cw;
+            r.slot_win = sw;
+            r.slot_cap = round8((long long)S.n + 8LL * S.dev.ncol + 8);
+            r.cl_win = sw / 8;
+            h->rep.push_back(r);
+            xo += S.n;
+            aw += S.n;
+            cw += S.dev.ncol + 1;
+            sw += r.slot_cap;
+        }
+    }
+    h->nrep = (int)h->rep.size();
+    h->total_particles = xo;
+    if (xo > (1LL << 30) || (long long)sw > (1LL << 30)) {
+        delete h;
+        return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "batch too large");
+    }
+    // arena layout
+    int tot_n = 0, tot_excl = 0, tot_D = 0, tot_cx = 0, tot_tab = 0, tot_cxidx = 0;
+    for (auto& s : h->sys) {
+        tot_n += s.n;
+        tot_excl += (int)s.excl_idx.size();
+        tot_D += (int)s.D.size();
+        tot_cx += (int)s.D.size() + 1;
+        tot_tab += 2 * (s.dev.M[0] + s.dev.M[1] + s.dev.M[2]) + 3;
+    }
+    // the displacement map may change later: reserve the worst case (every particle displaced)
+    tot_D = std::max(tot_D, tot_n);
+    tot_cx = tot_n + (int)h->sys.size();
+    tot_cxidx = std::max(tot_excl, 1);
+    const int nrep = h->nrep;
+    const long long A = aw, Ccol = cw, Sl = sw, Cl = sw / 8;
+    long long Pp = 0;
+    for (auto& r : h->rep) Pp += 2LL * h->sys[r.sys].n;
+    Arena ar;
+    SdmArgs& a = h->args;
+    const size_t o_sys = ar.take<SdmSys>(h->sys.size());
+    const size_t o_rep = ar.take<SdmRep>(nrep);
+    const size_t o_q = ar.take<float>(tot_n), o_hs = ar.take<float>(tot_n), o_se = ar.take<float>(tot_n);
+    const size_t o_grp = ar.take<int>(tot_n), o_d = ar.take<double>(3LL * tot_n);
+    const size_t o_eoff = ar.take<int>(tot_n + 1), o_eidx = ar.take<int>(std::max(tot_excl, 1));
+    const size_t o_D = ar.take<int>(std::max(tot_D, 1)), o_cxo = ar.take<int>(tot_cx + 1);
+    const size_t o_cxi = ar.take<int>(tot_cxidx), o_tab = ar.take<float>(tot_tab);
+    const size_t o_par = ar.take<double>((size_t)nrep * SDM_NPARAMS);
+    const size_t o_x = ar.take<double>(3 * xo), o_res = ar.take<double>((size_t)nrep * SDM_NRESULTS);
+    const size_t o_f = ar.take<double>(3 * xo);
+    const size_t o_w = ar.take<double>(3 * A), o_ci = ar.take<int2>(A), o_inv = ar.take<int>(A);
+    const size_t o_bk = ar.take<int>(A);
+    const size_t o_cnt = ar.take<int>(2 * Ccol + nrep + 4);  // counters block: col_cnt, col_fill, extz, work
+    const size_t o_aoff = ar.take<int>(Ccol), o_cl = ar.take<int>(Ccol);
+    const size_t o_perm = ar.take<int>(Sl), o_clX = ar.take<float4>(Sl), o_clP = ar.take<float2>(Sl);
+    const size_t o_sgrp = ar.take<int>(Sl), o_ex4 = ar.take<int4>(Sl);
+    const size_t o_F = ar.take<unsigned long long>(6 * Sl);
+    const size_t o_ref = ar.take<int4>(Cl), o_bbc = ar.take<float4>(Cl), o_bbh = ar.take<float4>(Cl);
+    const size_t o_lnk = ar.take<int4>(Cl), o_ep = ar.take<double>(Cl * SDM_MAX_SPLIT);
+    const size_t o_pp = ar.take<double>(std::max(Pp, 1LL));
+    const size_t o_ncl = ar.take<int>(nrep), o_st = ar.take<int>(4);
+    const size_t o_counts = ar.take<long long>(2 * nrep), o_ip = ar.take<int>(nrep + 1);
+    const size_t o_done = ar.take<int>(4);
+    h->arena_bytes = ar.off + 256;
+    cudaError_t ce = cudaMalloc(&h->arena, h->arena_bytes);
+    if (ce != cudaSuccess) { h->arena = nullptr; cuda_fail(h, ce, "cudaMalloc(arena)"); return bail(SDM_ERR_CUDA); }
+    ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) { cuda_fail(h, ce, "cudaStreamCreate"); return bail(SDM_ERR_CUDA); }
+    ce = cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
+    if (ce != cudaSuccess) { cuda_fail(h, ce, "cudaMemset(arena)"); return bail(SDM_ERR_CUDA); }
+    for (int k = 0; k < 12; ++k) cudaEventCreate(&h->ev[k]);
+    char* B = h->arena;
+    a.nsys = (int)h->sys.size();
+    a.nrep = nrep;
+    a.sys = at<SdmSys>(B, o_sys);
+    a.rep = at<SdmRep>(B, o_rep);
+    a.topo_q = at<float>(B, o_q);
+    a.topo_hs = at<float>(B, o_hs);
+    a.topo_se = at<float>(B, o_se);
+    a.topo_grp = at<int>(B, o_grp);
+    a.topo_d = at<double>(B, o_d);
+    a.excl_off = at<int>(B, o_eoff);
+    a.excl_idx = at<int>(B, o_eidx);
+    a.D_idx = at<int>(B, o_D);
+    a.cx_off = at<int>(B, o_cxo);
+    a.cx_idx = at<int>(B, o_cxi);
+    a.shift_tab = at<float>(B, o_tab);
+    a.params = at<double>(B, o_par);
+    h->params_dev = at<double>(B, o_par);
+    h->x_in = at<double>(B, o_x);
+    h->res_in = at<double>(B, o_res);
+    h->f_in = at<double>(B, o_f);
+    a.w = at<double>(B, o_w);
+    a.cellinfo = at<int2>(B, o_ci);
+    a.inv = at<int>(B, o_inv);
+    a.bucket = at<int>(B, o_bk);
+    a.col_cnt = at<int>(B, o_cnt);
+    a.col_fill = a.col_cnt + Ccol;
+    a.extz = reinterpret_cast<unsigned*>(a.col_fill + Ccol);
+    a.work_counter = reinterpret_cast<int*>(a.extz + nrep);
+    h->counters = a.col_cnt;
+    h->counters_bytes = sizeof(int) * (size_t)(2 * Ccol + nrep + 4);
+    a.col_aoff = at<int>(B, o_aoff);
+    a.col_cl = at<int>(B, o_cl);
+    a.perm = at<int>(B, o_perm);
+    a.clX = at<float4>(B, o_clX);
+    a.clP = at<float2>(B, o_clP);
+    a.grp = at<int>(B, o_sgrp);
+    a.excl4 = at<int4>(B, o_ex4);
+    unsigned long long* F = at<unsigned long long>(B, o_F);
+    a.F0x = F; a.F0y = F + Sl; a.F0z = F + 2 * Sl;
+    a.dFx = F + 3 * Sl; a.dFy = F + 4 * Sl; a.dFz = F + 5 * Sl;
+    a.cl_ref = at<int4>(B, o_ref);
+    a.cl_bbc = at<float4>(B, o_bbc);
+    a.cl_bbh = at<float4>(B, o_bbh);
+    a.cl_link = at<int4>(B, o_lnk);
+    a.e_part = at<double>(B, o_ep);
+    a.p_part = at<double>(B, o_pp);
+    a.ncl = at<int>(B, o_ncl);
+    a.status = at<int>(B, o_st);
+    a.counts = at<long long>(B, o_counts);
+    h->item_prefix = at<int>(B, o_ip);
+    h->done = at<int>(B, o_done);
+    a.total_atoms = (int)A;
+    a.total_cols = (int)Ccol;
+    a.total_slots = (int)Sl;
+    a.split = 1;
+    a.ex_cap = 0;
+    a.ex_rep = -1;
+    // parameters
+    h->params.resize((size_t)nrep * SDM_NPARAMS);
+    for (int r = 0; r < nrep; ++r) default_params(&h->params[(size_t)r * SDM_NPARAMS]);
+    ce = cudaMallocHost(&h->params_pinned, h->params.size() * sizeof(double));
+    if (ce != cudaSuccess) { h->params_pinned = nullptr; cuda_fail(h, ce, "cudaMallocHost"); return bail(SDM_ERR_CUDA); }
+    sdm_status st = upload_topology(h);
+    if (st) return bail(st);
+    *out = h;
+    return SDM_OK;
+}
+
+sdm_status sdm_destroy(sdm_handle* h) {
+    if (!h) return SDM_OK;
+    if (h->arena) cudaSetDevice(h->device);
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    for (int k = 0; k < 12; ++k) if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+    if (h->stream) { cudaStreamSynchronize(h->stream); cudaStreamDestroy(h->stream); }
+    if (h->arena) cudaFree(h->arena);
+    if (h->params_pinned) cudaFreeHost(h->params_pinned);
+    delete h;
+    return SDM_OK;
+}
+
+const char* sdm_last_error(const sdm_handle* h) {
+    return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+sdm_status sdm_num_replicas(const sdm_handle* h, int* out) {
+    if (!h || !out) return SDM_ERR_INVALID_ARGUMENT;
+    *out = h->nrep;
+    return SDM_OK;
+}
+
+sdm_status sdm_set_displacement(sdm_handle* h, int system, const double* displacement) {
+    if (!h) return SDM_ERR_INVALID_ARGUMENT;
+    if (system < 0 || system >= (int)h->sys.size()) return fail(h, SDM_ERR_INVALID_ARGUMENT, "system index out of range");
+    if (displacement)
+        for (size_t k = 0; k < 3 * (size_t)h->sys[system].n; ++k)
+            if (!std::isfinite(displacement[k])) return fail(h, SDM_ERR_INVALID_ARGUMENT, "non-finite displacement");
+    cudaSetDevice(h->device);
+    SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    setup_displacement(h->sys[system], displacement);
+    return upload_topology(h);
+}
+
+sdm_status sdm_set_params(sdm_handle* h, int replica, const double* params) {
+    if (!h || !params) return SDM_ERR_INVALID_ARGUMENT;
+    if (replica < 0 || replica >= h->nrep) return fail(h, SDM_ERR_INVALID_ARGUMENT, "replica index out of range");
+    const int bm = (int)params[SDM_P_BIAS_METHOD], sm = (int)params[SDM_P_SOFTCORE_METHOD];
+    if (bm < 0 || bm > 2 || bm != params[SDM_P_BIAS_METHOD]) return fail(h, SDM_ERR_UNKNOWN_METHOD, "Unknown bias method");
+    if (sm < 0 || sm > 2 || sm != params[SDM_P_SOFTCORE_METHOD]) return fail(h, SDM_ERR_UNKNOWN_METHOD, "Unknown soft core method");
+    std::memcpy(&h->params[(size_t)replica * SDM_NPARAMS], params, sizeof(double) * SDM_NPARAMS);
+    h->params_dirty = true;
+    return SDM_OK;
+}
+
+sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double* forces) {
+    if (!h || !x) return SDM_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    const size_t nx = 3 * (size_t)h->total_particles;
+    SDM_CUDA(h, cudaMemcpyAsync(h->x_in, x, nx * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    sdm_status s = run(h, h->x_in, h->res_in, h->f_in, h->stream, 0, true);
+    if (s) return s;
+    if (results)
+        SDM_CUDA(h, cudaMemcpyAsync(results, h->res_in, sizeof(double) * SDM_NRESULTS * h->nrep,
+                                    cudaMemcpyDeviceToHost, h->stream));
+    if (forces)
+        SDM_CUDA(h, cudaMemcpyAsync(forces, h->f_in, nx * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->opt_verify) {
+        int v = 0;
+        s = check_dev_status(h, &v, true);
+        if (s) return s;
+        if (v) return fail(h, SDM_ERR_OVERFLOW, "device status " + std::to_string(v) +
+                                                    ": force overflow or non-finite energy");
+    }
+    return SDM_OK;
+}
+
+sdm_status sdm_evaluate_device(sdm_handle* h, const double* x, double* results, double* forces, void* stream) {
+    if (!h || !x || !results) return SDM_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+    return run(h, x, results, forces, st, 0, true);
+}
+
+sdm_status sdm_get_state_forces(sdm_handle* h, double* F0, double* F1, int on_device) {
+    if (!h) return SDM_ERR_INVALID_ARGUMENT;
+    if (!h->have_eval) return fail(h, SDM_ERR_INVALID_ARGUMENT, "no evaluation yet");
+    cudaSetDevice(h->device);
+    SDM_CUDA(h, cudaDeviceSynchronize());
+    const size_t nx = 3 * (size_t)h->total_particles;
+    SdmArgs a = h->args;
+    a.forces = nullptr;
+    a.results = h->res_in;
+    if (on_device) {
+        a.F0out = F0;
+        a.F1out = F1;
+        SDM_CUDA(h, sdm_launch_mix(a, h->stream));
+    } else {
+        // stage through the internal force buffer, one state at a time
+        if (F0) {
+            a.F0out = h->f_in;
+            a.F1out = nullptr;
+            SDM_CUDA(h, sdm_launch_mix(a, h->stream));
+            SDM_CUDA(h, cudaMemcpyAsync(F0, h->f_in, nx * 8, cudaMemcpyDeviceToHost, h->stream));
+        }
+        if (F1) {
+            a.F0out = nullptr;
+            a.F1out = h->f_in;
+            SDM_CUDA(h, sdm_launch_mix(a, h->stream));
+            SDM_CUDA(h, cudaMemcpyAsync(F1, h->f_in, nx * 8, cudaMemcpyDeviceToHost, h->stream));
+        }
+    }
+    SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SDM_OK;
+}
+
+sdm_status sdm_check_status(sdm_handle* h, int* device_status) {
+    if (!h) return SDM_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    SDM_CUDA(h, cudaDeviceSynchronize());
+    return check_dev_status(h, device_status, true);
+}
+
+sdm_status sdm_set_option(sdm_handle* h, int option, int value) {
+    if (!h) return SDM_ERR_INVALID_ARGUMENT;
+    switch (option) {
+        case SDM_OPT_GRAPH: h->opt_graph = value ? 1 : 0; break;
+        case SDM_OPT_PROFILE: h->opt_profile = value ? 1 : 0; break;
+        case SDM_OPT_SPLIT:
+            if (value != 1 && value != 2 && value != 4) return fail(h, SDM_ERR_INVALID_ARGUMENT, "split must be 1, 2 or 4");
+            h->opt_split = value;
+            break;
+        case SDM_OPT_CTAS_PER_SM:
+            if (value < 1 || value > 8) return fail(h, SDM_ERR_INVALID_ARGUMENT, "ctas per SM must be in 1..8");
+            h->opt_ctas = value;
+            break;
+        case SDM_OPT_VERIFY: h->opt_verify = value ? 1 : 0; break;
+        default: return fail(h, SDM_ERR_INVALID_ARGUMENT, "unknown option");
+    }
+    return SDM_OK;
+}
+
+sdm_status sdm_get_option(const sdm_handle* h, int option, int* value) {
+    if (!h || !value) return SDM_ERR_INVALID_ARGUMENT;
+    switch (option) {
+        case SDM_OPT_GRAPH: *value = h->opt_graph; break;
+        case SDM_OPT_PROFILE: *value = h->opt_profile; break;
+        case SDM_OPT_SPLIT: *value = h->opt_split; break;
+        case SDM_OPT_CTAS_PER_SM: *value = h->opt_ctas; break;
+        case SDM_OPT_VERIFY: *value = h->opt_verify; break;
+        default: return SDM_ERR_INVALID_ARGUMENT;
+    }
+    return SDM_OK;
+}
+
+sdm_status sdm_get_kernel_times(const sdm_handle* h, const char** names, float* ms, int* count) {
+    if (!h || !count) return SDM_ERR_INVALID_ARGUMENT;
+    const int n = std::min(*count, h->last_nk);
+    for (int k = 0; k < n; ++k) {
+        if (names) names[k] = kKernelNames[k];
+        if (ms) ms[k] = h->last_ms[k];
+    }
+    *count = n;
+    return SDM_OK;
+}
+
+sdm_status sdm_autotune(sdm_handle* h, const double* x_device, int* split, int* ctas_per_sm) {
+    if (!h || !x_device) return SDM_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    const int osplit = h->opt_split, octas = h->opt_ctas, oprof = h->opt_profile;
+    h->opt_profile = 1;
+    float best = 1e30f;
+    int bs = osplit, bc = octas;
+    const int splits[] = {1, 2, 4};
+    const int ctas[] = {2, 3, 4, 6};
+    for (int sp : splits)
+        for (int c : ctas) {
+            h->opt_split = sp;
+            h->opt_ctas = c;
+            float t = 0.f;
+            for (int rep = 0; rep < 4; ++rep) {
+                sdm_status s = run(h, x_device, h->res_in, h->f_in, h->stream, 0, false);
+                if (s) { h->opt_split = osplit; h->opt_ctas = octas; h->opt_profile = oprof; return s; }
+                if (rep > 0) t += h->last_ms[5] + h->last_ms[6];
+            }
+            if (t < best) { best = t; bs = sp; bc = c; }
+        }
+    h->opt_split = bs;
+    h->opt_ctas = bc;
+    h->opt_profile = oprof;
+    if (split) *split = bs;
+    if (ctas_per_sm) *ctas_per_sm = bc;
+    return SDM_OK;
+}
+
+sdm_status sdm_count_pairs(sdm_handle* h, const double* x, long long* counts) {
+    if (!h || !x || !counts) return SDM_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    const size_t nx = 3 * (size_t)h->total_particles;
+    SDM_CUDA(h, cudaMemcpyAsync(h->x_in, x, nx * 8, cudaMemcpyHostToDevice, h->stream));
+    SDM_CUDA(h, cudaMemsetAsync(h->args.counts, 0, sizeof(long long) * 2 * h->nrep, h->stream));
+    sdm_status s = run(h, h->x_in, h->res_in, h->f_in, h->stream, 1, false);
+    if (s) return s;
+    SDM_CUDA(h, cudaMemcpyAsync(counts, h->args.counts, sizeof(long long) * 2 * h->nrep,
+                                cudaMemcpyDeviceToHost, h->stream));
+    SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SDM_OK;
+}
+
+sdm_status sdm_get_grid(const sdm_handle* h, int system, int* M) {
+    if (!h || !M || system < 0 || system >= (int)h->sys.size()) return SDM_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < 3; ++k) M[k] = h->sys[system].dev.M[k];
+    return SDM_OK;
+}
+
+sdm_status sdm_export_lists(sdm_handle* h, int replica, const double* x, int cap_slots, int cap_clusters,
+                            int cap_per_cluster, int* perm, int* ncl, int* cnt, int* ent_slot,
+                            unsigned char* ent_mask) {
+    if (!h || !x || !perm || !ncl || !cnt || !ent_slot || !ent_mask) return SDM_ERR_INVALID_ARGUMENT;
+    if (replica < 0 || replica >= h->nrep) return fail(h, SDM_ERR_INVALID_ARGUMENT, "replica index out of range");
+    if (cap_per_cluster < 1) return fail(h, SDM_ERR_INVALID_ARGUMENT, "cap_per_cluster must be >= 1");
+    cudaSetDevice(h->device);
+    const SdmRep& R = h->rep[replica];
+    const int n = R.n;
+    SDM_CUDA(h, cudaMemcpyAsync(h->x_in + 3 * R.x_off, x, 3 * (size_t)n * 8, cudaMemcpyHostToDevice, h->stream));
+    const int capcl = R.slot_cap / 8;
+    void* dbuf = nullptr;
+    const size_t nent = (size_t)capcl * cap_per_cluster;
+    SDM_CUDA(h, cudaMalloc(&dbuf, nent * 5 + (size_t)capcl * 4 + 64));
+    int* d_cnt = (int*)dbuf;
+    int* d_slot = d_cnt + capcl;
+    unsigned char* d_mask = (unsigned char*)(d_slot + nent);
+    SdmArgs save = h->args;
+    h->args.ex_cnt = d_cnt;
+    h->args.ex_slot = d_slot;
+    h->args.ex_mask = d_mask;
+    h->args.ex_cap = cap_per_cluster;
+    h->args.ex_rep = replica;
+    sdm_status s = run(h, h->x_in, h->res_in, h->f_in, h->stream, 2, false);
+    h->args = save;
+    if (s) { cudaFree(dbuf); return s; }
+    int k = 0, st = 0;
+    cudaMemcpyAsync(&k, h->args.ncl + replica, 4, cudaMemcpyDeviceToHost, h->stream);
+    cudaStreamSynchronize(h->stream);
+    check_dev_status(h, &st, true);
+    if (8 * k > cap_slots || k > cap_clusters || (st & (1 << 16))) {
+        cudaFree(dbuf);
+        return fail(h, SDM_ERR_CAPACITY, "export capacity too small");
+    }
+    *ncl = k;
+    cudaError_t ce = cudaMemcpy(perm, h->args.perm + R.slot_win, 8 * (size_t)k * 4, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(cnt, d_cnt, (size_t)k * 4, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(ent_slot, d_slot, (size_t)k * cap_per_cluster * 4, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(ent_mask, d_mask, (size_t)k * cap_per_cluster, cudaMemcpyDeviceToHost);
+    cudaFree(dbuf);
+    if (ce != cudaSuccess) return cuda_fail(h, ce, "export copy");
+    return SDM_OK;
+}
+
+}  // extern "C"

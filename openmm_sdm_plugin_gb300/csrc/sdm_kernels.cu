@@ -1,0 +1,1271 @@
+// sdm_kernels.cu -- CUDA kernels (sm_103a) of the SDM two-state force.
+//
+// Pipeline of one evaluation (every launch covers all replicas of all systems):
+//   k_cells     wrap coordinates, integer cells, column histogram
+//   k_scan      per-replica column prefix sums (particles, clusters) and the
+//               global work-item prefix (last block)
+//   k_bucket    scatter particles into their column
+//   k_colsort   stable rank sort of each column by (z, particle index) -> slots
+//   k_clusters  cluster-local FP32 coordinates, parameters, bounding boxes,
+//               exclusion partners as slots
+//   k_pair      persistent main pass: every pair at the original coordinates
+//               (U0, F0), LJ + reaction field, FP32 math, fixed-point forces
+//   k_perturb   perturbation pass: only pairs whose displacements differ, at
+//               both states -> u (FP64) and dF = F1 - F0 (fixed point)
+//   k_finalize  deterministic energy reductions, soft core, bias, weight s
+//   k_mix       F = F0 + s dF in original particle order
+//
+// Reference correspondence: the two nonbonded evaluations of
+// openmmapi/src/LangevinIntegratorSDM.cpp:158-176 (OpenMM NonbondedForce at x
+// and x+d), the displacement MakeState2 (platforms/opencl/src/kernels/
+// langevin.cl:198-206), the combine of platforms/reference/src/
+// ReferenceSDMKernels.cpp:247-318 and the mix kernel sdmForce
+// (langevin.cl:72-87).  The save/restore copies of the reference
+// (SaveState1/SaveState2/RestoreState1, langevin.cl:147-192) disappear: both
+// states are evaluated from the same resident coordinates.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/sdm_capi.h"
+#include "sdm_types.h"
+
+#define SDM_WARPS 4
+#define SDM_JL_CAP 256
+#define SDM_RING 64
+#define SDM_INVALID_COORD 1.0e6f
+
+namespace {
+
+// ------------------------------------------------------------------------- //
+// small helpers                                                             //
+// ------------------------------------------------------------------------- //
+__device__ __forceinline__ double wrap1(double v, double L, double invL) {
+    double t = floor(__dmul_rn(v, invL));
+    double w = __dsub_rn(v, __dmul_rn(t, L));
+    if (w >= L) w = __dsub_rn(w, L);
+    if (w < 0.0) w = __dadd_rn(w, L);
+    return w;
+}
+
+__device__ __forceinline__ int cell_of(double w, double invg, int M) {
+    int c = __double2int_rd(__dmul_rn(w, invg));
+    c = c < 0 ? 0 : c;
+    return c > M - 1 ? M - 1 : c;
+}
+
+__device__ __forceinline__ int wrap_cell(int n, int M) {
+    if (2 * n > M) n -= M;
+    else if (2 * n <= -M) n += M;
+    return n;
+}
+
+__device__ __forceinline__ int pmod(int a, int M) {
+    int r = a % M;
+    return r < 0 ? r + M : r;
+}
+
+__device__ __forceinline__ float img32(float d, float L, float invL) {
+    float t = rintf(__fmul_rn(d, invL));
+    return __fmaf_rn(-L, t, d);
+}
+
+__device__ __forceinline__ float r2_chain(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+__device__ __forceinline__ float fast_rsqrt(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ void red_fixed(unsigned long long* p, float v, int* status) {
+    if (!(fabsf(v) < 2.0e9f)) atomicOr(status, SDM_DEV_FORCE_OVERFLOW);
+    long long q = __float2ll_rn(v * 4294967296.0f);
+    atomicAdd(p, (unsigned long long)q);
+}
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// replica lookup by window base (rep[] sorted by every window)
+__device__ __forceinline__ int rep_by_atom(const SdmRep* rep, int nrep, int gi) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rep[mid].atom_win <= gi) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int rep_by_col(const SdmRep* rep, int nrep, int gi) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rep[mid].col_win <= gi) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int rep_by_slot(const SdmRep* rep, int nrep, int gi) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rep[mid].slot_win <= gi) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int rep_by_pert(const SdmRep* rep, int nrep, int gi) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rep[mid].pert_win <= gi) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int rep_by_item(const int* prefix, int nrep, int item) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ------------------------------------------------------------------------- //
+// K1: cells                                                                 //
+// ------------------------------------------------------------------------- //
+__global__ void k_cells(SdmArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < a.total_atoms; gi += stride) {
+        const int r = rep_by_atom(a.rep, a.nrep, gi);
+        const SdmRep& R = a.rep[r];
+        const SdmSys& S = a.sys[R.sys];
+        const int i = gi - R.atom_win;
+        const double* xp = a.x + 3 * (R.x_off + i);
+        int c[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double w = wrap1(xp[k], S.box[k], S.invL[k]);
+            a.w[3 * (size_t)gi + k] = w;
+            c[k] = cell_of(w, S.invg[k], S.M[k]);
+        }
+        const int col = c[0] * S.M[1] + c[1];
+        a.cellinfo[gi] = make_int2(col, c[2]);
+        atomicAdd(&a.col_cnt[R.col_win + col], 1);
+    }
+    for (int gs = blockIdx.x * blockDim.x + threadIdx.x; gs < a.total_slots; gs += stride) {
+        a.F0x[gs] = 0ull; a.F0y[gs] = 0ull; a.F0z[gs] = 0ull;
+        a.dFx[gs] = 0ull; a.dFy[gs] = 0ull; a.dFz[gs] = 0ull;
+    }
+}
+
+// ------------------------------------------------------------------------- //
+// K2: column prefix sums; the last block builds the work-item prefix        //
+// ------------------------------------------------------------------------- //
+__device__ __forceinline__ int2 warp_incl_scan2(int2 v) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int x = __shfl_up_sync(0xffffffffu, v.x, o);
+        int y = __shfl_up_sync(0xffffffffu, v.y, o);
+        if (lane_id() >= o) { v.x += x; v.y += y; }
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int* done) {
+    __shared__ int2 wsum[32];
+    __shared__ int last;
+    const int r = blockIdx.x;
+    const SdmRep& R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int ncol = S.ncol;
+    const int* cnt = a.col_cnt + R.col_win;
+    int* aoff = a.col_aoff + R.col_win;
+    int* cl = a.col_cl + R.col_win;
+    const int per = (ncol + blockDim.x - 1) / blockDim.x;
+    const int beg = min(ncol, (int)threadIdx.x * per);
+    const int end = min(ncol, beg + per);
+    int2 s = make_int2(0, 0);
+    for (int c = beg; c < end; ++c) { s.x += cnt[c]; s.y += (cnt[c] + 7) >> 3; }
+    int2 inc = warp_incl_scan2(s);
+    const int wid = threadIdx.x >> 5;
+    if (lane_id() == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int2 v = (lane_id() < (int)(blockDim.x >> 5)) ? wsum[lane_id()] : make_int2(0, 0);
+        v = warp_incl_scan2(v);
+        wsum[lane_id()] = v;
+    }
+    __syncthreads();
+    int2 base = make_int2(inc.x - s.x, inc.y - s.y);
+    if (wid > 0) { base.x += wsum[wid - 1].x; base.y += wsum[wid - 1].y; }
+    for (int c = beg; c < end; ++c) {
+        aoff[c] = base.x;
+        cl[c] = base.y;
+        base.x += cnt[c];
+        base.y += (cnt[c] + 7) >> 3;
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        aoff[ncol] = base.x;
+        cl[ncol] = base.y;
+        a.ncl[r] = base.y;
+    }
+    // last block computes the item prefix over replicas (no waiting involved)
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(done, 1) == (int)gridDim.x - 1);
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        // sequential chunks + block scan, same as above
+        const int nrep = a.nrep;
+        const int per2 = (nrep + blockDim.x - 1) / blockDim.x;
+        const int b2 = min(nrep, (int)threadIdx.x * per2);
+        const int e2 = min(nrep, b2 + per2);
+        int2 t = make_int2(0, 0);
+        for (int q = b2; q < e2; ++q) t.x += ((volatile int*)a.ncl)[q] * a.split;
+        int2 inc2 = warp_incl_scan2(t);
+        __syncthreads();
+        if (lane_id() == 31) wsum[wid] = inc2;
+        __syncthreads();
+        if (wid == 0) {
+            int2 v = (lane_id() < (int)(blockDim.x >> 5)) ? wsum[lane_id()] : make_int2(0, 0);
+            v = warp_incl_scan2(v);
+            wsum[lane_id()] = v;
+        }
+        __syncthreads();
+        int b = inc2.x - t.x + (wid > 0 ? wsum[wid - 1].x : 0);
+        for (int q = b2; q < e2; ++q) {
+            item_prefix[q] = b;
+            b += ((volatile int*)a.ncl)[q] * a.split;
+        }
+        if (threadIdx.x == blockDim.x - 1) item_prefix[nrep] = b;
+        if (threadIdx.x == 0) *done = 0;
+    }
+}
+
+// ------------------------------------------------------------------------- //
+// K3: bucket                                                                //
+// ------------------------------------------------------------------------- //
+__global__ void k_bucket(SdmArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < a.total_atoms; gi += stride) {
+        const int r = rep_by_atom(a.rep, a.nrep, gi);
+        const SdmRep& R = a.rep[r];
+        const int col = a.cellinfo[gi].x;
+        const int pos = atomicAdd(&a.col_fill[R.col_win + col], 1);
+        a.bucket[R.atom_win + a.col_aoff[R.col_win + col] + pos] = gi - R.atom_win;
+    }
+}
+
+// ------------------------------------------------------------------------- //
+// K4: rank sort of every column by (z, particle)                            //
+// ------------------------------------------------------------------------- //
+__global__ void __launch_bounds__(128) k_colsort(SdmArgs a) {
+    __shared__ double kz[4][128];
+    __shared__ int ki[4][128];
+    const int wib = threadIdx.x >> 5;
+    const int lane = lane_id();
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    for (int gc = blockIdx.x * (blockDim.x >> 5) + wib; gc < a.total_cols; gc += nwarps) {
+        const int r = rep_by_col(a.rep, a.nrep, gc);
+        const SdmRep& R = a.rep[r];
+        const SdmSys& S = a.sys[R.sys];
+        const int c = gc - R.col_win;
+        if (c >= S.ncol) continue;
+        const int n = a.col_cnt[R.col_win + c];
+        const int a0 = a.col_aoff[R.col_win + c];
+        const int sbase = 8 * a.col_cl[R.col_win + c];
+        const int send = 8 * a.col_cl[R.col_win + c + 1];
+        const int* bk = a.bucket + R.atom_win + a0;
+        for (int ib = 0; ib < n; ib += 32) {
+            const int ii = ib + lane;
+            int ai = -1;
+            double zi = 0.0;
+            if (ii < n) { ai = bk[ii]; zi = a.w[3 * (size_t)(R.atom_win + ai) + 2]; }
+            int rank = 0;
+            for (int jb = 0; jb < n; jb += 128) {
+                __syncwarp();
+                for (int q = lane; q < 128 && jb + q < n; q += 32) {
+                    const int aj = bk[jb + q];
+                    ki[wib][q] = aj;
+                    kz[wib][q] = a.w[3 * (size_t)(R.atom_win + aj) + 2];
+                }
+                __syncwarp();
+                const int m = min(128, n - jb);
+                if (ii < n)
+                    for (int q = 0; q < m; ++q) {
+                        const double zj = kz[wib][q];
+                        const int aj = ki[wib][q];
+                        rank += (zj < zi) || (zj == zi && aj < ai);
+                    }
+            }
+            if (ii < n) {
+                const int slot = sbase + rank;
+                a.perm[R.slot_win + slot] = ai;
+                a.inv[R.atom_win + ai] = slot;
+            }
+        }
+        for (int s = sbase + n + lane; s < send; s += 32) a.perm[R.slot_win + s] = -1;
+    }
+}
+
+// ------------------------------------------------------------------------- //
+// K5: cluster data                                                          //
+// ------------------------------------------------------------------------- //
+__global__ void k_clusters(SdmArgs a) {
+    const int stride = gridDim.x * blockDim.x;   // multiple of 8 (block size multiple of 32)
+    const int lane = lane_id();
+    const unsigned gmask = 0xffu << (lane & 24);
+    for (int gs = blockIdx.x * blockDim.x + threadIdx.x; gs < a.total_slots; gs += stride) {
+        const int r = rep_by_slot(a.rep, a.nrep, gs);
+        const SdmRep& R = a.rep[r];
+        const SdmSys& S = a.sys[R.sys];
+        const int s = gs - R.slot_win;
+        const int C = s >> 3, t = s & 7;
+        if (C >= a.ncl[r]) continue;   // uniform over the 8-lane group
+        const int p = a.perm[gs];
+        const int p0 = a.perm[R.slot_win + 8 * C];
+        const int2 ci0 = a.cellinfo[R.atom_win + p0];
+        const int cx = ci0.x / S.M[1], cy = ci0.x - cx * S.M[1], cz = ci0.y;
+        const double Rr[3] = {__dmul_rn((double)cx, S.g[0]), __dmul_rn((double)cy, S.g[1]),
+                              __dmul_rn((double)cz, S.g[2])};
+        float X[3];
+        float4 q4;
+        float2 p2;
+        int g = 0;
+        int4 ex = make_int4(-1, -1, -1, -1);
+        if (p >= 0) {
+            const double* wp = a.w + 3 * (size_t)(R.atom_win + p);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) X[k] = __double2float_rn(__dsub_rn(wp[k], Rr[k]));
+            const int ta = S.atom_base + p;
+            q4 = make_float4(X[0], X[1], X[2], a.topo_q[ta]);
+            p2 = make_float2(a.topo_hs[ta], a.topo_se[ta]);
+            g = a.topo_grp[ta];
+            const int eb = a.excl_off[ta], ee = a.excl_off[ta + 1];
+            if (ee - eb > 4) {
+                ex = make_int4(-2, -2, -2, -2);
+            } else {
+                int v[4] = {-1, -1, -1, -1};
+                for (int k = eb; k < ee; ++k) v[k - eb] = a.inv[R.atom_win + a.excl_idx[k]];
+                ex = make_int4(v[0], v[1], v[2], v[3]);
+            }
+        } else {
+            X[0] = X[1] = X[2] = SDM_INVALID_COORD;
+            q4 = make_float4(X[0], X[1], X[2], 0.0f);
+            p2 = make_float2(0.0f, 0.0f);
+        }
+        a.clX[gs] = q4;
+        a.clP[gs] = p2;
+        a.grp[gs] = g;
+        a.excl4[gs] = ex;
+        // bounding box over valid slots
+        float lo[3], hi[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = (p >= 0) ? X[k] : 3.0e38f;
+            hi[k] = (p >= 0) ? X[k] : -3.0e38f;
+        }
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(gmask, lo[k], o, 8));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(gmask, hi[k], o, 8));
+            }
+        // exclusion-linked clusters: distinct clusters (other than C) holding
+        // partners of this cluster's particles; -2 when more than 4 or unknown
+        int link[4] = {-1, -1, -1, -1};
+        int nlink = 0;
+        bool many = false;
+        for (int l = 0; l < 8; ++l) {
+            int e4[4];
+            e4[0] = __shfl_sync(gmask, ex.x, l, 8);
+            e4[1] = __shfl_sync(gmask, ex.y, l, 8);
+            e4[2] = __shfl_sync(gmask, ex.z, l, 8);
+            e4[3] = __shfl_sync(gmask, ex.w, l, 8);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int e = e4[k];
+                if (e == -2) many = true;
+                if (e < 0) continue;
+                const int cc = e >> 3;
+                if (cc == C) continue;
+                bool seen = false;
+                for (int u = 0; u < nlink; ++u) seen |= (link[u] == cc);
+                if (!seen) {
+                    if (nlink < 4) link[nlink++] = cc; else many = true;
+                }
+            }
+        }
+        if (t == 0) {
+            const int cw = R.cl_win + C;
+            a.cl_ref[cw] = make_int4(cx, cy, cz, ci0.x);
+            a.cl_bbc[cw] = make_float4(__fmul_rn(0.5f, __fadd_rn(lo[0], hi[0])),
+                                       __fmul_rn(0.5f, __fadd_rn(lo[1], hi[1])),
+                                       __fmul_rn(0.5f, __fadd_rn(lo[2], hi[2])), 0.0f);
+            a.cl_bbh[cw] = make_float4(__fmul_rn(0.5f, __fsub_rn(hi[0], lo[0])),
+                                       __fmul_rn(0.5f, __fsub_rn(hi[1], lo[1])),
+                                       __fmul_rn(0.5f, __fsub_rn(hi[2], lo[2])), 0.0f);
+            a.cl_link[cw] = many ? make_int4(-2, -2, -2, -2)
+                                 : make_int4(link[0], link[1], link[2], link[3]);
+            atomicMax(&a.extz[r], __float_as_uint(fmaxf(hi[2], 0.0f)));
+        }
+    }
+}
+
+__device__ __forceinline__ bool replica_image_mode(const SdmArgs& a, const SdmSys& S, int r) {
+    if (S.img_static) return true;
+    const double ez = fmax(S.g[2], (double)__uint_as_float(a.extz[r]));
+    return !(0.5 * S.box[2] - S.rc - ez > 1.0e-3);
+}
+
+// ------------------------------------------------------------------------- //
+// K6: main pass                                                             //
+// ------------------------------------------------------------------------- //
+enum { MODE_EVAL = 0, MODE_COUNT = 1, MODE_EMIT = 2 };
+
+struct WarpSmem {
+    int4 jl[SDM_JL_CAP];        // (J | needmask<<31, Sx, Sy, Sz)
+    int4 rng[32];               // (Jbegin, prefix, Sx bits, Sy bits)
+    float4 ja[SDM_RING];        // (xs, ys, zs, q)
+    float4 jb[SDM_RING];        // (hs, se, mask bits, slot bits)
+};
+
+struct ICluster {
+    float x[8], y[8], z[8], q[8], hs[8], se[8];
+    float fx[8], fy[8], fz[8];
+};
+
+template <int MODE, bool IMG>
+__device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
+                                          WarpSmem& sm, unsigned head, int count, ICluster& ic,
+                                          double& ed, long long& npair) {
+    const int lane = lane_id();
+    const unsigned idx = (head + lane) & (SDM_RING - 1);
+    const bool active = lane < count;
+    // inactive lanes use zeros, never stale ring contents
+    const float4 A = active ? sm.ja[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 B = active ? sm.jb[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned m = active ? __float_as_uint(B.z) : 0u;
+    const float xs = A.x, ys = A.y, zs = A.z, qj = A.w, hj = B.x, ej = B.y;
+    const float rc2 = S.rc2f, krf = S.krf, crf = S.crf, krf2 = -2.0f * S.krf;
+    float fjx = 0.f, fjy = 0.f, fjz = 0.f, e = 0.f;
+    int cnt = 0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        float dx = __fsub_rn(xs, ic.x[t]);
+        float dy = __fsub_rn(ys, ic.y[t]);
+        float dz = __fsub_rn(zs, ic.z[t]);
+        if (IMG) {
+            dx = img32(dx, S.Lf[0], S.invLf[0]);
+            dy = img32(dy, S.Lf[1], S.invLf[1]);
+            dz = img32(dz, S.Lf[2], S.invLf[2]);
+        }
+        const float r2 = r2_chain(dx, dy, dz);
+        const bool ok = (r2 < rc2) && ((m >> t) & 1u);
+        if (MODE == MODE_COUNT) {
+            cnt += ok ? 1 : 0;
+        } else {
+            const float r2s = ok ? r2 : 1.0f;
+            const float ir = fast_rsqrt(r2s);
+            const float ir2 = ir * ir;
+            const float sg = ic.hs[t] + hj;
+            const float s2 = sg * sg * ir2;
+            const float s6 = s2 * s2 * s2;
+            const float epsm = ok ? ic.se[t] * ej : 0.0f;
+            const float qqm = ok ? ic.q[t] * qj : 0.0f;
+            const float t6 = epsm * s6;
+            e = fmaf(t6, s6 - 1.0f, e);
+            e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
+            const float fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qqm * fmaf(krf2, r2s, ir)) * ir2;
+            fjx = fmaf(fs, dx, fjx);
+            fjy = fmaf(fs, dy, fjy);
+            fjz = fmaf(fs, dz, fjz);
+            ic.fx[t] = fmaf(-fs, dx, ic.fx[t]);
+            ic.fy[t] = fmaf(-fs, dy, ic.fy[t]);
+            ic.fz[t] = fmaf(-fs, dz, ic.fz[t]);
+        }
+    }
+    if (MODE == MODE_COUNT) {
+        npair += cnt;
+    } else if (active) {
+        const int slot = __float_as_int(B.w);
+        const size_t gsl = (size_t)R.slot_win + slot;
+        red_fixed(a.F0x + gsl, fjx, a.status);
+        red_fixed(a.F0y + gsl, fjy, a.status);
+        red_fixed(a.F0z + gsl, fjz, a.status);
+        ed += (double)e;
+    }
+}
+
+// Computes the allowed-i mask of candidate slot j (cluster J) against
+// i-cluster I (valid-i bits vmask).
+__device__ __forceinline__ unsigned j_mask(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
+                                           int I, int J, int sj, unsigned vmask, bool needmask) {
+    unsigned m = vmask;
+    if (!needmask) return m;
+    const int t = sj & 7;
+    if (J == I) m &= (1u << t) - 1u;
+    const int4 ex = a.excl4[R.slot_win + sj];
+    const int i0 = 8 * I;
+    if (ex.x == -2) {
+        const int p = a.perm[R.slot_win + sj];
+        const int ta = S.atom_base + p;
+        for (int k = a.excl_off[ta]; k < a.excl_off[ta + 1]; ++k) {
+            const int s2 = a.inv[R.atom_win + a.excl_idx[k]];
+            if (s2 >= i0 && s2 < i0 + 8) m &= ~(1u << (s2 - i0));
+        }
+    } else {
+        const int e4[4] = {ex.x, ex.y, ex.z, ex.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (e4[k] >= i0 && e4[k] < i0 + 8) m &= ~(1u << (e4[k] - i0));
+    }
+    return m;
+}
+
+template <int MODE, bool IMG>
+__device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSmem& sm) {
+    const int lane = lane_id();
+    const SdmRep R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int cw = R.cl_win + I;
+    const int slot0 = R.slot_win + 8 * I;
+    // i-cluster particles, replicated in every lane
+    ICluster ic;
+    {
+        float4 xi4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 pi2 = make_float2(0.f, 0.f);
+        if (lane < 8) { xi4 = a.clX[slot0 + lane]; pi2 = a.clP[slot0 + lane]; }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            ic.x[t] = __shfl_sync(0xffffffffu, xi4.x, t);
+            ic.y[t] = __shfl_sync(0xffffffffu, xi4.y, t);
+            ic.z[t] = __shfl_sync(0xffffffffu, xi4.z, t);
+            ic.q[t] = __shfl_sync(0xffffffffu, xi4.w, t);
+            ic.hs[t] = __shfl_sync(0xffffffffu, pi2.x, t);
+            ic.se[t] = __shfl_sync(0xffffffffu, pi2.y, t);
+            ic.fx[t] = 0.f; ic.fy[t] = 0.f; ic.fz[t] = 0.f;
+        }
+    }
+    const unsigned vmask = __ballot_sync(0xffffffffu, lane < 8 && a.perm[slot0 + (lane & 7)] >= 0) & 0xffu;
+    const float4 bc = a.cl_bbc[cw];
+    const float4 bh = a.cl_bbh[cw];
+    const int4 ref = a.cl_ref[cw];
+    const float rcl2 = S.rcl2f;
+    const float rclc = S.rcl + 2.0e-4f;
+    const float rclc2 = rclc * rclc;
+    const float* tabx = a.shift_tab + S.shift_base;
+    const float* taby = tabx + 2 * S.M[0] + 1;
+    const float* tabz = taby + 2 * S.M[1] + 1;
+    const int nyst = S.sthi[1] - S.stlo[1] + 1;
+    const int nst = (S.sthi[0] - S.stlo[0] + 1) * nyst;
+    const int kbeg = (nst * part) / a.split, kend = (nst * (part + 1)) / a.split;
+    const int* colcl = a.col_cl + R.col_win;
+
+    int jl_n = 0;               // J-list entries (uniform)
+    unsigned head = 0, tail = 0;  // ring counters (uniform)
+    double ed = 0.0;
+    long long npair = 0;
+    int emit_n = 0;
+
+    auto phase_b = [&]() {
+        for (int g0 = 0; g0 < jl_n; g0 += 4) {
+            const int e = g0 + (lane >> 3);
+            const int t = lane & 7;
+            bool pass = false;
+            float xs = 0.f, ys = 0.f, zs = 0.f, qj = 0.f;
+            int sj = 0;
+            unsigned m = 0;
+            if (e < jl_n) {
+                const int4 en = sm.jl[e];
+                const int J = en.x & 0x7fffffff;
+                const bool nm = en.x < 0;
+                sj = 8 * J + t;
+                const float4 X4 = a.clX[R.slot_win + sj];
+                xs = __fadd_rn(X4.x, __int_as_float(en.y));
+                ys = __fadd_rn(X4.y, __int_as_float(en.z));
+                zs = __fadd_rn(X4.z, __int_as_float(en.w));
+                qj = X4.w;
+                float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
+                if (IMG) {
+                    tx = img32(tx, S.Lf[0], S.invLf[0]);
+                    ty = img32(ty, S.Lf[1], S.invLf[1]);
+                    tz = img32(tz, S.Lf[2], S.invLf[2]);
+                }
+                const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
+                const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
+                const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
+                // padding slots carry 1e6 coordinates; in image mode they could wrap
+                pass = (X4.x < 1.0e5f) && r2_chain(ex, ey, ez) < rcl2;
+                if (pass) {
+                    m = j_mask(a, S, R, I, J, sj, vmask, nm);
+                    pass = m != 0u;
+                }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, pass);
+            const int pos = __popc(bal & ((1u << lane) - 1u));
+            if (MODE == MODE_EMIT) {
+                if (pass && emit_n + pos < a.ex_cap) {
+                    const size_t o = (size_t)I * a.ex_cap + emit_n + pos;
+                    a.ex_slot[o] = sj;
+                    a.ex_mask[o] = (unsigned char)m;
+                }
+                emit_n += __popc(bal);
+                continue;
+            }
+            if (pass) {
+                const float2 P = a.clP[R.slot_win + sj];
+                const unsigned idx = (tail + pos) & (SDM_RING - 1);
+                sm.ja[idx] = make_float4(xs, ys, zs, qj);
+                sm.jb[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
+            }
+            tail += __popc(bal);
+            __syncwarp();
+            while (tail - head >= 32u) {
+                eval_tile<MODE, IMG>(a, S, R, sm, head, 32, ic, ed, npair);
+                head += 32u;
+            }
+            __syncwarp();
+        }
+        jl_n = 0;
+    };
+
+    for (int k0 = kbeg; k0 < kend; k0 += 32) {
+        // ranges of clusters from up to 32 stencil columns
+        const int k = k0 + lane;
+        int cntJ = 0, Jb = 0;
+        float Sx = 0.f, Sy = 0.f;
+        if (k < kend) {
+            const int ox = S.stlo[0] + k / nyst;
+            const int oy = S.stlo[1] + k % nyst;
+            const int ccx = pmod(ref.x + ox, S.M[0]);
+            const int ccy = pmod(ref.y + oy, S.M[1]);
+            const int colid = ccx * S.M[1] + ccy;
+            bool ok = colid >= ref.w;
+            Sx = tabx[wrap_cell(ccx - ref.x, S.M[0]) + S.M[0]];
+            Sy = taby[wrap_cell(ccy - ref.y, S.M[1]) + S.M[1]];
+            if (!IMG && ok) {
+                // conservative xy gap between the i box and the column's slab
+                const float lox = Sx - 1.0e-4f, hix = Sx + S.gf[0] + 1.0e-4f;
+                const float loy = Sy - 1.0e-4f, hiy = Sy + S.gf[1] + 1.0e-4f;
+                const float gx = fmaxf(0.0f, fmaxf(lox - (bc.x + bh.x), (bc.x - bh.x) - hix));
+                const float gy = fmaxf(0.0f, fmaxf(loy - (bc.y + bh.y), (bc.y - bh.y) - hiy));
+                ok = gx * gx + gy * gy < rclc2;
+            }
+            if (ok) {
+                Jb = (colid == ref.w) ? I : colcl[colid];
+                const int Je = colcl[colid + 1];
+                cntJ = max(Je - Jb, 0);
+            }
+        }
+        const bool has = cntJ > 0;
+        const unsigned hb = __ballot_sync(0xffffffffu, has);
+        int incl = cntJ;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (has) {
+            const int ri = __popc(hb & ((1u << lane) - 1u));
+            sm.rng[ri] = make_int4(Jb, incl - cntJ, __float_as_int(Sx), __float_as_int(Sy));
+        }
+        const int nr = __popc(hb);
+        __syncwarp();
+        for (int e0 = 0; e0 < total; e0 += 32) {
+            const int e = e0 + lane;
+            bool pass = false;
+            int4 en = make_int4(0, 0, 0, 0);
+            if (e < total) {
+                int lo = 0, hi = nr - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sm.rng[mid].y <= e) lo = mid; else hi = mid - 1;
+                }
+                const int4 rg = sm.rng[lo];
+                const int J = rg.x + (e - rg.y);
+                const int jw = R.cl_win + J;
+                const int4 rj = a.cl_ref[jw];
+                const float sz = tabz[wrap_cell(rj.z - ref.z, S.M[2]) + S.M[2]];
+                const float sx = __int_as_float(rg.z), sy = __int_as_float(rg.w);
+                const float4 cj = a.cl_bbc[jw];
+                const float4 hjb = a.cl_bbh[jw];
+                float dx = cj.x + sx - bc.x, dy = cj.y + sy - bc.y, dz = cj.z + sz - bc.z;
+                if (IMG) {
+                    dx = img32(dx, S.Lf[0], S.invLf[0]);
+                    dy = img32(dy, S.Lf[1], S.invLf[1]);
+                    dz = img32(dz, S.Lf[2], S.invLf[2]);
+                }
+                const float gx = fmaxf(fabsf(dx) - bh.x - hjb.x, 0.0f);
+                const float gy = fmaxf(fabsf(dy) - bh.y - hjb.y, 0.0f);
+                const float gz = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
+                pass = gx * gx + gy * gy + gz * gz < rclc2;
+                if (pass) {
+                    const int4 lk = a.cl_link[jw];
+                    const bool nm = (J == I) || lk.x == -2 || lk.x == I || lk.y == I ||
+                                    lk.z == I || lk.w == I;
+                    en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(sx),
+                                   __float_as_int(sy), __float_as_int(sz));
+                }
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, pass);
+            if (pass) sm.jl[jl_n + __popc(bal & ((1u << lane) - 1u))] = en;
+            jl_n += __popc(bal);
+            __syncwarp();
+            if (jl_n > SDM_JL_CAP - 32) phase_b();
+        }
+        __syncwarp();
+    }
+    phase_b();
+    if (MODE == MODE_EMIT) {
+        if (lane == 0) {
+            a.ex_cnt[I] = emit_n;
+            if (emit_n > a.ex_cap) atomicOr(a.status, 1 << 16);
+        }
+        return;
+    }
+    if (tail != head) {
+        eval_tile<MODE, IMG>(a, S, R, sm, head, (int)(tail - head), ic, ed, npair);
+        head = tail;
+    }
+    if (MODE == MODE_COUNT) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) npair += __shfl_xor_sync(0xffffffffu, npair, o);
+        if (lane == 0) atomicAdd((unsigned long long*)&a.counts[2 * r], (unsigned long long)npair);
+        return;
+    }
+    // reduce-scatter of the 24 i-force partial sums
+    float v[24];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) { v[3 * t] = ic.fx[t]; v[3 * t + 1] = ic.fy[t]; v[3 * t + 2] = ic.fz[t]; }
+    {
+        const bool up = lane & 16;
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+            const float send = up ? v[k] : v[k + 12];
+            const float keep = up ? v[k + 12] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+    }
+    {
+        const bool up = lane & 8;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float send = up ? v[k] : v[k + 6];
+            const float keep = up ? v[k + 6] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+    }
+    {
+        const bool up = lane & 4;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float send = up ? v[k] : v[k + 3];
+            const float keep = up ? v[k + 3] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        v[k] += __shfl_xor_sync(0xffffffffu, v[k], 2);
+        v[k] += __shfl_xor_sync(0xffffffffu, v[k], 1);
+    }
+    if ((lane & 3) == 0) {
+        const int t = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+        if ((vmask >> t) & 1u) {
+            const size_t gsl = (size_t)slot0 + t;
+            red_fixed(a.F0x + gsl, v[0], a.status);
+            red_fixed(a.F0y + gsl, v[1], a.status);
+            red_fixed(a.F0z + gsl, v[2], a.status);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ed += __shfl_xor_sync(0xffffffffu, ed, o);
+    if (lane == 0) a.e_part[(size_t)cw * a.split + part] = ed;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(SDM_WARPS * 32, 3)
+k_pair(SdmArgs a, const int* item_prefix) {
+    __shared__ WarpSmem smem[SDM_WARPS];
+    WarpSmem& sm = smem[threadIdx.x >> 5];
+    const int lane = lane_id();
+    const int total = item_prefix[a.nrep];
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(&a.work_counter[0], 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        const int r = rep_by_item(item_prefix, a.nrep, item);
+        const int local = item - item_prefix[r];
+        const int I = local / a.split, part = local - I * a.split;
+        if (MODE == MODE_EMIT && r != a.ex_rep) continue;
+        const SdmSys& S = a.sys[a.rep[r].sys];
+        if (replica_image_mode(a, S, r)) process_cluster<MODE, true>(a, r, I, part, sm);
+        else process_cluster<MODE, false>(a, r, I, part, sm);
+    }
+}
+
+// ------------------------------------------------------------------------- //
+// K7: perturbation pass                                                     //
+// ------------------------------------------------------------------------- //
+__device__ __forceinline__ void pair_terms(const SdmSys& S, float r2, float qq, float sg, float eps4,
+                                           float& e, float& fs) {
+    const float ir = fast_rsqrt(r2);
+    const float ir2 = ir * ir;
+    const float s2 = sg * sg * ir2;
+    const float s6 = s2 * s2 * s2;
+    const float t6 = eps4 * s6;
+    e = fmaf(t6, s6 - 1.0f, qq * fmaf(S.krf, r2, ir - S.crf));
+    fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qq * fmaf(-2.0f * S.krf, r2, ir)) * ir2;
+}
+
+template <int MODE, bool IMG>
+__device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm) {
+    const int lane = lane_id();
+    const SdmRep R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int pidx = local >> 1, st = local & 1;
+    const float sgn = st ? 1.0f : -1.0f;
+    const int p = a.D_idx[S.D_base + pidx];
+    const int tp = S.atom_base + p;
+    const int gp = a.topo_grp[tp];
+    double y[3];
+    int cy[3];
+    float o[3];
+    const double* wp = a.w + 3 * (size_t)(R.atom_win + p);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double v = st ? __dadd_rn(wp[k], a.topo_d[3 * (size_t)tp + k]) : wp[k];
+        y[k] = wrap1(v, S.box[k], S.invL[k]);
+        cy[k] = cell_of(y[k], S.invg[k], S.M[k]);
+        o[k] = __double2float_rn(__dsub_rn(y[k], __dmul_rn((double)cy[k], S.g[k])));
+    }
+    const float qp = a.topo_q[tp], hp = a.topo_hs[tp], sp_ = a.topo_se[tp];
+    const int cxb = a.cx_off[S.cx_base + pidx], cxe = a.cx_off[S.cx_base + pidx + 1];
+    const float rcl2 = S.rcl2f;
+    const float rclc = S.rcl + 2.0e-4f;
+    const float rclc2 = rclc * rclc;
+    const float* tabx = a.shift_tab + S.shift_base;
+    const float* taby = tabx + 2 * S.M[0] + 1;
+    const float* tabz = taby + 2 * S.M[1] + 1;
+    const int nyst = S.sthi[1] - S.stlo[1] + 1;
+    const int nst = (S.sthi[0] - S.stlo[0] + 1) * nyst;
+    const int* colcl = a.col_cl + R.col_win;
+    double ed = 0.0;
+    float fpx = 0.f, fpy = 0.f, fpz = 0.f;
+    long long npair = 0;
+    int jl_n = 0;
+
+    auto eval_j = [&](float dx, float dy, float dz, float r2, float qj, float hj, float ej, int sj) {
+        float e, fs;
+        pair_terms(S, r2, qp * qj, hp + hj, sp_ * ej, e, fs);
+        ed += (double)(sgn * e);
+        const float f = sgn * fs;
+        if (sj >= 0) {
+            const size_t gsl = (size_t)R.slot_win + sj;
+            red_fixed(a.dFx + gsl, f * dx, a.status);
+            red_fixed(a.dFy + gsl, f * dy, a.status);
+            red_fixed(a.dFz + gsl, f * dz, a.status);
+        }
+        fpx = fmaf(-f, dx, fpx);
+        fpy = fmaf(-f, dy, fpy);
+        fpz = fmaf(-f, dz, fpz);
+    };
+
+    auto phase_b = [&]() {
+        for (int g0 = 0; g0 < jl_n; g0 += 4) {
+            const int e = g0 + (lane >> 3);
+            if (e < jl_n) {
+                const int4 en = sm.jl[e];
+                const int sj = 8 * en.x + (lane & 7);
+                const size_t gsl = (size_t)R.slot_win + sj;
+                const float4 X4 = a.clX[gsl];
+                float dx = __fsub_rn(__fadd_rn(X4.x, __int_as_float(en.y)), o[0]);
+                float dy = __fsub_rn(__fadd_rn(X4.y, __int_as_float(en.z)), o[1]);
+                float dz = __fsub_rn(__fadd_rn(X4.z, __int_as_float(en.w)), o[2]);
+                if (IMG) {
+                    dx = img32(dx, S.Lf[0], S.invLf[0]);
+                    dy = img32(dy, S.Lf[1], S.invLf[1]);
+                    dz = img32(dz, S.Lf[2], S.invLf[2]);
+                }
+                const float r2 = r2_chain(dx, dy, dz);
+                bool ok = (r2 < S.rc2f) && X4.x < 1.0e5f && a.grp[gsl] == 0;
+                if (ok && cxe > cxb) {
+                    const int pj = a.perm[gsl];
+                    for (int k = cxb; k < cxe; ++k) ok = ok && (a.cx_idx[k] != pj);
+                }
+                if (ok) {
+                    if (MODE == MODE_COUNT) npair += st;
+                    else {
+                        const float2 P = a.clP[gsl];
+                        eval_j(dx, dy, dz, r2, X4.w, P.x, P.y, sj);
+                    }
+                }
+            }
+        }
+        jl_n = 0;
+    };
+
+    for (int k0 = 0; k0 < nst; k0 += 32) {
+        const int k = k0 + lane;
+        int cntJ = 0, Jb = 0;
+        float Sx = 0.f, Sy = 0.f;
+        if (k < nst) {
+            const int ox = S.stlo[0] + k / nyst;
+            const int oy = S.stlo[1] + k % nyst;
+            const int ccx = pmod(cy[0] + ox, S.M[0]);
+            const int ccy = pmod(cy[1] + oy, S.M[1]);
+            const int colid = ccx * S.M[1] + ccy;
+            Sx = tabx[wrap_cell(ccx - cy[0], S.M[0]) + S.M[0]];
+            Sy = taby[wrap_cell(ccy - cy[1], S.M[1]) + S.M[1]];
+            bool ok = true;
+            if (!IMG) {
+                const float lox = Sx - 1.0e-4f, hix = Sx + S.gf[0] + 1.0e-4f;
+                const float loy = Sy - 1.0e-4f, hiy = Sy + S.gf[1] + 1.0e-4f;
+                const float gx = fmaxf(0.0f, fmaxf(lox - o[0], o[0] - hix));
+                const float gy = fmaxf(0.0f, fmaxf(loy - o[1], o[1] - hiy));
+                ok = gx * gx + gy * gy < rclc2;
+            }
+            if (ok) {
+                Jb = colcl[colid];
+                cntJ = max(colcl[colid + 1] - Jb, 0);
+            }
+        }
+        const bool has = cntJ > 0;
+        const unsigned hb = __ballot_sync(0xffffffffu, has);
+        int incl = cntJ;
+#pragma unroll
+        for (int oo = 1; oo < 32; oo <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, oo);
+            if (lane >= oo) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (has) {
+            const int ri = __popc(hb & ((1u << lane) - 1u));
+            sm.rng[ri] = make_int4(Jb, incl - cntJ, __float_as_int(Sx), __float_as_int(Sy));
+        }
+        const int nr = __popc(hb);
+        __syncwarp();
+        for (int e0 = 0; e0 < total; e0 += 32) {
+            const int e = e0 + lane;
+            bool pass = false;
+            int4 en = make_int4(0, 0, 0, 0);
+            if (e < total) {
+                int lo = 0, hi = nr - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sm.rng[mid].y <= e) lo = mid; else hi = mid - 1;
+                }
+                const int4 rg = sm.rng[lo];
+                const int J = rg.x + (e - rg.y);
+                const int jw = R.cl_win + J;
+                const int4 rj = a.cl_ref[jw];
+                const float sz = tabz[wrap_cell(rj.z - cy[2], S.M[2]) + S.M[2]];
+                const float sx = __int_as_float(rg.z), sy = __int_as_float(rg.w);
+                const float4 cj = a.cl_bbc[jw];
+                const float4 hjb = a.cl_bbh[jw];
+                float dx = cj.x + sx - o[0], dy = cj.y + sy - o[1], dz = cj.z + sz - o[2];
+                if (IMG) {
+                    dx = img32(dx, S.Lf[0], S.invLf[0]);
+                    dy = img32(dy, S.Lf[1], S.invLf[1]);
+                    dz = img32(dz, S.Lf[2], S.invLf[2]);
+                }
+                const float gx = fmaxf(fabsf(dx) - hjb.x, 0.0f);
+                const float gy = fmaxf(fabsf(dy) - hjb.y, 0.0f);
+                const float gz = fmaxf(fabsf(dz) - hjb.z, 0.0f);
+                pass = gx * gx + gy * gy + gz * gz < rclc2;
+                en = make_int4(J, __float_as_int(sx), __float_as_int(sy), __float_as_int(sz));
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, pass);
+            if (pass) sm.jl[jl_n + __popc(bal & ((1u << lane) - 1u))] = en;
+            jl_n += __popc(bal);
+            __syncwarp();
+            if (jl_n > SDM_JL_CAP - 32) phase_b();
+            __syncwarp();
+        }
+    }
+    phase_b();
+    // displaced-displaced pairs with different displacement vectors
+    for (int q0 = 0; q0 < S.nD; q0 += 32) {
+        const int qi = q0 + lane;
+        if (qi < S.nD) {
+            const int qa = a.D_idx[S.D_base + qi];
+            const int tq = S.atom_base + qa;
+            const int gq = a.topo_grp[tq];
+            if (gq != gp && gq != 0 && qa > p) {
+                const double* wq = a.w + 3 * (size_t)(R.atom_win + qa);
+                float d[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const double vq = st ? __dadd_rn(wq[k], a.topo_d[3 * (size_t)tq + k]) : wq[k];
+                    const double yq = wrap1(vq, S.box[k], S.invL[k]);
+                    double v = __dsub_rn(yq, y[k]);
+                    const double tt = rint(__dmul_rn(v, S.invL[k]));
+                    v = __dsub_rn(v, __dmul_rn(tt, S.box[k]));
+                    d[k] = __double2float_rn(v);
+                }
+                const float r2 = r2_chain(d[0], d[1], d[2]);
+                bool ok = r2 < S.rc2f;
+                for (int k = cxb; k < cxe && ok; ++k) ok = (a.cx_idx[k] != qa);
+                if (ok) {
+                    if (MODE == MODE_COUNT) npair += st;
+                    else eval_j(d[0], d[1], d[2], r2, a.topo_q[tq], a.topo_hs[tq], a.topo_se[tq],
+                                a.inv[R.atom_win + qa]);
+                }
+            }
+        }
+    }
+    if (MODE == MODE_COUNT) {
+#pragma unroll
+        for (int oo = 16; oo > 0; oo >>= 1) npair += __shfl_xor_sync(0xffffffffu, npair, oo);
+        if (lane == 0 && npair) atomicAdd((unsigned long long*)&a.counts[2 * r + 1], (unsigned long long)npair);
+        return;
+    }
+#pragma unroll
+    for (int oo = 16; oo > 0; oo >>= 1) {
+        fpx += __shfl_xor_sync(0xffffffffu, fpx, oo);
+        fpy += __shfl_xor_sync(0xffffffffu, fpy, oo);
+        fpz += __shfl_xor_sync(0xffffffffu, fpz, oo);
+        ed += __shfl_xor_sync(0xffffffffu, ed, oo);
+    }
+    if (lane == 0) {
+        const size_t gsl = (size_t)R.slot_win + a.inv[R.atom_win + p];
+        red_fixed(a.dFx + gsl, fpx, a.status);
+        red_fixed(a.dFy + gsl, fpy, a.status);
+        red_fixed(a.dFz + gsl, fpz, a.status);
+        a.p_part[R.pert_win + local] = ed;
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(SDM_WARPS * 32) k_perturb(SdmArgs a) {
+    __shared__ WarpSmem smem[SDM_WARPS];
+    WarpSmem& sm = smem[threadIdx.x >> 5];
+    const int lane = lane_id();
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(&a.work_counter[1], 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= a.total_pert) break;
+        const int r = rep_by_pert(a.rep, a.nrep, item);
+        const int local = item - a.rep[r].pert_win;
+        const SdmSys& S = a.sys[a.rep[r].sys];
+        if (replica_image_mode(a, S, r)) process_perturb<MODE, true>(a, r, local, sm);
+        else process_perturb<MODE, false>(a, r, local, sm);
+    }
+}
+
+// ------------------------------------------------------------------------- //
+// K8: energies, soft core, bias (FP64)                                      //
+// ------------------------------------------------------------------------- //
+__device__ double block_sum(double v, double* red) {
+    // deterministic: fixed-shape tree over a fixed partition
+    const int t = threadIdx.x;
+    red[t] = v;
+    __syncthreads();
+    for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+        if (t < s) red[t] += red[t + s];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+// soft core of openmmapi/src/LangevinIntegratorSDM.cpp:125-149
+__device__ double softcore(double u, int method, double umax, double a, double ub, double* fp) {
+    if (u <= ub || method == SDM_NO_SOFTCORE) { *fp = 1.0; return u; }
+    if (method == SDM_TANH_SOFTCORE) {
+        const double t = tanh((u - ub) / umax);
+        *fp = 1.0 - t * t;
+        return umax * t + ub;
+    }
+    const double gu = (u - ub) / (a * (umax - ub));
+    const double zeta = 1.0 + 2.0 * gu * (gu + 1.0);
+    const double za = pow(zeta, a);
+    *fp = 4.0 * (2.0 * gu + 1.0) / zeta * za / ((1.0 + za) * (1.0 + za));
+    return (umax - ub) * (za - 1.0) / (za + 1.0) + ub;
+}
+
+__global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
+    __shared__ double red[256];
+    const int r = blockIdx.x;
+    const SdmRep& R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int ncl = a.ncl[r];
+    double e0 = 0.0;
+    const double* ep = a.e_part + (size_t)R.cl_win * a.split;
+    for (int k = threadIdx.x; k < ncl * a.split; k += blockDim.x) e0 += ep[k];
+    const double U0 = block_sum(e0, red);
+    double eu = 0.0;
+    for (int k = threadIdx.x; k < 2 * S.nD; k += blockDim.x) eu += a.p_part[R.pert_win + k];
+    const double u = block_sum(eu, red);
+    if (threadIdx.x != 0) return;
+    const double* p = a.params + (size_t)r * SDM_NPARAMS;
+    const int method = (int)p[SDM_P_BIAS_METHOD];
+    const int noneq = (int)p[SDM_P_NONEQ];
+    const double lambdac = p[SDM_P_LAMBDA];
+    double gamma = 0.0, wb = lambdac, w0 = 0.0, l1 = lambdac, l2 = lambdac, alpha = 1.0, u0 = 0.0;
+    if (noneq == 1) {
+        l1 = p[SDM_P_M_LAMBDA1] * lambdac + p[SDM_P_B_LAMBDA1];
+        l2 = p[SDM_P_M_LAMBDA2] * lambdac + p[SDM_P_B_LAMBDA2];
+        u0 = p[SDM_P_M_U0] * lambdac + p[SDM_P_B_U0];
+        w0 = p[SDM_P_M_W0] * lambdac + p[SDM_P_B_W0];
+    }
+    if (method == SDM_QUADRATIC) {
+        gamma = p[SDM_P_GAMMA];
+        wb = p[SDM_P_WB];
+        if (noneq != 1) w0 = p[SDM_P_W0];
+    } else if (method == SDM_ILOGISTIC) {
+        if (noneq != 1) { l1 = p[SDM_P_LAMBDA1]; l2 = p[SDM_P_LAMBDA2]; u0 = p[SDM_P_U0]; w0 = p[SDM_P_W0]; }
+        alpha = p[SDM_P_ALPHA];
+    }
+    double fp;
+    const double be = softcore(u, (int)p[SDM_P_SOFTCORE_METHOD], p[SDM_P_UMAX], p[SDM_P_ACORE],
+                               p[SDM_P_UBCORE], &fp);
+    double ebias, bfp;
+    if (method == SDM_QUADRATIC) {
+        ebias = 0.5 * gamma * be * be + wb * be + w0;
+        bfp = gamma * be + wb;
+    } else if (method == SDM_ILOGISTIC) {
+        const double ee = 1.0 + exp(-alpha * (be - u0));
+        ebias = 0.0;
+        if (alpha > 0) ebias = ((l2 - l1) / alpha) * log(ee);
+        ebias += l2 * be + w0;
+        bfp = (l2 - l1) / ee + l1;
+    } else {
+        ebias = lambdac * be;
+        bfp = lambdac;
+    }
+    double dwdl = 0.0;
+    if (noneq == 1) {
+        const double ee = 1.0 + exp(-alpha * (be - u0));
+        dwdl = (-log(ee) / alpha) * p[SDM_P_M_LAMBDA1] + (be + log(ee) / alpha) * p[SDM_P_M_LAMBDA2] +
+               ((l2 - l1) * exp(-alpha * (be - u0)) / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
+    }
+    int st = *(volatile int*)a.status;
+    if (!isfinite(U0) || !isfinite(u)) { st |= SDM_DEV_ENERGY_NONFINITE; atomicOr(a.status, SDM_DEV_ENERGY_NONFINITE); }
+    double* o = a.results + (size_t)r * SDM_NRESULTS;
+    o[SDM_R_U0] = U0;
+    o[SDM_R_U1] = U0 + u;
+    o[SDM_R_U] = u;
+    o[SDM_R_BINDE] = be;
+    o[SDM_R_FP] = fp;
+    o[SDM_R_W] = ebias;
+    o[SDM_R_DW] = bfp;
+    o[SDM_R_S] = bfp * fp;
+    o[SDM_R_EPOT] = U0 + ebias;
+    o[SDM_R_DWDLAMBDA] = dwdl;
+    o[SDM_R_LAMBDA1] = l1;
+    o[SDM_R_LAMBDA2] = l2;
+    o[SDM_R_U0PARAM] = u0;
+    o[SDM_R_W0PARAM] = w0;
+    o[SDM_R_STATUS] = (double)st;
+    o[SDM_R_RESERVED] = (double)ncl;
+}
+
+// ------------------------------------------------------------------------- //
+// K9: mix                                                                   //
+// ------------------------------------------------------------------------- //
+__global__ void k_mix(SdmArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    const double sc = 1.0 / SDM_FIX_SCALE;
+    for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < a.total_atoms; gi += stride) {
+        const int r = rep_by_atom(a.rep, a.nrep, gi);
+        const SdmRep& R = a.rep[r];
+        const int i = gi - R.atom_win;
+        const size_t gsl = (size_t)R.slot_win + a.inv[gi];
+        const double s = a.forces ? a.results[(size_t)r * SDM_NRESULTS + SDM_R_S] : 0.0;
+        const double f0[3] = {(double)(long long)a.F0x[gsl] * sc, (double)(long long)a.F0y[gsl] * sc,
+                              (double)(long long)a.F0z[gsl] * sc};
+        const double df[3] = {(double)(long long)a.dFx[gsl] * sc, (double)(long long)a.dFy[gsl] * sc,
+                              (double)(long long)a.dFz[gsl] * sc};
+        const size_t o = 3 * (size_t)(R.x_off + i);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (a.forces) a.forces[o + k] = f0[k] + s * df[k];
+            if (a.F0out) a.F0out[o + k] = f0[k];
+            if (a.F1out) a.F1out[o + k] = f0[k] + df[k];
+        }
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------- //
+// launchers (called by sdm_capi.cpp)                                        //
+// ------------------------------------------------------------------------- //
+static int g_num_sms = 0;
+
+static int num_sms() {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    return g_num_sms;
+}
+
+static int grid_for(long long n, int block) {
+    long long g = (n + block - 1) / block;
+    long long cap = (long long)num_sms() * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+extern "C++" {
+
+cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* done, cudaStream_t st,
+                            cudaEvent_t* ev, int nev) {
+    int e = 0;
+    auto mark = [&]() { if (ev && e < nev) cudaEventRecord(ev[e++], st); };
+    mark();
+    k_cells<<<grid_for(a.total_atoms > a.total_slots ? a.total_atoms : a.total_slots, 256), 256, 0, st>>>(a);
+    mark();
+    k_scan<<<a.nrep, 1024, 0, st>>>(a, item_prefix, done);
+    mark();
+    k_bucket<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
+    mark();
+    k_colsort<<<grid_for((long long)a.total_cols * 32, 128), 128, 0, st>>>(a);
+    mark();
+    k_clusters<<<grid_for(a.total_slots, 256), 256, 0, st>>>(a);
+    mark();
+    return cudaGetLastError();
+}
+
+cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
+                            cudaStream_t st) {
+    const int grid = num_sms() * ctas_per_sm;
+    if (mode == MODE_EVAL) k_pair<MODE_EVAL><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+    else if (mode == MODE_COUNT) k_pair<MODE_COUNT><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+    else k_pair<MODE_EMIT><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+    return cudaGetLastError();
+}
+
+cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st) {
+    if (a.total_pert == 0) return cudaSuccess;
+    int grid = (a.total_pert + SDM_WARPS - 1) / SDM_WARPS;
+    const int cap = num_sms() * 4;
+    if (grid > cap) grid = cap;
+    if (mode == MODE_COUNT) k_perturb<MODE_COUNT><<<grid, SDM_WARPS * 32, 0, st>>>(a);
+    else k_perturb<MODE_EVAL><<<grid, SDM_WARPS * 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st) {
+    k_mix<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st) {
+    k_finalize<<<a.nrep, 256, 0, st>>>(a);
+    k_mix<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // extern "C++"

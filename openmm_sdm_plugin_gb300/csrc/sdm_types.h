@@ -1,0 +1,141 @@
+// sdm_types.h -- plain-old-data tables shared by the host orchestration
+// (sdm_capi.cpp) and the CUDA kernels (sdm_kernels.cu).
+//
+// HBM layout (all per-replica arrays are concatenated replica after replica,
+// each replica owning a fixed-capacity window computed at handle creation):
+//
+//   topology (per particle of every system, original order)
+//     topo_q   float   q * sqrt(K_coulomb)            (so qi*qj carries K)
+//     topo_hs  float   sigma / 2                      (sigma_ij = hs_i + hs_j)
+//     topo_se  float   2 sqrt(epsilon)                (se_i*se_j = 4 eps_ij)
+//     topo_grp int     displacement group (0 = not displaced)
+//     topo_d   double3 displacement
+//     excl_off/excl_idx  symmetric CSR of exclusions (system-local indices)
+//   per replica, particle-indexed (window = num_particles)
+//     w        double3 coordinates wrapped into the box
+//     cellinfo int2    (column id, z cell)
+//     inv      int     particle -> slot
+//   per replica, column-indexed (window = ncol+1)
+//     col_cnt, col_fill (counters), col_aoff (atom prefix), col_cl (cluster prefix)
+//   per replica, slot-indexed (window = slot_cap = num_particles + 8*ncol + 8)
+//     perm     int     slot -> particle (-1 padding)
+//     clX      float4  cluster-local x,y,z (FP32) and q*sqrt(K)
+//     clP      float2  sigma/2, 2 sqrt(eps)
+//     grp      int     displacement group of the slot's particle
+//     excl4    int4    up to 4 exclusion partners as slots (-1 none, -2 overflow)
+//     F0x/F0y/F0z, dFx/dFy/dFz   int64 fixed point 2^32
+//   per replica, cluster-indexed (window = slot_cap/8)
+//     cl_ref   int4    reference cell (cx, cy, cz) and column id
+//     cl_bbc   float4  bounding-box centre (cluster frame)
+//     cl_bbh   float4  bounding-box half extents
+//     cl_link  int4    clusters holding exclusion partners of this cluster (-1 none, -2 many)
+//     e_part   double  main-pass energy of the cluster's work items
+#pragma once
+#include <stdint.h>
+
+#define SDM_CL 8                 // particles per cluster
+#define SDM_FIX_SCALE 4294967296.0 // 2^32 fixed point for forces
+#define SDM_LIST_MARGIN 1.0e-4   // nm added to the cutoff in the list filter
+#define SDM_MAX_SPLIT 4
+
+struct SdmSys {
+    int n;            // particles
+    int atom_base;    // offset into the topology arrays
+    int excl_base;    // offset into excl_idx (excl_off is indexed atom_base + i, values are absolute)
+    int M[3];         // cells per axis
+    int ncol;         // M[0]*M[1]
+    int stlo[2], sthi[2];  // stencil column offsets per axis (x,y)
+    int img_static;   // 1 if the x/y extents already force per-pair minimum image
+    double box[3], invL[3], g[3], invg[3];
+    double rc;
+    float Lf[3], invLf[3];
+    float gf[3];      // (float)g, for conservative prefilters only
+    float rc2f;       // (float)(rc*rc): pair rule
+    float rcl, rcl2f; // list filter cutoff (rc + margin) and its square
+    float krf, crf;   // reaction-field constants (FP32)
+    int nD;           // displaced particles
+    int D_base;       // offset into D_idx
+    int shift_base;   // offset into shift_tab: 3 tables of 2*Mk+1 floats (index n+Mk)
+    int cx_base;      // offset into cx_off/cx_idx (changed-pair exclusions per displaced particle)
+};
+
+struct SdmRep {
+    int sys;
+    int n;            // particles of the system
+    long long x_off;  // particle offset into the concatenated coordinates / forces
+    int atom_win;     // particle-indexed window base
+    int col_win;      // column-indexed window base (ncol+1 per replica)
+    int slot_win;     // slot window base
+    int slot_cap;     // slots in the window
+    int cl_win;       // cluster window base (slot_win/8)
+    int pert_win;     // perturbation partial base (2*nD per replica)
+};
+
+// Everything a kernel needs, passed by value (fits the 32 KB parameter space).
+struct SdmArgs {
+    int nsys, nrep;
+    const SdmSys* sys;
+    const SdmRep* rep;
+    // topology
+    const float* topo_q;
+    const float* topo_hs;
+    const float* topo_se;
+    const int* topo_grp;
+    const double* topo_d;
+    const int* excl_off;
+    const int* excl_idx;
+    const int* D_idx;     // system-local particle indices of displaced particles
+    const int* cx_off;    // per displaced particle: changed-pair exclusion partners
+    const int* cx_idx;
+    const float* shift_tab;
+    const double* params; // nrep * SDM_NPARAMS
+    // input / output
+    const double* x;      // concatenated coordinates
+    double* results;      // nrep * SDM_NRESULTS
+    double* forces;       // mixed forces (may be null)
+    double* F0out;        // optional per-state forces
+    double* F1out;
+    // scratch
+    double* w;
+    int2* cellinfo;
+    int* inv;
+    int* col_cnt;
+    int* col_fill;
+    int* col_aoff;
+    int* col_cl;
+    int* bucket;
+    int* perm;
+    float4* clX;
+    float2* clP;
+    int* grp;
+    int4* excl4;
+    unsigned long long* F0x;
+    unsigned long long* F0y;
+    unsigned long long* F0z;
+    unsigned long long* dFx;
+    unsigned long long* dFy;
+    unsigned long long* dFz;
+    int4* cl_ref;
+    float4* cl_bbc;
+    float4* cl_bbh;
+    int4* cl_link;
+    double* e_part;      // cl window * SDM_MAX_SPLIT
+    double* p_part;      // perturbation partials
+    int* ncl;            // clusters per replica
+    unsigned* extz;      // per replica max cluster z extent (float bits)
+    int* work_counter;   // [0] main pass, [1] perturbation pass
+    int* status;         // device status word
+    long long* counts;   // optional: per replica P0, P1delta (count mode)
+    // list export (diagnostic)
+    int* ex_cnt;
+    int* ex_slot;
+    unsigned char* ex_mask;
+    int ex_cap;
+    int ex_rep;
+    // totals
+    int total_atoms;     // sum of n over replicas
+    int total_cols;      // sum of ncol over replicas
+    int total_slots;     // sum of slot_cap over replicas
+    int total_pert;      // sum of 2*nD
+    int split;           // work items per i-cluster
+};

@@ -1,0 +1,252 @@
+"""Host-side mirror of the reference's SDM parameter API over the C ABI.
+
+``SDMForce`` carries exactly the SDM parameter surface of the reference's
+``LangevinIntegratorSDM`` (openmmapi/include/LangevinIntegratorSDM.h:53-522,
+exposed to Python by python/SDMplugin.i:71-146): the same setter/getter
+names, argument meanings, defaults (openmmapi/src/LangevinIntegratorSDM.cpp:48-85)
+and error behaviour (an unknown soft-core method raises, as
+LangevinIntegratorSDM.cpp:147 throws).  On top of that it holds what the
+reference takes from OpenMM's NonbondedForce in force group 2: per-particle
+charge/sigma/epsilon, exclusions, cutoff, reaction-field dielectric and the
+periodic box.
+
+``evaluate`` does what one reference step does to the nonbonded group
+(LangevinIntegratorSDM.cpp:158-176 plus ReferenceSDMKernels.cpp:202-318 without
+the Langevin update) on the GPU and returns the hybrid energy and forces;
+``getBindE``/``getPotEnergy`` then return the values the reference's getters
+would.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import capi
+from .systems import SDMParams, SDMSystem
+
+
+class SDMForce:
+    # method ids (LangevinIntegratorSDM.h:120-122, :143-145)
+    LinearMethod = 0
+    QuadraticMethod = 1
+    ILogisticMethod = 2
+    NoSoftCoreMethod = 0
+    TanhMethod = 1
+    RationalMethod = 2
+
+    def __init__(self, nParticles: int = 0):
+        self._q: List[float] = []
+        self._sig: List[float] = []
+        self._eps: List[float] = []
+        self._excl: List[tuple] = []
+        self._displ = np.zeros((nParticles, 3))
+        for _ in range(nParticles):
+            self.addParticle(0.0, 0.0, 0.0)
+        self._box = np.array([0.0, 0.0, 0.0])
+        self._cutoff = 1.0
+        self._eps_rf = 78.3
+        self._p = SDMParams(bias_method=0, softcore_method=0, lambdac=1.0, lambda1=1.0,
+                            lambda2=1.0, alpha=1.0, u0=0.0, w0=0.0, gamma=0.0, wb=1.0,
+                            umax=200.0, acore=0.25, ubcore=0.0)
+        self._ntmax = 0.0
+        self._work = 0.0
+        self._bind_e = 0.0
+        self._pot_e = 0.0
+        self._last = None
+        self._handle: Optional[capi.Handle] = None
+        self._topology_dirty = True
+        self._displ_dirty = False
+        self._params_dirty = True
+
+    # -- NonbondedForce-like topology ---------------------------------------
+    def addParticle(self, charge: float, sigma: float, epsilon: float) -> int:
+        self._q.append(float(charge))
+        self._sig.append(float(sigma))
+        self._eps.append(float(epsilon))
+        if self._displ.shape[0] < len(self._q):
+            self._displ = np.vstack([self._displ, np.zeros((1, 3))])
+        self._topology_dirty = True
+        return len(self._q) - 1
+
+    def setParticleParameters(self, index: int, charge: float, sigma: float, epsilon: float):
+        self._q[index], self._sig[index], self._eps[index] = float(charge), float(sigma), float(epsilon)
+        self._topology_dirty = True
+
+    def getParticleParameters(self, index: int):
+        return self._q[index], self._sig[index], self._eps[index]
+
+    def getNumParticles(self) -> int:
+        return len(self._q)
+
+    def addExclusion(self, i: int, j: int) -> int:
+        self._excl.append((int(i), int(j)))
+        self._topology_dirty = True
+        return len(self._excl) - 1
+
+    def getNumExclusions(self) -> int:
+        return len(self._excl)
+
+    def setCutoffDistance(self, rc: float):
+        self._cutoff = float(rc)
+        self._topology_dirty = True
+
+    def getCutoffDistance(self) -> float:
+        return self._cutoff
+
+    def setReactionFieldDielectric(self, e: float):
+        self._eps_rf = float(e)
+        self._topology_dirty = True
+
+    def getReactionFieldDielectric(self) -> float:
+        return self._eps_rf
+
+    def setPeriodicBoxVectors(self, a, b, c):
+        a, b, c = (np.asarray(v, np.float64) for v in (a, b, c))
+        if np.count_nonzero(a[1:]) or b[0] or b[2] or c[0] or c[1]:
+            raise ValueError("only orthorhombic boxes are supported")
+        self._box = np.array([a[0], b[1], c[2]])
+        self._topology_dirty = True
+
+    def getPeriodicBoxVectors(self):
+        return (np.array([self._box[0], 0, 0]), np.array([0, self._box[1], 0]),
+                np.array([0, 0, self._box[2]]))
+
+    # -- SDM parameters (names of LangevinIntegratorSDM) --------------------
+    def _set(self, field, v):
+        setattr(self._p, field, float(v))
+        self._params_dirty = True
+
+    def setLambda(self, v): self._set("lambdac", v)
+    def getLambda(self): return self._p.lambdac
+    def setBiasMethod(self, m): self._p.bias_method = int(m); self._params_dirty = True
+    def getBiasMethod(self): return int(self._p.bias_method)
+    def setSoftCoreMethod(self, m): self._p.softcore_method = int(m); self._params_dirty = True
+    def getSoftCoreMethod(self): return int(self._p.softcore_method)
+    def setGamma(self, v): self._set("gamma", v)
+    def getGamma(self): return self._p.gamma
+    def setWBcoeff(self, v): self._set("wb", v)
+    def getWBcoeff(self): return self._p.wb
+    def setW0coeff(self, v): self._set("w0", v)
+    def getW0coeff(self): return self._p.w0
+    def setLambda1(self, v): self._set("lambda1", v)
+    def getLambda1(self): return self._p.lambda1
+    def setLambda2(self, v): self._set("lambda2", v)
+    def getLambda2(self): return self._p.lambda2
+    def setAlpha(self, v): self._set("alpha", v)
+    def getAlpha(self): return self._p.alpha
+    def setU0(self, v): self._set("u0", v)
+    def getU0(self): return self._p.u0
+    def setUmax(self, v): self._set("umax", v)
+    def getUmax(self): return self._p.umax
+    def setAcore(self, v): self._set("acore", v)
+    def getAcore(self): return self._p.acore
+    def setUbcore(self, v): self._set("ubcore", v)
+    def getUbcore(self): return self._p.ubcore
+    def setNoneqtmax(self, v): self._ntmax = float(v)
+    def getNoneqtmax(self): return self._ntmax
+    def setNonEquilibrium(self, v): self._p.noneq = int(v); self._params_dirty = True
+    def getNonEquilibrium(self): return int(self._p.noneq)
+    def setNoneqWorkvalue(self, v): self._work = float(v)
+    def getNoneqWorkvalue(self): return self._work
+    def setlambda1Slope(self, v): self._set("m_lambda1", v)
+    def getlambda1Slope(self): return self._p.m_lambda1
+    def setlambda2Slope(self, v): self._set("m_lambda2", v)
+    def getlambda2Slope(self): return self._p.m_lambda2
+    def setu0Slope(self, v): self._set("m_u0", v)
+    def getu0Slope(self): return self._p.m_u0
+    def setw0Slope(self, v): self._set("m_w0", v)
+    def getw0Slope(self): return self._p.m_w0
+    def setlambda1intercept(self, v): self._set("b_lambda1", v)
+    def getlambda1intercept(self): return self._p.b_lambda1
+    def setlambda2intercept(self, v): self._set("b_lambda2", v)
+    def getlambda2intercept(self): return self._p.b_lambda2
+    def setu0intercept(self, v): self._set("b_u0", v)
+    def getu0intercept(self): return self._p.b_u0
+    def setw0intercept(self, v): self._set("b_w0", v)
+    def getw0intercept(self): return self._p.b_w0
+
+    def setDisplacement(self, atom: int, dx: float, dy: float, dz: float):
+        self._displ[atom] = (dx, dy, dz)
+        self._displ_dirty = True
+
+    def getDisplacement(self, atom: int):
+        return tuple(float(v) for v in self._displ[atom])
+
+    def getBindE(self) -> float:
+        return self._bind_e
+
+    def setBindE(self, v: float):
+        self._bind_e = float(v)
+
+    def getPotEnergy(self) -> float:
+        return self._pot_e
+
+    def setPotEnergy(self, v: float):
+        self._pot_e = float(v)
+
+    def getPerturbationEnergy(self):
+        """(u, U0, U1, W, W') of the last evaluation."""
+        r = self._last
+        if r is None:
+            raise RuntimeError("no evaluation yet")
+        return (r[capi.R_U], r[capi.R_U0], r[capi.R_U1], r[capi.R_W], r[capi.R_DW])
+
+    # -- evaluation -------------------------------------------------------
+    def _system(self) -> SDMSystem:
+        n = len(self._q)
+        ex = np.array(self._excl, np.int32).reshape(-1, 2) if self._excl else np.zeros((0, 2), np.int32)
+        return SDMSystem("SDMForce", self._box.copy(), np.array(self._q), np.array(self._sig),
+                         np.array(self._eps), ex, self._displ[:n].copy(), np.zeros((1, n, 3)),
+                         [self._p], cutoff=self._cutoff, eps_rf=self._eps_rf)
+
+    def _sync(self, device: int = 0):
+        if self._topology_dirty or self._handle is None:
+            if self._handle is not None:
+                self._handle.close()
+            self._handle = capi.Handle([self._system()], device=device)
+            self._topology_dirty = False
+            self._displ_dirty = False
+            self._params_dirty = True
+        if self._displ_dirty:
+            self._handle.set_displacement(0, self._displ[:len(self._q)])
+            self._displ_dirty = False
+        if self._params_dirty:
+            if self._p.softcore_method not in (0, 1, 2):
+                raise capi.SdmError(capi.SDM_ERR_UNKNOWN_METHOD, "Unknown soft core method")
+            self._handle.set_params(0, self._p.as_array())
+            self._params_dirty = False
+
+    def evaluate(self, positions, device: int = 0):
+        """Returns (E_pot, forces[N,3]) of the nonbonded group, FP64."""
+        self._sync(device)
+        res, f = self._handle.evaluate(np.asarray(positions, np.float64).reshape(-1, 3))
+        r = res[0]
+        self._last = r
+        self._bind_e = float(r[capi.R_BINDE])
+        self._pot_e = float(r[capi.R_EPOT])
+        return self._pot_e, f
+
+    def close(self):
+        if self._handle is not None:
+            self._handle.close()
+            self._handle = None
+
+
+def force_from_system(s: SDMSystem, replica: int = 0) -> SDMForce:
+    """Builds an SDMForce from a synthetic system (parameters of `replica`)."""
+    f = SDMForce()
+    for q, sg, ep in zip(s.charge, s.sigma, s.epsilon):
+        f.addParticle(q, sg, ep)
+    for i, j in np.asarray(s.exclusions).reshape(-1, 2):
+        f.addExclusion(int(i), int(j))
+    f.setCutoffDistance(s.cutoff)
+    f.setReactionFieldDielectric(s.eps_rf)
+    f.setPeriodicBoxVectors((s.box[0], 0, 0), (0, s.box[1], 0), (0, 0, s.box[2]))
+    for i in np.nonzero(np.any(s.displacement != 0, axis=1))[0]:
+        f.setDisplacement(int(i), *s.displacement[i])
+    p = s.params[replica]
+    f._p = dataclasses.replace(p)
+    f._params_dirty = True
+    return f

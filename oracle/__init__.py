@@ -1,0 +1,205 @@
+"""ctypes bindings of the FP64 CPU oracle (``oracle/sdm_oracle.c``).
+
+TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py``, where it is the checker or the timed
+CPU baseline -- never the product path.  See ``sdm_oracle.c`` for the
+reference files each routine restates.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "sdm_oracle.c")
+_LIB = os.path.join(_HERE, "libsdm_oracle.so")
+_lock = threading.Lock()
+_lib = None
+
+_d = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_f = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_i = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_l = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle with gcc (OpenMP, no FP contraction)."""
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
+        cmd = ["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-fopenmp",
+               "-o", _LIB + ".tmp", _SRC, "-lm"]
+        subprocess.check_call(cmd)
+        os.replace(_LIB + ".tmp", _LIB)
+    return _LIB
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(_LIB)
+            sysargs = [C.c_int, _d, _d, _d, _i, _i, _d, C.c_double, C.c_double]
+            L.orc_nonbonded.argtypes = sysargs + [_d, C.c_void_p, C.c_void_p, C.c_int]
+            L.orc_nonbonded.restype = C.c_double
+            L.orc_sdm_states.argtypes = sysargs + [_d, _d, _d, C.c_void_p, C.c_void_p, _l, C.c_int]
+            L.orc_softcore.argtypes = [C.c_double, C.c_int, C.c_double, C.c_double, C.c_double,
+                                       C.POINTER(C.c_double)]
+            L.orc_softcore.restype = C.c_double
+            L.orc_combine.argtypes = [_d, C.c_double, C.c_double, _d]
+            L.orc_eval_state.argtypes = sysargs + [_d, _d, _d, _d, C.c_void_p, C.c_int]
+            L.orc_build_clusters.argtypes = [C.c_int, _d, _d, _i, C.c_int, _i,
+                                             C.POINTER(C.c_int), _i, _f, _i]
+            L.orc_build_clusters.restype = C.c_int
+            L.orc_image_mode.argtypes = [_d, _i, C.c_double, C.c_int, _i, _f]
+            L.orc_sdm_f32rule.argtypes = sysargs + [_i, _d, _d, _d, C.c_void_p, C.c_void_p, _l]
+            L.orc_sdm_f32rule.restype = C.c_int
+            L.orc_emit_lists.argtypes = [C.c_int, _i, _i, _d, C.c_double, _i, _d, C.c_int,
+                                         C.POINTER(C.c_int), _i, _i, _i, _u8]
+            L.orc_emit_lists.restype = C.c_longlong
+            _lib = L
+    return _lib
+
+
+# --------------------------------------------------------------------------- #
+def excl_csr(n: int, pairs: np.ndarray):
+    """Symmetric CSR (offsets, sorted partners) of an (E,2) exclusion list."""
+    pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    a = np.concatenate([pairs[:, 0], pairs[:, 1]])
+    b = np.concatenate([pairs[:, 1], pairs[:, 0]])
+    order = np.lexsort((b, a))
+    a, b = a[order], b[order]
+    keep = np.ones(len(a), bool)
+    if len(a):
+        keep[1:] = (a[1:] != a[:-1]) | (b[1:] != b[:-1])
+    a, b = a[keep], b[keep]
+    off = np.zeros(n + 1, np.int32)
+    np.add.at(off, a + 1, 1)
+    off = np.cumsum(off).astype(np.int32)
+    return off, np.ascontiguousarray(b.astype(np.int32))
+
+
+class OracleSystem:
+    """Topology bundle for the oracle calls (one SDMSystem, any replica)."""
+
+    def __init__(self, sysm):
+        self.sys = sysm
+        self.n = sysm.n
+        self.q = np.ascontiguousarray(sysm.charge, np.float64)
+        self.sig = np.ascontiguousarray(sysm.sigma, np.float64)
+        self.eps = np.ascontiguousarray(sysm.epsilon, np.float64)
+        self.off, self.idx = excl_csr(self.n, sysm.exclusions)
+        if len(self.idx) == 0:
+            self.idx = np.zeros(1, np.int32)
+        self.box = np.ascontiguousarray(sysm.box, np.float64)
+        self.rc = float(sysm.cutoff)
+        self.eps_rf = float(sysm.eps_rf)
+        self.d = np.ascontiguousarray(sysm.displacement, np.float64).reshape(-1)
+
+    def _args(self):
+        return (self.n, self.q, self.sig, self.eps, self.off, self.idx, self.box, self.rc,
+                self.eps_rf)
+
+    def nonbonded(self, y, forces=True, nthreads=1):
+        y = np.ascontiguousarray(y, np.float64).reshape(-1)
+        f = np.zeros(3 * self.n) if forces else None
+        npairs = C.c_longlong(0)
+        e = lib().orc_nonbonded(*self._args(), y,
+                                f.ctypes.data if forces else None, C.addressof(npairs), nthreads)
+        return e, (f.reshape(-1, 3) if forces else None), npairs.value
+
+    def states(self, x, forces=True, nthreads=1):
+        """FP64 rule: returns dict U0, U1, u_direct, F0, F1, counts."""
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        out = np.zeros(3)
+        F0 = np.zeros(3 * self.n) if forces else None
+        F1 = np.zeros(3 * self.n) if forces else None
+        cnt = np.zeros(4, np.int64)
+        lib().orc_sdm_states(*self._args(), x, self.d, out,
+                             F0.ctypes.data if forces else None,
+                             F1.ctypes.data if forces else None, cnt, nthreads)
+        r = dict(U0=out[0], U1=out[1], u_direct=out[2], P0=int(cnt[0]), P1=int(cnt[1]),
+                 P1delta=int(cnt[2]), Pc0=int(cnt[3]))
+        if forces:
+            r["F0"], r["F1"] = F0.reshape(-1, 3), F1.reshape(-1, 3)
+        return r
+
+    def f32rule(self, x, M):
+        """FP32 pair-inclusion rule of the CUDA path, FP64 arithmetic."""
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        out = np.zeros(3)
+        F0 = np.zeros(3 * self.n)
+        dF = np.zeros(3 * self.n)
+        cnt = np.zeros(3, np.int64)
+        img = lib().orc_sdm_f32rule(*self._args(), np.ascontiguousarray(M, np.int32), x, self.d,
+                                    out, F0.ctypes.data, dF.ctypes.data, cnt)
+        if img < 0:
+            raise RuntimeError("oracle clustering capacity exceeded")
+        return dict(U0=out[0], u=out[1], U1=out[2], F0=F0.reshape(-1, 3), dF=dF.reshape(-1, 3),
+                    P0=int(cnt[0]), P1delta=int(cnt[1]), Pc0=int(cnt[2]), image_mode=img)
+
+    def clusters(self, x, M):
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        M = np.ascontiguousarray(M, np.int32)
+        ncol = int(M[0] * M[1])
+        cap = self.n + 8 * ncol + 8
+        perm = np.zeros(cap, np.int32)
+        ref = np.zeros(3 * cap, np.int32)
+        X = np.zeros(4 * cap, np.float32)
+        colcl = np.zeros(ncol + 1, np.int32)
+        ncl = C.c_int(0)
+        ns = lib().orc_build_clusters(self.n, x, self.box, M, cap, perm, C.byref(ncl), ref, X, colcl)
+        if ns < 0:
+            raise RuntimeError("capacity")
+        k = ncl.value
+        img = lib().orc_image_mode(self.box, M, self.rc, k, perm, X)
+        return dict(perm=perm[:ns], ref=ref[:3 * k].reshape(-1, 3), X=X[:4 * ns].reshape(-1, 4),
+                    colcl=colcl, ncl=k, image_mode=img)
+
+    def lists(self, x, M, cap_per_cluster=2048):
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        M = np.ascontiguousarray(M, np.int32)
+        ncol = int(M[0] * M[1])
+        capcl = (self.n + 8 * ncol + 8) // 8 + 1
+        perm = np.zeros(8 * capcl + 8, np.int32)
+        cnt = np.zeros(capcl, np.int32)
+        es = np.zeros(capcl * cap_per_cluster, np.int32)
+        em = np.zeros(capcl * cap_per_cluster, np.uint8)
+        ncl = C.c_int(0)
+        tot = lib().orc_emit_lists(self.n, self.off, self.idx, self.box, self.rc, M, x,
+                                   cap_per_cluster, C.byref(ncl), perm, cnt, es, em)
+        if tot < 0:
+            raise RuntimeError("list capacity exceeded")
+        k = ncl.value
+        return dict(ncl=k, cnt=cnt[:k], slot=es.reshape(capcl, -1)[:k], mask=em.reshape(capcl, -1)[:k],
+                    total=int(tot))
+
+
+def softcore(u, method, umax, acore, ub):
+    fp = C.c_double(0.0)
+    v = lib().orc_softcore(float(u), int(method), float(umax), float(acore), float(ub), C.byref(fp))
+    return v, fp.value
+
+
+def combine(params: np.ndarray, U0: float, U1: float) -> np.ndarray:
+    out = np.zeros(12)
+    lib().orc_combine(np.ascontiguousarray(params, np.float64), float(U0), float(U1), out)
+    return out
+
+
+COMBINE_FIELDS = ("u", "u_soft", "fp", "W", "dW", "s", "E_pot", "dWdlambda", "lambda1",
+                  "lambda2", "u0", "w0")
+
+
+def eval_state(osys: OracleSystem, x, params, nthreads=1, forces=True):
+    """One full FP64 lambda-state evaluation (two nonbonded passes + combine)."""
+    x = np.ascontiguousarray(x, np.float64).reshape(-1)
+    res = np.zeros(14)
+    F = np.zeros(3 * osys.n) if forces else None
+    lib().orc_eval_state(*osys._args(), x, osys.d, np.ascontiguousarray(params, np.float64), res,
+                         F.ctypes.data if forces else None, nthreads)
+    return res, (F.reshape(-1, 3) if forces else None)

@@ -1,0 +1,234 @@
+"""GPU parity tests: the CUDA path through the C ABI against the FP64 oracle.
+
+Two oracle rules are used (see oracle/sdm_oracle.c):
+  * fp32 rule  -- the exact pair sets of the CUDA kernels, FP64 arithmetic:
+                  index maps, lists and pair counts must agree bit for bit,
+                  energies/forces to FP32-rounding level;
+  * fp64 rule  -- the physics oracle (a pair interacts iff its FP64 distance
+                  is below the cutoff): u within 5e-3 kJ/mol, forces within
+                  1e-4 rms relative.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import FORCE_RMS_REL_TOL, U_ABS_TOL, energy_tol, rms_rel
+from openmm_sdm_plugin_gb300 import capi, systems as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _handle(sysms):
+    h = capi.Handle(sysms)
+    r = 0
+    for s in sysms:
+        for p in s.params:
+            h.set_params(r, p.as_array())
+            r += 1
+    return h
+
+
+def _check_replica(s, x, res, F, F0, F1, M, strict_u=True):
+    o = oracle.OracleSystem(s)
+    a = o.f32rule(x, M)
+    b = o.states(x)
+    n0 = max(a["P0"], 1)
+    assert abs(res[capi.R_U0] - a["U0"]) < energy_tol(a["U0"], n0), (res[capi.R_U0], a["U0"])
+    assert abs(res[capi.R_U0] - b["U0"]) < energy_tol(b["U0"], n0) + 0.05
+    assert rms_rel(F0, a["F0"]) < 1e-5
+    assert rms_rel(F0, b["F0"]) < FORCE_RMS_REL_TOL
+    assert rms_rel(F1, a["F0"] + a["dF"]) < 1e-5
+    assert rms_rel(F1, b["F1"]) < FORCE_RMS_REL_TOL
+    u_ref = b["u_direct"]
+    tol = U_ABS_TOL if strict_u else max(U_ABS_TOL, 1e-6 * abs(u_ref))
+    assert abs(res[capi.R_U] - a["u"]) < tol, (res[capi.R_U], a["u"])
+    assert abs(res[capi.R_U] - u_ref) < tol, (res[capi.R_U], u_ref)
+    assert res[capi.R_U1] == pytest.approx(res[capi.R_U0] + res[capi.R_U], rel=1e-15)
+    # combine on the GPU's own energies matches the restated reference combine
+    p = s.params[0].as_array()
+    comb = oracle.combine(p, res[capi.R_U0], res[capi.R_U1])
+    assert res[capi.R_BINDE] == pytest.approx(comb[1], rel=1e-9, abs=1e-9)
+    assert res[capi.R_W] == pytest.approx(comb[3], rel=1e-9, abs=1e-9)
+    assert res[capi.R_DW] == pytest.approx(comb[4], rel=1e-9, abs=1e-12)
+    assert res[capi.R_S] == pytest.approx(comb[5], rel=1e-9, abs=1e-12)
+    assert res[capi.R_EPOT] == pytest.approx(comb[6], rel=1e-12)
+    # mixed force
+    sw = res[capi.R_S]
+    Fref = sw * b["F1"] + (1 - sw) * b["F0"]
+    assert rms_rel(F, Fref) < FORCE_RMS_REL_TOL
+    return a, b
+
+
+@pytest.mark.parametrize("variant", ["a", "b"])
+def test_config0_parity(variant):
+    s = S.config0(variant=variant)
+    h = _handle([s])
+    x = s.positions[0]
+    res, F = h.evaluate(x)
+    F0, F1 = h.state_forces()
+    _check_replica(s, x, res[0], F, F0, F1, h.grid(0), strict_u=(variant == "b"))
+    assert res[0, capi.R_STATUS] == 0
+
+
+def test_config1_parity():
+    s = S.config1()
+    h = _handle([s])
+    x = s.positions[0]
+    res, F = h.evaluate(x)
+    F0, F1 = h.state_forces()
+    a, b = _check_replica(s, x, res[0], F, F0, F1, h.grid(0))
+    print("config1 U0", res[0, capi.R_U0], "u", res[0, capi.R_U], "oracle u", b["u_direct"])
+
+
+def test_config1b_logistic_term():
+    s = S.config1(variant="b")
+    h = _handle([s])
+    x = s.positions[0]
+    res, F = h.evaluate(x)
+    F0, F1 = h.state_forces()
+    _check_replica(s, x, res[0], F, F0, F1, h.grid(0))
+
+
+def test_pair_counts_exact():
+    for s in (S.config0(), S.config0(variant="b"), S.config1()):
+        h = _handle([s])
+        c = h.count_pairs(s.positions[0])
+        a = oracle.OracleSystem(s).f32rule(s.positions[0], h.grid(0))
+        assert int(c[0, 0]) == a["P0"]
+        assert int(c[0, 1]) == a["P1delta"]
+
+
+@pytest.mark.parametrize("which", ["config0", "config1"])
+def test_clusters_and_lists_bit_exact(which):
+    s = S.config0() if which == "config0" else S.config1()
+    h = _handle([s])
+    x = s.positions[0]
+    M = h.grid(0)
+    g = h.export_lists(0, x)
+    o = oracle.OracleSystem(s)
+    c = o.clusters(x, M)
+    assert g["ncl"] == c["ncl"]
+    assert np.array_equal(g["perm"], c["perm"])
+    ol = o.lists(x, M)
+    assert np.array_equal(g["cnt"], ol["cnt"])
+    for I in range(g["ncl"]):
+        k = g["cnt"][I]
+        gs, gm = g["slot"][I, :k], g["mask"][I, :k]
+        order = np.argsort(gs, kind="stable")
+        assert np.array_equal(gs[order], ol["slot"][I, :k])
+        assert np.array_equal(gm[order], ol["mask"][I, :k])
+
+
+def test_batched_replicas_match_single():
+    s = S.config2(nrep=4)
+    h = _handle([s])
+    x = s.positions.reshape(-1, 3)
+    res, F = h.evaluate(x)
+    F0, F1 = h.state_forces()
+    n = s.n
+    M = h.grid(0)
+    for r in range(4):
+        sr = s.replica(r)
+        sl = slice(r * n, (r + 1) * n)
+        _check_replica(sr, s.positions[r], res[r], F[sl], F0[sl], F1[sl], M)
+
+
+def test_uneven_multisystem_batch():
+    sysms = [S.host_guest(2500, 11, nstates=2), S.host_guest(7000, 12, nstates=3),
+             S.host_guest(4000, 13, nstates=1)]
+    h = _handle(sysms)
+    x = np.concatenate([s.positions.reshape(-1, 3) for s in sysms])
+    res, F = h.evaluate(x)
+    F0, F1 = h.state_forces()
+    off = 0
+    r = 0
+    for k, s in enumerate(sysms):
+        M = h.grid(k)
+        for q in range(s.replicas):
+            sr = s.replica(q)
+            sl = slice(off, off + s.n)
+            _check_replica(sr, s.positions[q], res[r], F[sl], F0[sl], F1[sl], M)
+            off += s.n
+            r += 1
+
+
+def test_deterministic_bitwise():
+    s = S.config1()
+    h = _handle([s])
+    x = s.positions[0]
+    r1, F1 = h.evaluate(x)
+    r2, F2 = h.evaluate(x)
+    assert np.array_equal(r1, r2)
+    assert np.array_equal(F1, F2)
+
+
+@pytest.mark.parametrize("bias", [0, 1, 2])
+@pytest.mark.parametrize("soft", [0, 1, 2])
+def test_bias_and_softcore_methods(bias, soft):
+    s = S.config0(variant="b")
+    s.params = [S.SDMParams(bias_method=bias, softcore_method=soft, lambdac=0.4, lambda1=0.25,
+                            lambda2=0.6, alpha=0.05, u0=50.0, w0=1.5, gamma=0.002, wb=0.3,
+                            umax=200.0, acore=1 / 16, ubcore=20.0)]
+    h = _handle([s])
+    res, F = h.evaluate(s.positions[0])
+    comb = oracle.combine(s.params[0].as_array(), res[0, capi.R_U0], res[0, capi.R_U1])
+    for k, idx in ((1, capi.R_BINDE), (2, capi.R_FP), (3, capi.R_W), (4, capi.R_DW), (5, capi.R_S)):
+        assert res[0, idx] == pytest.approx(comb[k], rel=1e-9, abs=1e-12)
+
+
+def test_nonequilibrium_dwdlambda():
+    s = S.config0(variant="b")
+    s.params = [S.SDMParams(bias_method=2, softcore_method=2, alpha=0.1, noneq=1, lambdac=0.3,
+                            m_lambda1=0.8, m_lambda2=1.0, m_u0=20.0, m_w0=2.0, b_lambda1=0.05,
+                            b_u0=100.0, umax=200, acore=1 / 16, ubcore=100)]
+    h = _handle([s])
+    res, _ = h.evaluate(s.positions[0])
+    comb = oracle.combine(s.params[0].as_array(), res[0, capi.R_U0], res[0, capi.R_U1])
+    assert res[0, capi.R_DWDL] == pytest.approx(comb[7], rel=1e-9)
+    assert res[0, capi.R_L1] == pytest.approx(0.8 * 0.3 + 0.05)
+
+
+def test_device_api_and_graph_replay():
+    import torch
+    s = S.config2(nrep=2)
+    h = _handle([s])
+    x = np.ascontiguousarray(s.positions.reshape(-1, 3))
+    rh, Fh = h.evaluate(x)
+    xd = torch.from_numpy(x).cuda()
+    rd = torch.zeros((h.nrep, capi.NRESULTS), dtype=torch.float64, device="cuda")
+    fd = torch.zeros_like(xd)
+    st = torch.cuda.current_stream().cuda_stream
+    for _ in range(3):  # first call captures, the next ones replay the graph
+        h.evaluate_device(xd.data_ptr(), rd.data_ptr(), fd.data_ptr(), st)
+    torch.cuda.synchronize()
+    assert np.array_equal(rd.cpu().numpy()[:, :14], rh[:, :14])
+    assert np.array_equal(fd.cpu().numpy(), Fh)
+
+
+def test_translation_invariance_and_zero_displacement():
+    s = S.config0(variant="b")
+    h = _handle([s])
+    x = s.positions[0]
+    r1, _ = h.evaluate(x)
+    r2, _ = h.evaluate(x + np.array([3.0 * 7 + 0.25, -3.0 * 2, 0.5]))
+    assert abs(r1[0, capi.R_U] - r2[0, capi.R_U]) < U_ABS_TOL
+    h.set_displacement(0, np.zeros((s.n, 3)))
+    r3, F3 = h.evaluate(x)
+    assert r3[0, capi.R_U] == 0.0
+    F0, F1 = h.state_forces()
+    assert np.array_equal(F0, F1)
+
+
+def test_sdmforce_api_end_to_end():
+    from openmm_sdm_plugin_gb300 import force_from_system
+    s = S.config0(variant="b")
+    f = force_from_system(s)
+    E, F = f.evaluate(s.positions[0])
+    o = oracle.OracleSystem(s)
+    res, Fr = oracle.eval_state(o, s.positions[0], s.params[0].as_array())
+    assert f.getBindE() == pytest.approx(res[1], abs=U_ABS_TOL)
+    assert E == pytest.approx(res[6], abs=0.05)
+    assert rms_rel(F, Fr) < FORCE_RMS_REL_TOL
+    f.setSoftCoreMethod(9)
+    with pytest.raises(capi.SdmError):
+        f.evaluate(s.positions[0])
