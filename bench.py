@@ -1,0 +1,373 @@
+#!/usr/bin/env python3
+"""Benchmark of the SDM two-state force on GB300.
+
+Metric: lambda-state force evaluations per second.  One lambda-state
+evaluation = U0, U1, u (FP64), u', W, W' and the mixed force F for all
+particles of one replica, from the current coordinates (cells, clusters and
+neighbour candidates are rebuilt every call; nothing is reused).
+
+Workload (headline): 22 replicas of the 22,580-particle relative-binding
+system (7,500 rigid 3-site waters + two 40-atom ligands displaced by +/-d,
+6.2 nm box, 1.0 nm reaction-field cutoff), each replica with its own seeded
+coordinates and lambda state, evaluated in one batched call replayed as a
+CUDA graph.  The plain form (one replica per call) is timed beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank runs its own 22-replica batch on its own GPU (weak
+scaling, no data-path collective); times are max-reduced over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SDM lambda-state force evals/s at 23k atoms x 22 lambda, batched vs plain, 1 GB300"
+UNIT = "lambda-state evals/s"
+FLOP_PER_PAIR = 52  # FP32 flops per pair per state (FMA = 2, rsqrt = 1)
+NREP = 22
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"sm_max_mhz": 2070.0, "hbm_gbs": 6800.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampler during the timed region (clocks + throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_port(sysm, nthreads: int, budget_s: float = 10.0):
+    """FP64 oracle (the CPU restatement of the reference path) on a bounded
+    sample: whole lambda states of the workload, one after another."""
+    import oracle
+    o = oracle.OracleSystem(sysm)
+    x = sysm.positions
+    p = [q.as_array() for q in sysm.params]
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        oracle.eval_state(o, x[n % len(x)], p[n % len(p)], nthreads=nthreads)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt
+
+
+def run_reference(args):
+    """--impl reference: the reference path's CPU implementation on the host cores.
+
+    The reference's own Reference platform cannot be built here (it links
+    OpenMM, which is absent), so the FP64 oracle port stands in, using every
+    host thread."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from openmm_sdm_plugin_gb300 import systems as S
+    import oracle
+    oracle.build()
+    sysm = S.config2(NREP)
+    nth = os.cpu_count() or 1
+    o = oracle.OracleSystem(sysm)
+    params = [q.as_array() for q in sysm.params]
+    # each step: a bounded sample of the 22-state batch (states k, k+1, ... round robin)
+    per_step = max(1, min(NREP, int(os.environ.get("SDM_REF_STATES_PER_STEP", "4"))))
+    k = 0
+    for _ in range(args.warmup):
+        for _ in range(per_step):
+            oracle.eval_state(o, sysm.positions[k % NREP], params[k % NREP], nthreads=nth)
+            k += 1
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for _ in range(per_step):
+            oracle.eval_state(o, sysm.positions[k % NREP], params[k % NREP], nthreads=nth)
+            k += 1
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    v = per_step * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "config2: 22 replicas x 22,580 particles, rc 1.0 nm RF, 6.2 nm box",
+                   "sample": f"{per_step} lambda states per step (round robin over the 22)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
+                         "sample": f"{per_step} full FP64 lambda-state evaluations per step"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference Reference platform unbuildable here (needs OpenMM); FP64 oracle port"}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import __graft_entry__ as ge
+    from openmm_sdm_plugin_gb300 import capi, systems as S
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    if rank == 0:
+        ge.build()
+    if dist is not None:
+        dist.barrier()
+    warm = max(3, args.warmup)
+
+    # ---------------- workload ----------------
+    sysm = S.config2(NREP)
+    n = sysm.n
+    h = capi.Handle([sysm], device=local)
+    for r in range(NREP):
+        h.set_params(r, sysm.params[r].as_array())
+    xh = np.ascontiguousarray(sysm.positions.reshape(-1, 3))
+    counts = h.count_pairs(xh)           # product diagnostic: P0, P1delta per replica
+    P0 = int(counts[:, 0].sum())
+    P1 = int(counts[:, 1].sum())
+    flop_per_launch = FLOP_PER_PAIR * (P0 + P1)
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    xd = torch.from_numpy(xh).to(dev)
+    rd = torch.zeros((NREP, capi.NRESULTS), dtype=torch.float64, device=dev)
+    fd = torch.zeros_like(xd)
+    if args.autotune:
+        h.autotune(xd.data_ptr())
+    l2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+
+    def flush():
+        l2.zero_()
+
+    # plain form: one replica per call
+    s1 = sysm.replica(0)
+    h1 = capi.Handle([s1], device=local)
+    h1.set_params(0, s1.params[0].as_array())
+    x1 = xd[:n].contiguous()
+    r1 = torch.zeros((1, capi.NRESULTS), dtype=torch.float64, device=dev)
+    f1 = torch.zeros_like(x1)
+
+    def timed(fn, steps, warmup, per_kernel=None):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        pk = []
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for k in range(steps):
+            flush()
+            ev[k][0].record(stream)
+            fn()
+            ev[k][1].record(stream)
+            if per_kernel is not None:
+                ev[k][1].synchronize()
+                pk.append(per_kernel())
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        ms = [a.elapsed_time(b) for a, b in ev]
+        return ms, pk
+
+    # ---- batched (headline), pair kernel timed by events inside the graph ----
+    h.set_option(capi.OPT_PROFILE, 2)
+    sampler = ClockSampler(local)
+    sampler.start()
+    t_wall0 = time.perf_counter()
+    ms_b, pk = timed(lambda: h.evaluate_device(xd.data_ptr(), rd.data_ptr(), fd.data_ptr(), sptr),
+                     args.steps, warm, per_kernel=h.kernel_times)
+    t_wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop()
+    tot_b = sum(ms_b) / 1e3
+    if dist is not None:
+        t = torch.tensor([tot_b], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_b = float(t.item())
+    value = NREP * args.steps * world / tot_b
+    pair_ms = [d["k_pair"] for d in pk]
+    pert_ms = [d["k_perturb"] for d in pk]
+    pair_avg = sum(pair_ms) / len(pair_ms)
+    breakdown = {k: sum(d[k] for d in pk) / len(pk) for k in pk[0]}
+
+    # ---- plain: one replica per call ----
+    h1.set_option(capi.OPT_PROFILE, 0)
+    ms_p, _ = timed(lambda: h1.evaluate_device(x1.data_ptr(), r1.data_ptr(), f1.data_ptr(), sptr),
+                    args.steps, warm)
+    plain = args.steps / (sum(ms_p) / 1e3)
+
+    # ---- e2e through the host C ABI: pinned host inputs/outputs ----
+    h.set_option(capi.OPT_PROFILE, 0)
+    xpin = torch.from_numpy(xh.copy()).pin_memory()
+    rpin = torch.zeros((NREP, capi.NRESULTS), dtype=torch.float64).pin_memory()
+    fpin = torch.zeros_like(xpin).pin_memory()
+    import ctypes as C
+    L = capi.load_library()
+
+    def e2e_step():
+        st = L.sdm_evaluate(h.h, C.c_void_p(xpin.data_ptr()), C.c_void_p(rpin.data_ptr()),
+                            C.c_void_p(fpin.data_ptr()))
+        if st != 0:
+            raise capi.SdmError(st, L.sdm_last_error(h.h).decode())
+
+    for _ in range(warm):
+        e2e_step()
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()   # H2D copy, evaluation, D2H copy, synchronise
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    tot_e = sum(e2e_ms) / 1e3
+    if dist is not None:
+        t = torch.tensor([tot_e], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_e = float(t.item())
+    e2e = NREP * args.steps * world / tot_e
+    # check the batch result once against nothing but itself: status clean
+    status = h.check_status()
+
+    # ---- roofline of the pair kernel (FP32 pipe) ----
+    peaks, src = _peaks()
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fmax = float(peaks.get("sm_max_mhz", 2070.0))
+    peak_tf = nsm * 128 * 2 * fmax * 1e6 / 1e12
+    achieved_tf = flop_per_launch / (pair_avg * 1e-3) / 1e12
+    f_run = clocks.get("sm_mhz")
+    roof = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+            "frac": achieved_tf / peak_tf, "traffic": None,
+            "kernel": "k_pair (main pass, all 22 replicas)",
+            "peak_source": f"{nsm} SMs x 128 FP32 lanes x 2 x {fmax:.0f} MHz ({src} sm_max_mhz)",
+            "frac_at_run_clock": (achieved_tf / (nsm * 256 * f_run * 1e6 / 1e12)) if f_run else None,
+            "pair_kernel_ms": pair_avg, "perturb_kernel_ms": sum(pert_ms) / len(pert_ms),
+            "flop_per_launch": flop_per_launch, "P0": P0, "P1delta": P1}
+    traffic_file = os.path.join(ROOT, "profiles", "k_pair_traffic.json")
+    if os.path.exists(traffic_file):
+        with open(traffic_file) as f:
+            roof["traffic"] = json.load(f).get("bytes_per_launch")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v1, nst, dt = cpu_baseline_port(sysm.replica(0), nthreads=1, budget_s=10.0)
+        cpu = {"value": v1, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{nst} FP64 lambda-state evaluations of one 22,580-particle replica in {dt:.1f} s"}
+
+    h2d = xh.nbytes
+    d2h = xh.nbytes + NREP * capi.NRESULTS * 8
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": warm, "ms_per_step": sum(ms_b) / len(ms_b), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 pairs, int64 fixed-point forces, f64 energies",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "config2: 22 replicas x 22,580 particles (7,500 waters + 2x40 ligand), "
+                               "6.2 nm box, rc 1.0 nm reaction field, one batched call per step as a CUDA graph",
+                   "replicas_per_gpu": NREP, "particles": n, "l2": "flushed (256 MB write) before every timed step",
+                   "parallelism": f"replicas only, {world} independent rank(s)"},
+        "plain": {"value": plain, "unit": UNIT, "ms_per_call": sum(ms_p) / len(ms_p),
+                  "workload": "config1: one 22,580-particle replica per call (CUDA graph)"},
+        "batched_over_plain": value / world / plain,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": sum(e2e_ms) / len(e2e_ms), "path": "sdm_evaluate (host C ABI, pinned buffers)"},
+        "roofline": roof,
+        "kernel_ms": breakdown,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": 9 * args.steps,
+        "device_status": status,
+        "wall_s_timed_region": t_wall,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    h.close()
+    h1.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -183,7 +183,8 @@ sdm_status sdm_check_status(sdm_handle* h, int* device_status);
 /* Options. */
 enum {
     SDM_OPT_GRAPH = 0,        /* 1 = capture/replay CUDA graphs in sdm_evaluate_device (default 1) */
-    SDM_OPT_PROFILE = 1,      /* 1 = time every kernel with CUDA events (disables graphs) */
+    SDM_OPT_PROFILE = 1,      /* 1 = time every kernel with CUDA events (eager launches);
+                                 2 = record the same events inside the replayed graph */
     SDM_OPT_SPLIT = 2,        /* work items per i-cluster in the pair kernel (1,2,4) */
     SDM_OPT_CTAS_PER_SM = 3,  /* persistent pair-kernel CTAs per SM (1..8) */
     SDM_OPT_VERIFY = 4        /* 1 = sdm_evaluate checks the device status word after each call */

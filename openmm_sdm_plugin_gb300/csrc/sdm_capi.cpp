@@ -370,7 +370,9 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
     a.split = mode == 2 ? 1 : h->opt_split;
     sdm_status s = flush_params(h, st);
     if (s) return s;
-    const bool profile = h->opt_profile != 0;
+    // profile 1: eager launches timed with events; profile 2: the same events
+    // recorded inside the captured graph (read back by sdm_get_kernel_times)
+    const bool profile = h->opt_profile == 1;
     if (profile || !h->opt_graph || !allow_graph || mode != 0) {
         s = enqueue(h, a, mode, st, profile);
         if (s) return s;
@@ -382,12 +384,13 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
         h->have_eval = (mode == 0);
         return SDM_OK;
     }
-    GraphKey key{x, res, f, st, a.split, h->opt_ctas};
+    const bool gprof = h->opt_profile == 2;
+    GraphKey key{x, res, f, st, a.split, h->opt_ctas + (gprof ? 100 : 0)};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
         cudaGraph_t g = nullptr;
         SDM_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        s = enqueue(h, a, mode, st, false);
+        s = enqueue(h, a, mode, st, gprof);
         cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (s) { if (g) cudaGraphDestroy(g); return s; }
         if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaStreamEndCapture");
@@ -403,6 +406,7 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
     }
     SDM_CUDA(h, cudaGraphLaunch(it->second, st));
     h->have_eval = true;
+    h->last_nk = gprof ? -8 : 0;  // negative: times pending inside the last replay
     return SDM_OK;
 }
 
@@ -722,7 +726,10 @@ sdm_status sdm_set_option(sdm_handle* h, int option, int value) {
     if (!h) return SDM_ERR_INVALID_ARGUMENT;
     switch (option) {
         case SDM_OPT_GRAPH: h->opt_graph = value ? 1 : 0; break;
-        case SDM_OPT_PROFILE: h->opt_profile = value ? 1 : 0; break;
+        case SDM_OPT_PROFILE:
+            if (value < 0 || value > 2) return fail(h, SDM_ERR_INVALID_ARGUMENT, "profile must be 0, 1 or 2");
+            h->opt_profile = value;
+            break;
         case SDM_OPT_SPLIT:
             if (value != 1 && value != 2 && value != 4) return fail(h, SDM_ERR_INVALID_ARGUMENT, "split must be 1, 2 or 4");
             h->opt_split = value;
@@ -750,8 +757,15 @@ sdm_status sdm_get_option(const sdm_handle* h, int option, int* value) {
     return SDM_OK;
 }
 
-sdm_status sdm_get_kernel_times(const sdm_handle* h, const char** names, float* ms, int* count) {
-    if (!h || !count) return SDM_ERR_INVALID_ARGUMENT;
+sdm_status sdm_get_kernel_times(const sdm_handle* hc, const char** names, float* ms, int* count) {
+    if (!hc || !count) return SDM_ERR_INVALID_ARGUMENT;
+    sdm_handle* h = const_cast<sdm_handle*>(hc);
+    if (h->last_nk < 0) {
+        cudaSetDevice(h->device);
+        SDM_CUDA(h, cudaEventSynchronize(h->ev[8]));
+        for (int k = 0; k < 8; ++k) SDM_CUDA(h, cudaEventElapsedTime(&h->last_ms[k], h->ev[k], h->ev[k + 1]));
+        h->last_nk = 8;
+    }
     const int n = std::min(*count, h->last_nk);
     for (int k = 0; k < n; ++k) {
         if (names) names[k] = kKernelNames[k];

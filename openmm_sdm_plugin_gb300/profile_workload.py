@@ -1,0 +1,50 @@
+"""Runs a fixed synthetic SDM workload a few times (for profilers).
+
+  python -m openmm_sdm_plugin_gb300.profile_workload [--replicas 22] [--calls 3] [--eager]
+
+The workload is the batched relative-binding system used by the benchmark:
+`--replicas` copies of the 22,580-particle system with independent seeded
+coordinates.  Each call is one evaluation of all replicas (device buffers).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+
+import numpy as np
+
+from . import build as _build
+from . import capi, systems
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--replicas", type=int, default=22)
+    ap.add_argument("--calls", type=int, default=3)
+    ap.add_argument("--eager", action="store_true", help="no CUDA graph")
+    ap.add_argument("--config", default="config2", choices=["config2", "config0"])
+    a = ap.parse_args()
+    _build.build()
+    import torch
+    s = systems.config2(a.replicas) if a.config == "config2" else systems.config0(variant="b")
+    h = capi.Handle([s])
+    for r in range(h.nrep):
+        h.set_params(r, s.params[r].as_array())
+    if a.eager:
+        h.set_option(capi.OPT_GRAPH, 0)
+    x = torch.from_numpy(np.ascontiguousarray(s.positions.reshape(-1, 3))).cuda()
+    res = torch.zeros((h.nrep, capi.NRESULTS), dtype=torch.float64, device="cuda")
+    f = torch.zeros_like(x)
+    st = torch.cuda.current_stream().cuda_stream
+    for _ in range(a.calls):
+        h.evaluate_device(x.data_ptr(), res.data_ptr(), f.data_ptr(), st)
+    torch.cuda.synchronize()
+    status = h.check_status()
+    r = res.cpu().numpy()
+    print(f"replicas={h.nrep} U0[0]={r[0, capi.R_U0]:.4f} u[0]={r[0, capi.R_U]:.6f} status={status}")
+    h.close()
+    return 0 if status == 0 else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -295,7 +295,7 @@ def lambda_schedule(nstates: int) -> List[SDMParams]:
     lambda1=lambda_k-0.1*sin(pi*lambda_k), alpha=0.1, u0=110, w0=0."""
     out = []
     for k in range(nstates):
-        lam = k / (nstates - 1)
+        lam = k / (nstates - 1) if nstates > 1 else 1.0
         out.append(SDMParams(lambdac=lam, lambda1=lam - 0.1 * math.sin(math.pi * lam),
                              lambda2=lam, alpha=0.1, u0=110.0, w0=0.0, umax=200.0,
                              acore=1.0 / 16.0, ubcore=100.0))

@@ -59,15 +59,39 @@ def _check_replica(s, x, res, F, F0, F1, M, strict_u=True):
     return a, b
 
 
-@pytest.mark.parametrize("variant", ["a", "b"])
-def test_config0_parity(variant):
-    s = S.config0(variant=variant)
+def test_config0_parity():
+    s = S.config0(variant="b")
     h = _handle([s])
     x = s.positions[0]
     res, F = h.evaluate(x)
     F0, F1 = h.state_forces()
-    _check_replica(s, x, res[0], F, F0, F1, h.grid(0), strict_u=(variant == "b"))
+    _check_replica(s, x, res[0], F, F0, F1, h.grid(0))
     assert res[0, capi.R_STATUS] == 0
+
+
+def test_config0a_clash_overflow_is_reported():
+    """Config 0a displaces the ligand into solvent: state-2 forces reach
+    ~5.6e9 kJ/mol/nm, beyond the 2^31 range of the 2^32-scaled fixed point.
+    The host call must fail with SDM_ERR_OVERFLOW; energies, u and F0 stay
+    valid and are still checked."""
+    s = S.config0(variant="a")
+    h = _handle([s])
+    x = s.positions[0]
+    with pytest.raises(capi.SdmError) as e:
+        h.evaluate(x)
+    assert e.value.status == capi.SDM_ERR_OVERFLOW
+    h.set_option(capi.OPT_VERIFY, 0)
+    res, F = h.evaluate(x)
+    assert int(res[0, capi.R_STATUS]) & 1
+    assert h.check_status() & 1
+    F0, _ = h.state_forces()
+    o = oracle.OracleSystem(s)
+    b = o.states(x)
+    a = o.f32rule(x, h.grid(0))
+    assert abs(res[0, capi.R_U0] - b["U0"]) < energy_tol(b["U0"], b["P0"]) + 0.05
+    assert abs(res[0, capi.R_U] - a["u"]) < 1e-6 * abs(a["u"])
+    assert abs(res[0, capi.R_U] - b["u_direct"]) < 1e-6 * abs(b["u_direct"])
+    assert rms_rel(F0, b["F0"]) < FORCE_RMS_REL_TOL
 
 
 def test_config1_parity():
