@@ -169,7 +169,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -209,8 +209,11 @@ def main():
     flop_per_launch = FLOP_PER_PAIR * (P0 + P1)
 
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: flushes, events and graph replays all go on it (the
+    # legacy default stream has handle 0, which the C ABI reads as "own stream")
+    stream = torch.cuda.Stream(device=dev)
     sptr = stream.cuda_stream
+    assert sptr != 0
     xd = torch.from_numpy(xh).to(dev)
     rd = torch.zeros((NREP, capi.NRESULTS), dtype=torch.float64, device=dev)
     fd = torch.zeros_like(xd)
@@ -219,7 +222,8 @@ def main():
     l2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
 
     def flush():
-        l2.zero_()
+        with torch.cuda.stream(stream):
+            l2.zero_()
 
     # plain form: one replica per call
     s1 = sysm.replica(0)

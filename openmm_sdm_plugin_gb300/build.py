@@ -41,6 +41,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
     common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+              "-diag-suppress", "128,177",
                      "-I", os.path.join(HERE, "..", "include")]
 
     def compile_one(src):

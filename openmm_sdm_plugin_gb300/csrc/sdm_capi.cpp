@@ -20,7 +20,7 @@
 #include "sdm_types.h"
 
 cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* done, cudaStream_t st,
-                            cudaEvent_t* ev, int nev);
+                            cudaEvent_t* ev, int nev, unsigned ev_flags);
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
                             cudaStream_t st);
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
@@ -335,16 +335,20 @@ sdm_status upload_topology(sdm_handle* h) {
     return SDM_OK;
 }
 
-sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, bool profile) {
+// capture: event records become graph event-record nodes only with the
+// External flag (otherwise they are capture-internal dependency markers)
+sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, bool profile,
+                   bool capturing) {
+    const unsigned fl = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     SDM_CUDA(h, cudaMemsetAsync(h->counters, 0, h->counters_bytes, st));
     cudaEvent_t* ev = profile ? h->ev : nullptr;
-    SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->done, st, ev, 6));
+    SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->done, st, ev, 6, fl));
     SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, st));
-    if (profile) SDM_CUDA(h, cudaEventRecord(h->ev[6], st));
+    if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[6], st, fl));
     if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
-    if (profile) SDM_CUDA(h, cudaEventRecord(h->ev[7], st));
+    if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
     if (mode == 0) SDM_CUDA(h, sdm_launch_finalize(a, st));
-    if (profile) SDM_CUDA(h, cudaEventRecord(h->ev[8], st));
+    if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[8], st, fl));
     return SDM_OK;
 }
 
@@ -374,7 +378,7 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
     // recorded inside the captured graph (read back by sdm_get_kernel_times)
     const bool profile = h->opt_profile == 1;
     if (profile || !h->opt_graph || !allow_graph || mode != 0) {
-        s = enqueue(h, a, mode, st, profile);
+        s = enqueue(h, a, mode, st, profile, false);
         if (s) return s;
         if (profile) {
             SDM_CUDA(h, cudaEventSynchronize(h->ev[8]));
@@ -390,7 +394,7 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
     if (it == h->graphs.end()) {
         cudaGraph_t g = nullptr;
         SDM_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        s = enqueue(h, a, mode, st, gprof);
+        s = enqueue(h, a, mode, st, gprof, true);
         cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (s) { if (g) cudaGraphDestroy(g); return s; }
         if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaStreamEndCapture");
@@ -462,7 +466,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     }
     // replica windows
     long long xo = 0;
-    int aw = 0, cw = 0, sw = 0;
+    int aw = 0, cw = 0, sw = 0, zw = 0;
     for (int s = 0; s < num_systems; ++s) {
         const SysHost& S = h->sys[s];
         for (int k = 0; k < S.replicas; ++k) {
@@ -475,7 +479,9 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
             r.slot_win = sw;
             r.slot_cap = round8((long long)S.n + 8LL * S.dev.ncol + 8);
             r.cl_win = sw / 8;
+            r.ztab_win = zw;
             h->rep.push_back(r);
+            zw += S.dev.ncol * (S.dev.M[2] + 1);
             xo += S.n;
             aw += S.n;
             cw += S.dev.ncol + 1;
@@ -526,6 +532,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_F = ar.take<unsigned long long>(6 * Sl);
     const size_t o_ref = ar.take<int4>(Cl), o_bbc = ar.take<float4>(Cl), o_bbh = ar.take<float4>(Cl);
     const size_t o_lnk = ar.take<int4>(Cl), o_ep = ar.take<double>(Cl * SDM_MAX_SPLIT);
+    const size_t o_zt = ar.take<int>(std::max(zw, 1));
     const size_t o_pp = ar.take<double>(std::max(Pp, 1LL));
     const size_t o_ncl = ar.take<int>(nrep), o_st = ar.take<int>(4);
     const size_t o_counts = ar.take<long long>(2 * nrep), o_ip = ar.take<int>(nrep + 1);
@@ -583,6 +590,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.cl_bbc = at<float4>(B, o_bbc);
     a.cl_bbh = at<float4>(B, o_bbh);
     a.cl_link = at<int4>(B, o_lnk);
+    a.ztab = at<int>(B, o_zt);
     a.e_part = at<double>(B, o_ep);
     a.p_part = at<double>(B, o_pp);
     a.ncl = at<int>(B, o_ncl);

@@ -259,8 +259,15 @@ __global__ void k_bucket(SdmArgs a) {
 // ------------------------------------------------------------------------- //
 // K4: rank sort of every column by (z, particle)                            //
 // ------------------------------------------------------------------------- //
+// keys are the bit patterns of the wrapped z coordinates (non-negative
+// doubles order like their bits once -0.0 is canonicalised) with the particle
+// index as tie-break: integer compares only (FP64 compares are slow on GB300)
+__device__ __forceinline__ unsigned long long zkey(double z) {
+    return (unsigned long long)__double_as_longlong(__dadd_rn(z, 0.0));
+}
+
 __global__ void __launch_bounds__(128) k_colsort(SdmArgs a) {
-    __shared__ double kz[4][128];
+    __shared__ unsigned long long kz[4][128];
     __shared__ int ki[4][128];
     const int wib = threadIdx.x >> 5;
     const int lane = lane_id();
@@ -273,27 +280,34 @@ __global__ void __launch_bounds__(128) k_colsort(SdmArgs a) {
         if (c >= S.ncol) continue;
         const int n = a.col_cnt[R.col_win + c];
         const int a0 = a.col_aoff[R.col_win + c];
-        const int sbase = 8 * a.col_cl[R.col_win + c];
+        const int cl0 = a.col_cl[R.col_win + c];
+        const int sbase = 8 * cl0;
         const int send = 8 * a.col_cl[R.col_win + c + 1];
         const int* bk = a.bucket + R.atom_win + a0;
+        if (n == 0) {
+            // empty column: every z entry of its cluster table points at its (empty) range
+            int* zt = a.ztab + R.ztab_win + c * (S.M[2] + 1);
+            for (int z = lane; z <= S.M[2]; z += 32) zt[z] = cl0;
+            continue;
+        }
         for (int ib = 0; ib < n; ib += 32) {
             const int ii = ib + lane;
             int ai = -1;
-            double zi = 0.0;
-            if (ii < n) { ai = bk[ii]; zi = a.w[3 * (size_t)(R.atom_win + ai) + 2]; }
+            unsigned long long zi = 0ull;
+            if (ii < n) { ai = bk[ii]; zi = zkey(a.w[3 * (size_t)(R.atom_win + ai) + 2]); }
             int rank = 0;
             for (int jb = 0; jb < n; jb += 128) {
                 __syncwarp();
                 for (int q = lane; q < 128 && jb + q < n; q += 32) {
                     const int aj = bk[jb + q];
                     ki[wib][q] = aj;
-                    kz[wib][q] = a.w[3 * (size_t)(R.atom_win + aj) + 2];
+                    kz[wib][q] = zkey(a.w[3 * (size_t)(R.atom_win + aj) + 2]);
                 }
                 __syncwarp();
                 const int m = min(128, n - jb);
                 if (ii < n)
                     for (int q = 0; q < m; ++q) {
-                        const double zj = kz[wib][q];
+                        const unsigned long long zj = kz[wib][q];
                         const int aj = ki[wib][q];
                         rank += (zj < zi) || (zj == zi && aj < ai);
                     }
@@ -409,6 +423,15 @@ __global__ void k_clusters(SdmArgs a) {
             a.cl_link[cw] = many ? make_int4(-2, -2, -2, -2)
                                  : make_int4(link[0], link[1], link[2], link[3]);
             atomicMax(&a.extz[r], __float_as_uint(fmaxf(hi[2], 0.0f)));
+            // column z-table: entries (z of the previous cluster, z of C] -> C
+            const int cfirst = a.col_cl[R.col_win + ci0.x];
+            const int cend = a.col_cl[R.col_win + ci0.x + 1];
+            int zprev = -1;
+            if (C > cfirst) zprev = a.cellinfo[R.atom_win + a.perm[R.slot_win + 8 * (C - 1)]].y;
+            int* zt = a.ztab + R.ztab_win + ci0.x * (S.M[2] + 1);
+            for (int z = zprev + 1; z <= cz; ++z) zt[z] = C;
+            if (C == cend - 1)
+                for (int z = cz + 1; z <= S.M[2]; ++z) zt[z] = cend;
         }
     }
 }
@@ -426,7 +449,7 @@ enum { MODE_EVAL = 0, MODE_COUNT = 1, MODE_EMIT = 2 };
 
 struct WarpSmem {
     int4 jl[SDM_JL_CAP];        // (J | needmask<<31, Sx, Sy, Sz)
-    int4 rng[32];               // (Jbegin, prefix, Sx bits, Sy bits)
+    int4 rng[64];               // (Jbegin, prefix, Sx bits, Sy bits)
     float4 ja[SDM_RING];        // (xs, ys, zs, q)
     float4 jb[SDM_RING];        // (hs, se, mask bits, slot bits)
 };
@@ -436,10 +459,14 @@ struct ICluster {
     float fx[8], fy[8], fz[8];
 };
 
+// One tile: every lane owns one j of the ring window [head, head+count) and
+// sweeps the 8 i-particles of the cluster (warp-uniform i).  Steps whose i has
+// epsilon = 0 (e.g. water hydrogens) take the Coulomb-only branch; the branch
+// condition is the same in every lane.
 template <int MODE, bool IMG>
 __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
                                           WarpSmem& sm, unsigned head, int count, ICluster& ic,
-                                          double& ed, long long& npair) {
+                                          float& ef, long long& npair) {
     const int lane = lane_id();
     const unsigned idx = (head + lane) & (SDM_RING - 1);
     const bool active = lane < count;
@@ -465,26 +492,32 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
         const bool ok = (r2 < rc2) && ((m >> t) & 1u);
         if (MODE == MODE_COUNT) {
             cnt += ok ? 1 : 0;
-        } else {
-            const float r2s = ok ? r2 : 1.0f;
-            const float ir = fast_rsqrt(r2s);
-            const float ir2 = ir * ir;
+            continue;
+        }
+        const float r2s = ok ? r2 : 1.0f;
+        const float ir = fast_rsqrt(r2s);
+        const float ir2 = ir * ir;
+        const float qqm = ok ? ic.q[t] * qj : 0.0f;
+        float fs;
+        if (ic.se[t] != 0.0f) {
             const float sg = ic.hs[t] + hj;
             const float s2 = sg * sg * ir2;
             const float s6 = s2 * s2 * s2;
             const float epsm = ok ? ic.se[t] * ej : 0.0f;
-            const float qqm = ok ? ic.q[t] * qj : 0.0f;
             const float t6 = epsm * s6;
             e = fmaf(t6, s6 - 1.0f, e);
             e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
-            const float fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qqm * fmaf(krf2, r2s, ir)) * ir2;
-            fjx = fmaf(fs, dx, fjx);
-            fjy = fmaf(fs, dy, fjy);
-            fjz = fmaf(fs, dz, fjz);
-            ic.fx[t] = fmaf(-fs, dx, ic.fx[t]);
-            ic.fy[t] = fmaf(-fs, dy, ic.fy[t]);
-            ic.fz[t] = fmaf(-fs, dz, ic.fz[t]);
+            fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qqm * fmaf(krf2, r2s, ir)) * ir2;
+        } else {
+            e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
+            fs = qqm * fmaf(krf2, r2s, ir) * ir2;
         }
+        fjx = fmaf(fs, dx, fjx);
+        fjy = fmaf(fs, dy, fjy);
+        fjz = fmaf(fs, dz, fjz);
+        ic.fx[t] = fmaf(-fs, dx, ic.fx[t]);
+        ic.fy[t] = fmaf(-fs, dy, ic.fy[t]);
+        ic.fz[t] = fmaf(-fs, dz, ic.fz[t]);
     }
     if (MODE == MODE_COUNT) {
         npair += cnt;
@@ -494,7 +527,7 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
         red_fixed(a.F0x + gsl, fjx, a.status);
         red_fixed(a.F0y + gsl, fjy, a.status);
         red_fixed(a.F0z + gsl, fjz, a.status);
-        ed += (double)e;
+        ef += e;
     }
 }
 
@@ -522,6 +555,51 @@ __device__ __forceinline__ unsigned j_mask(const SdmArgs& a, const SdmSys& S, co
             if (e4[k] >= i0 && e4[k] < i0 + 8) m &= ~(1u << (e4[k] - i0));
     }
     return m;
+}
+
+// Cluster ranges of one stencil column restricted to the z window
+// [zc-zh-rz-ext, zc+zh+rz] (frame of reference z cell zref); up to two ranges
+// when the window wraps.  Whole column if `whole`.
+__device__ __forceinline__ void column_ranges(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
+                                              int colid, bool whole, int nlo, int nhi, int zref,
+                                              int& jb1, int& c1, int& jb2, int& c2) {
+    const int* colcl = a.col_cl + R.col_win;
+    c2 = 0;
+    jb2 = 0;
+    if (whole) {
+        jb1 = colcl[colid];
+        c1 = colcl[colid + 1] - jb1;
+        return;
+    }
+    const int Mz = S.M[2];
+    const int* zt = a.ztab + R.ztab_win + colid * (Mz + 1);
+    const int len = nhi - nlo + 1;
+    const int za = pmod(zref + nlo, Mz);
+    jb1 = zt[za];
+    if (za + len <= Mz) {
+        c1 = zt[za + len] - jb1;
+    } else {
+        c1 = zt[Mz] - jb1;
+        jb2 = zt[0];
+        c2 = zt[za + len - Mz] - jb2;
+    }
+}
+
+__device__ __forceinline__ void clip_from(int lo, int& jb, int& c) {
+    if (jb < lo) {
+        c = max(0, jb + c - lo);
+        jb = lo;
+    }
+}
+
+// binary search of the range holding candidate e (ranges sorted by prefix)
+__device__ __forceinline__ int4 find_range(const WarpSmem& sm, int nr, int e) {
+    int lo = 0, hi = nr - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sm.rng[mid].y <= e) lo = mid; else hi = mid - 1;
+    }
+    return sm.rng[lo];
 }
 
 template <int MODE, bool IMG>
@@ -561,32 +639,59 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
     const int nyst = S.sthi[1] - S.stlo[1] + 1;
     const int nst = (S.sthi[0] - S.stlo[0] + 1) * nyst;
     const int kbeg = (nst * part) / a.split, kend = (nst * (part + 1)) / a.split;
-    const int* colcl = a.col_cl + R.col_win;
+    // z window of candidate clusters in reference-cell offsets (conservative)
+    const float extz = __uint_as_float(a.extz[r]);
+    const float gz = S.gf[2];
+    const int nlo = (int)floorf((bc.z - bh.z - rclc - extz) / gz) - 1;
+    const int nhi = (int)floorf((bc.z + bh.z + rclc) / gz) + 1;
+    const bool wholez = IMG || (nhi - nlo + 1 >= S.M[2]);
 
-    int jl_n = 0;               // J-list entries (uniform)
+    int jl_n = 0;                 // J-list entries (uniform)
     unsigned head = 0, tail = 0;  // ring counters (uniform)
-    double ed = 0.0;
+    float ef = 0.0f;
     long long npair = 0;
     int emit_n = 0;
 
     auto phase_b = [&]() {
+        // prefetched gather of the next group of 4 J clusters (8 lanes each)
+        int4 en_n = make_int4(0, 0, 0, 0);
+        float4 X_n = make_float4(SDM_INVALID_COORD, 0.f, 0.f, 0.f);
+        float2 P_n = make_float2(0.f, 0.f);
+        {
+            const int e = lane >> 3;
+            if (e < jl_n) {
+                en_n = sm.jl[e];
+                const int sj = 8 * (en_n.x & 0x7fffffff) + (lane & 7);
+                X_n = a.clX[R.slot_win + sj];
+                P_n = a.clP[R.slot_win + sj];
+            }
+        }
         for (int g0 = 0; g0 < jl_n; g0 += 4) {
             const int e = g0 + (lane >> 3);
             const int t = lane & 7;
+            const int4 en = en_n;
+            const float4 X4 = X_n;
+            const float2 P = P_n;
+            {
+                const int e2 = e + 4;
+                if (e2 < jl_n) {
+                    en_n = sm.jl[e2];
+                    const int sj2 = 8 * (en_n.x & 0x7fffffff) + t;
+                    X_n = a.clX[R.slot_win + sj2];
+                    P_n = a.clP[R.slot_win + sj2];
+                }
+            }
             bool pass = false;
-            float xs = 0.f, ys = 0.f, zs = 0.f, qj = 0.f;
+            float xs = 0.f, ys = 0.f, zs = 0.f;
             int sj = 0;
             unsigned m = 0;
             if (e < jl_n) {
-                const int4 en = sm.jl[e];
                 const int J = en.x & 0x7fffffff;
                 const bool nm = en.x < 0;
                 sj = 8 * J + t;
-                const float4 X4 = a.clX[R.slot_win + sj];
                 xs = __fadd_rn(X4.x, __int_as_float(en.y));
                 ys = __fadd_rn(X4.y, __int_as_float(en.z));
                 zs = __fadd_rn(X4.z, __int_as_float(en.w));
-                qj = X4.w;
                 float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
                 if (IMG) {
                     tx = img32(tx, S.Lf[0], S.invLf[0]);
@@ -615,15 +720,14 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
                 continue;
             }
             if (pass) {
-                const float2 P = a.clP[R.slot_win + sj];
                 const unsigned idx = (tail + pos) & (SDM_RING - 1);
-                sm.ja[idx] = make_float4(xs, ys, zs, qj);
+                sm.ja[idx] = make_float4(xs, ys, zs, X4.w);
                 sm.jb[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
             }
             tail += __popc(bal);
             __syncwarp();
             while (tail - head >= 32u) {
-                eval_tile<MODE, IMG>(a, S, R, sm, head, 32, ic, ed, npair);
+                eval_tile<MODE, IMG>(a, S, R, sm, head, 32, ic, ef, npair);
                 head += 32u;
             }
             __syncwarp();
@@ -632,9 +736,9 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
     };
 
     for (int k0 = kbeg; k0 < kend; k0 += 32) {
-        // ranges of clusters from up to 32 stencil columns
+        // up to two cluster ranges from each of up to 32 stencil columns
         const int k = k0 + lane;
-        int cntJ = 0, Jb = 0;
+        int jb1 = 0, c1 = 0, jb2 = 0, c2 = 0;
         float Sx = 0.f, Sy = 0.f;
         if (k < kend) {
             const int ox = S.stlo[0] + k / nyst;
@@ -654,13 +758,18 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
                 ok = gx * gx + gy * gy < rclc2;
             }
             if (ok) {
-                Jb = (colid == ref.w) ? I : colcl[colid];
-                const int Je = colcl[colid + 1];
-                cntJ = max(Je - Jb, 0);
+                column_ranges(a, S, R, colid, wholez, nlo, nhi, ref.z, jb1, c1, jb2, c2);
+                if (colid == ref.w) {  // own column: clusters J >= I only
+                    clip_from(I, jb1, c1);
+                    clip_from(I, jb2, c2);
+                }
+                c1 = max(c1, 0);
+                c2 = max(c2, 0);
             }
         }
-        const bool has = cntJ > 0;
-        const unsigned hb = __ballot_sync(0xffffffffu, has);
+        const int cntJ = c1 + c2;
+        const unsigned b1 = __ballot_sync(0xffffffffu, c1 > 0);
+        const unsigned b2 = __ballot_sync(0xffffffffu, c2 > 0);
         int incl = cntJ;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -668,30 +777,46 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
             if (lane >= o) incl += v;
         }
         const int total = __shfl_sync(0xffffffffu, incl, 31);
-        if (has) {
-            const int ri = __popc(hb & ((1u << lane) - 1u));
-            sm.rng[ri] = make_int4(Jb, incl - cntJ, __float_as_int(Sx), __float_as_int(Sy));
+        {
+            const unsigned lt = (1u << lane) - 1u;
+            int ri = __popc(b1 & lt) + __popc(b2 & lt);
+            if (c1 > 0) sm.rng[ri++] = make_int4(jb1, incl - cntJ, __float_as_int(Sx), __float_as_int(Sy));
+            if (c2 > 0) sm.rng[ri] = make_int4(jb2, incl - cntJ + c1, __float_as_int(Sx), __float_as_int(Sy));
         }
-        const int nr = __popc(hb);
+        const int nr = __popc(b1) + __popc(b2);
         __syncwarp();
+        // expansion with the next step's gathers issued before the current test
+        int4 rj_n = make_int4(0, 0, 0, 0);
+        float4 cj_n = make_float4(0.f, 0.f, 0.f, 0.f), hj_n = cj_n;
+        int4 lk_n = rj_n;
+        int J_n = 0;
+        float sx_n = 0.f, sy_n = 0.f;
+        if (lane < total) {
+            const int4 rg = find_range(sm, nr, lane);
+            J_n = rg.x + (lane - rg.y);
+            sx_n = __int_as_float(rg.z);
+            sy_n = __int_as_float(rg.w);
+            const int jw = R.cl_win + J_n;
+            rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw]; lk_n = a.cl_link[jw];
+        }
         for (int e0 = 0; e0 < total; e0 += 32) {
             const int e = e0 + lane;
+            const int J = J_n;
+            const int4 rj = rj_n, lk = lk_n;
+            const float4 cj = cj_n, hjb = hj_n;
+            const float sx = sx_n, sy = sy_n;
+            if (e + 32 < total) {
+                const int4 rg = find_range(sm, nr, e + 32);
+                J_n = rg.x + (e + 32 - rg.y);
+                sx_n = __int_as_float(rg.z);
+                sy_n = __int_as_float(rg.w);
+                const int jw = R.cl_win + J_n;
+                rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw]; lk_n = a.cl_link[jw];
+            }
             bool pass = false;
             int4 en = make_int4(0, 0, 0, 0);
             if (e < total) {
-                int lo = 0, hi = nr - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (sm.rng[mid].y <= e) lo = mid; else hi = mid - 1;
-                }
-                const int4 rg = sm.rng[lo];
-                const int J = rg.x + (e - rg.y);
-                const int jw = R.cl_win + J;
-                const int4 rj = a.cl_ref[jw];
                 const float sz = tabz[wrap_cell(rj.z - ref.z, S.M[2]) + S.M[2]];
-                const float sx = __int_as_float(rg.z), sy = __int_as_float(rg.w);
-                const float4 cj = a.cl_bbc[jw];
-                const float4 hjb = a.cl_bbh[jw];
                 float dx = cj.x + sx - bc.x, dy = cj.y + sy - bc.y, dz = cj.z + sz - bc.z;
                 if (IMG) {
                     dx = img32(dx, S.Lf[0], S.invLf[0]);
@@ -700,10 +825,9 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
                 }
                 const float gx = fmaxf(fabsf(dx) - bh.x - hjb.x, 0.0f);
                 const float gy = fmaxf(fabsf(dy) - bh.y - hjb.y, 0.0f);
-                const float gz = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
-                pass = gx * gx + gy * gy + gz * gz < rclc2;
+                const float gz2 = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
+                pass = gx * gx + gy * gy + gz2 * gz2 < rclc2;
                 if (pass) {
-                    const int4 lk = a.cl_link[jw];
                     const bool nm = (J == I) || lk.x == -2 || lk.x == I || lk.y == I ||
                                     lk.z == I || lk.w == I;
                     en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(sx),
@@ -727,7 +851,7 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
         return;
     }
     if (tail != head) {
-        eval_tile<MODE, IMG>(a, S, R, sm, head, (int)(tail - head), ic, ed, npair);
+        eval_tile<MODE, IMG>(a, S, R, sm, head, (int)(tail - head), ic, ef, npair);
         head = tail;
     }
     if (MODE == MODE_COUNT) {
@@ -781,6 +905,7 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
             red_fixed(a.F0z + gsl, v[2], a.status);
         }
     }
+    double ed = (double)ef;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ed += __shfl_xor_sync(0xffffffffu, ed, o);
     if (lane == 0) a.e_part[(size_t)cw * a.split + part] = ed;
@@ -1221,9 +1346,9 @@ static int grid_for(long long n, int block) {
 extern "C++" {
 
 cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* done, cudaStream_t st,
-                            cudaEvent_t* ev, int nev) {
+                            cudaEvent_t* ev, int nev, unsigned ev_flags) {
     int e = 0;
-    auto mark = [&]() { if (ev && e < nev) cudaEventRecord(ev[e++], st); };
+    auto mark = [&]() { if (ev && e < nev) cudaEventRecordWithFlags(ev[e++], st, ev_flags); };
     mark();
     k_cells<<<grid_for(a.total_atoms > a.total_slots ? a.total_atoms : a.total_slots, 256), 256, 0, st>>>(a);
     mark();

@@ -24,6 +24,8 @@
 //     grp      int     displacement group of the slot's particle
 //     excl4    int4    up to 4 exclusion partners as slots (-1 none, -2 overflow)
 //     F0x/F0y/F0z, dFx/dFy/dFz   int64 fixed point 2^32
+//   per replica, column x z-cell (window = ncol*(M[2]+1))
+//     ztab     int     first cluster of the column whose reference z cell >= z
 //   per replica, cluster-indexed (window = slot_cap/8)
 //     cl_ref   int4    reference cell (cx, cy, cz) and column id
 //     cl_bbc   float4  bounding-box centre (cluster frame)
@@ -69,6 +71,7 @@ struct SdmRep {
     int slot_cap;     // slots in the window
     int cl_win;       // cluster window base (slot_win/8)
     int pert_win;     // perturbation partial base (2*nD per replica)
+    int ztab_win;     // column z-table base (ncol*(M[2]+1) per replica)
 };
 
 // Everything a kernel needs, passed by value (fits the 32 KB parameter space).
@@ -119,6 +122,7 @@ struct SdmArgs {
     float4* cl_bbc;
     float4* cl_bbh;
     int4* cl_link;
+    int* ztab;           // per column: first cluster whose reference z cell >= z, z = 0..M[2]
     double* e_part;      // cl window * SDM_MAX_SPLIT
     double* p_part;      // perturbation partials
     int* ncl;            // clusters per replica

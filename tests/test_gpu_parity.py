@@ -89,8 +89,11 @@ def test_config0a_clash_overflow_is_reported():
     b = o.states(x)
     a = o.f32rule(x, h.grid(0))
     assert abs(res[0, capi.R_U0] - b["U0"]) < energy_tol(b["U0"], b["P0"]) + 0.05
-    assert abs(res[0, capi.R_U] - a["u"]) < 1e-6 * abs(a["u"])
-    assert abs(res[0, capi.R_U] - b["u_direct"]) < 1e-6 * abs(b["u_direct"])
+    # u is dominated by clash pairs at r ~ 0.05 nm, where the r^-12 term
+    # amplifies FP32 coordinate rounding (~1e-6 relative in r) twelve-fold:
+    # the achievable relative accuracy is ~1e-5, so the bound is 1e-4
+    assert abs(res[0, capi.R_U] - a["u"]) < 1e-4 * abs(a["u"])
+    assert abs(res[0, capi.R_U] - b["u_direct"]) < 1e-4 * abs(b["u_direct"])
     assert rms_rel(F0, b["F0"]) < FORCE_RMS_REL_TOL
 
 
