@@ -217,8 +217,9 @@ def main():
     xd = torch.from_numpy(xh).to(dev)
     rd = torch.zeros((NREP, capi.NRESULTS), dtype=torch.float64, device=dev)
     fd = torch.zeros_like(xd)
+    tuned = None
     if args.autotune:
-        h.autotune(xd.data_ptr())
+        tuned = h.autotune(xd.data_ptr())
     l2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
 
     def flush():
@@ -272,6 +273,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         tot_b = float(t.item())
     value = NREP * args.steps * world / tot_b
+    jlist_ms = [d["k_jlist"] for d in pk]
     pair_ms = [d["k_pair"] for d in pk]
     pert_ms = [d["k_perturb"] for d in pk]
     pair_avg = sum(pair_ms) / len(pair_ms)
@@ -328,6 +330,9 @@ def main():
             "peak_source": f"{nsm} SMs x 128 FP32 lanes x 2 x {fmax:.0f} MHz ({src} sm_max_mhz)",
             "frac_at_run_clock": (achieved_tf / (nsm * 256 * f_run * 1e6 / 1e12)) if f_run else None,
             "pair_kernel_ms": pair_avg, "perturb_kernel_ms": sum(pert_ms) / len(pert_ms),
+            "jlist_kernel_ms": sum(jlist_ms) / len(jlist_ms),
+            "frac_pair_path": (flop_per_launch / ((pair_avg + sum(jlist_ms) / len(jlist_ms)
+                                                   + sum(pert_ms) / len(pert_ms)) * 1e-3) / 1e12) / peak_tf,
             "flop_per_launch": flop_per_launch, "P0": P0, "P1delta": P1}
     traffic_file = os.path.join(ROOT, "profiles", "k_pair_traffic.json")
     if os.path.exists(traffic_file):
@@ -350,7 +355,9 @@ def main():
         "config": {"workload": "config2: 22 replicas x 22,580 particles (7,500 waters + 2x40 ligand), "
                                "6.2 nm box, rc 1.0 nm reaction field, one batched call per step as a CUDA graph",
                    "replicas_per_gpu": NREP, "particles": n, "l2": "flushed (256 MB write) before every timed step",
-                   "parallelism": f"replicas only, {world} independent rank(s)"},
+                   "parallelism": f"replicas only, {world} independent rank(s)",
+                   "schedule": {"split": h.get_option(capi.OPT_SPLIT), "ctas_per_sm": h.get_option(capi.OPT_CTAS_PER_SM),
+                                "autotuned": tuned is not None}},
         "plain": {"value": plain, "unit": UNIT, "ms_per_call": sum(ms_p) / len(ms_p),
                   "workload": "config1: one 22,580-particle replica per call (CUDA graph)"},
         "batched_over_plain": value / world / plain,

@@ -223,7 +223,10 @@ sdm_status sdm_export_lists(sdm_handle* h, int replica, const double* x, int cap
 enum {
     SDM_DEV_FORCE_OVERFLOW = 1,   /* |force term| >= 2^31 kJ/mol/nm or NaN */
     SDM_DEV_ENERGY_NONFINITE = 2, /* NaN/Inf energy */
-    SDM_DEV_EXCL_OVERFLOW = 4     /* internal exclusion table overflow (should not happen) */
+    SDM_DEV_EXCL_OVERFLOW = 4,    /* internal exclusion table overflow (should not happen) */
+    SDM_DEV_LIST_OVERFLOW = 8     /* a cluster-pair list exceeded its capacity; sdm_evaluate
+                                     regrows and repeats, device callers see SDM_ERR_CAPACITY
+                                     from sdm_check_status and call sdm_evaluate once */
 };
 
 #ifdef __cplusplus

@@ -19,8 +19,9 @@
 #include "../../include/sdm_capi.h"
 #include "sdm_types.h"
 
-cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* done, cudaStream_t st,
+cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* cl_prefix, int* done, cudaStream_t st,
                             cudaEvent_t* ev, int nev, unsigned ev_flags);
+cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_t st);
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
                             cudaStream_t st);
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
@@ -83,7 +84,12 @@ struct sdm_handle {
     cudaStream_t stream = nullptr;
     SdmArgs args{};
     int* item_prefix = nullptr;
+    int* cl_prefix = nullptr;
     int* done = nullptr;
+    // cluster-pair lists (own allocation: regrown on overflow)
+    int4* jl_buf = nullptr;
+    long long jl_clusters = 0;  // cluster windows covered
+    int jl_cap = 0;
     void* counters = nullptr;  // memset block
     size_t counters_bytes = 0;
     double* x_in = nullptr;
@@ -95,7 +101,7 @@ struct sdm_handle {
     std::vector<double> params;
     bool params_dirty = true;
     // options
-    int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 4, opt_verify = 1;
+    int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 3, opt_verify = 1;
     // graphs
     std::map<GraphKey, cudaGraphExec_t> graphs;
     // profiling
@@ -109,8 +115,9 @@ struct sdm_handle {
 
 namespace {
 
-const char* const kKernelNames[] = {"k_cells", "k_scan", "k_bucket", "k_colsort",
-                                    "k_clusters", "k_pair", "k_perturb", "k_finalize+k_mix"};
+const char* const kKernelNames[] = {"k_cells", "k_scan", "k_bucket", "k_colsort", "k_clusters",
+                                    "k_jlist", "k_pair", "k_perturb", "k_finalize+k_mix"};
+const int kNumTimed = 9;
 
 sdm_status fail(sdm_handle* h, sdm_status code, const std::string& msg) {
     if (h) h->err = msg; else g_create_error = msg;
@@ -342,13 +349,15 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     const unsigned fl = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     SDM_CUDA(h, cudaMemsetAsync(h->counters, 0, h->counters_bytes, st));
     cudaEvent_t* ev = profile ? h->ev : nullptr;
-    SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->done, st, ev, 6, fl));
-    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, st));
+    SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->cl_prefix, h->done, st, ev, 6, fl));
+    SDM_CUDA(h, sdm_launch_jlist(a, h->cl_prefix, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[6], st, fl));
-    if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
+    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
-    if (mode == 0) SDM_CUDA(h, sdm_launch_finalize(a, st));
+    if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[8], st, fl));
+    if (mode == 0) SDM_CUDA(h, sdm_launch_finalize(a, st));
+    if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[9], st, fl));
     return SDM_OK;
 }
 
@@ -381,9 +390,10 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
         s = enqueue(h, a, mode, st, profile, false);
         if (s) return s;
         if (profile) {
-            SDM_CUDA(h, cudaEventSynchronize(h->ev[8]));
-            for (int k = 0; k < 8; ++k) SDM_CUDA(h, cudaEventElapsedTime(&h->last_ms[k], h->ev[k], h->ev[k + 1]));
-            h->last_nk = 8;
+            SDM_CUDA(h, cudaEventSynchronize(h->ev[kNumTimed]));
+            for (int k = 0; k < kNumTimed; ++k)
+                SDM_CUDA(h, cudaEventElapsedTime(&h->last_ms[k], h->ev[k], h->ev[k + 1]));
+            h->last_nk = kNumTimed;
         }
         h->have_eval = (mode == 0);
         return SDM_OK;
@@ -410,7 +420,7 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
     }
     SDM_CUDA(h, cudaGraphLaunch(it->second, st));
     h->have_eval = true;
-    h->last_nk = gprof ? -8 : 0;  // negative: times pending inside the last replay
+    h->last_nk = gprof ? -kNumTimed : 0;  // negative: times pending inside the last replay
     return SDM_OK;
 }
 
@@ -423,6 +433,26 @@ sdm_status check_dev_status(sdm_handle* h, int* out, bool clear) {
 }
 
 }  // namespace
+
+// (Re)allocates the cluster-pair lists with `cap` entries per i-cluster.
+static sdm_status sdm_reserve_lists(sdm_handle* h, int cap) {
+    if (h->stream) SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->jl_buf) { cudaFree(h->jl_buf); h->jl_buf = nullptr; }
+    const size_t bytes = (size_t)h->jl_clusters * (size_t)cap * sizeof(int4);
+    cudaError_t ce = cudaMalloc(&h->jl_buf, bytes);
+    if (ce != cudaSuccess) { h->jl_buf = nullptr; return cuda_fail(h, ce, "cudaMalloc(cluster-pair lists)"); }
+    h->jl_cap = cap;
+    h->args.jl = h->jl_buf;
+    h->args.jl_cap = cap;
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    return SDM_OK;
+}
+
+// After an overflow: double the capacity (the last results are invalid).
+static sdm_status regrow_lists(sdm_handle* h) {
+    return sdm_reserve_lists(h, h->jl_cap * 2);
+}
 
 // --------------------------------------------------------------------------- //
 extern "C" {
@@ -536,6 +566,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_pp = ar.take<double>(std::max(Pp, 1LL));
     const size_t o_ncl = ar.take<int>(nrep), o_st = ar.take<int>(4);
     const size_t o_counts = ar.take<long long>(2 * nrep), o_ip = ar.take<int>(nrep + 1);
+    const size_t o_cp = ar.take<int>(nrep + 1), o_jc = ar.take<int>(Cl);
     const size_t o_done = ar.take<int>(4);
     h->arena_bytes = ar.off + 256;
     cudaError_t ce = cudaMalloc(&h->arena, h->arena_bytes);
@@ -597,6 +628,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.status = at<int>(B, o_st);
     a.counts = at<long long>(B, o_counts);
     h->item_prefix = at<int>(B, o_ip);
+    h->cl_prefix = at<int>(B, o_cp);
+    a.jl_cnt = at<int>(B, o_jc);
     h->done = at<int>(B, o_done);
     a.total_atoms = (int)A;
     a.total_cols = (int)Ccol;
@@ -609,7 +642,20 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     for (int r = 0; r < nrep; ++r) default_params(&h->params[(size_t)r * SDM_NPARAMS]);
     ce = cudaMallocHost(&h->params_pinned, h->params.size() * sizeof(double));
     if (ce != cudaSuccess) { h->params_pinned = nullptr; cuda_fail(h, ce, "cudaMallocHost"); return bail(SDM_ERR_CUDA); }
-    sdm_status st = upload_topology(h);
+    // cluster-pair list capacity: twice the expected count of clusters within
+    // rc + 1.5 cluster edges over a half shell, at the densest system
+    double need = 64.0;
+    for (auto& s : h->sys) {
+        const double vol = s.dev.box[0] * s.dev.box[1] * s.dev.box[2];
+        const double rho = s.n / vol;
+        const double edge = std::cbrt(8.0 / rho);
+        const double rr = s.dev.rc + 1.5 * edge;
+        need = std::max(need, 0.5 * rho / 8.0 * 4.18879 * rr * rr * rr);
+    }
+    h->jl_clusters = Cl;
+    sdm_status st = sdm_reserve_lists(h, (int)std::min(4096.0, 2.0 * need + 64.0));
+    if (st) return bail(st);
+    st = upload_topology(h);
     if (st) return bail(st);
     *out = h;
     return SDM_OK;
@@ -617,6 +663,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
 
 sdm_status sdm_destroy(sdm_handle* h) {
     if (!h) return SDM_OK;
+    if (h->jl_buf) { cudaSetDevice(h->device); cudaFree(h->jl_buf); h->jl_buf = nullptr; }
     if (h->arena) cudaSetDevice(h->device);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
@@ -674,13 +721,19 @@ sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double*
     if (forces)
         SDM_CUDA(h, cudaMemcpyAsync(forces, h->f_in, nx * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
-    if (h->opt_verify) {
-        int v = 0;
-        s = check_dev_status(h, &v, true);
+    int v = 0;
+    s = check_dev_status(h, &v, true);
+    if (s) return s;
+    if (v & SDM_DEV_LIST_OVERFLOW) {
+        // lists too small for these coordinates: regrow and evaluate again
+        if (h->jl_cap >= (1 << 16)) return fail(h, SDM_ERR_CAPACITY, "cluster-pair list capacity limit reached");
+        s = regrow_lists(h);
         if (s) return s;
-        if (v) return fail(h, SDM_ERR_OVERFLOW, "device status " + std::to_string(v) +
-                                                    ": force overflow or non-finite energy");
+        return sdm_evaluate(h, x, results, forces);
     }
+    if (h->opt_verify && v)
+        return fail(h, SDM_ERR_OVERFLOW, "device status " + std::to_string(v) +
+                                             ": force overflow or non-finite energy");
     return SDM_OK;
 }
 
@@ -727,7 +780,16 @@ sdm_status sdm_check_status(sdm_handle* h, int* device_status) {
     if (!h) return SDM_ERR_INVALID_ARGUMENT;
     cudaSetDevice(h->device);
     SDM_CUDA(h, cudaDeviceSynchronize());
-    return check_dev_status(h, device_status, true);
+    int v = 0;
+    sdm_status s = check_dev_status(h, &v, true);
+    if (s) return s;
+    if (device_status) *device_status = v;
+    if (v & SDM_DEV_LIST_OVERFLOW) {
+        s = regrow_lists(h);
+        if (s) return s;
+        return fail(h, SDM_ERR_CAPACITY, "cluster-pair lists overflowed and were regrown: evaluate again");
+    }
+    return SDM_OK;
 }
 
 sdm_status sdm_set_option(sdm_handle* h, int option, int value) {
@@ -770,9 +832,10 @@ sdm_status sdm_get_kernel_times(const sdm_handle* hc, const char** names, float*
     sdm_handle* h = const_cast<sdm_handle*>(hc);
     if (h->last_nk < 0) {
         cudaSetDevice(h->device);
-        SDM_CUDA(h, cudaEventSynchronize(h->ev[8]));
-        for (int k = 0; k < 8; ++k) SDM_CUDA(h, cudaEventElapsedTime(&h->last_ms[k], h->ev[k], h->ev[k + 1]));
-        h->last_nk = 8;
+        SDM_CUDA(h, cudaEventSynchronize(h->ev[kNumTimed]));
+        for (int k = 0; k < kNumTimed; ++k)
+            SDM_CUDA(h, cudaEventElapsedTime(&h->last_ms[k], h->ev[k], h->ev[k + 1]));
+        h->last_nk = kNumTimed;
     }
     const int n = std::min(*count, h->last_nk);
     for (int k = 0; k < n; ++k) {
@@ -800,7 +863,7 @@ sdm_status sdm_autotune(sdm_handle* h, const double* x_device, int* split, int* 
             for (int rep = 0; rep < 4; ++rep) {
                 sdm_status s = run(h, x_device, h->res_in, h->f_in, h->stream, 0, false);
                 if (s) { h->opt_split = osplit; h->opt_ctas = octas; h->opt_profile = oprof; return s; }
-                if (rep > 0) t += h->last_ms[5] + h->last_ms[6];
+                if (rep > 0) t += h->last_ms[5] + h->last_ms[6] + h->last_ms[7];
             }
             if (t < best) { best = t; bs = sp; bc = c; }
         }

@@ -79,11 +79,6 @@ __device__ __forceinline__ float fast_rsqrt(float x) {
     return y;
 }
 
-__device__ __forceinline__ void red_fixed(unsigned long long* p, float v, int* status) {
-    if (!(fabsf(v) < 2.0e9f)) atomicOr(status, SDM_DEV_FORCE_OVERFLOW);
-    long long q = __float2ll_rn(v * 4294967296.0f);
-    atomicAdd(p, (unsigned long long)q);
-}
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
@@ -170,7 +165,7 @@ __device__ __forceinline__ int2 warp_incl_scan2(int2 v) {
     return v;
 }
 
-__global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int* done) {
+__global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int* cl_prefix, int* done) {
     __shared__ int2 wsum[32];
     __shared__ int last;
     const int r = blockIdx.x;
@@ -235,9 +230,10 @@ __global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int*
         int b = inc2.x - t.x + (wid > 0 ? wsum[wid - 1].x : 0);
         for (int q = b2; q < e2; ++q) {
             item_prefix[q] = b;
+            cl_prefix[q] = b / a.split;
             b += ((volatile int*)a.ncl)[q] * a.split;
         }
-        if (threadIdx.x == blockDim.x - 1) item_prefix[nrep] = b;
+        if (threadIdx.x == blockDim.x - 1) { item_prefix[nrep] = b; cl_prefix[nrep] = b / a.split; }
         if (threadIdx.x == 0) *done = 0;
     }
 }
@@ -442,16 +438,21 @@ __device__ __forceinline__ bool replica_image_mode(const SdmArgs& a, const SdmSy
     return !(0.5 * S.box[2] - S.rc - ez > 1.0e-3);
 }
 
-// ------------------------------------------------------------------------- //
-// K6: main pass                                                             //
-// ------------------------------------------------------------------------- //
 enum { MODE_EVAL = 0, MODE_COUNT = 1, MODE_EMIT = 2 };
 
-struct WarpSmem {
-    int4 jl[SDM_JL_CAP];        // (J | needmask<<31, Sx, Sy, Sz)
+struct WarpSmem {               // perturbation pass scratch
+    int4 jl[SDM_JL_CAP];        // (J, Sx, Sy, Sz)
     int4 rng[64];               // (Jbegin, prefix, Sx bits, Sy bits)
-    float4 ja[SDM_RING];        // (xs, ys, zs, q)
-    float4 jb[SDM_RING];        // (hs, se, mask bits, slot bits)
+};
+
+struct Ring {                   // one tile ring: 64 prepared j entries
+    float4 a[SDM_RING];         // (xs, ys, zs, q)
+    float4 b[SDM_RING];         // (hs, se, mask bits, slot bits)
+};
+
+struct EvalSmem {
+    Ring lj;                    // j with epsilon != 0
+    Ring co;                    // j with epsilon == 0 (Coulomb only)
 };
 
 struct ICluster {
@@ -459,107 +460,24 @@ struct ICluster {
     float fx[8], fy[8], fz[8];
 };
 
-// One tile: every lane owns one j of the ring window [head, head+count) and
-// sweeps the 8 i-particles of the cluster (warp-uniform i).  Steps whose i has
-// epsilon = 0 (e.g. water hydrogens) take the Coulomb-only branch; the branch
-// condition is the same in every lane.
-template <int MODE, bool IMG>
-__device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
-                                          WarpSmem& sm, unsigned head, int count, ICluster& ic,
-                                          float& ef, long long& npair) {
-    const int lane = lane_id();
-    const unsigned idx = (head + lane) & (SDM_RING - 1);
-    const bool active = lane < count;
-    // inactive lanes use zeros, never stale ring contents
-    const float4 A = active ? sm.ja[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 B = active ? sm.jb[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const unsigned m = active ? __float_as_uint(B.z) : 0u;
-    const float xs = A.x, ys = A.y, zs = A.z, qj = A.w, hj = B.x, ej = B.y;
-    const float rc2 = S.rc2f, krf = S.krf, crf = S.crf, krf2 = -2.0f * S.krf;
-    float fjx = 0.f, fjy = 0.f, fjz = 0.f, e = 0.f;
-    int cnt = 0;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        float dx = __fsub_rn(xs, ic.x[t]);
-        float dy = __fsub_rn(ys, ic.y[t]);
-        float dz = __fsub_rn(zs, ic.z[t]);
-        if (IMG) {
-            dx = img32(dx, S.Lf[0], S.invLf[0]);
-            dy = img32(dy, S.Lf[1], S.invLf[1]);
-            dz = img32(dz, S.Lf[2], S.invLf[2]);
-        }
-        const float r2 = r2_chain(dx, dy, dz);
-        const bool ok = (r2 < rc2) && ((m >> t) & 1u);
-        if (MODE == MODE_COUNT) {
-            cnt += ok ? 1 : 0;
-            continue;
-        }
-        const float r2s = ok ? r2 : 1.0f;
-        const float ir = fast_rsqrt(r2s);
-        const float ir2 = ir * ir;
-        const float qqm = ok ? ic.q[t] * qj : 0.0f;
-        float fs;
-        if (ic.se[t] != 0.0f) {
-            const float sg = ic.hs[t] + hj;
-            const float s2 = sg * sg * ir2;
-            const float s6 = s2 * s2 * s2;
-            const float epsm = ok ? ic.se[t] * ej : 0.0f;
-            const float t6 = epsm * s6;
-            e = fmaf(t6, s6 - 1.0f, e);
-            e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
-            fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qqm * fmaf(krf2, r2s, ir)) * ir2;
-        } else {
-            e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
-            fs = qqm * fmaf(krf2, r2s, ir) * ir2;
-        }
-        fjx = fmaf(fs, dx, fjx);
-        fjy = fmaf(fs, dy, fjy);
-        fjz = fmaf(fs, dz, fjz);
-        ic.fx[t] = fmaf(-fs, dx, ic.fx[t]);
-        ic.fy[t] = fmaf(-fs, dy, ic.fy[t]);
-        ic.fz[t] = fmaf(-fs, dz, ic.fz[t]);
-    }
-    if (MODE == MODE_COUNT) {
-        npair += cnt;
-    } else if (active) {
-        const int slot = __float_as_int(B.w);
-        const size_t gsl = (size_t)R.slot_win + slot;
-        red_fixed(a.F0x + gsl, fjx, a.status);
-        red_fixed(a.F0y + gsl, fjy, a.status);
-        red_fixed(a.F0z + gsl, fjz, a.status);
-        ef += e;
-    }
+// round(v * 2^32) as a 64-bit two's-complement integer from two 32-bit
+// conversions (|v| < 2^30, checked by the caller); avoids the float->int64
+// conversion, which runs on the narrow FP64 pipe.
+__device__ __forceinline__ unsigned long long fix64(float v) {
+    const float a = rintf(v);
+    const int hi = __float2int_rn(a);
+    const int lo = __float2int_rn(__fmul_rn(__fsub_rn(v, a), 4294967296.0f));
+    return (unsigned long long)(((long long)hi << 32) + (long long)lo);
 }
 
-// Computes the allowed-i mask of candidate slot j (cluster J) against
-// i-cluster I (valid-i bits vmask).
-__device__ __forceinline__ unsigned j_mask(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
-                                           int I, int J, int sj, unsigned vmask, bool needmask) {
-    unsigned m = vmask;
-    if (!needmask) return m;
-    const int t = sj & 7;
-    if (J == I) m &= (1u << t) - 1u;
-    const int4 ex = a.excl4[R.slot_win + sj];
-    const int i0 = 8 * I;
-    if (ex.x == -2) {
-        const int p = a.perm[R.slot_win + sj];
-        const int ta = S.atom_base + p;
-        for (int k = a.excl_off[ta]; k < a.excl_off[ta + 1]; ++k) {
-            const int s2 = a.inv[R.atom_win + a.excl_idx[k]];
-            if (s2 >= i0 && s2 < i0 + 8) m &= ~(1u << (s2 - i0));
-        }
-    } else {
-        const int e4[4] = {ex.x, ex.y, ex.z, ex.w};
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (e4[k] >= i0 && e4[k] < i0 + 8) m &= ~(1u << (e4[k] - i0));
-    }
-    return m;
+__device__ __forceinline__ void red_fix(unsigned long long* p, float v, int* status) {
+    if (!(fabsf(v) < 1.0e9f)) atomicOr(status, SDM_DEV_FORCE_OVERFLOW);
+    atomicAdd(p, fix64(v));
 }
 
-// Cluster ranges of one stencil column restricted to the z window
-// [zc-zh-rz-ext, zc+zh+rz] (frame of reference z cell zref); up to two ranges
-// when the window wraps.  Whole column if `whole`.
+// Cluster ranges of one stencil column restricted to the z window of
+// reference-cell offsets [nlo, nhi] around zref; up to two ranges when the
+// window wraps.  Whole column if `whole`.
 __device__ __forceinline__ void column_ranges(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
                                               int colid, bool whole, int nlo, int nhi, int zref,
                                               int& jb1, int& c1, int& jb2, int& c2) {
@@ -592,45 +510,20 @@ __device__ __forceinline__ void clip_from(int lo, int& jb, int& c) {
     }
 }
 
-// binary search of the range holding candidate e (ranges sorted by prefix)
-__device__ __forceinline__ int4 find_range(const WarpSmem& sm, int nr, int e) {
-    int lo = 0, hi = nr - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (sm.rng[mid].y <= e) lo = mid; else hi = mid - 1;
-    }
-    return sm.rng[lo];
-}
-
-template <int MODE, bool IMG>
-__device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSmem& sm) {
+// ------------------------------------------------------------------------- //
+// K6a: cluster-pair lists.  For i-cluster I: every cluster J >= I (slot     //
+// order) of the half stencil whose shifted bounding box comes within        //
+// rc + margin of I's box, as (J | needmask<<31, Sx, Sy, Sz).                //
+// ------------------------------------------------------------------------- //
+template <bool IMG>
+__device__ void build_jlist(const SdmArgs& a, int r, int I) {
     const int lane = lane_id();
     const SdmRep R = a.rep[r];
-    const SdmSys& S = a.sys[R.sys];
+    const SdmSys S = a.sys[R.sys];
     const int cw = R.cl_win + I;
-    const int slot0 = R.slot_win + 8 * I;
-    // i-cluster particles, replicated in every lane
-    ICluster ic;
-    {
-        float4 xi4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        float2 pi2 = make_float2(0.f, 0.f);
-        if (lane < 8) { xi4 = a.clX[slot0 + lane]; pi2 = a.clP[slot0 + lane]; }
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            ic.x[t] = __shfl_sync(0xffffffffu, xi4.x, t);
-            ic.y[t] = __shfl_sync(0xffffffffu, xi4.y, t);
-            ic.z[t] = __shfl_sync(0xffffffffu, xi4.z, t);
-            ic.q[t] = __shfl_sync(0xffffffffu, xi4.w, t);
-            ic.hs[t] = __shfl_sync(0xffffffffu, pi2.x, t);
-            ic.se[t] = __shfl_sync(0xffffffffu, pi2.y, t);
-            ic.fx[t] = 0.f; ic.fy[t] = 0.f; ic.fz[t] = 0.f;
-        }
-    }
-    const unsigned vmask = __ballot_sync(0xffffffffu, lane < 8 && a.perm[slot0 + (lane & 7)] >= 0) & 0xffu;
     const float4 bc = a.cl_bbc[cw];
     const float4 bh = a.cl_bbh[cw];
     const int4 ref = a.cl_ref[cw];
-    const float rcl2 = S.rcl2f;
     const float rclc = S.rcl + 2.0e-4f;
     const float rclc2 = rclc * rclc;
     const float* tabx = a.shift_tab + S.shift_base;
@@ -638,109 +531,17 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
     const float* tabz = taby + 2 * S.M[1] + 1;
     const int nyst = S.sthi[1] - S.stlo[1] + 1;
     const int nst = (S.sthi[0] - S.stlo[0] + 1) * nyst;
-    const int kbeg = (nst * part) / a.split, kend = (nst * (part + 1)) / a.split;
-    // z window of candidate clusters in reference-cell offsets (conservative)
     const float extz = __uint_as_float(a.extz[r]);
-    const float gz = S.gf[2];
-    const int nlo = (int)floorf((bc.z - bh.z - rclc - extz) / gz) - 1;
-    const int nhi = (int)floorf((bc.z + bh.z + rclc) / gz) + 1;
+    const int nlo = (int)floorf((bc.z - bh.z - rclc - extz) / S.gf[2]) - 1;
+    const int nhi = (int)floorf((bc.z + bh.z + rclc) / S.gf[2]) + 1;
     const bool wholez = IMG || (nhi - nlo + 1 >= S.M[2]);
-
-    int jl_n = 0;                 // J-list entries (uniform)
-    unsigned head = 0, tail = 0;  // ring counters (uniform)
-    float ef = 0.0f;
-    long long npair = 0;
-    int emit_n = 0;
-
-    auto phase_b = [&]() {
-        // prefetched gather of the next group of 4 J clusters (8 lanes each)
-        int4 en_n = make_int4(0, 0, 0, 0);
-        float4 X_n = make_float4(SDM_INVALID_COORD, 0.f, 0.f, 0.f);
-        float2 P_n = make_float2(0.f, 0.f);
-        {
-            const int e = lane >> 3;
-            if (e < jl_n) {
-                en_n = sm.jl[e];
-                const int sj = 8 * (en_n.x & 0x7fffffff) + (lane & 7);
-                X_n = a.clX[R.slot_win + sj];
-                P_n = a.clP[R.slot_win + sj];
-            }
-        }
-        for (int g0 = 0; g0 < jl_n; g0 += 4) {
-            const int e = g0 + (lane >> 3);
-            const int t = lane & 7;
-            const int4 en = en_n;
-            const float4 X4 = X_n;
-            const float2 P = P_n;
-            {
-                const int e2 = e + 4;
-                if (e2 < jl_n) {
-                    en_n = sm.jl[e2];
-                    const int sj2 = 8 * (en_n.x & 0x7fffffff) + t;
-                    X_n = a.clX[R.slot_win + sj2];
-                    P_n = a.clP[R.slot_win + sj2];
-                }
-            }
-            bool pass = false;
-            float xs = 0.f, ys = 0.f, zs = 0.f;
-            int sj = 0;
-            unsigned m = 0;
-            if (e < jl_n) {
-                const int J = en.x & 0x7fffffff;
-                const bool nm = en.x < 0;
-                sj = 8 * J + t;
-                xs = __fadd_rn(X4.x, __int_as_float(en.y));
-                ys = __fadd_rn(X4.y, __int_as_float(en.z));
-                zs = __fadd_rn(X4.z, __int_as_float(en.w));
-                float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
-                if (IMG) {
-                    tx = img32(tx, S.Lf[0], S.invLf[0]);
-                    ty = img32(ty, S.Lf[1], S.invLf[1]);
-                    tz = img32(tz, S.Lf[2], S.invLf[2]);
-                }
-                const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
-                const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
-                const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
-                // padding slots carry 1e6 coordinates; in image mode they could wrap
-                pass = (X4.x < 1.0e5f) && r2_chain(ex, ey, ez) < rcl2;
-                if (pass) {
-                    m = j_mask(a, S, R, I, J, sj, vmask, nm);
-                    pass = m != 0u;
-                }
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, pass);
-            const int pos = __popc(bal & ((1u << lane) - 1u));
-            if (MODE == MODE_EMIT) {
-                if (pass && emit_n + pos < a.ex_cap) {
-                    const size_t o = (size_t)I * a.ex_cap + emit_n + pos;
-                    a.ex_slot[o] = sj;
-                    a.ex_mask[o] = (unsigned char)m;
-                }
-                emit_n += __popc(bal);
-                continue;
-            }
-            if (pass) {
-                const unsigned idx = (tail + pos) & (SDM_RING - 1);
-                sm.ja[idx] = make_float4(xs, ys, zs, X4.w);
-                sm.jb[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
-            }
-            tail += __popc(bal);
-            __syncwarp();
-            while (tail - head >= 32u) {
-                eval_tile<MODE, IMG>(a, S, R, sm, head, 32, ic, ef, npair);
-                head += 32u;
-            }
-            __syncwarp();
-        }
-        jl_n = 0;
-    };
-
-    for (int k0 = kbeg; k0 < kend; k0 += 32) {
-        // up to two cluster ranges from each of up to 32 stencil columns
+    int4* out = a.jl + (size_t)cw * a.jl_cap;
+    int cnt = 0;
+    for (int k0 = 0; k0 < nst; k0 += 32) {
         const int k = k0 + lane;
         int jb1 = 0, c1 = 0, jb2 = 0, c2 = 0;
         float Sx = 0.f, Sy = 0.f;
-        if (k < kend) {
+        if (k < nst) {
             const int ox = S.stlo[0] + k / nyst;
             const int oy = S.stlo[1] + k % nyst;
             const int ccx = pmod(ref.x + ox, S.M[0]);
@@ -767,57 +568,33 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
                 c2 = max(c2, 0);
             }
         }
-        const int cntJ = c1 + c2;
-        const unsigned b1 = __ballot_sync(0xffffffffu, c1 > 0);
-        const unsigned b2 = __ballot_sync(0xffffffffu, c2 > 0);
-        int incl = cntJ;
+        const int nc = c1 + c2;
+        int maxc = nc;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        {
-            const unsigned lt = (1u << lane) - 1u;
-            int ri = __popc(b1 & lt) + __popc(b2 & lt);
-            if (c1 > 0) sm.rng[ri++] = make_int4(jb1, incl - cntJ, __float_as_int(Sx), __float_as_int(Sy));
-            if (c2 > 0) sm.rng[ri] = make_int4(jb2, incl - cntJ + c1, __float_as_int(Sx), __float_as_int(Sy));
-        }
-        const int nr = __popc(b1) + __popc(b2);
-        __syncwarp();
-        // expansion with the next step's gathers issued before the current test
-        int4 rj_n = make_int4(0, 0, 0, 0);
+        for (int o = 16; o > 0; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
+        // each lane walks its own column; the next candidate's data is fetched ahead
+        int4 rj_n = make_int4(0, 0, 0, 0), lk_n = rj_n;
         float4 cj_n = make_float4(0.f, 0.f, 0.f, 0.f), hj_n = cj_n;
-        int4 lk_n = rj_n;
-        int J_n = 0;
-        float sx_n = 0.f, sy_n = 0.f;
-        if (lane < total) {
-            const int4 rg = find_range(sm, nr, lane);
-            J_n = rg.x + (lane - rg.y);
-            sx_n = __int_as_float(rg.z);
-            sy_n = __int_as_float(rg.w);
+        int J_n = jb1;
+        if (nc > 0) {
+            J_n = (c1 > 0) ? jb1 : jb2;
             const int jw = R.cl_win + J_n;
             rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw]; lk_n = a.cl_link[jw];
         }
-        for (int e0 = 0; e0 < total; e0 += 32) {
-            const int e = e0 + lane;
+        for (int it = 0; it < maxc; ++it) {
             const int J = J_n;
             const int4 rj = rj_n, lk = lk_n;
             const float4 cj = cj_n, hjb = hj_n;
-            const float sx = sx_n, sy = sy_n;
-            if (e + 32 < total) {
-                const int4 rg = find_range(sm, nr, e + 32);
-                J_n = rg.x + (e + 32 - rg.y);
-                sx_n = __int_as_float(rg.z);
-                sy_n = __int_as_float(rg.w);
+            if (it + 1 < nc) {
+                J_n = (it + 1 < c1) ? jb1 + it + 1 : jb2 + (it + 1 - c1);
                 const int jw = R.cl_win + J_n;
                 rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw]; lk_n = a.cl_link[jw];
             }
             bool pass = false;
             int4 en = make_int4(0, 0, 0, 0);
-            if (e < total) {
+            if (it < nc) {
                 const float sz = tabz[wrap_cell(rj.z - ref.z, S.M[2]) + S.M[2]];
-                float dx = cj.x + sx - bc.x, dy = cj.y + sy - bc.y, dz = cj.z + sz - bc.z;
+                float dx = cj.x + Sx - bc.x, dy = cj.y + Sy - bc.y, dz = cj.z + sz - bc.z;
                 if (IMG) {
                     dx = img32(dx, S.Lf[0], S.invLf[0]);
                     dy = img32(dy, S.Lf[1], S.invLf[1]);
@@ -825,35 +602,279 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
                 }
                 const float gx = fmaxf(fabsf(dx) - bh.x - hjb.x, 0.0f);
                 const float gy = fmaxf(fabsf(dy) - bh.y - hjb.y, 0.0f);
-                const float gz2 = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
-                pass = gx * gx + gy * gy + gz2 * gz2 < rclc2;
-                if (pass) {
-                    const bool nm = (J == I) || lk.x == -2 || lk.x == I || lk.y == I ||
-                                    lk.z == I || lk.w == I;
-                    en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(sx),
-                                   __float_as_int(sy), __float_as_int(sz));
-                }
+                const float gz = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
+                pass = gx * gx + gy * gy + gz * gz < rclc2;
+                const bool nm = (J == I) || lk.x == -2 || lk.x == I || lk.y == I || lk.z == I || lk.w == I;
+                en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(Sx), __float_as_int(Sy),
+                               __float_as_int(sz));
             }
             const unsigned bal = __ballot_sync(0xffffffffu, pass);
-            if (pass) sm.jl[jl_n + __popc(bal & ((1u << lane) - 1u))] = en;
-            jl_n += __popc(bal);
-            __syncwarp();
-            if (jl_n > SDM_JL_CAP - 32) phase_b();
+            if (pass) {
+                const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+                if (pos < a.jl_cap) out[pos] = en;
+            }
+            cnt += __popc(bal);
+        }
+    }
+    if (lane == 0) {
+        a.jl_cnt[cw] = cnt;
+        if (cnt > a.jl_cap) atomicOr(a.status, SDM_DEV_LIST_OVERFLOW);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_jlist(SdmArgs a, const int* cl_prefix) {
+    const int lane = lane_id();
+    const int total = cl_prefix[a.nrep];
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(&a.work_counter[2], 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        const int r = rep_by_item(cl_prefix, a.nrep, item);
+        const int I = item - cl_prefix[r];
+        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) build_jlist<true>(a, r, I);
+        else build_jlist<false>(a, r, I);
+    }
+}
+
+// ------------------------------------------------------------------------- //
+// K6b: main pass                                                            //
+// ------------------------------------------------------------------------- //
+
+// One tile: every lane owns one j of the ring window [head, head+count) and
+// sweeps the 8 i-particles of the cluster (warp-uniform i).  LJ = false is the
+// ring of j with epsilon = 0: Lennard-Jones vanishes for every i, Coulomb only.
+template <int MODE, bool IMG, bool LJ>
+__device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
+                                          const Ring& rg, unsigned head, int count, ICluster& ic,
+                                          float& ef, long long& npair) {
+    const int lane = lane_id();
+    const unsigned idx = (head + lane) & (SDM_RING - 1);
+    const bool active = lane < count;
+    // inactive lanes use zeros, never stale ring contents
+    const float4 A = active ? rg.a[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 B = active ? rg.b[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned m = active ? __float_as_uint(B.z) : 0u;
+    const float xs = A.x, ys = A.y, zs = A.z, qj = A.w, hj = B.x, ej = B.y;
+    const float rc2 = S.rc2f, krf = S.krf, crf = S.crf, krf2 = -2.0f * S.krf;
+    float fjx = 0.f, fjy = 0.f, fjz = 0.f, e = 0.f;
+    int cnt = 0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        float dx = __fsub_rn(xs, ic.x[t]);
+        float dy = __fsub_rn(ys, ic.y[t]);
+        float dz = __fsub_rn(zs, ic.z[t]);
+        if (IMG) {
+            dx = img32(dx, S.Lf[0], S.invLf[0]);
+            dy = img32(dy, S.Lf[1], S.invLf[1]);
+            dz = img32(dz, S.Lf[2], S.invLf[2]);
+        }
+        const float r2 = r2_chain(dx, dy, dz);
+        const bool ok = (r2 < rc2) && ((m >> t) & 1u);
+        if (MODE == MODE_COUNT) {
+            cnt += ok ? 1 : 0;
+            continue;
+        }
+        const float r2s = ok ? r2 : 1.0f;
+        const float ir = fast_rsqrt(r2s);
+        const float ir2 = ir * ir;
+        const float qqm = ok ? ic.q[t] * qj : 0.0f;
+        float fs;
+        if (LJ) {
+            const float sg = ic.hs[t] + hj;
+            const float s2 = sg * sg * ir2;
+            const float s6 = s2 * s2 * s2;
+            const float epsm = ok ? ic.se[t] * ej : 0.0f;
+            const float t6 = epsm * s6;
+            e = fmaf(t6, s6 - 1.0f, e);
+            e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
+            fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qqm * fmaf(krf2, r2s, ir)) * ir2;
+        } else {
+            e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
+            fs = qqm * fmaf(krf2, r2s, ir) * ir2;
+        }
+        fjx = fmaf(fs, dx, fjx);
+        fjy = fmaf(fs, dy, fjy);
+        fjz = fmaf(fs, dz, fjz);
+        ic.fx[t] = fmaf(-fs, dx, ic.fx[t]);
+        ic.fy[t] = fmaf(-fs, dy, ic.fy[t]);
+        ic.fz[t] = fmaf(-fs, dz, ic.fz[t]);
+    }
+    if (MODE == MODE_COUNT) {
+        npair += cnt;
+    } else if (active) {
+        const int slot = __float_as_int(B.w);
+        const size_t gsl = (size_t)R.slot_win + slot;
+        red_fix(a.F0x + gsl, fjx, a.status);
+        red_fix(a.F0y + gsl, fjy, a.status);
+        red_fix(a.F0z + gsl, fjz, a.status);
+        ef += e;
+    }
+}
+
+// Computes the allowed-i mask of candidate slot j (cluster J) against
+// i-cluster I (valid-i bits vmask).
+__device__ __forceinline__ unsigned j_mask(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
+                                           int I, int J, int sj, unsigned vmask, bool needmask) {
+    unsigned m = vmask;
+    if (!needmask) return m;
+    const int t = sj & 7;
+    if (J == I) m &= (1u << t) - 1u;
+    const int4 ex = a.excl4[R.slot_win + sj];
+    const int i0 = 8 * I;
+    if (ex.x == -2) {
+        const int p = a.perm[R.slot_win + sj];
+        const int ta = S.atom_base + p;
+        for (int k = a.excl_off[ta]; k < a.excl_off[ta + 1]; ++k) {
+            const int s2 = a.inv[R.atom_win + a.excl_idx[k]];
+            if (s2 >= i0 && s2 < i0 + 8) m &= ~(1u << (s2 - i0));
+        }
+    } else {
+        const int e4[4] = {ex.x, ex.y, ex.z, ex.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (e4[k] >= i0 && e4[k] < i0 + 8) m &= ~(1u << (e4[k] - i0));
+    }
+    return m;
+}
+
+template <int MODE, bool IMG>
+__device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSmem& sm) {
+    const int lane = lane_id();
+    const SdmRep R = a.rep[r];
+    const SdmSys S = a.sys[R.sys];
+    const int cw = R.cl_win + I;
+    const int slot0 = R.slot_win + 8 * I;
+    // i-cluster particles, replicated in every lane
+    ICluster ic;
+    {
+        float4 xi4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 pi2 = make_float2(0.f, 0.f);
+        if (lane < 8) { xi4 = a.clX[slot0 + lane]; pi2 = a.clP[slot0 + lane]; }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            ic.x[t] = __shfl_sync(0xffffffffu, xi4.x, t);
+            ic.y[t] = __shfl_sync(0xffffffffu, xi4.y, t);
+            ic.z[t] = __shfl_sync(0xffffffffu, xi4.z, t);
+            ic.q[t] = __shfl_sync(0xffffffffu, xi4.w, t);
+            ic.hs[t] = __shfl_sync(0xffffffffu, pi2.x, t);
+            ic.se[t] = __shfl_sync(0xffffffffu, pi2.y, t);
+            ic.fx[t] = 0.f; ic.fy[t] = 0.f; ic.fz[t] = 0.f;
+        }
+    }
+    const unsigned vmask = __ballot_sync(0xffffffffu, lane < 8 && a.perm[slot0 + (lane & 7)] >= 0) & 0xffu;
+    const float4 bc = a.cl_bbc[cw];
+    const float4 bh = a.cl_bbh[cw];
+    const float rcl2 = S.rcl2f;
+    const int njl = min(a.jl_cnt[cw], a.jl_cap);
+    const int ebeg = (njl * part) / a.split, eend = (njl * (part + 1)) / a.split;
+    const int4* jl = a.jl + (size_t)cw * a.jl_cap;
+
+    unsigned hl = 0, tl = 0, hc = 0, tc = 0;  // ring counters (uniform)
+    float ef = 0.0f;
+    long long npair = 0;
+    int emit_n = 0;
+
+    // groups of 4 J clusters x 8 lanes; the next group's gathers are issued first
+    const int t = lane & 7;
+    int4 en_n = make_int4(0, 0, 0, 0);
+    float4 X_n = make_float4(SDM_INVALID_COORD, 0.f, 0.f, 0.f);
+    float2 P_n = make_float2(0.f, 0.f);
+    {
+        const int e = ebeg + (lane >> 3);
+        if (e < eend) {
+            en_n = jl[e];
+            const int sj = 8 * (en_n.x & 0x7fffffff) + t;
+            X_n = a.clX[R.slot_win + sj];
+            P_n = a.clP[R.slot_win + sj];
+        }
+    }
+    for (int g0 = ebeg; g0 < eend; g0 += 4) {
+        const int e = g0 + (lane >> 3);
+        const int4 en = en_n;
+        const float4 X4 = X_n;
+        const float2 P = P_n;
+        if (e + 4 < eend) {
+            en_n = jl[e + 4];
+            const int sj2 = 8 * (en_n.x & 0x7fffffff) + t;
+            X_n = a.clX[R.slot_win + sj2];
+            P_n = a.clP[R.slot_win + sj2];
+        }
+        bool pass = false;
+        float xs = 0.f, ys = 0.f, zs = 0.f;
+        int sj = 0;
+        unsigned m = 0;
+        if (e < eend) {
+            const int J = en.x & 0x7fffffff;
+            const bool nm = en.x < 0;
+            sj = 8 * J + t;
+            xs = __fadd_rn(X4.x, __int_as_float(en.y));
+            ys = __fadd_rn(X4.y, __int_as_float(en.z));
+            zs = __fadd_rn(X4.z, __int_as_float(en.w));
+            float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
+            if (IMG) {
+                tx = img32(tx, S.Lf[0], S.invLf[0]);
+                ty = img32(ty, S.Lf[1], S.invLf[1]);
+                tz = img32(tz, S.Lf[2], S.invLf[2]);
+            }
+            const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
+            const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
+            const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
+            // padding slots carry 1e6 coordinates; in image mode they could wrap
+            pass = (X4.x < 1.0e5f) && r2_chain(ex, ey, ez) < rcl2;
+            if (pass) {
+                m = j_mask(a, S, R, I, J, sj, vmask, nm);
+                pass = m != 0u;
+            }
+        }
+        if (MODE == MODE_EMIT) {
+            const unsigned bal = __ballot_sync(0xffffffffu, pass);
+            const int pos = __popc(bal & ((1u << lane) - 1u));
+            if (pass && emit_n + pos < a.ex_cap) {
+                const size_t o = (size_t)I * a.ex_cap + emit_n + pos;
+                a.ex_slot[o] = sj;
+                a.ex_mask[o] = (unsigned char)m;
+            }
+            emit_n += __popc(bal);
+            continue;
+        }
+        const bool lj = pass && P.y != 0.0f;
+        const bool co = pass && P.y == 0.0f;
+        const unsigned bl = __ballot_sync(0xffffffffu, lj);
+        const unsigned bco = __ballot_sync(0xffffffffu, co);
+        const unsigned lt = (1u << lane) - 1u;
+        if (lj) {
+            const unsigned idx = (tl + __popc(bl & lt)) & (SDM_RING - 1);
+            sm.lj.a[idx] = make_float4(xs, ys, zs, X4.w);
+            sm.lj.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
+        }
+        if (co) {
+            const unsigned idx = (tc + __popc(bco & lt)) & (SDM_RING - 1);
+            sm.co.a[idx] = make_float4(xs, ys, zs, X4.w);
+            sm.co.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
+        }
+        tl += __popc(bl);
+        tc += __popc(bco);
+        __syncwarp();
+        if (tl - hl >= 32u) {
+            eval_tile<MODE, IMG, true>(a, S, R, sm.lj, hl, 32, ic, ef, npair);
+            hl += 32u;
+        }
+        if (tc - hc >= 32u) {
+            eval_tile<MODE, IMG, false>(a, S, R, sm.co, hc, 32, ic, ef, npair);
+            hc += 32u;
         }
         __syncwarp();
     }
-    phase_b();
     if (MODE == MODE_EMIT) {
-        if (lane == 0) {
+        if (lane == 0 && part == 0) {
             a.ex_cnt[I] = emit_n;
             if (emit_n > a.ex_cap) atomicOr(a.status, 1 << 16);
         }
         return;
     }
-    if (tail != head) {
-        eval_tile<MODE, IMG>(a, S, R, sm, head, (int)(tail - head), ic, ef, npair);
-        head = tail;
-    }
+    if (tl != hl) eval_tile<MODE, IMG, true>(a, S, R, sm.lj, hl, (int)(tl - hl), ic, ef, npair);
+    if (tc != hc) eval_tile<MODE, IMG, false>(a, S, R, sm.co, hc, (int)(tc - hc), ic, ef, npair);
     if (MODE == MODE_COUNT) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) npair += __shfl_xor_sync(0xffffffffu, npair, o);
@@ -863,7 +884,7 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
     // reduce-scatter of the 24 i-force partial sums
     float v[24];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) { v[3 * t] = ic.fx[t]; v[3 * t + 1] = ic.fy[t]; v[3 * t + 2] = ic.fz[t]; }
+    for (int q = 0; q < 8; ++q) { v[3 * q] = ic.fx[q]; v[3 * q + 1] = ic.fy[q]; v[3 * q + 2] = ic.fz[q]; }
     {
         const bool up = lane & 16;
 #pragma unroll
@@ -897,12 +918,12 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
         v[k] += __shfl_xor_sync(0xffffffffu, v[k], 1);
     }
     if ((lane & 3) == 0) {
-        const int t = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
-        if ((vmask >> t) & 1u) {
-            const size_t gsl = (size_t)slot0 + t;
-            red_fixed(a.F0x + gsl, v[0], a.status);
-            red_fixed(a.F0y + gsl, v[1], a.status);
-            red_fixed(a.F0z + gsl, v[2], a.status);
+        const int ti = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+        if ((vmask >> ti) & 1u) {
+            const size_t gsl = (size_t)slot0 + ti;
+            red_fix(a.F0x + gsl, v[0], a.status);
+            red_fix(a.F0y + gsl, v[1], a.status);
+            red_fix(a.F0z + gsl, v[2], a.status);
         }
     }
     double ed = (double)ef;
@@ -911,11 +932,13 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, WarpSm
     if (lane == 0) a.e_part[(size_t)cw * a.split + part] = ed;
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(SDM_WARPS * 32, 3)
+// MINB: minimum resident CTAs per SM the register allocation is bounded for
+// (3: up to 168 registers; 4: up to 128)
+template <int MODE, int MINB>
+__global__ void __launch_bounds__(SDM_WARPS * 32, MINB)
 k_pair(SdmArgs a, const int* item_prefix) {
-    __shared__ WarpSmem smem[SDM_WARPS];
-    WarpSmem& sm = smem[threadIdx.x >> 5];
+    __shared__ EvalSmem smem[SDM_WARPS];
+    EvalSmem& sm = smem[threadIdx.x >> 5];
     const int lane = lane_id();
     const int total = item_prefix[a.nrep];
     for (;;) {
@@ -927,8 +950,7 @@ k_pair(SdmArgs a, const int* item_prefix) {
         const int local = item - item_prefix[r];
         const int I = local / a.split, part = local - I * a.split;
         if (MODE == MODE_EMIT && r != a.ex_rep) continue;
-        const SdmSys& S = a.sys[a.rep[r].sys];
-        if (replica_image_mode(a, S, r)) process_cluster<MODE, true>(a, r, I, part, sm);
+        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) process_cluster<MODE, true>(a, r, I, part, sm);
         else process_cluster<MODE, false>(a, r, I, part, sm);
     }
 }
@@ -991,9 +1013,9 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm
         const float f = sgn * fs;
         if (sj >= 0) {
             const size_t gsl = (size_t)R.slot_win + sj;
-            red_fixed(a.dFx + gsl, f * dx, a.status);
-            red_fixed(a.dFy + gsl, f * dy, a.status);
-            red_fixed(a.dFz + gsl, f * dz, a.status);
+            red_fix(a.dFx + gsl, f * dx, a.status);
+            red_fix(a.dFy + gsl, f * dy, a.status);
+            red_fix(a.dFz + gsl, f * dz, a.status);
         }
         fpx = fmaf(-f, dx, fpx);
         fpy = fmaf(-f, dy, fpy);
@@ -1158,9 +1180,9 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm
     }
     if (lane == 0) {
         const size_t gsl = (size_t)R.slot_win + a.inv[R.atom_win + p];
-        red_fixed(a.dFx + gsl, fpx, a.status);
-        red_fixed(a.dFy + gsl, fpy, a.status);
-        red_fixed(a.dFz + gsl, fpz, a.status);
+        red_fix(a.dFx + gsl, fpx, a.status);
+        red_fix(a.dFy + gsl, fpy, a.status);
+        red_fix(a.dFz + gsl, fpz, a.status);
         a.p_part[R.pert_win + local] = ed;
     }
 }
@@ -1345,14 +1367,14 @@ static int grid_for(long long n, int block) {
 
 extern "C++" {
 
-cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* done, cudaStream_t st,
+cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* cl_prefix, int* done, cudaStream_t st,
                             cudaEvent_t* ev, int nev, unsigned ev_flags) {
     int e = 0;
     auto mark = [&]() { if (ev && e < nev) cudaEventRecordWithFlags(ev[e++], st, ev_flags); };
     mark();
     k_cells<<<grid_for(a.total_atoms > a.total_slots ? a.total_atoms : a.total_slots, 256), 256, 0, st>>>(a);
     mark();
-    k_scan<<<a.nrep, 1024, 0, st>>>(a, item_prefix, done);
+    k_scan<<<a.nrep, 1024, 0, st>>>(a, item_prefix, cl_prefix, done);
     mark();
     k_bucket<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
     mark();
@@ -1363,12 +1385,22 @@ cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* done, cudaS
     return cudaGetLastError();
 }
 
+cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_t st) {
+    k_jlist<<<num_sms() * 8, 256, 0, st>>>(a, cl_prefix);
+    return cudaGetLastError();
+}
+
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
                             cudaStream_t st) {
     const int grid = num_sms() * ctas_per_sm;
-    if (mode == MODE_EVAL) k_pair<MODE_EVAL><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
-    else if (mode == MODE_COUNT) k_pair<MODE_COUNT><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
-    else k_pair<MODE_EMIT><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+    if (mode == MODE_EVAL) {
+        if (ctas_per_sm >= 4) k_pair<MODE_EVAL, 4><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+        else k_pair<MODE_EVAL, 3><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+    } else if (mode == MODE_COUNT) {
+        k_pair<MODE_COUNT, 3><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+    } else {
+        k_pair<MODE_EMIT, 3><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+    }
     return cudaGetLastError();
 }
 

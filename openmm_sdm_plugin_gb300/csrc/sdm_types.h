@@ -27,6 +27,7 @@
 //   per replica, column x z-cell (window = ncol*(M[2]+1))
 //     ztab     int     first cluster of the column whose reference z cell >= z
 //   per replica, cluster-indexed (window = slot_cap/8)
+//     jl       int4[jl_cap]  cluster-pair list of the i-cluster, jl_cnt entries
 //     cl_ref   int4    reference cell (cx, cy, cz) and column id
 //     cl_bbc   float4  bounding-box centre (cluster frame)
 //     cl_bbh   float4  bounding-box half extents
@@ -123,6 +124,9 @@ struct SdmArgs {
     float4* cl_bbh;
     int4* cl_link;
     int* ztab;           // per column: first cluster whose reference z cell >= z, z = 0..M[2]
+    int4* jl;            // cluster-pair lists: cl window * jl_cap entries (J|needmask<<31, Sx, Sy, Sz)
+    int* jl_cnt;         // entries per i-cluster (may exceed jl_cap: overflow)
+    int jl_cap;
     double* e_part;      // cl window * SDM_MAX_SPLIT
     double* p_part;      // perturbation partials
     int* ncl;            // clusters per replica
