@@ -43,6 +43,7 @@ struct SysHost {
     std::vector<int> D;         // displaced particles
     std::vector<int> cx_off;    // nD+1 (local)
     std::vector<int> cx_idx;
+    std::vector<int2> hst, fst;  // owner / full column stencils
     SdmSys dev;
     int replicas;
 };
@@ -227,6 +228,30 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
         else { g.stlo[k] = -((g.M[k] - 1) / 2); g.sthi[k] = g.M[k] / 2; }
         if (!(0.5 * d.box[k] - d.cutoff - g.g[k] > 1.0e-3)) g.img_static = 1;
     }
+    // owner stencil: the forward half when the stencil cannot wrap onto itself
+    int Kx = (int)std::floor((d.cutoff + 2.0e-4) / g.g[0]) + 1;
+    int Ky = (int)std::floor((d.cutoff + 2.0e-4) / g.g[1]) + 1;
+    g.half_geo = (2 * Kx + 1 <= g.M[0] && 2 * Ky + 1 <= g.M[1]) ? 1 : 0;
+    s.hst.clear();
+    s.fst.clear();
+    const double rcs = d.cutoff + 3.0e-4;
+    auto near = [&](int ox, int oy) {
+        // columns offset by (ox,oy) can hold particles closer than the cutoff
+        const double gx = std::max(std::abs(ox) - 1, 0) * g.g[0];
+        const double gy = std::max(std::abs(oy) - 1, 0) * g.g[1];
+        return gx * gx + gy * gy < rcs * rcs;
+    };
+    for (int ox = g.stlo[0]; ox <= g.sthi[0]; ++ox)
+        for (int oy = g.stlo[1]; oy <= g.sthi[1]; ++oy)
+            if (near(ox, oy)) s.fst.push_back({ox, oy});
+    if (g.half_geo) {
+        s.hst.push_back({0, 0});
+        for (int ox = 0; ox <= Kx; ++ox)
+            for (int oy = -Ky; oy <= Ky; ++oy)
+                if ((ox > 0 || oy > 0) && near(ox, oy)) s.hst.push_back({ox, oy});
+    } else {
+        s.hst = s.fst;
+    }
     const double e = d.reaction_field_dielectric, rc = d.cutoff;
     g.krf = (float)((e - 1.0) / ((2.0 * e + 1.0) * rc * rc * rc));
     g.crf = (float)(3.0 * e / ((2.0 * e + 1.0) * rc));
@@ -277,6 +302,7 @@ sdm_status upload_topology(sdm_handle* h) {
     std::vector<int> grp, eoff, eidx, D, cxo, cxi;
     std::vector<double> dd;
     std::vector<float> tab;
+    std::vector<int2> sten;
     std::vector<SdmSys> sd;
     int atom = 0, excl = 0, dbase = 0, cxbase = 0, tabbase = 0;
     for (auto& s : h->sys) {
@@ -301,6 +327,12 @@ sdm_status upload_topology(sdm_handle* h) {
         cxo.push_back(cx_total);
         for (int k = 0; k < 3; ++k)
             for (int m = -g.M[k]; m <= g.M[k]; ++m) tab.push_back((float)((double)m * g.g[k]));
+        g.hst_base = (int)sten.size();
+        g.hst_count = (int)s.hst.size();
+        sten.insert(sten.end(), s.hst.begin(), s.hst.end());
+        g.fst_base = (int)sten.size();
+        g.fst_count = (int)s.fst.size();
+        sten.insert(sten.end(), s.fst.begin(), s.fst.end());
         atom += s.n;
         excl += (int)s.excl_idx.size();
         dbase += (int)s.D.size();
@@ -331,6 +363,7 @@ sdm_status upload_topology(sdm_handle* h) {
     if ((st = put(a.cx_off, cxo.data(), cxo.size() * 4))) return st;
     if ((st = put(a.cx_idx, cxi.data(), cxi.size() * 4))) return st;
     if ((st = put(a.shift_tab, tab.data(), tab.size() * 4))) return st;
+    if ((st = put(a.stencil, sten.data(), sten.size() * sizeof(int2)))) return st;
     // perturbation windows depend on nD
     int pw = 0;
     for (auto& r : h->rep) { r.pert_win = pw; pw += 2 * h->sys[r.sys].dev.nD; }
@@ -496,7 +529,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     }
     // replica windows
     long long xo = 0;
-    int aw = 0, cw = 0, sw = 0, zw = 0;
+    int aw = 0, cw = 0, sw = 0;
     for (int s = 0; s < num_systems; ++s) {
         const SysHost& S = h->sys[s];
         for (int k = 0; k < S.replicas; ++k) {
@@ -509,9 +542,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
             r.slot_win = sw;
             r.slot_cap = round8((long long)S.n + 8LL * S.dev.ncol + 8);
             r.cl_win = sw / 8;
-            r.ztab_win = zw;
             h->rep.push_back(r);
-            zw += S.dev.ncol * (S.dev.M[2] + 1);
             xo += S.n;
             aw += S.n;
             cw += S.dev.ncol + 1;
@@ -550,6 +581,9 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_eoff = ar.take<int>(tot_n + 1), o_eidx = ar.take<int>(std::max(tot_excl, 1));
     const size_t o_D = ar.take<int>(std::max(tot_D, 1)), o_cxo = ar.take<int>(tot_cx + 1);
     const size_t o_cxi = ar.take<int>(tot_cxidx), o_tab = ar.take<float>(tot_tab);
+    int tot_st = 0;
+    for (auto& s : h->sys) tot_st += (int)(s.hst.size() + s.fst.size());
+    const size_t o_st2 = ar.take<int2>(std::max(tot_st, 1));
     const size_t o_par = ar.take<double>((size_t)nrep * SDM_NPARAMS);
     const size_t o_x = ar.take<double>(3 * xo), o_res = ar.take<double>((size_t)nrep * SDM_NRESULTS);
     const size_t o_f = ar.take<double>(3 * xo);
@@ -562,7 +596,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_F = ar.take<unsigned long long>(6 * Sl);
     const size_t o_ref = ar.take<int4>(Cl), o_bbc = ar.take<float4>(Cl), o_bbh = ar.take<float4>(Cl);
     const size_t o_lnk = ar.take<int4>(Cl), o_ep = ar.take<double>(Cl * SDM_MAX_SPLIT);
-    const size_t o_zt = ar.take<int>(std::max(zw, 1));
+    const size_t o_zb = ar.take<float2>(Cl);
     const size_t o_pp = ar.take<double>(std::max(Pp, 1LL));
     const size_t o_ncl = ar.take<int>(nrep), o_st = ar.take<int>(4);
     const size_t o_counts = ar.take<long long>(2 * nrep), o_ip = ar.take<int>(nrep + 1);
@@ -621,7 +655,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.cl_bbc = at<float4>(B, o_bbc);
     a.cl_bbh = at<float4>(B, o_bbh);
     a.cl_link = at<int4>(B, o_lnk);
-    a.ztab = at<int>(B, o_zt);
+    a.cl_zb = at<float2>(B, o_zb);
+    a.stencil = at<int2>(B, o_st2);
     a.e_part = at<double>(B, o_ep);
     a.p_part = at<double>(B, o_pp);
     a.ncl = at<int>(B, o_ncl);
@@ -721,19 +756,24 @@ sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double*
     if (forces)
         SDM_CUDA(h, cudaMemcpyAsync(forces, h->f_in, nx * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    // the status word is read after every host call; it is cleared here only
+    // when this call acts on it (list regrow, or verification on)
     int v = 0;
-    s = check_dev_status(h, &v, true);
+    s = check_dev_status(h, &v, false);
     if (s) return s;
     if (v & SDM_DEV_LIST_OVERFLOW) {
+        SDM_CUDA(h, cudaMemset(h->args.status, 0, sizeof(int)));
         // lists too small for these coordinates: regrow and evaluate again
         if (h->jl_cap >= (1 << 16)) return fail(h, SDM_ERR_CAPACITY, "cluster-pair list capacity limit reached");
         s = regrow_lists(h);
         if (s) return s;
         return sdm_evaluate(h, x, results, forces);
     }
-    if (h->opt_verify && v)
+    if (h->opt_verify && v) {
+        SDM_CUDA(h, cudaMemset(h->args.status, 0, sizeof(int)));
         return fail(h, SDM_ERR_OVERFLOW, "device status " + std::to_string(v) +
                                              ": force overflow or non-finite energy");
+    }
     return SDM_OK;
 }
 

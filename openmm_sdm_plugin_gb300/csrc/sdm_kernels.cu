@@ -276,16 +276,10 @@ __global__ void __launch_bounds__(128) k_colsort(SdmArgs a) {
         if (c >= S.ncol) continue;
         const int n = a.col_cnt[R.col_win + c];
         const int a0 = a.col_aoff[R.col_win + c];
-        const int cl0 = a.col_cl[R.col_win + c];
-        const int sbase = 8 * cl0;
+        const int sbase = 8 * a.col_cl[R.col_win + c];
         const int send = 8 * a.col_cl[R.col_win + c + 1];
         const int* bk = a.bucket + R.atom_win + a0;
-        if (n == 0) {
-            // empty column: every z entry of its cluster table points at its (empty) range
-            int* zt = a.ztab + R.ztab_win + c * (S.M[2] + 1);
-            for (int z = lane; z <= S.M[2]; z += 32) zt[z] = cl0;
-            continue;
-        }
+        if (n == 0) continue;
         for (int ib = 0; ib < n; ib += 32) {
             const int ii = ib + lane;
             int ai = -1;
@@ -407,8 +401,16 @@ __global__ void k_clusters(SdmArgs a) {
                 }
             }
         }
+        // absolute z of the first and last particle (rounded outwards, monotone
+        // along a column), for the z-range searches of the list builder
+        const double wz = (p >= 0) ? a.w[3 * (size_t)(R.atom_win + p) + 2] : 0.0;
+        const unsigned vm = (__ballot_sync(gmask, p >= 0) >> (lane & 24)) & 0xffu;
+        const int lastv = 31 - __clz(vm);
+        const double wz0 = __shfl_sync(gmask, wz, 0, 8);
+        const double wzl = __shfl_sync(gmask, wz, lastv, 8);
         if (t == 0) {
             const int cw = R.cl_win + C;
+            a.cl_zb[cw] = make_float2(__double2float_rd(wz0) - 1.0e-4f, __double2float_ru(wzl) + 1.0e-4f);
             a.cl_ref[cw] = make_int4(cx, cy, cz, ci0.x);
             a.cl_bbc[cw] = make_float4(__fmul_rn(0.5f, __fadd_rn(lo[0], hi[0])),
                                        __fmul_rn(0.5f, __fadd_rn(lo[1], hi[1])),
@@ -419,15 +421,6 @@ __global__ void k_clusters(SdmArgs a) {
             a.cl_link[cw] = many ? make_int4(-2, -2, -2, -2)
                                  : make_int4(link[0], link[1], link[2], link[3]);
             atomicMax(&a.extz[r], __float_as_uint(fmaxf(hi[2], 0.0f)));
-            // column z-table: entries (z of the previous cluster, z of C] -> C
-            const int cfirst = a.col_cl[R.col_win + ci0.x];
-            const int cend = a.col_cl[R.col_win + ci0.x + 1];
-            int zprev = -1;
-            if (C > cfirst) zprev = a.cellinfo[R.atom_win + a.perm[R.slot_win + 8 * (C - 1)]].y;
-            int* zt = a.ztab + R.ztab_win + ci0.x * (S.M[2] + 1);
-            for (int z = zprev + 1; z <= cz; ++z) zt[z] = C;
-            if (C == cend - 1)
-                for (int z = cz + 1; z <= S.M[2]; ++z) zt[z] = cend;
         }
     }
 }
@@ -450,10 +443,28 @@ struct Ring {                   // one tile ring: 64 prepared j entries
     float4 b[SDM_RING];         // (hs, se, mask bits, slot bits)
 };
 
+#define SDM_NST 3               // cp.async stages of candidate particle data
+
 struct EvalSmem {
     Ring lj;                    // j with epsilon != 0
     Ring co;                    // j with epsilon == 0 (Coulomb only)
+    int4 jc[32];                // current chunk of the cluster-pair list
+    float4 sx[SDM_NST][32];     // staged cluster-local coordinates + charge of candidates
+    float2 sp[SDM_NST][32];     // staged (sigma/2, 2 sqrt(eps)) of candidates
 };
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 struct ICluster {
     float x[8], y[8], z[8], q[8], hs[8], se[8];
@@ -475,46 +486,35 @@ __device__ __forceinline__ void red_fix(unsigned long long* p, float v, int* sta
     atomicAdd(p, fix64(v));
 }
 
-// Cluster ranges of one stencil column restricted to the z window of
-// reference-cell offsets [nlo, nhi] around zref; up to two ranges when the
-// window wraps.  Whole column if `whole`.
-__device__ __forceinline__ void column_ranges(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
-                                              int colid, bool whole, int nlo, int nhi, int zref,
-                                              int& jb1, int& c1, int& jb2, int& c2) {
-    const int* colcl = a.col_cl + R.col_win;
-    c2 = 0;
-    jb2 = 0;
-    if (whole) {
-        jb1 = colcl[colid];
-        c1 = colcl[colid + 1] - jb1;
-        return;
-    }
-    const int Mz = S.M[2];
-    const int* zt = a.ztab + R.ztab_win + colid * (Mz + 1);
-    const int len = nhi - nlo + 1;
-    const int za = pmod(zref + nlo, Mz);
-    jb1 = zt[za];
-    if (za + len <= Mz) {
-        c1 = zt[za + len] - jb1;
-    } else {
-        c1 = zt[Mz] - jb1;
-        jb2 = zt[0];
-        c2 = zt[za + len - Mz] - jb2;
-    }
-}
-
-__device__ __forceinline__ void clip_from(int lo, int& jb, int& c) {
-    if (jb < lo) {
-        c = max(0, jb + c - lo);
-        jb = lo;
-    }
-}
-
 // ------------------------------------------------------------------------- //
 // K6a: cluster-pair lists.  For i-cluster I: every cluster J >= I (slot     //
 // order) of the half stencil whose shifted bounding box comes within        //
 // rc + margin of I's box, as (J | needmask<<31, Sx, Sy, Sz).                //
 // ------------------------------------------------------------------------- //
+__device__ __forceinline__ int wrap_add(int c, int o, int M) {
+    c += o;
+    if (c < 0) c += M;
+    else if (c >= M) c -= M;
+    return c;
+}
+
+// first J in [lo, hi) of a column with zhi_J >= z (zhi non-decreasing)
+__device__ __forceinline__ int lower_zhi(const float2* zb, int lo, int hi, float z) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (zb[mid].y < z) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+// first J in [lo, hi) with zlo_J > z (zlo non-decreasing)
+__device__ __forceinline__ int upper_zlo(const float2* zb, int lo, int hi, float z) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (zb[mid].x <= z) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
 template <bool IMG>
 __device__ void build_jlist(const SdmArgs& a, int r, int I) {
     const int lane = lane_id();
@@ -529,25 +529,28 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
     const float* tabx = a.shift_tab + S.shift_base;
     const float* taby = tabx + 2 * S.M[0] + 1;
     const float* tabz = taby + 2 * S.M[1] + 1;
-    const int nyst = S.sthi[1] - S.stlo[1] + 1;
-    const int nst = (S.sthi[0] - S.stlo[0] + 1) * nyst;
-    const float extz = __uint_as_float(a.extz[r]);
-    const int nlo = (int)floorf((bc.z - bh.z - rclc - extz) / S.gf[2]) - 1;
-    const int nhi = (int)floorf((bc.z + bh.z + rclc) / S.gf[2]) + 1;
-    const bool wholez = IMG || (nhi - nlo + 1 >= S.M[2]);
+    const int* colcl = a.col_cl + R.col_win;
+    const float2* zb = a.cl_zb + R.cl_win;
+    // z window of I (absolute, conservative) and its pieces inside [0, Lz)
+    const float z0 = tabz[ref.z + S.M[2]] + bc.z;
+    const float ZA = z0 - bh.z - rclc - 1.0e-4f, ZB = z0 + bh.z + rclc + 1.0e-4f;
+    const float Lz = S.Lf[2];
+    const bool wholez = IMG || (ZB - ZA >= Lz);
+    float za1 = fmaxf(ZA, 0.0f), zb1 = fminf(ZB, Lz), za2 = 1.0f, zb2 = 0.0f;  // empty 2nd piece
+    if (ZA < 0.0f) { za2 = ZA + Lz; zb2 = Lz; }
+    else if (ZB > Lz) { za2 = 0.0f; zb2 = ZB - Lz; }
     int4* out = a.jl + (size_t)cw * a.jl_cap;
     int cnt = 0;
-    for (int k0 = 0; k0 < nst; k0 += 32) {
+    for (int k0 = 0; k0 < S.hst_count; k0 += 32) {
         const int k = k0 + lane;
         int jb1 = 0, c1 = 0, jb2 = 0, c2 = 0;
         float Sx = 0.f, Sy = 0.f;
-        if (k < nst) {
-            const int ox = S.stlo[0] + k / nyst;
-            const int oy = S.stlo[1] + k % nyst;
-            const int ccx = pmod(ref.x + ox, S.M[0]);
-            const int ccy = pmod(ref.y + oy, S.M[1]);
+        if (k < S.hst_count) {
+            const int2 off = a.stencil[S.hst_base + k];
+            const int ccx = wrap_add(ref.x, off.x, S.M[0]);
+            const int ccy = wrap_add(ref.y, off.y, S.M[1]);
             const int colid = ccx * S.M[1] + ccy;
-            bool ok = colid >= ref.w;
+            bool ok = S.half_geo ? true : (colid >= ref.w);
             Sx = tabx[wrap_cell(ccx - ref.x, S.M[0]) + S.M[0]];
             Sy = taby[wrap_cell(ccy - ref.y, S.M[1]) + S.M[1]];
             if (!IMG && ok) {
@@ -559,10 +562,24 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
                 ok = gx * gx + gy * gy < rclc2;
             }
             if (ok) {
-                column_ranges(a, S, R, colid, wholez, nlo, nhi, ref.z, jb1, c1, jb2, c2);
-                if (colid == ref.w) {  // own column: clusters J >= I only
-                    clip_from(I, jb1, c1);
-                    clip_from(I, jb2, c2);
+                int lo = colcl[colid];
+                const int hi = colcl[colid + 1];
+                if (colid == ref.w) lo = I;  // own column: clusters J >= I only
+                if (wholez) {
+                    jb1 = lo;
+                    c1 = hi - lo;
+                } else {
+                    jb1 = lower_zhi(zb, lo, hi, za1);
+                    c1 = upper_zlo(zb, jb1, hi, zb1) - jb1;
+                    if (za2 <= zb2) {
+                        jb2 = lower_zhi(zb, lo, hi, za2);
+                        c2 = upper_zlo(zb, jb2, hi, zb2) - jb2;
+                        // the two pieces are disjoint in z; clusters are counted once
+                        if (jb2 < jb1 + c1 && jb2 + c2 > jb1) {
+                            const int u0 = min(jb1, jb2), u1 = max(jb1 + c1, jb2 + c2);
+                            jb1 = u0; c1 = u1 - u0; c2 = 0;
+                        }
+                    }
                 }
                 c1 = max(c1, 0);
                 c2 = max(c2, 0);
@@ -622,14 +639,11 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
     }
 }
 
+// static schedule: warp w takes items w, w+W, w+2W, ...
 __global__ void __launch_bounds__(256) k_jlist(SdmArgs a, const int* cl_prefix) {
-    const int lane = lane_id();
     const int total = cl_prefix[a.nrep];
-    for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(&a.work_counter[2], 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= total) break;
+    const int W = gridDim.x * (blockDim.x >> 5);
+    for (int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < total; item += W) {
         const int r = rep_by_item(cl_prefix, a.nrep, item);
         const int I = item - cl_prefix[r];
         if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) build_jlist<true>(a, r, I);
@@ -774,97 +788,106 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
     float ef = 0.0f;
     long long npair = 0;
     int emit_n = 0;
+    const int t = lane & 7, q = lane >> 3;
 
-    // groups of 4 J clusters x 8 lanes; the next group's gathers are issued first
-    const int t = lane & 7;
-    int4 en_n = make_int4(0, 0, 0, 0);
-    float4 X_n = make_float4(SDM_INVALID_COORD, 0.f, 0.f, 0.f);
-    float2 P_n = make_float2(0.f, 0.f);
-    {
-        const int e = ebeg + (lane >> 3);
-        if (e < eend) {
-            en_n = jl[e];
-            const int sj = 8 * (en_n.x & 0x7fffffff) + t;
-            X_n = a.clX[R.slot_win + sj];
-            P_n = a.clP[R.slot_win + sj];
-        }
-    }
-    for (int g0 = ebeg; g0 < eend; g0 += 4) {
-        const int e = g0 + (lane >> 3);
-        const int4 en = en_n;
-        const float4 X4 = X_n;
-        const float2 P = P_n;
-        if (e + 4 < eend) {
-            en_n = jl[e + 4];
-            const int sj2 = 8 * (en_n.x & 0x7fffffff) + t;
-            X_n = a.clX[R.slot_win + sj2];
-            P_n = a.clP[R.slot_win + sj2];
-        }
-        bool pass = false;
-        float xs = 0.f, ys = 0.f, zs = 0.f;
-        int sj = 0;
-        unsigned m = 0;
-        if (e < eend) {
-            const int J = en.x & 0x7fffffff;
-            const bool nm = en.x < 0;
-            sj = 8 * J + t;
-            xs = __fadd_rn(X4.x, __int_as_float(en.y));
-            ys = __fadd_rn(X4.y, __int_as_float(en.z));
-            zs = __fadd_rn(X4.z, __int_as_float(en.w));
-            float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
-            if (IMG) {
-                tx = img32(tx, S.Lf[0], S.invLf[0]);
-                ty = img32(ty, S.Lf[1], S.invLf[1]);
-                tz = img32(tz, S.Lf[2], S.invLf[2]);
-            }
-            const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
-            const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
-            const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
-            // padding slots carry 1e6 coordinates; in image mode they could wrap
-            pass = (X4.x < 1.0e5f) && r2_chain(ex, ey, ez) < rcl2;
-            if (pass) {
-                m = j_mask(a, S, R, I, J, sj, vmask, nm);
-                pass = m != 0u;
-            }
-        }
-        if (MODE == MODE_EMIT) {
-            const unsigned bal = __ballot_sync(0xffffffffu, pass);
-            const int pos = __popc(bal & ((1u << lane) - 1u));
-            if (pass && emit_n + pos < a.ex_cap) {
-                const size_t o = (size_t)I * a.ex_cap + emit_n + pos;
-                a.ex_slot[o] = sj;
-                a.ex_mask[o] = (unsigned char)m;
-            }
-            emit_n += __popc(bal);
-            continue;
-        }
-        const bool lj = pass && P.y != 0.0f;
-        const bool co = pass && P.y == 0.0f;
-        const unsigned bl = __ballot_sync(0xffffffffu, lj);
-        const unsigned bco = __ballot_sync(0xffffffffu, co);
-        const unsigned lt = (1u << lane) - 1u;
-        if (lj) {
-            const unsigned idx = (tl + __popc(bl & lt)) & (SDM_RING - 1);
-            sm.lj.a[idx] = make_float4(xs, ys, zs, X4.w);
-            sm.lj.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
-        }
-        if (co) {
-            const unsigned idx = (tc + __popc(bco & lt)) & (SDM_RING - 1);
-            sm.co.a[idx] = make_float4(xs, ys, zs, X4.w);
-            sm.co.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
-        }
-        tl += __popc(bl);
-        tc += __popc(bco);
+    for (int c0 = ebeg; c0 < eend; c0 += 32) {
+        // chunk of up to 32 list entries: one coalesced load, kept in shared memory
+        const int nch = min(32, eend - c0);
         __syncwarp();
-        if (tl - hl >= 32u) {
-            eval_tile<MODE, IMG, true>(a, S, R, sm.lj, hl, 32, ic, ef, npair);
-            hl += 32u;
-        }
-        if (tc - hc >= 32u) {
-            eval_tile<MODE, IMG, false>(a, S, R, sm.co, hc, 32, ic, ef, npair);
-            hc += 32u;
-        }
+        sm.jc[lane] = (lane < nch) ? jl[c0 + lane] : make_int4(0, 0, 0, 0);
         __syncwarp();
+        const int ngr = (nch + 3) >> 2;
+        // lane (q, t) stages particle t of entry 4g+q of group g
+        auto issue = [&](int g) {
+            const int e = 4 * g + q;
+            if (e < nch) {
+                const int sj = 8 * (sm.jc[e].x & 0x7fffffff) + t;
+                cp_async16(&sm.sx[g % SDM_NST][lane], a.clX + R.slot_win + sj);
+                cp_async8(&sm.sp[g % SDM_NST][lane], a.clP + R.slot_win + sj);
+            }
+        };
+#pragma unroll
+        for (int g = 0; g < SDM_NST - 1; ++g) {
+            if (g < ngr) issue(g);
+            cp_async_commit();
+        }
+        for (int g = 0; g < ngr; ++g) {
+            if (g + SDM_NST - 1 < ngr) issue(g + SDM_NST - 1);
+            cp_async_commit();
+            cp_async_wait<SDM_NST - 1>();   // this lane's copies of group g have landed
+            const int e = 4 * g + q;
+            bool pass = false;
+            float xs = 0.f, ys = 0.f, zs = 0.f;
+            int sj = 0;
+            unsigned m = 0;
+            float4 X4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 P = make_float2(0.f, 0.f);
+            if (e < nch) {
+                const int4 en = sm.jc[e];
+                X4 = sm.sx[g % SDM_NST][lane];
+                P = sm.sp[g % SDM_NST][lane];
+                const int J = en.x & 0x7fffffff;
+                const bool nm = en.x < 0;
+                sj = 8 * J + t;
+                xs = __fadd_rn(X4.x, __int_as_float(en.y));
+                ys = __fadd_rn(X4.y, __int_as_float(en.z));
+                zs = __fadd_rn(X4.z, __int_as_float(en.w));
+                float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
+                if (IMG) {
+                    tx = img32(tx, S.Lf[0], S.invLf[0]);
+                    ty = img32(ty, S.Lf[1], S.invLf[1]);
+                    tz = img32(tz, S.Lf[2], S.invLf[2]);
+                }
+                const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
+                const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
+                const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
+                // padding slots carry 1e6 coordinates; in image mode they could wrap
+                pass = (X4.x < 1.0e5f) && r2_chain(ex, ey, ez) < rcl2;
+                if (pass) {
+                    m = j_mask(a, S, R, I, J, sj, vmask, nm);
+                    pass = m != 0u;
+                }
+            }
+            if (MODE == MODE_EMIT) {
+                const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                const int pos = __popc(bal & ((1u << lane) - 1u));
+                if (pass && emit_n + pos < a.ex_cap) {
+                    const size_t o = (size_t)I * a.ex_cap + emit_n + pos;
+                    a.ex_slot[o] = sj;
+                    a.ex_mask[o] = (unsigned char)m;
+                }
+                emit_n += __popc(bal);
+                continue;
+            }
+            const bool lj = pass && P.y != 0.0f;
+            const bool co = pass && P.y == 0.0f;
+            const unsigned bl = __ballot_sync(0xffffffffu, lj);
+            const unsigned bco = __ballot_sync(0xffffffffu, co);
+            const unsigned lt = (1u << lane) - 1u;
+            if (lj) {
+                const unsigned idx = (tl + __popc(bl & lt)) & (SDM_RING - 1);
+                sm.lj.a[idx] = make_float4(xs, ys, zs, X4.w);
+                sm.lj.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
+            }
+            if (co) {
+                const unsigned idx = (tc + __popc(bco & lt)) & (SDM_RING - 1);
+                sm.co.a[idx] = make_float4(xs, ys, zs, X4.w);
+                sm.co.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
+            }
+            tl += __popc(bl);
+            tc += __popc(bco);
+            __syncwarp();
+            if (tl - hl >= 32u) {
+                eval_tile<MODE, IMG, true>(a, S, R, sm.lj, hl, 32, ic, ef, npair);
+                hl += 32u;
+            }
+            if (tc - hc >= 32u) {
+                eval_tile<MODE, IMG, false>(a, S, R, sm.co, hc, 32, ic, ef, npair);
+                hc += 32u;
+            }
+            __syncwarp();
+        }
+        cp_async_wait<0>();
     }
     if (MODE == MODE_EMIT) {
         if (lane == 0 && part == 0) {
@@ -939,13 +962,10 @@ __global__ void __launch_bounds__(SDM_WARPS * 32, MINB)
 k_pair(SdmArgs a, const int* item_prefix) {
     __shared__ EvalSmem smem[SDM_WARPS];
     EvalSmem& sm = smem[threadIdx.x >> 5];
-    const int lane = lane_id();
     const int total = item_prefix[a.nrep];
-    for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(&a.work_counter[0], 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= total) break;
+    const int W = gridDim.x * SDM_WARPS;
+    // static schedule: warp w takes items w, w+W, ...
+    for (int item = blockIdx.x * SDM_WARPS + (threadIdx.x >> 5); item < total; item += W) {
         const int r = rep_by_item(item_prefix, a.nrep, item);
         const int local = item - item_prefix[r];
         const int I = local / a.split, part = local - I * a.split;
@@ -998,8 +1018,7 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm
     const float* tabx = a.shift_tab + S.shift_base;
     const float* taby = tabx + 2 * S.M[0] + 1;
     const float* tabz = taby + 2 * S.M[1] + 1;
-    const int nyst = S.sthi[1] - S.stlo[1] + 1;
-    const int nst = (S.sthi[0] - S.stlo[0] + 1) * nyst;
+    const int nst = S.fst_count;
     const int* colcl = a.col_cl + R.col_win;
     double ed = 0.0;
     float fpx = 0.f, fpy = 0.f, fpz = 0.f;
@@ -1061,10 +1080,9 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm
         int cntJ = 0, Jb = 0;
         float Sx = 0.f, Sy = 0.f;
         if (k < nst) {
-            const int ox = S.stlo[0] + k / nyst;
-            const int oy = S.stlo[1] + k % nyst;
-            const int ccx = pmod(cy[0] + ox, S.M[0]);
-            const int ccy = pmod(cy[1] + oy, S.M[1]);
+            const int2 off = a.stencil[S.fst_base + k];
+            const int ccx = wrap_add(cy[0], off.x, S.M[0]);
+            const int ccy = wrap_add(cy[1], off.y, S.M[1]);
             const int colid = ccx * S.M[1] + ccy;
             Sx = tabx[wrap_cell(ccx - cy[0], S.M[0]) + S.M[0]];
             Sy = taby[wrap_cell(ccy - cy[1], S.M[1]) + S.M[1]];

@@ -24,14 +24,13 @@
 //     grp      int     displacement group of the slot's particle
 //     excl4    int4    up to 4 exclusion partners as slots (-1 none, -2 overflow)
 //     F0x/F0y/F0z, dFx/dFy/dFz   int64 fixed point 2^32
-//   per replica, column x z-cell (window = ncol*(M[2]+1))
-//     ztab     int     first cluster of the column whose reference z cell >= z
 //   per replica, cluster-indexed (window = slot_cap/8)
 //     jl       int4[jl_cap]  cluster-pair list of the i-cluster, jl_cnt entries
 //     cl_ref   int4    reference cell (cx, cy, cz) and column id
 //     cl_bbc   float4  bounding-box centre (cluster frame)
 //     cl_bbh   float4  bounding-box half extents
 //     cl_link  int4    clusters holding exclusion partners of this cluster (-1 none, -2 many)
+//     cl_zb    float2  absolute z of the first / last particle (outward rounded)
 //     e_part   double  main-pass energy of the cluster's work items
 #pragma once
 #include <stdint.h>
@@ -60,6 +59,10 @@ struct SdmSys {
     int D_base;       // offset into D_idx
     int shift_base;   // offset into shift_tab: 3 tables of 2*Mk+1 floats (index n+Mk)
     int cx_base;      // offset into cx_off/cx_idx (changed-pair exclusions per displaced particle)
+    int half_geo;     // 1: pairs of columns are owned through the forward half stencil
+                      // (offset ox>0, or ox==0 and oy>0; own column J>=I); 0: by lower column id
+    int hst_base, hst_count;  // owner stencil (int2 column offsets), own column first
+    int fst_base, fst_count;  // full stencil for point queries
 };
 
 struct SdmRep {
@@ -72,7 +75,6 @@ struct SdmRep {
     int slot_cap;     // slots in the window
     int cl_win;       // cluster window base (slot_win/8)
     int pert_win;     // perturbation partial base (2*nD per replica)
-    int ztab_win;     // column z-table base (ncol*(M[2]+1) per replica)
 };
 
 // Everything a kernel needs, passed by value (fits the 32 KB parameter space).
@@ -123,7 +125,8 @@ struct SdmArgs {
     float4* cl_bbc;
     float4* cl_bbh;
     int4* cl_link;
-    int* ztab;           // per column: first cluster whose reference z cell >= z, z = 0..M[2]
+    float2* cl_zb;       // per cluster: absolute z of its first and last particle (-/+ 1e-4 nm)
+    const int2* stencil; // column offset tables (see SdmSys hst/fst)
     int4* jl;            // cluster-pair lists: cl window * jl_cap entries (J|needmask<<31, Sx, Sy, Sz)
     int* jl_cnt;         // entries per i-cluster (may exceed jl_cap: overflow)
     int jl_cap;

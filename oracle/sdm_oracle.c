@@ -536,6 +536,33 @@ static int wrap_cell(int n, int M) {
     return n;
 }
 
+/* Pair ownership of the CUDA main pass (which cluster's list holds a pair).
+ * When the column stencil cannot wrap onto itself (2K+1 <= M in x and y,
+ * K = floor((rc+2e-4)/g)+1) a pair of different columns belongs to the
+ * cluster from whose column the other lies at a forward offset
+ * (ox > 0, or ox == 0 and oy > 0); otherwise to the lower column id.  In one
+ * column the lower cluster owns; in one cluster the lower slot is i. */
+static int half_geo(const double* box, const int* M, double rc) {
+    for (int k = 0; k < 2; ++k) {
+        double g = box[k] / (double)M[k];
+        int K = (int)floor((rc + 2.0e-4) / g) + 1;
+        if (2 * K + 1 > M[k]) return 0;
+    }
+    return 1;
+}
+
+static int wrap_cell(int n, int M);
+
+static int owns(const int* ref, int A, int B, const int* M, int geo) {
+    int colA = ref[3 * A] * M[1] + ref[3 * A + 1];
+    int colB = ref[3 * B] * M[1] + ref[3 * B + 1];
+    if (colA == colB) return A <= B;
+    if (!geo) return colA < colB;
+    int ox = wrap_cell(ref[3 * B] - ref[3 * A], M[0]);
+    int oy = wrap_cell(ref[3 * B + 1] - ref[3 * A + 1], M[1]);
+    return ox > 0 || (ox == 0 && oy > 0);
+}
+
 typedef struct {
     float Lf[3], invLf[3], g[3];
     double gd[3];
@@ -630,6 +657,7 @@ int orc_sdm_f32rule(int n, const double* q, const double* sig, const double* eps
     int ns = orc_build_clusters(n, x, box, M, cap, perm, &ncl, ref, X, colcl);
     if (ns < 0) { free(perm); free(ref); free(X); free(colcl); return -1; }
     int img = orc_image_mode(box, M, rc, ncl, perm, X);
+    int geo = half_geo(box, M, rc);
     f32rule R;
     f32rule_init(&R, box, M, rc, img);
     int* slot_of = (int*)malloc(sizeof(int) * (size_t)n);
@@ -669,7 +697,11 @@ int orc_sdm_f32rule(int n, const double* q, const double* sig, const double* eps
                     for (int j = jstart; ilist_b ? (j < n) : (j >= 0); j = ilist_b ? j + 1 : c.next[j]) {
                         if (j == i) continue;
                         int si = slot_of[i], sj = slot_of[j];
-                        if (si > sj) continue; /* ordered by slot: lower slot is "i" */
+                        if (si / 8 == sj / 8) {
+                            if (si > sj) continue; /* one cluster: lower slot is "i" */
+                        } else if (!owns(ref, si / 8, sj / 8, M, geo)) {
+                            continue;
+                        }
                         if (is_excluded(&s, i, j)) continue;
                         float r2f = r2_main32(&R, ref, X, si / 8, si, sj / 8, sj);
                         if (!(r2f < R.rc2f)) continue;
@@ -754,6 +786,7 @@ long long orc_emit_lists(int n, const int* excl_off, const int* excl_idx, const 
     int ns = orc_build_clusters(n, x, box, M, cap, perm, &ncl, ref, X, colcl);
     if (ns < 0) { free(ref); free(X); free(colcl); return -1; }
     int img = orc_image_mode(box, M, rc, ncl, perm, X);
+    int geo = half_geo(box, M, rc);
     f32rule R;
     f32rule_init(&R, box, M, rc, img);
     int* slot_of = (int*)malloc(sizeof(int) * (size_t)n);
@@ -775,10 +808,11 @@ long long orc_emit_lists(int n, const int* excl_off, const int* excl_idx, const 
         float c[3], h[3];
         for (int k = 0; k < 3; ++k) { c[k] = 0.5f * (lo[k] + hi[k]); h[k] = 0.5f * (hi[k] - lo[k]); }
         int k_out = 0;
-        for (int sj = 8 * I; sj < 8 * ncl; ++sj) {
+        for (int sj = 0; sj < 8 * ncl; ++sj) {
             int b = perm[sj];
             if (b < 0) continue;
             int J = sj / 8;
+            if (J != I && !owns(ref, I, J, M, geo)) continue;
             float e[3];
             for (int k = 0; k < 3; ++k) {
                 int nn = wrap_cell(ref[3 * J + k] - ref[3 * I + k], M[k]);
