@@ -228,6 +228,12 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
         else { g.stlo[k] = -((g.M[k] - 1) / 2); g.sthi[k] = g.M[k] / 2; }
         if (!(0.5 * d.box[k] - d.cutoff - g.g[k] > 1.0e-3)) g.img_static = 1;
     }
+    // z: the cell edge is a static lower bound of the cluster extent
+    const double tzd = 0.5 * d.box[2] - d.cutoff - 1.0e-3;
+    if (!(g.g[2] < tzd)) g.img_static = 1;
+    float tzf = (float)tzd;
+    if ((double)tzf > tzd) tzf = std::nextafter(tzf, -1.0f);
+    g.tz = tzf;
     // owner stencil: the forward half when the stencil cannot wrap onto itself
     int Kx = (int)std::floor((d.cutoff + 2.0e-4) / g.g[0]) + 1;
     int Ky = (int)std::floor((d.cutoff + 2.0e-4) / g.g[1]) + 1;
@@ -894,7 +900,7 @@ sdm_status sdm_autotune(sdm_handle* h, const double* x_device, int* split, int* 
     float best = 1e30f;
     int bs = osplit, bc = octas;
     const int splits[] = {1, 2, 4};
-    const int ctas[] = {2, 3, 4, 6};
+    const int ctas[] = {3, 4, 5, 6};
     for (int sp : splits)
         for (int c : ctas) {
             h->opt_split = sp;

@@ -425,10 +425,11 @@ __global__ void k_clusters(SdmArgs a) {
     }
 }
 
+// per-pair minimum image is needed unless the largest cluster z extent stays
+// below the host threshold tz = 0.5*Lz - rc - 1e-3 (rounded down to float)
 __device__ __forceinline__ bool replica_image_mode(const SdmArgs& a, const SdmSys& S, int r) {
     if (S.img_static) return true;
-    const double ez = fmax(S.g[2], (double)__uint_as_float(a.extz[r]));
-    return !(0.5 * S.box[2] - S.rc - ez > 1.0e-3);
+    return !(__uint_as_float(a.extz[r]) < S.tz);
 }
 
 enum { MODE_EVAL = 0, MODE_COUNT = 1, MODE_EMIT = 2 };
@@ -451,6 +452,7 @@ struct EvalSmem {
     int4 jc[32];                // current chunk of the cluster-pair list
     float4 sx[SDM_NST][32];     // staged cluster-local coordinates + charge of candidates
     float2 sp[SDM_NST][32];     // staged (sigma/2, 2 sqrt(eps)) of candidates
+    float4 ip[8];               // i-cluster (q, sigma/2, 2 sqrt(eps), 0), read as broadcasts
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -467,7 +469,7 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 struct ICluster {
-    float x[8], y[8], z[8], q[8], hs[8], se[8];
+    float x[8], y[8], z[8];
     float fx[8], fy[8], fz[8];
 };
 
@@ -660,8 +662,8 @@ __global__ void __launch_bounds__(256) k_jlist(SdmArgs a, const int* cl_prefix) 
 // ring of j with epsilon = 0: Lennard-Jones vanishes for every i, Coulomb only.
 template <int MODE, bool IMG, bool LJ>
 __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
-                                          const Ring& rg, unsigned head, int count, ICluster& ic,
-                                          float& ef, long long& npair) {
+                                          const Ring& rg, const float4* ip, unsigned head, int count,
+                                          ICluster& ic, float& ef, long long& npair) {
     const int lane = lane_id();
     const unsigned idx = (head + lane) & (SDM_RING - 1);
     const bool active = lane < count;
@@ -692,13 +694,14 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
         const float r2s = ok ? r2 : 1.0f;
         const float ir = fast_rsqrt(r2s);
         const float ir2 = ir * ir;
-        const float qqm = ok ? ic.q[t] * qj : 0.0f;
+        const float4 pi = ip[t];   // same address in every lane: one broadcast
+        const float qqm = ok ? pi.x * qj : 0.0f;
         float fs;
         if (LJ) {
-            const float sg = ic.hs[t] + hj;
+            const float sg = pi.y + hj;
             const float s2 = sg * sg * ir2;
             const float s6 = s2 * s2 * s2;
-            const float epsm = ok ? ic.se[t] * ej : 0.0f;
+            const float epsm = ok ? pi.z * ej : 0.0f;
             const float t6 = epsm * s6;
             e = fmaf(t6, s6 - 1.0f, e);
             e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
@@ -719,9 +722,10 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
     } else if (active) {
         const int slot = __float_as_int(B.w);
         const size_t gsl = (size_t)R.slot_win + slot;
-        red_fix(a.F0x + gsl, fjx, a.status);
-        red_fix(a.F0y + gsl, fjy, a.status);
-        red_fix(a.F0z + gsl, fjz, a.status);
+        if (!(fmaxf(fabsf(fjx), fmaxf(fabsf(fjy), fabsf(fjz))) < 1.0e9f)) atomicOr(a.status, SDM_DEV_FORCE_OVERFLOW);
+        atomicAdd(a.F0x + gsl, fix64(fjx));
+        atomicAdd(a.F0y + gsl, fix64(fjy));
+        atomicAdd(a.F0z + gsl, fix64(fjz));
         ef += e;
     }
 }
@@ -765,16 +769,16 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         float4 xi4 = make_float4(0.f, 0.f, 0.f, 0.f);
         float2 pi2 = make_float2(0.f, 0.f);
         if (lane < 8) { xi4 = a.clX[slot0 + lane]; pi2 = a.clP[slot0 + lane]; }
+        __syncwarp();
+        if (lane < 8) sm.ip[lane] = make_float4(xi4.w, pi2.x, pi2.y, 0.0f);
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
             ic.x[t] = __shfl_sync(0xffffffffu, xi4.x, t);
             ic.y[t] = __shfl_sync(0xffffffffu, xi4.y, t);
             ic.z[t] = __shfl_sync(0xffffffffu, xi4.z, t);
-            ic.q[t] = __shfl_sync(0xffffffffu, xi4.w, t);
-            ic.hs[t] = __shfl_sync(0xffffffffu, pi2.x, t);
-            ic.se[t] = __shfl_sync(0xffffffffu, pi2.y, t);
             ic.fx[t] = 0.f; ic.fy[t] = 0.f; ic.fz[t] = 0.f;
         }
+        __syncwarp();
     }
     const unsigned vmask = __ballot_sync(0xffffffffu, lane < 8 && a.perm[slot0 + (lane & 7)] >= 0) & 0xffu;
     const float4 bc = a.cl_bbc[cw];
@@ -841,8 +845,10 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
                 const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
                 const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
                 const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
-                // padding slots carry 1e6 coordinates; in image mode they could wrap
-                pass = (X4.x < 1.0e5f) && r2_chain(ex, ey, ez) < rcl2;
+                // padding slots carry 1e6 coordinates: they fail the box test
+                // unless image mode wraps them back, hence the explicit test there
+                pass = r2_chain(ex, ey, ez) < rcl2;
+                if (IMG) pass = pass && (X4.x < 1.0e5f);
                 if (pass) {
                     m = j_mask(a, S, R, I, J, sj, vmask, nm);
                     pass = m != 0u;
@@ -878,11 +884,11 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
             tc += __popc(bco);
             __syncwarp();
             if (tl - hl >= 32u) {
-                eval_tile<MODE, IMG, true>(a, S, R, sm.lj, hl, 32, ic, ef, npair);
+                eval_tile<MODE, IMG, true>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
                 hl += 32u;
             }
             if (tc - hc >= 32u) {
-                eval_tile<MODE, IMG, false>(a, S, R, sm.co, hc, 32, ic, ef, npair);
+                eval_tile<MODE, IMG, false>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
                 hc += 32u;
             }
             __syncwarp();
@@ -896,8 +902,8 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         }
         return;
     }
-    if (tl != hl) eval_tile<MODE, IMG, true>(a, S, R, sm.lj, hl, (int)(tl - hl), ic, ef, npair);
-    if (tc != hc) eval_tile<MODE, IMG, false>(a, S, R, sm.co, hc, (int)(tc - hc), ic, ef, npair);
+    if (tl != hl) eval_tile<MODE, IMG, true>(a, S, R, sm.lj, sm.ip, hl, (int)(tl - hl), ic, ef, npair);
+    if (tc != hc) eval_tile<MODE, IMG, false>(a, S, R, sm.co, sm.ip, hc, (int)(tc - hc), ic, ef, npair);
     if (MODE == MODE_COUNT) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) npair += __shfl_xor_sync(0xffffffffu, npair, o);
@@ -956,7 +962,7 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
 }
 
 // MINB: minimum resident CTAs per SM the register allocation is bounded for
-// (3: up to 168 registers; 4: up to 128)
+// (3: up to 168 registers; 4: up to 128; 5: up to 102)
 template <int MODE, int MINB>
 __global__ void __launch_bounds__(SDM_WARPS * 32, MINB)
 k_pair(SdmArgs a, const int* item_prefix) {
@@ -1412,7 +1418,8 @@ cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, 
                             cudaStream_t st) {
     const int grid = num_sms() * ctas_per_sm;
     if (mode == MODE_EVAL) {
-        if (ctas_per_sm >= 4) k_pair<MODE_EVAL, 4><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+        if (ctas_per_sm >= 5) k_pair<MODE_EVAL, 5><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+        else if (ctas_per_sm == 4) k_pair<MODE_EVAL, 4><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
         else k_pair<MODE_EVAL, 3><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
     } else if (mode == MODE_COUNT) {
         k_pair<MODE_COUNT, 3><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);

@@ -48,6 +48,7 @@ struct SdmSys {
     int ncol;         // M[0]*M[1]
     int stlo[2], sthi[2];  // stencil column offsets per axis (x,y)
     int img_static;   // 1 if the x/y extents already force per-pair minimum image
+    float tz;         // z threshold: image mode unless max cluster z extent < tz
     double box[3], invL[3], g[3], invg[3];
     double rc;
     float Lf[3], invLf[3];

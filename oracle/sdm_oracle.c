@@ -520,14 +520,18 @@ int orc_build_clusters(int n, const double* x, const double* box, const int* M, 
  * cluster pair gives the minimum image for every interacting pair. */
 int orc_image_mode(const double* box, const int* M, double rc, int ncl, const int* perm,
                    const float* X) {
+    /* x, y: the cell edge bounds the in-column extent; z: the cell edge, then the
+     * largest cluster extent against a float threshold rounded down */
+    for (int k = 0; k < 2; ++k)
+        if (!(0.5 * box[k] - rc - box[k] / M[k] > 1.0e-3)) return 1;
+    double tzd = 0.5 * box[2] - rc - 1.0e-3;
+    if (!(box[2] / M[2] < tzd)) return 1;
+    float tzf = (float)tzd;
+    if ((double)tzf > tzd) tzf = nextafterf(tzf, -1.0f);
     float ext = 0.0f;
     for (int s = 0; s < 8 * ncl; ++s)
         if (perm[s] >= 0 && X[4 * s + 2] > ext) ext = X[4 * s + 2];
-    double gz = box[2] / M[2];
-    double e[3] = {box[0] / M[0], box[1] / M[1], gz > (double)ext ? gz : (double)ext};
-    for (int k = 0; k < 3; ++k)
-        if (!(0.5 * box[k] - rc - e[k] > 1.0e-3)) return 1;
-    return 0;
+    return !(ext < tzf);
 }
 
 static int wrap_cell(int n, int M) {
