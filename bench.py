@@ -174,6 +174,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--ctas", type=int, default=0, help="pair-kernel CTAs per SM (0 = library default)")
+    ap.add_argument("--split", type=int, default=0, help="work items per i-cluster (0 = default)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -217,6 +219,11 @@ def main():
     xd = torch.from_numpy(xh).to(dev)
     rd = torch.zeros((NREP, capi.NRESULTS), dtype=torch.float64, device=dev)
     fd = torch.zeros_like(xd)
+    for hh in (h,):
+        if args.ctas:
+            hh.set_option(capi.OPT_CTAS_PER_SM, args.ctas)
+        if args.split:
+            hh.set_option(capi.OPT_SPLIT, args.split)
     tuned = None
     if args.autotune:
         tuned = h.autotune(xd.data_ptr())
@@ -230,6 +237,10 @@ def main():
     s1 = sysm.replica(0)
     h1 = capi.Handle([s1], device=local)
     h1.set_params(0, s1.params[0].as_array())
+    if args.ctas:
+        h1.set_option(capi.OPT_CTAS_PER_SM, args.ctas)
+    if args.split:
+        h1.set_option(capi.OPT_SPLIT, args.split)
     x1 = xd[:n].contiguous()
     r1 = torch.zeros((1, capi.NRESULTS), dtype=torch.float64, device=dev)
     f1 = torch.zeros_like(x1)

@@ -102,7 +102,7 @@ struct sdm_handle {
     std::vector<double> params;
     bool params_dirty = true;
     // options
-    int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 3, opt_verify = 1;
+    int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 4, opt_verify = 1;
     // graphs
     std::map<GraphKey, cudaGraphExec_t> graphs;
     // profiling
