@@ -139,7 +139,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
 sdm_status sdm_destroy(sdm_handle* h);
 
 /* Message of the last failing call on this handle ("" if none).  With a NULL
- * handle: the message of the last failing sdm_create on this thread. */
+ * handle: the message of the last failing sdm_create or sdm_evaluate_noalloc
+ * on this thread. */
 const char* sdm_last_error(const sdm_handle* h);
 
 /* Number of replicas over all systems. */
@@ -218,6 +219,49 @@ sdm_status sdm_get_grid(const sdm_handle* h, int system, int* M);
 sdm_status sdm_export_lists(sdm_handle* h, int replica, const double* x, int cap_slots,
                             int cap_clusters, int cap_per_cluster, int* perm, int* ncl, int* cnt,
                             int* ent_slot, unsigned char* ent_mask);
+
+/* Allocation-free evaluation of ONE system (one coordinate set).  There is
+ * no counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory at the point where they
+ * need a force: code recording into a CUDA graph (cudaMalloc is not allowed
+ * while a stream is being captured), hosts whose memory manager owns every
+ * device byte (a simulation engine's context, a framework's caching
+ * allocator: an allocation behind their back breaks their accounting or
+ * fails under a fixed budget), and latency-bound loops that cannot afford
+ * the implicit device synchronisation of cudaMalloc/cudaFree.  This call
+ * allocates nothing, on the device or on the host, and creates no handle.
+ *
+ * All scratch lives in one file-scope device array of
+ * SDM_NOALLOC_SCRATCH_BYTES bytes that every GPU loading the library holds
+ * until the process exits.  The first call on a device, with that device
+ * current, looks up the array's device address once; make that first call
+ * before any stream capture.  Every call shares the array: calls whose work
+ * overlaps on the GPU (other streams, other host threads) race and corrupt
+ * each other's results; serialise them.  Each call clears what must start at
+ * zero itself.
+ *
+ * Limits: 1 <= num_particles <= SDM_NOALLOC_MAX_PARTICLES (else
+ * SDM_ERR_INVALID_ARGUMENT, nothing launched); 0 < cutoff < box/2.  The
+ * pair work is all-pairs (N^2), with the handle path's pair terms, 2^32
+ * fixed-point forces and FP64 energies; the pair rule is the FP64 minimum
+ * image rounded to FP32, so pairs within ~1e-7 nm of the cutoff may differ
+ * from the handle path.
+ *
+ * Device pointers: x [3n], charge/sigma/epsilon [n], excl_offsets [n+1] and
+ * excl_indices (symmetric CSR of excluded partners), displacement [3n] or
+ * NULL, results [SDM_NRESULTS], forces [3n] or NULL (mixed force F).
+ * Host pointers: box [3], params [SDM_NPARAMS].  Asynchronous on `stream`
+ * (NULL = the legacy default stream); errors in the arguments are reported
+ * through sdm_last_error(NULL). */
+#define SDM_NOALLOC_MAX_PARTICLES 8192
+#define SDM_NOALLOC_SCRATCH_BYTES 727296
+sdm_status sdm_evaluate_noalloc(int num_particles, const double* x, const double* charge,
+                                const double* sigma, const double* epsilon,
+                                const int* excl_offsets, const int* excl_indices,
+                                const double* displacement, const double* box, double cutoff,
+                                double reaction_field_dielectric, const double* params,
+                                double* results, double* forces, void* stream);
 
 /* Device status bits (sdm_check_status, SDM_R_STATUS). */
 enum {

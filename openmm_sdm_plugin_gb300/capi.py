@@ -38,7 +38,10 @@ EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_set_displacement", "sdm_set_params", "sdm_evaluate", "sdm_evaluate_device",
             "sdm_get_state_forces", "sdm_check_status", "sdm_set_option", "sdm_get_option",
             "sdm_get_kernel_times", "sdm_autotune", "sdm_count_pairs", "sdm_get_grid",
-            "sdm_export_lists")
+            "sdm_export_lists", "sdm_evaluate_noalloc")
+
+NOALLOC_MAX_PARTICLES = 8192
+NOALLOC_SCRATCH_BYTES = 727296
 
 
 class SdmError(RuntimeError):
@@ -95,6 +98,8 @@ def load_library(path: str = LIB_PATH):
         L.sdm_count_pairs.argtypes = [vp, vp, vp]
         L.sdm_get_grid.argtypes = [vp, C.c_int, ip]
         L.sdm_export_lists.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, ip, vp, vp, vp]
+        L.sdm_evaluate_noalloc.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, C.c_double,
+                                           C.c_double, vp, vp, vp, vp]
         for name in EXPORTED:
             if name != "sdm_last_error":
                 getattr(L, name).restype = C.c_int
@@ -255,3 +260,20 @@ class Handle:
         k = ncl.value
         return dict(ncl=k, perm=perm[:8 * k], cnt=cnt[:k], slot=es.reshape(capcl, -1)[:k],
                     mask=em.reshape(capcl, -1)[:k])
+
+
+def evaluate_noalloc(n, x_ptr, q_ptr, sig_ptr, eps_ptr, eoff_ptr, eidx_ptr, d_ptr, box, cutoff,
+                     eps_rf, params, res_ptr, f_ptr=0, stream=0):
+    """Allocation-free evaluation of one system (device pointers, see
+    sdm_evaluate_noalloc in include/sdm_capi.h)."""
+    L = load_library()
+    b = np.ascontiguousarray(np.asarray(box, np.float64).reshape(3))
+    p = np.ascontiguousarray(np.asarray(params, np.float64).reshape(-1))
+    st = L.sdm_evaluate_noalloc(int(n), C.c_void_p(x_ptr), C.c_void_p(q_ptr), C.c_void_p(sig_ptr),
+                                C.c_void_p(eps_ptr), C.c_void_p(eoff_ptr), C.c_void_p(eidx_ptr),
+                                C.c_void_p(d_ptr) if d_ptr else None, b.ctypes.data,
+                                float(cutoff), float(eps_rf), p.ctypes.data, C.c_void_p(res_ptr),
+                                C.c_void_p(f_ptr) if f_ptr else None,
+                                C.c_void_p(stream) if stream else None)
+    if st != SDM_OK:
+        raise SdmError(st, L.sdm_last_error(None).decode())

@@ -473,6 +473,9 @@ sdm_status check_dev_status(sdm_handle* h, int* out, bool clear) {
 
 }  // namespace
 
+// Message for sdm_last_error(NULL) from entry points that have no handle.
+void sdm_set_thread_error(const char* msg) { g_create_error = msg ? msg : ""; }
+
 // (Re)allocates the cluster-pair lists with `cap` entries per i-cluster.
 static sdm_status sdm_reserve_lists(sdm_handle* h, int cap) {
     if (h->stream) SDM_CUDA(h, cudaStreamSynchronize(h->stream));

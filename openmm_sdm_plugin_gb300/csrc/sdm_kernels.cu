@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "../../include/sdm_capi.h"
 #include "sdm_types.h"
 
@@ -1451,3 +1453,376 @@ cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st) {
 }
 
 }  // extern "C++"
+
+// ========================================================================= //
+// Allocation-free evaluation of one small system (sdm_evaluate_noalloc)     //
+// ========================================================================= //
+//
+// Some callers cannot allocate device memory when they need a force: code
+// that records the call into a CUDA graph (cudaMalloc is not allowed while a
+// stream is being captured), hosts whose memory manager owns every device
+// byte (a simulation engine's context or a framework's caching allocator,
+// where an allocation behind their back breaks their accounting or fails
+// under a fixed budget), and latency-bound drivers that cannot afford the
+// implicit device synchronisation of cudaMalloc/cudaFree.  For them this
+// entry point evaluates one system of at most SDM_NOALLOC_MAX_PARTICLES
+// particles with every piece of scratch in one file-scope device array.
+//
+// The pair work is the all-pairs variant of the main and perturbation
+// passes: every pair i<j is evaluated at the original coordinates and, when
+// the displacements of i and j differ, at the displaced coordinates too, with
+// the same FP32 pair terms, 2^32 fixed-point force accumulation and FP64
+// energies as the handle path.  Cost grows as N^2, which is why the size is
+// capped.
+
+namespace {
+
+constexpr int kNaMax = SDM_NOALLOC_MAX_PARTICLES;
+constexpr int kNaBlocks = 304;            // 2 x 152 SMs
+constexpr int kNaThreads = 256;
+constexpr int kNaWarps = kNaBlocks * (kNaThreads / 32);
+constexpr int kNaExclSmem = 128;          // per-warp cached exclusion partners
+
+// byte layout of the scratch array
+constexpr size_t kNaF0 = 0;                                       // u64[3*max]
+constexpr size_t kNaDF = kNaF0 + 3ull * kNaMax * 8;              // u64[3*max]
+constexpr size_t kNaQ = kNaDF + 3ull * kNaMax * 8;               // float[max] q*sqrt(K)
+constexpr size_t kNaHS = kNaQ + 4ull * kNaMax;                   // float[max] sigma/2
+constexpr size_t kNaSE = kNaHS + 4ull * kNaMax;                  // float[max] 2 sqrt(eps)
+constexpr size_t kNaDB = kNaSE + 4ull * kNaMax;                  // u64[3*max] displacement bits
+constexpr size_t kNaEP = kNaDB + 3ull * kNaMax * 8;              // double[warps] U0 partials
+constexpr size_t kNaUP = kNaEP + 8ull * kNaWarps;                // double[warps] u partials
+constexpr size_t kNaST = kNaUP + 8ull * kNaWarps;                // int status
+constexpr size_t kNaBytes = (kNaST + 256 + 255) & ~size_t(255);
+
+static_assert(kNaBytes == SDM_NOALLOC_SCRATCH_BYTES, "scratch size must match the header");
+
+// The scratch.  Every GPU that loads the library holds it until exit.  In
+// host code this name is only a host-side stand-in: kernels receive the
+// device address taken with cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_sdm_noalloc_scratch[kNaBytes];
+
+struct NaArgs {
+    int n;
+    const double* x;
+    const double* q;
+    const double* sig;
+    const double* eps;
+    const int* eoff;
+    const int* eidx;
+    const double* d;
+    double box[3], invL[3];
+    float rc2f, krf, crf;
+    double p[SDM_NPARAMS];
+    double* results;
+    double* forces;
+    unsigned char* scratch;  // device address of g_sdm_noalloc_scratch
+};
+
+__device__ __forceinline__ unsigned long long* na_u64(const NaArgs& a, size_t off) {
+    return reinterpret_cast<unsigned long long*>(a.scratch + off);
+}
+__device__ __forceinline__ float* na_f32(const NaArgs& a, size_t off) {
+    return reinterpret_cast<float*>(a.scratch + off);
+}
+__device__ __forceinline__ double* na_f64(const NaArgs& a, size_t off) {
+    return reinterpret_cast<double*>(a.scratch + off);
+}
+
+// clears what must start at zero and converts the per-particle parameters
+__global__ void k_na_prep(NaArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    const double sk = 11.787089759563214;  // sqrt(138.935456)
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * a.n; k += stride) {
+        na_u64(a, kNaF0)[k] = 0ull;
+        na_u64(a, kNaDF)[k] = 0ull;
+        const double dv = a.d ? a.d[k] : 0.0;
+        na_u64(a, kNaDB)[k] = (unsigned long long)__double_as_longlong(__dadd_rn(dv, 0.0));
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        na_f32(a, kNaQ)[i] = (float)(a.q[i] * sk);
+        na_f32(a, kNaHS)[i] = (float)(0.5 * a.sig[i]);
+        na_f32(a, kNaSE)[i] = (float)(2.0 * sqrt(a.eps[i]));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *reinterpret_cast<int*>(a.scratch + kNaST) = 0;
+}
+
+__device__ __forceinline__ float na_delta(const NaArgs& a, double xi, double xj, int k) {
+    double v = __dsub_rn(xj, xi);
+    v = __dsub_rn(v, __dmul_rn(rint(__dmul_rn(v, a.invL[k])), a.box[k]));
+    return __double2float_rn(v);
+}
+
+__device__ __forceinline__ void na_red(const NaArgs& a, unsigned long long* p, float v) {
+    if (!(fabsf(v) < 1.0e9f)) atomicOr(reinterpret_cast<int*>(a.scratch + kNaST), SDM_DEV_FORCE_OVERFLOW);
+    atomicAdd(p, fix64(v));
+}
+
+__global__ void __launch_bounds__(kNaThreads) k_na_pairs(NaArgs a) {
+    __shared__ int ex[kNaThreads / 32][kNaExclSmem];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int w = blockIdx.x * (blockDim.x >> 5) + wib;
+    const float* qf = na_f32(a, kNaQ);
+    const float* hs = na_f32(a, kNaHS);
+    const float* se = na_f32(a, kNaSE);
+    const unsigned long long* db = na_u64(a, kNaDB);
+    unsigned long long* F0 = na_u64(a, kNaF0);
+    unsigned long long* dF = na_u64(a, kNaDF);
+    double e0 = 0.0, eu = 0.0;
+    for (int i = w; i < a.n; i += kNaWarps) {
+        const int eb = a.eoff[i], ee = a.eoff[i + 1];
+        const int ne = ee - eb;
+        __syncwarp();
+        for (int k = lane; k < ne && k < kNaExclSmem; k += 32) ex[wib][k] = a.eidx[eb + k];
+        __syncwarp();
+        const double xi0 = a.x[3 * i], xi1 = a.x[3 * i + 1], xi2 = a.x[3 * i + 2];
+        const unsigned long long di0 = db[3 * i], di1 = db[3 * i + 1], di2 = db[3 * i + 2];
+        const double dd0 = __longlong_as_double((long long)di0), dd1 = __longlong_as_double((long long)di1),
+                     dd2 = __longlong_as_double((long long)di2);
+        const float qi = qf[i], hi = hs[i], ei = se[i];
+        float f0x = 0.f, f0y = 0.f, f0z = 0.f, dfx = 0.f, dfy = 0.f, dfz = 0.f;
+        for (int j = i + 1 + lane; j < a.n; j += 32) {
+            bool excl = false;
+            if (ne <= kNaExclSmem) {
+                for (int k = 0; k < ne; ++k) excl |= (ex[wib][k] == j);
+            } else {
+                for (int k = eb; k < ee; ++k) excl |= (a.eidx[k] == j);
+            }
+            if (excl) continue;
+            const double xj0 = a.x[3 * j], xj1 = a.x[3 * j + 1], xj2 = a.x[3 * j + 2];
+            const float qq = qi * qf[j], sg = hi + hs[j], e4 = ei * se[j];
+            // state 1 of the reference: original coordinates
+            const float ax = na_delta(a, xi0, xj0, 0), ay = na_delta(a, xi1, xj1, 1), az = na_delta(a, xi2, xj2, 2);
+            const float r2a = r2_chain(ax, ay, az);
+            float ea = 0.f, fa = 0.f;
+            const bool oka = r2a < a.rc2f;
+            if (oka) {
+                const float ir = fast_rsqrt(r2a), ir2 = ir * ir;
+                const float s2 = sg * sg * ir2, s6 = s2 * s2 * s2, t6 = e4 * s6;
+                ea = fmaf(t6, s6 - 1.0f, qq * fmaf(a.krf, r2a, ir - a.crf));
+                fa = fmaf(t6, fmaf(12.0f, s6, -6.0f), qq * fmaf(-2.0f * a.krf, r2a, ir)) * ir2;
+                e0 += (double)ea;
+                f0x = fmaf(-fa, ax, f0x); f0y = fmaf(-fa, ay, f0y); f0z = fmaf(-fa, az, f0z);
+                na_red(a, F0 + 3 * j, fa * ax);
+                na_red(a, F0 + 3 * j + 1, fa * ay);
+                na_red(a, F0 + 3 * j + 2, fa * az);
+            }
+            const unsigned long long dj0 = db[3 * j], dj1 = db[3 * j + 1], dj2 = db[3 * j + 2];
+            if (dj0 == di0 && dj1 == di1 && dj2 == di2) continue;   // unchanged pair
+            // state 2 of the reference: displaced coordinates
+            const double yj0 = __dadd_rn(xj0, __longlong_as_double((long long)dj0));
+            const double yj1 = __dadd_rn(xj1, __longlong_as_double((long long)dj1));
+            const double yj2 = __dadd_rn(xj2, __longlong_as_double((long long)dj2));
+            const float bx = na_delta(a, __dadd_rn(xi0, dd0), yj0, 0);
+            const float by = na_delta(a, __dadd_rn(xi1, dd1), yj1, 1);
+            const float bz = na_delta(a, __dadd_rn(xi2, dd2), yj2, 2);
+            const float r2b = r2_chain(bx, by, bz);
+            float eb2 = 0.f, fb = 0.f;
+            if (r2b < a.rc2f) {
+                const float ir = fast_rsqrt(r2b), ir2 = ir * ir;
+                const float s2 = sg * sg * ir2, s6 = s2 * s2 * s2, t6 = e4 * s6;
+                eb2 = fmaf(t6, s6 - 1.0f, qq * fmaf(a.krf, r2b, ir - a.crf));
+                fb = fmaf(t6, fmaf(12.0f, s6, -6.0f), qq * fmaf(-2.0f * a.krf, r2b, ir)) * ir2;
+            }
+            eu += (double)eb2 - (double)ea;
+            const float gx = fb * bx - fa * ax, gy = fb * by - fa * ay, gz = fb * bz - fa * az;
+            dfx -= gx; dfy -= gy; dfz -= gz;
+            na_red(a, dF + 3 * j, gx);
+            na_red(a, dF + 3 * j + 1, gy);
+            na_red(a, dF + 3 * j + 2, gz);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            f0x += __shfl_xor_sync(0xffffffffu, f0x, o);
+            f0y += __shfl_xor_sync(0xffffffffu, f0y, o);
+            f0z += __shfl_xor_sync(0xffffffffu, f0z, o);
+            dfx += __shfl_xor_sync(0xffffffffu, dfx, o);
+            dfy += __shfl_xor_sync(0xffffffffu, dfy, o);
+            dfz += __shfl_xor_sync(0xffffffffu, dfz, o);
+        }
+        if (lane == 0) {
+            na_red(a, F0 + 3 * i, f0x); na_red(a, F0 + 3 * i + 1, f0y); na_red(a, F0 + 3 * i + 2, f0z);
+            na_red(a, dF + 3 * i, dfx); na_red(a, dF + 3 * i + 1, dfy); na_red(a, dF + 3 * i + 2, dfz);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        e0 += __shfl_xor_sync(0xffffffffu, e0, o);
+        eu += __shfl_xor_sync(0xffffffffu, eu, o);
+    }
+    if (lane == 0) {
+        na_f64(a, kNaEP)[w] = e0;
+        na_f64(a, kNaUP)[w] = eu;
+    }
+}
+
+// soft core, bias and weight of one lambda state, the same formulas as the
+// handle path's finalize kernel
+__device__ void na_combine(const double* p, double U0, double u, int st, double* o) {
+    const int method = (int)p[SDM_P_BIAS_METHOD];
+    const int noneq = (int)p[SDM_P_NONEQ];
+    const double lambdac = p[SDM_P_LAMBDA];
+    double gamma = 0.0, wb = lambdac, w0 = 0.0, l1 = lambdac, l2 = lambdac, alpha = 1.0, u0 = 0.0;
+    if (noneq == 1) {
+        l1 = p[SDM_P_M_LAMBDA1] * lambdac + p[SDM_P_B_LAMBDA1];
+        l2 = p[SDM_P_M_LAMBDA2] * lambdac + p[SDM_P_B_LAMBDA2];
+        u0 = p[SDM_P_M_U0] * lambdac + p[SDM_P_B_U0];
+        w0 = p[SDM_P_M_W0] * lambdac + p[SDM_P_B_W0];
+    }
+    if (method == SDM_QUADRATIC) {
+        gamma = p[SDM_P_GAMMA];
+        wb = p[SDM_P_WB];
+        if (noneq != 1) w0 = p[SDM_P_W0];
+    } else if (method == SDM_ILOGISTIC) {
+        if (noneq != 1) { l1 = p[SDM_P_LAMBDA1]; l2 = p[SDM_P_LAMBDA2]; u0 = p[SDM_P_U0]; w0 = p[SDM_P_W0]; }
+        alpha = p[SDM_P_ALPHA];
+    }
+    double fp;
+    const double be = softcore(u, (int)p[SDM_P_SOFTCORE_METHOD], p[SDM_P_UMAX], p[SDM_P_ACORE],
+                               p[SDM_P_UBCORE], &fp);
+    double ebias, bfp;
+    if (method == SDM_QUADRATIC) {
+        ebias = 0.5 * gamma * be * be + wb * be + w0;
+        bfp = gamma * be + wb;
+    } else if (method == SDM_ILOGISTIC) {
+        const double ee = 1.0 + exp(-alpha * (be - u0));
+        ebias = 0.0;
+        if (alpha > 0) ebias = ((l2 - l1) / alpha) * log(ee);
+        ebias += l2 * be + w0;
+        bfp = (l2 - l1) / ee + l1;
+    } else {
+        ebias = lambdac * be;
+        bfp = lambdac;
+    }
+    double dwdl = 0.0;
+    if (noneq == 1) {
+        const double ee = 1.0 + exp(-alpha * (be - u0));
+        dwdl = (-log(ee) / alpha) * p[SDM_P_M_LAMBDA1] + (be + log(ee) / alpha) * p[SDM_P_M_LAMBDA2] +
+               ((l2 - l1) * exp(-alpha * (be - u0)) / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
+    }
+    if (!isfinite(U0) || !isfinite(u)) st |= SDM_DEV_ENERGY_NONFINITE;
+    o[SDM_R_U0] = U0;
+    o[SDM_R_U1] = U0 + u;
+    o[SDM_R_U] = u;
+    o[SDM_R_BINDE] = be;
+    o[SDM_R_FP] = fp;
+    o[SDM_R_W] = ebias;
+    o[SDM_R_DW] = bfp;
+    o[SDM_R_S] = bfp * fp;
+    o[SDM_R_EPOT] = U0 + ebias;
+    o[SDM_R_DWDLAMBDA] = dwdl;
+    o[SDM_R_LAMBDA1] = l1;
+    o[SDM_R_LAMBDA2] = l2;
+    o[SDM_R_U0PARAM] = u0;
+    o[SDM_R_W0PARAM] = w0;
+    o[SDM_R_STATUS] = (double)st;
+    o[SDM_R_RESERVED] = 0.0;
+}
+
+__global__ void __launch_bounds__(256) k_na_finalize(NaArgs a) {
+    __shared__ double red[256];
+    double e0 = 0.0, eu = 0.0;
+    for (int k = threadIdx.x; k < kNaWarps; k += blockDim.x) {
+        e0 += na_f64(a, kNaEP)[k];
+        eu += na_f64(a, kNaUP)[k];
+    }
+    const double U0 = block_sum(e0, red);
+    const double u = block_sum(eu, red);
+    if (threadIdx.x == 0)
+        na_combine(a.p, U0, u, *reinterpret_cast<volatile int*>(a.scratch + kNaST), a.results);
+}
+
+__global__ void k_na_mix(NaArgs a) {
+    const double sc = 1.0 / SDM_FIX_SCALE;
+    const double s = a.results[SDM_R_S];
+    const unsigned long long* F0 = na_u64(a, kNaF0);
+    const unsigned long long* dF = na_u64(a, kNaDF);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * a.n; k += gridDim.x * blockDim.x)
+        a.forces[k] = (double)(long long)F0[k] * sc + s * ((double)(long long)dF[k] * sc);
+}
+
+}  // namespace
+
+void sdm_set_thread_error(const char* msg);
+
+// device address of the scratch array, taken once per device with that device current
+static unsigned char* g_na_addr[64];
+static bool g_na_ready[64];
+static std::mutex g_na_mutex;
+
+extern "C" sdm_status sdm_evaluate_noalloc(int num_particles, const double* x, const double* charge,
+                                           const double* sigma, const double* epsilon,
+                                           const int* excl_offsets, const int* excl_indices,
+                                           const double* displacement, const double* box,
+                                           double cutoff, double eps_rf, const double* params,
+                                           double* results, double* forces, void* stream) {
+    if (num_particles < 1 || num_particles > SDM_NOALLOC_MAX_PARTICLES) {
+        sdm_set_thread_error("sdm_evaluate_noalloc: num_particles must be in 1..SDM_NOALLOC_MAX_PARTICLES (8192)");
+        return SDM_ERR_INVALID_ARGUMENT;
+    }
+    if (!x || !charge || !sigma || !epsilon || !excl_offsets || !excl_indices || !box || !params || !results) {
+        sdm_set_thread_error("sdm_evaluate_noalloc: a required pointer is NULL");
+        return SDM_ERR_INVALID_ARGUMENT;
+    }
+    for (int k = 0; k < 3; ++k)
+        if (!(box[k] > 0.0) || !(cutoff > 0.0) || !(cutoff < 0.5 * box[k])) {
+            sdm_set_thread_error("sdm_evaluate_noalloc: need 0 < cutoff < box/2 in every axis");
+            return SDM_ERR_INVALID_ARGUMENT;
+        }
+    if (!(eps_rf > 0.0)) {
+        sdm_set_thread_error("sdm_evaluate_noalloc: reaction_field_dielectric must be > 0");
+        return SDM_ERR_INVALID_ARGUMENT;
+    }
+    const double bm = params[SDM_P_BIAS_METHOD], sm = params[SDM_P_SOFTCORE_METHOD];
+    if (!(bm == 0.0 || bm == 1.0 || bm == 2.0) || !(sm == 0.0 || sm == 1.0 || sm == 2.0)) {
+        sdm_set_thread_error("sdm_evaluate_noalloc: Unknown bias or soft core method");
+        return SDM_ERR_UNKNOWN_METHOD;
+    }
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess || dev < 0 || dev >= 64) {
+        sdm_set_thread_error("sdm_evaluate_noalloc: no current CUDA device");
+        return SDM_ERR_NO_DEVICE;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_na_mutex);
+        if (!g_na_ready[dev]) {
+            void* p = nullptr;
+            ce = cudaGetSymbolAddress(&p, g_sdm_noalloc_scratch);
+            if (ce != cudaSuccess || !p) {
+                sdm_set_thread_error("sdm_evaluate_noalloc: cudaGetSymbolAddress failed");
+                return SDM_ERR_CUDA;
+            }
+            g_na_addr[dev] = static_cast<unsigned char*>(p);
+            g_na_ready[dev] = true;
+        }
+    }
+    NaArgs a;
+    a.n = num_particles;
+    a.x = x;
+    a.q = charge;
+    a.sig = sigma;
+    a.eps = epsilon;
+    a.eoff = excl_offsets;
+    a.eidx = excl_indices;
+    a.d = displacement;
+    for (int k = 0; k < 3; ++k) { a.box[k] = box[k]; a.invL[k] = 1.0 / box[k]; }
+    a.rc2f = (float)(cutoff * cutoff);
+    a.krf = (float)((eps_rf - 1.0) / ((2.0 * eps_rf + 1.0) * cutoff * cutoff * cutoff));
+    a.crf = (float)(3.0 * eps_rf / ((2.0 * eps_rf + 1.0) * cutoff));
+    for (int k = 0; k < SDM_NPARAMS; ++k) a.p[k] = params[k];
+    a.results = results;
+    a.forces = forces;
+    a.scratch = g_na_addr[dev];
+    cudaStream_t st = (cudaStream_t)stream;
+    k_na_prep<<<64, 256, 0, st>>>(a);
+    k_na_pairs<<<kNaBlocks, kNaThreads, 0, st>>>(a);
+    k_na_finalize<<<1, 256, 0, st>>>(a);
+    if (forces) k_na_mix<<<32, 256, 0, st>>>(a);
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) {
+        sdm_set_thread_error(cudaGetErrorString(ce));
+        return SDM_ERR_CUDA;
+    }
+    return SDM_OK;
+}
