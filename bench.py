@@ -101,6 +101,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(seconds: float, dist, device=None) -> float:
+    """Slowest rank's time (the job's time); identity on a single process."""
+    if dist is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: int, world: int, seconds_max: float) -> float:
+    """Units processed by all ranks over the slowest rank's time (weak scaling)."""
+    return units_per_rank * world / seconds_max
+
+
 def cpu_baseline_port(sysm, nthreads: int, budget_s: float = 10.0):
     """FP64 oracle (the CPU restatement of the reference path) on a bounded
     sample: whole lambda states of the workload, one after another."""
@@ -135,13 +150,15 @@ def run_reference(args):
     nth = os.cpu_count() or 1
     o = oracle.OracleSystem(sysm)
     params = [q.as_array() for q in sysm.params]
-    # each step: a bounded sample of the 22-state batch (states k, k+1, ... round robin)
-    per_step = max(1, min(NREP, int(os.environ.get("SDM_REF_STATES_PER_STEP", "4"))))
+    # each step: a bounded sample of the 22-state batch (states k, k+1, ...
+    # round robin), sized from the warm-up so that all steps take ~60 s
     k = 0
-    for _ in range(args.warmup):
-        for _ in range(per_step):
-            oracle.eval_state(o, sysm.positions[k % NREP], params[k % NREP], nthreads=nth)
-            k += 1
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.warmup)):
+        oracle.eval_state(o, sysm.positions[k % NREP], params[k % NREP], nthreads=nth)
+        k += 1
+    t_state = (time.perf_counter() - t0) / max(1, args.warmup)
+    per_step = max(1, min(NREP, int(60.0 / max(args.steps * t_state, 1e-9))))
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
@@ -278,12 +295,8 @@ def main():
                      args.steps, warm, per_kernel=h.kernel_times)
     t_wall = time.perf_counter() - t_wall0
     clocks = sampler.stop()
-    tot_b = sum(ms_b) / 1e3
-    if dist is not None:
-        t = torch.tensor([tot_b], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_b = float(t.item())
-    value = NREP * args.steps * world / tot_b
+    tot_b = max_over_ranks(sum(ms_b) / 1e3, dist, dev)
+    value = whole_job_rate(NREP * args.steps, world, tot_b)
     jlist_ms = [d["k_jlist"] for d in pk]
     pair_ms = [d["k_pair"] for d in pk]
     pert_ms = [d["k_perturb"] for d in pk]
@@ -319,12 +332,8 @@ def main():
         t0 = time.perf_counter()
         e2e_step()   # H2D copy, evaluation, D2H copy, synchronise
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    tot_e = sum(e2e_ms) / 1e3
-    if dist is not None:
-        t = torch.tensor([tot_e], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_e = float(t.item())
-    e2e = NREP * args.steps * world / tot_e
+    tot_e = max_over_ranks(sum(e2e_ms) / 1e3, dist, dev)
+    e2e = whole_job_rate(NREP * args.steps, world, tot_e)
     # check the batch result once against nothing but itself: status clean
     status = h.check_status()
 
