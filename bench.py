@@ -37,6 +37,7 @@ METRIC = "SDM lambda-state force evals/s at 23k atoms x 22 lambda, batched vs pl
 UNIT = "lambda-state evals/s"
 FLOP_PER_PAIR = 52  # FP32 flops per pair per state (FMA = 2, rsqrt = 1)
 NREP = 22
+K_PAIR_DRAM_BYTES_PER_LAUNCH = 128.639232e6 + 6.411776e6
 
 
 def _peaks():
@@ -354,10 +355,10 @@ def main():
             "frac_pair_path": (flop_per_launch / ((pair_avg + sum(jlist_ms) / len(jlist_ms)
                                                    + sum(pert_ms) / len(pert_ms)) * 1e-3) / 1e12) / peak_tf,
             "flop_per_launch": flop_per_launch, "P0": P0, "P1delta": P1}
-    traffic_file = os.path.join(ROOT, "profiles", "k_pair_traffic.json")
-    if os.path.exists(traffic_file):
-        with open(traffic_file) as f:
-            roof["traffic"] = json.load(f).get("bytes_per_launch")
+    # dram__bytes_read.sum + dram__bytes_write.sum of one k_pair launch on this
+    # workload (ncu --set full, cold cache): profiles/k_pair_k_jlist_k_perturb_config2x22.md
+    roof["traffic"] = K_PAIR_DRAM_BYTES_PER_LAUNCH
+    roof["traffic_note"] = "ncu capture of the same workload, cold cache between replay passes"
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
