@@ -209,6 +209,29 @@ sdm_status sdm_count_pairs(sdm_handle* h, const double* x, long long* counts);
 /* Cell grid of one system: M[0..2] cells per axis (columns are M[0]*M[1]). */
 sdm_status sdm_get_grid(const sdm_handle* h, int system, int* M);
 
+/* Replaces charge/sigma/epsilon of n particles of one system (indices into
+ * the system; values in nm, kJ/mol, e).  The reference sets them on OpenMM's
+ * NonbondedForce (example/desmonddmsfile75.py:776-808); here they feed the
+ * next evaluation and the adjoint. */
+sdm_status sdm_set_particle_params(sdm_handle* h, int system, int n, const int* index,
+                                   const double* charge, const double* sigma,
+                                   const double* epsilon);
+
+/* Adjoint of the last evaluation with respect to the parameters of the
+ * displaced particles (no counterpart in the reference, whose only
+ * derivative is the non-equilibrium dW/dlambda of ReferenceSDMKernels.cpp:289-302).
+ * For every replica r, every displaced particle k of its system (ascending
+ * particle index) and both states s (0: original, 1: displaced coordinates)
+ * writes three FP64 sums over the interacting partners j of k in state s:
+ *   out[((D_r + k)*2 + s)*3 + 0] = sum_j K q_j (1/r + krf r^2 - crf)   = dU_s/dq_k
+ *   out[((D_r + k)*2 + s)*3 + 1] = sum_j d e_LJ / d sigma_k             = dU_s/dsigma_k
+ *   out[((D_r + k)*2 + s)*3 + 2] = sum_j e_LJ(k,j)                       (= 2 eps_k dU_s/deps_k)
+ * D_r = displaced particles of the replicas before r.  Host pointer;
+ * synchronises.  The parameter gradient of U_lambda = U0 + W is
+ * (1-s) dU_0 + s dU_1 with s = results[SDM_R_S]; the displacement gradient
+ * is -s F1 (sdm_get_state_forces). */
+sdm_status sdm_adjoint(sdm_handle* h, double* out);
+
 /* Diagnostic export of the clustering and neighbour lists of replica
  * `replica` for coordinates x (host pointer, that replica's 3*num_particles):
  *   perm[cap_slots]                slot -> particle (-1 = padding)

@@ -38,7 +38,8 @@ EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_set_displacement", "sdm_set_params", "sdm_evaluate", "sdm_evaluate_device",
             "sdm_get_state_forces", "sdm_check_status", "sdm_set_option", "sdm_get_option",
             "sdm_get_kernel_times", "sdm_autotune", "sdm_count_pairs", "sdm_get_grid",
-            "sdm_export_lists", "sdm_evaluate_noalloc")
+            "sdm_export_lists", "sdm_evaluate_noalloc", "sdm_set_particle_params",
+            "sdm_adjoint")
 
 NOALLOC_MAX_PARTICLES = 8192
 NOALLOC_SCRATCH_BYTES = 727296
@@ -100,6 +101,8 @@ def load_library(path: str = LIB_PATH):
         L.sdm_export_lists.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, ip, vp, vp, vp]
         L.sdm_evaluate_noalloc.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, C.c_double,
                                            C.c_double, vp, vp, vp, vp]
+        L.sdm_set_particle_params.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp]
+        L.sdm_adjoint.argtypes = [vp, vp]
         for name in EXPORTED:
             if name != "sdm_last_error":
                 getattr(L, name).restype = C.c_int
@@ -199,6 +202,20 @@ class Handle:
         return np.array(list(M), np.int32)
 
     # -- evaluation -------------------------------------------------------
+    def set_particle_params(self, system: int, index, charge, sigma, epsilon):
+        idx = np.ascontiguousarray(np.asarray(index, np.int32).reshape(-1))
+        q = np.ascontiguousarray(np.asarray(charge, np.float64).reshape(-1))
+        sg = np.ascontiguousarray(np.asarray(sigma, np.float64).reshape(-1))
+        ep = np.ascontiguousarray(np.asarray(epsilon, np.float64).reshape(-1))
+        self._check(self.lib.sdm_set_particle_params(self.h, int(system), int(idx.size), idx.ctypes.data,
+                                                     q.ctypes.data, sg.ctypes.data, ep.ctypes.data))
+
+    def adjoint(self, n_displaced):
+        """Adjoint sums of the last evaluation: (sum over replicas of nD, 2 states, 3)."""
+        out = np.zeros(6 * int(n_displaced))
+        self._check(self.lib.sdm_adjoint(self.h, out.ctypes.data))
+        return out.reshape(-1, 2, 3)
+
     def evaluate(self, x, forces: bool = True):
         """Host evaluation of all replicas. x: (total_particles, 3) float64."""
         x = np.ascontiguousarray(np.asarray(x, np.float64).reshape(-1))

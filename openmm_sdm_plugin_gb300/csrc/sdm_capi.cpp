@@ -27,6 +27,7 @@ cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, 
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st);
+cudaError_t sdm_launch_adjoint(const SdmArgs& a, cudaStream_t st);
 
 namespace {
 
@@ -607,6 +608,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_lnk = ar.take<int4>(Cl), o_ep = ar.take<double>(Cl * SDM_MAX_SPLIT);
     const size_t o_zb = ar.take<float2>(Cl);
     const size_t o_pp = ar.take<double>(std::max(Pp, 1LL));
+    const size_t o_adj = ar.take<double>(3 * std::max(Pp, 1LL));
     const size_t o_ncl = ar.take<int>(nrep), o_st = ar.take<int>(4);
     const size_t o_counts = ar.take<long long>(2 * nrep), o_ip = ar.take<int>(nrep + 1);
     const size_t o_cp = ar.take<int>(nrep + 1), o_jc = ar.take<int>(Cl);
@@ -668,6 +670,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.stencil = at<int2>(B, o_st2);
     a.e_part = at<double>(B, o_ep);
     a.p_part = at<double>(B, o_pp);
+    a.adj = at<double>(B, o_adj);
     a.ncl = at<int>(B, o_ncl);
     a.status = at<int>(B, o_st);
     a.counts = at<long long>(B, o_counts);
@@ -821,6 +824,42 @@ sdm_status sdm_get_state_forces(sdm_handle* h, double* F0, double* F1, int on_de
             SDM_CUDA(h, cudaMemcpyAsync(F1, h->f_in, nx * 8, cudaMemcpyDeviceToHost, h->stream));
         }
     }
+    SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SDM_OK;
+}
+
+sdm_status sdm_set_particle_params(sdm_handle* h, int system, int n, const int* index,
+                                   const double* charge, const double* sigma, const double* epsilon) {
+    if (!h || n < 0 || (n > 0 && (!index || !charge || !sigma || !epsilon))) return SDM_ERR_INVALID_ARGUMENT;
+    if (system < 0 || system >= (int)h->sys.size()) return fail(h, SDM_ERR_INVALID_ARGUMENT, "system index out of range");
+    SysHost& S = h->sys[system];
+    const double sk = std::sqrt(kCoulomb);
+    for (int k = 0; k < n; ++k) {
+        const int i = index[k];
+        if (i < 0 || i >= S.n) return fail(h, SDM_ERR_INVALID_ARGUMENT, "particle index out of range");
+        if (!(sigma[k] >= 0.0) || !(epsilon[k] >= 0.0) || !std::isfinite(charge[k]))
+            return fail(h, SDM_ERR_INVALID_ARGUMENT, "sigma/epsilon must be >= 0 and charges finite");
+    }
+    cudaSetDevice(h->device);
+    SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < n; ++k) {
+        const int i = index[k];
+        S.q[i] = (float)(charge[k] * sk);
+        S.hs[i] = (float)(0.5 * sigma[k]);
+        S.se[i] = (float)(2.0 * std::sqrt(epsilon[k]));
+    }
+    h->have_eval = false;
+    return upload_topology(h);
+}
+
+sdm_status sdm_adjoint(sdm_handle* h, double* out) {
+    if (!h || !out) return SDM_ERR_INVALID_ARGUMENT;
+    if (!h->have_eval) return fail(h, SDM_ERR_INVALID_ARGUMENT, "no evaluation yet");
+    cudaSetDevice(h->device);
+    SDM_CUDA(h, cudaDeviceSynchronize());
+    SDM_CUDA(h, sdm_launch_adjoint(h->args, h->stream));
+    const size_t n = 3 * (size_t)h->args.total_pert;
+    if (n) SDM_CUDA(h, cudaMemcpyAsync(out, h->args.adj, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
     return SDM_OK;
 }

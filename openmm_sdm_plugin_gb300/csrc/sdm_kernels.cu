@@ -1232,6 +1232,229 @@ __global__ void __launch_bounds__(SDM_WARPS * 32) k_perturb(SdmArgs a) {
 }
 
 // ------------------------------------------------------------------------- //
+// Adjoint: parameter derivatives of U0 and U1 for the displaced particles   //
+// ------------------------------------------------------------------------- //
+struct AdjSmem {
+    int4 jl[SDM_JL_CAP];
+    int4 rng[64];
+    int ex[128];                // exclusion partners of the particle (system-local)
+};
+
+__device__ __forceinline__ bool adj_excluded(const AdjSmem& sm, const SdmArgs& a, int eb, int ne, int j) {
+    bool e = false;
+    if (ne <= 128) {
+        for (int k = 0; k < ne; ++k) e |= (sm.ex[k] == j);
+    } else {
+        for (int k = 0; k < ne; ++k) e |= (a.excl_idx[eb + k] == j);
+    }
+    return e;
+}
+
+template <bool IMG>
+__device__ void process_adjoint(const SdmArgs& a, int r, int local, AdjSmem& sm) {
+    const int lane = lane_id();
+    const SdmRep R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int pidx = local >> 1, st = local & 1;
+    const int p = a.D_idx[S.D_base + pidx];
+    const int tp = S.atom_base + p;
+    double y[3];
+    int cy[3];
+    float o[3];
+    const double* wp = a.w + 3 * (size_t)(R.atom_win + p);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double v = st ? __dadd_rn(wp[k], a.topo_d[3 * (size_t)tp + k]) : wp[k];
+        y[k] = wrap1(v, S.box[k], S.invL[k]);
+        cy[k] = cell_of(y[k], S.invg[k], S.M[k]);
+        o[k] = __double2float_rn(__dsub_rn(y[k], __dmul_rn((double)cy[k], S.g[k])));
+    }
+    const float hp = a.topo_hs[tp], sp_ = a.topo_se[tp];
+    const int eb = a.excl_off[tp], ne = a.excl_off[tp + 1] - eb;
+    __syncwarp();
+    for (int k = lane; k < ne && k < 128; k += 32) sm.ex[k] = a.excl_idx[eb + k];
+    __syncwarp();
+    const float rclc = S.rcl + 2.0e-4f;
+    const float rclc2 = rclc * rclc;
+    const float* tabx = a.shift_tab + S.shift_base;
+    const float* taby = tabx + 2 * S.M[0] + 1;
+    const float* tabz = taby + 2 * S.M[1] + 1;
+    const int nst = S.fst_count;
+    const int* colcl = a.col_cl + R.col_win;
+    const float sqrtK = 11.787089759563214f;
+    double gq = 0.0, gs = 0.0, ge = 0.0;
+    int jl_n = 0;
+
+    auto acc = [&](float r2, float qj, float hj, float ej) {
+        const float ir = fast_rsqrt(r2), ir2 = ir * ir;
+        const float phi = sqrtK * qj * fmaf(S.krf, r2, ir - S.crf);
+        const float sg = hp + hj;
+        const float s2 = sg * sg * ir2, s6 = s2 * s2 * s2, t6 = sp_ * ej * s6;
+        const float elj = t6 * (s6 - 1.0f);
+        const float dsg = sg > 0.0f ? 0.5f * t6 * fmaf(12.0f, s6, -6.0f) / sg : 0.0f;
+        gq += (double)phi;
+        gs += (double)dsg;
+        ge += (double)elj;
+    };
+
+    auto phase_b = [&]() {
+        for (int g0 = 0; g0 < jl_n; g0 += 4) {
+            const int e = g0 + (lane >> 3);
+            if (e < jl_n) {
+                const int4 en = sm.jl[e];
+                const int sj = 8 * en.x + (lane & 7);
+                const size_t gsl = (size_t)R.slot_win + sj;
+                const float4 X4 = a.clX[gsl];
+                float dx = __fsub_rn(__fadd_rn(X4.x, __int_as_float(en.y)), o[0]);
+                float dy = __fsub_rn(__fadd_rn(X4.y, __int_as_float(en.z)), o[1]);
+                float dz = __fsub_rn(__fadd_rn(X4.z, __int_as_float(en.w)), o[2]);
+                if (IMG) {
+                    dx = img32(dx, S.Lf[0], S.invLf[0]);
+                    dy = img32(dy, S.Lf[1], S.invLf[1]);
+                    dz = img32(dz, S.Lf[2], S.invLf[2]);
+                }
+                const float r2 = r2_chain(dx, dy, dz);
+                bool ok = (r2 < S.rc2f) && X4.x < 1.0e5f && a.grp[gsl] == 0;
+                if (ok && ne > 0) ok = !adj_excluded(sm, a, eb, ne, a.perm[gsl]);
+                if (ok) {
+                    const float2 P = a.clP[gsl];
+                    acc(r2, X4.w, P.x, P.y);
+                }
+            }
+        }
+        jl_n = 0;
+    };
+
+    for (int k0 = 0; k0 < nst; k0 += 32) {
+        const int k = k0 + lane;
+        int cntJ = 0, Jb = 0;
+        float Sx = 0.f, Sy = 0.f;
+        if (k < nst) {
+            const int2 off = a.stencil[S.fst_base + k];
+            const int ccx = wrap_add(cy[0], off.x, S.M[0]);
+            const int ccy = wrap_add(cy[1], off.y, S.M[1]);
+            const int colid = ccx * S.M[1] + ccy;
+            Sx = tabx[wrap_cell(ccx - cy[0], S.M[0]) + S.M[0]];
+            Sy = taby[wrap_cell(ccy - cy[1], S.M[1]) + S.M[1]];
+            bool ok = true;
+            if (!IMG) {
+                const float lox = Sx - 1.0e-4f, hix = Sx + S.gf[0] + 1.0e-4f;
+                const float loy = Sy - 1.0e-4f, hiy = Sy + S.gf[1] + 1.0e-4f;
+                const float gx = fmaxf(0.0f, fmaxf(lox - o[0], o[0] - hix));
+                const float gy = fmaxf(0.0f, fmaxf(loy - o[1], o[1] - hiy));
+                ok = gx * gx + gy * gy < rclc2;
+            }
+            if (ok) {
+                Jb = colcl[colid];
+                cntJ = max(colcl[colid + 1] - Jb, 0);
+            }
+        }
+        const bool has = cntJ > 0;
+        const unsigned hb = __ballot_sync(0xffffffffu, has);
+        int incl = cntJ;
+#pragma unroll
+        for (int oo = 1; oo < 32; oo <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, oo);
+            if (lane >= oo) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (has) {
+            const int ri = __popc(hb & ((1u << lane) - 1u));
+            sm.rng[ri] = make_int4(Jb, incl - cntJ, __float_as_int(Sx), __float_as_int(Sy));
+        }
+        const int nr = __popc(hb);
+        __syncwarp();
+        for (int e0 = 0; e0 < total; e0 += 32) {
+            const int e = e0 + lane;
+            bool pass = false;
+            int4 en = make_int4(0, 0, 0, 0);
+            if (e < total) {
+                int lo = 0, hi = nr - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sm.rng[mid].y <= e) lo = mid; else hi = mid - 1;
+                }
+                const int4 rg = sm.rng[lo];
+                const int J = rg.x + (e - rg.y);
+                const int jw = R.cl_win + J;
+                const int4 rj = a.cl_ref[jw];
+                const float sz = tabz[wrap_cell(rj.z - cy[2], S.M[2]) + S.M[2]];
+                const float sx = __int_as_float(rg.z), sy = __int_as_float(rg.w);
+                const float4 cj = a.cl_bbc[jw];
+                const float4 hjb = a.cl_bbh[jw];
+                float dx = cj.x + sx - o[0], dy = cj.y + sy - o[1], dz = cj.z + sz - o[2];
+                if (IMG) {
+                    dx = img32(dx, S.Lf[0], S.invLf[0]);
+                    dy = img32(dy, S.Lf[1], S.invLf[1]);
+                    dz = img32(dz, S.Lf[2], S.invLf[2]);
+                }
+                const float gx = fmaxf(fabsf(dx) - hjb.x, 0.0f);
+                const float gy = fmaxf(fabsf(dy) - hjb.y, 0.0f);
+                const float gz = fmaxf(fabsf(dz) - hjb.z, 0.0f);
+                pass = gx * gx + gy * gy + gz * gz < rclc2;
+                en = make_int4(J, __float_as_int(sx), __float_as_int(sy), __float_as_int(sz));
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, pass);
+            if (pass) sm.jl[jl_n + __popc(bal & ((1u << lane) - 1u))] = en;
+            jl_n += __popc(bal);
+            __syncwarp();
+            if (jl_n > SDM_JL_CAP - 32) phase_b();
+            __syncwarp();
+        }
+    }
+    phase_b();
+    // every other displaced particle, at its own state-s position
+    for (int q0 = 0; q0 < S.nD; q0 += 32) {
+        const int qi = q0 + lane;
+        if (qi < S.nD) {
+            const int qa = a.D_idx[S.D_base + qi];
+            if (qa != p) {
+                const int tq = S.atom_base + qa;
+                const double* wq = a.w + 3 * (size_t)(R.atom_win + qa);
+                float d[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const double vq = st ? __dadd_rn(wq[k], a.topo_d[3 * (size_t)tq + k]) : wq[k];
+                    const double yq = wrap1(vq, S.box[k], S.invL[k]);
+                    double v = __dsub_rn(yq, y[k]);
+                    const double tt = rint(__dmul_rn(v, S.invL[k]));
+                    v = __dsub_rn(v, __dmul_rn(tt, S.box[k]));
+                    d[k] = __double2float_rn(v);
+                }
+                const float r2 = r2_chain(d[0], d[1], d[2]);
+                if (r2 < S.rc2f && !adj_excluded(sm, a, eb, ne, qa))
+                    acc(r2, a.topo_q[tq], a.topo_hs[tq], a.topo_se[tq]);
+            }
+        }
+    }
+#pragma unroll
+    for (int oo = 16; oo > 0; oo >>= 1) {
+        gq += __shfl_xor_sync(0xffffffffu, gq, oo);
+        gs += __shfl_xor_sync(0xffffffffu, gs, oo);
+        ge += __shfl_xor_sync(0xffffffffu, ge, oo);
+    }
+    if (lane == 0) {
+        double* out = a.adj + 3 * (size_t)(R.pert_win + local);
+        out[0] = gq;
+        out[1] = gs;
+        out[2] = ge;
+    }
+}
+
+__global__ void __launch_bounds__(SDM_WARPS * 32) k_adjoint(SdmArgs a) {
+    __shared__ AdjSmem smem[SDM_WARPS];
+    AdjSmem& sm = smem[threadIdx.x >> 5];
+    const int W = gridDim.x * SDM_WARPS;
+    for (int item = blockIdx.x * SDM_WARPS + (threadIdx.x >> 5); item < a.total_pert; item += W) {
+        const int r = rep_by_pert(a.rep, a.nrep, item);
+        const int local = item - a.rep[r].pert_win;
+        const SdmSys& S = a.sys[a.rep[r].sys];
+        if (replica_image_mode(a, S, r)) process_adjoint<true>(a, r, local, sm);
+        else process_adjoint<false>(a, r, local, sm);
+    }
+}
+
+// ------------------------------------------------------------------------- //
 // K8: energies, soft core, bias (FP64)                                      //
 // ------------------------------------------------------------------------- //
 __device__ double block_sum(double v, double* red) {
@@ -1438,6 +1661,15 @@ cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st) {
     if (grid > cap) grid = cap;
     if (mode == MODE_COUNT) k_perturb<MODE_COUNT><<<grid, SDM_WARPS * 32, 0, st>>>(a);
     else k_perturb<MODE_EVAL><<<grid, SDM_WARPS * 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sdm_launch_adjoint(const SdmArgs& a, cudaStream_t st) {
+    if (a.total_pert == 0) return cudaSuccess;
+    int grid = (a.total_pert + SDM_WARPS - 1) / SDM_WARPS;
+    const int cap = num_sms() * 4;
+    if (grid > cap) grid = cap;
+    k_adjoint<<<grid, SDM_WARPS * 32, 0, st>>>(a);
     return cudaGetLastError();
 }
 

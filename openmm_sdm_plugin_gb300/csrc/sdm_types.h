@@ -133,6 +133,7 @@ struct SdmArgs {
     int jl_cap;
     double* e_part;      // cl window * SDM_MAX_SPLIT
     double* p_part;      // perturbation partials
+    double* adj;         // adjoint sums: 3 per perturbation item
     int* ncl;            // clusters per replica
     unsigned* extz;      // per replica max cluster z extent (float bits)
     int* work_counter;   // [0] main pass, [1] perturbation pass

@@ -1,0 +1,189 @@
+"""Differentiation (backward of the SDM potential).
+
+CPU: the dense FP64 torch reference against the oracle; the partial
+derivatives of W against finite differences of the restated combine.
+GPU: the autograd Function (adjoint kernel) against FP64 central finite
+differences of the oracle (h = 1e-5, the 930-site system) and against the
+dense FP64 torch reference (a 2k-particle host-guest system).
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from dense_sdm import candidate_pairs, potential
+from openmm_sdm_plugin_gb300 import systems as S
+from openmm_sdm_plugin_gb300.autograd import bias_partials
+
+GRAD_REL_TOL = 2e-4   # gradient vs FP64 reference: FP32 pair terms, FP64 sums
+
+
+def _params(alpha=0.1):
+    return S.SDMParams(bias_method=2, softcore_method=2, lambdac=0.4, lambda1=0.2, lambda2=0.5,
+                       alpha=alpha, u0=110.0, w0=1.5, umax=200.0, acore=1 / 16, ubcore=100.0)
+
+
+def _system():
+    s = S.config0(variant="b")
+    s.params = [_params()]
+    return s
+
+
+def _u_lambda_oracle(s, p, q=None, sig=None, eps=None, d=None, x=None):
+    s2 = dataclasses.replace(s, charge=s.charge if q is None else q, sigma=s.sigma if sig is None else sig,
+                             epsilon=s.epsilon if eps is None else eps,
+                             displacement=s.displacement if d is None else d)
+    o = oracle.OracleSystem(s2)
+    res, _ = oracle.eval_state(o, s.positions[0] if x is None else x, p.as_array(), forces=False)
+    return res[6]
+
+
+def test_dense_reference_matches_oracle():
+    s = _system()
+    p = s.params[0]
+    x = torch.tensor(s.positions[0])
+    t = lambda a: torch.tensor(np.asarray(a, np.float64))
+    U, u = potential(s, x, t(s.charge), t(s.sigma), t(s.epsilon), t(s.displacement), t(p.lambda1),
+                     t(p.lambda2), t(p.alpha), t(p.u0), t(p.w0), p)
+    o = oracle.OracleSystem(s)
+    res, _ = oracle.eval_state(o, s.positions[0], p.as_array(), forces=False)
+    assert float(u) == pytest.approx(res[0], rel=1e-10, abs=1e-8)
+    assert float(U) == pytest.approx(res[6], rel=1e-10, abs=1e-8)
+
+
+@pytest.mark.parametrize("be", [-30.0, 50.0, 110.0, 180.0])
+def test_bias_partials_fd(be):
+    p = _params()
+    h = 1e-6
+    d = bias_partials(p, be)
+    for key in ("lambda1", "lambda2", "alpha", "u0", "w0"):
+        pp = dataclasses.replace(p, **{key: getattr(p, key) + h})
+        pm = dataclasses.replace(p, **{key: getattr(p, key) - h})
+        # W at fixed u' = be: combine with soft core off and u = be
+        Wp = oracle.combine(dataclasses.replace(pp, softcore_method=0).as_array(), 0.0, be)[3]
+        Wm = oracle.combine(dataclasses.replace(pm, softcore_method=0).as_array(), 0.0, be)[3]
+        assert d[key] == pytest.approx((Wp - Wm) / (2 * h), rel=1e-6, abs=1e-8), key
+
+
+def _gpu_grads(s):
+    from openmm_sdm_plugin_gb300.autograd import SDMEngine, sdm_potential
+    eng = SDMEngine(s)
+    D = eng.D
+    f64 = dict(dtype=torch.float64)
+    x = torch.tensor(s.positions, **f64, requires_grad=True)
+    qD = torch.tensor(s.charge[D], **f64, requires_grad=True)
+    sD = torch.tensor(s.sigma[D], **f64, requires_grad=True)
+    eD = torch.tensor(s.epsilon[D], **f64, requires_grad=True)
+    d = torch.tensor(s.displacement, **f64, requires_grad=True)
+    ps = s.params
+    vec = lambda k: torch.tensor([getattr(p, k) for p in ps], **f64, requires_grad=True)
+    l1, l2, al, u0, w0 = vec("lambda1"), vec("lambda2"), vec("alpha"), vec("u0"), vec("w0")
+    U = sdm_potential(eng, x, qD, sD, eD, d, l1, l2, al, u0, w0)
+    U.sum().backward()
+    eng.close()
+    return D, U.detach(), dict(x=x.grad, q=qD.grad, sigma=sD.grad, eps=eD.grad, d=d.grad, lambda1=l1.grad,
+                               lambda2=l2.grad, alpha=al.grad, u0=u0.grad, w0=w0.grad)
+
+
+@pytest.mark.gpu
+def test_gradients_vs_oracle_central_differences():
+    s = _system()
+    p = s.params[0]
+    D, U, g = _gpu_grads(s)
+    U_ref = _u_lambda_oracle(s, p)
+    assert float(U[0]) == pytest.approx(U_ref, abs=0.05)
+    h = 1e-5
+    rng = np.random.default_rng(0)
+    ks = rng.choice(len(D), 4, replace=False)
+    for name, arr, grad in (("q", s.charge, g["q"]), ("sigma", s.sigma, g["sigma"]),
+                            ("eps", s.epsilon, g["eps"])):
+        for k in ks:
+            a_p = arr.copy(); a_p[D[k]] += h
+            a_m = arr.copy(); a_m[D[k]] -= h
+            Up = _u_lambda_oracle(s, p, **{("q" if name == "q" else "sig" if name == "sigma" else "eps"): a_p})
+            Um = _u_lambda_oracle(s, p, **{("q" if name == "q" else "sig" if name == "sigma" else "eps"): a_m})
+            fd = (Up - Um) / (2 * h)
+            assert float(grad[k]) == pytest.approx(fd, rel=GRAD_REL_TOL, abs=1e-3), (name, k)
+    # the ligand's displacement vector: d = v * (1,0,0) for every ligand site
+    for c in range(3):
+        dp = s.displacement.copy(); dp[D, c] += h
+        dm = s.displacement.copy(); dm[D, c] -= h
+        fd = (_u_lambda_oracle(s, p, d=dp) - _u_lambda_oracle(s, p, d=dm)) / (2 * h)
+        assert float(g["d"][D, c].sum()) == pytest.approx(fd, rel=GRAD_REL_TOL, abs=1e-3), c
+    for key in ("lambda1", "lambda2", "alpha", "u0", "w0"):
+        fd = (_u_lambda_oracle(s, dataclasses.replace(p, **{key: getattr(p, key) + h})) -
+              _u_lambda_oracle(s, dataclasses.replace(p, **{key: getattr(p, key) - h}))) / (2 * h)
+        assert float(g[key][0]) == pytest.approx(fd, rel=GRAD_REL_TOL, abs=1e-4), key
+    # positions: one solvent site and one ligand site
+    for i in (5, int(D[3])):
+        xp = s.positions[0].copy(); xp[i, 1] += h
+        xm = s.positions[0].copy(); xm[i, 1] -= h
+        fd = (_u_lambda_oracle(s, p, x=xp) - _u_lambda_oracle(s, p, x=xm)) / (2 * h)
+        assert float(g["x"][0, i, 1]) == pytest.approx(fd, rel=GRAD_REL_TOL, abs=1e-3), i
+
+
+@pytest.mark.gpu
+def test_gradients_vs_dense_torch_2k():
+    s = S.host_guest(2000, 4, nstates=2)
+    s.params = [_params(), dataclasses.replace(_params(), lambda1=0.6, lambda2=0.7, u0=90.0)]
+    D, U, g = _gpu_grads(s)
+    t = lambda a, rg=False: torch.tensor(np.asarray(a, np.float64), requires_grad=rg)
+    for r in range(2):
+        p = s.params[r]
+        x = t(s.positions[r], True)
+        q, sg, ep, d = t(s.charge, True), t(s.sigma, True), t(s.epsilon, True), t(s.displacement, True)
+        sc = [t(getattr(p, k), True) for k in ("lambda1", "lambda2", "alpha", "u0", "w0")]
+        pairs = candidate_pairs(s, s.positions[r], s.displacement)
+        Ur, _ = potential(s, x, q, sg, ep, d, *sc, p, pairs=pairs)
+        Ur.backward()
+        assert float(U[r]) == pytest.approx(float(Ur), abs=0.05)
+        gr = {"q": q.grad[D], "sigma": sg.grad[D], "eps": ep.grad[D]}
+        for k, key in enumerate(("lambda1", "lambda2", "alpha", "u0", "w0")):
+            assert float(g[key][r]) == pytest.approx(float(sc[k].grad), rel=GRAD_REL_TOL, abs=1e-4), key
+        assert torch.allclose(g["x"][r], x.grad, rtol=1e-4, atol=1e-3 * float(x.grad.abs().max()))
+        if r == 0:
+            acc = {k: v.clone() for k, v in gr.items()}
+            accd = d.grad.clone()
+        else:
+            for k in acc:
+                acc[k] += gr[k]
+            accd += d.grad
+    # parameters are shared by both replicas: gradients add up
+    for key in ("q", "sigma", "eps"):
+        ref = acc[key]
+        scale = float(ref.abs().max())
+        assert torch.allclose(g[key], ref, rtol=GRAD_REL_TOL, atol=1e-4 * scale), key
+    scale = float(accd.abs().max())
+    assert torch.allclose(g["d"], accd, rtol=GRAD_REL_TOL, atol=1e-4 * scale)
+
+
+@pytest.mark.gpu
+def test_ti_dudlambda_chain_rule():
+    """dU/dlambda of the stand-in two-leg schedule (lambda2 = l, lambda1 =
+    l - 0.1 sin(pi l)) by autograd through the schedule vs finite differences."""
+    from openmm_sdm_plugin_gb300.autograd import SDMEngine, sdm_potential
+    s = _system()
+    eng = SDMEngine(s)
+    D = eng.D
+    f64 = dict(dtype=torch.float64)
+
+    def U_of(lam_value, grad=False):
+        lam = torch.tensor([lam_value], **f64, requires_grad=grad)
+        l2 = lam
+        l1 = lam - 0.1 * torch.sin(np.pi * lam)
+        a = torch.tensor([0.1], **f64)
+        u0 = torch.tensor([110.0], **f64)
+        w0 = torch.tensor([0.0], **f64)
+        U = sdm_potential(eng, torch.tensor(s.positions, **f64), torch.tensor(s.charge[D], **f64),
+                          torch.tensor(s.sigma[D], **f64), torch.tensor(s.epsilon[D], **f64),
+                          torch.tensor(s.displacement, **f64), l1, l2, a, u0, w0)
+        return U, lam
+
+    U, lam = U_of(0.37, grad=True)
+    U.sum().backward()
+    h = 1e-5
+    fd = (float(U_of(0.37 + h)[0]) - float(U_of(0.37 - h)[0])) / (2 * h)
+    eng.close()
+    assert float(lam.grad) == pytest.approx(fd, rel=1e-6, abs=1e-6)
