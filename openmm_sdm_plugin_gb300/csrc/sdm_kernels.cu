@@ -626,8 +626,14 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
                 const float gz = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
                 pass = gx * gx + gy * gy + gz * gz < rclc2;
                 const bool nm = (J == I) || lk.x == -2 || lk.x == I || lk.y == I || lk.z == I || lk.w == I;
-                en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(Sx), __float_as_int(Sy),
-                               __float_as_int(sz));
+                // every particle of J lies within rc of I's box with 1e-3 nm to
+                // spare: the per-particle box test of the pair kernel is skipped
+                const float mx = fabsf(dx) + bh.x + hjb.x, my = fabsf(dy) + bh.y + hjb.y,
+                            mz = fabsf(dz) + bh.z + hjb.z;
+                const float rin = S.rcl - 1.0e-3f;
+                const bool full = !IMG && (mx * mx + my * my + mz * mz < rin * rin);
+                en = make_int4(J | (nm ? (int)0x80000000 : 0) | (full ? 0x40000000 : 0), __float_as_int(Sx),
+                               __float_as_int(Sy), __float_as_int(sz));
             }
             const unsigned bal = __ballot_sync(0xffffffffu, pass);
             if (pass) {
@@ -662,13 +668,16 @@ __global__ void __launch_bounds__(256) k_jlist(SdmArgs a, const int* cl_prefix) 
 // One tile: every lane owns one j of the ring window [head, head+count) and
 // sweeps the 8 i-particles of the cluster (warp-uniform i).  LJ = false is the
 // ring of j with epsilon = 0: Lennard-Jones vanishes for every i, Coulomb only.
-template <int MODE, bool IMG, bool LJ>
+// FAST: a full tile (32 entries) whose entries all carry the plain valid-i
+// mask, outside image mode: out-of-range and invalid-i pairs fail r2 < rc2 on
+// their own, so neither mask bits nor guards are evaluated.
+template <int MODE, bool IMG, bool LJ, bool FAST>
 __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
                                           const Ring& rg, const float4* ip, unsigned head, int count,
                                           ICluster& ic, float& ef, long long& npair) {
     const int lane = lane_id();
     const unsigned idx = (head + lane) & (SDM_RING - 1);
-    const bool active = lane < count;
+    const bool active = FAST || lane < count;
     // inactive lanes use zeros, never stale ring contents
     const float4 A = active ? rg.a[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 B = active ? rg.b[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -688,12 +697,12 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
             dz = img32(dz, S.Lf[2], S.invLf[2]);
         }
         const float r2 = r2_chain(dx, dy, dz);
-        const bool ok = (r2 < rc2) && ((m >> t) & 1u);
+        const bool ok = FAST ? (r2 < rc2) : ((r2 < rc2) && ((m >> t) & 1u));
         if (MODE == MODE_COUNT) {
             cnt += ok ? 1 : 0;
             continue;
         }
-        const float r2s = ok ? r2 : 1.0f;
+        const float r2s = (FAST || ok) ? r2 : 1.0f;
         const float ir = fast_rsqrt(r2s);
         const float ir2 = ir * ir;
         const float4 pi = ip[t];   // same address in every lane: one broadcast
@@ -724,10 +733,18 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
     } else if (active) {
         const int slot = __float_as_int(B.w);
         const size_t gsl = (size_t)R.slot_win + slot;
-        if (!(fmaxf(fabsf(fjx), fmaxf(fabsf(fjy), fabsf(fjz))) < 1.0e9f)) atomicOr(a.status, SDM_DEV_FORCE_OVERFLOW);
-        atomicAdd(a.F0x + gsl, fix64(fjx));
-        atomicAdd(a.F0y + gsl, fix64(fjy));
-        atomicAdd(a.F0z + gsl, fix64(fjz));
+        const float fm = fmaxf(fabsf(fjx), fmaxf(fabsf(fjy), fabsf(fjz)));
+        if (fm < 32768.0f) {
+            // 2^16-scaled 32-bit conversion, sign-extended into the 2^32 accumulator
+            atomicAdd(a.F0x + gsl, (unsigned long long)((long long)__float2int_rn(fjx * 65536.0f) * 65536LL));
+            atomicAdd(a.F0y + gsl, (unsigned long long)((long long)__float2int_rn(fjy * 65536.0f) * 65536LL));
+            atomicAdd(a.F0z + gsl, (unsigned long long)((long long)__float2int_rn(fjz * 65536.0f) * 65536LL));
+        } else {
+            if (!(fm < 1.0e9f)) atomicOr(a.status, SDM_DEV_FORCE_OVERFLOW);
+            atomicAdd(a.F0x + gsl, fix64(fjx));
+            atomicAdd(a.F0y + gsl, fix64(fjy));
+            atomicAdd(a.F0z + gsl, fix64(fjz));
+        }
         ef += e;
     }
 }
@@ -807,7 +824,7 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         auto issue = [&](int g) {
             const int e = 4 * g + q;
             if (e < nch) {
-                const int sj = 8 * (sm.jc[e].x & 0x7fffffff) + t;
+                const int sj = 8 * (sm.jc[e].x & 0x3fffffff) + t;
                 cp_async16(&sm.sx[g % SDM_NST][lane], a.clX + R.slot_win + sj);
                 cp_async8(&sm.sp[g % SDM_NST][lane], a.clP + R.slot_win + sj);
             }
@@ -832,25 +849,30 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
                 const int4 en = sm.jc[e];
                 X4 = sm.sx[g % SDM_NST][lane];
                 P = sm.sp[g % SDM_NST][lane];
-                const int J = en.x & 0x7fffffff;
+                const int J = en.x & 0x3fffffff;
                 const bool nm = en.x < 0;
+                const bool full = (en.x & 0x40000000) != 0;
                 sj = 8 * J + t;
                 xs = __fadd_rn(X4.x, __int_as_float(en.y));
                 ys = __fadd_rn(X4.y, __int_as_float(en.z));
                 zs = __fadd_rn(X4.z, __int_as_float(en.w));
-                float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
-                if (IMG) {
-                    tx = img32(tx, S.Lf[0], S.invLf[0]);
-                    ty = img32(ty, S.Lf[1], S.invLf[1]);
-                    tz = img32(tz, S.Lf[2], S.invLf[2]);
+                if (full) {
+                    pass = X4.x < 1.0e5f;   // only the padding test
+                } else {
+                    float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
+                    if (IMG) {
+                        tx = img32(tx, S.Lf[0], S.invLf[0]);
+                        ty = img32(ty, S.Lf[1], S.invLf[1]);
+                        tz = img32(tz, S.Lf[2], S.invLf[2]);
+                    }
+                    const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
+                    const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
+                    const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
+                    // padding slots carry 1e6 coordinates: they fail the box test
+                    // unless image mode wraps them back, hence the explicit test there
+                    pass = r2_chain(ex, ey, ez) < rcl2;
+                    if (IMG) pass = pass && (X4.x < 1.0e5f);
                 }
-                const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
-                const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
-                const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
-                // padding slots carry 1e6 coordinates: they fail the box test
-                // unless image mode wraps them back, hence the explicit test there
-                pass = r2_chain(ex, ey, ez) < rcl2;
-                if (IMG) pass = pass && (X4.x < 1.0e5f);
                 if (pass) {
                     m = j_mask(a, S, R, I, J, sj, vmask, nm);
                     pass = m != 0u;
@@ -868,29 +890,29 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
                 continue;
             }
             const bool lj = pass && P.y != 0.0f;
-            const bool co = pass && P.y == 0.0f;
+            const unsigned bp = __ballot_sync(0xffffffffu, pass);
             const unsigned bl = __ballot_sync(0xffffffffu, lj);
-            const unsigned bco = __ballot_sync(0xffffffffu, co);
-            const unsigned lt = (1u << lane) - 1u;
-            if (lj) {
-                const unsigned idx = (tl + __popc(bl & lt)) & (SDM_RING - 1);
-                sm.lj.a[idx] = make_float4(xs, ys, zs, X4.w);
-                sm.lj.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
-            }
-            if (co) {
-                const unsigned idx = (tc + __popc(bco & lt)) & (SDM_RING - 1);
-                sm.co.a[idx] = make_float4(xs, ys, zs, X4.w);
-                sm.co.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
+            const unsigned bco = bp & ~bl;
+            if (pass) {
+                const unsigned lt = (1u << lane) - 1u;
+                Ring& rg = lj ? sm.lj : sm.co;
+                const unsigned idx = ((lj ? tl : tc) + __popc((lj ? bl : bco) & lt)) & (SDM_RING - 1);
+                rg.a[idx] = make_float4(xs, ys, zs, X4.w);
+                rg.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
             }
             tl += __popc(bl);
             tc += __popc(bco);
             __syncwarp();
             if (tl - hl >= 32u) {
-                eval_tile<MODE, IMG, true>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
+                const bool plain = !IMG && __all_sync(0xffffffffu, __float_as_uint(sm.lj.b[(hl + lane) & (SDM_RING - 1)].z) == vmask);
+                if (plain) eval_tile<MODE, IMG, true, true>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
+                else eval_tile<MODE, IMG, true, false>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
                 hl += 32u;
             }
             if (tc - hc >= 32u) {
-                eval_tile<MODE, IMG, false>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
+                const bool plain = !IMG && __all_sync(0xffffffffu, __float_as_uint(sm.co.b[(hc + lane) & (SDM_RING - 1)].z) == vmask);
+                if (plain) eval_tile<MODE, IMG, false, true>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
+                else eval_tile<MODE, IMG, false, false>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
                 hc += 32u;
             }
             __syncwarp();
@@ -904,8 +926,8 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         }
         return;
     }
-    if (tl != hl) eval_tile<MODE, IMG, true>(a, S, R, sm.lj, sm.ip, hl, (int)(tl - hl), ic, ef, npair);
-    if (tc != hc) eval_tile<MODE, IMG, false>(a, S, R, sm.co, sm.ip, hc, (int)(tc - hc), ic, ef, npair);
+    if (tl != hl) eval_tile<MODE, IMG, true, false>(a, S, R, sm.lj, sm.ip, hl, (int)(tl - hl), ic, ef, npair);
+    if (tc != hc) eval_tile<MODE, IMG, false, false>(a, S, R, sm.co, sm.ip, hc, (int)(tc - hc), ic, ef, npair);
     if (MODE == MODE_COUNT) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) npair += __shfl_xor_sync(0xffffffffu, npair, o);
