@@ -38,6 +38,7 @@ struct SysHost {
     int n;
     std::vector<float> q, hs, se;
     std::vector<int> grp;
+    std::vector<int> mol;       // exclusion component id
     std::vector<double> d;      // 3n
     std::vector<int> excl_off;  // n+1 (local)
     std::vector<int> excl_idx;
@@ -45,6 +46,7 @@ struct SysHost {
     std::vector<int> cx_off;    // nD+1 (local)
     std::vector<int> cx_idx;
     std::vector<int2> hst, fst;  // owner / full column stencils
+    bool clique = false;
     SdmSys dev;
     int replicas;
 };
@@ -202,10 +204,33 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
         s.excl_idx.insert(s.excl_idx.end(), v.begin(), v.end());
         s.excl_off[i + 1] = (int)s.excl_idx.size();
     }
+    // exclusion components: when each is a clique, "excluded" is "same component"
+    s.mol.resize(n);
+    {
+        std::vector<int> par(n);
+        for (int i = 0; i < n; ++i) par[i] = i;
+        auto root = [&](int x) { while (par[x] != x) { par[x] = par[par[x]]; x = par[x]; } return x; };
+        for (int i = 0; i < n; ++i)
+            for (int k = s.excl_off[i]; k < s.excl_off[i + 1]; ++k) {
+                const int a = root(i), b = root(s.excl_idx[k]);
+                if (a != b) par[std::max(a, b)] = std::min(a, b);
+            }
+        std::vector<long long> size(n, 0), edges(n, 0);
+        for (int i = 0; i < n; ++i) {
+            s.mol[i] = root(i);
+            size[s.mol[i]] += 1;
+            edges[s.mol[i]] += s.excl_off[i + 1] - s.excl_off[i];  // each edge twice
+        }
+        bool clique = true;
+        for (int i = 0; i < n && clique; ++i)
+            if (size[i] > 0 && edges[i] != size[i] * (size[i] - 1)) clique = false;
+        s.clique = clique;
+    }
     // grid
     SdmSys& g = s.dev;
     std::memset(&g, 0, sizeof g);
     g.n = n;
+    g.excl_clique = s.clique ? 1 : 0;
     const double vol = d.box[0] * d.box[1] * d.box[2];
     const double side = std::cbrt(8.0 * vol / n);
     for (int k = 0; k < 3; ++k) {
@@ -306,7 +331,7 @@ sdm_status upload_topology(sdm_handle* h) {
     // rebuilds the per-particle topology arrays of every system (after a
     // displacement change) in the arena
     std::vector<float> q, hs, se;
-    std::vector<int> grp, eoff, eidx, D, cxo, cxi;
+    std::vector<int> grp, mol, eoff, eidx, D, cxo, cxi;
     std::vector<double> dd;
     std::vector<float> tab;
     std::vector<int2> sten;
@@ -324,6 +349,7 @@ sdm_status upload_topology(sdm_handle* h) {
         hs.insert(hs.end(), s.hs.begin(), s.hs.end());
         se.insert(se.end(), s.se.begin(), s.se.end());
         grp.insert(grp.end(), s.grp.begin(), s.grp.end());
+        mol.insert(mol.end(), s.mol.begin(), s.mol.end());
         dd.insert(dd.end(), s.d.begin(), s.d.end());
         for (int i = 0; i < s.n; ++i) eoff.push_back(excl + s.excl_off[i]);
         eidx.insert(eidx.end(), s.excl_idx.begin(), s.excl_idx.end());
@@ -363,6 +389,7 @@ sdm_status upload_topology(sdm_handle* h) {
     if ((st = put(a.topo_hs, hs.data(), hs.size() * 4))) return st;
     if ((st = put(a.topo_se, se.data(), se.size() * 4))) return st;
     if ((st = put(a.topo_grp, grp.data(), grp.size() * 4))) return st;
+    if ((st = put(a.topo_mol, mol.data(), mol.size() * 4))) return st;
     if ((st = put(a.topo_d, dd.data(), dd.size() * 8))) return st;
     if ((st = put(a.excl_off, eoff.data(), eoff.size() * 4))) return st;
     if ((st = put(a.excl_idx, eidx.data(), eidx.size() * 4))) return st;
@@ -588,6 +615,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_rep = ar.take<SdmRep>(nrep);
     const size_t o_q = ar.take<float>(tot_n), o_hs = ar.take<float>(tot_n), o_se = ar.take<float>(tot_n);
     const size_t o_grp = ar.take<int>(tot_n), o_d = ar.take<double>(3LL * tot_n);
+    const size_t o_mol = ar.take<int>(tot_n);
     const size_t o_eoff = ar.take<int>(tot_n + 1), o_eidx = ar.take<int>(std::max(tot_excl, 1));
     const size_t o_D = ar.take<int>(std::max(tot_D, 1)), o_cxo = ar.take<int>(tot_cx + 1);
     const size_t o_cxi = ar.take<int>(tot_cxidx), o_tab = ar.take<float>(tot_tab);
@@ -603,6 +631,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_aoff = ar.take<int>(Ccol), o_cl = ar.take<int>(Ccol);
     const size_t o_perm = ar.take<int>(Sl), o_clX = ar.take<float4>(Sl), o_clP = ar.take<float2>(Sl);
     const size_t o_sgrp = ar.take<int>(Sl), o_ex4 = ar.take<int4>(Sl);
+    const size_t o_clm = ar.take<int>(Sl);
     const size_t o_F = ar.take<unsigned long long>(6 * Sl);
     const size_t o_ref = ar.take<int4>(Cl), o_bbc = ar.take<float4>(Cl), o_bbh = ar.take<float4>(Cl);
     const size_t o_lnk = ar.take<int4>(Cl), o_ep = ar.take<double>(Cl * SDM_MAX_SPLIT);
@@ -630,6 +659,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.topo_hs = at<float>(B, o_hs);
     a.topo_se = at<float>(B, o_se);
     a.topo_grp = at<int>(B, o_grp);
+    a.topo_mol = at<int>(B, o_mol);
     a.topo_d = at<double>(B, o_d);
     a.excl_off = at<int>(B, o_eoff);
     a.excl_idx = at<int>(B, o_eidx);
@@ -659,6 +689,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.clP = at<float2>(B, o_clP);
     a.grp = at<int>(B, o_sgrp);
     a.excl4 = at<int4>(B, o_ex4);
+    a.clM = at<int>(B, o_clm);
     unsigned long long* F = at<unsigned long long>(B, o_F);
     a.F0x = F; a.F0y = F + Sl; a.F0z = F + 2 * Sl;
     a.dFx = F + 3 * Sl; a.dFy = F + 4 * Sl; a.dFz = F + 5 * Sl;

@@ -363,6 +363,7 @@ __global__ void k_clusters(SdmArgs a) {
         a.clX[gs] = q4;
         a.clP[gs] = p2;
         a.grp[gs] = g;
+        a.clM[gs] = (p >= 0) ? a.topo_mol[S.atom_base + p] : -1 - t;
         a.excl4[gs] = ex;
         // bounding box over valid slots
         float lo[3], hi[3];
@@ -446,16 +447,21 @@ struct Ring {                   // one tile ring: 64 prepared j entries
     float4 b[SDM_RING];         // (hs, se, mask bits, slot bits)
 };
 
-#define SDM_NST 3               // cp.async stages of candidate particle data
+#define SDM_CH 16               // cluster-pair list entries per staged chunk
 
+// Two-level cp.async pipeline: list entries two chunks ahead, the candidate
+// particles (8 per entry) one chunk ahead of the chunk being filtered.
 struct EvalSmem {
     Ring lj;                    // j with epsilon != 0
     Ring co;                    // j with epsilon == 0 (Coulomb only)
-    int4 jc[32];                // current chunk of the cluster-pair list
-    float4 sx[SDM_NST][32];     // staged cluster-local coordinates + charge of candidates
-    float2 sp[SDM_NST][32];     // staged (sigma/2, 2 sqrt(eps)) of candidates
+    int4 je[3][SDM_CH];         // list entries of chunks c, c+1, c+2
+    float4 sx[2][SDM_CH * 8];   // staged cluster-local coordinates + charge of candidates
+    float2 sp[2][SDM_CH * 8];   // staged (sigma/2, 2 sqrt(eps)) of candidates
+    int sm_[2][SDM_CH * 8];     // staged molecule ids of candidates
     float4 ip[8];               // i-cluster (q, sigma/2, 2 sqrt(eps), 0), read as broadcasts
+    int im[8];                  // i-cluster molecule ids
 };
+
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -465,6 +471,9 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
@@ -626,14 +635,8 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
                 const float gz = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
                 pass = gx * gx + gy * gy + gz * gz < rclc2;
                 const bool nm = (J == I) || lk.x == -2 || lk.x == I || lk.y == I || lk.z == I || lk.w == I;
-                // every particle of J lies within rc of I's box with 1e-3 nm to
-                // spare: the per-particle box test of the pair kernel is skipped
-                const float mx = fabsf(dx) + bh.x + hjb.x, my = fabsf(dy) + bh.y + hjb.y,
-                            mz = fabsf(dz) + bh.z + hjb.z;
-                const float rin = S.rcl - 1.0e-3f;
-                const bool full = !IMG && (mx * mx + my * my + mz * mz < rin * rin);
-                en = make_int4(J | (nm ? (int)0x80000000 : 0) | (full ? 0x40000000 : 0), __float_as_int(Sx),
-                               __float_as_int(Sy), __float_as_int(sz));
+                en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(Sx), __float_as_int(Sy),
+                               __float_as_int(sz));
             }
             const unsigned bal = __ballot_sync(0xffffffffu, pass);
             if (pass) {
@@ -668,16 +671,13 @@ __global__ void __launch_bounds__(256) k_jlist(SdmArgs a, const int* cl_prefix) 
 // One tile: every lane owns one j of the ring window [head, head+count) and
 // sweeps the 8 i-particles of the cluster (warp-uniform i).  LJ = false is the
 // ring of j with epsilon = 0: Lennard-Jones vanishes for every i, Coulomb only.
-// FAST: a full tile (32 entries) whose entries all carry the plain valid-i
-// mask, outside image mode: out-of-range and invalid-i pairs fail r2 < rc2 on
-// their own, so neither mask bits nor guards are evaluated.
-template <int MODE, bool IMG, bool LJ, bool FAST>
+template <int MODE, bool IMG, bool LJ>
 __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
                                           const Ring& rg, const float4* ip, unsigned head, int count,
                                           ICluster& ic, float& ef, long long& npair) {
     const int lane = lane_id();
     const unsigned idx = (head + lane) & (SDM_RING - 1);
-    const bool active = FAST || lane < count;
+    const bool active = lane < count;
     // inactive lanes use zeros, never stale ring contents
     const float4 A = active ? rg.a[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 B = active ? rg.b[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -697,12 +697,12 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
             dz = img32(dz, S.Lf[2], S.invLf[2]);
         }
         const float r2 = r2_chain(dx, dy, dz);
-        const bool ok = FAST ? (r2 < rc2) : ((r2 < rc2) && ((m >> t) & 1u));
+        const bool ok = (r2 < rc2) && ((m >> t) & 1u);
         if (MODE == MODE_COUNT) {
             cnt += ok ? 1 : 0;
             continue;
         }
-        const float r2s = (FAST || ok) ? r2 : 1.0f;
+        const float r2s = ok ? r2 : 1.0f;
         const float ir = fast_rsqrt(r2s);
         const float ir2 = ir * ir;
         const float4 pi = ip[t];   // same address in every lane: one broadcast
@@ -733,18 +733,10 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
     } else if (active) {
         const int slot = __float_as_int(B.w);
         const size_t gsl = (size_t)R.slot_win + slot;
-        const float fm = fmaxf(fabsf(fjx), fmaxf(fabsf(fjy), fabsf(fjz)));
-        if (fm < 32768.0f) {
-            // 2^16-scaled 32-bit conversion, sign-extended into the 2^32 accumulator
-            atomicAdd(a.F0x + gsl, (unsigned long long)((long long)__float2int_rn(fjx * 65536.0f) * 65536LL));
-            atomicAdd(a.F0y + gsl, (unsigned long long)((long long)__float2int_rn(fjy * 65536.0f) * 65536LL));
-            atomicAdd(a.F0z + gsl, (unsigned long long)((long long)__float2int_rn(fjz * 65536.0f) * 65536LL));
-        } else {
-            if (!(fm < 1.0e9f)) atomicOr(a.status, SDM_DEV_FORCE_OVERFLOW);
-            atomicAdd(a.F0x + gsl, fix64(fjx));
-            atomicAdd(a.F0y + gsl, fix64(fjy));
-            atomicAdd(a.F0z + gsl, fix64(fjz));
-        }
+        if (!(fmaxf(fabsf(fjx), fmaxf(fabsf(fjy), fabsf(fjz))) < 1.0e9f)) atomicOr(a.status, SDM_DEV_FORCE_OVERFLOW);
+        atomicAdd(a.F0x + gsl, fix64(fjx));
+        atomicAdd(a.F0y + gsl, fix64(fjy));
+        atomicAdd(a.F0z + gsl, fix64(fjz));
         ef += e;
     }
 }
@@ -789,7 +781,10 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         float2 pi2 = make_float2(0.f, 0.f);
         if (lane < 8) { xi4 = a.clX[slot0 + lane]; pi2 = a.clP[slot0 + lane]; }
         __syncwarp();
-        if (lane < 8) sm.ip[lane] = make_float4(xi4.w, pi2.x, pi2.y, 0.0f);
+        if (lane < 8) {
+            sm.ip[lane] = make_float4(xi4.w, pi2.x, pi2.y, 0.0f);
+            sm.im[lane] = a.clM[slot0 + lane];
+        }
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
             ic.x[t] = __shfl_sync(0xffffffffu, xi4.x, t);
@@ -813,32 +808,50 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
     int emit_n = 0;
     const int t = lane & 7, q = lane >> 3;
 
-    for (int c0 = ebeg; c0 < eend; c0 += 32) {
-        // chunk of up to 32 list entries: one coalesced load, kept in shared memory
-        const int nch = min(32, eend - c0);
-        __syncwarp();
-        sm.jc[lane] = (lane < nch) ? jl[c0 + lane] : make_int4(0, 0, 0, 0);
-        __syncwarp();
-        const int ngr = (nch + 3) >> 2;
-        // lane (q, t) stages particle t of entry 4g+q of group g
-        auto issue = [&](int g) {
-            const int e = 4 * g + q;
-            if (e < nch) {
-                const int sj = 8 * (sm.jc[e].x & 0x3fffffff) + t;
-                cp_async16(&sm.sx[g % SDM_NST][lane], a.clX + R.slot_win + sj);
-                cp_async8(&sm.sp[g % SDM_NST][lane], a.clP + R.slot_win + sj);
-            }
-        };
-#pragma unroll
-        for (int g = 0; g < SDM_NST - 1; ++g) {
-            if (g < ngr) issue(g);
-            cp_async_commit();
+    const int nent = eend - ebeg;
+    const int nchunk = (nent + SDM_CH - 1) / SDM_CH;
+    // lanes 0..15 copy one list entry each
+    auto issue_entries = [&](int c) {
+        if (c < nchunk && lane < SDM_CH) {
+            const int e = ebeg + c * SDM_CH + lane;
+            if (e < eend) cp_async16(&sm.je[c % 3][lane], jl + e);
         }
-        for (int g = 0; g < ngr; ++g) {
-            if (g + SDM_NST - 1 < ngr) issue(g + SDM_NST - 1);
-            cp_async_commit();
-            cp_async_wait<SDM_NST - 1>();   // this lane's copies of group g have landed
-            const int e = 4 * g + q;
+    };
+    // 128 candidate particles of chunk c: lane copies particles lane, lane+32, lane+64, lane+96
+    auto issue_atoms = [&](int c) {
+        if (c >= nchunk) return;
+        const int nch = min(SDM_CH, eend - (ebeg + c * SDM_CH));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int idx = lane + 32 * k;
+            const int e = idx >> 3;
+            if (e < nch) {
+                const int sj = 8 * (sm.je[c % 3][e].x & 0x7fffffff) + (idx & 7);
+                cp_async16(&sm.sx[c & 1][idx], a.clX + R.slot_win + sj);
+                cp_async8(&sm.sp[c & 1][idx], a.clP + R.slot_win + sj);
+                if (S.excl_clique) cp_async4(&sm.sm_[c & 1][idx], a.clM + R.slot_win + sj);
+            }
+        }
+    };
+    issue_entries(0);
+    cp_async_commit();
+    issue_entries(1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
+    issue_atoms(0);
+    cp_async_commit();
+    for (int c = 0; c < nchunk; ++c) {
+        issue_entries(c + 2);
+        cp_async_commit();
+        cp_async_wait<1>();   // entries of c+1 and particles of c have landed (this lane)
+        __syncwarp();         // ... and for every lane
+        issue_atoms(c + 1);
+        cp_async_commit();
+        const int nch = min(SDM_CH, eend - (ebeg + c * SDM_CH));
+        for (int g = 0; g < SDM_CH / 4; ++g) {
+            const int e = 4 * g + q;   // entry of this lane's 8-lane group
+            if (4 * g >= nch) break;   // uniform
             bool pass = false;
             float xs = 0.f, ys = 0.f, zs = 0.f;
             int sj = 0;
@@ -846,35 +859,42 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
             float4 X4 = make_float4(0.f, 0.f, 0.f, 0.f);
             float2 P = make_float2(0.f, 0.f);
             if (e < nch) {
-                const int4 en = sm.jc[e];
-                X4 = sm.sx[g % SDM_NST][lane];
-                P = sm.sp[g % SDM_NST][lane];
-                const int J = en.x & 0x3fffffff;
+                const int4 en = sm.je[c % 3][e];
+                X4 = sm.sx[c & 1][8 * e + t];
+                P = sm.sp[c & 1][8 * e + t];
+                const int J = en.x & 0x7fffffff;
                 const bool nm = en.x < 0;
-                const bool full = (en.x & 0x40000000) != 0;
                 sj = 8 * J + t;
                 xs = __fadd_rn(X4.x, __int_as_float(en.y));
                 ys = __fadd_rn(X4.y, __int_as_float(en.z));
                 zs = __fadd_rn(X4.z, __int_as_float(en.w));
-                if (full) {
-                    pass = X4.x < 1.0e5f;   // only the padding test
-                } else {
-                    float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
-                    if (IMG) {
-                        tx = img32(tx, S.Lf[0], S.invLf[0]);
-                        ty = img32(ty, S.Lf[1], S.invLf[1]);
-                        tz = img32(tz, S.Lf[2], S.invLf[2]);
-                    }
-                    const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
-                    const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
-                    const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
-                    // padding slots carry 1e6 coordinates: they fail the box test
-                    // unless image mode wraps them back, hence the explicit test there
-                    pass = r2_chain(ex, ey, ez) < rcl2;
-                    if (IMG) pass = pass && (X4.x < 1.0e5f);
+                float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
+                if (IMG) {
+                    tx = img32(tx, S.Lf[0], S.invLf[0]);
+                    ty = img32(ty, S.Lf[1], S.invLf[1]);
+                    tz = img32(tz, S.Lf[2], S.invLf[2]);
                 }
+                const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
+                const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
+                const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
+                // padding slots carry 1e6 coordinates: they fail the box test
+                // unless image mode wraps them back, hence the explicit test there
+                pass = r2_chain(ex, ey, ez) < rcl2;
+                if (IMG) pass = pass && (X4.x < 1.0e5f);
                 if (pass) {
-                    m = j_mask(a, S, R, I, J, sj, vmask, nm);
+                    if (S.excl_clique) {
+                        // excluded <=> same molecule: compare with the 8 i ids
+                        m = vmask;
+                        if (nm) {
+                            if (J == I) m &= (1u << t) - 1u;
+                            const int mj = sm.sm_[c & 1][8 * e + t];
+#pragma unroll
+                            for (int u = 0; u < 8; ++u)
+                                if (sm.im[u] == mj) m &= ~(1u << u);
+                        }
+                    } else {
+                        m = j_mask(a, S, R, I, J, sj, vmask, nm);
+                    }
                     pass = m != 0u;
                 }
             }
@@ -890,35 +910,36 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
                 continue;
             }
             const bool lj = pass && P.y != 0.0f;
-            const unsigned bp = __ballot_sync(0xffffffffu, pass);
+            const bool co = pass && P.y == 0.0f;
             const unsigned bl = __ballot_sync(0xffffffffu, lj);
-            const unsigned bco = bp & ~bl;
-            if (pass) {
-                const unsigned lt = (1u << lane) - 1u;
-                Ring& rg = lj ? sm.lj : sm.co;
-                const unsigned idx = ((lj ? tl : tc) + __popc((lj ? bl : bco) & lt)) & (SDM_RING - 1);
-                rg.a[idx] = make_float4(xs, ys, zs, X4.w);
-                rg.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
+            const unsigned bco = __ballot_sync(0xffffffffu, co);
+            const unsigned lt = (1u << lane) - 1u;
+            if (lj) {
+                const unsigned idx = (tl + __popc(bl & lt)) & (SDM_RING - 1);
+                sm.lj.a[idx] = make_float4(xs, ys, zs, X4.w);
+                sm.lj.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
+            }
+            if (co) {
+                const unsigned idx = (tc + __popc(bco & lt)) & (SDM_RING - 1);
+                sm.co.a[idx] = make_float4(xs, ys, zs, X4.w);
+                sm.co.b[idx] = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(sj));
             }
             tl += __popc(bl);
             tc += __popc(bco);
             __syncwarp();
             if (tl - hl >= 32u) {
-                const bool plain = !IMG && __all_sync(0xffffffffu, __float_as_uint(sm.lj.b[(hl + lane) & (SDM_RING - 1)].z) == vmask);
-                if (plain) eval_tile<MODE, IMG, true, true>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
-                else eval_tile<MODE, IMG, true, false>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
+                eval_tile<MODE, IMG, true>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
                 hl += 32u;
             }
             if (tc - hc >= 32u) {
-                const bool plain = !IMG && __all_sync(0xffffffffu, __float_as_uint(sm.co.b[(hc + lane) & (SDM_RING - 1)].z) == vmask);
-                if (plain) eval_tile<MODE, IMG, false, true>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
-                else eval_tile<MODE, IMG, false, false>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
+                eval_tile<MODE, IMG, false>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
                 hc += 32u;
             }
             __syncwarp();
         }
-        cp_async_wait<0>();
     }
+    cp_async_wait<0>();
+    __syncwarp();
     if (MODE == MODE_EMIT) {
         if (lane == 0 && part == 0) {
             a.ex_cnt[I] = emit_n;
@@ -926,8 +947,8 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         }
         return;
     }
-    if (tl != hl) eval_tile<MODE, IMG, true, false>(a, S, R, sm.lj, sm.ip, hl, (int)(tl - hl), ic, ef, npair);
-    if (tc != hc) eval_tile<MODE, IMG, false, false>(a, S, R, sm.co, sm.ip, hc, (int)(tc - hc), ic, ef, npair);
+    if (tl != hl) eval_tile<MODE, IMG, true>(a, S, R, sm.lj, sm.ip, hl, (int)(tl - hl), ic, ef, npair);
+    if (tc != hc) eval_tile<MODE, IMG, false>(a, S, R, sm.co, sm.ip, hc, (int)(tc - hc), ic, ef, npair);
     if (MODE == MODE_COUNT) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) npair += __shfl_xor_sync(0xffffffffu, npair, o);

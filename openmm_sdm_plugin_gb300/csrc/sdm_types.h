@@ -23,6 +23,7 @@
 //     clP      float2  sigma/2, 2 sqrt(eps)
 //     grp      int     displacement group of the slot's particle
 //     excl4    int4    up to 4 exclusion partners as slots (-1 none, -2 overflow)
+//     clM      int     molecule (exclusion component) id of the slot's particle
 //     F0x/F0y/F0z, dFx/dFy/dFz   int64 fixed point 2^32
 //   per replica, cluster-indexed (window = slot_cap/8)
 //     jl       int4[jl_cap]  cluster-pair list of the i-cluster, jl_cnt entries
@@ -62,6 +63,7 @@ struct SdmSys {
     int cx_base;      // offset into cx_off/cx_idx (changed-pair exclusions per displaced particle)
     int half_geo;     // 1: pairs of columns are owned through the forward half stencil
                       // (offset ox>0, or ox==0 and oy>0; own column J>=I); 0: by lower column id
+    int excl_clique;  // 1: every exclusion component is a clique (excluded <=> same molecule id)
     int hst_base, hst_count;  // owner stencil (int2 column offsets), own column first
     int fst_base, fst_count;  // full stencil for point queries
 };
@@ -88,6 +90,7 @@ struct SdmArgs {
     const float* topo_hs;
     const float* topo_se;
     const int* topo_grp;
+    const int* topo_mol;  // exclusion component (molecule) id
     const double* topo_d;
     const int* excl_off;
     const int* excl_idx;
@@ -116,6 +119,7 @@ struct SdmArgs {
     float2* clP;
     int* grp;
     int4* excl4;
+    int* clM;            // per slot: molecule id (clique exclusion mode)
     unsigned long long* F0x;
     unsigned long long* F0y;
     unsigned long long* F0z;

@@ -8,6 +8,8 @@ Two oracle rules are used (see oracle/sdm_oracle.c):
                   is below the cutoff): u within 5e-3 kJ/mol, forces within
                   1e-4 rms relative.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -259,3 +261,36 @@ def test_sdmforce_api_end_to_end():
     f.setSoftCoreMethod(9)
     with pytest.raises(capi.SdmError):
         f.evaluate(s.positions[0])
+
+
+def _nonclique(s):
+    """config1 with extra exclusions that make the exclusion graph non-clique:
+    each water oxygen excluded with the next water's oxygen (one chain through
+    the solvent), and each ligand particle with one solvent oxygen."""
+    nw = (s.n - 80) // 3
+    o = np.arange(nw - 1) * 3
+    lig = np.arange(s.n - 80, s.n)
+    extra = [np.stack([o, o + 3], 1), np.stack([(np.arange(80) * 97 % nw) * 3, lig], 1)]
+    excl = np.concatenate([s.exclusions] + extra).astype(np.int32)
+    return dataclasses.replace(s, name=s.name + "-nonclique", exclusions=excl)
+
+
+def test_nonclique_exclusions_parity():
+    s = _nonclique(S.config1())
+    h = _handle([s])
+    x = s.positions[0]
+    res, F = h.evaluate(x)
+    F0, F1 = h.state_forces()
+    _check_replica(s, x, res[0], F, F0, F1, h.grid(0))
+    c = h.count_pairs(x)
+    a = oracle.OracleSystem(s).f32rule(x, h.grid(0))
+    assert int(c[0, 0]) == a["P0"]
+    assert int(c[0, 1]) == a["P1delta"]
+    g = h.export_lists(0, x)
+    ol = oracle.OracleSystem(s).lists(x, h.grid(0))
+    assert np.array_equal(g["cnt"], ol["cnt"])
+    for I in range(g["ncl"]):
+        k = g["cnt"][I]
+        order = np.argsort(g["slot"][I, :k], kind="stable")
+        assert np.array_equal(g["slot"][I, :k][order], ol["slot"][I, :k])
+        assert np.array_equal(g["mask"][I, :k][order], ol["mask"][I, :k])
