@@ -378,6 +378,7 @@ def main():
                    "replicas_per_gpu": NREP, "particles": n, "l2": "flushed (256 MB write) before every timed step",
                    "parallelism": f"replicas only, {world} independent rank(s)",
                    "schedule": {"split": h.get_option(capi.OPT_SPLIT), "ctas_per_sm": h.get_option(capi.OPT_CTAS_PER_SM),
+                                "ctas_resident": h.get_option(capi.OPT_PAIR_RESIDENT),
                                 "autotuned": tuned is not None}},
         "plain": {"value": plain, "unit": UNIT, "ms_per_call": sum(ms_p) / len(ms_p),
                   "workload": "config1: one 22,580-particle replica per call (CUDA graph)"},

@@ -187,8 +187,11 @@ enum {
     SDM_OPT_PROFILE = 1,      /* 1 = time every kernel with CUDA events (eager launches);
                                  2 = record the same events inside the replayed graph */
     SDM_OPT_SPLIT = 2,        /* work items per i-cluster in the pair kernel (1,2,4) */
-    SDM_OPT_CTAS_PER_SM = 3,  /* persistent pair-kernel CTAs per SM (1..8) */
-    SDM_OPT_VERIFY = 4        /* 1 = sdm_evaluate checks the device status word after each call */
+    SDM_OPT_CTAS_PER_SM = 3,  /* persistent pair-kernel CTAs per SM (1..4, default 4); the launch
+                                 never exceeds the CTAs that fit (SDM_OPT_PAIR_RESIDENT) */
+    SDM_OPT_VERIFY = 4,       /* 1 = sdm_evaluate checks the device status word after each call */
+    SDM_OPT_PAIR_RESIDENT = 5 /* read only: pair-kernel CTAs per SM that are resident for the
+                                 current SDM_OPT_CTAS_PER_SM (occupancy calculator) */
 };
 sdm_status sdm_set_option(sdm_handle* h, int option, int value);
 sdm_status sdm_get_option(const sdm_handle* h, int option, int* value);

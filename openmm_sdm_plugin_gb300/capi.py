@@ -32,7 +32,7 @@ RESULT_FIELDS = ("U0", "U1", "u", "BindE", "fp", "W", "dW", "s", "E_pot", "dWdla
 (R_U0, R_U1, R_U, R_BINDE, R_FP, R_W, R_DW, R_S, R_EPOT, R_DWDL, R_L1, R_L2, R_U0P, R_W0P,
  R_STATUS, R_NCL) = range(16)
 
-OPT_GRAPH, OPT_PROFILE, OPT_SPLIT, OPT_CTAS_PER_SM, OPT_VERIFY = range(5)
+OPT_GRAPH, OPT_PROFILE, OPT_SPLIT, OPT_CTAS_PER_SM, OPT_VERIFY, OPT_PAIR_RESIDENT = range(6)
 
 EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_set_displacement", "sdm_set_params", "sdm_evaluate", "sdm_evaluate_device",

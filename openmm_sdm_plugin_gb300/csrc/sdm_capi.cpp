@@ -22,8 +22,11 @@
 cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* cl_prefix, int* done, cudaStream_t st,
                             cudaEvent_t* ev, int nev, unsigned ev_flags);
 cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_t st);
+cudaError_t sdm_pair_prepare();
+#define SDM_MAX_CTAS 4  // pair-kernel CTAs per SM with a built register bound
+int sdm_pair_resident(int ctas_per_sm);
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
-                            cudaStream_t st);
+                            int resident, cudaStream_t st);
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st);
@@ -106,6 +109,7 @@ struct sdm_handle {
     bool params_dirty = true;
     // options
     int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 4, opt_verify = 1;
+    int pair_res[SDM_MAX_CTAS + 1] = {};  // resident pair-kernel CTAs per SM by request
     // graphs
     std::map<GraphKey, cudaGraphExec_t> graphs;
     // profiling
@@ -419,7 +423,7 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->cl_prefix, h->done, st, ev, 6, fl));
     SDM_CUDA(h, sdm_launch_jlist(a, h->cl_prefix, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[6], st, fl));
-    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, st));
+    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[h->opt_ctas], st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
     if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[8], st, fl));
@@ -549,6 +553,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     }
     h->device = device;
     if (cudaSetDevice(device) != cudaSuccess) { delete h; return fail(nullptr, SDM_ERR_CUDA, "cudaSetDevice failed"); }
+    if (sdm_pair_prepare() != cudaSuccess) { delete h; return fail(nullptr, SDM_ERR_CUDA, "pair kernel setup failed"); }
+    for (int c = 1; c <= SDM_MAX_CTAS; ++c) h->pair_res[c] = sdm_pair_resident(c);
     cudaDeviceProp prop{};
     cudaGetDeviceProperties(&prop, device);
     if (prop.major < 10) {
@@ -924,7 +930,8 @@ sdm_status sdm_set_option(sdm_handle* h, int option, int value) {
             h->opt_split = value;
             break;
         case SDM_OPT_CTAS_PER_SM:
-            if (value < 1 || value > 8) return fail(h, SDM_ERR_INVALID_ARGUMENT, "ctas per SM must be in 1..8");
+            if (value < 1 || value > SDM_MAX_CTAS)
+                return fail(h, SDM_ERR_INVALID_ARGUMENT, "ctas per SM must be in 1..4");
             h->opt_ctas = value;
             break;
         case SDM_OPT_VERIFY: h->opt_verify = value ? 1 : 0; break;
@@ -941,6 +948,7 @@ sdm_status sdm_get_option(const sdm_handle* h, int option, int* value) {
         case SDM_OPT_SPLIT: *value = h->opt_split; break;
         case SDM_OPT_CTAS_PER_SM: *value = h->opt_ctas; break;
         case SDM_OPT_VERIFY: *value = h->opt_verify; break;
+        case SDM_OPT_PAIR_RESIDENT: *value = h->pair_res[h->opt_ctas]; break;
         default: return SDM_ERR_INVALID_ARGUMENT;
     }
     return SDM_OK;
@@ -973,7 +981,7 @@ sdm_status sdm_autotune(sdm_handle* h, const double* x_device, int* split, int* 
     float best = 1e30f;
     int bs = osplit, bc = octas;
     const int splits[] = {1, 2, 4};
-    const int ctas[] = {3, 4, 5, 6};
+    const int ctas[] = {3, 4};
     for (int sp : splits)
         for (int c : ctas) {
             h->opt_split = sp;

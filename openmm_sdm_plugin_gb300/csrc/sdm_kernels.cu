@@ -451,6 +451,13 @@ struct Ring {                   // one tile ring: 64 prepared j entries
 
 // Two-level cp.async pipeline: list entries two chunks ahead, the candidate
 // particles (8 per entry) one chunk ahead of the chunk being filtered.
+// i-cluster parameters of particles (2u, 2u+1): qh[u] = (q, q', sigma/2, sigma'/2),
+// se[u] = (2 sqrt(eps), 2 sqrt(eps'))
+struct IParams {
+    float4 qh[4];
+    float2 se[4];
+};
+
 struct EvalSmem {
     Ring lj;                    // j with epsilon != 0
     Ring co;                    // j with epsilon == 0 (Coulomb only)
@@ -458,8 +465,9 @@ struct EvalSmem {
     float4 sx[2][SDM_CH * 8];   // staged cluster-local coordinates + charge of candidates
     float2 sp[2][SDM_CH * 8];   // staged (sigma/2, 2 sqrt(eps)) of candidates
     int sm_[2][SDM_CH * 8];     // staged molecule ids of candidates
-    float4 ip[8];               // i-cluster (q, sigma/2, 2 sqrt(eps), 0), read as broadcasts
+    IParams ip;                 // i-cluster parameters by particle pair, read as broadcasts
     int im[8];                  // i-cluster molecule ids
+    float4 ib[2];               // i-cluster box centre and half extents (w: list cutoff squared)
 };
 
 
@@ -479,9 +487,12 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// The 8 i particles in pairs (2u, 2u+1) for the packed FP32x2 pipe:
+// coordinates negated (d = x_j + (-x_i) rounds like x_j - x_i) and force
+// accumulators holding sum_j fs (x_j - x_i), i.e. minus the force on i.
 struct ICluster {
-    float x[8], y[8], z[8];
-    float fx[8], fy[8], fz[8];
+    float2 nx[4], ny[4], nz[4];
+    float2 ax[4], ay[4], az[4];
 };
 
 // round(v * 2^32) as a 64-bit two's-complement integer from two 32-bit
@@ -673,7 +684,7 @@ __global__ void __launch_bounds__(256) k_jlist(SdmArgs a, const int* cl_prefix) 
 // ring of j with epsilon = 0: Lennard-Jones vanishes for every i, Coulomb only.
 template <int MODE, bool IMG, bool LJ>
 __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
-                                          const Ring& rg, const float4* ip, unsigned head, int count,
+                                          const Ring& rg, const IParams& ip, unsigned head, int count,
                                           ICluster& ic, float& ef, long long& npair) {
     const int lane = lane_id();
     const unsigned idx = (head + lane) & (SDM_RING - 1);
@@ -682,62 +693,73 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
     const float4 A = active ? rg.a[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 B = active ? rg.b[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
     const unsigned m = active ? __float_as_uint(B.z) : 0u;
-    const float xs = A.x, ys = A.y, zs = A.z, qj = A.w, hj = B.x, ej = B.y;
-    const float rc2 = S.rc2f, krf = S.krf, crf = S.crf, krf2 = -2.0f * S.krf;
-    float fjx = 0.f, fjy = 0.f, fjz = 0.f, e = 0.f;
+    const float2 xs = make_float2(A.x, A.x), ys = make_float2(A.y, A.y), zs = make_float2(A.z, A.z);
+    const float2 qj = make_float2(A.w, A.w), hj = make_float2(B.x, B.x), ej = make_float2(B.y, B.y);
+    const float rc2 = S.rc2f;
+    const float2 krf = make_float2(S.krf, S.krf), ncrf = make_float2(-S.crf, -S.crf);
+    const float2 krf2 = make_float2(-2.0f * S.krf, -2.0f * S.krf);
+    const float2 one_n = make_float2(-1.0f, -1.0f), c12 = make_float2(12.0f, 12.0f),
+                 c6n = make_float2(-6.0f, -6.0f);
+    float2 fjx = make_float2(0.f, 0.f), fjy = fjx, fjz = fjx, e = fjx;
     int cnt = 0;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        float dx = __fsub_rn(xs, ic.x[t]);
-        float dy = __fsub_rn(ys, ic.y[t]);
-        float dz = __fsub_rn(zs, ic.z[t]);
+    for (int u = 0; u < 4; ++u) {
+        float2 dx = __fadd2_rn(xs, ic.nx[u]);
+        float2 dy = __fadd2_rn(ys, ic.ny[u]);
+        float2 dz = __fadd2_rn(zs, ic.nz[u]);
         if (IMG) {
-            dx = img32(dx, S.Lf[0], S.invLf[0]);
-            dy = img32(dy, S.Lf[1], S.invLf[1]);
-            dz = img32(dz, S.Lf[2], S.invLf[2]);
+            dx = make_float2(img32(dx.x, S.Lf[0], S.invLf[0]), img32(dx.y, S.Lf[0], S.invLf[0]));
+            dy = make_float2(img32(dy.x, S.Lf[1], S.invLf[1]), img32(dy.y, S.Lf[1], S.invLf[1]));
+            dz = make_float2(img32(dz.x, S.Lf[2], S.invLf[2]), img32(dz.y, S.Lf[2], S.invLf[2]));
         }
-        const float r2 = r2_chain(dx, dy, dz);
-        const bool ok = (r2 < rc2) && ((m >> t) & 1u);
+        // same roundings as r2_chain: dz*dz + (dy*dy + dx*dx)
+        const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+        const bool ok0 = (r2.x < rc2) && ((m >> (2 * u)) & 1u);
+        const bool ok1 = (r2.y < rc2) && ((m >> (2 * u + 1)) & 1u);
         if (MODE == MODE_COUNT) {
-            cnt += ok ? 1 : 0;
+            cnt += (ok0 ? 1 : 0) + (ok1 ? 1 : 0);
             continue;
         }
-        const float r2s = ok ? r2 : 1.0f;
-        const float ir = fast_rsqrt(r2s);
-        const float ir2 = ir * ir;
-        const float4 pi = ip[t];   // same address in every lane: one broadcast
-        const float qqm = ok ? pi.x * qj : 0.0f;
-        float fs;
+        const float2 r2s = make_float2(ok0 ? r2.x : 1.0f, ok1 ? r2.y : 1.0f);
+        const float2 ir = make_float2(fast_rsqrt(r2s.x), fast_rsqrt(r2s.y));
+        const float2 ir2 = __fmul2_rn(ir, ir);
+        const float4 qh = ip.qh[u];   // same address in every lane: one broadcast
+        float2 qq = __fmul2_rn(make_float2(qh.x, qh.y), qj);
+        qq = make_float2(ok0 ? qq.x : 0.0f, ok1 ? qq.y : 0.0f);
+        float2 fs;
+        const float2 fc = __fmul2_rn(qq, __ffma2_rn(krf2, r2s, ir));
         if (LJ) {
-            const float sg = pi.y + hj;
-            const float s2 = sg * sg * ir2;
-            const float s6 = s2 * s2 * s2;
-            const float epsm = ok ? pi.z * ej : 0.0f;
-            const float t6 = epsm * s6;
-            e = fmaf(t6, s6 - 1.0f, e);
-            e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
-            fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qqm * fmaf(krf2, r2s, ir)) * ir2;
+            const float2 sg = __fadd2_rn(make_float2(qh.z, qh.w), hj);
+            const float2 s2 = __fmul2_rn(__fmul2_rn(sg, sg), ir2);
+            const float2 s6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
+            float2 epsm = __fmul2_rn(ip.se[u], ej);
+            epsm = make_float2(ok0 ? epsm.x : 0.0f, ok1 ? epsm.y : 0.0f);
+            const float2 t6 = __fmul2_rn(epsm, s6);
+            e = __ffma2_rn(t6, __fadd2_rn(s6, one_n), e);
+            e = __ffma2_rn(qq, __ffma2_rn(krf, r2s, __fadd2_rn(ir, ncrf)), e);
+            fs = __fmul2_rn(__ffma2_rn(t6, __ffma2_rn(c12, s6, c6n), fc), ir2);
         } else {
-            e = fmaf(qqm, fmaf(krf, r2s, ir - crf), e);
-            fs = qqm * fmaf(krf2, r2s, ir) * ir2;
+            e = __ffma2_rn(qq, __ffma2_rn(krf, r2s, __fadd2_rn(ir, ncrf)), e);
+            fs = __fmul2_rn(fc, ir2);
         }
-        fjx = fmaf(fs, dx, fjx);
-        fjy = fmaf(fs, dy, fjy);
-        fjz = fmaf(fs, dz, fjz);
-        ic.fx[t] = fmaf(-fs, dx, ic.fx[t]);
-        ic.fy[t] = fmaf(-fs, dy, ic.fy[t]);
-        ic.fz[t] = fmaf(-fs, dz, ic.fz[t]);
+        fjx = __ffma2_rn(fs, dx, fjx);
+        fjy = __ffma2_rn(fs, dy, fjy);
+        fjz = __ffma2_rn(fs, dz, fjz);
+        ic.ax[u] = __ffma2_rn(fs, dx, ic.ax[u]);
+        ic.ay[u] = __ffma2_rn(fs, dy, ic.ay[u]);
+        ic.az[u] = __ffma2_rn(fs, dz, ic.az[u]);
     }
     if (MODE == MODE_COUNT) {
         npair += cnt;
     } else if (active) {
+        const float gx = __fadd_rn(fjx.x, fjx.y), gy = __fadd_rn(fjy.x, fjy.y), gz = __fadd_rn(fjz.x, fjz.y);
         const int slot = __float_as_int(B.w);
         const size_t gsl = (size_t)R.slot_win + slot;
-        if (!(fmaxf(fabsf(fjx), fmaxf(fabsf(fjy), fabsf(fjz))) < 1.0e9f)) atomicOr(a.status, SDM_DEV_FORCE_OVERFLOW);
-        atomicAdd(a.F0x + gsl, fix64(fjx));
-        atomicAdd(a.F0y + gsl, fix64(fjy));
-        atomicAdd(a.F0z + gsl, fix64(fjz));
-        ef += e;
+        if (!(fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) < 1.0e9f)) atomicOr(a.status, SDM_DEV_FORCE_OVERFLOW);
+        atomicAdd(a.F0x + gsl, fix64(gx));
+        atomicAdd(a.F0y + gsl, fix64(gy));
+        atomicAdd(a.F0z + gsl, fix64(gz));
+        ef += __fadd_rn(e.x, e.y);
     }
 }
 
@@ -782,22 +804,28 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         if (lane < 8) { xi4 = a.clX[slot0 + lane]; pi2 = a.clP[slot0 + lane]; }
         __syncwarp();
         if (lane < 8) {
-            sm.ip[lane] = make_float4(xi4.w, pi2.x, pi2.y, 0.0f);
+            float* qh = reinterpret_cast<float*>(&sm.ip.qh[lane >> 1]);
+            qh[lane & 1] = xi4.w;
+            qh[2 + (lane & 1)] = pi2.x;
+            reinterpret_cast<float*>(&sm.ip.se[lane >> 1])[lane & 1] = pi2.y;
             sm.im[lane] = a.clM[slot0 + lane];
         }
+        if (lane == 0) {
+            float4 c = a.cl_bbc[cw], h = a.cl_bbh[cw];
+            h.w = S.rcl2f;
+            sm.ib[0] = c;
+            sm.ib[1] = h;
+        }
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            ic.x[t] = __shfl_sync(0xffffffffu, xi4.x, t);
-            ic.y[t] = __shfl_sync(0xffffffffu, xi4.y, t);
-            ic.z[t] = __shfl_sync(0xffffffffu, xi4.z, t);
-            ic.fx[t] = 0.f; ic.fy[t] = 0.f; ic.fz[t] = 0.f;
+        for (int u = 0; u < 4; ++u) {
+            ic.nx[u] = make_float2(-__shfl_sync(0xffffffffu, xi4.x, 2 * u), -__shfl_sync(0xffffffffu, xi4.x, 2 * u + 1));
+            ic.ny[u] = make_float2(-__shfl_sync(0xffffffffu, xi4.y, 2 * u), -__shfl_sync(0xffffffffu, xi4.y, 2 * u + 1));
+            ic.nz[u] = make_float2(-__shfl_sync(0xffffffffu, xi4.z, 2 * u), -__shfl_sync(0xffffffffu, xi4.z, 2 * u + 1));
+            ic.ax[u] = make_float2(0.f, 0.f); ic.ay[u] = ic.ax[u]; ic.az[u] = ic.ax[u];
         }
         __syncwarp();
     }
     const unsigned vmask = __ballot_sync(0xffffffffu, lane < 8 && a.perm[slot0 + (lane & 7)] >= 0) & 0xffu;
-    const float4 bc = a.cl_bbc[cw];
-    const float4 bh = a.cl_bbh[cw];
-    const float rcl2 = S.rcl2f;
     const int njl = min(a.jl_cnt[cw], a.jl_cap);
     const int ebeg = (njl * part) / a.split, eend = (njl * (part + 1)) / a.split;
     const int4* jl = a.jl + (size_t)cw * a.jl_cap;
@@ -868,6 +896,7 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
                 xs = __fadd_rn(X4.x, __int_as_float(en.y));
                 ys = __fadd_rn(X4.y, __int_as_float(en.z));
                 zs = __fadd_rn(X4.z, __int_as_float(en.w));
+                const float4 bc = sm.ib[0], bh = sm.ib[1];   // re-read: keeps registers free
                 float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
                 if (IMG) {
                     tx = img32(tx, S.Lf[0], S.invLf[0]);
@@ -879,7 +908,7 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
                 const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
                 // padding slots carry 1e6 coordinates: they fail the box test
                 // unless image mode wraps them back, hence the explicit test there
-                pass = r2_chain(ex, ey, ez) < rcl2;
+                pass = r2_chain(ex, ey, ez) < bh.w;
                 if (IMG) pass = pass && (X4.x < 1.0e5f);
                 if (pass) {
                     if (S.excl_clique) {
@@ -958,7 +987,10 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
     // reduce-scatter of the 24 i-force partial sums
     float v[24];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) { v[3 * q] = ic.fx[q]; v[3 * q + 1] = ic.fy[q]; v[3 * q + 2] = ic.fz[q]; }
+    for (int u = 0; u < 4; ++u) {
+        v[6 * u] = -ic.ax[u].x; v[6 * u + 1] = -ic.ay[u].x; v[6 * u + 2] = -ic.az[u].x;
+        v[6 * u + 3] = -ic.ax[u].y; v[6 * u + 4] = -ic.ay[u].y; v[6 * u + 5] = -ic.az[u].y;
+    }
     {
         const bool up = lane & 16;
 #pragma unroll
@@ -1006,17 +1038,18 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
     if (lane == 0) a.e_part[(size_t)cw * a.split + part] = ed;
 }
 
-// MINB: minimum resident CTAs per SM the register allocation is bounded for
-// (3: up to 168 registers; 4: up to 128; 5: up to 102)
-template <int MODE, int MINB>
-__global__ void __launch_bounds__(SDM_WARPS * 32, MINB)
+// NW warps per CTA, each with its own EvalSmem in dynamic shared memory;
+// MINB CTAs per SM fit the register file: registers per thread are capped at
+// 65536 / (MINB * NW * 32), rounded down to the allocation unit of 8
+template <int MODE, int MINB, int NW>
+__global__ void __launch_bounds__(NW * 32) __maxnreg__((65536 / (MINB * NW * 32)) & ~7)
 k_pair(SdmArgs a, const int* item_prefix) {
-    __shared__ EvalSmem smem[SDM_WARPS];
-    EvalSmem& sm = smem[threadIdx.x >> 5];
+    extern __shared__ __align__(16) unsigned char pair_smem[];
+    EvalSmem& sm = reinterpret_cast<EvalSmem*>(pair_smem)[threadIdx.x >> 5];
     const int total = item_prefix[a.nrep];
-    const int W = gridDim.x * SDM_WARPS;
+    const int W = gridDim.x * NW;
     // static schedule: warp w takes items w, w+W, ...
-    for (int item = blockIdx.x * SDM_WARPS + (threadIdx.x >> 5); item < total; item += W) {
+    for (int item = blockIdx.x * NW + (threadIdx.x >> 5); item < total; item += W) {
         const int r = rep_by_item(item_prefix, a.nrep, item);
         const int local = item - item_prefix[r];
         const int I = local / a.split, part = local - I * a.split;
@@ -1682,17 +1715,83 @@ cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_
     return cudaGetLastError();
 }
 
+// Pair-kernel shapes: (warps per CTA, CTAs per SM the registers are bounded for).
+// Registers are held per SM sub-partition and a CTA's warps are spread over
+// the 4 sub-partitions, so only CTAs of 4 warps balance: 3 or 4 warps per
+// sub-partition give 168 or 128 registers per thread (5 would give 96, where
+// the kernel spills).
+#define SDM_PAIR_SHAPES(X) X(4, 3) X(4, 4)
+
+template <int MODE, int MINB, int NW>
+static cudaError_t pair_attr() {
+    return cudaFuncSetAttribute(k_pair<MODE, MINB, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(NW * sizeof(EvalSmem)));
+}
+
+// Raises the dynamic shared memory limit of every pair-kernel shape on the
+// current device (called once per handle, outside any stream capture).
+cudaError_t sdm_pair_prepare() {
+    cudaError_t e = cudaSuccess;
+#define SDM_ATTR(NW, MB) \
+    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW>();
+    SDM_PAIR_SHAPES(SDM_ATTR)
+#undef SDM_ATTR
+    if (e == cudaSuccess) e = pair_attr<MODE_COUNT, 3, 4>();
+    if (e == cudaSuccess) e = pair_attr<MODE_EMIT, 3, 4>();
+    return e;
+}
+
+// Register bound (MINB) of the pair kernel launched with ctas_per_sm CTAs:
+// the tightest built bound that still admits that many CTAs, 0 if none.
+static int pair_minb(int ctas_per_sm) {
+    int best = 0;
+#define SDM_PICK(NW, MB) \
+    if (ctas_per_sm <= MB && (best == 0 || MB < best)) best = MB;
+    SDM_PAIR_SHAPES(SDM_PICK)
+#undef SDM_PICK
+    return best;
+}
+
+// CTAs of pair-kernel shape (NW, MB) the occupancy calculator places on one SM
+template <int MODE, int MINB, int NW>
+static int pair_resident() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pair<MODE, MINB, NW>, NW * 32,
+                                                      NW * sizeof(EvalSmem)) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+// CTAs per SM that are resident when ctas_per_sm are requested (current device);
+// 0 when no pair kernel is built for the request
+int sdm_pair_resident(int ctas_per_sm) {
+    const int mb = pair_minb(ctas_per_sm);
+#define SDM_RES(NW, MB) \
+    if (mb == MB) return std::min(ctas_per_sm, pair_resident<MODE_EVAL, MB, NW>());
+    SDM_PAIR_SHAPES(SDM_RES)
+#undef SDM_RES
+    return 0;
+}
+
+// resident = CTAs per SM that fit (sdm_pair_resident): the persistent static
+// schedule covers every item with any grid, so the grid never exceeds one wave
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
-                            cudaStream_t st) {
-    const int grid = num_sms() * ctas_per_sm;
+                            int resident, cudaStream_t st) {
+    const int grid = num_sms() * std::max(1, std::min(ctas_per_sm, resident));
     if (mode == MODE_EVAL) {
-        if (ctas_per_sm >= 5) k_pair<MODE_EVAL, 5><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
-        else if (ctas_per_sm == 4) k_pair<MODE_EVAL, 4><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
-        else k_pair<MODE_EVAL, 3><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+        const int mb = pair_minb(ctas_per_sm);
+#define SDM_GO(NW, MB)                                                                                   \
+        if (mb == MB) {                                                                               \
+            k_pair<MODE_EVAL, MB, NW><<<grid, NW * 32, NW * sizeof(EvalSmem), st>>>(a, item_prefix); \
+            return cudaGetLastError();                                                                \
+        }
+        SDM_PAIR_SHAPES(SDM_GO)
+#undef SDM_GO
+        return cudaErrorInvalidValue;
     } else if (mode == MODE_COUNT) {
-        k_pair<MODE_COUNT, 3><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+        k_pair<MODE_COUNT, 3, 4><<<num_sms() * 3, 4 * 32, 4 * sizeof(EvalSmem), st>>>(a, item_prefix);
     } else {
-        k_pair<MODE_EMIT, 3><<<grid, SDM_WARPS * 32, 0, st>>>(a, item_prefix);
+        k_pair<MODE_EMIT, 3, 4><<<num_sms() * 3, 4 * 32, 4 * sizeof(EvalSmem), st>>>(a, item_prefix);
     }
     return cudaGetLastError();
 }

@@ -294,3 +294,29 @@ def test_nonclique_exclusions_parity():
         order = np.argsort(g["slot"][I, :k], kind="stable")
         assert np.array_equal(g["slot"][I, :k][order], ol["slot"][I, :k])
         assert np.array_equal(g["mask"][I, :k][order], ol["mask"][I, :k])
+
+
+def test_pair_schedule_options():
+    """Every accepted CTAs-per-SM request gives the same results; requests
+    without a built register bound are refused; the launch never exceeds
+    the resident CTAs."""
+    s = S.config0(variant="b")
+    h = _handle([s])
+    x = s.positions[0]
+    ref, Fref = h.evaluate(x)
+    for c in (1, 2, 3, 4):
+        h.set_option(capi.OPT_CTAS_PER_SM, c)
+        res_c = h.get_option(capi.OPT_PAIR_RESIDENT)
+        assert 1 <= res_c <= c
+        for sp in (1, 2, 4):
+            h.set_option(capi.OPT_SPLIT, sp)
+            res, F = h.evaluate(x)
+            if sp == 1:   # same work items, other warps: bit-identical
+                assert np.array_equal(res[:, :capi.R_STATUS], ref[:, :capi.R_STATUS])
+                assert np.array_equal(F, Fref)
+            else:         # FP32 partial sums over other groups of list entries
+                assert np.allclose(res[:, :capi.R_STATUS], ref[:, :capi.R_STATUS], rtol=1e-6, atol=1e-6)
+                assert rms_rel(F, Fref) < 1e-6
+    for bad in (0, 5):
+        with pytest.raises(capi.SdmError):
+            h.set_option(capi.OPT_CTAS_PER_SM, bad)
