@@ -880,22 +880,21 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         for (int g = 0; g < SDM_CH / 4; ++g) {
             const int e = 4 * g + q;   // entry of this lane's 8-lane group
             if (4 * g >= nch) break;   // uniform
-            bool pass = false;
-            float xs = 0.f, ys = 0.f, zs = 0.f;
-            int sj = 0;
-            unsigned m = 0;
-            float4 X4 = make_float4(0.f, 0.f, 0.f, 0.f);
-            float2 P = make_float2(0.f, 0.f);
-            if (e < nch) {
-                const int4 en = sm.je[c % 3][e];
-                X4 = sm.sx[c & 1][8 * e + t];
-                P = sm.sp[c & 1][8 * e + t];
-                const int J = en.x & 0x7fffffff;
-                const bool nm = en.x < 0;
-                sj = 8 * J + t;
-                xs = __fadd_rn(X4.x, __int_as_float(en.y));
-                ys = __fadd_rn(X4.y, __int_as_float(en.z));
-                zs = __fadd_rn(X4.z, __int_as_float(en.w));
+            // lanes past the chunk's last entry read that entry (initialised
+            // staging) and are dropped by `valid`: straight-line code for all lanes
+            const bool valid = e < nch;
+            const int ee = valid ? e : nch - 1;
+            const int4 en = sm.je[c % 3][ee];
+            const float4 X4 = sm.sx[c & 1][8 * ee + t];
+            const float2 P = sm.sp[c & 1][8 * ee + t];
+            const int J = en.x & 0x7fffffff;
+            const bool nm = en.x < 0;
+            const int sj = 8 * J + t;
+            const float xs = __fadd_rn(X4.x, __int_as_float(en.y));
+            const float ys = __fadd_rn(X4.y, __int_as_float(en.z));
+            const float zs = __fadd_rn(X4.z, __int_as_float(en.w));
+            bool pass;
+            {
                 const float4 bc = sm.ib[0], bh = sm.ib[1];   // re-read: keeps registers free
                 float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
                 if (IMG) {
@@ -908,24 +907,23 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
                 const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
                 // padding slots carry 1e6 coordinates: they fail the box test
                 // unless image mode wraps them back, hence the explicit test there
-                pass = r2_chain(ex, ey, ez) < bh.w;
+                pass = valid && r2_chain(ex, ey, ez) < bh.w;
                 if (IMG) pass = pass && (X4.x < 1.0e5f);
-                if (pass) {
-                    if (S.excl_clique) {
-                        // excluded <=> same molecule: compare with the 8 i ids
-                        m = vmask;
-                        if (nm) {
-                            if (J == I) m &= (1u << t) - 1u;
-                            const int mj = sm.sm_[c & 1][8 * e + t];
+            }
+            unsigned m = vmask;
+            if (S.excl_clique) {
+                // excluded <=> same molecule: compare with the 8 i ids (uniform branch)
+                if (__any_sync(0xffffffffu, pass && nm)) {
+                    const int mj = sm.sm_[c & 1][8 * ee + t];
+                    unsigned mm = vmask & ((J == I) ? ((1u << t) - 1u) : 0xffu);
 #pragma unroll
-                            for (int u = 0; u < 8; ++u)
-                                if (sm.im[u] == mj) m &= ~(1u << u);
-                        }
-                    } else {
-                        m = j_mask(a, S, R, I, J, sj, vmask, nm);
-                    }
-                    pass = m != 0u;
+                    for (int u = 0; u < 8; ++u) mm = (sm.im[u] == mj) ? (mm & ~(1u << u)) : mm;
+                    m = nm ? mm : vmask;
                 }
+                pass = pass && m != 0u;
+            } else if (pass) {
+                m = j_mask(a, S, R, I, J, sj, vmask, nm);
+                pass = m != 0u;
             }
             if (MODE == MODE_EMIT) {
                 const unsigned bal = __ballot_sync(0xffffffffu, pass);
