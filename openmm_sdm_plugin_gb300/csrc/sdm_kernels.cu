@@ -380,8 +380,8 @@ __global__ void k_clusters(SdmArgs a) {
                 hi[k] = fmaxf(hi[k], __shfl_xor_sync(gmask, hi[k], o, 8));
             }
         // exclusion-linked clusters: distinct clusters (other than C) holding
-        // partners of this cluster's particles; -2 when more than 4 or unknown
-        int link[4] = {-1, -1, -1, -1};
+        // partners of this cluster's particles; -2 when more than 8 or unknown
+        int link[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
         int nlink = 0;
         bool many = false;
         for (int l = 0; l < 8; ++l) {
@@ -400,7 +400,7 @@ __global__ void k_clusters(SdmArgs a) {
                 bool seen = false;
                 for (int u = 0; u < nlink; ++u) seen |= (link[u] == cc);
                 if (!seen) {
-                    if (nlink < 4) link[nlink++] = cc; else many = true;
+                    if (nlink < 8) link[nlink++] = cc; else many = true;
                 }
             }
         }
@@ -421,8 +421,10 @@ __global__ void k_clusters(SdmArgs a) {
             a.cl_bbh[cw] = make_float4(__fmul_rn(0.5f, __fsub_rn(hi[0], lo[0])),
                                        __fmul_rn(0.5f, __fsub_rn(hi[1], lo[1])),
                                        __fmul_rn(0.5f, __fsub_rn(hi[2], lo[2])), 0.0f);
-            a.cl_link[cw] = many ? make_int4(-2, -2, -2, -2)
-                                 : make_int4(link[0], link[1], link[2], link[3]);
+            a.cl_link[2 * (size_t)cw] = many ? make_int4(-2, -2, -2, -2)
+                                             : make_int4(link[0], link[1], link[2], link[3]);
+            a.cl_link[2 * (size_t)cw + 1] = many ? make_int4(-2, -2, -2, -2)
+                                                 : make_int4(link[4], link[5], link[6], link[7]);
             atomicMax(&a.extz[r], __float_as_uint(fmaxf(hi[2], 0.0f)));
         }
     }
@@ -548,6 +550,9 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
     const float4 bc = a.cl_bbc[cw];
     const float4 bh = a.cl_bbh[cw];
     const int4 ref = a.cl_ref[cw];
+    // clusters sharing an exclusion with I: the relation is symmetric, so I's
+    // own (complete unless -2) partner list decides every candidate J
+    const int4 lkA = a.cl_link[2 * (size_t)cw], lkB = a.cl_link[2 * (size_t)cw + 1];
     const float rclc = S.rcl + 2.0e-4f;
     const float rclc2 = rclc * rclc;
     const float* tabx = a.shift_tab + S.shift_base;
@@ -614,22 +619,22 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
         // each lane walks its own column; the next candidate's data is fetched ahead
-        int4 rj_n = make_int4(0, 0, 0, 0), lk_n = rj_n;
+        int4 rj_n = make_int4(0, 0, 0, 0);
         float4 cj_n = make_float4(0.f, 0.f, 0.f, 0.f), hj_n = cj_n;
         int J_n = jb1;
         if (nc > 0) {
             J_n = (c1 > 0) ? jb1 : jb2;
             const int jw = R.cl_win + J_n;
-            rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw]; lk_n = a.cl_link[jw];
+            rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw];
         }
         for (int it = 0; it < maxc; ++it) {
             const int J = J_n;
-            const int4 rj = rj_n, lk = lk_n;
+            const int4 rj = rj_n;
             const float4 cj = cj_n, hjb = hj_n;
             if (it + 1 < nc) {
                 J_n = (it + 1 < c1) ? jb1 + it + 1 : jb2 + (it + 1 - c1);
                 const int jw = R.cl_win + J_n;
-                rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw]; lk_n = a.cl_link[jw];
+                rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw];
             }
             bool pass = false;
             int4 en = make_int4(0, 0, 0, 0);
@@ -645,7 +650,8 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
                 const float gy = fmaxf(fabsf(dy) - bh.y - hjb.y, 0.0f);
                 const float gz = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
                 pass = gx * gx + gy * gy + gz * gz < rclc2;
-                const bool nm = (J == I) || lk.x == -2 || lk.x == I || lk.y == I || lk.z == I || lk.w == I;
+                const bool nm = (J == I) || lkA.x == -2 || lkA.x == J || lkA.y == J || lkA.z == J ||
+                                lkA.w == J || lkB.x == J || lkB.y == J || lkB.z == J || lkB.w == J;
                 en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(Sx), __float_as_int(Sy),
                                __float_as_int(sz));
             }

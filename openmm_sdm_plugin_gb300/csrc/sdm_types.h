@@ -30,7 +30,7 @@
 //     cl_ref   int4    reference cell (cx, cy, cz) and column id
 //     cl_bbc   float4  bounding-box centre (cluster frame)
 //     cl_bbh   float4  bounding-box half extents
-//     cl_link  int4    clusters holding exclusion partners of this cluster (-1 none, -2 many)
+//     cl_link  int4[2] up to 8 clusters holding exclusion partners of this cluster (-1 none, -2 many)
 //     cl_zb    float2  absolute z of the first / last particle (outward rounded)
 //     e_part   double  main-pass energy of the cluster's work items
 #pragma once
