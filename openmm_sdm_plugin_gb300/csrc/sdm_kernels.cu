@@ -33,6 +33,7 @@
 
 #define SDM_WARPS 4
 #define SDM_JL_CAP 256
+#define SDM_PERT_PARTS 4         // warps per perturbation item (stencil columns split between them)
 #define SDM_RING 64
 #define SDM_INVALID_COORD 1.0e6f
 
@@ -1078,7 +1079,7 @@ __device__ __forceinline__ void pair_terms(const SdmSys& S, float r2, float qq, 
 }
 
 template <int MODE, bool IMG>
-__device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm) {
+__device__ void process_perturb(const SdmArgs& a, int r, int local, int part, WarpSmem& sm) {
     const int lane = lane_id();
     const SdmRep R = a.rep[r];
     const SdmSys& S = a.sys[R.sys];
@@ -1163,11 +1164,23 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm
         jl_n = 0;
     };
 
-    for (int k0 = 0; k0 < nst; k0 += 32) {
+    // z window of the point (absolute, conservative) and its pieces inside [0, Lz):
+    // clusters of a column outside it are farther than the cutoff in z
+    const float2* zb = a.cl_zb + R.cl_win;
+    const float zq = __double2float_rn(y[2]);
+    const float ZA = zq - rclc - 1.0e-4f, ZB = zq + rclc + 1.0e-4f;
+    const float Lz = S.Lf[2];
+    const bool wholez = IMG || (ZB - ZA >= Lz);
+    float za1 = fmaxf(ZA, 0.0f), zb1 = fminf(ZB, Lz), za2 = 1.0f, zb2 = 0.0f;  // empty 2nd piece
+    if (ZA < 0.0f) { za2 = ZA + Lz; zb2 = Lz; }
+    else if (ZB > Lz) { za2 = 0.0f; zb2 = ZB - Lz; }
+    // this part's share of the full stencil
+    const int kb = (nst * part) / SDM_PERT_PARTS, ke = (nst * (part + 1)) / SDM_PERT_PARTS;
+    for (int k0 = kb; k0 < ke; k0 += 32) {
         const int k = k0 + lane;
-        int cntJ = 0, Jb = 0;
+        int cntJ = 0, Jb = 0, cnt2 = 0, Jb2 = 0;
         float Sx = 0.f, Sy = 0.f;
-        if (k < nst) {
+        if (k < ke) {
             const int2 off = a.stencil[S.fst_base + k];
             const int ccx = wrap_add(cy[0], off.x, S.M[0]);
             const int ccy = wrap_add(cy[1], off.y, S.M[1]);
@@ -1183,24 +1196,44 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm
                 ok = gx * gx + gy * gy < rclc2;
             }
             if (ok) {
-                Jb = colcl[colid];
-                cntJ = max(colcl[colid + 1] - Jb, 0);
+                const int lo = colcl[colid], hi = colcl[colid + 1];
+                if (wholez) {
+                    Jb = lo;
+                    cntJ = hi - lo;
+                } else {
+                    Jb = lower_zhi(zb, lo, hi, za1);
+                    cntJ = upper_zlo(zb, Jb, hi, zb1) - Jb;
+                    if (za2 <= zb2) {
+                        Jb2 = lower_zhi(zb, lo, hi, za2);
+                        cnt2 = upper_zlo(zb, Jb2, hi, zb2) - Jb2;
+                        // the two pieces are disjoint in z; clusters are counted once
+                        if (cnt2 > 0 && cntJ > 0 && Jb2 < Jb + cntJ && Jb2 + cnt2 > Jb) {
+                            const int u0 = min(Jb, Jb2), u1 = max(Jb + cntJ, Jb2 + cnt2);
+                            Jb = u0; cntJ = u1 - u0; cnt2 = 0;
+                        }
+                    }
+                }
+                cntJ = max(cntJ, 0);
+                cnt2 = max(cnt2, 0);
             }
         }
-        const bool has = cntJ > 0;
-        const unsigned hb = __ballot_sync(0xffffffffu, has);
-        int incl = cntJ;
+        // up to two cluster ranges per column, in lane order
+        const bool h1 = cntJ > 0, h2 = cnt2 > 0;
+        const unsigned hb1 = __ballot_sync(0xffffffffu, h1), hb2 = __ballot_sync(0xffffffffu, h2);
+        int incl = cntJ + cnt2;
 #pragma unroll
         for (int oo = 1; oo < 32; oo <<= 1) {
             const int v = __shfl_up_sync(0xffffffffu, incl, oo);
             if (lane >= oo) incl += v;
         }
         const int total = __shfl_sync(0xffffffffu, incl, 31);
-        if (has) {
-            const int ri = __popc(hb & ((1u << lane) - 1u));
-            sm.rng[ri] = make_int4(Jb, incl - cntJ, __float_as_int(Sx), __float_as_int(Sy));
+        {
+            const unsigned lt = (1u << lane) - 1u;
+            const int ri = __popc(hb1 & lt) + __popc(hb2 & lt);
+            if (h1) sm.rng[ri] = make_int4(Jb, incl - cntJ - cnt2, __float_as_int(Sx), __float_as_int(Sy));
+            if (h2) sm.rng[ri + (h1 ? 1 : 0)] = make_int4(Jb2, incl - cnt2, __float_as_int(Sx), __float_as_int(Sy));
         }
-        const int nr = __popc(hb);
+        const int nr = __popc(hb1) + __popc(hb2);
         __syncwarp();
         for (int e0 = 0; e0 < total; e0 += 32) {
             const int e = e0 + lane;
@@ -1241,8 +1274,8 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm
         }
     }
     phase_b();
-    // displaced-displaced pairs with different displacement vectors
-    for (int q0 = 0; q0 < S.nD; q0 += 32) {
+    // displaced-displaced pairs with different displacement vectors (part 0)
+    for (int q0 = 0; q0 < (part == 0 ? S.nD : 0); q0 += 32) {
         const int qi = q0 + lane;
         if (qi < S.nD) {
             const int qa = a.D_idx[S.D_base + qi];
@@ -1289,7 +1322,7 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, WarpSmem& sm
         red_fix(a.dFx + gsl, fpx, a.status);
         red_fix(a.dFy + gsl, fpy, a.status);
         red_fix(a.dFz + gsl, fpz, a.status);
-        a.p_part[R.pert_win + local] = ed;
+        a.p_part[(size_t)(R.pert_win + local) * SDM_PERT_PARTS + part] = ed;
     }
 }
 
@@ -1302,12 +1335,13 @@ __global__ void __launch_bounds__(SDM_WARPS * 32) k_perturb(SdmArgs a) {
         int item = 0;
         if (lane == 0) item = atomicAdd(&a.work_counter[1], 1);
         item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= a.total_pert) break;
-        const int r = rep_by_pert(a.rep, a.nrep, item);
-        const int local = item - a.rep[r].pert_win;
+        if (item >= a.total_pert * SDM_PERT_PARTS) break;
+        const int pi = item / SDM_PERT_PARTS, part = item - pi * SDM_PERT_PARTS;
+        const int r = rep_by_pert(a.rep, a.nrep, pi);
+        const int local = pi - a.rep[r].pert_win;
         const SdmSys& S = a.sys[a.rep[r].sys];
-        if (replica_image_mode(a, S, r)) process_perturb<MODE, true>(a, r, local, sm);
-        else process_perturb<MODE, false>(a, r, local, sm);
+        if (replica_image_mode(a, S, r)) process_perturb<MODE, true>(a, r, local, part, sm);
+        else process_perturb<MODE, false>(a, r, local, part, sm);
     }
 }
 
@@ -1577,7 +1611,8 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     for (int k = threadIdx.x; k < ncl * a.split; k += blockDim.x) e0 += ep[k];
     const double U0 = block_sum(e0, red);
     double eu = 0.0;
-    for (int k = threadIdx.x; k < 2 * S.nD; k += blockDim.x) eu += a.p_part[R.pert_win + k];
+    for (int k = threadIdx.x; k < 2 * S.nD * SDM_PERT_PARTS; k += blockDim.x)
+        eu += a.p_part[(size_t)R.pert_win * SDM_PERT_PARTS + k];
     const double u = block_sum(eu, red);
     if (threadIdx.x != 0) return;
     const double* p = a.params + (size_t)r * SDM_NPARAMS;
@@ -1802,8 +1837,8 @@ cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, 
 
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st) {
     if (a.total_pert == 0) return cudaSuccess;
-    int grid = (a.total_pert + SDM_WARPS - 1) / SDM_WARPS;
-    const int cap = num_sms() * 4;
+    int grid = (a.total_pert * SDM_PERT_PARTS + SDM_WARPS - 1) / SDM_WARPS;
+    const int cap = num_sms() * 8;
     if (grid > cap) grid = cap;
     if (mode == MODE_COUNT) k_perturb<MODE_COUNT><<<grid, SDM_WARPS * 32, 0, st>>>(a);
     else k_perturb<MODE_EVAL><<<grid, SDM_WARPS * 32, 0, st>>>(a);
