@@ -124,7 +124,7 @@ struct sdm_handle {
 namespace {
 
 const char* const kKernelNames[] = {"k_cells", "k_scan", "k_bucket", "k_colsort", "k_clusters",
-                                    "k_jlist", "k_pair", "k_perturb", "k_finalize+k_mix"};
+                                    "k_jlist", "k_pair", "k_pert_prep+k_perturb", "k_finalize+k_mix"};
 const int kNumTimed = 9;
 
 sdm_status fail(sdm_handle* h, sdm_status code, const std::string& msg) {
@@ -643,6 +643,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_lnk = ar.take<int4>(2 * Cl), o_ep = ar.take<double>(Cl * SDM_MAX_SPLIT);
     const size_t o_zb = ar.take<float2>(Cl);
     const size_t o_pp = ar.take<double>(std::max(Pp, 1LL) * 4);   // SDM_PERT_PARTS partials per item
+    const size_t o_ppos = ar.take<SdmPertPos>(std::max(Pp, 1LL));
     const size_t o_adj = ar.take<double>(3 * std::max(Pp, 1LL));
     const size_t o_ncl = ar.take<int>(nrep), o_st = ar.take<int>(4);
     const size_t o_counts = ar.take<long long>(2 * nrep), o_ip = ar.take<int>(nrep + 1);
@@ -707,6 +708,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.stencil = at<int2>(B, o_st2);
     a.e_part = at<double>(B, o_ep);
     a.p_part = at<double>(B, o_pp);
+    a.pert_pos = at<SdmPertPos>(B, o_ppos);
     a.adj = at<double>(B, o_adj);
     a.ncl = at<int>(B, o_ncl);
     a.status = at<int>(B, o_st);

@@ -1078,6 +1078,30 @@ __device__ __forceinline__ void pair_terms(const SdmSys& S, float r2, float qq, 
     fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qq * fmaf(-2.0f * S.krf, r2, ir)) * ir2;
 }
 
+// Position of every perturbation item's displaced particle in its state:
+// y = wrap(w + st d), its cell and cell-local FP32 coordinates (one thread per item)
+__global__ void k_pert_prep(SdmArgs a) {
+    const int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= a.total_pert) return;
+    const int r = rep_by_pert(a.rep, a.nrep, item);
+    const SdmRep R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int local = item - R.pert_win;
+    const int pidx = local >> 1, st = local & 1;
+    const int p = a.D_idx[S.D_base + pidx];
+    const int tp = S.atom_base + p;
+    const double* wp = a.w + 3 * (size_t)(R.atom_win + p);
+    SdmPertPos pp;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double v = st ? __dadd_rn(wp[k], a.topo_d[3 * (size_t)tp + k]) : wp[k];
+        pp.y[k] = wrap1(v, S.box[k], S.invL[k]);
+        pp.cy[k] = cell_of(pp.y[k], S.invg[k], S.M[k]);
+        pp.o[k] = __double2float_rn(__dsub_rn(pp.y[k], __dmul_rn((double)pp.cy[k], S.g[k])));
+    }
+    a.pert_pos[item] = pp;
+}
+
 template <int MODE, bool IMG>
 __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, WarpSmem& sm) {
     const int lane = lane_id();
@@ -1088,17 +1112,11 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, Wa
     const int p = a.D_idx[S.D_base + pidx];
     const int tp = S.atom_base + p;
     const int gp = a.topo_grp[tp];
-    double y[3];
-    int cy[3];
-    float o[3];
-    const double* wp = a.w + 3 * (size_t)(R.atom_win + p);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const double v = st ? __dadd_rn(wp[k], a.topo_d[3 * (size_t)tp + k]) : wp[k];
-        y[k] = wrap1(v, S.box[k], S.invL[k]);
-        cy[k] = cell_of(y[k], S.invg[k], S.M[k]);
-        o[k] = __double2float_rn(__dsub_rn(y[k], __dmul_rn((double)cy[k], S.g[k])));
-    }
+    // position of the displaced particle in this state (computed once per item by k_pert_prep)
+    const SdmPertPos pp = a.pert_pos[R.pert_win + local];
+    const double y[3] = {pp.y[0], pp.y[1], pp.y[2]};
+    const int cy[3] = {pp.cy[0], pp.cy[1], pp.cy[2]};
+    const float o[3] = {pp.o[0], pp.o[1], pp.o[2]};
     const float qp = a.topo_q[tp], hp = a.topo_hs[tp], sp_ = a.topo_se[tp];
     const int cxb = a.cx_off[S.cx_base + pidx], cxe = a.cx_off[S.cx_base + pidx + 1];
     const float rcl2 = S.rcl2f;
@@ -1109,7 +1127,15 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, Wa
     const float* tabz = taby + 2 * S.M[1] + 1;
     const int nst = S.fst_count;
     const int* colcl = a.col_cl + R.col_win;
-    double ed = 0.0;
+    // energy as an unevaluated float-float sum es + ec (TwoSum on the FP32
+    // pipe): FP64-level accuracy without per-pair work on the narrow FP64 pipe
+    float es = 0.f, ec = 0.f;
+    auto acc = [&](float v) {
+        const float t = __fadd_rn(es, v);
+        const float bp = __fsub_rn(t, es);
+        ec = __fadd_rn(ec, __fadd_rn(__fsub_rn(es, __fsub_rn(t, bp)), __fsub_rn(v, bp)));
+        es = t;
+    };
     float fpx = 0.f, fpy = 0.f, fpz = 0.f;
     long long npair = 0;
     int jl_n = 0;
@@ -1117,7 +1143,7 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, Wa
     auto eval_j = [&](float dx, float dy, float dz, float r2, float qj, float hj, float ej, int sj) {
         float e, fs;
         pair_terms(S, r2, qp * qj, hp + hj, sp_ * ej, e, fs);
-        ed += (double)(sgn * e);
+        acc(sgn * e);
         const float f = sgn * fs;
         if (sj >= 0) {
             const size_t gsl = (size_t)R.slot_win + sj;
@@ -1274,20 +1300,20 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, Wa
         }
     }
     phase_b();
-    // displaced-displaced pairs with different displacement vectors (part 0)
-    for (int q0 = 0; q0 < (part == 0 ? S.nD : 0); q0 += 32) {
+    // displaced-displaced pairs with different displacement vectors (this part's share)
+    const int qb = (S.nD * part) / SDM_PERT_PARTS, qe = (S.nD * (part + 1)) / SDM_PERT_PARTS;
+    for (int q0 = qb; q0 < qe; q0 += 32) {
         const int qi = q0 + lane;
-        if (qi < S.nD) {
+        if (qi < qe) {
             const int qa = a.D_idx[S.D_base + qi];
             const int tq = S.atom_base + qa;
             const int gq = a.topo_grp[tq];
             if (gq != gp && gq != 0 && qa > p) {
-                const double* wq = a.w + 3 * (size_t)(R.atom_win + qa);
+                const SdmPertPos& pq = a.pert_pos[R.pert_win + 2 * qi + st];
                 float d[3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    const double vq = st ? __dadd_rn(wq[k], a.topo_d[3 * (size_t)tq + k]) : wq[k];
-                    const double yq = wrap1(vq, S.box[k], S.invL[k]);
+                    const double yq = pq.y[k];
                     double v = __dsub_rn(yq, y[k]);
                     const double tt = rint(__dmul_rn(v, S.invL[k]));
                     v = __dsub_rn(v, __dmul_rn(tt, S.box[k]));
@@ -1315,14 +1341,16 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, Wa
         fpx += __shfl_xor_sync(0xffffffffu, fpx, oo);
         fpy += __shfl_xor_sync(0xffffffffu, fpy, oo);
         fpz += __shfl_xor_sync(0xffffffffu, fpz, oo);
-        ed += __shfl_xor_sync(0xffffffffu, ed, oo);
+        const float os = __shfl_xor_sync(0xffffffffu, es, oo), oc = __shfl_xor_sync(0xffffffffu, ec, oo);
+        acc(os);
+        ec = __fadd_rn(ec, oc);
     }
     if (lane == 0) {
         const size_t gsl = (size_t)R.slot_win + a.inv[R.atom_win + p];
         red_fix(a.dFx + gsl, fpx, a.status);
         red_fix(a.dFy + gsl, fpy, a.status);
         red_fix(a.dFz + gsl, fpz, a.status);
-        a.p_part[(size_t)(R.pert_win + local) * SDM_PERT_PARTS + part] = ed;
+        a.p_part[(size_t)(R.pert_win + local) * SDM_PERT_PARTS + part] = (double)es + (double)ec;
     }
 }
 
@@ -1837,6 +1865,7 @@ cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, 
 
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st) {
     if (a.total_pert == 0) return cudaSuccess;
+    k_pert_prep<<<(a.total_pert + 127) / 128, 128, 0, st>>>(a);
     int grid = (a.total_pert * SDM_PERT_PARTS + SDM_WARPS - 1) / SDM_WARPS;
     const int cap = num_sms() * 8;
     if (grid > cap) grid = cap;

@@ -68,6 +68,14 @@ struct SdmSys {
     int fst_base, fst_count;  // full stencil for point queries
 };
 
+// per perturbation item (replica, displaced particle, state): the wrapped
+// position in that state, its cell and its cell-local FP32 coordinates
+struct SdmPertPos {
+    double y[3];
+    int cy[3];
+    float o[3];
+};
+
 struct SdmRep {
     int sys;
     int n;            // particles of the system
@@ -137,6 +145,7 @@ struct SdmArgs {
     int jl_cap;
     double* e_part;      // cl window * SDM_MAX_SPLIT
     double* p_part;      // perturbation partials
+    SdmPertPos* pert_pos; // per perturbation item (total_pert entries)
     double* adj;         // adjoint sums: 3 per perturbation item
     int* ncl;            // clusters per replica
     unsigned* extz;      // per replica max cluster z extent (float bits)
