@@ -416,9 +416,10 @@ __global__ void k_clusters(SdmArgs a) {
             const int cw = R.cl_win + C;
             a.cl_zb[cw] = make_float2(__double2float_rd(wz0) - 1.0e-4f, __double2float_ru(wzl) + 1.0e-4f);
             a.cl_ref[cw] = make_int4(cx, cy, cz, ci0.x);
+            // w: the reference z cell, so candidate scans need no cl_ref load
             a.cl_bbc[cw] = make_float4(__fmul_rn(0.5f, __fadd_rn(lo[0], hi[0])),
                                        __fmul_rn(0.5f, __fadd_rn(lo[1], hi[1])),
-                                       __fmul_rn(0.5f, __fadd_rn(lo[2], hi[2])), 0.0f);
+                                       __fmul_rn(0.5f, __fadd_rn(lo[2], hi[2])), __int_as_float(cz));
             a.cl_bbh[cw] = make_float4(__fmul_rn(0.5f, __fsub_rn(hi[0], lo[0])),
                                        __fmul_rn(0.5f, __fsub_rn(hi[1], lo[1])),
                                        __fmul_rn(0.5f, __fsub_rn(hi[2], lo[2])), 0.0f);
@@ -620,27 +621,25 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
         // each lane walks its own column; the next candidate's data is fetched ahead
-        int4 rj_n = make_int4(0, 0, 0, 0);
         float4 cj_n = make_float4(0.f, 0.f, 0.f, 0.f), hj_n = cj_n;
         int J_n = jb1;
         if (nc > 0) {
             J_n = (c1 > 0) ? jb1 : jb2;
             const int jw = R.cl_win + J_n;
-            rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw];
+            cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw];
         }
         for (int it = 0; it < maxc; ++it) {
             const int J = J_n;
-            const int4 rj = rj_n;
             const float4 cj = cj_n, hjb = hj_n;
             if (it + 1 < nc) {
                 J_n = (it + 1 < c1) ? jb1 + it + 1 : jb2 + (it + 1 - c1);
                 const int jw = R.cl_win + J_n;
-                rj_n = a.cl_ref[jw]; cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw];
+                cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw];
             }
             bool pass = false;
             int4 en = make_int4(0, 0, 0, 0);
             if (it < nc) {
-                const float sz = tabz[wrap_cell(rj.z - ref.z, S.M[2]) + S.M[2]];
+                const float sz = tabz[wrap_cell(__float_as_int(cj.w) - ref.z, S.M[2]) + S.M[2]];
                 float dx = cj.x + Sx - bc.x, dy = cj.y + Sy - bc.y, dz = cj.z + sz - bc.z;
                 if (IMG) {
                     dx = img32(dx, S.Lf[0], S.invLf[0]);
@@ -671,7 +670,7 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
 }
 
 // static schedule: warp w takes items w, w+W, w+2W, ...
-__global__ void __launch_bounds__(256) k_jlist(SdmArgs a, const int* cl_prefix) {
+__global__ void __launch_bounds__(256, 4) k_jlist(SdmArgs a, const int* cl_prefix) {
     const int total = cl_prefix[a.nrep];
     const int W = gridDim.x * (blockDim.x >> 5);
     for (int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < total; item += W) {
@@ -1274,11 +1273,10 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, Wa
                 const int4 rg = sm.rng[lo];
                 const int J = rg.x + (e - rg.y);
                 const int jw = R.cl_win + J;
-                const int4 rj = a.cl_ref[jw];
-                const float sz = tabz[wrap_cell(rj.z - cy[2], S.M[2]) + S.M[2]];
-                const float sx = __int_as_float(rg.z), sy = __int_as_float(rg.w);
                 const float4 cj = a.cl_bbc[jw];
                 const float4 hjb = a.cl_bbh[jw];
+                const float sz = tabz[wrap_cell(__float_as_int(cj.w) - cy[2], S.M[2]) + S.M[2]];
+                const float sx = __int_as_float(rg.z), sy = __int_as_float(rg.w);
                 float dx = cj.x + sx - o[0], dy = cj.y + sy - o[1], dz = cj.z + sz - o[2];
                 if (IMG) {
                     dx = img32(dx, S.Lf[0], S.invLf[0]);
@@ -1519,11 +1517,10 @@ __device__ void process_adjoint(const SdmArgs& a, int r, int local, AdjSmem& sm)
                 const int4 rg = sm.rng[lo];
                 const int J = rg.x + (e - rg.y);
                 const int jw = R.cl_win + J;
-                const int4 rj = a.cl_ref[jw];
-                const float sz = tabz[wrap_cell(rj.z - cy[2], S.M[2]) + S.M[2]];
-                const float sx = __int_as_float(rg.z), sy = __int_as_float(rg.w);
                 const float4 cj = a.cl_bbc[jw];
                 const float4 hjb = a.cl_bbh[jw];
+                const float sz = tabz[wrap_cell(__float_as_int(cj.w) - cy[2], S.M[2]) + S.M[2]];
+                const float sx = __int_as_float(rg.z), sy = __int_as_float(rg.w);
                 float dx = cj.x + sx - o[0], dy = cj.y + sy - o[1], dz = cj.z + sz - o[2];
                 if (IMG) {
                     dx = img32(dx, S.Lf[0], S.invLf[0]);
