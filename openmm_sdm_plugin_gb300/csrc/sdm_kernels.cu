@@ -544,7 +544,7 @@ __device__ __forceinline__ int upper_zlo(const float2* zb, int lo, int hi, float
 }
 
 template <bool IMG>
-__device__ void build_jlist(const SdmArgs& a, int r, int I) {
+__device__ void build_jlist(const SdmArgs& a, int r, int I, int4* rng) {
     const int lane = lane_id();
     const SdmRep R = a.rep[r];
     const SdmSys S = a.sys[R.sys];
@@ -616,31 +616,42 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
                 c2 = max(c2, 0);
             }
         }
-        const int nc = c1 + c2;
-        int maxc = nc;
+        // the columns' candidate ranges (up to two per lane) in lane order, then
+        // the candidates flattened over all lanes: every lane tests one per round
+        const bool h1 = c1 > 0, h2 = c2 > 0;
+        const unsigned hb1 = __ballot_sync(0xffffffffu, h1), hb2 = __ballot_sync(0xffffffffu, h2);
+        int incl = c1 + c2;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
-        // each lane walks its own column; the next candidate's data is fetched ahead
-        float4 cj_n = make_float4(0.f, 0.f, 0.f, 0.f), hj_n = cj_n;
-        int J_n = jb1;
-        if (nc > 0) {
-            J_n = (c1 > 0) ? jb1 : jb2;
-            const int jw = R.cl_win + J_n;
-            cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
         }
-        for (int it = 0; it < maxc; ++it) {
-            const int J = J_n;
-            const float4 cj = cj_n, hjb = hj_n;
-            if (it + 1 < nc) {
-                J_n = (it + 1 < c1) ? jb1 + it + 1 : jb2 + (it + 1 - c1);
-                const int jw = R.cl_win + J_n;
-                cj_n = a.cl_bbc[jw]; hj_n = a.cl_bbh[jw];
-            }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        {
+            const unsigned lt = (1u << lane) - 1u;
+            const int ri = __popc(hb1 & lt) + __popc(hb2 & lt);
+            if (h1) rng[ri] = make_int4(jb1, incl - c1 - c2, __float_as_int(Sx), __float_as_int(Sy));
+            if (h2) rng[ri + (h1 ? 1 : 0)] = make_int4(jb2, incl - c2, __float_as_int(Sx), __float_as_int(Sy));
+        }
+        const int nr = __popc(hb1) + __popc(hb2);
+        __syncwarp();
+        for (int e0 = 0; e0 < total; e0 += 32) {
+            const int e = e0 + lane;
             bool pass = false;
             int4 en = make_int4(0, 0, 0, 0);
-            if (it < nc) {
+            if (e < total) {
+                int lo = 0, hi = nr - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (rng[mid].y <= e) lo = mid; else hi = mid - 1;
+                }
+                const int4 rg = rng[lo];
+                const int J = rg.x + (e - rg.y);
+                const float cSx = __int_as_float(rg.z), cSy = __int_as_float(rg.w);
+                const int jw = R.cl_win + J;
+                const float4 cj = a.cl_bbc[jw], hjb = a.cl_bbh[jw];
                 const float sz = tabz[wrap_cell(__float_as_int(cj.w) - ref.z, S.M[2]) + S.M[2]];
-                float dx = cj.x + Sx - bc.x, dy = cj.y + Sy - bc.y, dz = cj.z + sz - bc.z;
+                float dx = cj.x + cSx - bc.x, dy = cj.y + cSy - bc.y, dz = cj.z + sz - bc.z;
                 if (IMG) {
                     dx = img32(dx, S.Lf[0], S.invLf[0]);
                     dy = img32(dy, S.Lf[1], S.invLf[1]);
@@ -652,7 +663,7 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
                 pass = gx * gx + gy * gy + gz * gz < rclc2;
                 const bool nm = (J == I) || lkA.x == -2 || lkA.x == J || lkA.y == J || lkA.z == J ||
                                 lkA.w == J || lkB.x == J || lkB.y == J || lkB.z == J || lkB.w == J;
-                en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(Sx), __float_as_int(Sy),
+                en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(cSx), __float_as_int(cSy),
                                __float_as_int(sz));
             }
             const unsigned bal = __ballot_sync(0xffffffffu, pass);
@@ -662,6 +673,7 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
             }
             cnt += __popc(bal);
         }
+        __syncwarp();   // rng is rewritten by the next stencil round
     }
     if (lane == 0) {
         a.jl_cnt[cw] = cnt;
@@ -671,13 +683,15 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I) {
 
 // static schedule: warp w takes items w, w+W, w+2W, ...
 __global__ void __launch_bounds__(256, 4) k_jlist(SdmArgs a, const int* cl_prefix) {
+    __shared__ int4 rng_all[8][64];   // per warp: candidate ranges of one stencil round
+    int4* rng = rng_all[threadIdx.x >> 5];
     const int total = cl_prefix[a.nrep];
     const int W = gridDim.x * (blockDim.x >> 5);
     for (int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < total; item += W) {
         const int r = rep_by_item(cl_prefix, a.nrep, item);
         const int I = item - cl_prefix[r];
-        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) build_jlist<true>(a, r, I);
-        else build_jlist<false>(a, r, I);
+        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) build_jlist<true>(a, r, I, rng);
+        else build_jlist<false>(a, r, I, rng);
     }
 }
 
