@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 METRIC = "SDM lambda-state force evals/s at 23k atoms x 22 lambda, batched vs plain, 1 GB300"
 UNIT = "lambda-state evals/s"
 FLOP_PER_PAIR = 52  # FP32 flops per pair per state (FMA = 2, rsqrt = 1)
-# kernels of one batched evaluation: k_cells k_scan k_bucket k_colsort k_clusters
+# kernels of one batched evaluation: k_cells k_scan k_bucket k_cellsort k_clusters
 # k_jlist k_pair k_pert_prep k_perturb k_finalize k_mix
 KERNELS_PER_STEP = 11
 NREP = 22

@@ -123,7 +123,7 @@ struct sdm_handle {
 
 namespace {
 
-const char* const kKernelNames[] = {"k_cells", "k_scan", "k_bucket", "k_colsort", "k_clusters",
+const char* const kKernelNames[] = {"k_cells", "k_scan", "k_bucket", "k_cellsort", "k_clusters",
                                     "k_jlist", "k_pair", "k_pert_prep+k_perturb", "k_finalize+k_mix"};
 const int kNumTimed = 9;
 
@@ -572,7 +572,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     }
     // replica windows
     long long xo = 0;
-    int aw = 0, cw = 0, sw = 0;
+    int aw = 0, cw = 0, sw = 0, zw = 0;
     for (int s = 0; s < num_systems; ++s) {
         const SysHost& S = h->sys[s];
         for (int k = 0; k < S.replicas; ++k) {
@@ -582,6 +582,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
             r.x_off = xo;
             r.atom_win = aw;
             r.col_win = cw;
+            r.cel_win = zw;
             r.slot_win = sw;
             r.slot_cap = round8((long long)S.n + 8LL * S.dev.ncol + 8);
             r.cl_win = sw / 8;
@@ -589,12 +590,13 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
             xo += S.n;
             aw += S.n;
             cw += S.dev.ncol + 1;
+            zw += S.dev.ncol * S.dev.M[2] + 1;
             sw += r.slot_cap;
         }
     }
     h->nrep = (int)h->rep.size();
     h->total_particles = xo;
-    if (xo > (1LL << 30) || (long long)sw > (1LL << 30)) {
+    if (xo > (1LL << 30) || (long long)sw > (1LL << 30) || (long long)zw > (1LL << 30)) {
         delete h;
         return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "batch too large");
     }
@@ -612,7 +614,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     tot_cx = tot_n + (int)h->sys.size();
     tot_cxidx = std::max(tot_excl, 1);
     const int nrep = h->nrep;
-    const long long A = aw, Ccol = cw, Sl = sw, Cl = sw / 8;
+    const long long A = aw, Ccol = cw, Sl = sw, Cl = sw / 8, Ccel = zw;
     long long Pp = 0;
     for (auto& r : h->rep) Pp += 2LL * h->sys[r.sys].n;
     Arena ar;
@@ -633,8 +635,9 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_f = ar.take<double>(3 * xo);
     const size_t o_w = ar.take<double>(3 * A), o_ci = ar.take<int2>(A), o_inv = ar.take<int>(A);
     const size_t o_bk = ar.take<int>(A);
-    const size_t o_cnt = ar.take<int>(2 * Ccol + nrep + 4);  // counters block: col_cnt, col_fill, extz, work
-    const size_t o_aoff = ar.take<int>(Ccol), o_cl = ar.take<int>(Ccol);
+    const size_t o_cnt = ar.take<int>(2 * Ccel + nrep + 4);  // counters block: cel_cnt, cel_fill, extz, work
+    const size_t o_aoff = ar.take<int>(Ccol), o_cl = ar.take<int>(Ccol), o_ccnt = ar.take<int>(Ccol);
+    const size_t o_coff = ar.take<int>(Ccel);
     const size_t o_perm = ar.take<int>(Sl), o_clX = ar.take<float4>(Sl), o_clP = ar.take<float2>(Sl);
     const size_t o_sgrp = ar.take<int>(Sl), o_ex4 = ar.take<int4>(Sl);
     const size_t o_clm = ar.take<int>(Sl);
@@ -683,12 +686,14 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.cellinfo = at<int2>(B, o_ci);
     a.inv = at<int>(B, o_inv);
     a.bucket = at<int>(B, o_bk);
-    a.col_cnt = at<int>(B, o_cnt);
-    a.col_fill = a.col_cnt + Ccol;
-    a.extz = reinterpret_cast<unsigned*>(a.col_fill + Ccol);
+    a.cel_cnt = at<int>(B, o_cnt);
+    a.cel_fill = a.cel_cnt + Ccel;
+    a.extz = reinterpret_cast<unsigned*>(a.cel_fill + Ccel);
     a.work_counter = reinterpret_cast<int*>(a.extz + nrep);
-    h->counters = a.col_cnt;
-    h->counters_bytes = sizeof(int) * (size_t)(2 * Ccol + nrep + 4);
+    h->counters = a.cel_cnt;
+    h->counters_bytes = sizeof(int) * (size_t)(2 * Ccel + nrep + 4);
+    a.col_cnt = at<int>(B, o_ccnt);
+    a.cel_off = at<int>(B, o_coff);
     a.col_aoff = at<int>(B, o_aoff);
     a.col_cl = at<int>(B, o_cl);
     a.perm = at<int>(B, o_perm);
@@ -719,6 +724,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     h->done = at<int>(B, o_done);
     a.total_atoms = (int)A;
     a.total_cols = (int)Ccol;
+    a.total_cells = (int)Ccel;
     a.total_slots = (int)Sl;
     a.split = 1;
     a.ex_cap = 0;

@@ -1,15 +1,17 @@
 // sdm_kernels.cu -- CUDA kernels (sm_103a) of the SDM two-state force.
 //
 // Pipeline of one evaluation (every launch covers all replicas of all systems):
-//   k_cells     wrap coordinates, integer cells, column histogram
+//   k_cells     wrap coordinates, integer cells, cell histogram
 //   k_scan      per-replica column prefix sums (particles, clusters) and the
 //               global work-item prefix (last block)
-//   k_bucket    scatter particles into their column
-//   k_colsort   stable rank sort of each column by (z, particle index) -> slots
+//   k_bucket    scatter particles into their cell (cells of a column consecutive)
+//   k_cellsort  rank of every particle inside its cell by (z, particle index);
+//               cells are z-ordered within a column -> column slots
 //   k_clusters  cluster-local FP32 coordinates, parameters, bounding boxes,
 //               exclusion partners as slots
 //   k_pair      persistent main pass: every pair at the original coordinates
 //               (U0, F0), LJ + reaction field, FP32 math, fixed-point forces
+//   k_pert_prep the displaced particles' positions in both states
 //   k_perturb   perturbation pass: only pairs whose displacements differ, at
 //               both states -> u (FP64) and dF = F1 - F0 (fixed point)
 //   k_finalize  deterministic energy reductions, soft core, bias, weight s
@@ -147,7 +149,7 @@ __global__ void k_cells(SdmArgs a) {
         }
         const int col = c[0] * S.M[1] + c[1];
         a.cellinfo[gi] = make_int2(col, c[2]);
-        atomicAdd(&a.col_cnt[R.col_win + col], 1);
+        atomicAdd(&a.cel_cnt[R.cel_win + col * S.M[2] + c[2]], 1);
     }
     for (int gs = blockIdx.x * blockDim.x + threadIdx.x; gs < a.total_slots; gs += stride) {
         a.F0x[gs] = 0ull; a.F0y[gs] = 0ull; a.F0z[gs] = 0ull;
@@ -174,15 +176,23 @@ __global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int*
     const int r = blockIdx.x;
     const SdmRep& R = a.rep[r];
     const SdmSys& S = a.sys[R.sys];
-    const int ncol = S.ncol;
-    const int* cnt = a.col_cnt + R.col_win;
+    const int ncol = S.ncol, mz = S.M[2];
+    const int* ccnt = a.cel_cnt + R.cel_win;
+    int* coff = a.cel_off + R.cel_win;
+    int* cnt = a.col_cnt + R.col_win;
     int* aoff = a.col_aoff + R.col_win;
     int* cl = a.col_cl + R.col_win;
     const int per = (ncol + blockDim.x - 1) / blockDim.x;
     const int beg = min(ncol, (int)threadIdx.x * per);
     const int end = min(ncol, beg + per);
     int2 s = make_int2(0, 0);
-    for (int c = beg; c < end; ++c) { s.x += cnt[c]; s.y += (cnt[c] + 7) >> 3; }
+    for (int c = beg; c < end; ++c) {
+        int n = 0;
+        for (int z = 0; z < mz; ++z) n += ccnt[c * mz + z];
+        cnt[c] = n;
+        s.x += n;
+        s.y += (n + 7) >> 3;
+    }
     int2 inc = warp_incl_scan2(s);
     const int wid = threadIdx.x >> 5;
     if (lane_id() == 31) wsum[wid] = inc;
@@ -198,12 +208,15 @@ __global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int*
     for (int c = beg; c < end; ++c) {
         aoff[c] = base.x;
         cl[c] = base.y;
+        int o = base.x;
+        for (int z = 0; z < mz; ++z) { coff[c * mz + z] = o; o += ccnt[c * mz + z]; }
         base.x += cnt[c];
         base.y += (cnt[c] + 7) >> 3;
     }
     if (threadIdx.x == blockDim.x - 1) {
         aoff[ncol] = base.x;
         cl[ncol] = base.y;
+        coff[ncol * mz] = base.x;
         a.ncl[r] = base.y;
     }
     // last block computes the item prefix over replicas (no waiting involved)
@@ -249,69 +262,55 @@ __global__ void k_bucket(SdmArgs a) {
     for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < a.total_atoms; gi += stride) {
         const int r = rep_by_atom(a.rep, a.nrep, gi);
         const SdmRep& R = a.rep[r];
-        const int col = a.cellinfo[gi].x;
-        const int pos = atomicAdd(&a.col_fill[R.col_win + col], 1);
-        a.bucket[R.atom_win + a.col_aoff[R.col_win + col] + pos] = gi - R.atom_win;
+        const int2 ci = a.cellinfo[gi];
+        const int cell = R.cel_win + ci.x * a.sys[R.sys].M[2] + ci.y;
+        const int pos = atomicAdd(&a.cel_fill[cell], 1);
+        a.bucket[R.atom_win + a.cel_off[cell] + pos] = gi - R.atom_win;
     }
 }
 
 // ------------------------------------------------------------------------- //
-// K4: rank sort of every column by (z, particle)                            //
+// K4: rank sort of every cell by (z, particle)                              //
 // ------------------------------------------------------------------------- //
-// keys are the bit patterns of the wrapped z coordinates (non-negative
-// doubles order like their bits once -0.0 is canonicalised) with the particle
-// index as tie-break: integer compares only (FP64 compares are slow on GB300)
+// The bucket holds each column's particles cell by cell (z cells ascending),
+// and the z cell is monotone in z: ranking every particle inside its own cell
+// gives the column's order by (z, particle).  Keys are the bit patterns of the
+// wrapped z coordinates (non-negative doubles order like their bits once -0.0
+// is canonicalised) with the particle index as tie-break: integer compares
+// only (FP64 compares are slow on GB300).
 __device__ __forceinline__ unsigned long long zkey(double z) {
     return (unsigned long long)__double_as_longlong(__dadd_rn(z, 0.0));
 }
 
-__global__ void __launch_bounds__(128) k_colsort(SdmArgs a) {
-    __shared__ unsigned long long kz[4][128];
-    __shared__ int ki[4][128];
-    const int wib = threadIdx.x >> 5;
-    const int lane = lane_id();
-    const int nwarps = gridDim.x * (blockDim.x >> 5);
-    for (int gc = blockIdx.x * (blockDim.x >> 5) + wib; gc < a.total_cols; gc += nwarps) {
+__global__ void k_cellsort(SdmArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < a.total_atoms; gi += stride) {
+        const int r = rep_by_atom(a.rep, a.nrep, gi);
+        const SdmRep& R = a.rep[r];
+        const int mz = a.sys[R.sys].M[2];
+        const int ai = a.bucket[gi];
+        const int2 ci = a.cellinfo[R.atom_win + ai];
+        const int cell = R.cel_win + ci.x * mz + ci.y;
+        const int cb = a.cel_off[cell], ce = a.cel_off[cell + 1];
+        const unsigned long long zi = zkey(a.w[3 * (size_t)(R.atom_win + ai) + 2]);
+        int rank = 0;
+        for (int q = cb; q < ce; ++q) {
+            const int aj = a.bucket[R.atom_win + q];
+            const unsigned long long zj = zkey(a.w[3 * (size_t)(R.atom_win + aj) + 2]);
+            rank += (zj < zi) || (zj == zi && aj < ai);
+        }
+        const int col = R.col_win + ci.x;
+        const int slot = 8 * a.col_cl[col] + (cb - a.col_aoff[col]) + rank;
+        a.perm[R.slot_win + slot] = ai;
+        a.inv[R.atom_win + ai] = slot;
+    }
+    // padding slots at the end of every column
+    for (int gc = blockIdx.x * blockDim.x + threadIdx.x; gc < a.total_cols; gc += stride) {
         const int r = rep_by_col(a.rep, a.nrep, gc);
         const SdmRep& R = a.rep[r];
-        const SdmSys& S = a.sys[R.sys];
-        const int c = gc - R.col_win;
-        if (c >= S.ncol) continue;
-        const int n = a.col_cnt[R.col_win + c];
-        const int a0 = a.col_aoff[R.col_win + c];
-        const int sbase = 8 * a.col_cl[R.col_win + c];
-        const int send = 8 * a.col_cl[R.col_win + c + 1];
-        const int* bk = a.bucket + R.atom_win + a0;
-        if (n == 0) continue;
-        for (int ib = 0; ib < n; ib += 32) {
-            const int ii = ib + lane;
-            int ai = -1;
-            unsigned long long zi = 0ull;
-            if (ii < n) { ai = bk[ii]; zi = zkey(a.w[3 * (size_t)(R.atom_win + ai) + 2]); }
-            int rank = 0;
-            for (int jb = 0; jb < n; jb += 128) {
-                __syncwarp();
-                for (int q = lane; q < 128 && jb + q < n; q += 32) {
-                    const int aj = bk[jb + q];
-                    ki[wib][q] = aj;
-                    kz[wib][q] = zkey(a.w[3 * (size_t)(R.atom_win + aj) + 2]);
-                }
-                __syncwarp();
-                const int m = min(128, n - jb);
-                if (ii < n)
-                    for (int q = 0; q < m; ++q) {
-                        const unsigned long long zj = kz[wib][q];
-                        const int aj = ki[wib][q];
-                        rank += (zj < zi) || (zj == zi && aj < ai);
-                    }
-            }
-            if (ii < n) {
-                const int slot = sbase + rank;
-                a.perm[R.slot_win + slot] = ai;
-                a.inv[R.atom_win + ai] = slot;
-            }
-        }
-        for (int s = sbase + n + lane; s < send; s += 32) a.perm[R.slot_win + s] = -1;
+        if (gc - R.col_win >= a.sys[R.sys].ncol) continue;
+        const int send = 8 * a.col_cl[gc + 1];
+        for (int s = 8 * a.col_cl[gc] + a.col_cnt[gc]; s < send; ++s) a.perm[R.slot_win + s] = -1;
     }
 }
 
@@ -1781,7 +1780,7 @@ cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* cl_prefix, 
     mark();
     k_bucket<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
     mark();
-    k_colsort<<<grid_for((long long)a.total_cols * 32, 128), 128, 0, st>>>(a);
+    k_cellsort<<<grid_for(a.total_atoms > a.total_cols ? a.total_atoms : a.total_cols, 256), 256, 0, st>>>(a);
     mark();
     k_clusters<<<grid_for(a.total_slots, 256), 256, 0, st>>>(a);
     mark();

@@ -16,7 +16,9 @@
 //     cellinfo int2    (column id, z cell)
 //     inv      int     particle -> slot
 //   per replica, column-indexed (window = ncol+1)
-//     col_cnt, col_fill (counters), col_aoff (atom prefix), col_cl (cluster prefix)
+//     col_cnt, col_aoff (atom prefix), col_cl (cluster prefix)
+//   per replica, cell-indexed (window = ncol*Mz+1; cell = column*Mz + z cell)
+//     cel_cnt, cel_fill (counters), cel_off (atom prefix; a column's cells are consecutive)
 //   per replica, slot-indexed (window = slot_cap = num_particles + 8*ncol + 8)
 //     perm     int     slot -> particle (-1 padding)
 //     clX      float4  cluster-local x,y,z (FP32) and q*sqrt(K)
@@ -82,6 +84,7 @@ struct SdmRep {
     long long x_off;  // particle offset into the concatenated coordinates / forces
     int atom_win;     // particle-indexed window base
     int col_win;      // column-indexed window base (ncol+1 per replica)
+    int cel_win;      // cell-indexed window base (ncol*M[2]+1 per replica; cell = column*M[2] + z cell)
     int slot_win;     // slot window base
     int slot_cap;     // slots in the window
     int cl_win;       // cluster window base (slot_win/8)
@@ -117,8 +120,10 @@ struct SdmArgs {
     double* w;
     int2* cellinfo;
     int* inv;
-    int* col_cnt;
-    int* col_fill;
+    int* col_cnt;        // particles per column (written by k_scan)
+    int* cel_cnt;        // particles per cell (counter)
+    int* cel_fill;       // bucket fill per cell (counter)
+    int* cel_off;        // particle prefix per cell within the replica
     int* col_aoff;
     int* col_cl;
     int* bucket;
@@ -161,6 +166,7 @@ struct SdmArgs {
     // totals
     int total_atoms;     // sum of n over replicas
     int total_cols;      // sum of ncol over replicas
+    int total_cells;     // sum of ncol*M[2]+1 over replicas
     int total_slots;     // sum of slot_cap over replicas
     int total_pert;      // sum of 2*nD
     int split;           // work items per i-cluster
