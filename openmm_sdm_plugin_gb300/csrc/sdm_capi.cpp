@@ -243,6 +243,10 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
         g.M[k] = M;
         g.box[k] = d.box[k];
         g.invL[k] = 1.0 / d.box[k];
+        {
+            const double lim = d.box[k] * (1.0 - 9.094947017729282e-13);   // L (1 - 2^-40)
+            std::memcpy(&g.wrap_lim[k], &lim, sizeof lim);
+        }
         g.g[k] = d.box[k] / (double)M;
         g.invg[k] = (double)M / d.box[k];
         g.Lf[k] = (float)d.box[k];

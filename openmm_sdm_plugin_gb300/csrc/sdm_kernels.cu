@@ -143,7 +143,11 @@ __global__ void k_cells(SdmArgs a) {
         int c[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            double w = wrap1(xp[k], S.box[k], S.invL[k]);
+            // 0 <= v < L (1 - 2^-40): floor(v / L) rounds to 0 and the wrap is
+            // the identity; only other coordinates take the FP64 wrap
+            double w = xp[k];
+            const long long b = __double_as_longlong(w);
+            if (!(b >= 0 && b < S.wrap_lim[k])) w = wrap1(w, S.box[k], S.invL[k]);
             a.w[3 * (size_t)gi + k] = w;
             c[k] = cell_of(w, S.invg[k], S.M[k]);
         }
@@ -279,7 +283,8 @@ __global__ void k_bucket(SdmArgs a) {
 // is canonicalised) with the particle index as tie-break: integer compares
 // only (FP64 compares are slow on GB300).
 __device__ __forceinline__ unsigned long long zkey(double z) {
-    return (unsigned long long)__double_as_longlong(__dadd_rn(z, 0.0));
+    const unsigned long long b = (unsigned long long)__double_as_longlong(z);
+    return b == 0x8000000000000000ull ? 0ull : b;   // -0.0 -> +0.0 without the FP64 pipe
 }
 
 __global__ void k_cellsort(SdmArgs a) {
@@ -351,8 +356,9 @@ __global__ void k_clusters(SdmArgs a) {
             if (ee - eb > 4) {
                 ex = make_int4(-2, -2, -2, -2);
             } else {
-                int v[4] = {-1, -1, -1, -1};
-                for (int k = eb; k < ee; ++k) v[k - eb] = a.inv[R.atom_win + a.excl_idx[k]];
+                int v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = (eb + u < ee) ? a.inv[R.atom_win + a.excl_idx[eb + u]] : -1;
                 ex = make_int4(v[0], v[1], v[2], v[3]);
             }
         } else {
@@ -380,29 +386,30 @@ __global__ void k_clusters(SdmArgs a) {
                 hi[k] = fmaxf(hi[k], __shfl_xor_sync(gmask, hi[k], o, 8));
             }
         // exclusion-linked clusters: distinct clusters (other than C) holding
-        // partners of this cluster's particles; -2 when more than 8 or unknown
-        int link[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
-        int nlink = 0;
+        // partners of this cluster's particles, ascending; -2 when more than 8
+        // or unknown.  Extracted as successive minima over the 8-lane group.
+        const int e4[4] = {ex.x, ex.y, ex.z, ex.w};
+        int pc[4];
         bool many = false;
-        for (int l = 0; l < 8; ++l) {
-            int e4[4];
-            e4[0] = __shfl_sync(gmask, ex.x, l, 8);
-            e4[1] = __shfl_sync(gmask, ex.y, l, 8);
-            e4[2] = __shfl_sync(gmask, ex.z, l, 8);
-            e4[3] = __shfl_sync(gmask, ex.w, l, 8);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int e = e4[k];
-                if (e == -2) many = true;
-                if (e < 0) continue;
-                const int cc = e >> 3;
-                if (cc == C) continue;
-                bool seen = false;
-                for (int u = 0; u < nlink; ++u) seen |= (link[u] == cc);
-                if (!seen) {
-                    if (nlink < 8) link[nlink++] = cc; else many = true;
-                }
-            }
+        for (int k = 0; k < 4; ++k) {
+            many |= (e4[k] == -2);
+            const int cc = e4[k] >> 3;
+            pc[k] = (e4[k] >= 0 && cc != C) ? cc : 0x7fffffff;
+        }
+        many = __any_sync(gmask, many);
+        int link[8];
+        int last = -1;
+#pragma unroll
+        for (int u = 0; u < 9; ++u) {
+            int m = 0x7fffffff;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) m = (pc[k] > last && pc[k] < m) ? pc[k] : m;
+#pragma unroll
+            for (int o = 1; o < 8; o <<= 1) m = min(m, __shfl_xor_sync(gmask, m, o, 8));
+            if (u < 8) link[u] = (m == 0x7fffffff) ? -1 : m;
+            else if (m != 0x7fffffff) many = true;
+            last = m;
         }
         // absolute z of the first and last particle (rounded outwards, monotone
         // along a column), for the z-range searches of the list builder
@@ -1719,23 +1726,28 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
 // ------------------------------------------------------------------------- //
 // K9: mix                                                                   //
 // ------------------------------------------------------------------------- //
+// fixed point 2^32 -> double: one conversion, the scale applied to the
+// exponent field (exact: every nonzero value is >= 1 before scaling)
+__device__ __forceinline__ double fix_to_double(unsigned long long v) {
+    const double d = (double)(long long)v;
+    if (v == 0ull) return 0.0;
+    return __hiloint2double(__double2hiint(d) - (32 << 20), __double2loint(d));
+}
+
 __global__ void k_mix(SdmArgs a) {
     const int stride = gridDim.x * blockDim.x;
-    const double sc = 1.0 / SDM_FIX_SCALE;
     for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < a.total_atoms; gi += stride) {
         const int r = rep_by_atom(a.rep, a.nrep, gi);
         const SdmRep& R = a.rep[r];
         const int i = gi - R.atom_win;
         const size_t gsl = (size_t)R.slot_win + a.inv[gi];
         const double s = a.forces ? a.results[(size_t)r * SDM_NRESULTS + SDM_R_S] : 0.0;
-        const double f0[3] = {(double)(long long)a.F0x[gsl] * sc, (double)(long long)a.F0y[gsl] * sc,
-                              (double)(long long)a.F0z[gsl] * sc};
-        const double df[3] = {(double)(long long)a.dFx[gsl] * sc, (double)(long long)a.dFy[gsl] * sc,
-                              (double)(long long)a.dFz[gsl] * sc};
+        const double f0[3] = {fix_to_double(a.F0x[gsl]), fix_to_double(a.F0y[gsl]), fix_to_double(a.F0z[gsl])};
+        const double df[3] = {fix_to_double(a.dFx[gsl]), fix_to_double(a.dFy[gsl]), fix_to_double(a.dFz[gsl])};
         const size_t o = 3 * (size_t)(R.x_off + i);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            if (a.forces) a.forces[o + k] = f0[k] + s * df[k];
+            if (a.forces) a.forces[o + k] = __fma_rn(s, df[k], f0[k]);
             if (a.F0out) a.F0out[o + k] = f0[k];
             if (a.F1out) a.F1out[o + k] = f0[k] + df[k];
         }

@@ -53,6 +53,7 @@ struct SdmSys {
     int img_static;   // 1 if the x/y extents already force per-pair minimum image
     float tz;         // z threshold: image mode unless max cluster z extent < tz
     double box[3], invL[3], g[3], invg[3];
+    long long wrap_lim[3];  // bit pattern of L(1 - 2^-40): 0 <= v below it wraps to v itself
     double rc;
     float Lf[3], invLf[3];
     float gf[3];      // (float)g, for conservative prefilters only
