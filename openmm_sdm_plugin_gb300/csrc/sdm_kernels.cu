@@ -457,15 +457,17 @@ struct Ring {                   // one tile ring: 64 prepared j entries
     float4 b[SDM_RING];         // (hs, se, mask bits, slot bits)
 };
 
-#define SDM_CH 16               // cluster-pair list entries per staged chunk
+#define SDM_CH 12               // cluster-pair list entries per staged chunk
 
 // Two-level cp.async pipeline: list entries two chunks ahead, the candidate
 // particles (8 per entry) one chunk ahead of the chunk being filtered.
-// i-cluster parameters of particles (2u, 2u+1): qh[u] = (q, q', sigma/2, sigma'/2),
-// se[u] = (2 sqrt(eps), 2 sqrt(eps'))
+// i-cluster data of particles (2u, 2u+1), read as broadcasts: qh[u] = (q, q',
+// sigma/2, sigma'/2), se[u] = (2 sqrt(eps), 2 sqrt(eps')), nx/ny/nz[u] the
+// negated coordinates (d = x_j + (-x_i) rounds like x_j - x_i)
 struct IParams {
     float4 qh[4];
     float2 se[4];
+    float2 nx[4], ny[4], nz[4];
 };
 
 struct EvalSmem {
@@ -497,11 +499,9 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// The 8 i particles in pairs (2u, 2u+1) for the packed FP32x2 pipe:
-// coordinates negated (d = x_j + (-x_i) rounds like x_j - x_i) and force
-// accumulators holding sum_j fs (x_j - x_i), i.e. minus the force on i.
+// Force accumulators of the 8 i particles in pairs (2u, 2u+1) for the packed
+// FP32x2 pipe: sum_j fs (x_j - x_i), i.e. minus the force on i.
 struct ICluster {
-    float2 nx[4], ny[4], nz[4];
     float2 ax[4], ay[4], az[4];
 };
 
@@ -730,9 +730,9 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
     int cnt = 0;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        float2 dx = __fadd2_rn(xs, ic.nx[u]);
-        float2 dy = __fadd2_rn(ys, ic.ny[u]);
-        float2 dz = __fadd2_rn(zs, ic.nz[u]);
+        float2 dx = __fadd2_rn(xs, ip.nx[u]);
+        float2 dy = __fadd2_rn(ys, ip.ny[u]);
+        float2 dz = __fadd2_rn(zs, ip.nz[u]);
         if (IMG) {
             dx = make_float2(img32(dx.x, S.Lf[0], S.invLf[0]), img32(dx.y, S.Lf[0], S.invLf[0]));
             dy = make_float2(img32(dy.x, S.Lf[1], S.invLf[1]), img32(dy.y, S.Lf[1], S.invLf[1]));
@@ -844,9 +844,11 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            ic.nx[u] = make_float2(-__shfl_sync(0xffffffffu, xi4.x, 2 * u), -__shfl_sync(0xffffffffu, xi4.x, 2 * u + 1));
-            ic.ny[u] = make_float2(-__shfl_sync(0xffffffffu, xi4.y, 2 * u), -__shfl_sync(0xffffffffu, xi4.y, 2 * u + 1));
-            ic.nz[u] = make_float2(-__shfl_sync(0xffffffffu, xi4.z, 2 * u), -__shfl_sync(0xffffffffu, xi4.z, 2 * u + 1));
+            if (lane < 8 && (lane >> 1) == u) {
+                reinterpret_cast<float*>(&sm.ip.nx[u])[lane & 1] = -xi4.x;
+                reinterpret_cast<float*>(&sm.ip.ny[u])[lane & 1] = -xi4.y;
+                reinterpret_cast<float*>(&sm.ip.nz[u])[lane & 1] = -xi4.z;
+            }
             ic.ax[u] = make_float2(0.f, 0.f); ic.ay[u] = ic.ax[u]; ic.az[u] = ic.ax[u];
         }
         __syncwarp();
