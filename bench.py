@@ -40,7 +40,7 @@ FLOP_PER_PAIR = 52  # FP32 flops per pair per state (FMA = 2, rsqrt = 1)
 # k_jlist k_pair k_pert_prep k_perturb k_finalize k_mix
 KERNELS_PER_STEP = 11
 NREP = 22
-K_PAIR_DRAM_BYTES_PER_LAUNCH = 128.639232e6 + 6.411776e6
+K_PAIR_DRAM_BYTES_PER_LAUNCH = 122.466560e6 + 6.279680e6
 
 
 def _peaks():
