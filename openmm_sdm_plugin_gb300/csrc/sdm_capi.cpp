@@ -340,11 +340,12 @@ sdm_status upload_topology(sdm_handle* h) {
     // displacement change) in the arena
     std::vector<float> q, hs, se;
     std::vector<int> grp, mol, eoff, eidx, D, cxo, cxi;
-    std::vector<double> dd;
+    std::vector<double> dd, org;
     std::vector<float> tab;
+    std::vector<int4> ex4;
     std::vector<int2> sten;
     std::vector<SdmSys> sd;
-    int atom = 0, excl = 0, dbase = 0, cxbase = 0, tabbase = 0;
+    int atom = 0, excl = 0, dbase = 0, cxbase = 0, tabbase = 0, orgbase = 0;
     for (auto& s : h->sys) {
         SdmSys g = s.dev;
         g.atom_base = atom;
@@ -353,6 +354,7 @@ sdm_status upload_topology(sdm_handle* h) {
         g.nD = (int)s.D.size();
         g.cx_base = cxbase;
         g.shift_base = tabbase;
+        g.org_base = orgbase;
         q.insert(q.end(), s.q.begin(), s.q.end());
         hs.insert(hs.end(), s.hs.begin(), s.hs.end());
         se.insert(se.end(), s.se.begin(), s.se.end());
@@ -360,6 +362,13 @@ sdm_status upload_topology(sdm_handle* h) {
         mol.insert(mol.end(), s.mol.begin(), s.mol.end());
         dd.insert(dd.end(), s.d.begin(), s.d.end());
         for (int i = 0; i < s.n; ++i) eoff.push_back(excl + s.excl_off[i]);
+        for (int i = 0; i < s.n; ++i) {
+            const int b = s.excl_off[i], e = s.excl_off[i + 1];
+            int v[4] = {-1, -1, -1, -1};
+            if (e - b > 4) v[0] = v[1] = v[2] = v[3] = -2;
+            else for (int k = b; k < e; ++k) v[k - b] = s.excl_idx[k];
+            ex4.push_back(make_int4(v[0], v[1], v[2], v[3]));
+        }
         eidx.insert(eidx.end(), s.excl_idx.begin(), s.excl_idx.end());
         D.insert(D.end(), s.D.begin(), s.D.end());
         for (size_t k = 0; k < s.D.size(); ++k) cxo.push_back((int)cxi.size() + s.cx_off[k]);
@@ -368,6 +377,8 @@ sdm_status upload_topology(sdm_handle* h) {
         cxo.push_back(cx_total);
         for (int k = 0; k < 3; ++k)
             for (int m = -g.M[k]; m <= g.M[k]; ++m) tab.push_back((float)((double)m * g.g[k]));
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < g.M[k]; ++c) org.push_back((double)c * g.g[k]);
         g.hst_base = (int)sten.size();
         g.hst_count = (int)s.hst.size();
         sten.insert(sten.end(), s.hst.begin(), s.hst.end());
@@ -379,6 +390,7 @@ sdm_status upload_topology(sdm_handle* h) {
         dbase += (int)s.D.size();
         cxbase += (int)s.D.size() + 1;
         tabbase += 2 * (g.M[0] + g.M[1] + g.M[2]) + 3;
+        orgbase += g.M[0] + g.M[1] + g.M[2];
         s.dev = g;
         sd.push_back(g);
     }
@@ -398,6 +410,8 @@ sdm_status upload_topology(sdm_handle* h) {
     if ((st = put(a.topo_se, se.data(), se.size() * 4))) return st;
     if ((st = put(a.topo_grp, grp.data(), grp.size() * 4))) return st;
     if ((st = put(a.topo_mol, mol.data(), mol.size() * 4))) return st;
+    if ((st = put(a.topo_ex4, ex4.data(), ex4.size() * sizeof(int4)))) return st;
+    if ((st = put(a.cell_org, org.data(), org.size() * sizeof(double)))) return st;
     if ((st = put(a.topo_d, dd.data(), dd.size() * 8))) return st;
     if ((st = put(a.excl_off, eoff.data(), eoff.size() * 4))) return st;
     if ((st = put(a.excl_idx, eidx.data(), eidx.size() * 4))) return st;
@@ -605,13 +619,14 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
         return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "batch too large");
     }
     // arena layout
-    int tot_n = 0, tot_excl = 0, tot_D = 0, tot_cx = 0, tot_tab = 0, tot_cxidx = 0;
+    int tot_n = 0, tot_excl = 0, tot_D = 0, tot_cx = 0, tot_tab = 0, tot_cxidx = 0, tot_org = 0;
     for (auto& s : h->sys) {
         tot_n += s.n;
         tot_excl += (int)s.excl_idx.size();
         tot_D += (int)s.D.size();
         tot_cx += (int)s.D.size() + 1;
         tot_tab += 2 * (s.dev.M[0] + s.dev.M[1] + s.dev.M[2]) + 3;
+        tot_org += s.dev.M[0] + s.dev.M[1] + s.dev.M[2];
     }
     // the displacement map may change later: reserve the worst case (every particle displaced)
     tot_D = std::max(tot_D, tot_n);
@@ -627,7 +642,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_rep = ar.take<SdmRep>(nrep);
     const size_t o_q = ar.take<float>(tot_n), o_hs = ar.take<float>(tot_n), o_se = ar.take<float>(tot_n);
     const size_t o_grp = ar.take<int>(tot_n), o_d = ar.take<double>(3LL * tot_n);
-    const size_t o_mol = ar.take<int>(tot_n);
+    const size_t o_mol = ar.take<int>(tot_n), o_ex4t = ar.take<int4>(tot_n);
+    const size_t o_org = ar.take<double>(std::max(tot_org, 1));
     const size_t o_eoff = ar.take<int>(tot_n + 1), o_eidx = ar.take<int>(std::max(tot_excl, 1));
     const size_t o_D = ar.take<int>(std::max(tot_D, 1)), o_cxo = ar.take<int>(tot_cx + 1);
     const size_t o_cxi = ar.take<int>(tot_cxidx), o_tab = ar.take<float>(tot_tab);
@@ -674,6 +690,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.topo_se = at<float>(B, o_se);
     a.topo_grp = at<int>(B, o_grp);
     a.topo_mol = at<int>(B, o_mol);
+    a.topo_ex4 = at<int4>(B, o_ex4t);
+    a.cell_org = at<double>(B, o_org);
     a.topo_d = at<double>(B, o_d);
     a.excl_off = at<int>(B, o_eoff);
     a.excl_idx = at<int>(B, o_eidx);

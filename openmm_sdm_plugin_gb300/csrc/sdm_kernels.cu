@@ -308,6 +308,11 @@ __global__ void k_cellsort(SdmArgs a) {
         const int slot = 8 * a.col_cl[col] + (cb - a.col_aoff[col]) + rank;
         a.perm[R.slot_win + slot] = ai;
         a.inv[R.atom_win + ai] = slot;
+        if ((slot & 7) == 0) {   // a cluster's reference cell is its first particle's cell
+            const int m1 = a.sys[R.sys].M[1];
+            const int cx = ci.x / m1;
+            a.cl_ref[R.cl_win + (slot >> 3)] = make_int4(cx, ci.x - cx * m1, ci.y, ci.x);
+        }
     }
     // padding slots at the end of every column
     for (int gc = blockIdx.x * blockDim.x + threadIdx.x; gc < a.total_cols; gc += stride) {
@@ -334,11 +339,10 @@ __global__ void k_clusters(SdmArgs a) {
         const int C = s >> 3, t = s & 7;
         if (C >= a.ncl[r]) continue;   // uniform over the 8-lane group
         const int p = a.perm[gs];
-        const int p0 = a.perm[R.slot_win + 8 * C];
-        const int2 ci0 = a.cellinfo[R.atom_win + p0];
-        const int cx = ci0.x / S.M[1], cy = ci0.x - cx * S.M[1], cz = ci0.y;
-        const double Rr[3] = {__dmul_rn((double)cx, S.g[0]), __dmul_rn((double)cy, S.g[1]),
-                              __dmul_rn((double)cz, S.g[2])};
+        const int4 ref = a.cl_ref[R.cl_win + C];   // written by k_cellsort
+        const int cx = ref.x, cy = ref.y, cz = ref.z;
+        const double* org = a.cell_org + S.org_base;
+        const double Rr[3] = {org[cx], org[S.M[0] + cy], org[S.M[0] + S.M[1] + cz]};
         float X[3];
         float4 q4;
         float2 p2;
@@ -352,13 +356,14 @@ __global__ void k_clusters(SdmArgs a) {
             q4 = make_float4(X[0], X[1], X[2], a.topo_q[ta]);
             p2 = make_float2(a.topo_hs[ta], a.topo_se[ta]);
             g = a.topo_grp[ta];
-            const int eb = a.excl_off[ta], ee = a.excl_off[ta + 1];
-            if (ee - eb > 4) {
+            const int4 pe = a.topo_ex4[ta];
+            if (pe.x == -2) {
                 ex = make_int4(-2, -2, -2, -2);
             } else {
+                const int pv[4] = {pe.x, pe.y, pe.z, pe.w};
                 int v[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = (eb + u < ee) ? a.inv[R.atom_win + a.excl_idx[eb + u]] : -1;
+                for (int u = 0; u < 4; ++u) v[u] = (pv[u] >= 0) ? a.inv[R.atom_win + pv[u]] : -1;
                 ex = make_int4(v[0], v[1], v[2], v[3]);
             }
         } else {
@@ -421,7 +426,6 @@ __global__ void k_clusters(SdmArgs a) {
         if (t == 0) {
             const int cw = R.cl_win + C;
             a.cl_zb[cw] = make_float2(__double2float_rd(wz0) - 1.0e-4f, __double2float_ru(wzl) + 1.0e-4f);
-            a.cl_ref[cw] = make_int4(cx, cy, cz, ci0.x);
             // w: the reference z cell, so candidate scans need no cl_ref load
             a.cl_bbc[cw] = make_float4(__fmul_rn(0.5f, __fadd_rn(lo[0], hi[0])),
                                        __fmul_rn(0.5f, __fadd_rn(lo[1], hi[1])),

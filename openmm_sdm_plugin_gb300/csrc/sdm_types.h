@@ -63,6 +63,7 @@ struct SdmSys {
     int nD;           // displaced particles
     int D_base;       // offset into D_idx
     int shift_base;   // offset into shift_tab: 3 tables of 2*Mk+1 floats (index n+Mk)
+    int org_base;     // offset into cell_org: 3 tables of Mk doubles, c * g[k]
     int cx_base;      // offset into cx_off/cx_idx (changed-pair exclusions per displaced particle)
     int half_geo;     // 1: pairs of columns are owned through the forward half stencil
                       // (offset ox>0, or ox==0 and oy>0; own column J>=I); 0: by lower column id
@@ -103,6 +104,7 @@ struct SdmArgs {
     const float* topo_se;
     const int* topo_grp;
     const int* topo_mol;  // exclusion component (molecule) id
+    const int4* topo_ex4; // up to 4 exclusion partners (system-local; -1 none, -2 more than 4)
     const double* topo_d;
     const int* excl_off;
     const int* excl_idx;
@@ -110,6 +112,7 @@ struct SdmArgs {
     const int* cx_off;    // per displaced particle: changed-pair exclusion partners
     const int* cx_idx;
     const float* shift_tab;
+    const double* cell_org;  // cell origins c * g[k] (FP64, as the kernels would compute them)
     const double* params; // nrep * SDM_NPARAMS
     // input / output
     const double* x;      // concatenated coordinates
