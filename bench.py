@@ -327,17 +327,30 @@ def main():
         if st != 0:
             raise capi.SdmError(st, L.sdm_last_error(h.h).decode())
 
-    for _ in range(warm):
-        e2e_step()
-    e2e_ms = []
-    for _ in range(args.steps):
-        flush()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_step()   # H2D copy, evaluation, D2H copy, synchronise
-        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    def e2e_run():
+        for _ in range(warm):
+            e2e_step()
+        ms = []
+        for _ in range(args.steps):
+            flush()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2e_step()   # host coordinates in, evaluation, host results and forces out, synchronise
+            ms.append(1e3 * (time.perf_counter() - t0))
+        return ms
+
+    # page-locked buffers: k_cells reads the coordinates in host memory over the
+    # host link (SDM_OPT_ZERO_COPY, the library default), results and forces
+    # return by copy ...
+    e2e_ms = e2e_run()
     tot_e = max_over_ranks(sum(e2e_ms) / 1e3, dist, dev)
     e2e = whole_job_rate(NREP * args.steps, world, tot_e)
+    # ... and, for comparison, coordinates staged through a device copy too
+    h.set_option(capi.OPT_ZERO_COPY, 0)
+    e2e_ms_st = e2e_run()
+    h.set_option(capi.OPT_ZERO_COPY, 1)
+    tot_es = max_over_ranks(sum(e2e_ms_st) / 1e3, dist, dev)
+    e2e_staged = whole_job_rate(NREP * args.steps, world, tot_es)
     # check the batch result once against nothing but itself: status clean
     status = h.check_status()
 
@@ -387,7 +400,10 @@ def main():
                   "workload": "config1: one 22,580-particle replica per call (CUDA graph)"},
         "batched_over_plain": value / world / plain,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": sum(e2e_ms) / len(e2e_ms), "path": "sdm_evaluate (host C ABI, pinned buffers)"},
+                "ms_per_step": sum(e2e_ms) / len(e2e_ms),
+                "path": "sdm_evaluate (host C ABI) on page-locked host buffers: coordinates read in place, results and forces copied out",
+                "staged_copies": {"value": e2e_staged, "ms_per_step": sum(e2e_ms_st) / len(e2e_ms_st),
+                                  "path": "same call, SDM_OPT_ZERO_COPY=0: cudaMemcpyAsync in and out"}},
         "roofline": roof,
         "kernel_ms": breakdown,
         "cpu_baseline": cpu,

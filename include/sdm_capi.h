@@ -161,7 +161,8 @@ sdm_status sdm_set_params(sdm_handle* h, int replica, const double* params);
  *   x        [sum over replicas of 3*num_particles] FP64 coordinates
  *   results  [num_replicas * SDM_NRESULTS] (may be NULL)
  *   forces   [sum over replicas of 3*num_particles] mixed force F (may be NULL)
- * Copies in, evaluates, copies out and synchronises.  Replaces one SDM step's
+ * Copies in, evaluates, copies out and synchronises (page-locked coordinates
+ * are read in place, see SDM_OPT_ZERO_COPY).  Replaces one SDM step's
  * force part: LangevinIntegratorSDM.cpp:158-176 with
  * ReferenceSDMKernels.cpp:202-318 (minus the Langevin update). */
 sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double* forces);
@@ -190,8 +191,11 @@ enum {
     SDM_OPT_CTAS_PER_SM = 3,  /* persistent pair-kernel CTAs per SM (1..4, default 4); the launch
                                  never exceeds the CTAs that fit (SDM_OPT_PAIR_RESIDENT) */
     SDM_OPT_VERIFY = 4,       /* 1 = sdm_evaluate checks the device status word after each call */
-    SDM_OPT_PAIR_RESIDENT = 5 /* read only: pair-kernel CTAs per SM that are resident for the
-                                 current SDM_OPT_CTAS_PER_SM (occupancy calculator) */
+    SDM_OPT_PAIR_RESIDENT = 5, /* read only: pair-kernel CTAs per SM that are resident for the
+                                  current SDM_OPT_CTAS_PER_SM (occupancy calculator) */
+    SDM_OPT_ZERO_COPY = 6     /* 1 = sdm_evaluate reads page-locked coordinates (cudaHostAlloc /
+                                 cudaHostRegister) in place instead of staging them through a
+                                 device copy; results and forces are always copied out (default 1) */
 };
 sdm_status sdm_set_option(sdm_handle* h, int option, int value);
 sdm_status sdm_get_option(const sdm_handle* h, int option, int* value);

@@ -32,7 +32,7 @@ RESULT_FIELDS = ("U0", "U1", "u", "BindE", "fp", "W", "dW", "s", "E_pot", "dWdla
 (R_U0, R_U1, R_U, R_BINDE, R_FP, R_W, R_DW, R_S, R_EPOT, R_DWDL, R_L1, R_L2, R_U0P, R_W0P,
  R_STATUS, R_NCL) = range(16)
 
-OPT_GRAPH, OPT_PROFILE, OPT_SPLIT, OPT_CTAS_PER_SM, OPT_VERIFY, OPT_PAIR_RESIDENT = range(6)
+OPT_GRAPH, OPT_PROFILE, OPT_SPLIT, OPT_CTAS_PER_SM, OPT_VERIFY, OPT_PAIR_RESIDENT, OPT_ZERO_COPY = range(7)
 
 EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_set_displacement", "sdm_set_params", "sdm_evaluate", "sdm_evaluate_device",
@@ -225,6 +225,12 @@ class Handle:
         f = np.zeros(3 * self.total_particles) if forces else None
         self._check(self.lib.sdm_evaluate(self.h, x.ctypes.data, res.ctypes.data, _ptr(f)))
         return res, (f.reshape(-1, 3) if forces else None)
+
+    def evaluate_host_ptrs(self, x_ptr: int, res_ptr: int, f_ptr: int = 0):
+        """sdm_evaluate on caller-owned host buffers given by address (page-locked
+        coordinates are read in place by the kernels)."""
+        self._check(self.lib.sdm_evaluate(self.h, C.c_void_p(x_ptr), C.c_void_p(res_ptr) if res_ptr else None,
+                                          C.c_void_p(f_ptr) if f_ptr else None))
 
     def evaluate_device(self, x_ptr: int, res_ptr: int, f_ptr: int = 0, stream: int = 0):
         self._check(self.lib.sdm_evaluate_device(self.h, C.c_void_p(x_ptr), C.c_void_p(res_ptr),

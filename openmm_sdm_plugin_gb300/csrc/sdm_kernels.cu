@@ -1719,6 +1719,7 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     o[SDM_R_W] = ebias;
     o[SDM_R_DW] = bfp;
     o[SDM_R_S] = bfp * fp;
+    a.s_rep[r] = bfp * fp;
     o[SDM_R_EPOT] = U0 + ebias;
     o[SDM_R_DWDLAMBDA] = dwdl;
     o[SDM_R_LAMBDA1] = l1;
@@ -1747,7 +1748,7 @@ __global__ void k_mix(SdmArgs a) {
         const SdmRep& R = a.rep[r];
         const int i = gi - R.atom_win;
         const size_t gsl = (size_t)R.slot_win + a.inv[gi];
-        const double s = a.forces ? a.results[(size_t)r * SDM_NRESULTS + SDM_R_S] : 0.0;
+        const double s = a.forces ? a.s_rep[r] : 0.0;
         const double f0[3] = {fix_to_double(a.F0x[gsl]), fix_to_double(a.F0y[gsl]), fix_to_double(a.F0z[gsl])};
         const double df[3] = {fix_to_double(a.dFx[gsl]), fix_to_double(a.dFy[gsl]), fix_to_double(a.dFz[gsl])};
         const size_t o = 3 * (size_t)(R.x_off + i);

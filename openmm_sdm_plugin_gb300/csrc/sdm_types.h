@@ -116,7 +116,8 @@ struct SdmArgs {
     const double* params; // nrep * SDM_NPARAMS
     // input / output
     const double* x;      // concatenated coordinates
-    double* results;      // nrep * SDM_NRESULTS
+    double* results;      // nrep * SDM_NRESULTS (device or mapped host memory)
+    double* s_rep;        // nrep: mixing weight s of the last finalize (device)
     double* forces;       // mixed forces (may be null)
     double* F0out;        // optional per-state forces
     double* F1out;
