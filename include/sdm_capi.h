@@ -161,8 +161,8 @@ sdm_status sdm_set_params(sdm_handle* h, int replica, const double* params);
  *   x        [sum over replicas of 3*num_particles] FP64 coordinates
  *   results  [num_replicas * SDM_NRESULTS] (may be NULL)
  *   forces   [sum over replicas of 3*num_particles] mixed force F (may be NULL)
- * Copies in, evaluates, copies out and synchronises (page-locked coordinates
- * are read in place, see SDM_OPT_ZERO_COPY).  Replaces one SDM step's
+ * Copies in, evaluates, copies out and synchronises (SDM_OPT_ZERO_COPY: read
+ * page-locked coordinates in place).  Replaces one SDM step's
  * force part: LangevinIntegratorSDM.cpp:158-176 with
  * ReferenceSDMKernels.cpp:202-318 (minus the Langevin update). */
 sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double* forces);
@@ -178,6 +178,42 @@ sdm_status sdm_evaluate_device(sdm_handle* h, const double* x, double* results, 
 /* Per-state forces of the last evaluation (device pointers or host pointers
  * selected by `on_device`): F0 and F1 = F0 + dF, [sum 3*num_particles] each. */
 sdm_status sdm_get_state_forces(sdm_handle* h, double* F0, double* F1, int on_device);
+
+/* Langevin dynamics on the SDM force (the caller side of the path).  One
+ * sdm_langevin_step step = the two-state evaluation of every replica, then the
+ * stochastic-dynamics update of platforms/reference/src/
+ * ReferenceStochasticDynamicsSDM.cpp:131-266 on the hybrid force of
+ * ReferenceSDMKernels.cpp:309-318 (+ f_extra, e.g. the group-1 bonded and
+ * restraint forces the reference adds, ReferenceSDMKernels.cpp:310-316):
+ *   v <- vscale v + fscale F/m + noise N(0,1)/sqrt(m);  x' = x + dt v;
+ *   v <- (x' - x)/dt;  x <- x'
+ * vscale = exp(-dt friction), fscale = (1 - vscale)/friction, noise =
+ * sqrt(2 kT friction) sqrt((1 - vscale^2)/(2 friction)).  Replaces
+ * IntegrateLangevinStepSDMKernel::execute (SDMKernels.h:47-113) and
+ * LangevinIntegratorSDM::step (LangevinIntegratorSDM.cpp:153-183) with one
+ * CUDA graph per step and no host synchronisation.  Constraints are not
+ * applied (the reference applies the context's constraint algorithm). */
+typedef struct {
+    double step_size;        /* ps */
+    double friction;         /* 1/ps, > 0 */
+    double temperature;      /* K, >= 0 (0: no noise) */
+    unsigned long long seed; /* counter-based generator key */
+} sdm_langevin_params;
+
+/* Sets the integrator parameters; `step` is the generator's step counter
+ * (advanced by one on the device after every step). */
+sdm_status sdm_set_langevin(sdm_handle* h, const sdm_langevin_params* params, unsigned long long step);
+
+/* nsteps steps on device buffers, asynchronous on `stream` (NULL: the
+ * handle's stream):
+ *   x        [3*total particles] FP64 positions, updated in place
+ *   v        [3*total particles] FP64 velocities (nm/ps), updated in place
+ *   inv_mass [total particles] 1/m (mol/g); 0 holds a particle fixed
+ *   f_extra  [3*total particles] forces added to the SDM force (may be NULL)
+ *   results  [num_replicas * SDM_NRESULTS] the last step's energies
+ * No counterpart in the reference's C++ API beyond the step above. */
+sdm_status sdm_langevin_step(sdm_handle* h, double* x, double* v, const double* inv_mass,
+                             const double* f_extra, double* results, int nsteps, void* stream);
 
 /* Reads and clears the device status word (SDM_DEV_* bits).  Synchronises. */
 sdm_status sdm_check_status(sdm_handle* h, int* device_status);
@@ -195,7 +231,8 @@ enum {
                                   current SDM_OPT_CTAS_PER_SM (occupancy calculator) */
     SDM_OPT_ZERO_COPY = 6     /* 1 = sdm_evaluate reads page-locked coordinates (cudaHostAlloc /
                                  cudaHostRegister) in place instead of staging them through a
-                                 device copy; results and forces are always copied out (default 1) */
+                                 device copy; results and forces are always copied out (default 0:
+                                 on GB300 the two measured on par) */
 };
 sdm_status sdm_set_option(sdm_handle* h, int option, int value);
 sdm_status sdm_get_option(const sdm_handle* h, int option, int* value);

@@ -8,6 +8,7 @@ Public surface:
 """
 from . import systems  # noqa: F401
 from .capi import Handle, SdmError, load_library  # noqa: F401
-from .force import SDMForce, force_from_system  # noqa: F401
+from .force import LangevinIntegratorSDM, SDMForce, force_from_system  # noqa: F401
 
-__all__ = ["systems", "Handle", "SdmError", "load_library", "SDMForce", "force_from_system"]
+__all__ = ["systems", "Handle", "SdmError", "load_library", "SDMForce", "LangevinIntegratorSDM",
+           "force_from_system"]

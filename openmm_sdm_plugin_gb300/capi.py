@@ -39,7 +39,7 @@ EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_get_state_forces", "sdm_check_status", "sdm_set_option", "sdm_get_option",
             "sdm_get_kernel_times", "sdm_autotune", "sdm_count_pairs", "sdm_get_grid",
             "sdm_export_lists", "sdm_evaluate_noalloc", "sdm_set_particle_params",
-            "sdm_adjoint")
+            "sdm_adjoint", "sdm_set_langevin", "sdm_langevin_step")
 
 NOALLOC_MAX_PARTICLES = 8192
 NOALLOC_SCRATCH_BYTES = 727296
@@ -103,6 +103,8 @@ def load_library(path: str = LIB_PATH):
                                            C.c_double, vp, vp, vp, vp]
         L.sdm_set_particle_params.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp]
         L.sdm_adjoint.argtypes = [vp, vp]
+        L.sdm_set_langevin.argtypes = [vp, C.POINTER(LangevinParams), C.c_ulonglong]
+        L.sdm_langevin_step.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int, vp]
         for name in EXPORTED:
             if name != "sdm_last_error":
                 getattr(L, name).restype = C.c_int
@@ -112,6 +114,12 @@ def load_library(path: str = LIB_PATH):
 
 def _ptr(a):
     return None if a is None else a.ctypes.data
+
+
+class LangevinParams(C.Structure):
+    """``sdm_langevin_params``: step size (ps), friction (1/ps), temperature (K), seed."""
+    _fields_ = [("step_size", C.c_double), ("friction", C.c_double), ("temperature", C.c_double),
+                ("seed", C.c_ulonglong)]
 
 
 class Handle:
@@ -215,6 +223,20 @@ class Handle:
         out = np.zeros(6 * int(n_displaced))
         self._check(self.lib.sdm_adjoint(self.h, out.ctypes.data))
         return out.reshape(-1, 2, 3)
+
+    def set_langevin(self, step_size: float, friction: float, temperature: float, seed: int = 0,
+                     step: int = 0):
+        p = LangevinParams(float(step_size), float(friction), float(temperature), int(seed))
+        self._check(self.lib.sdm_set_langevin(self.h, C.byref(p), int(step)))
+
+    def langevin_step(self, x_ptr: int, v_ptr: int, inv_mass_ptr: int, res_ptr: int, nsteps: int = 1,
+                      f_extra_ptr: int = 0, stream: int = 0):
+        """nsteps fused Langevin steps on device buffers (asynchronous on ``stream``)."""
+        self._check(self.lib.sdm_langevin_step(self.h, C.c_void_p(x_ptr), C.c_void_p(v_ptr),
+                                               C.c_void_p(inv_mass_ptr),
+                                               C.c_void_p(f_extra_ptr) if f_extra_ptr else None,
+                                               C.c_void_p(res_ptr), int(nsteps),
+                                               C.c_void_p(stream) if stream else None))
 
     def evaluate(self, x, forces: bool = True):
         """Host evaluation of all replicas. x: (total_particles, 3) float64."""

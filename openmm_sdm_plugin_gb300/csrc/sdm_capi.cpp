@@ -35,6 +35,7 @@ cudaError_t sdm_launch_adjoint(const SdmArgs& a, cudaStream_t st);
 namespace {
 
 const double kCoulomb = 138.935456;  // kJ nm / (mol e^2), OpenMM's ONE_4PI_EPS0
+const double kMolarGasConstant = 0.008314462618;  // kJ / (mol K), R of CODATA 2018 (k_B N_A)
 thread_local std::string g_create_error;
 
 struct SysHost {
@@ -71,10 +72,21 @@ struct GraphKey {
     const void* f;
     const void* stream;
     int split, ctas;
+    const void* v = nullptr;      // Langevin step: velocities, inverse masses, external forces
+    const void* invm = nullptr;
+    const void* fext = nullptr;
     bool operator<(const GraphKey& o) const {
-        return std::tie(x, res, f, stream, split, ctas) <
-               std::tie(o.x, o.res, o.f, o.stream, o.split, o.ctas);
+        return std::tie(x, res, f, stream, split, ctas, v, invm, fext) <
+               std::tie(o.x, o.res, o.f, o.stream, o.split, o.ctas, o.v, o.invm, o.fext);
     }
+};
+
+// device buffers of a Langevin step (positions double as the evaluation's x)
+struct LvBind {
+    double* x;
+    double* v;
+    const double* invm;
+    const double* fext;
 };
 
 }  // namespace
@@ -103,12 +115,15 @@ struct sdm_handle {
     double* res_in = nullptr;
     double* f_in = nullptr;
     double* params_dev = nullptr;
+    double* lv_dev = nullptr;     // SDM_LV_COUNT doubles
     // host
-    double* params_pinned = nullptr;
+    double* params_pinned = nullptr;  // params, then SDM_LV_COUNT Langevin doubles
     std::vector<double> params;
     bool params_dirty = true;
+    double lv_host[SDM_LV_COUNT] = {};
+    bool lv_set = false, lv_dirty = false;
     // options
-    int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 4, opt_verify = 1, opt_zero_copy = 1;
+    int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 4, opt_verify = 1, opt_zero_copy = 0;
     int pair_res[SDM_MAX_CTAS + 1] = {};  // resident pair-kernel CTAs per SM by request
     // graphs
     std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -461,13 +476,32 @@ sdm_status flush_params(sdm_handle* h, cudaStream_t st) {
     return SDM_OK;
 }
 
+sdm_status flush_langevin(sdm_handle* h, cudaStream_t st) {
+    if (!h->lv_dirty) return SDM_OK;
+    double* stage = h->params_pinned + h->params.size();
+    std::memcpy(stage, h->lv_host, sizeof h->lv_host);
+    SDM_CUDA(h, cudaMemcpyAsync(h->lv_dev, stage, sizeof h->lv_host, cudaMemcpyHostToDevice, st));
+    SDM_CUDA(h, cudaStreamSynchronize(st));
+    h->lv_dirty = false;
+    return SDM_OK;
+}
+
 sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStream_t st, int mode,
-               bool allow_graph) {
+               bool allow_graph, const LvBind* lv = nullptr) {
     SdmArgs a = h->args;
     a.x = x;
     a.results = res;
     a.forces = f;
     a.F0out = nullptr;
+    a.lv_x = lv ? lv->x : nullptr;
+    a.lv_v = lv ? lv->v : nullptr;
+    a.lv_invm = lv ? lv->invm : nullptr;
+    a.lv_fext = lv ? lv->fext : nullptr;
+    a.lv_prm = lv ? h->lv_dev : nullptr;
+    if (lv) {
+        sdm_status s0 = flush_langevin(h, st);
+        if (s0) return s0;
+    }
     a.F1out = nullptr;
     a.split = mode == 2 ? 1 : h->opt_split;
     sdm_status s = flush_params(h, st);
@@ -489,6 +523,7 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
     }
     const bool gprof = h->opt_profile == 2;
     GraphKey key{x, res, f, st, a.split, h->opt_ctas + (gprof ? 100 : 0)};
+    if (lv) { key.v = lv->v; key.invm = lv->invm; key.fext = lv->fext; }
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
         cudaGraph_t g = nullptr;
@@ -669,6 +704,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_ppos = ar.take<SdmPertPos>(std::max(Pp, 1LL));
     const size_t o_adj = ar.take<double>(3 * std::max(Pp, 1LL));
     const size_t o_ncl = ar.take<int>(nrep), o_st = ar.take<int>(4), o_srep = ar.take<double>(nrep);
+    const size_t o_lv = ar.take<double>(SDM_LV_COUNT);
     const size_t o_counts = ar.take<long long>(2 * nrep), o_ip = ar.take<int>(nrep + 1);
     const size_t o_cp = ar.take<int>(nrep + 1), o_jc = ar.take<int>(Cl);
     const size_t o_done = ar.take<int>(4);
@@ -701,6 +737,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.shift_tab = at<float>(B, o_tab);
     a.params = at<double>(B, o_par);
     h->params_dev = at<double>(B, o_par);
+    h->lv_dev = at<double>(B, o_lv);
     h->x_in = at<double>(B, o_x);
     h->res_in = at<double>(B, o_res);
     h->f_in = at<double>(B, o_f);
@@ -755,7 +792,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     // parameters
     h->params.resize((size_t)nrep * SDM_NPARAMS);
     for (int r = 0; r < nrep; ++r) default_params(&h->params[(size_t)r * SDM_NPARAMS]);
-    ce = cudaMallocHost(&h->params_pinned, h->params.size() * sizeof(double));
+    ce = cudaMallocHost(&h->params_pinned, (h->params.size() + SDM_LV_COUNT) * sizeof(double));
     if (ce != cudaSuccess) { h->params_pinned = nullptr; cuda_fail(h, ce, "cudaMallocHost"); return bail(SDM_ERR_CUDA); }
     // cluster-pair list capacity: twice the expected count of clusters within
     // rc + 1.5 cluster edges over a half shell, at the densest system
@@ -838,9 +875,10 @@ sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double*
     if (!h || !x) return SDM_ERR_INVALID_ARGUMENT;
     cudaSetDevice(h->device);
     const size_t nx = 3 * (size_t)h->total_particles;
-    // page-locked coordinates are read in place by k_cells (no staging copy);
-    // results and forces always return through copy-engine transfers, which
-    // beat kernel stores into host memory (0.98 vs 1.11 ms per 22-replica call)
+    // optionally page-locked coordinates are read in place by k_cells (no
+    // staging copy; measured on par with the copy); results and forces always
+    // return through copy-engine transfers, which beat kernel stores into host
+    // memory (0.98 vs 1.11 ms per 22-replica call)
     const double* xd = h->opt_zero_copy ? static_cast<const double*>(mapped_host(x)) : nullptr;
     if (!xd) {
         SDM_CUDA(h, cudaMemcpyAsync(h->x_in, x, nx * sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -880,6 +918,49 @@ sdm_status sdm_evaluate_device(sdm_handle* h, const double* x, double* results, 
     cudaSetDevice(h->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
     return run(h, x, results, forces, st, 0, true);
+}
+
+sdm_status sdm_set_langevin(sdm_handle* h, const sdm_langevin_params* p, unsigned long long step) {
+    if (!h || !p) return SDM_ERR_INVALID_ARGUMENT;
+    if (!(p->step_size > 0.0) || !std::isfinite(p->step_size))
+        return fail(h, SDM_ERR_INVALID_ARGUMENT, "step size must be positive");
+    // the reference sets tau = 1/friction and 0 for zero friction, which makes
+    // its noise scale sqrt(2kT/0) undefined (ReferenceSDMKernels.cpp:327)
+    if (!(p->friction > 0.0) || !std::isfinite(p->friction))
+        return fail(h, SDM_ERR_INVALID_ARGUMENT, "friction must be positive");
+    if (!(p->temperature >= 0.0) || !std::isfinite(p->temperature))
+        return fail(h, SDM_ERR_INVALID_ARGUMENT, "temperature must be non-negative");
+    // ReferenceStochasticDynamicsSDM.cpp:145-148
+    const double tau = 1.0 / p->friction, dt = p->step_size;
+    const double vscale = std::exp(-dt / tau);
+    const double fscale = (1.0 - vscale) * tau;
+    const double kT = kMolarGasConstant * p->temperature;
+    const double noise = std::sqrt(2.0 * kT / tau) * std::sqrt(0.5 * (1.0 - vscale * vscale) * tau);
+    double* q = h->lv_host;
+    q[SDM_LV_DT] = dt;
+    q[SDM_LV_VSCALE] = vscale;
+    q[SDM_LV_FSCALE] = fscale;
+    q[SDM_LV_NOISE] = noise;
+    q[SDM_LV_INVDT] = 1.0 / dt;
+    std::memcpy(&q[SDM_LV_SEED], &p->seed, 8);
+    std::memcpy(&q[SDM_LV_STEP], &step, 8);
+    h->lv_set = true;
+    h->lv_dirty = true;
+    return SDM_OK;
+}
+
+sdm_status sdm_langevin_step(sdm_handle* h, double* x, double* v, const double* inv_mass, const double* f_extra,
+                             double* results, int nsteps, void* stream) {
+    if (!h || !x || !v || !inv_mass || !results || nsteps < 0) return SDM_ERR_INVALID_ARGUMENT;
+    if (!h->lv_set) return fail(h, SDM_ERR_INVALID_ARGUMENT, "sdm_set_langevin was not called");
+    cudaSetDevice(h->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+    const LvBind lv{x, v, inv_mass, f_extra};
+    for (int k = 0; k < nsteps; ++k) {
+        sdm_status s = run(h, x, results, nullptr, st, 0, true, &lv);
+        if (s) return s;
+    }
+    return SDM_OK;
 }
 
 sdm_status sdm_get_state_forces(sdm_handle* h, double* F0, double* F1, int on_device) {

@@ -1761,6 +1761,80 @@ __global__ void k_mix(SdmArgs a) {
     }
 }
 
+// ------------------------------------------------------------------------- //
+// K10: Langevin update with the mixed force                                  //
+// ------------------------------------------------------------------------- //
+// The stochastic-dynamics step of
+// platforms/reference/src/ReferenceStochasticDynamicsSDM.cpp:131-266 (the SD
+// leap-frog of GROMACS 3.1.4 do_update_sd) on the hybrid force of
+// platforms/reference/src/ReferenceSDMKernels.cpp:309-318, per particle:
+//   v  <- vscale v + fscale m^-1 F + noise m^-1/2 N(0,1)
+//   x' =  x + dt v,   v <- (x' - x) / dt,   x <- x'
+// with F = F0 + s dF (+ external forces).  Same operation order as the
+// reference, no contraction, FP64.  Particles with m^-1 = 0 do not move.
+// The normal deviates come from a counter-based generator: SplitMix64's
+// output mixing (Steele, Lea and Flood, OOPSLA 2014) of (seed, step, particle
+// component pair) gives two 32-bit uniforms per hash, Box-Muller turns them
+// into two normals (FP32).
+__device__ __forceinline__ unsigned long long sm64_mix(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ float2 lv_normals(unsigned long long seed, unsigned long long step,
+                                             unsigned long long counter) {
+    const unsigned long long h =
+        sm64_mix(seed ^ sm64_mix(step * 0x9E3779B97F4A7C15ull ^ counter * 0xD1B54A32D192ED03ull));
+    const float u1 = (float)((unsigned)(h >> 40) + 1u) * 5.9604644775390625e-08f;   // (0, 1]
+    const float u2 = (float)((unsigned)(h >> 8) & 0xffffffu) * 5.9604644775390625e-08f;
+    const float r = sqrtf(-2.0f * logf(u1));
+    float sn, cs;
+    sincospif(2.0f * u2, &sn, &cs);
+    return make_float2(r * cs, r * sn);
+}
+
+__global__ void k_langevin(SdmArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    const double* prm = a.lv_prm;
+    const double dt = prm[SDM_LV_DT], vscale = prm[SDM_LV_VSCALE], fscale = prm[SDM_LV_FSCALE];
+    const double noise = prm[SDM_LV_NOISE], invdt = prm[SDM_LV_INVDT];
+    const unsigned long long seed = (unsigned long long)__double_as_longlong(prm[SDM_LV_SEED]);
+    const unsigned long long step = (unsigned long long)__double_as_longlong(prm[SDM_LV_STEP]);
+    for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < a.total_atoms; gi += stride) {
+        const int r = rep_by_atom(a.rep, a.nrep, gi);
+        const SdmRep& R = a.rep[r];
+        const size_t pi = (size_t)R.x_off + (gi - R.atom_win);   // particle in the concatenated order
+        const double im = a.lv_invm[pi];
+        if (im == 0.0) continue;
+        const size_t gsl = (size_t)R.slot_win + a.inv[gi];
+        const double s = a.s_rep[r];
+        const double f0[3] = {fix_to_double(a.F0x[gsl]), fix_to_double(a.F0y[gsl]), fix_to_double(a.F0z[gsl])};
+        const double df[3] = {fix_to_double(a.dFx[gsl]), fix_to_double(a.dFy[gsl]), fix_to_double(a.dFz[gsl])};
+        const float2 n01 = lv_normals(seed, step, 2 * pi), n2x = lv_normals(seed, step, 2 * pi + 1);
+        const double nrm[3] = {(double)n01.x, (double)n01.y, (double)n2x.x};
+        const double sq = sqrt(im);
+        const double fsi = __dmul_rn(fscale, im), nsq = __dmul_rn(noise, sq);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double f = __fma_rn(s, df[k], f0[k]);
+            if (a.lv_fext) f = __dadd_rn(f, a.lv_fext[3 * pi + k]);
+            const double x = a.lv_x[3 * pi + k];
+            const double v = __dadd_rn(__dadd_rn(__dmul_rn(vscale, a.lv_v[3 * pi + k]), __dmul_rn(fsi, f)),
+                                       __dmul_rn(nsq, nrm[k]));
+            const double xp = __dadd_rn(x, __dmul_rn(dt, v));
+            a.lv_v[3 * pi + k] = __dmul_rn(invdt, __dsub_rn(xp, x));
+            a.lv_x[3 * pi + k] = xp;
+        }
+    }
+}
+
+// advances the step counter of the Langevin parameter block (last node of a step)
+__global__ void k_lv_tick(double* prm) {
+    const unsigned long long st = (unsigned long long)__double_as_longlong(prm[SDM_LV_STEP]);
+    prm[SDM_LV_STEP] = __longlong_as_double((long long)(st + 1));
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------------- //
@@ -1919,7 +1993,12 @@ cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st) {
 
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st) {
     k_finalize<<<a.nrep, 256, 0, st>>>(a);
-    k_mix<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
+    if (a.lv_x) {   // Langevin step: the mixed force feeds the update directly
+        k_langevin<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
+        k_lv_tick<<<1, 1, 0, st>>>(a.lv_prm);
+    } else {
+        k_mix<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
+    }
     return cudaGetLastError();
 }
 

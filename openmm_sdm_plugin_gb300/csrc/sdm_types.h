@@ -43,6 +43,16 @@
 #define SDM_LIST_MARGIN 1.0e-4   // nm added to the cutoff in the list filter
 #define SDM_MAX_SPLIT 4
 
+// Langevin parameter block (doubles; seed and step are stored as integer bits)
+#define SDM_LV_DT 0
+#define SDM_LV_VSCALE 1
+#define SDM_LV_FSCALE 2
+#define SDM_LV_NOISE 3
+#define SDM_LV_INVDT 4
+#define SDM_LV_SEED 5
+#define SDM_LV_STEP 6
+#define SDM_LV_COUNT 8
+
 struct SdmSys {
     int n;            // particles
     int atom_base;    // offset into the topology arrays
@@ -118,6 +128,12 @@ struct SdmArgs {
     const double* x;      // concatenated coordinates
     double* results;      // nrep * SDM_NRESULTS (device or mapped host memory)
     double* s_rep;        // nrep: mixing weight s of the last finalize (device)
+    // Langevin step (sdm_langevin_step): positions lv_x are also the evaluation's x
+    double* lv_x;         // [3 * total particles] updated in place
+    double* lv_v;         // [3 * total particles] updated in place
+    const double* lv_invm;  // [total particles] inverse masses (0: particle held fixed)
+    const double* lv_fext;  // [3 * total particles] forces added to the SDM force (may be null)
+    double* lv_prm;       // SDM_LV_* (device): dt, vscale, fscale, noise scale, 1/dt, seed, step
     double* forces;       // mixed forces (may be null)
     double* F0out;        // optional per-state forces
     double* F1out;

@@ -234,6 +234,88 @@ class SDMForce:
             self._handle = None
 
 
+class LangevinIntegratorSDM(SDMForce):
+    """Host mirror of the reference integrator (``LangevinIntegratorSDM.h``,
+    ``openmmapi/src/LangevinIntegratorSDM.cpp``): the SDM parameters of
+    :class:`SDMForce` plus temperature (K), friction (1/ps), step size (ps) and
+    random seed.  ``step(n)`` advances positions and velocities on the GPU:
+    per step the two-state evaluation and the stochastic-dynamics update
+    (``sdm_langevin_step``, one CUDA graph per step, no host synchronisation).
+    Masses come from ``setParticleMass`` (0 holds a particle fixed, as a zero
+    mass does in the reference); constraints are not applied."""
+
+    def __init__(self, temperature: float, frictionCoeff: float, stepSize: float, nParticles: int = 0):
+        self._mass = []
+        super().__init__(nParticles)
+        self._temperature = float(temperature)
+        self._friction = float(frictionCoeff)
+        self._step_size = float(stepSize)
+        self._seed = 0
+        self._lv_dirty = True
+        self._step_count = 0
+        self._x = self._v = self._im = self._res = None
+
+    def addParticle(self, charge: float, sigma: float, epsilon: float, mass: float = 1.0) -> int:
+        k = super().addParticle(charge, sigma, epsilon)
+        self._mass.append(float(mass))
+        return k
+
+    def setParticleMass(self, index: int, mass: float):
+        self._mass[index] = float(mass)
+        self._im = None
+
+    def getParticleMass(self, index: int) -> float:
+        return self._mass[index]
+
+    def setTemperature(self, t): self._temperature = float(t); self._lv_dirty = True
+    def getTemperature(self): return self._temperature
+    def setFriction(self, f): self._friction = float(f); self._lv_dirty = True
+    def getFriction(self): return self._friction
+    def setStepSize(self, dt): self._step_size = float(dt); self._lv_dirty = True
+    def getStepSize(self): return self._step_size
+    def setRandomNumberSeed(self, seed): self._seed = int(seed); self._lv_dirty = True
+    def getRandomNumberSeed(self): return self._seed
+
+    def setState(self, positions, velocities=None, device: int = 0):
+        """Uploads positions (and velocities, default zero), FP64 (N, 3)."""
+        import torch
+        x = np.ascontiguousarray(np.asarray(positions, np.float64).reshape(-1, 3))
+        v = np.zeros_like(x) if velocities is None else np.asarray(velocities, np.float64).reshape(-1, 3)
+        dev = torch.device("cuda", device)
+        self._x = torch.from_numpy(x.copy()).to(dev)
+        self._v = torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+        self._res = torch.zeros((1, capi.NRESULTS), dtype=torch.float64, device=dev)
+        self._im = None
+
+    def getState(self):
+        """(positions, velocities) as host FP64 arrays."""
+        import torch
+        torch.cuda.synchronize(self._x.device)
+        return self._x.cpu().numpy(), self._v.cpu().numpy()
+
+    def step(self, steps: int = 1):
+        import torch
+        if self._x is None:
+            raise RuntimeError("setState first")
+        self._sync(self._x.device.index or 0)
+        if self._im is None:
+            m = np.asarray(self._mass[:len(self._q)], np.float64)
+            im = np.where(m > 0, 1.0 / np.where(m > 0, m, 1.0), 0.0)
+            self._im = torch.from_numpy(im).to(self._x.device)
+        if self._lv_dirty:
+            self._handle.set_langevin(self._step_size, self._friction, self._temperature, self._seed,
+                                      self._step_count)
+            self._lv_dirty = False
+        self._handle.langevin_step(self._x.data_ptr(), self._v.data_ptr(), self._im.data_ptr(),
+                                   self._res.data_ptr(), int(steps),
+                                   stream=torch.cuda.current_stream(self._x.device).cuda_stream)
+        self._step_count += int(steps)
+        r = self._res[0].cpu().numpy()
+        self._last = r
+        self._bind_e = float(r[capi.R_BINDE])
+        self._pot_e = float(r[capi.R_EPOT])
+
+
 def force_from_system(s: SDMSystem, replica: int = 0) -> SDMForce:
     """Builds an SDMForce from a synthetic system (parameters of `replica`)."""
     f = SDMForce()

@@ -203,3 +203,40 @@ def eval_state(osys: OracleSystem, x, params, nthreads=1, forces=True):
     lib().orc_eval_state(*osys._args(), x, osys.d, np.ascontiguousarray(params, np.float64), res,
                          F.ctypes.data if forces else None, nthreads)
     return res, (F.reshape(-1, 3) if forces else None)
+
+
+# --------------------------------------------------------------------------- #
+# Langevin update (platforms/reference/src/ReferenceStochasticDynamicsSDM.cpp)
+# --------------------------------------------------------------------------- #
+MOLAR_GAS_CONSTANT = 0.008314462618   # kJ/(mol K), k_B N_A (CODATA 2018)
+
+
+def langevin_coefficients(step_size, friction, temperature):
+    """(vscale, fscale, noise scale) of ReferenceStochasticDynamicsSDM.cpp:145-148
+    with tau = 1/friction (ReferenceSDMKernels.cpp:327)."""
+    tau = 1.0 / friction
+    vscale = np.exp(-step_size / tau)
+    fscale = (1.0 - vscale) * tau
+    kT = MOLAR_GAS_CONSTANT * temperature
+    noise = np.sqrt(2.0 * kT / tau) * np.sqrt(0.5 * (1.0 - vscale * vscale) * tau)
+    return vscale, fscale, noise
+
+
+def langevin_update(x, v, inv_mass, F, step_size, friction, temperature, normals=None):
+    """One stochastic-dynamics step (updatePart1, updatePart2 and the velocity
+    recomputation of ReferenceStochasticDynamicsSDM.cpp:131-266, no
+    constraints), FP64 in the reference's operation order.  x, v, F: (N, 3);
+    inv_mass: (N,); normals: (N, 3) standard normal deviates (None: zeros)."""
+    vscale, fscale, noise = langevin_coefficients(step_size, friction, temperature)
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    v = np.asarray(v, np.float64).reshape(-1, 3)
+    F = np.asarray(F, np.float64).reshape(-1, 3)
+    im = np.asarray(inv_mass, np.float64).reshape(-1, 1)
+    n = np.zeros_like(x) if normals is None else np.asarray(normals, np.float64).reshape(-1, 3)
+    move = (im[:, 0] != 0.0)
+    v1 = vscale * v + (fscale * im) * F + (noise * np.sqrt(im)) * n
+    xp = x + step_size * v1
+    v2 = (1.0 / step_size) * (xp - x)
+    xo = np.where(move[:, None], xp, x)
+    vo = np.where(move[:, None], v2, v)
+    return xo, vo

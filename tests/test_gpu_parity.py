@@ -242,7 +242,7 @@ def test_page_locked_host_buffers_in_place():
     s = S.config2(nrep=2)
     h = _handle([s])
     x = np.ascontiguousarray(s.positions.reshape(-1, 3))
-    h.set_option(capi.OPT_ZERO_COPY, 0)
+    assert h.get_option(capi.OPT_ZERO_COPY) == 0   # default: staged copies
     r_st, F_st = h.evaluate(x)
     h.set_option(capi.OPT_ZERO_COPY, 1)
     xp = torch.from_numpy(x.copy()).pin_memory()

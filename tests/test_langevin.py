@@ -1,0 +1,145 @@
+"""GPU tests of the fused Langevin step (sdm_langevin_step) against the
+restated stochastic-dynamics update of the oracle
+(ReferenceStochasticDynamicsSDM.cpp:131-266 on the hybrid force of
+ReferenceSDMKernels.cpp:309-318)."""
+import numpy as np
+import pytest
+
+import oracle
+from openmm_sdm_plugin_gb300 import capi, systems as S
+
+pytestmark = pytest.mark.gpu
+
+DT, FRICTION = 0.002, 5.0
+
+
+def _setup(nrep=2, seed=11):
+    import torch
+    s = S.config2(nrep=nrep)
+    h = capi.Handle([s])
+    for r, p in enumerate(s.params):
+        h.set_params(r, p.as_array())
+    rng = np.random.default_rng(seed)
+    x = np.ascontiguousarray(s.positions.reshape(-1, 3))
+    n = x.shape[0]
+    v = rng.normal(scale=0.5, size=(n, 3))
+    im = 1.0 / rng.uniform(1.0, 16.0, n)
+    im[rng.choice(n, 50, replace=False)] = 0.0    # fixed particles
+    fext = rng.normal(scale=10.0, size=(n, 3))
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    return s, h, x, v, im, fext, dev
+
+
+def test_langevin_step_matches_restated_update_at_zero_temperature():
+    import torch
+    s, h, x, v, im, fext, dev = _setup()
+    res_h, F = h.evaluate(x)                      # the SDM force at x
+    h.set_langevin(DT, FRICTION, 0.0, seed=5)
+    xd, vd, imd, fd = dev(x), dev(v), dev(im), dev(fext)
+    rd = torch.zeros((h.nrep, capi.NRESULTS), dtype=torch.float64, device="cuda")
+    h.langevin_step(xd.data_ptr(), vd.data_ptr(), imd.data_ptr(), rd.data_ptr(), 1, fd.data_ptr())
+    torch.cuda.synchronize()
+    xo, vo = oracle.langevin_update(x, v, im, F + fext, DT, FRICTION, 0.0)
+    assert np.array_equal(xd.cpu().numpy(), xo)
+    assert np.array_equal(vd.cpu().numpy(), vo)
+    assert np.array_equal(rd.cpu().numpy()[:, :14], res_h[:, :14])   # energies at the start point
+    assert h.check_status() == 0
+
+
+def test_langevin_noise_is_standard_normal_and_fresh_each_step():
+    import torch
+    s, h, x, v, im, fext, dev = _setup(nrep=1)
+    rd = torch.zeros((h.nrep, capi.NRESULTS), dtype=torch.float64, device="cuda")
+    imd = dev(im)
+
+    def one(T, step):
+        h.set_langevin(DT, FRICTION, T, seed=123, step=step)
+        xd, vd = dev(x), dev(v)
+        h.langevin_step(xd.data_ptr(), vd.data_ptr(), imd.data_ptr(), rd.data_ptr(), 1)
+        torch.cuda.synchronize()
+        return vd.cpu().numpy()
+
+    v0 = one(0.0, 0)
+    _, _, ns = oracle.langevin_coefficients(DT, FRICTION, 300.0)
+    mv = im != 0
+    scale = ns * np.sqrt(im[mv])[:, None]
+    n_a = ((one(300.0, 0) - v0)[mv] / scale).reshape(-1)
+    n_b = ((one(300.0, 1) - v0)[mv] / scale).reshape(-1)
+    n_a2 = ((one(300.0, 0) - v0)[mv] / scale).reshape(-1)
+    m = n_a.size
+    assert abs(n_a.mean()) < 5.0 / np.sqrt(m)
+    assert abs(n_a.var() - 1.0) < 6.0 * np.sqrt(2.0 / m)
+    assert abs(np.mean(n_a ** 3)) < 6.0 * np.sqrt(15.0 / m)           # symmetric
+    assert abs(np.mean(n_a ** 4) - 3.0) < 6.0 * np.sqrt(96.0 / m)      # Gaussian tails
+    assert abs(np.corrcoef(n_a, n_b)[0, 1]) < 5.0 / np.sqrt(m)         # other step: fresh deviates
+    assert np.allclose(n_a, n_a2, atol=1e-6)                           # same (seed, step): same deviates
+
+
+def test_langevin_steps_chain_and_fixed_particles():
+    import torch
+    s, h, x, v, im, fext, dev = _setup()
+    rd = torch.zeros((h.nrep, capi.NRESULTS), dtype=torch.float64, device="cuda")
+    imd, fd = dev(im), dev(fext)
+    h.set_langevin(DT, FRICTION, 300.0, seed=9, step=40)
+    xa, va = dev(x), dev(v)
+    h.langevin_step(xa.data_ptr(), va.data_ptr(), imd.data_ptr(), rd.data_ptr(), 3, fd.data_ptr())
+    h.set_langevin(DT, FRICTION, 300.0, seed=9, step=40)
+    xb, vb = dev(x), dev(v)
+    for _ in range(3):   # graph replays, the device step counter advances
+        h.langevin_step(xb.data_ptr(), vb.data_ptr(), imd.data_ptr(), rd.data_ptr(), 1, fd.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(xa.cpu().numpy(), xb.cpu().numpy())
+    assert np.array_equal(va.cpu().numpy(), vb.cpu().numpy())
+    fixed = im == 0
+    assert np.array_equal(xa.cpu().numpy()[fixed], x[fixed])
+    assert np.array_equal(va.cpu().numpy()[fixed], v[fixed])
+    moved = np.abs(xa.cpu().numpy() - x).max(axis=1)
+    assert (moved[~fixed] > 0).all() and np.isfinite(moved).all()
+    # the energies are those of the last step's start point
+    assert np.isfinite(rd.cpu().numpy()[:, :14]).all()
+    assert h.check_status() == 0
+
+
+def test_langevin_parameter_checks():
+    s, h, *_ = _setup(nrep=1)
+    for bad in ((0.0, 1.0, 300.0), (0.002, 0.0, 300.0), (0.002, 1.0, -1.0)):
+        with pytest.raises(capi.SdmError):
+            h.set_langevin(*bad)
+
+
+def test_integrator_mirror_chains_steps_like_the_restated_update():
+    """LangevinIntegratorSDM (host mirror of the reference integrator): three
+    T = 0 steps equal three restated updates, each on the force the library
+    evaluates at the current positions."""
+    from openmm_sdm_plugin_gb300.force import LangevinIntegratorSDM, force_from_system
+    s = S.config0(variant="b")
+    ref = force_from_system(s)
+    integ = LangevinIntegratorSDM(0.0, 2.0, 0.001)
+    for q, sg, ep in zip(s.charge, s.sigma, s.epsilon):
+        integ.addParticle(q, sg, ep, mass=14.0)
+    for i, j in s.exclusions:
+        integ.addExclusion(int(i), int(j))
+    integ.setCutoffDistance(s.cutoff)
+    integ.setReactionFieldDielectric(s.eps_rf)
+    integ.setPeriodicBoxVectors((s.box[0], 0, 0), (0, s.box[1], 0), (0, 0, s.box[2]))
+    for i in np.nonzero(np.any(s.displacement != 0, axis=1))[0]:
+        integ.setDisplacement(int(i), *s.displacement[i])
+    integ._p = ref._p
+    integ.setParticleMass(0, 0.0)     # held fixed
+    rng = np.random.default_rng(3)
+    x = s.positions[0].copy()
+    v = rng.normal(scale=0.2, size=x.shape)
+    integ.setState(x, v)
+    integ.step(3)
+    xg, vg = integ.getState()
+    im = np.full(s.n, 1.0 / 14.0)
+    im[0] = 0.0
+    for _ in range(3):
+        _, F = ref.evaluate(x)
+        x, v = oracle.langevin_update(x, v, im, F, 0.001, 2.0, 0.0)
+    assert np.array_equal(xg, x)
+    assert np.array_equal(vg, v)
+    assert np.isfinite(integ.getPerturbationEnergy()).all()
+    assert np.isfinite(integ.getBindE()) and np.isfinite(integ.getPotEnergy())
+    integ.close()
+    ref.close()

@@ -265,3 +265,23 @@ def test_cluster_build_properties():
     for row in p8:
         v = row >= 0
         assert not (np.diff(v.astype(int)) > 0).any()
+
+
+def test_langevin_coefficients_and_update():
+    """Restated stochastic-dynamics step: closed forms at T = 0 and its limits."""
+    dt, fr = 0.004, 1.0
+    vs, fs, ns = oracle.langevin_coefficients(dt, fr, 0.0)
+    assert vs == pytest.approx(np.exp(-dt * fr), rel=1e-15)
+    assert fs == pytest.approx((1 - np.exp(-dt * fr)) / fr, rel=1e-15)
+    assert ns == 0.0
+    # noise^2 = kT (1 - vscale^2): the velocity variance of one step from rest
+    _, _, n300 = oracle.langevin_coefficients(dt, fr, 300.0)
+    assert n300 ** 2 == pytest.approx(oracle.MOLAR_GAS_CONSTANT * 300.0 * (1 - np.exp(-2 * dt * fr)), rel=1e-12)
+    rng = np.random.default_rng(7)
+    x = rng.uniform(0, 3, (5, 3)); v = rng.normal(size=(5, 3)); F = rng.normal(size=(5, 3))
+    im = np.array([1 / 12.0, 1 / 16.0, 0.0, 1.0, 0.5])
+    xo, vo = oracle.langevin_update(x, v, im, F, dt, fr, 0.0)
+    v1 = vs * v + fs * im[:, None] * F
+    assert np.allclose(vo[im != 0], v1[im != 0], rtol=1e-12)
+    assert np.allclose(xo[im != 0], (x + dt * v1)[im != 0], rtol=1e-15)
+    assert np.array_equal(xo[2], x[2]) and np.array_equal(vo[2], v[2])   # m^-1 = 0: fixed
