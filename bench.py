@@ -351,6 +351,29 @@ def main():
                             "stochastic-dynamics update in one CUDA graph per step (dt 2 fs, 1/ps, 300 K), "
                             "every step from the benchmark configuration"}
 
+    # ---- a real system: the TEMOA DMS fixture (20,446 particles, 606 1-4
+    # exceptions), the same 22-state schedule, one batched call per step ----
+    temoa = None
+    tpath = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "temoa_g1_g4.npz")
+    if os.path.exists(tpath):
+        from openmm_sdm_plugin_gb300 import dms
+        st_t = dms.load_compact(tpath, displacement={2: (2.2, 2.2, 2.2), 3: (-2.2, -2.2, -2.2)},
+                                params=sysm.params)
+        ht = capi.Handle([st_t], device=local)
+        for r in range(NREP):
+            ht.set_params(r, st_t.params[r].as_array())
+        xt = torch.from_numpy(np.ascontiguousarray(st_t.positions.reshape(-1, 3))).to(dev)
+        rt = torch.zeros((NREP, capi.NRESULTS), dtype=torch.float64, device=dev)
+        ft = torch.zeros_like(xt)
+        nt = min(args.steps, 100)
+        ms_t, _ = timed(lambda: ht.evaluate_device(xt.data_ptr(), rt.data_ptr(), ft.data_ptr(), sptr), nt, warm)
+        tot_t = max_over_ranks(sum(ms_t) / 1e3, dist, dev)
+        temoa = {"value": whole_job_rate(NREP * nt, world, tot_t), "unit": UNIT, "ms_per_call": sum(ms_t) / nt,
+                 "steps": nt, "device_status": ht.check_status(),
+                 "workload": "temoa-g1-g4 (tests/golden fixture of the reference's example DMS): 22 lambda "
+                             "states x 20,446 particles, the stored coordinates, guests displaced +-2.2 nm/axis"}
+        ht.close()
+
     # ---- e2e through the host C ABI: pinned host inputs/outputs ----
     h.set_option(capi.OPT_PROFILE, 0)
     xpin = torch.from_numpy(xh.copy()).pin_memory()
@@ -443,6 +466,7 @@ def main():
                 "coords_in_place": {"value": e2e_zc, "ms_per_step": sum(e2e_ms_zc) / len(e2e_ms_zc),
                                     "path": "same call, SDM_OPT_ZERO_COPY=1: k_cells reads the host coordinates"}},
         "langevin": langevin,
+        "dms_temoa": temoa,
         "roofline": roof,
         "kernel_ms": breakdown,
         "cpu_baseline": cpu,

@@ -126,6 +126,15 @@ typedef struct {
     double cutoff;               /* nm; must satisfy cutoff < box/2 in every axis */
     double reaction_field_dielectric;
     int num_replicas;            /* coordinate sets (lambda states) per call, >= 1 */
+    /* Exceptions: pairs with their own parameters (OpenMM NonbondedForce
+     * exceptions, e.g. the 1-4 pairs the reference's DMS reader adds from
+     * pair_12_6_es_term, example/desmonddmsfile75.py:813-848).  Each pair must
+     * also be in the exclusion list.  E = K qq/r + 4 eps ((sigma/r)^12 -
+     * (sigma/r)^6) on the caller's coordinates: no cutoff, no reaction field,
+     * no periodic image.  Zero-initialised fields: no exceptions. */
+    int num_exceptions;
+    const int* exception_pairs;     /* [2*num_exceptions] particle indices */
+    const double* exception_params; /* [3*num_exceptions] charge product (e^2), sigma (nm), epsilon (kJ/mol) */
 } sdm_system_desc;
 
 /* Creates a handle for num_systems systems on CUDA device `device`, owning all

@@ -64,6 +64,9 @@ class SystemDesc(C.Structure):
         ("cutoff", C.c_double),
         ("reaction_field_dielectric", C.c_double),
         ("num_replicas", C.c_int),
+        ("num_exceptions", C.c_int),
+        ("exception_pairs", C.POINTER(C.c_int)),
+        ("exception_params", C.POINTER(C.c_double)),
     ]
 
 
@@ -153,6 +156,16 @@ class Handle:
             d.cutoff = float(s.cutoff)
             d.reaction_field_dielectric = float(s.eps_rf)
             d.num_replicas = int(s.positions.shape[0]) if getattr(s, "positions", None) is not None else 1
+            xp = getattr(s, "exceptions", None)
+            if xp is not None and len(xp):
+                xpi = np.ascontiguousarray(np.asarray(xp, np.int32).reshape(-1))
+                xpp = np.ascontiguousarray(np.asarray(s.exception_params, np.float64).reshape(-1))
+                if xpp.size != 3 * (xpi.size // 2):
+                    raise ValueError("exception_params needs (charge product, sigma, epsilon) per pair")
+                self._keep += [xpi, xpp]
+                d.num_exceptions = int(xpi.size // 2)
+                d.exception_pairs = xpi.ctypes.data_as(C.POINTER(C.c_int))
+                d.exception_params = xpp.ctypes.data_as(C.POINTER(C.c_double))
         h = C.c_void_p()
         st = self.lib.sdm_create(descs, len(self.systems), int(device), C.byref(h))
         if st != SDM_OK:

@@ -28,6 +28,7 @@ int sdm_pair_resident(int ctas_per_sm);
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
                             int resident, cudaStream_t st);
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
+cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_adjoint(const SdmArgs& a, cudaStream_t st);
@@ -50,6 +51,8 @@ struct SysHost {
     std::vector<int> cx_off;    // nD+1 (local)
     std::vector<int> cx_idx;
     std::vector<int2> hst, fst;  // owner / full column stencils
+    std::vector<int2> ex_pair;   // exceptions (local indices)
+    std::vector<double4> ex_prm; // (K qq, sigma, 4 eps, 0)
     bool clique = false;
     SdmSys dev;
     int replicas;
@@ -245,6 +248,23 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
             if (size[i] > 0 && edges[i] != size[i] * (size[i] - 1)) clique = false;
         s.clique = clique;
     }
+    // exceptions: every pair must be excluded from the nonbonded sum
+    if (d.num_exceptions < 0 || (d.num_exceptions > 0 && (!d.exception_pairs || !d.exception_params)))
+        return "invalid exception list";
+    s.ex_pair.clear();
+    s.ex_prm.clear();
+    for (int e = 0; e < d.num_exceptions; ++e) {
+        const int a = d.exception_pairs[2 * e], b = d.exception_pairs[2 * e + 1];
+        if (a < 0 || b < 0 || a >= n || b >= n || a == b) return "exception index out of range or self pair";
+        if (!std::binary_search(s.excl_idx.begin() + s.excl_off[a], s.excl_idx.begin() + s.excl_off[a + 1], b))
+            return "exception pair " + std::to_string(a) + "-" + std::to_string(b) + " is not excluded";
+        const double qq = d.exception_params[3 * e], sg = d.exception_params[3 * e + 1],
+                     ep = d.exception_params[3 * e + 2];
+        if (!std::isfinite(qq) || !std::isfinite(sg) || !std::isfinite(ep) || ep < 0.0)
+            return "invalid exception parameters";
+        s.ex_pair.push_back(make_int2(a, b));
+        s.ex_prm.push_back(make_double4(kCoulomb * qq, sg, 4.0 * ep, 0.0));
+    }
     // grid
     SdmSys& g = s.dev;
     std::memset(&g, 0, sizeof g);
@@ -358,7 +378,8 @@ sdm_status upload_topology(sdm_handle* h) {
     std::vector<double> dd, org;
     std::vector<float> tab;
     std::vector<int4> ex4;
-    std::vector<int2> sten;
+    std::vector<int2> sten, exp_;
+    std::vector<double4> exq;
     std::vector<SdmSys> sd;
     int atom = 0, excl = 0, dbase = 0, cxbase = 0, tabbase = 0, orgbase = 0;
     for (auto& s : h->sys) {
@@ -370,6 +391,10 @@ sdm_status upload_topology(sdm_handle* h) {
         g.cx_base = cxbase;
         g.shift_base = tabbase;
         g.org_base = orgbase;
+        g.ex_base = (int)exp_.size();
+        g.ex_count = (int)s.ex_pair.size();
+        exp_.insert(exp_.end(), s.ex_pair.begin(), s.ex_pair.end());
+        exq.insert(exq.end(), s.ex_prm.begin(), s.ex_prm.end());
         q.insert(q.end(), s.q.begin(), s.q.end());
         hs.insert(hs.end(), s.hs.begin(), s.hs.end());
         se.insert(se.end(), s.se.begin(), s.se.end());
@@ -435,10 +460,20 @@ sdm_status upload_topology(sdm_handle* h) {
     if ((st = put(a.cx_idx, cxi.data(), cxi.size() * 4))) return st;
     if ((st = put(a.shift_tab, tab.data(), tab.size() * 4))) return st;
     if ((st = put(a.stencil, sten.data(), sten.size() * sizeof(int2)))) return st;
+    if (!exp_.empty()) {
+        if ((st = put(a.ex_pair, exp_.data(), exp_.size() * sizeof(int2)))) return st;
+        if ((st = put(a.ex_prm, exq.data(), exq.size() * sizeof(double4)))) return st;
+    }
     // perturbation windows depend on nD
-    int pw = 0;
-    for (auto& r : h->rep) { r.pert_win = pw; pw += 2 * h->sys[r.sys].dev.nD; }
+    int pw = 0, ew = 0;
+    for (auto& r : h->rep) {
+        r.pert_win = pw;
+        pw += 2 * h->sys[r.sys].dev.nD;
+        r.ex_win = ew;
+        ew += h->sys[r.sys].dev.ex_count;
+    }
     a.total_pert = pw;
+    a.total_ex = ew;
     if ((st = put(a.rep, h->rep.data(), h->rep.size() * sizeof(SdmRep)))) return st;
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
@@ -459,6 +494,7 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[h->opt_ctas], st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
     if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
+    if (mode == 0) SDM_CUDA(h, sdm_launch_exceptions(a, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[8], st, fl));
     if (mode == 0) SDM_CUDA(h, sdm_launch_finalize(a, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[9], st, fl));
@@ -655,6 +691,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     }
     // arena layout
     int tot_n = 0, tot_excl = 0, tot_D = 0, tot_cx = 0, tot_tab = 0, tot_cxidx = 0, tot_org = 0;
+    int tot_expair = 0;
+    long long tot_exitem = 0;
     for (auto& s : h->sys) {
         tot_n += s.n;
         tot_excl += (int)s.excl_idx.size();
@@ -662,6 +700,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
         tot_cx += (int)s.D.size() + 1;
         tot_tab += 2 * (s.dev.M[0] + s.dev.M[1] + s.dev.M[2]) + 3;
         tot_org += s.dev.M[0] + s.dev.M[1] + s.dev.M[2];
+        tot_expair += (int)s.ex_pair.size();
+        tot_exitem += (long long)s.ex_pair.size() * s.replicas;
     }
     // the displacement map may change later: reserve the worst case (every particle displaced)
     tot_D = std::max(tot_D, tot_n);
@@ -679,6 +719,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_grp = ar.take<int>(tot_n), o_d = ar.take<double>(3LL * tot_n);
     const size_t o_mol = ar.take<int>(tot_n), o_ex4t = ar.take<int4>(tot_n);
     const size_t o_org = ar.take<double>(std::max(tot_org, 1));
+    const size_t o_exp = ar.take<int2>(std::max(tot_expair, 1)), o_exq = ar.take<double4>(std::max(tot_expair, 1));
+    const size_t o_exe = ar.take<double>(std::max(tot_exitem, 1LL)), o_exu = ar.take<double>(std::max(tot_exitem, 1LL));
     const size_t o_eoff = ar.take<int>(tot_n + 1), o_eidx = ar.take<int>(std::max(tot_excl, 1));
     const size_t o_D = ar.take<int>(std::max(tot_D, 1)), o_cxo = ar.take<int>(tot_cx + 1);
     const size_t o_cxi = ar.take<int>(tot_cxidx), o_tab = ar.take<float>(tot_tab);
@@ -728,6 +770,10 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.topo_mol = at<int>(B, o_mol);
     a.topo_ex4 = at<int4>(B, o_ex4t);
     a.cell_org = at<double>(B, o_org);
+    a.ex_pair = at<int2>(B, o_exp);
+    a.ex_prm = at<double4>(B, o_exq);
+    a.ex_e0 = at<double>(B, o_exe);
+    a.ex_du = at<double>(B, o_exu);
     a.topo_d = at<double>(B, o_d);
     a.excl_off = at<int>(B, o_eoff);
     a.excl_idx = at<int>(B, o_eidx);

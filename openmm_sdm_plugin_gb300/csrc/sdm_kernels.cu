@@ -120,6 +120,14 @@ __device__ __forceinline__ int rep_by_pert(const SdmRep* rep, int nrep, int gi) 
     }
     return lo;
 }
+__device__ __forceinline__ int rep_by_ex(const SdmRep* rep, int nrep, int gi) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rep[mid].ex_win <= gi) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
 __device__ __forceinline__ int rep_by_item(const int* prefix, int nrep, int item) {
     int lo = 0, hi = nrep - 1;
     while (lo < hi) {
@@ -1622,6 +1630,73 @@ __global__ void __launch_bounds__(SDM_WARPS * 32) k_adjoint(SdmArgs a) {
 // ------------------------------------------------------------------------- //
 // K8: energies, soft core, bias (FP64)                                      //
 // ------------------------------------------------------------------------- //
+// ------------------------------------------------------------------------- //
+// Exceptions (OpenMM NonbondedForce exceptions, e.g. 1-4 pairs)             //
+// ------------------------------------------------------------------------- //
+// E = K qq / r + 4 eps ((sigma/r)^12 - (sigma/r)^6) on the caller's
+// coordinates (no cutoff, no reaction field, no periodic image), FP64; both
+// states when the two displacements differ.  One thread per (replica,
+// exception); forces enter the fixed-point F0 / dF of the two slots.
+__device__ __forceinline__ void ex_terms(const double4 p, double dx, double dy, double dz, double& e, double& fs) {
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    const double ir2 = 1.0 / r2, ir = sqrt(ir2);
+    const double s2 = p.y * p.y * ir2, s6 = s2 * s2 * s2, s12 = s6 * s6;
+    const double ec = p.x * ir;
+    e = ec + p.z * (s12 - s6);
+    fs = (ec + p.z * (12.0 * s12 - 6.0 * s6)) * ir2;
+}
+
+__device__ __forceinline__ void red_fixd(unsigned long long* p, double v, int* status) {
+    if (!(fabs(v) < 1.0e9)) {
+        atomicOr(status, SDM_DEV_FORCE_OVERFLOW);
+        return;
+    }
+    atomicAdd(p, (unsigned long long)__double2ll_rn(v * SDM_FIX_SCALE));
+}
+
+__global__ void k_except(SdmArgs a) {
+    const int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= a.total_ex) return;
+    const int r = rep_by_ex(a.rep, a.nrep, item);
+    const SdmRep& R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int e = item - R.ex_win;
+    const int2 pr = a.ex_pair[S.ex_base + e];
+    const double4 prm = a.ex_prm[S.ex_base + e];
+    const double* xi = a.x + 3 * (R.x_off + pr.x);
+    const double* xj = a.x + 3 * (R.x_off + pr.y);
+    const double* di = a.topo_d + 3 * (size_t)(S.atom_base + pr.x);
+    const double* dj = a.topo_d + 3 * (size_t)(S.atom_base + pr.y);
+    const size_t si = (size_t)R.slot_win + a.inv[R.atom_win + pr.x];
+    const size_t sj = (size_t)R.slot_win + a.inv[R.atom_win + pr.y];
+    const double d0[3] = {xj[0] - xi[0], xj[1] - xi[1], xj[2] - xi[2]};
+    double e0, f0;
+    ex_terms(prm, d0[0], d0[1], d0[2], e0, f0);
+    red_fixd(a.F0x + si, -f0 * d0[0], a.status);
+    red_fixd(a.F0y + si, -f0 * d0[1], a.status);
+    red_fixd(a.F0z + si, -f0 * d0[2], a.status);
+    red_fixd(a.F0x + sj, f0 * d0[0], a.status);
+    red_fixd(a.F0y + sj, f0 * d0[1], a.status);
+    red_fixd(a.F0z + sj, f0 * d0[2], a.status);
+    double du = 0.0;
+    if (di[0] != dj[0] || di[1] != dj[1] || di[2] != dj[2]) {
+        const double d1[3] = {(xj[0] + dj[0]) - (xi[0] + di[0]), (xj[1] + dj[1]) - (xi[1] + di[1]),
+                              (xj[2] + dj[2]) - (xi[2] + di[2])};
+        double e1, f1;
+        ex_terms(prm, d1[0], d1[1], d1[2], e1, f1);
+        du = e1 - e0;
+        unsigned long long* dF[3] = {a.dFx, a.dFy, a.dFz};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double g = f1 * d1[k] - f0 * d0[k];   // dF on j; -g on i
+            red_fixd(dF[k] + sj, g, a.status);
+            red_fixd(dF[k] + si, -g, a.status);
+        }
+    }
+    a.ex_e0[item] = e0;
+    a.ex_du[item] = du;
+}
+
 __device__ double block_sum(double v, double* red) {
     // deterministic: fixed-shape tree over a fixed partition
     const int t = threadIdx.x;
@@ -1660,10 +1735,12 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     double e0 = 0.0;
     const double* ep = a.e_part + (size_t)R.cl_win * a.split;
     for (int k = threadIdx.x; k < ncl * a.split; k += blockDim.x) e0 += ep[k];
+    for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) e0 += a.ex_e0[R.ex_win + k];
     const double U0 = block_sum(e0, red);
     double eu = 0.0;
     for (int k = threadIdx.x; k < 2 * S.nD * SDM_PERT_PARTS; k += blockDim.x)
         eu += a.p_part[(size_t)R.pert_win * SDM_PERT_PARTS + k];
+    for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) eu += a.ex_du[R.ex_win + k];
     const double u = block_sum(eu, red);
     if (threadIdx.x != 0) return;
     const double* p = a.params + (size_t)r * SDM_NPARAMS;
@@ -1974,6 +2051,12 @@ cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st) {
     if (grid > cap) grid = cap;
     if (mode == MODE_COUNT) k_perturb<MODE_COUNT><<<grid, SDM_WARPS * 32, 0, st>>>(a);
     else k_perturb<MODE_EVAL><<<grid, SDM_WARPS * 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st) {
+    if (a.total_ex == 0) return cudaSuccess;
+    k_except<<<(a.total_ex + 127) / 128, 128, 0, st>>>(a);
     return cudaGetLastError();
 }
 

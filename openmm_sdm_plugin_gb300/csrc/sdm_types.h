@@ -80,6 +80,7 @@ struct SdmSys {
     int excl_clique;  // 1: every exclusion component is a clique (excluded <=> same molecule id)
     int hst_base, hst_count;  // owner stencil (int2 column offsets), own column first
     int fst_base, fst_count;  // full stencil for point queries
+    int ex_base, ex_count;    // exceptions: offset into ex_pair/ex_prm, count
 };
 
 // per perturbation item (replica, displaced particle, state): the wrapped
@@ -101,6 +102,7 @@ struct SdmRep {
     int slot_cap;     // slots in the window
     int cl_win;       // cluster window base (slot_win/8)
     int pert_win;     // perturbation partial base (2*nD per replica)
+    int ex_win;       // exception item base (ex_count per replica)
 };
 
 // Everything a kernel needs, passed by value (fits the 32 KB parameter space).
@@ -116,6 +118,8 @@ struct SdmArgs {
     const int* topo_mol;  // exclusion component (molecule) id
     const int4* topo_ex4; // up to 4 exclusion partners (system-local; -1 none, -2 more than 4)
     const double* topo_d;
+    const int2* ex_pair;    // exceptions (system-local particle indices)
+    const double4* ex_prm;  // (K qq, sigma, 4 eps, 0)
     const int* excl_off;
     const int* excl_idx;
     const int* D_idx;     // system-local particle indices of displaced particles
@@ -171,6 +175,8 @@ struct SdmArgs {
     int jl_cap;
     double* e_part;      // cl window * SDM_MAX_SPLIT
     double* p_part;      // perturbation partials
+    double* ex_e0;       // per exception item: energy at x
+    double* ex_du;       // per exception item: E(x+d) - E(x) (0 when d_i = d_j)
     SdmPertPos* pert_pos; // per perturbation item (total_pert entries)
     double* adj;         // adjoint sums: 3 per perturbation item
     int* ncl;            // clusters per replica
@@ -190,5 +196,6 @@ struct SdmArgs {
     int total_cells;     // sum of ncol*M[2]+1 over replicas
     int total_slots;     // sum of slot_cap over replicas
     int total_pert;      // sum of 2*nD
+    int total_ex;        // sum of ex_count over replicas
     int split;           // work items per i-cluster
 };

@@ -91,6 +91,9 @@ class SDMSystem:
     cutoff: float = 1.0
     eps_rf: float = 78.5
     ligand_atoms: Optional[np.ndarray] = None   # indices of displaced particles
+    exceptions: Optional[np.ndarray] = None     # (X,2) int32 pairs with own parameters (also excluded)
+    exception_params: Optional[np.ndarray] = None  # (X,3) charge product e^2, sigma nm, epsilon kJ/mol
+    masses: Optional[np.ndarray] = None         # (N,) g/mol (dynamics only)
 
     @property
     def n(self) -> int:

@@ -26,6 +26,8 @@ _i = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _l = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 _u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 
+K_COULOMB = 138.935456   # kJ nm / (mol e^2) (OpenMM's ONE_4PI_EPS0, as in sdm_oracle.c)
+
 
 def build(force: bool = False) -> str:
     """Compiles the oracle with gcc (OpenMP, no FP contraction)."""
@@ -99,6 +101,9 @@ class OracleSystem:
         self.rc = float(sysm.cutoff)
         self.eps_rf = float(sysm.eps_rf)
         self.d = np.ascontiguousarray(sysm.displacement, np.float64).reshape(-1)
+        xp = getattr(sysm, "exceptions", None)
+        self.exc = None if xp is None or not len(xp) else np.asarray(xp, np.int64).reshape(-1, 2)
+        self.exc_prm = None if self.exc is None else np.asarray(sysm.exception_params, np.float64).reshape(-1, 3)
 
     def _args(self):
         return (self.n, self.q, self.sig, self.eps, self.off, self.idx, self.box, self.rc,
@@ -111,6 +116,46 @@ class OracleSystem:
         e = lib().orc_nonbonded(*self._args(), y,
                                 f.ctypes.data if forces else None, C.addressof(npairs), nthreads)
         return e, (f.reshape(-1, 3) if forces else None), npairs.value
+
+    def exceptions(self, x):
+        """Exception pairs (OpenMM NonbondedForce exceptions; the 1-4 pairs of
+        example/desmonddmsfile75.py:813-848): E = K qq/r + 4 eps((s/r)^12 - (s/r)^6)
+        on the given coordinates, no cutoff, no reaction field, no periodic image.
+        Returns (E0, du, F0, dF): du and dF only over pairs whose displacements
+        differ (the others are identical in both states)."""
+        n = self.n
+        F0 = np.zeros((n, 3))
+        dF = np.zeros((n, 3))
+        if self.exc is None:
+            return 0.0, 0.0, F0, dF
+        x = np.asarray(x, np.float64).reshape(-1, 3)
+        d = self.d.reshape(-1, 3)
+        i, j = self.exc[:, 0], self.exc[:, 1]
+        kqq = K_COULOMB * self.exc_prm[:, 0]
+        sg, e4 = self.exc_prm[:, 1], 4.0 * self.exc_prm[:, 2]
+
+        def terms(dv, sel):
+            r2 = (dv ** 2).sum(1)
+            ir2 = 1.0 / r2
+            ir = np.sqrt(ir2)
+            s6 = (sg[sel] * sg[sel] * ir2) ** 3
+            e = kqq[sel] * ir + e4[sel] * (s6 * s6 - s6)
+            fs = (kqq[sel] * ir + e4[sel] * (12.0 * s6 * s6 - 6.0 * s6)) * ir2
+            return e, fs[:, None] * dv    # force on j (minus: on i)
+        d0 = x[j] - x[i]
+        e0, f0 = terms(d0, slice(None))
+        np.add.at(F0, j, f0)
+        np.add.at(F0, i, -f0)
+        ch = np.any(d[i] != d[j], axis=1)
+        du = 0.0
+        if ch.any():
+            d1 = (x[j] + d[j]) - (x[i] + d[i])
+            e1, f1 = terms(d1[ch], ch)
+            du = float((e1 - e0[ch]).sum())
+            g = f1 - f0[ch]
+            np.add.at(dF, j[ch], g)
+            np.add.at(dF, i[ch], -g)
+        return float(e0.sum()), du, F0, dF
 
     def states(self, x, forces=True, nthreads=1):
         """FP64 rule: returns dict U0, U1, u_direct, F0, F1, counts."""
@@ -126,6 +171,14 @@ class OracleSystem:
                  P1delta=int(cnt[2]), Pc0=int(cnt[3]))
         if forces:
             r["F0"], r["F1"] = F0.reshape(-1, 3), F1.reshape(-1, 3)
+        if self.exc is not None:
+            e0, du, fx0, dfx = self.exceptions(x)
+            r["U0"] += e0
+            r["U1"] += e0 + du
+            r["u_direct"] += du
+            if forces:
+                r["F0"] = r["F0"] + fx0
+                r["F1"] = r["F1"] + fx0 + dfx
         return r
 
     def f32rule(self, x, M):
@@ -139,8 +192,16 @@ class OracleSystem:
                                     out, F0.ctypes.data, dF.ctypes.data, cnt)
         if img < 0:
             raise RuntimeError("oracle clustering capacity exceeded")
-        return dict(U0=out[0], u=out[1], U1=out[2], F0=F0.reshape(-1, 3), dF=dF.reshape(-1, 3),
-                    P0=int(cnt[0]), P1delta=int(cnt[1]), Pc0=int(cnt[2]), image_mode=img)
+        r = dict(U0=out[0], u=out[1], U1=out[2], F0=F0.reshape(-1, 3), dF=dF.reshape(-1, 3),
+                 P0=int(cnt[0]), P1delta=int(cnt[1]), Pc0=int(cnt[2]), image_mode=img)
+        if self.exc is not None:
+            e0, du, fx0, dfx = self.exceptions(x)
+            r["U0"] += e0
+            r["u"] += du
+            r["U1"] = r["U0"] + r["u"]
+            r["F0"] = r["F0"] + fx0
+            r["dF"] = r["dF"] + dfx
+        return r
 
     def clusters(self, x, M):
         x = np.ascontiguousarray(x, np.float64).reshape(-1)
