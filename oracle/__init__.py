@@ -301,3 +301,196 @@ def langevin_update(x, v, inv_mass, F, step_size, friction, temperature, normals
     xo = np.where(move[:, None], xp, x)
     vo = np.where(move[:, None], v2, v)
     return xo, vo
+
+
+# --------------------------------------------------------------------------- #
+# Ewald electrostatics (the reference's explicit-solvent setup uses PME,
+# example/test_explicit.py:64 through OpenMM NonbondedForce; restated from the
+# published Ewald decomposition, not from OpenMM source)
+# --------------------------------------------------------------------------- #
+def ewald_beta(cutoff, tolerance):
+    """Splitting parameter beta = sqrt(-ln(2 tol)) / rc (1/nm): erfc(beta rc) ~ tol."""
+    return np.sqrt(-np.log(2.0 * tolerance)) / cutoff
+
+
+def _min_image(dv, box):
+    return dv - box * np.round(dv / box)
+
+
+def ewald(x, q, box, beta, cutoff, exclusions=(), kmax=None, forces=True):
+    """Ewald sum, FP64, orthorhombic box.  Returns dict with the direct part
+    (pairs within the cutoff, minimum image, excluded pairs skipped), the
+    excluded-pair correction -K qq erf(beta r)/r, the reciprocal sum over
+    k = 2 pi n / L with |n_k| <= kmax, the self term -K beta/sqrt(pi) sum q^2,
+    the neutralising-background term -K pi Q^2 / (2 V beta^2), their total
+    and the forces (N, 3).  Direct space is all-pairs: for small systems."""
+    from math import erf, erfc
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    q = np.asarray(q, np.float64)
+    box = np.asarray(box, np.float64)
+    n = len(q)
+    V = float(np.prod(box))
+    F = np.zeros((n, 3))
+    excl = {(min(a, b), max(a, b)) for a, b in np.asarray(exclusions, np.int64).reshape(-1, 2)}
+    # direct space
+    iu, ju = np.triu_indices(n, 1)
+    dv = _min_image(x[ju] - x[iu], box)
+    r = np.sqrt((dv ** 2).sum(1))
+    keep = r < cutoff
+    if excl:
+        ex_mask = np.array([(a, b) in excl for a, b in zip(iu, ju)])
+        keep &= ~ex_mask
+    ec = np.array([erfc(beta * v) for v in r[keep]])
+    qq = K_COULOMB * q[iu[keep]] * q[ju[keep]]
+    rk = r[keep]
+    e_dir = float((qq * ec / rk).sum())
+    fs = qq * (ec / rk + 2.0 * beta / np.sqrt(np.pi) * np.exp(-(beta * rk) ** 2)) / rk ** 2
+    if forces:
+        fv = fs[:, None] * dv[keep]
+        np.add.at(F, ju[keep], fv)
+        np.add.at(F, iu[keep], -fv)
+    # excluded pairs: remove their reciprocal-space interaction
+    e_ex = 0.0
+    if excl:
+        pa = np.array(sorted(excl), np.int64)
+        dvx = _min_image(x[pa[:, 1]] - x[pa[:, 0]], box)
+        rx = np.sqrt((dvx ** 2).sum(1))
+        qqx = K_COULOMB * q[pa[:, 0]] * q[pa[:, 1]]
+        ef = np.array([erf(beta * v) for v in rx])
+        e_ex = float(-(qqx * ef / rx).sum())
+        fsx = -qqx * (ef / rx - 2.0 * beta / np.sqrt(np.pi) * np.exp(-(beta * rx) ** 2)) / rx ** 2
+        if forces:
+            fv = fsx[:, None] * dvx
+            np.add.at(F, pa[:, 1], fv)
+            np.add.at(F, pa[:, 0], -fv)
+    # reciprocal space
+    if kmax is None:
+        kmax = [int(np.ceil(1.8 * beta * L)) for L in box]   # exp(-pi^2 n^2/(beta L)^2) < ~1e-14
+    ns = np.stack(np.meshgrid(*[np.arange(-k, k + 1) for k in kmax], indexing="ij"), -1).reshape(-1, 3)
+    ns = ns[np.any(ns != 0, axis=1)]
+    kv = 2.0 * np.pi * ns / box
+    k2 = (kv ** 2).sum(1)
+    g = np.exp(-k2 / (4.0 * beta * beta)) / k2
+    e_rec = 0.0
+    for s in range(0, len(kv), 4096):
+        ph = x @ kv[s:s + 4096].T                   # (N, chunk)
+        c, sn = np.cos(ph), np.sin(ph)
+        Sc, Ss = q @ c, q @ sn
+        gs = g[s:s + 4096]
+        e_rec += float((gs * (Sc ** 2 + Ss ** 2)).sum())
+        if forces:
+            # F_i = (4 pi K / V) q_i sum_k g k (sin(k x_i) Sc - cos(k x_i) Ss)
+            w = gs * 1.0
+            F += (4.0 * np.pi * K_COULOMB / V) * q[:, None] * (
+                (sn * (w * Sc)[None, :] - c * (w * Ss)[None, :]) @ kv[s:s + 4096])
+    e_rec *= 2.0 * np.pi * K_COULOMB / V
+    e_self = float(-K_COULOMB * beta / np.sqrt(np.pi) * (q ** 2).sum())
+    Q = float(q.sum())
+    e_bg = float(-K_COULOMB * np.pi * Q * Q / (2.0 * V * beta * beta))
+    total = e_dir + e_ex + e_rec + e_self + e_bg
+    return dict(direct=e_dir, excluded=e_ex, reciprocal=e_rec, self=e_self, background=e_bg,
+                total=total, F=F)
+
+
+def pme_grid_size(beta, box, tolerance):
+    """Grid points per axis: the smallest n >= 2 beta L / (3 tol^(1/5)) whose
+    prime factors are 2, 3, 5 and 7 (the published OpenMM rule)."""
+    out = []
+    for L in np.asarray(box, np.float64):
+        n = int(np.ceil(2.0 * beta * L / (3.0 * tolerance ** 0.2)))
+        n = max(n, 6)
+        while True:
+            m = n
+            for p in (2, 3, 5, 7):
+                while m % p == 0:
+                    m //= p
+            if m == 1:
+                break
+            n += 1
+        out.append(n)
+    return np.array(out, np.int64)
+
+
+def _bspline(w, order):
+    """Cardinal B-spline weights M_order(w + j) and derivatives M'_order(w + j),
+    j = 0..order-1, for fractional offsets w in [0, 1) (vectorised over w).
+    Element j belongs to grid point floor(u) - j."""
+    w = np.asarray(w, np.float64)
+    M = np.zeros(w.shape + (order,))
+    M[..., 0] = w            # M_2(w)
+    M[..., 1] = 1.0 - w      # M_2(w + 1)
+    dM = None
+    for k in range(3, order + 1):
+        if k == order:       # M'_k(x) = M_{k-1}(x) - M_{k-1}(x - 1)
+            dM = np.zeros_like(M)
+            for j in range(k):
+                dM[..., j] = (M[..., j] if j < k - 1 else 0.0) - (M[..., j - 1] if j > 0 else 0.0)
+        new = np.zeros_like(M)
+        for j in range(k):   # M_k(x) = (x M_{k-1}(x) + (k - x) M_{k-1}(x - 1)) / (k - 1), x = w + j
+            xj = w + j
+            cur = M[..., j] if j < k - 1 else 0.0
+            prev = M[..., j - 1] if j > 0 else 0.0
+            new[..., j] = (xj * cur + (k - xj) * prev) / (k - 1)
+        M = new
+    return M, dM
+
+
+def spme(x, q, box, beta, grid, order=5, forces=True):
+    """Smooth particle-mesh Ewald reciprocal energy and forces (Essmann et
+    al., J. Chem. Phys. 103, 8577 (1995)), FP64, orthorhombic box.  Particle i
+    spreads onto grid points floor(u_i) - j, j = 0..order-1 (periodic), u_i =
+    K x_i / L.  Returns (E, F, phi) with phi the real-space potential grid
+    (theta_rec convolved with Q)."""
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    q = np.asarray(q, np.float64)
+    box = np.asarray(box, np.float64)
+    K = np.asarray(grid, np.int64)
+    n = len(q)
+    u = (x / box) % 1.0 * K
+    fl = np.floor(u).astype(np.int64)
+    w = u - fl
+    Ms, dMs, idx = [], [], []
+    for d in range(3):
+        M, dM = _bspline(w[:, d], order)
+        Ms.append(M); dMs.append(dM)
+        idx.append((fl[:, d][:, None] - np.arange(order)[None, :]) % K[d])
+    Q = np.zeros(tuple(K))
+    for a in range(order):
+        for b in range(order):
+            wab = q * Ms[0][:, a] * Ms[1][:, b]
+            for c in range(order):
+                np.add.at(Q, (idx[0][:, a], idx[1][:, b], idx[2][:, c]), wab * Ms[2][:, c])
+    # B-spline moduli |b(m)|^2 and the Ewald kernel
+    Mint, _ = _bspline(np.zeros(1), order)      # M_order(j), j = 0..order-1
+    bmod = []
+    for d in range(3):
+        m = np.arange(K[d])
+        j = np.arange(order - 1)
+        s2 = np.abs((Mint[0, j + 1][None, :] * np.exp(2j * np.pi * m[:, None] * j[None, :] / K[d])).sum(1)) ** 2
+        # for odd orders the sum vanishes at the Nyquist index: use the mean of the neighbours
+        z = s2 < 1e-7
+        if z.any():
+            s2[z] = 0.5 * (s2[(np.nonzero(z)[0] - 1) % K[d]] + s2[(np.nonzero(z)[0] + 1) % K[d]])
+        bmod.append(1.0 / s2)
+    mm = [np.where(np.arange(k) <= k // 2, np.arange(k), np.arange(k) - k) / L for k, L in zip(K, box)]
+    m2 = mm[0][:, None, None] ** 2 + mm[1][None, :, None] ** 2 + mm[2][None, None, :] ** 2
+    V = float(np.prod(box))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        C = np.exp(-np.pi ** 2 * m2 / beta ** 2) / (np.pi * V * m2)
+    C[0, 0, 0] = 0.0
+    BC = C * bmod[0][:, None, None] * bmod[1][None, :, None] * bmod[2][None, None, :]
+    FQ = np.fft.fftn(Q)
+    E = 0.5 * K_COULOMB * float((BC * np.abs(FQ) ** 2).sum())
+    phi = np.real(np.fft.ifftn(BC * FQ)) * np.prod(K)
+    F = None
+    if forces:
+        F = np.zeros((n, 3))
+        for a in range(order):
+            for b in range(order):
+                for c in range(order):
+                    p = phi[idx[0][:, a], idx[1][:, b], idx[2][:, c]]
+                    F[:, 0] -= dMs[0][:, a] * Ms[1][:, b] * Ms[2][:, c] * p
+                    F[:, 1] -= Ms[0][:, a] * dMs[1][:, b] * Ms[2][:, c] * p
+                    F[:, 2] -= Ms[0][:, a] * Ms[1][:, b] * dMs[2][:, c] * p
+        F *= K_COULOMB * q[:, None] * (K / box)[None, :]
+    return E, F, phi

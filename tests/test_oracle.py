@@ -285,3 +285,67 @@ def test_langevin_coefficients_and_update():
     assert np.allclose(vo[im != 0], v1[im != 0], rtol=1e-12)
     assert np.allclose(xo[im != 0], (x + dt * v1)[im != 0], rtol=1e-15)
     assert np.array_equal(xo[2], x[2]) and np.array_equal(vo[2], v[2])   # m^-1 = 0: fixed
+
+
+def test_ewald_madelung_constant_of_rock_salt():
+    """Golden value: the Madelung constant of NaCl, M = 1.747565 (per ion pair
+    E = -M K q^2 / r0), from a 2x2x2 conventional-cell lattice (64 ions)."""
+    a = 0.56                                  # nm, conventional cell; r0 = a/2
+    pts, qs = [], []
+    for i in range(4):
+        for j in range(4):
+            for k in range(4):
+                pts.append((i * a / 2, j * a / 2, k * a / 2))
+                qs.append(1.0 if (i + j + k) % 2 == 0 else -1.0)
+    x = np.array(pts) + 0.013
+    q = np.array(qs)
+    box = np.array([2 * a] * 3)
+    for beta in (10.0, 12.0):                 # erfc(beta rc) < 1e-13 at rc = 0.55 nm
+        e = oracle.ewald(x, q, box, beta, cutoff=0.55, forces=True)
+        M = -e["total"] * (a / 2) / (oracle.K_COULOMB * len(q) / 2)
+        assert M == pytest.approx(1.747565, abs=2e-6)
+        assert np.abs(e["F"]).max() < 1e-6 * oracle.K_COULOMB    # lattice sites: no net force
+
+
+def test_ewald_forces_are_minus_gradient():
+    rng = np.random.default_rng(4)
+    n = 24
+    box = np.array([1.9, 2.0, 2.1])
+    x = rng.uniform(0, 1, (n, 3)) * box
+    q = rng.choice([-0.5, 0.5], n)
+    q[0] += 0.1                                # net charge: background term
+    excl = np.array([[0, 1], [2, 3], [4, 7]])
+    beta, rc = 3.0, 0.9
+    e = oracle.ewald(x, q, box, beta, rc, excl)
+    h = 1e-6
+    for i, k in ((0, 0), (3, 1), (7, 2), (11, 0)):
+        xp, xm = x.copy(), x.copy()
+        xp[i, k] += h
+        xm[i, k] -= h
+        # small moves: no pair crosses the cutoff
+        g = (oracle.ewald(xp, q, box, beta, rc, excl, forces=False)["total"]
+             - oracle.ewald(xm, q, box, beta, rc, excl, forces=False)["total"]) / (2 * h)
+        assert e["F"][i, k] == pytest.approx(-g, rel=1e-5, abs=1e-4)
+    # independent of beta when converged (the split is exact)
+    e2 = oracle.ewald(x, q, box, 3.6, rc, excl)
+    assert e2["total"] == pytest.approx(e["total"], rel=2e-4, abs=2e-3)
+
+
+def test_spme_matches_ewald_reciprocal():
+    """The restated smooth PME converges to the exact reciprocal Ewald sum."""
+    rng = np.random.default_rng(8)
+    n = 60
+    box = np.array([2.0, 2.2, 2.4])
+    x = rng.uniform(0, 1, (n, 3)) * box
+    q = rng.uniform(-0.6, 0.6, n)
+    q -= q.mean()
+    beta = 3.2
+    ew = oracle.ewald(x, q, box, beta, 0.9)
+    # exact reciprocal forces: total minus direct minus nothing else (no exclusions)
+    ew_d = oracle.ewald(x, q, box, beta, 0.9, kmax=[0, 0, 0])
+    Frec = ew["F"] - ew_d["F"]
+    for K, tol in ((24, 2e-4), (48, 1e-6)):
+        E, F, _ = oracle.spme(x, q, box, beta, [K, K, K], order=5)
+        assert E == pytest.approx(ew["reciprocal"], rel=tol)
+        assert np.sqrt(((F - Frec) ** 2).sum() / (Frec ** 2).sum()) < 50 * tol
+    assert list(oracle.pme_grid_size(3.2, [6.2, 6.2, 6.2], 5e-4)) == [63, 63, 63]   # ceil(60.5) -> 3^2 7
