@@ -135,7 +135,19 @@ typedef struct {
     int num_exceptions;
     const int* exception_pairs;     /* [2*num_exceptions] particle indices */
     const double* exception_params; /* [3*num_exceptions] charge product (e^2), sigma (nm), epsilon (kJ/mol) */
+    /* Electrostatics: SDM_NB_REACTION_FIELD (0, default) or SDM_NB_PME (smooth
+     * particle-mesh Ewald as OpenMM's NonbondedForce.PME, the reference's
+     * explicit-solvent setup, example/test_explicit.py:64).  PME: splitting
+     * beta = sqrt(-ln(2 tol))/cutoff with tol = ewald_tolerance (0: 5e-4),
+     * grid pme_grid (0: the smallest 2,3,5,7-smooth n >= 2 beta L/(3 tol^0.2)),
+     * B-spline order 5; reaction_field_dielectric is ignored. */
+    int nonbonded_method;
+    double ewald_tolerance;
+    int pme_grid[3];
 } sdm_system_desc;
+
+#define SDM_NB_REACTION_FIELD 0
+#define SDM_NB_PME 1
 
 /* Creates a handle for num_systems systems on CUDA device `device`, owning all
  * device memory and one CUDA stream.  Replaces the reference's kernel

@@ -41,6 +41,7 @@ EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_export_lists", "sdm_evaluate_noalloc", "sdm_set_particle_params",
             "sdm_adjoint", "sdm_set_langevin", "sdm_langevin_step")
 
+NB_REACTION_FIELD, NB_PME = 0, 1
 NOALLOC_MAX_PARTICLES = 8192
 NOALLOC_SCRATCH_BYTES = 727296
 
@@ -67,6 +68,9 @@ class SystemDesc(C.Structure):
         ("num_exceptions", C.c_int),
         ("exception_pairs", C.POINTER(C.c_int)),
         ("exception_params", C.POINTER(C.c_double)),
+        ("nonbonded_method", C.c_int),
+        ("ewald_tolerance", C.c_double),
+        ("pme_grid", C.c_int * 3),
     ]
 
 
@@ -156,6 +160,12 @@ class Handle:
             d.cutoff = float(s.cutoff)
             d.reaction_field_dielectric = float(s.eps_rf)
             d.num_replicas = int(s.positions.shape[0]) if getattr(s, "positions", None) is not None else 1
+            if getattr(s, "nonbonded_method", "rf") == "pme":
+                d.nonbonded_method = NB_PME
+                d.ewald_tolerance = float(getattr(s, "ewald_tolerance", 5e-4))
+                g = getattr(s, "pme_grid", None)
+                if g is not None:
+                    d.pme_grid[:] = [int(v) for v in g]
             xp = getattr(s, "exceptions", None)
             if xp is not None and len(xp):
                 xpi = np.ascontiguousarray(np.asarray(xp, np.int32).reshape(-1))

@@ -26,7 +26,7 @@ cudaError_t sdm_pair_prepare();
 #define SDM_MAX_CTAS 4  // pair-kernel CTAs per SM with a built register bound
 int sdm_pair_resident(int ctas_per_sm);
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
-                            int resident, cudaStream_t st);
+                            int resident, bool pme, cudaStream_t st);
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
 cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
@@ -53,6 +53,8 @@ struct SysHost {
     std::vector<int2> hst, fst;  // owner / full column stencils
     std::vector<int2> ex_pair;   // exceptions (local indices)
     std::vector<double4> ex_prm; // (K qq, sigma, 4 eps, 0)
+    std::vector<int2> xc_pair;   // PME: excluded pairs i < j and K q_i q_j
+    std::vector<float> xc_qq;
     bool clique = false;
     SdmSys dev;
     int replicas;
@@ -137,6 +139,7 @@ struct sdm_handle {
     std::string err;
     // last evaluation pointers (for state forces)
     bool have_eval = false;
+    bool pme = false;            // every system uses PME (no mixed batches)
 };
 
 namespace {
@@ -196,7 +199,10 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
             return buf;
         }
     }
-    if (!(d.reaction_field_dielectric > 0.0)) return "reaction_field_dielectric must be > 0";
+    if (d.nonbonded_method != SDM_NB_REACTION_FIELD && d.nonbonded_method != SDM_NB_PME)
+        return "unknown nonbonded_method";
+    if (d.nonbonded_method == SDM_NB_REACTION_FIELD && !(d.reaction_field_dielectric > 0.0))
+        return "reaction_field_dielectric must be > 0";
     const int n = d.num_particles;
     s.n = n;
     s.replicas = d.num_replicas;
@@ -327,9 +333,52 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
     } else {
         s.hst = s.fst;
     }
-    const double e = d.reaction_field_dielectric, rc = d.cutoff;
-    g.krf = (float)((e - 1.0) / ((2.0 * e + 1.0) * rc * rc * rc));
-    g.crf = (float)(3.0 * e / ((2.0 * e + 1.0) * rc));
+    const double rc = d.cutoff;
+    if (d.nonbonded_method == SDM_NB_PME) {
+        const double tol = d.ewald_tolerance > 0.0 ? d.ewald_tolerance : 5e-4;
+        if (!(tol < 0.5)) return "ewald_tolerance must be below 0.5";
+        const double beta = std::sqrt(-std::log(2.0 * tol)) / rc;
+        g.pme = 1;
+        g.beta = beta;
+        g.beta_f = (float)beta;
+        g.c2_f = (float)(2.0 * beta / std::sqrt(M_PI));
+        g.krf = 0.0f;
+        g.crf = 0.0f;
+        for (int k = 0; k < 3; ++k) {
+            int m = d.pme_grid[k];
+            if (m <= 0) {   // smallest 2,3,5,7-smooth m >= 2 beta L / (3 tol^(1/5))
+                m = std::max(6, (int)std::ceil(2.0 * beta * d.box[k] / (3.0 * std::pow(tol, 0.2))));
+                for (;; ++m) {
+                    int v = m;
+                    for (int p : {2, 3, 5, 7})
+                        while (v % p == 0) v /= p;
+                    if (v == 1) break;
+                }
+            }
+            if (m < 6 || m > 1024) return "PME grid dimensions must be in 6..1024";
+            g.pme_grid[k] = m;
+        }
+        // self and neutralising-background terms (coordinate independent)
+        double q2 = 0.0, qs = 0.0;
+        for (int i = 0; i < n; ++i) { q2 += d.charge[i] * d.charge[i]; qs += d.charge[i]; }
+        const double V = d.box[0] * d.box[1] * d.box[2];
+        g.e_const = -kCoulomb * beta / std::sqrt(M_PI) * q2 - kCoulomb * M_PI * qs * qs / (2.0 * V * beta * beta);
+        // excluded pairs leave the reciprocal sum
+        s.xc_pair.clear();
+        s.xc_qq.clear();
+        for (int i = 0; i < n; ++i)
+            for (int k = s.excl_off[i]; k < s.excl_off[i + 1]; ++k) {
+                const int j = s.excl_idx[k];
+                if (j > i) {
+                    s.xc_pair.push_back(make_int2(i, j));
+                    s.xc_qq.push_back((float)(kCoulomb * d.charge[i] * d.charge[j]));
+                }
+            }
+    } else {
+        const double e = d.reaction_field_dielectric;
+        g.krf = (float)((e - 1.0) / ((2.0 * e + 1.0) * rc * rc * rc));
+        g.crf = (float)(3.0 * e / ((2.0 * e + 1.0) * rc));
+    }
     g.rc2f = (float)(rc * rc);
     g.rcl = (float)(rc + SDM_LIST_MARGIN);
     g.rcl2f = g.rcl * g.rcl;
@@ -378,8 +427,9 @@ sdm_status upload_topology(sdm_handle* h) {
     std::vector<double> dd, org;
     std::vector<float> tab;
     std::vector<int4> ex4;
-    std::vector<int2> sten, exp_;
+    std::vector<int2> sten, exp_, xcp;
     std::vector<double4> exq;
+    std::vector<float> xcq;
     std::vector<SdmSys> sd;
     int atom = 0, excl = 0, dbase = 0, cxbase = 0, tabbase = 0, orgbase = 0;
     for (auto& s : h->sys) {
@@ -395,6 +445,10 @@ sdm_status upload_topology(sdm_handle* h) {
         g.ex_count = (int)s.ex_pair.size();
         exp_.insert(exp_.end(), s.ex_pair.begin(), s.ex_pair.end());
         exq.insert(exq.end(), s.ex_prm.begin(), s.ex_prm.end());
+        g.xc_base = (int)xcp.size();
+        g.xc_count = (int)s.xc_pair.size();
+        xcp.insert(xcp.end(), s.xc_pair.begin(), s.xc_pair.end());
+        xcq.insert(xcq.end(), s.xc_qq.begin(), s.xc_qq.end());
         q.insert(q.end(), s.q.begin(), s.q.end());
         hs.insert(hs.end(), s.hs.begin(), s.hs.end());
         se.insert(se.end(), s.se.begin(), s.se.end());
@@ -464,16 +518,23 @@ sdm_status upload_topology(sdm_handle* h) {
         if ((st = put(a.ex_pair, exp_.data(), exp_.size() * sizeof(int2)))) return st;
         if ((st = put(a.ex_prm, exq.data(), exq.size() * sizeof(double4)))) return st;
     }
+    if (!xcp.empty()) {
+        if ((st = put(a.xc_pair, xcp.data(), xcp.size() * sizeof(int2)))) return st;
+        if ((st = put(a.xc_qq, xcq.data(), xcq.size() * sizeof(float)))) return st;
+    }
     // perturbation windows depend on nD
-    int pw = 0, ew = 0;
+    int pw = 0, ew = 0, xw = 0;
     for (auto& r : h->rep) {
         r.pert_win = pw;
         pw += 2 * h->sys[r.sys].dev.nD;
         r.ex_win = ew;
         ew += h->sys[r.sys].dev.ex_count;
+        r.xc_win = xw;
+        xw += h->sys[r.sys].dev.xc_count;
     }
     a.total_pert = pw;
     a.total_ex = ew;
+    a.total_xc = xw;
     if ((st = put(a.rep, h->rep.data(), h->rep.size() * sizeof(SdmRep)))) return st;
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
@@ -491,7 +552,7 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->cl_prefix, h->done, st, ev, 6, fl));
     SDM_CUDA(h, sdm_launch_jlist(a, h->cl_prefix, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[6], st, fl));
-    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[h->opt_ctas], st));
+    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[h->opt_ctas], h->pme, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
     if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
     if (mode == 0) SDM_CUDA(h, sdm_launch_exceptions(a, st));
@@ -659,6 +720,12 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
         }
         setup_displacement(h->sys[s], systems[s].displacement);
     }
+    h->pme = h->sys[0].dev.pme != 0;
+    for (int s = 1; s < num_systems; ++s)
+        if ((h->sys[s].dev.pme != 0) != h->pme) {
+            delete h;
+            return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "all systems of a handle must use the same nonbonded_method");
+        }
     // replica windows
     long long xo = 0;
     int aw = 0, cw = 0, sw = 0, zw = 0;
@@ -692,7 +759,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     // arena layout
     int tot_n = 0, tot_excl = 0, tot_D = 0, tot_cx = 0, tot_tab = 0, tot_cxidx = 0, tot_org = 0;
     int tot_expair = 0;
-    long long tot_exitem = 0;
+    long long tot_exitem = 0, tot_xcpair = 0, tot_xcitem = 0;
     for (auto& s : h->sys) {
         tot_n += s.n;
         tot_excl += (int)s.excl_idx.size();
@@ -702,6 +769,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
         tot_org += s.dev.M[0] + s.dev.M[1] + s.dev.M[2];
         tot_expair += (int)s.ex_pair.size();
         tot_exitem += (long long)s.ex_pair.size() * s.replicas;
+        tot_xcpair += (long long)s.xc_pair.size();
+        tot_xcitem += (long long)s.xc_pair.size() * s.replicas;
     }
     // the displacement map may change later: reserve the worst case (every particle displaced)
     tot_D = std::max(tot_D, tot_n);
@@ -721,6 +790,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_org = ar.take<double>(std::max(tot_org, 1));
     const size_t o_exp = ar.take<int2>(std::max(tot_expair, 1)), o_exq = ar.take<double4>(std::max(tot_expair, 1));
     const size_t o_exe = ar.take<double>(std::max(tot_exitem, 1LL)), o_exu = ar.take<double>(std::max(tot_exitem, 1LL));
+    const size_t o_xcp = ar.take<int2>(std::max(tot_xcpair, 1LL)), o_xcq = ar.take<float>(std::max(tot_xcpair, 1LL));
+    const size_t o_xce = ar.take<double>(std::max(tot_xcitem, 1LL)), o_xcu = ar.take<double>(std::max(tot_xcitem, 1LL));
     const size_t o_eoff = ar.take<int>(tot_n + 1), o_eidx = ar.take<int>(std::max(tot_excl, 1));
     const size_t o_D = ar.take<int>(std::max(tot_D, 1)), o_cxo = ar.take<int>(tot_cx + 1);
     const size_t o_cxi = ar.take<int>(tot_cxidx), o_tab = ar.take<float>(tot_tab);
@@ -774,6 +845,10 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.ex_prm = at<double4>(B, o_exq);
     a.ex_e0 = at<double>(B, o_exe);
     a.ex_du = at<double>(B, o_exu);
+    a.xc_pair = at<int2>(B, o_xcp);
+    a.xc_qq = at<float>(B, o_xcq);
+    a.xc_e0 = at<double>(B, o_xce);
+    a.xc_du = at<double>(B, o_xcu);
     a.topo_d = at<double>(B, o_d);
     a.excl_off = at<int>(B, o_eoff);
     a.excl_idx = at<int>(B, o_eidx);
@@ -1067,6 +1142,7 @@ sdm_status sdm_set_particle_params(sdm_handle* h, int system, int n, const int* 
 
 sdm_status sdm_adjoint(sdm_handle* h, double* out) {
     if (!h || !out) return SDM_ERR_INVALID_ARGUMENT;
+    if (h->pme) return fail(h, SDM_ERR_INVALID_ARGUMENT, "parameter derivatives are reaction-field only");
     if (!h->have_eval) return fail(h, SDM_ERR_INVALID_ARGUMENT, "no evaluation yet");
     cudaSetDevice(h->device);
     SDM_CUDA(h, cudaDeviceSynchronize());

@@ -720,7 +720,7 @@ __global__ void __launch_bounds__(256, 4) k_jlist(SdmArgs a, const int* cl_prefi
 // One tile: every lane owns one j of the ring window [head, head+count) and
 // sweeps the 8 i-particles of the cluster (warp-uniform i).  LJ = false is the
 // ring of j with epsilon = 0: Lennard-Jones vanishes for every i, Coulomb only.
-template <int MODE, bool IMG, bool LJ>
+template <int MODE, bool IMG, bool LJ, bool PME>
 __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
                                           const Ring& rg, const IParams& ip, unsigned head, int count,
                                           ICluster& ic, float& ef, long long& npair) {
@@ -765,7 +765,18 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
         float2 qq = __fmul2_rn(make_float2(qh.x, qh.y), qj);
         qq = make_float2(ok0 ? qq.x : 0.0f, ok1 ? qq.y : 0.0f);
         float2 fs;
-        const float2 fc = __fmul2_rn(qq, __ffma2_rn(krf2, r2s, ir));
+        float2 fc;
+        if (PME) {
+            // Ewald direct space: qq erfc(beta r)/r, force qq (erfc/r + 2beta/sqrt(pi) e^{-beta^2 r^2}) / r^2
+            const float2 xb = __fmul2_rn(__fmul2_rn(r2s, ir), make_float2(S.beta_f, S.beta_f));
+            const float2 ec = make_float2(erfcf(xb.x), erfcf(xb.y));
+            const float2 gx = make_float2(__expf(-xb.x * xb.x), __expf(-xb.y * xb.y));
+            const float2 eci = __fmul2_rn(ec, ir);
+            fc = __fmul2_rn(qq, __ffma2_rn(make_float2(S.c2_f, S.c2_f), gx, eci));
+            e = __ffma2_rn(qq, eci, e);
+        } else {
+            fc = __fmul2_rn(qq, __ffma2_rn(krf2, r2s, ir));
+        }
         if (LJ) {
             const float2 sg = __fadd2_rn(make_float2(qh.z, qh.w), hj);
             const float2 s2 = __fmul2_rn(__fmul2_rn(sg, sg), ir2);
@@ -774,10 +785,10 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
             epsm = make_float2(ok0 ? epsm.x : 0.0f, ok1 ? epsm.y : 0.0f);
             const float2 t6 = __fmul2_rn(epsm, s6);
             e = __ffma2_rn(t6, __fadd2_rn(s6, one_n), e);
-            e = __ffma2_rn(qq, __ffma2_rn(krf, r2s, __fadd2_rn(ir, ncrf)), e);
+            if (!PME) e = __ffma2_rn(qq, __ffma2_rn(krf, r2s, __fadd2_rn(ir, ncrf)), e);
             fs = __fmul2_rn(__ffma2_rn(t6, __ffma2_rn(c12, s6, c6n), fc), ir2);
         } else {
-            e = __ffma2_rn(qq, __ffma2_rn(krf, r2s, __fadd2_rn(ir, ncrf)), e);
+            if (!PME) e = __ffma2_rn(qq, __ffma2_rn(krf, r2s, __fadd2_rn(ir, ncrf)), e);
             fs = __fmul2_rn(fc, ir2);
         }
         fjx = __ffma2_rn(fs, dx, fjx);
@@ -827,7 +838,7 @@ __device__ __forceinline__ unsigned j_mask(const SdmArgs& a, const SdmSys& S, co
     return m;
 }
 
-template <int MODE, bool IMG>
+template <int MODE, bool IMG, bool PME>
 __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSmem& sm) {
     const int lane = lane_id();
     const SdmRep R = a.rep[r];
@@ -995,11 +1006,11 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
             tc += __popc(bco);
             __syncwarp();
             if (tl - hl >= 32u) {
-                eval_tile<MODE, IMG, true>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
+                eval_tile<MODE, IMG, true, PME>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
                 hl += 32u;
             }
             if (tc - hc >= 32u) {
-                eval_tile<MODE, IMG, false>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
+                eval_tile<MODE, IMG, false, PME>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
                 hc += 32u;
             }
             __syncwarp();
@@ -1014,8 +1025,8 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         }
         return;
     }
-    if (tl != hl) eval_tile<MODE, IMG, true>(a, S, R, sm.lj, sm.ip, hl, (int)(tl - hl), ic, ef, npair);
-    if (tc != hc) eval_tile<MODE, IMG, false>(a, S, R, sm.co, sm.ip, hc, (int)(tc - hc), ic, ef, npair);
+    if (tl != hl) eval_tile<MODE, IMG, true, PME>(a, S, R, sm.lj, sm.ip, hl, (int)(tl - hl), ic, ef, npair);
+    if (tc != hc) eval_tile<MODE, IMG, false, PME>(a, S, R, sm.co, sm.ip, hc, (int)(tc - hc), ic, ef, npair);
     if (MODE == MODE_COUNT) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) npair += __shfl_xor_sync(0xffffffffu, npair, o);
@@ -1079,7 +1090,7 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
 // NW warps per CTA, each with its own EvalSmem in dynamic shared memory;
 // MINB CTAs per SM fit the register file: registers per thread are capped at
 // 65536 / (MINB * NW * 32), rounded down to the allocation unit of 8
-template <int MODE, int MINB, int NW>
+template <int MODE, int MINB, int NW, bool PME = false>
 __global__ void __launch_bounds__(NW * 32) __maxnreg__((65536 / (MINB * NW * 32)) & ~7)
 k_pair(SdmArgs a, const int* item_prefix) {
     extern __shared__ __align__(16) unsigned char pair_smem[];
@@ -1092,8 +1103,8 @@ k_pair(SdmArgs a, const int* item_prefix) {
         const int local = item - item_prefix[r];
         const int I = local / a.split, part = local - I * a.split;
         if (MODE == MODE_EMIT && r != a.ex_rep) continue;
-        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) process_cluster<MODE, true>(a, r, I, part, sm);
-        else process_cluster<MODE, false>(a, r, I, part, sm);
+        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) process_cluster<MODE, true, PME>(a, r, I, part, sm);
+        else process_cluster<MODE, false, PME>(a, r, I, part, sm);
     }
 }
 
@@ -1107,6 +1118,13 @@ __device__ __forceinline__ void pair_terms(const SdmSys& S, float r2, float qq, 
     const float s2 = sg * sg * ir2;
     const float s6 = s2 * s2 * s2;
     const float t6 = eps4 * s6;
+    if (S.pme) {   // Ewald direct space
+        const float xb = r2 * ir * S.beta_f;
+        const float ec = erfcf(xb) * ir;
+        e = fmaf(t6, s6 - 1.0f, qq * ec);
+        fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qq * fmaf(S.c2_f, __expf(-xb * xb), ec)) * ir2;
+        return;
+    }
     e = fmaf(t6, s6 - 1.0f, qq * fmaf(S.krf, r2, ir - S.crf));
     fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qq * fmaf(-2.0f * S.krf, r2, ir)) * ir2;
 }
@@ -1697,6 +1715,80 @@ __global__ void k_except(SdmArgs a) {
     a.ex_du[item] = du;
 }
 
+// ------------------------------------------------------------------------- //
+// PME: excluded pairs leave the reciprocal sum (-K qq erf(beta r)/r)          //
+// ------------------------------------------------------------------------- //
+__device__ __forceinline__ int rep_by_xc(const SdmRep* rep, int nrep, int gi) {
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (rep[mid].xc_win <= gi) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// minimum-image separation in FP64 (the pair term itself is FP32)
+__device__ __forceinline__ void xc_delta(const SdmSys& S, const double* xi, const double* xj, const double* di,
+                                         const double* dj, bool state2, float d[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double v = state2 ? __dsub_rn(__dadd_rn(xj[k], dj[k]), __dadd_rn(xi[k], di[k])) : __dsub_rn(xj[k], xi[k]);
+        v = __fma_rn(-S.box[k], rint(__dmul_rn(v, S.invL[k])), v);
+        d[k] = __double2float_rn(v);
+    }
+}
+
+__device__ __forceinline__ void xc_terms(const SdmSys& S, float qq, const float d[3], float& e, float& fs) {
+    const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const float ir = rsqrtf(r2);
+    const float xb = r2 * ir * S.beta_f;
+    const float ef = erff(xb);
+    e = -qq * ef * ir;
+    fs = qq * (S.c2_f * __expf(-xb * xb) - ef * ir) * ir * ir;   // force on j = fs * d
+}
+
+__global__ void k_excl_corr(SdmArgs a) {
+    const int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= a.total_xc) return;
+    const int r = rep_by_xc(a.rep, a.nrep, item);
+    const SdmRep& R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int e = item - R.xc_win;
+    const int2 pr = a.xc_pair[S.xc_base + e];
+    const float qq = a.xc_qq[S.xc_base + e];
+    const double* xi = a.x + 3 * (R.x_off + pr.x);
+    const double* xj = a.x + 3 * (R.x_off + pr.y);
+    const double* di = a.topo_d + 3 * (size_t)(S.atom_base + pr.x);
+    const double* dj = a.topo_d + 3 * (size_t)(S.atom_base + pr.y);
+    const size_t si = (size_t)R.slot_win + a.inv[R.atom_win + pr.x];
+    const size_t sj = (size_t)R.slot_win + a.inv[R.atom_win + pr.y];
+    float d0[3], e0, f0;
+    xc_delta(S, xi, xj, di, dj, false, d0);
+    xc_terms(S, qq, d0, e0, f0);
+    unsigned long long* F0[3] = {a.F0x, a.F0y, a.F0z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        red_fix(F0[k] + sj, f0 * d0[k], a.status);
+        red_fix(F0[k] + si, -f0 * d0[k], a.status);
+    }
+    double du = 0.0;
+    if (di[0] != dj[0] || di[1] != dj[1] || di[2] != dj[2]) {
+        float d1[3], e1, f1;
+        xc_delta(S, xi, xj, di, dj, true, d1);
+        xc_terms(S, qq, d1, e1, f1);
+        du = (double)e1 - (double)e0;
+        unsigned long long* dF[3] = {a.dFx, a.dFy, a.dFz};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float g = f1 * d1[k] - f0 * d0[k];
+            red_fix(dF[k] + sj, g, a.status);
+            red_fix(dF[k] + si, -g, a.status);
+        }
+    }
+    a.xc_e0[item] = (double)e0;
+    a.xc_du[item] = du;
+}
+
 __device__ double block_sum(double v, double* red) {
     // deterministic: fixed-shape tree over a fixed partition
     const int t = threadIdx.x;
@@ -1736,11 +1828,13 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     const double* ep = a.e_part + (size_t)R.cl_win * a.split;
     for (int k = threadIdx.x; k < ncl * a.split; k += blockDim.x) e0 += ep[k];
     for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) e0 += a.ex_e0[R.ex_win + k];
-    const double U0 = block_sum(e0, red);
+    for (int k = threadIdx.x; k < S.xc_count; k += blockDim.x) e0 += a.xc_e0[R.xc_win + k];
+    const double U0 = block_sum(e0, red) + S.e_const;
     double eu = 0.0;
     for (int k = threadIdx.x; k < 2 * S.nD * SDM_PERT_PARTS; k += blockDim.x)
         eu += a.p_part[(size_t)R.pert_win * SDM_PERT_PARTS + k];
     for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) eu += a.ex_du[R.ex_win + k];
+    for (int k = threadIdx.x; k < S.xc_count; k += blockDim.x) eu += a.xc_du[R.xc_win + k];
     const double u = block_sum(eu, red);
     if (threadIdx.x != 0) return;
     const double* p = a.params + (size_t)r * SDM_NPARAMS;
@@ -1969,9 +2063,9 @@ cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_
 // the kernel spills).
 #define SDM_PAIR_SHAPES(X) X(4, 3) X(4, 4)
 
-template <int MODE, int MINB, int NW>
+template <int MODE, int MINB, int NW, bool PME = false>
 static cudaError_t pair_attr() {
-    return cudaFuncSetAttribute(k_pair<MODE, MINB, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_pair<MODE, MINB, NW, PME>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(NW * sizeof(EvalSmem)));
 }
 
@@ -1980,7 +2074,8 @@ static cudaError_t pair_attr() {
 cudaError_t sdm_pair_prepare() {
     cudaError_t e = cudaSuccess;
 #define SDM_ATTR(NW, MB) \
-    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW>();
+    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW>(); \
+    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW, true>();
     SDM_PAIR_SHAPES(SDM_ATTR)
 #undef SDM_ATTR
     if (e == cudaSuccess) e = pair_attr<MODE_COUNT, 3, 4>();
@@ -2023,14 +2118,15 @@ int sdm_pair_resident(int ctas_per_sm) {
 // resident = CTAs per SM that fit (sdm_pair_resident): the persistent static
 // schedule covers every item with any grid, so the grid never exceeds one wave
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
-                            int resident, cudaStream_t st) {
+                            int resident, bool pme, cudaStream_t st) {
     const int grid = num_sms() * std::max(1, std::min(ctas_per_sm, resident));
     if (mode == MODE_EVAL) {
         const int mb = pair_minb(ctas_per_sm);
-#define SDM_GO(NW, MB)                                                                                   \
-        if (mb == MB) {                                                                               \
-            k_pair<MODE_EVAL, MB, NW><<<grid, NW * 32, NW * sizeof(EvalSmem), st>>>(a, item_prefix); \
-            return cudaGetLastError();                                                                \
+#define SDM_GO(NW, MB)                                                                                        \
+        if (mb == MB) {                                                                                    \
+            if (pme) k_pair<MODE_EVAL, MB, NW, true><<<grid, NW * 32, NW * sizeof(EvalSmem), st>>>(a, item_prefix); \
+            else k_pair<MODE_EVAL, MB, NW><<<grid, NW * 32, NW * sizeof(EvalSmem), st>>>(a, item_prefix); \
+            return cudaGetLastError();                                                                     \
         }
         SDM_PAIR_SHAPES(SDM_GO)
 #undef SDM_GO
@@ -2055,8 +2151,8 @@ cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st) {
 }
 
 cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st) {
-    if (a.total_ex == 0) return cudaSuccess;
-    k_except<<<(a.total_ex + 127) / 128, 128, 0, st>>>(a);
+    if (a.total_ex) k_except<<<(a.total_ex + 127) / 128, 128, 0, st>>>(a);
+    if (a.total_xc) k_excl_corr<<<(a.total_xc + 127) / 128, 128, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -81,6 +81,14 @@ struct SdmSys {
     int hst_base, hst_count;  // owner stencil (int2 column offsets), own column first
     int fst_base, fst_count;  // full stencil for point queries
     int ex_base, ex_count;    // exceptions: offset into ex_pair/ex_prm, count
+    // PME (pme = 1): Ewald direct space replaces the reaction field
+    int pme;
+    float beta_f, c2_f;       // beta, 2 beta / sqrt(pi) (FP32 pair terms)
+    double beta;
+    double e_const;           // self + neutralising-background energy (constant)
+    int xc_base, xc_count;    // excluded-pair corrections: offset into xc_pair/xc_qq, count
+    int pme_grid[3];
+    int pme_base;             // offset of this system's B-spline moduli * Ewald kernel in pme_bc
 };
 
 // per perturbation item (replica, displaced particle, state): the wrapped
@@ -103,6 +111,7 @@ struct SdmRep {
     int cl_win;       // cluster window base (slot_win/8)
     int pert_win;     // perturbation partial base (2*nD per replica)
     int ex_win;       // exception item base (ex_count per replica)
+    int xc_win;       // excluded-pair correction item base (xc_count per replica)
 };
 
 // Everything a kernel needs, passed by value (fits the 32 KB parameter space).
@@ -120,6 +129,8 @@ struct SdmArgs {
     const double* topo_d;
     const int2* ex_pair;    // exceptions (system-local particle indices)
     const double4* ex_prm;  // (K qq, sigma, 4 eps, 0)
+    const int2* xc_pair;    // PME: excluded pairs (i < j, system-local) ...
+    const float* xc_qq;     // ... and their K q_i q_j
     const int* excl_off;
     const int* excl_idx;
     const int* D_idx;     // system-local particle indices of displaced particles
@@ -177,6 +188,8 @@ struct SdmArgs {
     double* p_part;      // perturbation partials
     double* ex_e0;       // per exception item: energy at x
     double* ex_du;       // per exception item: E(x+d) - E(x) (0 when d_i = d_j)
+    double* xc_e0;       // per excluded-pair item (PME): -K qq erf(beta r)/r at x
+    double* xc_du;       // ... and its change at x+d
     SdmPertPos* pert_pos; // per perturbation item (total_pert entries)
     double* adj;         // adjoint sums: 3 per perturbation item
     int* ncl;            // clusters per replica
@@ -197,5 +210,6 @@ struct SdmArgs {
     int total_slots;     // sum of slot_cap over replicas
     int total_pert;      // sum of 2*nD
     int total_ex;        // sum of ex_count over replicas
+    int total_xc;        // sum of xc_count over replicas
     int split;           // work items per i-cluster
 };

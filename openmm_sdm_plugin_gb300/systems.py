@@ -22,7 +22,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
-from typing import List, Optional
+from typing import List, Optional, Sequence
 
 import numpy as np
 
@@ -94,6 +94,9 @@ class SDMSystem:
     exceptions: Optional[np.ndarray] = None     # (X,2) int32 pairs with own parameters (also excluded)
     exception_params: Optional[np.ndarray] = None  # (X,3) charge product e^2, sigma nm, epsilon kJ/mol
     masses: Optional[np.ndarray] = None         # (N,) g/mol (dynamics only)
+    nonbonded_method: str = "rf"                # "rf" (reaction field) or "pme"
+    ewald_tolerance: float = 5e-4               # PME
+    pme_grid: Optional[Sequence[int]] = None    # PME grid (None: from the tolerance)
 
     @property
     def n(self) -> int:
