@@ -351,6 +351,22 @@ def main():
                             "stochastic-dynamics update in one CUDA graph per step (dt 2 fs, 1/ps, 300 K), "
                             "every step from the benchmark configuration"}
 
+    # ---- the same batch with PME electrostatics (smooth PME, order 5, tol 5e-4) ----
+    import dataclasses
+    sys_pme = dataclasses.replace(sysm, nonbonded_method="pme", ewald_tolerance=5e-4)
+    hp = capi.Handle([sys_pme], device=local)
+    for r in range(NREP):
+        hp.set_params(r, sys_pme.params[r].as_array())
+    npme = min(args.steps, 100)
+    ms_pm, _ = timed(lambda: hp.evaluate_device(xd.data_ptr(), rd.data_ptr(), fd.data_ptr(), sptr), npme, warm)
+    tot_pm = max_over_ranks(sum(ms_pm) / 1e3, dist, dev)
+    pme = {"value": whole_job_rate(NREP * npme, world, tot_pm), "unit": UNIT, "ms_per_call": sum(ms_pm) / npme,
+           "steps": npme, "device_status": hp.check_status(),
+           "workload": "the benchmark batch (22 x 22,580 particles) with PME instead of reaction field: "
+                       "Ewald direct space in the pair kernels, excluded-pair corrections, reciprocal space "
+                       "of both states (state-0 grid and the displaced-charge difference, cuFFT) per replica"}
+    hp.close()
+
     # ---- a real system: the TEMOA DMS fixture (20,446 particles, 606 1-4
     # exceptions), the same 22-state schedule, one batched call per step ----
     temoa = None
@@ -467,6 +483,7 @@ def main():
                                     "path": "same call, SDM_OPT_ZERO_COPY=1: k_cells reads the host coordinates"}},
         "langevin": langevin,
         "dms_temoa": temoa,
+        "pme": pme,
         "roofline": roof,
         "kernel_ms": breakdown,
         "cpu_baseline": cpu,

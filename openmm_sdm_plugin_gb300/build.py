@@ -1,7 +1,9 @@
 """Builds the in-tree CUDA library ``libsdm_gb300.so`` for sm_103a.
 
-Two translation units (kernels, host C-ABI) are compiled in parallel with
-nvcc and linked into one shared library next to this file.  No cmake.
+Three translation units (pair/list kernels, PME reciprocal space, host
+C-ABI) are compiled in parallel with nvcc and linked into one shared library
+next to this file, with the CUDA runtime static and cuFFT (PME) dynamic
+(rpath to the toolkit).  No cmake.
 """
 from __future__ import annotations
 
@@ -16,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsdm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["sdm_kernels.cu", "sdm_capi.cpp"]
+SOURCES = ["sdm_kernels.cu", "sdm_pme.cu", "sdm_capi.cpp"]
 HEADERS = ["sdm_types.h", os.path.join("..", "..", "include", "sdm_capi.h")]
 
 
@@ -59,7 +61,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+    libdir = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "lib64")
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-L", libdir, "-lcufft", "-Xlinker", "-rpath," + libdir,
+                                                           "-lcudart_static", "-lrt", "-ldl", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

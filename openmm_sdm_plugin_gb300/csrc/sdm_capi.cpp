@@ -5,6 +5,7 @@
 // graphs (one per distinct set of input/output pointers).  Nothing here throws
 // across the ABI: every entry point catches and converts to an sdm_status.
 #include <cuda_runtime.h>
+#include <cufft.h>
 
 #include <algorithm>
 #include <cmath>
@@ -29,6 +30,8 @@ cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, 
                             int resident, bool pme, cudaStream_t st);
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
 cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st);
+cudaError_t sdm_launch_pme(const SdmArgs& a, const cufftHandle* r2c, const cufftHandle* c2r, const long long* grid_off,
+                           const long long* spec_off, int nsys, int conv_blocks, cudaStream_t st);
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_adjoint(const SdmArgs& a, cudaStream_t st);
@@ -55,6 +58,7 @@ struct SysHost {
     std::vector<double4> ex_prm; // (K qq, sigma, 4 eps, 0)
     std::vector<int2> xc_pair;   // PME: excluded pairs i < j and K q_i q_j
     std::vector<float> xc_qq;
+    std::vector<float> theta;    // PME: Ewald kernel x B-spline moduli, half spectrum
     bool clique = false;
     SdmSys dev;
     int replicas;
@@ -140,6 +144,8 @@ struct sdm_handle {
     // last evaluation pointers (for state forces)
     bool have_eval = false;
     bool pme = false;            // every system uses PME (no mixed batches)
+    std::vector<cufftHandle> pme_r2c, pme_c2r;      // per system, batch 2 grids per replica
+    std::vector<long long> pme_grid_off, pme_spec_off;
 };
 
 namespace {
@@ -363,6 +369,42 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
         for (int i = 0; i < n; ++i) { q2 += d.charge[i] * d.charge[i]; qs += d.charge[i]; }
         const double V = d.box[0] * d.box[1] * d.box[2];
         g.e_const = -kCoulomb * beta / std::sqrt(M_PI) * q2 - kCoulomb * M_PI * qs * qs / (2.0 * V * beta * beta);
+        // Ewald kernel x B-spline moduli on the half spectrum (order 5):
+        // theta(m) = |b0|^2 |b1|^2 |b2|^2 exp(-pi^2 m^2 / beta^2) / (pi V m^2)
+        {
+            const double m5[4] = {1.0 / 24.0, 11.0 / 24.0, 11.0 / 24.0, 1.0 / 24.0};   // M_5(1..4)
+            std::vector<double> bm[3];
+            for (int k = 0; k < 3; ++k) {
+                const int K = g.pme_grid[k];
+                std::vector<double> s2(K);
+                for (int m = 0; m < K; ++m) {
+                    double re = 0.0, im = 0.0;
+                    for (int j = 0; j < 4; ++j) {
+                        re += m5[j] * std::cos(2.0 * M_PI * m * j / K);
+                        im += m5[j] * std::sin(2.0 * M_PI * m * j / K);
+                    }
+                    s2[m] = re * re + im * im;
+                }
+                for (int m = 0; m < K; ++m)   // odd order: zero at the Nyquist index, use the neighbours
+                    if (s2[m] < 1e-7) s2[m] = 0.5 * (s2[(m + K - 1) % K] + s2[(m + 1) % K]);
+                bm[k].resize(K);
+                for (int m = 0; m < K; ++m) bm[k][m] = 1.0 / s2[m];
+            }
+            const int K0 = g.pme_grid[0], K1 = g.pme_grid[1], K2 = g.pme_grid[2], K2h = K2 / 2 + 1;
+            const double V = d.box[0] * d.box[1] * d.box[2];
+            s.theta.assign((size_t)K0 * K1 * K2h, 0.0f);
+            for (int a = 0; a < K0; ++a)
+                for (int b = 0; b < K1; ++b)
+                    for (int c = 0; c < K2h; ++c) {
+                        if (a == 0 && b == 0 && c == 0) continue;
+                        const double ma = (a <= K0 / 2 ? a : a - K0) / d.box[0];
+                        const double mb = (b <= K1 / 2 ? b : b - K1) / d.box[1];
+                        const double mc = c / d.box[2];
+                        const double m2 = ma * ma + mb * mb + mc * mc;
+                        s.theta[((size_t)a * K1 + b) * K2h + c] = (float)(
+                            bm[0][a] * bm[1][b] * bm[2][c] * std::exp(-M_PI * M_PI * m2 / (beta * beta)) / (M_PI * V * m2));
+                    }
+        }
         // excluded pairs leave the reciprocal sum
         s.xc_pair.clear();
         s.xc_qq.clear();
@@ -429,7 +471,7 @@ sdm_status upload_topology(sdm_handle* h) {
     std::vector<int4> ex4;
     std::vector<int2> sten, exp_, xcp;
     std::vector<double4> exq;
-    std::vector<float> xcq;
+    std::vector<float> xcq, th;
     std::vector<SdmSys> sd;
     int atom = 0, excl = 0, dbase = 0, cxbase = 0, tabbase = 0, orgbase = 0;
     for (auto& s : h->sys) {
@@ -445,6 +487,8 @@ sdm_status upload_topology(sdm_handle* h) {
         g.ex_count = (int)s.ex_pair.size();
         exp_.insert(exp_.end(), s.ex_pair.begin(), s.ex_pair.end());
         exq.insert(exq.end(), s.ex_prm.begin(), s.ex_prm.end());
+        g.pme_base = (int)th.size();
+        th.insert(th.end(), s.theta.begin(), s.theta.end());
         g.xc_base = (int)xcp.size();
         g.xc_count = (int)s.xc_pair.size();
         xcp.insert(xcp.end(), s.xc_pair.begin(), s.xc_pair.end());
@@ -522,6 +566,8 @@ sdm_status upload_topology(sdm_handle* h) {
         if ((st = put(a.xc_pair, xcp.data(), xcp.size() * sizeof(int2)))) return st;
         if ((st = put(a.xc_qq, xcq.data(), xcq.size() * sizeof(float)))) return st;
     }
+    if (!th.empty())
+        if ((st = put(a.pme_theta, th.data(), th.size() * sizeof(float)))) return st;
     // perturbation windows depend on nD
     int pw = 0, ew = 0, xw = 0;
     for (auto& r : h->rep) {
@@ -556,6 +602,9 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
     if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
     if (mode == 0) SDM_CUDA(h, sdm_launch_exceptions(a, st));
+    if (mode == 0 && h->pme)
+        SDM_CUDA(h, sdm_launch_pme(a, h->pme_r2c.data(), h->pme_c2r.data(), h->pme_grid_off.data(),
+                                   h->pme_spec_off.data(), (int)h->sys.size(), a.pme_conv_blocks, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[8], st, fl));
     if (mode == 0) SDM_CUDA(h, sdm_launch_finalize(a, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[9], st, fl));
@@ -727,13 +776,22 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
             return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "all systems of a handle must use the same nonbonded_method");
         }
     // replica windows
-    long long xo = 0;
+    long long xo = 0, pg = 0, ps = 0;
     int aw = 0, cw = 0, sw = 0, zw = 0;
     for (int s = 0; s < num_systems; ++s) {
         const SysHost& S = h->sys[s];
+        const long long kp = S.dev.pme ? (long long)S.dev.pme_grid[0] * S.dev.pme_grid[1] * S.dev.pme_grid[2] : 0;
+        const long long kh = S.dev.pme ? (long long)S.dev.pme_grid[0] * S.dev.pme_grid[1] * (S.dev.pme_grid[2] / 2 + 1) : 0;
+        h->pme_grid_off.push_back(pg);
+        h->pme_spec_off.push_back(ps);
         for (int k = 0; k < S.replicas; ++k) {
             SdmRep r{};
             r.sys = s;
+            r.pg_win = pg;
+            r.pg_size = kp;
+            r.ps_win = ps;
+            pg += 2 * kp;
+            ps += 2 * kh;
             r.n = S.n;
             r.x_off = xo;
             r.atom_win = aw;
@@ -792,6 +850,12 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_exe = ar.take<double>(std::max(tot_exitem, 1LL)), o_exu = ar.take<double>(std::max(tot_exitem, 1LL));
     const size_t o_xcp = ar.take<int2>(std::max(tot_xcpair, 1LL)), o_xcq = ar.take<float>(std::max(tot_xcpair, 1LL));
     const size_t o_xce = ar.take<double>(std::max(tot_xcitem, 1LL)), o_xcu = ar.take<double>(std::max(tot_xcitem, 1LL));
+    long long tot_theta = 0;
+    for (auto& s : h->sys) tot_theta += (long long)s.theta.size();
+    const int conv_blocks = 64;
+    const size_t o_pacc = ar.take<unsigned long long>(std::max(pg, 1LL)), o_pgrid = ar.take<float>(std::max(pg, 1LL));
+    const size_t o_pspec = ar.take<float2>(std::max(ps, 1LL)), o_pth = ar.take<float>(std::max(tot_theta, 1LL));
+    const size_t o_pep = ar.take<double>((size_t)nrep * conv_blocks), o_pdu = ar.take<double>(std::max(Pp / 2, 1LL));
     const size_t o_eoff = ar.take<int>(tot_n + 1), o_eidx = ar.take<int>(std::max(tot_excl, 1));
     const size_t o_D = ar.take<int>(std::max(tot_D, 1)), o_cxo = ar.take<int>(tot_cx + 1);
     const size_t o_cxi = ar.take<int>(tot_cxidx), o_tab = ar.take<float>(tot_tab);
@@ -906,6 +970,28 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.total_atoms = (int)A;
     a.total_cols = (int)Ccol;
     a.total_cells = (int)Ccel;
+    a.pme_charge = a.topo_q;
+    a.pme_acc = at<unsigned long long>(B, o_pacc);
+    a.pme_grid = at<float>(B, o_pgrid);
+    a.pme_spec = at<float2>(B, o_pspec);
+    a.pme_theta = at<float>(B, o_pth);
+    a.pme_epart = at<double>(B, o_pep);
+    a.pme_du = at<double>(B, o_pdu);
+    a.pme_total_grid = pg;
+    a.pme_conv_blocks = conv_blocks;
+    if (h->pme) {   // cuFFT plans: per system, two grids (state 0, dQ) per replica
+        for (int s = 0; s < num_systems; ++s) {
+            int n[3] = {h->sys[s].dev.pme_grid[0], h->sys[s].dev.pme_grid[1], h->sys[s].dev.pme_grid[2]};
+            cufftHandle p1 = 0, p2 = 0;
+            if (cufftPlanMany(&p1, 3, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_R2C, 2 * h->sys[s].replicas) != CUFFT_SUCCESS ||
+                cufftPlanMany(&p2, 3, n, nullptr, 1, 0, nullptr, 1, 0, CUFFT_C2R, 2 * h->sys[s].replicas) != CUFFT_SUCCESS) {
+                fail(h, SDM_ERR_CUDA, "cufftPlanMany failed");
+                return bail(SDM_ERR_CUDA);
+            }
+            h->pme_r2c.push_back(p1);
+            h->pme_c2r.push_back(p2);
+        }
+    }
     a.total_slots = (int)Sl;
     a.split = 1;
     a.ex_cap = 0;
@@ -941,6 +1027,8 @@ sdm_status sdm_destroy(sdm_handle* h) {
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
     for (int k = 0; k < 12; ++k) if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+    for (auto p : h->pme_r2c) cufftDestroy(p);
+    for (auto p : h->pme_c2r) cufftDestroy(p);
     if (h->stream) { cudaStreamSynchronize(h->stream); cudaStreamDestroy(h->stream); }
     if (h->arena) cudaFree(h->arena);
     if (h->params_pinned) cudaFreeHost(h->params_pinned);

@@ -1829,12 +1829,16 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     for (int k = threadIdx.x; k < ncl * a.split; k += blockDim.x) e0 += ep[k];
     for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) e0 += a.ex_e0[R.ex_win + k];
     for (int k = threadIdx.x; k < S.xc_count; k += blockDim.x) e0 += a.xc_e0[R.xc_win + k];
+    if (S.pme)
+        for (int k = threadIdx.x; k < a.pme_conv_blocks; k += blockDim.x) e0 += a.pme_epart[(size_t)r * a.pme_conv_blocks + k];
     const double U0 = block_sum(e0, red) + S.e_const;
     double eu = 0.0;
     for (int k = threadIdx.x; k < 2 * S.nD * SDM_PERT_PARTS; k += blockDim.x)
         eu += a.p_part[(size_t)R.pert_win * SDM_PERT_PARTS + k];
     for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) eu += a.ex_du[R.ex_win + k];
     for (int k = threadIdx.x; k < S.xc_count; k += blockDim.x) eu += a.xc_du[R.xc_win + k];
+    if (S.pme)
+        for (int k = threadIdx.x; k < S.nD; k += blockDim.x) eu += a.pme_du[R.pert_win / 2 + k];
     const double u = block_sum(eu, red);
     if (threadIdx.x != 0) return;
     const double* p = a.params + (size_t)r * SDM_NPARAMS;

@@ -112,6 +112,9 @@ struct SdmRep {
     int pert_win;     // perturbation partial base (2*nD per replica)
     int ex_win;       // exception item base (ex_count per replica)
     int xc_win;       // excluded-pair correction item base (xc_count per replica)
+    long long pg_win; // PME: offset of this replica's state-0 grid (its dQ grid follows)
+    long long pg_size;  // PME: grid points of one grid
+    long long ps_win; // PME: offset of this replica's state-0 spectrum (its dQ spectrum follows)
 };
 
 // Everything a kernel needs, passed by value (fits the 32 KB parameter space).
@@ -190,6 +193,16 @@ struct SdmArgs {
     double* ex_du;       // per exception item: E(x+d) - E(x) (0 when d_i = d_j)
     double* xc_e0;       // per excluded-pair item (PME): -K qq erf(beta r)/r at x
     double* xc_du;       // ... and its change at x+d
+    // PME reciprocal space
+    const float* pme_charge;        // q sqrt(K) per particle (the topology charges)
+    unsigned long long* pme_acc;    // fixed-point spread grids (2 per replica)
+    float* pme_grid;                // float grids: spread charges, then potentials
+    float2* pme_spec;               // half spectra (2 per replica)
+    const float* pme_theta;         // per system: Ewald kernel x B-spline moduli, half spectrum
+    double* pme_epart;              // per replica x convolution block: state-0 energy partials
+    double* pme_du;                 // per displaced particle: reciprocal part of u
+    long long pme_total_grid;       // grid points over all grids
+    int pme_conv_blocks;
     SdmPertPos* pert_pos; // per perturbation item (total_pert entries)
     double* adj;         // adjoint sums: 3 per perturbation item
     int* ncl;            // clusters per replica
