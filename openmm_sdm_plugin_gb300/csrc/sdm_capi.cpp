@@ -343,6 +343,8 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
     if (d.nonbonded_method == SDM_NB_PME) {
         const double tol = d.ewald_tolerance > 0.0 ? d.ewald_tolerance : 5e-4;
         if (!(tol < 0.5)) return "ewald_tolerance must be below 0.5";
+        // the FP32 screening function of the pair kernels covers beta rc <= 4
+        if (!(tol >= 5.7e-8)) return "ewald_tolerance must be at least 5.7e-8";
         const double beta = std::sqrt(-std::log(2.0 * tol)) / rc;
         g.pme = 1;
         g.beta = beta;

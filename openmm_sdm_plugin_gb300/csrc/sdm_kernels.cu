@@ -84,6 +84,41 @@ __device__ __forceinline__ float fast_rsqrt(float x) {
     return y;
 }
 
+__device__ __forceinline__ float fast_rcp(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Ewald screening: erfc(x) = R(t) exp(-x^2), t = 1 / (1 + kErfcP x), R a
+// degree-7 polynomial in t fitted to erfc(x) exp(x^2) for 0 <= x <= 4
+// (least squares with Lawson reweighting, csrc/fit_erfc.py): relative error
+// 2e-8 in exact arithmetic, 4e-7 evaluated in FP32 with the exponential.
+// The exponential is the one the Ewald force needs anyway.  Valid for
+// beta rc <= 4, i.e. Ewald tolerances >= 5.7e-8 (checked on the host).
+constexpr float kErfcP = 0.46f;
+__device__ __forceinline__ float2 erfc_scaled2(float2 x) {
+    const float2 t = make_float2(fast_rcp(__fmaf_rn(kErfcP, x.x, 1.0f)), fast_rcp(__fmaf_rn(kErfcP, x.y, 1.0f)));
+    float2 r = __ffma2_rn(make_float2(0.10056333988904953f, 0.10056333988904953f), t,
+                          make_float2(-0.5065137147903442f, -0.5065137147903442f));
+    r = __ffma2_rn(r, t, make_float2(0.8315963745117188f, 0.8315963745117188f));
+    r = __ffma2_rn(r, t, make_float2(-0.3618384897708893f, -0.3618384897708893f));
+    r = __ffma2_rn(r, t, make_float2(0.4733056426048279f, 0.4733056426048279f));
+    r = __ffma2_rn(r, t, make_float2(0.19405683875083923f, 0.19405683875083923f));
+    r = __ffma2_rn(r, t, make_float2(0.269482284784317f, 0.269482284784317f));
+    return __ffma2_rn(r, t, make_float2(-0.0006523068295791745f, -0.0006523068295791745f));
+}
+__device__ __forceinline__ float erfc_scaled(float x) {
+    const float t = fast_rcp(__fmaf_rn(kErfcP, x, 1.0f));
+    float r = __fmaf_rn(0.10056333988904953f, t, -0.5065137147903442f);
+    r = __fmaf_rn(r, t, 0.8315963745117188f);
+    r = __fmaf_rn(r, t, -0.3618384897708893f);
+    r = __fmaf_rn(r, t, 0.4733056426048279f);
+    r = __fmaf_rn(r, t, 0.19405683875083923f);
+    r = __fmaf_rn(r, t, 0.269482284784317f);
+    return __fmaf_rn(r, t, -0.0006523068295791745f);
+}
+
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
@@ -769,9 +804,8 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
         if (PME) {
             // Ewald direct space: qq erfc(beta r)/r, force qq (erfc/r + 2beta/sqrt(pi) e^{-beta^2 r^2}) / r^2
             const float2 xb = __fmul2_rn(__fmul2_rn(r2s, ir), make_float2(S.beta_f, S.beta_f));
-            const float2 ec = make_float2(erfcf(xb.x), erfcf(xb.y));
             const float2 gx = make_float2(__expf(-xb.x * xb.x), __expf(-xb.y * xb.y));
-            const float2 eci = __fmul2_rn(ec, ir);
+            const float2 eci = __fmul2_rn(__fmul2_rn(erfc_scaled2(xb), gx), ir);
             fc = __fmul2_rn(qq, __ffma2_rn(make_float2(S.c2_f, S.c2_f), gx, eci));
             e = __ffma2_rn(qq, eci, e);
         } else {
@@ -1120,9 +1154,10 @@ __device__ __forceinline__ void pair_terms(const SdmSys& S, float r2, float qq, 
     const float t6 = eps4 * s6;
     if (S.pme) {   // Ewald direct space
         const float xb = r2 * ir * S.beta_f;
-        const float ec = erfcf(xb) * ir;
+        const float gx = __expf(-xb * xb);
+        const float ec = erfc_scaled(xb) * gx * ir;
         e = fmaf(t6, s6 - 1.0f, qq * ec);
-        fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qq * fmaf(S.c2_f, __expf(-xb * xb), ec)) * ir2;
+        fs = fmaf(t6, fmaf(12.0f, s6, -6.0f), qq * fmaf(S.c2_f, gx, ec)) * ir2;
         return;
     }
     e = fmaf(t6, s6 - 1.0f, qq * fmaf(S.krf, r2, ir - S.crf));
