@@ -32,6 +32,7 @@ cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
 cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_pme(const SdmArgs& a, const cufftHandle* r2c, const cufftHandle* c2r, const long long* grid_off,
                            const long long* spec_off, int nsys, int conv_blocks, cudaStream_t st);
+cudaError_t sdm_pme_prepare(int smem_bytes);
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_adjoint(const SdmArgs& a, cudaStream_t st);
@@ -40,6 +41,8 @@ namespace {
 
 const double kCoulomb = 138.935456;  // kJ nm / (mol e^2), OpenMM's ONE_4PI_EPS0
 const double kMolarGasConstant = 0.008314462618;  // kJ / (mol K), R of CODATA 2018 (k_B N_A)
+const long long kPmeBrickPoints = 6144;   // preferred sub-grid size of a PME brick (48 KB of fixed point)
+const long long kPmeBrickMax = 27648;     // largest sub-grid (216 KB); bricks beyond it use global atomics
 thread_local std::string g_create_error;
 
 struct SysHost {
@@ -365,6 +368,23 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
             }
             if (m < 6 || m > 1024) return "PME grid dimensions must be in 6..1024";
             g.pme_grid[k] = m;
+            g.pme_gs[k] = (float)((double)m / d.box[k]);
+        }
+        // spreading / interpolation bricks of bc cells per side: the stencils of
+        // a brick's particles cover at most ceil(bc K / M) + 5 grid points per
+        // dimension (+2 for FP32 rounding at the cell faces)
+        for (int bc = 5; bc >= 1; --bc) {
+            long long cap = 1;
+            for (int k = 0; k < 3; ++k)
+                cap *= (long long)std::ceil((double)std::min(bc, g.M[k]) * g.pme_grid[k] / g.M[k]) + 7;
+            if (cap <= kPmeBrickPoints || bc == 1) {
+                for (int k = 0; k < 3; ++k) {
+                    g.pme_bc[k] = std::min(bc, g.M[k]);
+                    g.pme_nb[k] = (g.M[k] + g.pme_bc[k] - 1) / g.pme_bc[k];
+                }
+                g.pme_cap = (int)std::min(cap, (long long)kPmeBrickMax);
+                break;
+            }
         }
         // self and neutralising-background terms (coordinate independent)
         double q2 = 0.0, qs = 0.0;
@@ -819,7 +839,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     // arena layout
     int tot_n = 0, tot_excl = 0, tot_D = 0, tot_cx = 0, tot_tab = 0, tot_cxidx = 0, tot_org = 0;
     int tot_expair = 0;
-    long long tot_exitem = 0, tot_xcpair = 0, tot_xcitem = 0;
+    long long tot_exitem = 0, tot_xcpair = 0;
     for (auto& s : h->sys) {
         tot_n += s.n;
         tot_excl += (int)s.excl_idx.size();
@@ -830,7 +850,6 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
         tot_expair += (int)s.ex_pair.size();
         tot_exitem += (long long)s.ex_pair.size() * s.replicas;
         tot_xcpair += (long long)s.xc_pair.size();
-        tot_xcitem += (long long)s.xc_pair.size() * s.replicas;
     }
     // the displacement map may change later: reserve the worst case (every particle displaced)
     tot_D = std::max(tot_D, tot_n);
@@ -851,13 +870,23 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_exp = ar.take<int2>(std::max(tot_expair, 1)), o_exq = ar.take<double4>(std::max(tot_expair, 1));
     const size_t o_exe = ar.take<double>(std::max(tot_exitem, 1LL)), o_exu = ar.take<double>(std::max(tot_exitem, 1LL));
     const size_t o_xcp = ar.take<int2>(std::max(tot_xcpair, 1LL)), o_xcq = ar.take<float>(std::max(tot_xcpair, 1LL));
-    const size_t o_xce = ar.take<double>(std::max(tot_xcitem, 1LL)), o_xcu = ar.take<double>(std::max(tot_xcitem, 1LL));
+    int max_xc = 0;
+    for (auto& s : h->sys) max_xc = std::max(max_xc, (int)s.xc_pair.size());
+    const int xc_blocks = std::max(1, (max_xc + 255) / 256);
+    const size_t o_xce = ar.take<double>((size_t)nrep * xc_blocks), o_xcu = ar.take<double>((size_t)nrep * xc_blocks);
     long long tot_theta = 0;
     for (auto& s : h->sys) tot_theta += (long long)s.theta.size();
     const int conv_blocks = 64;
     const size_t o_pacc = ar.take<unsigned long long>(std::max(pg, 1LL)), o_pgrid = ar.take<float>(std::max(pg, 1LL));
     const size_t o_pspec = ar.take<float2>(std::max(ps, 1LL)), o_pth = ar.take<float>(std::max(tot_theta, 1LL));
     const size_t o_pep = ar.take<double>((size_t)nrep * conv_blocks), o_pdu = ar.take<double>(std::max(Pp / 2, 1LL));
+    int max_bricks = 1, pme_smem = 0;
+    for (auto& s : h->sys)
+        if (s.dev.pme) {
+            max_bricks = std::max(max_bricks, s.dev.pme_nb[0] * s.dev.pme_nb[1] * s.dev.pme_nb[2]);
+            pme_smem = std::max(pme_smem, s.dev.pme_cap * 8);
+        }
+    const size_t o_pbr = ar.take<int4>(2 * (size_t)nrep * max_bricks);
     const size_t o_eoff = ar.take<int>(tot_n + 1), o_eidx = ar.take<int>(std::max(tot_excl, 1));
     const size_t o_D = ar.take<int>(std::max(tot_D, 1)), o_cxo = ar.take<int>(tot_cx + 1);
     const size_t o_cxi = ar.take<int>(tot_cxidx), o_tab = ar.take<float>(tot_tab);
@@ -915,6 +944,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.xc_qq = at<float>(B, o_xcq);
     a.xc_e0 = at<double>(B, o_xce);
     a.xc_du = at<double>(B, o_xcu);
+    a.xc_blocks = xc_blocks;
     a.topo_d = at<double>(B, o_d);
     a.excl_off = at<int>(B, o_eoff);
     a.excl_idx = at<int>(B, o_eidx);
@@ -981,7 +1011,12 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.pme_du = at<double>(B, o_pdu);
     a.pme_total_grid = pg;
     a.pme_conv_blocks = conv_blocks;
+    a.pme_brick = at<int4>(B, o_pbr);
+    a.pme_max_bricks = max_bricks;
+    a.pme_smem = pme_smem;
     if (h->pme) {   // cuFFT plans: per system, two grids (state 0, dQ) per replica
+        ce = sdm_pme_prepare(pme_smem);
+        if (ce != cudaSuccess) { cuda_fail(h, ce, "PME kernel setup"); return bail(SDM_ERR_CUDA); }
         for (int s = 0; s < num_systems; ++s) {
             int n[3] = {h->sys[s].dev.pme_grid[0], h->sys[s].dev.pme_grid[1], h->sys[s].dev.pme_grid[2]};
             cufftHandle p1 = 0, p2 = 0;

@@ -1753,15 +1753,6 @@ __global__ void k_except(SdmArgs a) {
 // ------------------------------------------------------------------------- //
 // PME: excluded pairs leave the reciprocal sum (-K qq erf(beta r)/r)          //
 // ------------------------------------------------------------------------- //
-__device__ __forceinline__ int rep_by_xc(const SdmRep* rep, int nrep, int gi) {
-    int lo = 0, hi = nrep - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (rep[mid].xc_win <= gi) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
 // minimum-image separation in FP64 (the pair term itself is FP32)
 __device__ __forceinline__ void xc_delta(const SdmSys& S, const double* xi, const double* xj, const double* di,
                                          const double* dj, bool state2, float d[3]) {
@@ -1782,13 +1773,12 @@ __device__ __forceinline__ void xc_terms(const SdmSys& S, float qq, const float 
     fs = qq * (S.c2_f * __expf(-xb * xb) - ef * ir) * ir * ir;   // force on j = fs * d
 }
 
-__global__ void k_excl_corr(SdmArgs a) {
-    const int item = blockIdx.x * blockDim.x + threadIdx.x;
-    if (item >= a.total_xc) return;
-    const int r = rep_by_xc(a.rep, a.nrep, item);
-    const SdmRep& R = a.rep[r];
-    const SdmSys& S = a.sys[R.sys];
-    const int e = item - R.xc_win;
+__device__ double block_sum(double v, double* red);
+
+// one block: 256 excluded pairs of replica blockIdx.y; the block's energy at
+// x and its change at x + d go out as two partial sums (fixed-shape tree)
+__device__ __forceinline__ void excl_corr_pair(const SdmArgs& a, const SdmRep& R, const SdmSys& S, int e,
+                                               double& e0sum, double& dusum) {
     const int2 pr = a.xc_pair[S.xc_base + e];
     const float qq = a.xc_qq[S.xc_base + e];
     const double* xi = a.x + 3 * (R.x_off + pr.x);
@@ -1820,8 +1810,24 @@ __global__ void k_excl_corr(SdmArgs a) {
             red_fix(dF[k] + si, -g, a.status);
         }
     }
-    a.xc_e0[item] = (double)e0;
-    a.xc_du[item] = du;
+    e0sum = (double)e0;
+    dusum = du;
+}
+
+__global__ void __launch_bounds__(256) k_excl_corr(SdmArgs a) {
+    __shared__ double red[256];
+    const int r = blockIdx.y;
+    const SdmRep& R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double e0 = 0.0, du = 0.0;
+    if (e < S.xc_count) excl_corr_pair(a, R, S, e, e0, du);
+    e0 = block_sum(e0, red);
+    du = block_sum(du, red);
+    if (threadIdx.x == 0) {
+        a.xc_e0[(size_t)r * gridDim.x + blockIdx.x] = e0;
+        a.xc_du[(size_t)r * gridDim.x + blockIdx.x] = du;
+    }
 }
 
 __device__ double block_sum(double v, double* red) {
@@ -1863,7 +1869,8 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     const double* ep = a.e_part + (size_t)R.cl_win * a.split;
     for (int k = threadIdx.x; k < ncl * a.split; k += blockDim.x) e0 += ep[k];
     for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) e0 += a.ex_e0[R.ex_win + k];
-    for (int k = threadIdx.x; k < S.xc_count; k += blockDim.x) e0 += a.xc_e0[R.xc_win + k];
+    if (a.total_xc)
+        for (int k = threadIdx.x; k < a.xc_blocks; k += blockDim.x) e0 += a.xc_e0[(size_t)r * a.xc_blocks + k];
     if (S.pme)
         for (int k = threadIdx.x; k < a.pme_conv_blocks; k += blockDim.x) e0 += a.pme_epart[(size_t)r * a.pme_conv_blocks + k];
     const double U0 = block_sum(e0, red) + S.e_const;
@@ -1871,7 +1878,8 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     for (int k = threadIdx.x; k < 2 * S.nD * SDM_PERT_PARTS; k += blockDim.x)
         eu += a.p_part[(size_t)R.pert_win * SDM_PERT_PARTS + k];
     for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) eu += a.ex_du[R.ex_win + k];
-    for (int k = threadIdx.x; k < S.xc_count; k += blockDim.x) eu += a.xc_du[R.xc_win + k];
+    if (a.total_xc)
+        for (int k = threadIdx.x; k < a.xc_blocks; k += blockDim.x) eu += a.xc_du[(size_t)r * a.xc_blocks + k];
     if (S.pme)
         for (int k = threadIdx.x; k < S.nD; k += blockDim.x) eu += a.pme_du[R.pert_win / 2 + k];
     const double u = block_sum(eu, red);
@@ -2191,7 +2199,7 @@ cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st) {
 
 cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st) {
     if (a.total_ex) k_except<<<(a.total_ex + 127) / 128, 128, 0, st>>>(a);
-    if (a.total_xc) k_excl_corr<<<(a.total_xc + 127) / 128, 128, 0, st>>>(a);
+    if (a.total_xc) k_excl_corr<<<dim3(a.xc_blocks, a.nrep), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

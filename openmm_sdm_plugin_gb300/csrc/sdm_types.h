@@ -89,6 +89,10 @@ struct SdmSys {
     int xc_base, xc_count;    // excluded-pair corrections: offset into xc_pair/xc_qq, count
     int pme_grid[3];
     int pme_base;             // offset of this system's B-spline moduli * Ewald kernel in pme_bc
+    float pme_gs[3];          // K / L: grid points per nm (FP32 stencils)
+    int pme_bc[3];            // cells per side of a spreading / interpolation brick
+    int pme_nb[3];            // bricks per dimension
+    int pme_cap;              // grid points of a brick's shared-memory sub-grid
 };
 
 // per perturbation item (replica, displaced particle, state): the wrapped
@@ -191,8 +195,9 @@ struct SdmArgs {
     double* p_part;      // perturbation partials
     double* ex_e0;       // per exception item: energy at x
     double* ex_du;       // per exception item: E(x+d) - E(x) (0 when d_i = d_j)
-    double* xc_e0;       // per excluded-pair item (PME): -K qq erf(beta r)/r at x
-    double* xc_du;       // ... and its change at x+d
+    double* xc_e0;       // per replica x xc block (PME): sums of -K qq erf(beta r)/r at x
+    double* xc_du;       // ... and of its change at x+d
+    int xc_blocks;       // blocks of 256 excluded pairs per replica (largest system)
     // PME reciprocal space
     const float* pme_charge;        // q sqrt(K) per particle (the topology charges)
     unsigned long long* pme_acc;    // fixed-point spread grids (2 per replica)
@@ -203,6 +208,9 @@ struct SdmArgs {
     double* pme_du;                 // per displaced particle: reciprocal part of u
     long long pme_total_grid;       // grid points over all grids
     int pme_conv_blocks;
+    int4* pme_brick;                // per replica x brick: {sub-grid origin, state}, {extents, 0}
+    int pme_max_bricks;             // bricks per replica (largest system)
+    int pme_smem;                   // dynamic shared memory of the brick kernels (bytes)
     SdmPertPos* pert_pos; // per perturbation item (total_pert entries)
     double* adj;         // adjoint sums: 3 per perturbation item
     int* ncl;            // clusters per replica
