@@ -1753,14 +1753,16 @@ __global__ void k_except(SdmArgs a) {
 // ------------------------------------------------------------------------- //
 // PME: excluded pairs leave the reciprocal sum (-K qq erf(beta r)/r)          //
 // ------------------------------------------------------------------------- //
-// minimum-image separation in FP64 (the pair term itself is FP32)
-__device__ __forceinline__ void xc_delta(const SdmSys& S, const double* xi, const double* xj, const double* di,
-                                         const double* dj, bool state2, float d[3]) {
+// minimum-image separation from the wrapped coordinates: one FP64
+// difference per component (|v| < L) rounded to FP32, plus dd (the FP32
+// difference of the two displacements, 0 in state 1), wrapped in FP32 (the
+// pair term itself is FP32; FP64 runs at 1/64 of the FP32 rate here)
+__device__ __forceinline__ void xc_delta(const SdmSys& S, const double* wi, const double* wj, const float dd[3],
+                                         float d[3]) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        double v = state2 ? __dsub_rn(__dadd_rn(xj[k], dj[k]), __dadd_rn(xi[k], di[k])) : __dsub_rn(xj[k], xi[k]);
-        v = __fma_rn(-S.box[k], rint(__dmul_rn(v, S.invL[k])), v);
-        d[k] = __double2float_rn(v);
+        const float v = __double2float_rn(__dsub_rn(wj[k], wi[k]));
+        d[k] = img32(__fadd_rn(v, dd[k]), S.Lf[k], S.invLf[k]);
     }
 }
 
@@ -1781,14 +1783,13 @@ __device__ __forceinline__ void excl_corr_pair(const SdmArgs& a, const SdmRep& R
                                                double& e0sum, double& dusum) {
     const int2 pr = a.xc_pair[S.xc_base + e];
     const float qq = a.xc_qq[S.xc_base + e];
-    const double* xi = a.x + 3 * (R.x_off + pr.x);
-    const double* xj = a.x + 3 * (R.x_off + pr.y);
-    const double* di = a.topo_d + 3 * (size_t)(S.atom_base + pr.x);
-    const double* dj = a.topo_d + 3 * (size_t)(S.atom_base + pr.y);
+    const double* wi = a.w + 3 * (size_t)(R.atom_win + pr.x);
+    const double* wj = a.w + 3 * (size_t)(R.atom_win + pr.y);
     const size_t si = (size_t)R.slot_win + a.inv[R.atom_win + pr.x];
     const size_t sj = (size_t)R.slot_win + a.inv[R.atom_win + pr.y];
     float d0[3], e0, f0;
-    xc_delta(S, xi, xj, di, dj, false, d0);
+    const float zero[3] = {0.0f, 0.0f, 0.0f};
+    xc_delta(S, wi, wj, zero, d0);
     xc_terms(S, qq, d0, e0, f0);
     unsigned long long* F0[3] = {a.F0x, a.F0y, a.F0z};
 #pragma unroll
@@ -1797,9 +1798,14 @@ __device__ __forceinline__ void excl_corr_pair(const SdmArgs& a, const SdmRep& R
         red_fix(F0[k] + si, -f0 * d0[k], a.status);
     }
     double du = 0.0;
-    if (di[0] != dj[0] || di[1] != dj[1] || di[2] != dj[2]) {
+    // distinct displacement groups <=> distinct displacement vectors
+    if (a.topo_grp[S.atom_base + pr.x] != a.topo_grp[S.atom_base + pr.y]) {
+        const double* di = a.topo_d + 3 * (size_t)(S.atom_base + pr.x);
+        const double* dj = a.topo_d + 3 * (size_t)(S.atom_base + pr.y);
+        const float dd[3] = {__double2float_rn(__dsub_rn(dj[0], di[0])), __double2float_rn(__dsub_rn(dj[1], di[1])),
+                             __double2float_rn(__dsub_rn(dj[2], di[2]))};
         float d1[3], e1, f1;
-        xc_delta(S, xi, xj, di, dj, true, d1);
+        xc_delta(S, wi, wj, dd, d1);
         xc_terms(S, qq, d1, e1, f1);
         du = (double)e1 - (double)e0;
         unsigned long long* dF[3] = {a.dFx, a.dFy, a.dFz};
