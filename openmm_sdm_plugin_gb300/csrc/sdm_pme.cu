@@ -76,6 +76,25 @@ __device__ __forceinline__ void bspline5(float w, float M[kOrder], float dM[kOrd
     for (int j = 0; j < kOrder; ++j) M[j] = P[j];
 }
 
+// element j of a 5-element register array, j warp-divergent (select chain,
+// no local memory)
+__device__ __forceinline__ float pick5(const float v[kOrder], int j) {
+    float r = v[0];
+#pragma unroll
+    for (int k = 1; k < kOrder; ++k) r = (j == k) ? v[k] : r;
+    return r;
+}
+
+// v 2^40 (the grid's fixed point) as hi 2^20 + lo: hi = floor(v 2^20), lo =
+// round(frac 2^20) in [0, 2^20].  Exact: v 2^20, its floor and its fraction
+// are exact in FP32, and hi 2^20 + lo = round(v 2^40) (|v| < 2^11)
+__device__ __forceinline__ void grid_split(float v, int& hi, int& lo) {
+    const float s = v * 1048576.0f;
+    const float f = floorf(s);
+    hi = (int)f;
+    lo = __float2int_rn((s - f) * 1048576.0f);
+}
+
 // scaled coordinate u = v K / L in FP32 (v already wrapped into [0, L): u in
 // [0, K]; placement error ~K 2^-24 grid spacings)
 struct Stencil {
@@ -164,11 +183,11 @@ __device__ void interp(const float* phi, const SdmSys& S, const Stencil& st, flo
 // E = max(ub) - lo + 1 per dimension, points indexed ((i0 E1) + i1) E2 + i2.
 constexpr int kBrickThreads = 256;
 constexpr int kMaxBrickCols = 25;   // bc <= 5
-// shared-memory accumulation: a grid contribution v (fixed point 2^40) goes
-// into two 32-bit sums, v >> kLoBits and the low kLoBits bits
+// shared-memory accumulation: a grid contribution (fixed point 2^40) goes
+// into two 32-bit sums, its high part (units of 2^kLoBits) and its low part
+// in [0, 2^kLoBits] (grid_split)
 constexpr int kLoBits = 20;
-constexpr long long kLoMask = (1ll << kLoBits) - 1;
-constexpr int kBrickMaxCharged = 2047;      // low-word sums < 2^31
+constexpr int kBrickMaxCharged = 2047;      // low-word sums <= 2047 2^20 < 2^31
 constexpr float kBrickMaxValue = 2000.0f;   // high-word sums < 2^31 (values < 2^(51-40))
 
 struct BrickCols {
@@ -304,9 +323,10 @@ __global__ void __launch_bounds__(kBrickThreads) k_pme_spread(SdmArgs a) {
                 int* row = sg + (i0 * E1 + (st.ub[1] - y - L1)) * E2 + (st.ub[2] - L2);
 #pragma unroll
                 for (int z = 0; z < kOrder; ++z) {
-                    const long long v = (long long)grid_fix(qab * st.M[2][z]);
-                    atomicAdd(row - z, (int)(v >> kLoBits));
-                    atomicAdd(row - z + npts, (int)(v & kLoMask));
+                    int hi, lo;
+                    grid_split(qab * st.M[2][z], hi, lo);
+                    atomicAdd(row - z, hi);
+                    atomicAdd(row - z + npts, lo);
                 }
             }
         }
@@ -314,6 +334,7 @@ __global__ void __launch_bounds__(kBrickThreads) k_pme_spread(SdmArgs a) {
     if (!fits) return;
     __syncthreads();
     const int K0 = S.pme_grid[0], K1 = S.pme_grid[1], K2 = S.pme_grid[2];
+#pragma unroll 4
     for (int q = t; q < npts; q += kBrickThreads) {
         const unsigned long long v = (unsigned long long)(((long long)sg[q] << kLoBits) + (long long)sg[npts + q]);
         if (v == 0ull) continue;
@@ -455,6 +476,7 @@ __global__ void __launch_bounds__(kBrickThreads, 3) k_pme_gather(SdmArgs a) {
     brick_columns(a, R, S, c0, c1, bc);
     if (fits) {
         const int npts = e.x * e.y * e.z;
+#pragma unroll 4
         for (int q = t; q < npts; q += kBrickThreads) {
             const int i2 = q % e.z, i01 = q / e.z;
             const int i1 = i01 % e.y, i0 = i01 / e.y;
@@ -491,15 +513,6 @@ __global__ void __launch_bounds__(kBrickThreads, 3) k_pme_gather(SdmArgs a) {
             for (int k = 0; k < 3; ++k) pme_red(dF[k] + gsl, -q * sc[k] * g[1][k], a.status);
         }
     }
-}
-
-// element j of a 5-element register array, j warp-divergent (select chain,
-// no local memory)
-__device__ __forceinline__ float pick5(const float v[kOrder], int j) {
-    float r = v[0];
-#pragma unroll
-    for (int k = 1; k < kOrder; ++k) r = (j == k) ? v[k] : r;
-    return r;
 }
 
 // one stencil row (a, b) of the interpolation: value and gradient parts of

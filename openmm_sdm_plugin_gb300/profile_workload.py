@@ -1,15 +1,17 @@
 """Runs a fixed synthetic SDM workload a few times (for profilers).
 
-  python -m openmm_sdm_plugin_gb300.profile_workload [--replicas 22] [--calls 3] [--eager]
+  python -m openmm_sdm_plugin_gb300.profile_workload [--replicas 22] [--calls 3] [--eager] [--pme]
 
 The workload is the batched relative-binding system used by the benchmark:
 `--replicas` copies of the 22,580-particle system with independent seeded
 coordinates.  Each call is one evaluation of all replicas (device buffers).
+`--pme` evaluates the same systems with PME electrostatics (tolerance 5e-4).
 """
 from __future__ import annotations
 
 import argparse
 import ctypes as C
+import dataclasses
 
 import numpy as np
 
@@ -23,10 +25,13 @@ def main():
     ap.add_argument("--calls", type=int, default=3)
     ap.add_argument("--eager", action="store_true", help="no CUDA graph")
     ap.add_argument("--config", default="config2", choices=["config2", "config0"])
+    ap.add_argument("--pme", action="store_true", help="PME electrostatics instead of reaction field")
     a = ap.parse_args()
     _build.build()
     import torch
     s = systems.config2(a.replicas) if a.config == "config2" else systems.config0(variant="b")
+    if a.pme:
+        s = dataclasses.replace(s, nonbonded_method="pme", ewald_tolerance=5e-4)
     h = capi.Handle([s])
     for r in range(h.nrep):
         h.set_params(r, s.params[r].as_array())
