@@ -24,7 +24,7 @@ def _pme(s):
 
 def _oracle_states(s, x):
     beta = oracle.ewald_beta(s.cutoff, TOL)
-    K = oracle.pme_grid_size(beta, s.box, TOL)
+    K = list(s.pme_grid) if s.pme_grid is not None else oracle.pme_grid_size(beta, s.box, TOL)
     lj = oracle.OracleSystem(dataclasses.replace(s, charge=np.zeros(s.n))).states(x)
 
     def coul(y):
@@ -81,6 +81,20 @@ def test_pme_batched_replicas_and_graph_replay():
     torch.cuda.synchronize()
     assert np.array_equal(rd.cpu().numpy()[:, :14], res[:, :14])
     assert np.array_equal(fd.cpu().numpy(), F)
+
+
+def test_pme_fine_grid_global_memory_path():
+    """A 160^3 grid on the 930-site box (one-cell bricks, sub-grids up to the
+    27,648-point shared-memory cap): one brick's stencils span more points
+    than the cap, so that brick spreads and interpolates through global
+    memory while the others use their sub-grids; both in one evaluation."""
+    s = dataclasses.replace(_pme(S.config0(variant="b")), pme_grid=(160, 160, 160))
+    h = capi.Handle([s])
+    h.set_params(0, s.params[0].as_array())
+    x = s.positions[0]
+    res, F = h.evaluate(x)
+    F0, F1 = h.state_forces()
+    _check(res[0], F, F0, F1, _oracle_states(s, x))
 
 
 def test_pme_rejects_mixed_methods_and_adjoint():
