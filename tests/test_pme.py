@@ -97,6 +97,43 @@ def test_pme_fine_grid_global_memory_path():
     _check(res[0], F, F0, F1, _oracle_states(s, x))
 
 
+def test_pme_uneven_systems_in_one_handle():
+    """Two different PME systems (own grids, own batched cuFFT plans) and
+    their replicas in one call."""
+    a = _pme(S.config0(variant="b"))
+    b = _pme(S.host_guest(1500, seed=7, nstates=2))
+    h = capi.Handle([a, b])
+    reps = [(a, 0), (b, 0), (b, 1)]
+    for r, (s, k) in enumerate(reps):
+        h.set_params(r, s.params[k].as_array())
+    x = np.concatenate([a.positions[0], b.positions[0], b.positions[1]])
+    res, F = h.evaluate(x)
+    F0, F1 = h.state_forces()
+    off = 0
+    for r, (s, k) in enumerate(reps):
+        sl = slice(off, off + s.n)
+        _check(res[r], F[sl], F0[sl], F1[sl], _oracle_states(s, s.positions[k]))
+        off += s.n
+
+
+def test_pme_net_charge_and_no_displacement():
+    """A charged system (neutralising-background term) with no displaced
+    particle: u = 0 and F1 = F0 exactly, U0 against the oracle."""
+    s0 = S.config0(variant="b")
+    q = s0.charge.copy()
+    q[np.nonzero(q)[0][:5]] += 0.2          # net charge +1
+    s = _pme(dataclasses.replace(s0, charge=q, displacement=np.zeros_like(s0.displacement)))
+    assert abs(s.charge.sum() - 1.0) < 1e-9
+    h = capi.Handle([s])
+    h.set_params(0, s.params[0].as_array())
+    x = s.positions[0]
+    res, F = h.evaluate(x)
+    F0, F1 = h.state_forces()
+    assert res[0, capi.R_U] == 0.0
+    assert np.array_equal(F0, F1)
+    _check(res[0], F, F0, F1, _oracle_states(s, x))
+
+
 def test_pme_rejects_mixed_methods_and_adjoint():
     s = S.config0(variant="b")
     with pytest.raises(capi.SdmError):
