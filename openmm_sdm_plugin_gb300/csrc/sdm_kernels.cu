@@ -480,7 +480,15 @@ __global__ void k_clusters(SdmArgs a) {
                                              : make_int4(link[0], link[1], link[2], link[3]);
             a.cl_link[2 * (size_t)cw + 1] = many ? make_int4(-2, -2, -2, -2)
                                                  : make_int4(link[4], link[5], link[6], link[7]);
-            atomicMax(&a.extz[r], __float_as_uint(fmaxf(hi[2], 0.0f)));
+        }
+        // the replica's largest cluster z extent: one atomic per replica present
+        // in the warp (same-address atomics serialise in L2: one per cluster
+        // cost ~30 us per call on the 22-replica batch)
+        {
+            const unsigned act = __activemask();   // the 8-lane groups of valid clusters
+            const unsigned same = __match_any_sync(act, r);
+            const unsigned zmax = __reduce_max_sync(same, __float_as_uint(fmaxf(hi[2], 0.0f)));
+            if (lane == __ffs(same) - 1) atomicMax(&a.extz[r], zmax);
         }
     }
 }
@@ -1912,14 +1920,21 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     double fp;
     const double be = softcore(u, (int)p[SDM_P_SOFTCORE_METHOD], p[SDM_P_UMAX], p[SDM_P_ACORE],
                                p[SDM_P_UBCORE], &fp);
+    // e^(-alpha (u' - u0)) and log(1 + e^...), shared by the integrated-logistic
+    // bias and dW/dlambda (one thread: the FP64 transcendentals are serial)
+    double ex = 0.0, ee = 1.0, lee = 0.0;
+    if (method == SDM_ILOGISTIC || noneq == 1) {
+        ex = exp(-alpha * (be - u0));
+        ee = 1.0 + ex;
+        lee = log(ee);
+    }
     double ebias, bfp;
     if (method == SDM_QUADRATIC) {
         ebias = 0.5 * gamma * be * be + wb * be + w0;
         bfp = gamma * be + wb;
     } else if (method == SDM_ILOGISTIC) {
-        const double ee = 1.0 + exp(-alpha * (be - u0));
         ebias = 0.0;
-        if (alpha > 0) ebias = ((l2 - l1) / alpha) * log(ee);
+        if (alpha > 0) ebias = ((l2 - l1) / alpha) * lee;
         ebias += l2 * be + w0;
         bfp = (l2 - l1) / ee + l1;
     } else {
@@ -1928,9 +1943,8 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     }
     double dwdl = 0.0;
     if (noneq == 1) {
-        const double ee = 1.0 + exp(-alpha * (be - u0));
-        dwdl = (-log(ee) / alpha) * p[SDM_P_M_LAMBDA1] + (be + log(ee) / alpha) * p[SDM_P_M_LAMBDA2] +
-               ((l2 - l1) * exp(-alpha * (be - u0)) / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
+        dwdl = (-lee / alpha) * p[SDM_P_M_LAMBDA1] + (be + lee / alpha) * p[SDM_P_M_LAMBDA2] +
+               ((l2 - l1) * ex / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
     }
     int st = *(volatile int*)a.status;
     if (!isfinite(U0) || !isfinite(u)) { st |= SDM_DEV_ENERGY_NONFINITE; atomicOr(a.status, SDM_DEV_ENERGY_NONFINITE); }
