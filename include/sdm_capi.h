@@ -356,9 +356,11 @@ enum {
     SDM_DEV_FORCE_OVERFLOW = 1,   /* |force term| >= 2^31 kJ/mol/nm or NaN */
     SDM_DEV_ENERGY_NONFINITE = 2, /* NaN/Inf energy */
     SDM_DEV_EXCL_OVERFLOW = 4,    /* internal exclusion table overflow (should not happen) */
-    SDM_DEV_LIST_OVERFLOW = 8     /* a cluster-pair list exceeded its capacity; sdm_evaluate
+    SDM_DEV_LIST_OVERFLOW = 8,    /* a cluster-pair list exceeded its capacity; sdm_evaluate
                                      regrows and repeats, device callers see SDM_ERR_CAPACITY
                                      from sdm_check_status and call sdm_evaluate once */
+    SDM_DEV_COORD_NONFINITE = 16  /* a coordinate is NaN or Inf (OpenMM raises for these; the
+                                     particle drops out of the pair search, results are invalid) */
 };
 
 #ifdef __cplusplus

@@ -25,6 +25,9 @@ SDM_ERR_CAPACITY = 5
 SDM_ERR_UNKNOWN_METHOD = 6
 SDM_ERR_TIMEOUT = 7
 
+# device status bits (sdm_check_status, results[:, R_STATUS])
+DEV_FORCE_OVERFLOW, DEV_ENERGY_NONFINITE, DEV_EXCL_OVERFLOW, DEV_LIST_OVERFLOW, DEV_COORD_NONFINITE = 1, 2, 4, 8, 16
+
 NPARAMS = 22
 NRESULTS = 16
 RESULT_FIELDS = ("U0", "U1", "u", "BindE", "fp", "W", "dW", "s", "E_pot", "dWdlambda",

@@ -1154,7 +1154,7 @@ sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double*
     if (h->opt_verify && v) {
         SDM_CUDA(h, cudaMemset(h->args.status, 0, sizeof(int)));
         return fail(h, SDM_ERR_OVERFLOW, "device status " + std::to_string(v) +
-                                             ": force overflow or non-finite energy");
+                                             ": force overflow, non-finite energy or non-finite coordinates");
     }
     return SDM_OK;
 }

@@ -190,7 +190,12 @@ __global__ void k_cells(SdmArgs a) {
             // the identity; only other coordinates take the FP64 wrap
             double w = xp[k];
             const long long b = __double_as_longlong(w);
-            if (!(b >= 0 && b < S.wrap_lim[k])) w = wrap1(w, S.box[k], S.invL[k]);
+            if (!(b >= 0 && b < S.wrap_lim[k])) {
+                // NaN / Inf (exponent all ones): reported; the particle lands in
+                // a clamped cell and fails every distance test
+                if (((b >> 52) & 0x7ff) == 0x7ff) atomicOr(a.status, SDM_DEV_COORD_NONFINITE);
+                w = wrap1(w, S.box[k], S.invL[k]);
+            }
             a.w[3 * (size_t)gi + k] = w;
             c[k] = cell_of(w, S.invg[k], S.M[k]);
         }

@@ -71,6 +71,27 @@ def test_config0_parity():
     assert res[0, capi.R_STATUS] == 0
 
 
+def test_nonfinite_coordinates_are_reported():
+    """A NaN or Inf coordinate sets SDM_DEV_COORD_NONFINITE: the host call
+    fails with SDM_ERR_OVERFLOW, the device status carries the bit, and the
+    next call on finite coordinates is clean."""
+    s = S.config0(variant="b")
+    h = _handle([s])
+    for bad in (np.nan, np.inf, -np.inf):
+        x = s.positions[0].copy()
+        x[17, 1] = bad
+        with pytest.raises(capi.SdmError) as e:
+            h.evaluate(x)
+        assert e.value.status == capi.SDM_ERR_OVERFLOW
+        h.set_option(capi.OPT_VERIFY, 0)
+        res, _ = h.evaluate(x)
+        h.set_option(capi.OPT_VERIFY, 1)
+        assert int(res[0, capi.R_STATUS]) & capi.DEV_COORD_NONFINITE
+        assert h.check_status() & capi.DEV_COORD_NONFINITE
+    res, F = h.evaluate(s.positions[0])
+    assert res[0, capi.R_STATUS] == 0 and np.isfinite(F).all()
+
+
 def test_config0a_clash_overflow_is_reported():
     """Config 0a displaces the ligand into solvent: state-2 forces reach
     ~5.6e9 kJ/mol/nm, beyond the 2^31 range of the 2^32-scaled fixed point.
