@@ -236,6 +236,65 @@ sdm_status sdm_set_langevin(sdm_handle* h, const sdm_langevin_params* params, un
 sdm_status sdm_langevin_step(sdm_handle* h, double* x, double* v, const double* inv_mass,
                              const double* f_extra, double* results, int nsteps, void* stream);
 
+/* ------------------------------------------------------------------------ *
+ * Group-1 restraints of the reference's SDMUtils (python/SDMUtils.py), as
+ * the reference builds them for LangevinIntegratorSDM's group 1: evaluated
+ * on the device in the same call, on the caller's coordinates x (no
+ * periodic images, like the reference's custom forces).  Units: nm, rad,
+ * kJ/mol.  Energies enter SDM_R_EPOT (and sdm_get_restraint_energies);
+ * forces enter F, and the state forces F0 and F1 alike (they do not depend
+ * on the SDM state).
+ *
+ * Centroid restraint (SDMUtils.py:32-157, CustomCentroidBondForce):
+ *   lambda_r (kfcm/2) step(d - tolcm) (d - tolcm)^2,
+ *   d = |c_lig - offset - c_rcpt|, c = sum w_i x_i / sum w_i (the reference
+ *   weights by particle mass: pass the masses as weights; NULL = 1).
+ * With use_angles, three flat-bottom terms over the reference particles
+ * r0 r1 r2 (receptor) and l0 l1 l2 (ligand), each
+ *   lambda_r (kf/2) (step(dm) max(0, db)^2 + step(-dm) max(0, -da)^2),
+ *   da, db, dm = the variable minus lo, hi, (lo + hi)/2 wrapped to (-P/2, P/2]:
+ *   theta = angle(r0, l0, l1) (P = pi), phi1 = dihedral(r1, r0, l0, l1),
+ *   phi2 = dihedral(r0, l0, l1, l2) (P = 2 pi); lo/hi = center -/+ tolerance.
+ * lambda_r is SDMRestraintControlParameter (per replica, default 1).
+ *
+ * Alignment restraint (SDMUtils.py:160-257, CustomCompoundBondForce) between
+ * reference particles a0 a1 a2 (ligand A) and b0 b1 b2 (ligand B):
+ *   (kf_displ/2) |b0 - offset - a0|^2
+ *   + (k_theta/2) (1 - cos theta), theta between b1 - b0 and a1 - a0
+ *   + (k_psi/4) (1 - cos psi_b) + (k_psi/4) (1 - cos psi_a), psi_b between the
+ *     components of b2 - b0 and a2 - a0 orthogonal to b1 - b0, psi_a the same
+ *     with A and B exchanged.
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    int num_lig, num_rcpt;          /* centroid groups (either 0: no centroid restraint) */
+    const int* lig_particles;       /* [num_lig] */
+    const int* rcpt_particles;      /* [num_rcpt] */
+    const double* lig_weights;      /* [num_lig] or NULL (all 1) */
+    const double* rcpt_weights;     /* [num_rcpt] or NULL (all 1) */
+    double kfcm, tolcm;             /* kJ/mol/nm^2, nm */
+    double offset[3];               /* nm */
+    int use_angles;                 /* 1: the angle / dihedral terms */
+    int rcpt_ref[3], lig_ref[3];    /* r0 r1 r2, l0 l1 l2 */
+    double kf_angle, angle_center, angle_tol;          /* kJ/mol/rad^2, rad, rad */
+    double kf_dihedral1, dihedral1_center, dihedral1_tol;
+    double kf_dihedral2, dihedral2_center, dihedral2_tol;
+    int use_alignment;              /* 1: the alignment restraint */
+    int liga_ref[3], ligb_ref[3];   /* a0 a1 a2, b0 b1 b2 */
+    double kf_displ, k_theta, k_psi;                   /* kJ/mol/nm^2, kJ/mol, kJ/mol */
+    double align_offset[3];         /* nm */
+} sdm_restraints;
+
+/* Restraints of system `system` (NULL removes them); applies to every
+ * replica of the system from the next evaluation.  Reference:
+ * SDMUtils.addRestraintForce / addAlignmentForce. */
+sdm_status sdm_set_restraints(sdm_handle* h, int system, const sdm_restraints* r);
+/* SDMRestraintControlParameter of one replica (reference: the global
+ * parameter SDMUtils.py:99, Context::setParameter). */
+sdm_status sdm_set_restraint_control(sdm_handle* h, int replica, double lambda_r);
+/* Restraint energy of every replica at the last evaluation ([num_replicas]).
+ * Synchronises. */
+sdm_status sdm_get_restraint_energies(sdm_handle* h, double* energies);
+
 /* Reads and clears the device status word (SDM_DEV_* bits).  Synchronises. */
 sdm_status sdm_check_status(sdm_handle* h, int* device_status);
 

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsdm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["sdm_kernels.cu", "sdm_pme.cu", "sdm_capi.cpp"]
+SOURCES = ["sdm_kernels.cu", "sdm_pme.cu", "sdm_restraints.cu", "sdm_capi.cpp"]
 HEADERS = ["sdm_types.h", os.path.join("..", "..", "include", "sdm_capi.h")]
 
 

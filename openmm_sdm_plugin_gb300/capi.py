@@ -42,7 +42,8 @@ EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_get_state_forces", "sdm_check_status", "sdm_set_option", "sdm_get_option",
             "sdm_get_kernel_times", "sdm_autotune", "sdm_count_pairs", "sdm_get_grid",
             "sdm_export_lists", "sdm_evaluate_noalloc", "sdm_set_particle_params",
-            "sdm_adjoint", "sdm_set_langevin", "sdm_langevin_step")
+            "sdm_adjoint", "sdm_set_langevin", "sdm_langevin_step", "sdm_set_restraints",
+            "sdm_set_restraint_control", "sdm_get_restraint_energies")
 
 NB_REACTION_FIELD, NB_PME = 0, 1
 NOALLOC_MAX_PARTICLES = 8192
@@ -115,6 +116,9 @@ def load_library(path: str = LIB_PATH):
         L.sdm_adjoint.argtypes = [vp, vp]
         L.sdm_set_langevin.argtypes = [vp, C.POINTER(LangevinParams), C.c_ulonglong]
         L.sdm_langevin_step.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int, vp]
+        L.sdm_set_restraints.argtypes = [vp, C.c_int, C.POINTER(RestraintDesc)]
+        L.sdm_set_restraint_control.argtypes = [vp, C.c_int, C.c_double]
+        L.sdm_get_restraint_energies.argtypes = [vp, vp]
         for name in EXPORTED:
             if name != "sdm_last_error":
                 getattr(L, name).restype = C.c_int
@@ -130,6 +134,48 @@ class LangevinParams(C.Structure):
     """``sdm_langevin_params``: step size (ps), friction (1/ps), temperature (K), seed."""
     _fields_ = [("step_size", C.c_double), ("friction", C.c_double), ("temperature", C.c_double),
                 ("seed", C.c_ulonglong)]
+
+
+class RestraintDesc(C.Structure):
+    """``sdm_restraints`` (group-1 restraints of the reference's SDMUtils)."""
+    _fields_ = [
+        ("num_lig", C.c_int), ("num_rcpt", C.c_int),
+        ("lig_particles", C.POINTER(C.c_int)), ("rcpt_particles", C.POINTER(C.c_int)),
+        ("lig_weights", C.POINTER(C.c_double)), ("rcpt_weights", C.POINTER(C.c_double)),
+        ("kfcm", C.c_double), ("tolcm", C.c_double), ("offset", C.c_double * 3),
+        ("use_angles", C.c_int), ("rcpt_ref", C.c_int * 3), ("lig_ref", C.c_int * 3),
+        ("kf_angle", C.c_double), ("angle_center", C.c_double), ("angle_tol", C.c_double),
+        ("kf_dihedral1", C.c_double), ("dihedral1_center", C.c_double), ("dihedral1_tol", C.c_double),
+        ("kf_dihedral2", C.c_double), ("dihedral2_center", C.c_double), ("dihedral2_tol", C.c_double),
+        ("use_alignment", C.c_int), ("liga_ref", C.c_int * 3), ("ligb_ref", C.c_int * 3),
+        ("kf_displ", C.c_double), ("k_theta", C.c_double), ("k_psi", C.c_double),
+        ("align_offset", C.c_double * 3),
+    ]
+
+
+def restraint_desc(rs, keep):
+    """RestraintDesc of a systems.Restraints (arrays appended to `keep`)."""
+    d = RestraintDesc()
+    lig = np.ascontiguousarray(np.asarray(rs.lig_particles, np.int32))
+    rcpt = np.ascontiguousarray(np.asarray(rs.rcpt_particles, np.int32))
+    keep += [lig, rcpt]
+    d.num_lig, d.num_rcpt = int(lig.size), int(rcpt.size)
+    d.lig_particles = lig.ctypes.data_as(C.POINTER(C.c_int)) if lig.size else None
+    d.rcpt_particles = rcpt.ctypes.data_as(C.POINTER(C.c_int)) if rcpt.size else None
+    for name, arr in (("lig_weights", rs.lig_weights), ("rcpt_weights", rs.rcpt_weights)):
+        if arr is not None:
+            w = np.ascontiguousarray(np.asarray(arr, np.float64))
+            keep.append(w)
+            setattr(d, name, w.ctypes.data_as(C.POINTER(C.c_double)))
+    for f in ("kfcm", "tolcm", "kf_angle", "angle_center", "angle_tol", "kf_dihedral1", "dihedral1_center",
+              "dihedral1_tol", "kf_dihedral2", "dihedral2_center", "dihedral2_tol", "kf_displ", "k_theta", "k_psi"):
+        setattr(d, f, float(getattr(rs, f)))
+    d.offset[:] = [float(v) for v in rs.offset]
+    d.align_offset[:] = [float(v) for v in rs.align_offset]
+    d.use_angles, d.use_alignment = int(bool(rs.use_angles)), int(bool(rs.use_alignment))
+    for f in ("rcpt_ref", "lig_ref", "liga_ref", "ligb_ref"):
+        getattr(d, f)[:] = [int(v) for v in getattr(rs, f)]
+    return d
 
 
 class Handle:
@@ -194,6 +240,24 @@ class Handle:
             self.rep_sys += [k] * r
             self.rep_n += [int(s.charge.shape[0])] * r
         self.total_particles = int(sum(self.rep_n))
+        for k, s in enumerate(self.systems):
+            if getattr(s, "restraints", None) is not None:
+                self.set_restraints(k, s.restraints)
+
+    # -- group-1 restraints ------------------------------------------------
+    def set_restraints(self, system: int, rs):
+        """Restraints (systems.Restraints or None) of one system."""
+        keep = []
+        d = restraint_desc(rs, keep) if rs is not None else None
+        self._check(self.lib.sdm_set_restraints(self.h, int(system), C.byref(d) if d is not None else None))
+
+    def set_restraint_control(self, replica: int, value: float):
+        self._check(self.lib.sdm_set_restraint_control(self.h, int(replica), float(value)))
+
+    def restraint_energies(self):
+        out = np.zeros(self.nrep)
+        self._check(self.lib.sdm_get_restraint_energies(self.h, out.ctypes.data))
+        return out
 
     # -- lifetime ---------------------------------------------------------
     def close(self):

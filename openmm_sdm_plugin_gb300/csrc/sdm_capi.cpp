@@ -33,6 +33,7 @@ cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_pme(const SdmArgs& a, const cufftHandle* r2c, const cufftHandle* c2r, const long long* grid_off,
                            const long long* spec_off, int nsys, int conv_blocks, cudaStream_t st);
 cudaError_t sdm_pme_prepare(int smem_bytes);
+cudaError_t sdm_launch_restraints(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_adjoint(const SdmArgs& a, cudaStream_t st);
@@ -62,6 +63,13 @@ struct SysHost {
     std::vector<int2> xc_pair;   // PME: excluded pairs i < j and K q_i q_j
     std::vector<float> xc_qq;
     std::vector<float> theta;    // PME: Ewald kernel x B-spline moduli, half spectrum
+    // group-1 restraints (sdm_set_restraints): particles / weights (ligand group,
+    // then receptor group), parameters (SDM_RS_*), reference particles, bits
+    std::vector<int> rs_idx;
+    std::vector<double> rs_w;
+    double rs_prm[SDM_RS_COUNT] = {};
+    int rs_ref[12] = {};
+    int rs_on = 0, rs_nlig = 0, rs_nrcpt = 0;
     bool clique = false;
     SdmSys dev;
     int replicas;
@@ -112,6 +120,7 @@ struct sdm_handle {
     // device
     char* arena = nullptr;
     size_t arena_bytes = 0;
+    void* rs_buf = nullptr;   // restraint data of every system (sdm_set_restraints)
     cudaStream_t stream = nullptr;
     SdmArgs args{};
     int* item_prefix = nullptr;
@@ -624,6 +633,7 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
     if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
     if (mode == 0) SDM_CUDA(h, sdm_launch_exceptions(a, st));
+    if (mode == 0) SDM_CUDA(h, sdm_launch_restraints(a, st));
     if (mode == 0 && h->pme)
         SDM_CUDA(h, sdm_launch_pme(a, h->pme_r2c.data(), h->pme_c2r.data(), h->pme_grid_off.data(),
                                    h->pme_spec_off.data(), (int)h->sys.size(), a.pme_conv_blocks, st));
@@ -887,6 +897,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
             pme_smem = std::max(pme_smem, s.dev.pme_cap * 8);
         }
     const size_t o_pbr = ar.take<int4>(2 * (size_t)nrep * max_bricks);
+    const size_t o_rsl = ar.take<double>(nrep), o_rse = ar.take<double>(nrep);
     const size_t o_eoff = ar.take<int>(tot_n + 1), o_eidx = ar.take<int>(std::max(tot_excl, 1));
     const size_t o_D = ar.take<int>(std::max(tot_D, 1)), o_cxo = ar.take<int>(tot_cx + 1);
     const size_t o_cxi = ar.take<int>(tot_cxidx), o_tab = ar.take<float>(tot_tab);
@@ -1012,6 +1023,14 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.pme_total_grid = pg;
     a.pme_conv_blocks = conv_blocks;
     a.pme_brick = at<int4>(B, o_pbr);
+    a.rs_lam = at<double>(B, o_rsl);
+    a.rs_e = at<double>(B, o_rse);
+    a.rs_any = 0;
+    {
+        std::vector<double> ones(nrep, 1.0);   // SDMRestraintControlParameter defaults to 1
+        ce = cudaMemcpy(const_cast<double*>(a.rs_lam), ones.data(), nrep * sizeof(double), cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) { cuda_fail(h, ce, "cudaMemcpy"); return bail(SDM_ERR_CUDA); }
+    }
     a.pme_max_bricks = max_bricks;
     a.pme_smem = pme_smem;
     if (h->pme) {   // cuFFT plans: per system, two grids (state 0, dQ) per replica
@@ -1060,6 +1079,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
 sdm_status sdm_destroy(sdm_handle* h) {
     if (!h) return SDM_OK;
     if (h->jl_buf) { cudaSetDevice(h->device); cudaFree(h->jl_buf); h->jl_buf = nullptr; }
+    if (h->rs_buf) { cudaSetDevice(h->device); cudaFree(h->rs_buf); h->rs_buf = nullptr; }
     if (h->arena) cudaSetDevice(h->device);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
@@ -1093,6 +1113,162 @@ sdm_status sdm_set_displacement(sdm_handle* h, int system, const double* displac
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
     setup_displacement(h->sys[system], displacement);
     return upload_topology(h);
+}
+
+// Restraint data of every system into one device buffer (parameters,
+// weights, particle indices) and the systems' offsets into the device SdmSys
+// array; the cached graphs hold the previous pointers and are dropped.
+static sdm_status upload_restraints(sdm_handle* h) {
+    std::vector<int> idx;
+    std::vector<double> w, prm;
+    int any = 0;
+    for (auto& s : h->sys) {
+        s.dev.rs_on = s.rs_on;
+        s.dev.rs_base = (int)idx.size();
+        s.dev.rs_nlig = s.rs_nlig;
+        s.dev.rs_nrcpt = s.rs_nrcpt;
+        s.dev.rs_prm = (int)prm.size();
+        std::copy(s.rs_ref, s.rs_ref + 12, s.dev.rs_ref);
+        idx.insert(idx.end(), s.rs_idx.begin(), s.rs_idx.end());
+        w.insert(w.end(), s.rs_w.begin(), s.rs_w.end());
+        prm.insert(prm.end(), s.rs_prm, s.rs_prm + SDM_RS_COUNT);
+        any |= s.rs_on ? 1 : 0;
+    }
+    SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    SDM_CUDA(h, cudaDeviceSynchronize());
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    if (h->rs_buf) { cudaFree(h->rs_buf); h->rs_buf = nullptr; }
+    const size_t nd = prm.size() + w.size();
+    SDM_CUDA(h, cudaMalloc(&h->rs_buf, nd * sizeof(double) + idx.size() * sizeof(int) + 16));
+    double* dp = static_cast<double*>(h->rs_buf);
+    SDM_CUDA(h, cudaMemcpy(dp, prm.data(), prm.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (!w.empty()) SDM_CUDA(h, cudaMemcpy(dp + prm.size(), w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice));
+    int* ip = reinterpret_cast<int*>(dp + nd);
+    if (!idx.empty()) SDM_CUDA(h, cudaMemcpy(ip, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice));
+    h->args.rs_prm = dp;
+    h->args.rs_w = dp + prm.size();
+    h->args.rs_idx = ip;
+    h->args.rs_any = any;
+    return upload_topology(h);
+}
+
+sdm_status sdm_set_restraints(sdm_handle* h, int system, const sdm_restraints* r) {
+    if (!h) return SDM_ERR_INVALID_ARGUMENT;
+    if (system < 0 || system >= (int)h->sys.size()) return fail(h, SDM_ERR_INVALID_ARGUMENT, "system index out of range");
+    cudaSetDevice(h->device);
+    SysHost& s = h->sys[system];
+    if (!r) {
+        s.rs_on = s.rs_nlig = s.rs_nrcpt = 0;
+        s.rs_idx.clear();
+        s.rs_w.clear();
+        return upload_restraints(h);
+    }
+    const int n = s.n;
+    auto bad = [&](const char* m) { return fail(h, SDM_ERR_INVALID_ARGUMENT, m); };
+    auto in_range = [n](int i) { return i >= 0 && i < n; };
+    auto finite = [](std::initializer_list<double> v) {
+        for (double x : v)
+            if (!std::isfinite(x)) return false;
+        return true;
+    };
+    if (r->num_lig < 0 || r->num_rcpt < 0) return bad("negative restraint group size");
+    int on = 0;
+    std::vector<int> idx;
+    std::vector<double> w;
+    double wsum[2] = {0.0, 0.0};
+    if (r->num_lig > 0 && r->num_rcpt > 0) {
+        if (!r->lig_particles || !r->rcpt_particles) return bad("restraint group particles missing");
+        for (int g = 0; g < 2; ++g) {
+            const int m = g ? r->num_rcpt : r->num_lig;
+            const int* p = g ? r->rcpt_particles : r->lig_particles;
+            const double* wt = g ? r->rcpt_weights : r->lig_weights;
+            for (int k = 0; k < m; ++k) {
+                if (!in_range(p[k])) return bad("restraint particle index out of range");
+                const double wk = wt ? wt[k] : 1.0;
+                if (!(wk > 0.0) || !std::isfinite(wk)) return bad("restraint weights must be positive");
+                idx.push_back(p[k]);
+                w.push_back(wk);
+                wsum[g] += wk;
+            }
+        }
+        if (!finite({r->kfcm, r->tolcm, r->offset[0], r->offset[1], r->offset[2]}) || r->tolcm < 0.0)
+            return bad("invalid centroid restraint parameters");
+        on |= 1;
+        if (r->use_angles) {
+            for (int k = 0; k < 3; ++k)
+                if (!in_range(r->rcpt_ref[k]) || !in_range(r->lig_ref[k])) return bad("reference particle out of range");
+            if (!finite({r->kf_angle, r->angle_center, r->angle_tol, r->kf_dihedral1, r->dihedral1_center,
+                         r->dihedral1_tol, r->kf_dihedral2, r->dihedral2_center, r->dihedral2_tol}))
+                return bad("invalid angle restraint parameters");
+            on |= 2;
+        }
+    } else if (r->use_angles) {
+        return bad("the angle restraint terms need both centroid groups");
+    }
+    if (r->use_alignment) {
+        for (int k = 0; k < 3; ++k)
+            if (!in_range(r->liga_ref[k]) || !in_range(r->ligb_ref[k])) return bad("alignment particle out of range");
+        if (!finite({r->kf_displ, r->k_theta, r->k_psi, r->align_offset[0], r->align_offset[1], r->align_offset[2]}))
+            return bad("invalid alignment restraint parameters");
+        on |= 4;
+    }
+    s.rs_idx = idx;
+    s.rs_w = w;
+    s.rs_nlig = (on & 1) ? r->num_lig : 0;
+    s.rs_nrcpt = (on & 1) ? r->num_rcpt : 0;
+    double* P = s.rs_prm;
+    std::fill(P, P + SDM_RS_COUNT, 0.0);
+    P[SDM_RS_KFCM] = r->kfcm;
+    P[SDM_RS_TOLCM] = r->tolcm;
+    for (int k = 0; k < 3; ++k) P[SDM_RS_OFF + k] = r->offset[k];
+    P[SDM_RS_INVW_LIG] = wsum[0] > 0.0 ? 1.0 / wsum[0] : 0.0;
+    P[SDM_RS_INVW_RCPT] = wsum[1] > 0.0 ? 1.0 / wsum[1] : 0.0;
+    // windows [center - tol, center + tol] (SDMUtils.py:140-149)
+    P[SDM_RS_KFA] = r->kf_angle;
+    P[SDM_RS_ALO] = r->angle_center - r->angle_tol;
+    P[SDM_RS_AHI] = r->angle_center + r->angle_tol;
+    P[SDM_RS_KFD1] = r->kf_dihedral1;
+    P[SDM_RS_D1LO] = r->dihedral1_center - r->dihedral1_tol;
+    P[SDM_RS_D1HI] = r->dihedral1_center + r->dihedral1_tol;
+    P[SDM_RS_KFD2] = r->kf_dihedral2;
+    P[SDM_RS_D2LO] = r->dihedral2_center - r->dihedral2_tol;
+    P[SDM_RS_D2HI] = r->dihedral2_center + r->dihedral2_tol;
+    P[SDM_RS_KDISPL] = r->kf_displ;
+    P[SDM_RS_KTHETA] = r->k_theta;
+    P[SDM_RS_KPSI] = r->k_psi;
+    for (int k = 0; k < 3; ++k) P[SDM_RS_AOFF + k] = r->align_offset[k];
+    for (int k = 0; k < 3; ++k) {
+        s.rs_ref[k] = (on & 2) ? r->rcpt_ref[k] : 0;
+        s.rs_ref[3 + k] = (on & 2) ? r->lig_ref[k] : 0;
+        s.rs_ref[6 + k] = (on & 4) ? r->liga_ref[k] : 0;
+        s.rs_ref[9 + k] = (on & 4) ? r->ligb_ref[k] : 0;
+    }
+    s.rs_on = on;
+    return upload_restraints(h);
+}
+
+sdm_status sdm_set_restraint_control(sdm_handle* h, int replica, double lambda_r) {
+    if (!h) return SDM_ERR_INVALID_ARGUMENT;
+    if (replica < 0 || replica >= h->nrep) return fail(h, SDM_ERR_INVALID_ARGUMENT, "replica index out of range");
+    if (!std::isfinite(lambda_r)) return fail(h, SDM_ERR_INVALID_ARGUMENT, "non-finite restraint control parameter");
+    cudaSetDevice(h->device);
+    SDM_CUDA(h, cudaDeviceSynchronize());   // no evaluation in flight reads the old value
+    SDM_CUDA(h, cudaMemcpy(const_cast<double*>(h->args.rs_lam) + replica, &lambda_r, sizeof(double),
+                           cudaMemcpyHostToDevice));
+    return SDM_OK;
+}
+
+sdm_status sdm_get_restraint_energies(sdm_handle* h, double* energies) {
+    if (!h || !energies) return SDM_ERR_INVALID_ARGUMENT;
+    if (!h->args.rs_any) {
+        std::fill(energies, energies + h->nrep, 0.0);
+        return SDM_OK;
+    }
+    cudaSetDevice(h->device);
+    SDM_CUDA(h, cudaDeviceSynchronize());
+    SDM_CUDA(h, cudaMemcpy(energies, h->args.rs_e, h->nrep * sizeof(double), cudaMemcpyDeviceToHost));
+    return SDM_OK;
 }
 
 sdm_status sdm_set_params(sdm_handle* h, int replica, const double* params) {

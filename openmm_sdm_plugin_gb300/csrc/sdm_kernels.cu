@@ -1963,7 +1963,7 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     o[SDM_R_DW] = bfp;
     o[SDM_R_S] = bfp * fp;
     a.s_rep[r] = bfp * fp;
-    o[SDM_R_EPOT] = U0 + ebias;
+    o[SDM_R_EPOT] = U0 + ebias + (a.rs_any ? a.rs_e[r] : 0.0);   // + group-1 restraints
     o[SDM_R_DWDLAMBDA] = dwdl;
     o[SDM_R_LAMBDA1] = l1;
     o[SDM_R_LAMBDA2] = l2;

@@ -93,6 +93,22 @@ struct SdmSys {
     int pme_bc[3];            // cells per side of a spreading / interpolation brick
     int pme_nb[3];            // bricks per dimension
     int pme_cap;              // grid points of a brick's shared-memory sub-grid
+    // group-1 restraints (SDMUtils): rs_on bit 0 centroid, 1 angles, 2 alignment
+    int rs_on;
+    int rs_base, rs_nlig, rs_nrcpt;   // offset into rs_idx / rs_w (ligand group, then receptor group), counts
+    int rs_prm;                       // offset of the system's SDM_RS_COUNT parameters in rs_prm
+    int rs_ref[12];                   // r0 r1 r2 l0 l1 l2 (centroid angles), a0 a1 a2 b0 b1 b2 (alignment)
+};
+
+// restraint parameters (doubles per system)
+enum {
+    SDM_RS_KFCM = 0, SDM_RS_TOLCM = 1, SDM_RS_OFF = 2,            // + 3
+    SDM_RS_INVW_LIG = 5, SDM_RS_INVW_RCPT = 6,
+    SDM_RS_KFA = 7, SDM_RS_ALO = 8, SDM_RS_AHI = 9,
+    SDM_RS_KFD1 = 10, SDM_RS_D1LO = 11, SDM_RS_D1HI = 12,
+    SDM_RS_KFD2 = 13, SDM_RS_D2LO = 14, SDM_RS_D2HI = 15,
+    SDM_RS_KDISPL = 16, SDM_RS_KTHETA = 17, SDM_RS_KPSI = 18, SDM_RS_AOFF = 19,   // + 3
+    SDM_RS_COUNT = 24
 };
 
 // per perturbation item (replica, displaced particle, state): the wrapped
@@ -213,6 +229,13 @@ struct SdmArgs {
     int pme_smem;                   // dynamic shared memory of the brick kernels (bytes)
     SdmPertPos* pert_pos; // per perturbation item (total_pert entries)
     double* adj;         // adjoint sums: 3 per perturbation item
+    // group-1 restraints
+    const int* rs_idx;      // restraint group particles of every system
+    const double* rs_w;     // their centroid weights
+    const double* rs_prm;   // SDM_RS_COUNT parameters per system
+    const double* rs_lam;   // per replica: SDMRestraintControlParameter
+    double* rs_e;           // per replica: restraint energy of the last evaluation
+    int rs_any;             // 1 when some system has restraints
     int* ncl;            // clusters per replica
     unsigned* extz;      // per replica max cluster z extent (float bits)
     int* work_counter;   // [0] main pass, [1] perturbation pass

@@ -78,6 +78,45 @@ class SDMParams:
 
 
 @dataclasses.dataclass
+class Restraints:
+    """Group-1 restraints of the reference's SDMUtils (python/SDMUtils.py),
+    in nm, rad and kJ/mol (see sdm_restraints in include/sdm_capi.h).
+
+    Centroid restraint (SDMUtils.addRestraintForce): flat-bottom harmonic on
+    the distance between the weighted centroids of `lig_particles` and
+    `rcpt_particles` (minus `offset`); with `use_angles`, flat-bottom windows
+    on angle(r0, l0, l1), dihedral(r1, r0, l0, l1), dihedral(r0, l0, l1, l2).
+    All scaled by the replica's control parameter.  Alignment restraint
+    (SDMUtils.addAlignmentForce) between ligands A and B."""
+    lig_particles: Sequence[int] = ()
+    rcpt_particles: Sequence[int] = ()
+    lig_weights: Optional[Sequence[float]] = None    # None: 1 (the reference weights by mass)
+    rcpt_weights: Optional[Sequence[float]] = None
+    kfcm: float = 0.0                # kJ/mol/nm^2
+    tolcm: float = 0.0               # nm
+    offset: Sequence[float] = (0.0, 0.0, 0.0)
+    use_angles: bool = False
+    rcpt_ref: Sequence[int] = (0, 0, 0)
+    lig_ref: Sequence[int] = (0, 0, 0)
+    kf_angle: float = 0.0            # kJ/mol/rad^2
+    angle_center: float = 0.0        # rad
+    angle_tol: float = 0.0
+    kf_dihedral1: float = 0.0
+    dihedral1_center: float = 0.0
+    dihedral1_tol: float = 0.0
+    kf_dihedral2: float = 0.0
+    dihedral2_center: float = 0.0
+    dihedral2_tol: float = 0.0
+    use_alignment: bool = False
+    liga_ref: Sequence[int] = (0, 0, 0)
+    ligb_ref: Sequence[int] = (0, 0, 0)
+    kf_displ: float = 0.0            # kJ/mol/nm^2
+    k_theta: float = 0.0             # kJ/mol
+    k_psi: float = 0.0               # kJ/mol
+    align_offset: Sequence[float] = (0.0, 0.0, 0.0)
+
+
+@dataclasses.dataclass
 class SDMSystem:
     name: str
     box: np.ndarray            # (3,) nm
@@ -97,6 +136,7 @@ class SDMSystem:
     nonbonded_method: str = "rf"                # "rf" (reaction field) or "pme"
     ewald_tolerance: float = 5e-4               # PME
     pme_grid: Optional[Sequence[int]] = None    # PME grid (None: from the tolerance)
+    restraints: Optional[Restraints] = None     # group-1 restraints (SDMUtils)
 
     @property
     def n(self) -> int:

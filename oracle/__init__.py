@@ -494,3 +494,97 @@ def spme(x, q, box, beta, grid, order=5, forces=True):
                     F[:, 2] -= Ms[0][:, a] * Ms[1][:, b] * dMs[2][:, c] * p
         F *= K_COULOMB * q[:, None] * (K / box)[None, :]
     return E, F, phi
+
+
+# --------------------------------------------------------------------------
+# Group-1 restraints of the reference's SDMUtils (python/SDMUtils.py): the
+# custom-force energy expressions restated in numpy (FP64, no periodic
+# images); forces by central differences of that energy, so the check does
+# not share the kernel's analytic gradients.
+# --------------------------------------------------------------------------
+def _rs_wrap(v, period):
+    """v - P floor(v/P + 0.5) (SDMUtils.py:78-88)."""
+    return v - period * np.floor(v / period + 0.5)
+
+
+def _rs_flat(v, lo, hi, period, kf):
+    """(kf/2) (step(dm) max(0, db)^2 + step(-dm) max(0, -da)^2), step(0) = 1."""
+    db, da = _rs_wrap(v - hi, period), _rs_wrap(v - lo, period)
+    dm = _rs_wrap(v - 0.5 * (lo + hi), period)
+    return 0.5 * kf * ((dm >= 0) * max(0.0, db) ** 2 + (-dm >= 0) * max(0.0, -da) ** 2)
+
+
+def _rs_angle(p1, p2, p3):
+    u, v = p1 - p2, p3 - p2
+    return np.arctan2(np.linalg.norm(np.cross(u, v)), u @ v)
+
+
+def _rs_dihedral(p1, p2, p3, p4):
+    """IUPAC dihedral: trans = pi, cis = 0."""
+    b1, b2, b3 = p2 - p1, p3 - p2, p4 - p3
+    n = np.cross(b2, b3)
+    return np.arctan2(np.linalg.norm(b2) * (b1 @ n), np.cross(b1, b2) @ n)
+
+
+def _rs_cos(u, v):
+    return (u @ v) / (np.linalg.norm(u) * np.linalg.norm(v))
+
+
+def _rs_perp(d, n1):
+    return d - (d @ n1) * n1
+
+
+def restraint_energy(x, rs, control=1.0):
+    """Energy (kJ/mol) of the restraints `rs` (fields of
+    openmm_sdm_plugin_gb300.systems.Restraints) at coordinates x (N, 3)."""
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    E = 0.0
+    lig, rcpt = list(rs.lig_particles), list(rs.rcpt_particles)
+    if lig and rcpt:
+        wl = np.ones(len(lig)) if rs.lig_weights is None else np.asarray(rs.lig_weights, np.float64)
+        wr = np.ones(len(rcpt)) if rs.rcpt_weights is None else np.asarray(rs.rcpt_weights, np.float64)
+        c1 = (wl[:, None] * x[lig]).sum(0) / wl.sum()
+        c2 = (wr[:, None] * x[rcpt]).sum(0) / wr.sum()
+        d = np.linalg.norm(c1 - np.asarray(rs.offset, np.float64) - c2)
+        E += control * 0.5 * rs.kfcm * (d >= rs.tolcm) * (d - rs.tolcm) ** 2
+        if rs.use_angles:
+            r0, r1, _ = (x[i] for i in rs.rcpt_ref)
+            l0, l1, l2 = (x[i] for i in rs.lig_ref)
+            terms = ((_rs_angle(r0, l0, l1), rs.kf_angle, rs.angle_center, rs.angle_tol, np.pi),
+                     (_rs_dihedral(r1, r0, l0, l1), rs.kf_dihedral1, rs.dihedral1_center, rs.dihedral1_tol,
+                      2 * np.pi),
+                     (_rs_dihedral(r0, l0, l1, l2), rs.kf_dihedral2, rs.dihedral2_center, rs.dihedral2_tol,
+                      2 * np.pi))
+            for v, kf, c, tol, per in terms:
+                E += control * _rs_flat(v, c - tol, c + tol, per, kf)
+    if rs.use_alignment:
+        a0, a1, a2 = (x[i] for i in rs.liga_ref)
+        b0, b1, b2 = (x[i] for i in rs.ligb_ref)
+        E += 0.5 * rs.kf_displ * np.sum((b0 - np.asarray(rs.align_offset, np.float64) - a0) ** 2)
+        E += 0.5 * rs.k_theta * (1.0 - _rs_cos(b1 - b0, a1 - a0))
+        nb = (b1 - b0) / np.linalg.norm(b1 - b0)
+        na = (a1 - a0) / np.linalg.norm(a1 - a0)
+        E += 0.25 * rs.k_psi * (1.0 - _rs_cos(_rs_perp(b2 - b0, nb), _rs_perp(a2 - a0, nb)))
+        E += 0.25 * rs.k_psi * (1.0 - _rs_cos(_rs_perp(a2 - a0, na), _rs_perp(b2 - b0, na)))
+    return float(E)
+
+
+def restraint_forces(x, rs, control=1.0, h=1e-6):
+    """-dE/dx (N, 3) by central differences over the restraint's particles."""
+    x = np.array(x, np.float64).reshape(-1, 3)
+    idx = set(rs.lig_particles) | set(rs.rcpt_particles)
+    if rs.use_angles:
+        idx |= set(rs.rcpt_ref) | set(rs.lig_ref)
+    if rs.use_alignment:
+        idx |= set(rs.liga_ref) | set(rs.ligb_ref)
+    F = np.zeros_like(x)
+    for i in sorted(idx):
+        for k in range(3):
+            v = x[i, k]
+            x[i, k] = v + h
+            ep = restraint_energy(x, rs, control)
+            x[i, k] = v - h
+            em = restraint_energy(x, rs, control)
+            x[i, k] = v
+            F[i, k] = -(ep - em) / (2 * h)
+    return F
