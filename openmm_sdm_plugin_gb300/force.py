@@ -19,12 +19,13 @@ would.
 from __future__ import annotations
 
 import dataclasses
+import math
 from typing import List, Optional, Sequence
 
 import numpy as np
 
 from . import capi
-from .systems import SDMParams, SDMSystem
+from .systems import Restraints, SDMParams, SDMSystem
 
 
 class SDMForce:
@@ -59,6 +60,10 @@ class SDMForce:
         self._topology_dirty = True
         self._displ_dirty = False
         self._params_dirty = True
+        self._restraints: Optional[Restraints] = None   # group-1 restraints (SDMUtils mirror)
+        self._restraints_dirty = False
+        self._restraint_control = 1.0
+        self._control_dirty = False
 
     # -- NonbondedForce-like topology ---------------------------------------
     def addParticle(self, charge: float, sigma: float, epsilon: float) -> int:
@@ -193,6 +198,27 @@ class SDMForce:
             raise RuntimeError("no evaluation yet")
         return (r[capi.R_U], r[capi.R_U0], r[capi.R_U1], r[capi.R_W], r[capi.R_DW])
 
+    # -- group-1 restraints (set through SDMUtils) --------------------------
+    def _set_restraints(self, rs: Optional[Restraints]):
+        self._restraints = rs
+        self._restraints_dirty = True
+
+    def setParameter(self, name: str, value: float):
+        """Context.setParameter for SDMRestraintControlParameter (SDMUtils.py:99)."""
+        if name != SDMUtils.RestraintControlParameterName:
+            raise KeyError(name)
+        self._restraint_control = float(value)
+        self._control_dirty = True
+
+    def getParameter(self, name: str) -> float:
+        if name != SDMUtils.RestraintControlParameterName:
+            raise KeyError(name)
+        return self._restraint_control
+
+    def getRestraintEnergy(self) -> float:
+        """Group-1 restraint energy of the last evaluation (part of getPotEnergy)."""
+        return float(self._handle.restraint_energies()[0]) if self._handle is not None else 0.0
+
     # -- evaluation -------------------------------------------------------
     def _system(self) -> SDMSystem:
         n = len(self._q)
@@ -209,6 +235,8 @@ class SDMForce:
             self._topology_dirty = False
             self._displ_dirty = False
             self._params_dirty = True
+            self._restraints_dirty = self._restraints is not None
+            self._control_dirty = self._restraint_control != 1.0
         if self._displ_dirty:
             self._handle.set_displacement(0, self._displ[:len(self._q)])
             self._displ_dirty = False
@@ -217,6 +245,12 @@ class SDMForce:
                 raise capi.SdmError(capi.SDM_ERR_UNKNOWN_METHOD, "Unknown soft core method")
             self._handle.set_params(0, self._p.as_array())
             self._params_dirty = False
+        if self._restraints_dirty:
+            self._handle.set_restraints(0, self._restraints)
+            self._restraints_dirty = False
+        if self._control_dirty:
+            self._handle.set_restraint_control(0, self._restraint_control)
+            self._control_dirty = False
 
     def evaluate(self, positions, device: int = 0):
         """Returns (E_pot, forces[N,3]) of the nonbonded group, FP64."""
@@ -314,6 +348,84 @@ class LangevinIntegratorSDM(SDMForce):
         self._last = r
         self._bind_e = float(r[capi.R_BINDE])
         self._pot_e = float(r[capi.R_EPOT])
+
+
+class SDMUtils:
+    """Host mirror of the reference's SDMUtils (python/SDMUtils.py) for a
+    mirror force (SDMForce or LangevinIntegratorSDM): the same method names,
+    argument names and meanings, with plain numbers in OpenMM's internal
+    units (nm, rad, kJ/mol) where the reference takes unit quantities.  The
+    restraints are evaluated on the device in the same call as the SDM force
+    (group 1 of the reference).  The centroids are mass weighted (the
+    reference's CustomCentroidBondForce default) when the force has masses
+    (LangevinIntegratorSDM), equally weighted otherwise.  One centroid
+    restraint and one alignment restraint per force."""
+    RestraintControlParameterName = "SDMRestraintControlParameter"
+    LinearMethod, QuadraticMethod, ILogisticMethod = 0, 1, 2
+    NoSoftCoreMethod, TanhSoftCoreMethod, RationalSoftCoreMethod = 0, 1, 2
+
+    def __init__(self, force: SDMForce):
+        self.force = force
+        self._cm = None      # fields of the centroid restraint
+        self._align = None   # fields of the alignment restraint
+
+    def getControlParameterName(self) -> str:
+        return self.RestraintControlParameterName
+
+    def _weights(self, particles):
+        m = getattr(self.force, "_mass", None)
+        return None if m is None else [m[i] for i in particles]
+
+    def _push(self):
+        fields = {}
+        if self._cm:
+            fields.update(self._cm)
+        if self._align:
+            fields.update(self._align)
+        self.force._set_restraints(Restraints(**fields) if fields else None)
+
+    def addRestraintForce(self, lig_cm_particles=None, rcpt_cm_particles=None, kfcm=0.0, tolcm=0.0,
+                          lig_ref_particles=None, rcpt_ref_particles=None, angle_center=0.0, kfangle=0.0,
+                          angletol=math.radians(10.0), dihedral1center=0.0, kfdihedral1=0.0,
+                          dihedral1tol=math.radians(10.0), dihedral2center=0.0, kfdihedral2=0.0,
+                          dihedral2tol=math.radians(10.0), offset=(0.0, 0.0, 0.0)):
+        """SDMUtils.addRestraintForce (python/SDMUtils.py:32-157)."""
+        if not (lig_cm_particles and rcpt_cm_particles):
+            return
+        if self._cm is not None:
+            raise NotImplementedError("one centroid restraint per force")
+        do_angles = False
+        if lig_ref_particles and rcpt_ref_particles:
+            if not (len(lig_ref_particles) == 3 and len(rcpt_ref_particles) == 3):
+                raise ValueError("Invalid lists of reference atoms")
+            do_angles = True
+        lig, rcpt = [int(i) for i in lig_cm_particles], [int(i) for i in rcpt_cm_particles]
+        self._cm = dict(lig_particles=lig, rcpt_particles=rcpt, lig_weights=self._weights(lig),
+                        rcpt_weights=self._weights(rcpt), kfcm=float(kfcm), tolcm=float(tolcm),
+                        offset=tuple(float(v) for v in offset), use_angles=do_angles)
+        if do_angles:
+            self._cm.update(rcpt_ref=tuple(int(i) for i in rcpt_ref_particles),
+                            lig_ref=tuple(int(i) for i in lig_ref_particles),
+                            kf_angle=float(kfangle), angle_center=float(angle_center), angle_tol=float(angletol),
+                            kf_dihedral1=float(kfdihedral1), dihedral1_center=float(dihedral1center),
+                            dihedral1_tol=float(dihedral1tol), kf_dihedral2=float(kfdihedral2),
+                            dihedral2_center=float(dihedral2center), dihedral2_tol=float(dihedral2tol))
+        self._push()
+
+    def addAlignmentForce(self, liga_ref_particles=None, ligb_ref_particles=None, kfdispl=0.0, ktheta=0.0,
+                          kpsi=0.0, offset=(0.0, 0.0, 0.0)):
+        """SDMUtils.addAlignmentForce (python/SDMUtils.py:160-257)."""
+        if not (liga_ref_particles and ligb_ref_particles):
+            raise ValueError("Invalid lists of reference atoms")
+        if not (len(liga_ref_particles) == 3 and len(ligb_ref_particles) == 3):
+            raise ValueError("Invalid lists of reference atoms")
+        if self._align is not None:
+            raise NotImplementedError("one alignment restraint per force")
+        self._align = dict(use_alignment=True, liga_ref=tuple(int(i) for i in liga_ref_particles),
+                           ligb_ref=tuple(int(i) for i in ligb_ref_particles), kf_displ=float(kfdispl),
+                           k_theta=float(ktheta), k_psi=float(kpsi),
+                           align_offset=tuple(float(v) for v in offset))
+        self._push()
 
 
 def force_from_system(s: SDMSystem, replica: int = 0) -> SDMForce:

@@ -172,3 +172,35 @@ def test_langevin_step_includes_the_restraint_forces():
     xo, vo = oracle.langevin_update(x, v, im, F, 0.001, 2.0, 0.0)
     assert np.array_equal(xd.cpu().numpy(), xo)
     assert np.array_equal(vd.cpu().numpy(), vo)
+
+
+def test_sdmutils_mirror_through_sdmforce():
+    """SDMUtils.addRestraintForce / addAlignmentForce on the SDMForce mirror:
+    the restraint energy inside getPotEnergy, the control parameter through
+    setParameter (SDMRestraintControlParameter)."""
+    from openmm_sdm_plugin_gb300.force import SDMUtils, force_from_system
+    s = _system(nrep=1)
+    x = s.positions[0]
+    rs = _restraints(s, x)
+    plain = force_from_system(s)
+    e_plain, _ = plain.evaluate(x)
+    f = force_from_system(s)
+    u = SDMUtils(f)
+    u.addRestraintForce(lig_cm_particles=list(rs.lig_particles), rcpt_cm_particles=list(rs.rcpt_particles),
+                        kfcm=rs.kfcm, tolcm=rs.tolcm, lig_ref_particles=list(rs.lig_ref),
+                        rcpt_ref_particles=list(rs.rcpt_ref), angle_center=rs.angle_center, kfangle=rs.kf_angle,
+                        angletol=rs.angle_tol, dihedral1center=rs.dihedral1_center,
+                        kfdihedral1=rs.kf_dihedral1, dihedral1tol=rs.dihedral1_tol,
+                        dihedral2center=rs.dihedral2_center, kfdihedral2=rs.kf_dihedral2,
+                        dihedral2tol=rs.dihedral2_tol, offset=rs.offset)
+    u.addAlignmentForce(liga_ref_particles=list(rs.liga_ref), ligb_ref_particles=list(rs.ligb_ref),
+                        kfdispl=rs.kf_displ, ktheta=rs.k_theta, kpsi=rs.k_psi, offset=rs.align_offset)
+    ref = dataclasses.replace(rs, lig_weights=None, rcpt_weights=None)   # SDMForce has no masses
+    e, _ = f.evaluate(x)
+    assert abs((e - e_plain) - oracle.restraint_energy(x, ref)) < 1e-8 * abs(e)
+    assert abs(f.getRestraintEnergy() - oracle.restraint_energy(x, ref)) < 1e-9 * abs(e - e_plain)
+    f.setParameter(u.getControlParameterName(), 0.5)
+    e_half, _ = f.evaluate(x)
+    assert abs(f.getRestraintEnergy() - oracle.restraint_energy(x, ref, control=0.5)) < 1e-9 * abs(e)
+    f.close()
+    plain.close()
