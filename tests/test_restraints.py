@@ -204,3 +204,31 @@ def test_sdmutils_mirror_through_sdmforce():
     assert abs(f.getRestraintEnergy() - oracle.restraint_energy(x, ref, control=0.5)) < 1e-9 * abs(e)
     f.close()
     plain.close()
+
+
+@pytest.mark.parametrize("method", ["rf", "pme"])
+def test_restraints_on_the_second_system_of_a_handle(method):
+    """Restraints on system 1 only of a two-system handle (own offsets into
+    the restraint data), reaction field and PME: system 0's replica has no
+    restraint energy, system 1's replicas match the oracle."""
+    a = dataclasses.replace(S.config0(variant="b"), nonbonded_method=method)
+    b = dataclasses.replace(S.host_guest(1500, seed=7, nstates=2), nonbonded_method=method)
+    xb = b.positions[0]
+    lig = np.asarray(b.ligand_atoms)
+    others = np.setdiff1d(np.arange(b.n), lig)
+    near = others[np.argsort(np.linalg.norm(xb[others] - xb[lig].mean(0), axis=1))[:50]]
+    rs = S.Restraints(lig_particles=lig, rcpt_particles=near, kfcm=600.0, tolcm=0.0,
+                      use_alignment=True, liga_ref=tuple(int(i) for i in lig[:3]),
+                      ligb_ref=tuple(int(i) for i in near[:3]), kf_displ=50.0, k_theta=10.0, k_psi=5.0)
+    h = capi.Handle([a, dataclasses.replace(b, restraints=rs)])
+    reps = [(a, 0), (b, 0), (b, 1)]
+    for r, (s, k) in enumerate(reps):
+        h.set_params(r, s.params[k].as_array())
+    x = np.concatenate([a.positions[0], b.positions[0], b.positions[1]])
+    res, F = h.evaluate(x)
+    e = h.restraint_energies()
+    assert e[0] == 0.0
+    for r in (1, 2):
+        eo = oracle.restraint_energy(b.positions[r - 1], rs)
+        assert eo > 0.0 and abs(e[r] - eo) < 1e-9 * eo
+    assert (res[:, capi.R_STATUS] == 0).all()
