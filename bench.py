@@ -351,6 +351,29 @@ def main():
                             "stochastic-dynamics update in one CUDA graph per step (dt 2 fs, 1/ps, 300 K), "
                             "every step from the benchmark configuration"}
 
+    # ---- parameter-gradient sums (the adjoint pass) after every evaluation ----
+    # sdm_adjoint synchronises and returns host sums, so this field is timed
+    # by the host clock around evaluation + adjoint
+    nd_tot = NREP * int(np.count_nonzero(np.any(sysm.displacement != 0, axis=1)))
+    nadj = min(args.steps, 100)
+
+    def adj_call():
+        h.evaluate_device(xd.data_ptr(), rd.data_ptr(), fd.data_ptr(), sptr)
+        h.adjoint(nd_tot)
+    for _ in range(warm):
+        adj_call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(nadj):
+        adj_call()
+    torch.cuda.synchronize()
+    t_adj = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    adjoint = {"value": whole_job_rate(NREP * nadj, world, t_adj),
+               "unit": "lambda-state evals with parameter-gradient sums/s",
+               "ms_per_call": 1e3 * t_adj / nadj, "steps": nadj, "clock": "host (the call synchronises)",
+               "workload": "the benchmark batch: evaluation, then sdm_adjoint (the sums behind dU0/dp, "
+                           "dU1/dp of the displaced particles' charge, sigma, epsilon) every call"}
+
     # ---- the same batch with PME electrostatics (smooth PME, order 5, tol 5e-4) ----
     import dataclasses
     sys_pme = dataclasses.replace(sysm, nonbonded_method="pme", ewald_tolerance=5e-4)
@@ -484,6 +507,7 @@ def main():
         "langevin": langevin,
         "dms_temoa": temoa,
         "pme": pme,
+        "adjoint": adjoint,
         "roofline": roof,
         "kernel_ms": breakdown,
         "cpu_baseline": cpu,
