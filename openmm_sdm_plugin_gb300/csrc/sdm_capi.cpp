@@ -1315,10 +1315,22 @@ sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double*
         SDM_CUDA(h, cudaMemcpyAsync(forces, h->f_in, nx * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
     // the status word is read after every host call; it is cleared here only
-    // when this call acts on it (list regrow, or verification on)
+    // when this call acts on it (list regrow, or verification on).  With a
+    // results buffer the word comes back in it: every status source runs
+    // before or inside the finalize kernel, and each replica's SDM_R_STATUS
+    // holds the word as its block saw it plus its own flags, so their OR is
+    // the word (a separate read only when it is nonzero)
     int v = 0;
-    s = check_dev_status(h, &v, false);
-    if (s) return s;
+    if (results) {
+        for (int r = 0; r < h->nrep; ++r) v |= (int)results[(size_t)r * SDM_NRESULTS + SDM_R_STATUS];
+        if (v) {
+            s = check_dev_status(h, &v, false);
+            if (s) return s;
+        }
+    } else {
+        s = check_dev_status(h, &v, false);
+        if (s) return s;
+    }
     if (v & SDM_DEV_LIST_OVERFLOW) {
         SDM_CUDA(h, cudaMemset(h->args.status, 0, sizeof(int)));
         // lists too small for these coordinates: regrow and evaluate again
