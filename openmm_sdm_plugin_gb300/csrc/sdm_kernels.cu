@@ -64,10 +64,6 @@ __device__ __forceinline__ int wrap_cell(int n, int M) {
     return n;
 }
 
-__device__ __forceinline__ int pmod(int a, int M) {
-    int r = a % M;
-    return r < 0 ? r + M : r;
-}
 
 __device__ __forceinline__ float img32(float d, float L, float invL) {
     float t = rintf(__fmul_rn(d, invL));
@@ -1218,7 +1214,6 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, Wa
     const float o[3] = {pp.o[0], pp.o[1], pp.o[2]};
     const float qp = a.topo_q[tp], hp = a.topo_hs[tp], sp_ = a.topo_se[tp];
     const int cxb = a.cx_off[S.cx_base + pidx], cxe = a.cx_off[S.cx_base + pidx + 1];
-    const float rcl2 = S.rcl2f;
     const float rclc = S.rcl + 2.0e-4f;
     const float rclc2 = rclc * rclc;
     const float* tabx = a.shift_tab + S.shift_base;
