@@ -295,6 +295,21 @@ sdm_status sdm_set_restraint_control(sdm_handle* h, int replica, double lambda_r
  * Synchronises. */
 sdm_status sdm_get_restraint_energies(sdm_handle* h, double* energies);
 
+/* Rigid 3-site waters in sdm_langevin_step: the constraint step the
+ * reference's integrator applies between the position update and the
+ * velocity recomputation (ReferenceStochasticDynamicsSDM.cpp:131-266, with
+ * the OpenMM context's constraint algorithm), solved per water in closed
+ * form (SETTLE, Miyamoto and Kollman, J. Comput. Chem. 13, 952 (1992)):
+ * the unconstrained positions move along the old bond vectors, mass
+ * weighted, until |O-H| = d_oh and |H-H| = d_hh; then v = (x' - x)/dt.
+ * waters: [3 * num_waters] (O, H, H) particle indices of `system` (each
+ * particle in at most one water; the hydrogens of a water share a mass).
+ * Hydrogens are taken in the minimum image of their oxygen.  A water with a
+ * fixed particle (1/m = 0) is left unconstrained.  num_waters = 0 removes
+ * them.  Applies to every replica of the system. */
+sdm_status sdm_set_rigid_waters(sdm_handle* h, int system, int num_waters, const int* waters, double d_oh,
+                                double d_hh);
+
 /* Reads and clears the device status word (SDM_DEV_* bits).  Synchronises. */
 sdm_status sdm_check_status(sdm_handle* h, int* device_status);
 

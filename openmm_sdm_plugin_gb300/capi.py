@@ -43,7 +43,7 @@ EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_get_kernel_times", "sdm_autotune", "sdm_count_pairs", "sdm_get_grid",
             "sdm_export_lists", "sdm_evaluate_noalloc", "sdm_set_particle_params",
             "sdm_adjoint", "sdm_set_langevin", "sdm_langevin_step", "sdm_set_restraints",
-            "sdm_set_restraint_control", "sdm_get_restraint_energies")
+            "sdm_set_restraint_control", "sdm_get_restraint_energies", "sdm_set_rigid_waters")
 
 NB_REACTION_FIELD, NB_PME = 0, 1
 NOALLOC_MAX_PARTICLES = 8192
@@ -119,6 +119,7 @@ def load_library(path: str = LIB_PATH):
         L.sdm_set_restraints.argtypes = [vp, C.c_int, C.POINTER(RestraintDesc)]
         L.sdm_set_restraint_control.argtypes = [vp, C.c_int, C.c_double]
         L.sdm_get_restraint_energies.argtypes = [vp, vp]
+        L.sdm_set_rigid_waters.argtypes = [vp, C.c_int, C.c_int, vp, C.c_double, C.c_double]
         for name in EXPORTED:
             if name != "sdm_last_error":
                 getattr(L, name).restype = C.c_int
@@ -253,6 +254,12 @@ class Handle:
 
     def set_restraint_control(self, replica: int, value: float):
         self._check(self.lib.sdm_set_restraint_control(self.h, int(replica), float(value)))
+
+    def set_rigid_waters(self, system: int, waters, d_oh: float = 0.0, d_hh: float = 0.0):
+        """Rigid (O, H, H) waters of one system in the Langevin step; waters (W, 3) or None."""
+        w = np.ascontiguousarray(np.asarray(waters if waters is not None else [], np.int32).reshape(-1))
+        self._check(self.lib.sdm_set_rigid_waters(self.h, int(system), int(w.size // 3),
+                                                  w.ctypes.data if w.size else None, float(d_oh), float(d_hh)))
 
     def restraint_energies(self):
         out = np.zeros(self.nrep)

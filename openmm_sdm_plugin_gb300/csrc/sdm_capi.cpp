@@ -70,6 +70,9 @@ struct SysHost {
     double rs_prm[SDM_RS_COUNT] = {};
     int rs_ref[12] = {};
     int rs_on = 0, rs_nlig = 0, rs_nrcpt = 0;
+    // rigid waters (sdm_set_rigid_waters): (O, H, H) triples, distances
+    std::vector<int> st_idx;
+    double st_doh = 0.0, st_dhh = 0.0;
     bool clique = false;
     SdmSys dev;
     int replicas;
@@ -121,6 +124,7 @@ struct sdm_handle {
     char* arena = nullptr;
     size_t arena_bytes = 0;
     void* rs_buf = nullptr;   // restraint data of every system (sdm_set_restraints)
+    void* st_buf = nullptr;   // rigid-water data and the unconstrained-position scratch
     cudaStream_t stream = nullptr;
     SdmArgs args{};
     int* item_prefix = nullptr;
@@ -1080,6 +1084,7 @@ sdm_status sdm_destroy(sdm_handle* h) {
     if (!h) return SDM_OK;
     if (h->jl_buf) { cudaSetDevice(h->device); cudaFree(h->jl_buf); h->jl_buf = nullptr; }
     if (h->rs_buf) { cudaSetDevice(h->device); cudaFree(h->rs_buf); h->rs_buf = nullptr; }
+    if (h->st_buf) { cudaSetDevice(h->device); cudaFree(h->st_buf); h->st_buf = nullptr; }
     if (h->arena) cudaSetDevice(h->device);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
@@ -1246,6 +1251,66 @@ sdm_status sdm_set_restraints(sdm_handle* h, int system, const sdm_restraints* r
     }
     s.rs_on = on;
     return upload_restraints(h);
+}
+
+// Rigid-water data of every system into one device buffer (water triples,
+// per-particle flags, the per-particle scratch of unconstrained positions);
+// the cached graphs hold the previous pointers and are dropped.
+static sdm_status upload_rigid_waters(sdm_handle* h) {
+    std::vector<int> idx, flag;
+    int any = 0, mx = 0;
+    for (auto& s : h->sys) {
+        s.dev.st_base = (int)(idx.size() / 3);
+        s.dev.st_count = (int)(s.st_idx.size() / 3);
+        s.dev.st_doh = s.st_doh;
+        s.dev.st_dhh = s.st_dhh;
+        idx.insert(idx.end(), s.st_idx.begin(), s.st_idx.end());
+        std::vector<int> f(s.n, 0);
+        for (int v : s.st_idx) f[v] = 1;
+        flag.insert(flag.end(), f.begin(), f.end());
+        any |= s.dev.st_count ? 1 : 0;
+        mx = std::max(mx, s.dev.st_count);
+    }
+    SDM_CUDA(h, cudaDeviceSynchronize());
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    if (h->st_buf) { cudaFree(h->st_buf); h->st_buf = nullptr; }
+    const size_t nxp = 3 * (size_t)h->total_particles;
+    SDM_CUDA(h, cudaMalloc(&h->st_buf, nxp * sizeof(double) + (idx.size() + flag.size()) * sizeof(int) + 16));
+    double* xp = static_cast<double*>(h->st_buf);
+    int* ip = reinterpret_cast<int*>(xp + nxp);
+    if (!idx.empty()) SDM_CUDA(h, cudaMemcpy(ip, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice));
+    SDM_CUDA(h, cudaMemcpy(ip + idx.size(), flag.data(), flag.size() * sizeof(int), cudaMemcpyHostToDevice));
+    h->args.lv_xp = xp;
+    h->args.st_idx = ip;
+    h->args.st_flag = ip + idx.size();
+    h->args.st_any = any;
+    h->args.st_max = mx;
+    return upload_topology(h);
+}
+
+sdm_status sdm_set_rigid_waters(sdm_handle* h, int system, int num_waters, const int* waters, double d_oh,
+                                double d_hh) {
+    if (!h) return SDM_ERR_INVALID_ARGUMENT;
+    if (system < 0 || system >= (int)h->sys.size()) return fail(h, SDM_ERR_INVALID_ARGUMENT, "system index out of range");
+    if (num_waters < 0 || (num_waters > 0 && !waters)) return fail(h, SDM_ERR_INVALID_ARGUMENT, "invalid water list");
+    SysHost& s = h->sys[system];
+    if (num_waters > 0) {
+        if (!(d_oh > 0.0) || !(d_hh > 0.0) || !(d_hh < 2.0 * d_oh) || !std::isfinite(d_oh) || !std::isfinite(d_hh))
+            return fail(h, SDM_ERR_INVALID_ARGUMENT, "water distances must satisfy 0 < d_hh < 2 d_oh");
+        std::vector<char> used(s.n, 0);
+        for (int k = 0; k < 3 * num_waters; ++k) {
+            const int i = waters[k];
+            if (i < 0 || i >= s.n) return fail(h, SDM_ERR_INVALID_ARGUMENT, "water particle index out of range");
+            if (used[i]) return fail(h, SDM_ERR_INVALID_ARGUMENT, "a particle belongs to two waters");
+            used[i] = 1;
+        }
+    }
+    cudaSetDevice(h->device);
+    s.st_idx.assign(waters, waters + 3 * (size_t)num_waters);
+    s.st_doh = num_waters ? d_oh : 0.0;
+    s.st_dhh = num_waters ? d_hh : 0.0;
+    return upload_rigid_waters(h);
 }
 
 sdm_status sdm_set_restraint_control(sdm_handle* h, int replica, double lambda_r) {

@@ -2044,7 +2044,13 @@ __global__ void k_langevin(SdmArgs a) {
         const SdmRep& R = a.rep[r];
         const size_t pi = (size_t)R.x_off + (gi - R.atom_win);   // particle in the concatenated order
         const double im = a.lv_invm[pi];
-        if (im == 0.0) continue;
+        // rigid-water particles leave x' in lv_xp; k_settle constrains and sets x and v
+        const bool cons = a.st_any && a.st_flag[a.sys[R.sys].atom_base + (gi - R.atom_win)];
+        if (im == 0.0) {
+            if (cons)
+                for (int k = 0; k < 3; ++k) a.lv_xp[3 * pi + k] = a.lv_x[3 * pi + k];
+            continue;
+        }
         const size_t gsl = (size_t)R.slot_win + a.inv[gi];
         const double s = a.s_rep[r];
         const double f0[3] = {fix_to_double(a.F0x[gsl]), fix_to_double(a.F0y[gsl]), fix_to_double(a.F0z[gsl])};
@@ -2061,8 +2067,123 @@ __global__ void k_langevin(SdmArgs a) {
             const double v = __dadd_rn(__dadd_rn(__dmul_rn(vscale, a.lv_v[3 * pi + k]), __dmul_rn(fsi, f)),
                                        __dmul_rn(nsq, nrm[k]));
             const double xp = __dadd_rn(x, __dmul_rn(dt, v));
-            a.lv_v[3 * pi + k] = __dmul_rn(invdt, __dsub_rn(xp, x));
-            a.lv_x[3 * pi + k] = xp;
+            if (cons) {
+                a.lv_xp[3 * pi + k] = xp;
+            } else {
+                a.lv_v[3 * pi + k] = __dmul_rn(invdt, __dsub_rn(xp, x));
+                a.lv_x[3 * pi + k] = xp;
+            }
+        }
+    }
+}
+
+// ---- rigid waters: SETTLE (Miyamoto and Kollman, J. Comput. Chem. 13, 952 (1992)) ----
+// Per water, old positions A0 B0 C0 (O H H, constrained) and unconstrained
+// new A1 B1 C1.  Frame: origin the new centre of mass D, z normal to the old
+// molecule plane, y along the new O's in-plane direction.  The constrained
+// positions keep the new z coordinates (corrections along old bonds lie in
+// the old plane); the canonical water is tilted by phi (from z of O) and psi
+// (from z of H - H), then turned by theta about z so that the corrections
+// exert no torque about the old positions (they are central forces along the
+// old bonds): alpha sin(theta) + beta cos(theta) = gamma.
+struct D3 {
+    double x, y, z;
+};
+__device__ __forceinline__ D3 d3sub(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ double d3dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ D3 d3cross(D3 a, D3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ D3 d3unit(D3 a) {
+    const double s = rsqrt(d3dot(a, a));
+    return {a.x * s, a.y * s, a.z * s};
+}
+__device__ __forceinline__ D3 d3frame(D3 o, D3 e1, D3 e2, D3 e0, double x, double y, double z) {
+    return {o.x + x * e1.x + y * e2.x + z * e0.x, o.y + x * e1.y + y * e2.y + z * e0.y,
+            o.z + x * e1.z + y * e2.z + z * e0.z};
+}
+
+// one thread per water of replica blockIdx.y
+__global__ void __launch_bounds__(128) k_settle(SdmArgs a) {
+    const int r = blockIdx.y;
+    const SdmRep& R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= S.st_count) return;
+    const int* t = a.st_idx + 3 * (size_t)(S.st_base + w);
+    const size_t p[3] = {(size_t)R.x_off + t[0], (size_t)R.x_off + t[1], (size_t)R.x_off + t[2]};
+    const double invdt = a.lv_prm[SDM_LV_INVDT];
+    const double im0 = a.lv_invm[p[0]], im1 = a.lv_invm[p[1]], im2 = a.lv_invm[p[2]];
+    // positions, hydrogens in the minimum image of their oxygen
+    double x0[3][3], x1[3][3], back[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            x0[j][k] = a.lv_x[3 * p[j] + k];
+            x1[j][k] = a.lv_xp[3 * p[j] + k];
+            back[j][k] = 0.0;
+        }
+#pragma unroll
+    for (int j = 1; j < 3; ++j)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            x0[j][k] -= S.box[k] * rint((x0[j][k] - x0[0][k]) * S.invL[k]);
+            const double s1 = S.box[k] * rint((x1[j][k] - x1[0][k]) * S.invL[k]);
+            x1[j][k] -= s1;
+            back[j][k] = s1;   // restores the new position's own image
+        }
+    double P[3][3];
+    if (im0 == 0.0 || im1 == 0.0 || im2 == 0.0) {   // a fixed particle: no constraint
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) P[j][k] = x1[j][k];
+    } else {
+        const double mo = 1.0 / im0, mh = 2.0 / (im1 + im2);
+        const double rc = 0.5 * S.st_dhh;
+        const double hgt = sqrt(fmax(S.st_doh * S.st_doh - rc * rc, 0.0));
+        const double ra = 2.0 * mh * hgt / (mo + 2.0 * mh), rb = hgt - ra;
+        const double invm = 1.0 / (mo + 2.0 * mh);
+        const D3 A0{x0[0][0], x0[0][1], x0[0][2]}, B0{x0[1][0], x0[1][1], x0[1][2]}, C0{x0[2][0], x0[2][1], x0[2][2]};
+        const D3 A1{x1[0][0], x1[0][1], x1[0][2]}, B1{x1[1][0], x1[1][1], x1[1][2]}, C1{x1[2][0], x1[2][1], x1[2][2]};
+        const D3 Dc{(mo * A1.x + mh * (B1.x + C1.x)) * invm, (mo * A1.y + mh * (B1.y + C1.y)) * invm,
+                    (mo * A1.z + mh * (B1.z + C1.z)) * invm};
+        const D3 b0 = d3sub(B0, A0), c0 = d3sub(C0, A0);
+        const D3 a1 = d3sub(A1, Dc), b1 = d3sub(B1, Dc), c1 = d3sub(C1, Dc);
+        const D3 e0 = d3unit(d3cross(b0, c0));
+        const D3 e1 = d3unit(d3cross(a1, e0));
+        const D3 e2 = d3cross(e0, e1);
+        const double xb0 = d3dot(e1, b0), yb0 = d3dot(e2, b0), xc0 = d3dot(e1, c0), yc0 = d3dot(e2, c0);
+        const double za1 = d3dot(e0, a1);
+        const double xb1 = d3dot(e1, b1), yb1 = d3dot(e2, b1), zb1 = d3dot(e0, b1);
+        const double xc1 = d3dot(e1, c1), yc1 = d3dot(e2, c1), zc1 = d3dot(e0, c1);
+        const double sphi = za1 / ra, cphi = sqrt(fmax(1.0 - sphi * sphi, 0.0));
+        const double spsi = (zb1 - zc1) / (2.0 * rc * cphi), cpsi = sqrt(fmax(1.0 - spsi * spsi, 0.0));
+        const double ya2 = ra * cphi;
+        const double xb2 = -rc * cpsi, yb2 = -rb * cphi - rc * spsi * sphi;
+        const double xc2 = rc * cpsi, yc2 = -rb * cphi + rc * spsi * sphi;
+        const double al = xb0 * xb2 + yb0 * yb2 + xc0 * xc2 + yc0 * yc2;
+        const double be = xb0 * yb2 - yb0 * xb2 + xc0 * yc2 - yc0 * xc2;
+        const double ga = xb0 * yb1 - yb0 * xb1 + xc0 * yc1 - yc0 * xc1;
+        const double ab = al * al + be * be;
+        const double sth = (al * ga - be * sqrt(fmax(ab - ga * ga, 0.0))) / ab;
+        const double cth = sqrt(fmax(1.0 - sth * sth, 0.0));
+        const D3 Pa = d3frame(Dc, e1, e2, e0, -ya2 * sth, ya2 * cth, za1);
+        const D3 Pb = d3frame(Dc, e1, e2, e0, xb2 * cth - yb2 * sth, xb2 * sth + yb2 * cth, zb1);
+        const D3 Pc = d3frame(Dc, e1, e2, e0, xc2 * cth - yc2 * sth, xc2 * sth + yc2 * cth, zc1);
+        P[0][0] = Pa.x; P[0][1] = Pa.y; P[0][2] = Pa.z;
+        P[1][0] = Pb.x; P[1][1] = Pb.y; P[1][2] = Pb.z;
+        P[2][0] = Pc.x; P[2][1] = Pc.y; P[2][2] = Pc.z;
+    }
+    const double imj[3] = {im0, im1, im2};
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        if (imj[j] == 0.0) continue;   // fixed: x and v untouched
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            a.lv_v[3 * p[j] + k] = (P[j][k] - x0[j][k]) * invdt;
+            a.lv_x[3 * p[j] + k] = P[j][k] + back[j][k];
         }
     }
 }
@@ -2241,6 +2362,7 @@ cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st) {
     k_finalize<<<a.nrep, 256, 0, st>>>(a);
     if (a.lv_x) {   // Langevin step: the mixed force feeds the update directly
         k_langevin<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
+        if (a.st_any) k_settle<<<dim3((a.st_max + 127) / 128, a.nrep), 128, 0, st>>>(a);
         k_lv_tick<<<1, 1, 0, st>>>(a.lv_prm);
     } else {
         k_mix<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);

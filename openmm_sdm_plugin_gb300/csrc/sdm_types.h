@@ -98,6 +98,9 @@ struct SdmSys {
     int rs_base, rs_nlig, rs_nrcpt;   // offset into rs_idx / rs_w (ligand group, then receptor group), counts
     int rs_prm;                       // offset of the system's SDM_RS_COUNT parameters in rs_prm
     int rs_ref[12];                   // r0 r1 r2 l0 l1 l2 (centroid angles), a0 a1 a2 b0 b1 b2 (alignment)
+    // rigid waters in the Langevin step (sdm_set_rigid_waters)
+    int st_base, st_count;            // offset into st_idx (triples), number of waters
+    double st_doh, st_dhh;            // O-H and H-H distances (nm)
 };
 
 // restraint parameters (doubles per system)
@@ -236,6 +239,12 @@ struct SdmArgs {
     const double* rs_lam;   // per replica: SDMRestraintControlParameter
     double* rs_e;           // per replica: restraint energy of the last evaluation
     int rs_any;             // 1 when some system has restraints
+    // rigid waters (Langevin step)
+    const int* st_idx;      // (O, H, H) system-local indices, every system's waters
+    const int* st_flag;     // per topology particle: 1 in a rigid water
+    double* lv_xp;          // per particle: unconstrained positions of water particles
+    int st_any;             // 1 when some system has rigid waters
+    int st_max;             // largest water count of a system
     int* ncl;            // clusters per replica
     unsigned* extz;      // per replica max cluster z extent (float bits)
     int* work_counter;   // [0] main pass, [1] perturbation pass

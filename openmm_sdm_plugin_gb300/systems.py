@@ -183,6 +183,20 @@ def _random_rotations(rng, k):
         axis=-1).reshape(k, 3, 3)
 
 
+def rigid_waters(s: "SDMSystem"):
+    """(waters (W, 3) O H H indices, d_oh, d_hh) of a synthetic system: its
+    leading particles are 3-site waters of the model geometry (O-H 0.09572 nm,
+    H-O-H 104.52 degrees); W counts the leading (O, H, H) triples, where the
+    hydrogens carry no Lennard-Jones term."""
+    sig = np.asarray(s.epsilon)
+    w = 0
+    while 3 * w + 2 < s.n and sig[3 * w] != 0.0 and sig[3 * w + 1] == 0.0 and sig[3 * w + 2] == 0.0:
+        w += 1
+    waters = np.arange(3 * w, dtype=np.int32).reshape(-1, 3)
+    d_hh = 2.0 * WATER_OH * math.sin(math.radians(WATER_HOH_DEG) / 2)
+    return waters, WATER_OH, d_hh
+
+
 def _water_frame():
     th = math.radians(WATER_HOH_DEG) / 2
     b = WATER_OH

@@ -283,11 +283,59 @@ def langevin_coefficients(step_size, friction, temperature):
     return vscale, fscale, noise
 
 
-def langevin_update(x, v, inv_mass, F, step_size, friction, temperature, normals=None):
+def shake_waters(x_old, xp, inv_mass, waters, d_oh, d_hh, box, tol=1e-13, maxit=200):
+    """Rigid 3-site waters (O, H, H) by SHAKE iterated to convergence: the
+    unconstrained positions xp move along the old bond vectors, mass
+    weighted, until |O-H| = d_oh and |H-H| = d_hh (the constraint step the
+    reference's integrator applies between the position update and the
+    velocity recomputation, ReferenceStochasticDynamicsSDM.cpp:131-266).
+    All waters at once; tol bounds |r^2 - d^2| / d^2 (FP64 coordinates of a
+    few nm round r^2 - d^2 to ~1e-14 of d^2).  Hydrogens are taken in the
+    minimum image of their oxygen and written back in their own image.
+    Waters with a fixed particle are left as they are.  Returns (N, 3)."""
+    x_old = np.asarray(x_old, np.float64).reshape(-1, 3)
+    out = np.array(xp, np.float64).reshape(-1, 3)
+    im = np.asarray(inv_mass, np.float64).reshape(-1)
+    box = np.asarray(box, np.float64)
+    W = np.asarray(waters, np.int64).reshape(-1, 3)
+    W = W[np.all(im[W] != 0.0, axis=1)]
+    if not len(W):
+        return out
+    x0 = x_old[W].copy()          # (nw, 3 atoms, 3)
+    x1 = out[W].copy()
+    shift = np.zeros_like(x1)
+    for j in (1, 2):
+        x0[:, j] = x0[:, 0] + _min_image(x0[:, j] - x0[:, 0], box)
+        u = x1[:, 0] + _min_image(x1[:, j] - x1[:, 0], box)
+        shift[:, j] = x1[:, j] - u
+        x1[:, j] = u
+    m = im[W]                     # (nw, 3) inverse masses
+    cons = ((0, 1, d_oh), (0, 2, d_oh), (1, 2, d_hh))
+    for _ in range(maxit):
+        worst = 0.0
+        for i, j, d in cons:
+            r, r0 = x1[:, i] - x1[:, j], x0[:, i] - x0[:, j]
+            diff = np.einsum("wk,wk->w", r, r) - d * d
+            worst = max(worst, float(np.abs(diff).max()) / (d * d))
+            g = diff / (2.0 * np.einsum("wk,wk->w", r0, r) * (m[:, i] + m[:, j]))
+            x1[:, i] -= (g * m[:, i])[:, None] * r0
+            x1[:, j] += (g * m[:, j])[:, None] * r0
+        if worst < tol:
+            break
+    else:
+        raise RuntimeError(f"SHAKE did not converge ({worst:.2e} after {maxit} iterations)")
+    out[W] = x1 + shift
+    return out
+
+
+def langevin_update(x, v, inv_mass, F, step_size, friction, temperature, normals=None, waters=None,
+                    d_oh=None, d_hh=None, box=None):
     """One stochastic-dynamics step (updatePart1, updatePart2 and the velocity
-    recomputation of ReferenceStochasticDynamicsSDM.cpp:131-266, no
-    constraints), FP64 in the reference's operation order.  x, v, F: (N, 3);
-    inv_mass: (N,); normals: (N, 3) standard normal deviates (None: zeros)."""
+    recomputation of ReferenceStochasticDynamicsSDM.cpp:131-266), FP64 in the
+    reference's operation order.  x, v, F: (N, 3); inv_mass: (N,); normals:
+    (N, 3) standard normal deviates (None: zeros).  With `waters` ((W, 3)
+    O, H, H indices), d_oh, d_hh and box the waters are held rigid
+    (shake_waters) before the velocities are recomputed."""
     vscale, fscale, noise = langevin_coefficients(step_size, friction, temperature)
     x = np.asarray(x, np.float64).reshape(-1, 3)
     v = np.asarray(v, np.float64).reshape(-1, 3)
@@ -297,7 +345,16 @@ def langevin_update(x, v, inv_mass, F, step_size, friction, temperature, normals
     move = (im[:, 0] != 0.0)
     v1 = vscale * v + (fscale * im) * F + (noise * np.sqrt(im)) * n
     xp = x + step_size * v1
-    v2 = (1.0 / step_size) * (xp - x)
+    if waters is not None and len(waters):
+        xp = np.where(move[:, None], xp, x)
+        xp = shake_waters(x, xp, im[:, 0], waters, d_oh, d_hh, box)
+        # a water's unwrapped velocity: (x' - x) of the images the constraint used
+        v2 = (1.0 / step_size) * (xp - x)
+        for w in np.asarray(waters, np.int64).reshape(-1, 3):
+            for j in (1, 2):
+                v2[w[j]] = (1.0 / step_size) * _min_image(xp[w[j]] - x[w[j]], np.asarray(box, np.float64))
+    else:
+        v2 = (1.0 / step_size) * (xp - x)
     xo = np.where(move[:, None], xp, x)
     vo = np.where(move[:, None], v2, v)
     return xo, vo

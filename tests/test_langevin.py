@@ -143,3 +143,84 @@ def test_integrator_mirror_chains_steps_like_the_restated_update():
     assert np.isfinite(integ.getBindE()) and np.isfinite(integ.getPotEnergy())
     integ.close()
     ref.close()
+
+
+def _rigid_setup(nrep=2):
+    s, h, x, v, im, fext, dev = _setup(nrep=nrep)
+    w, d_oh, d_hh = S.rigid_waters(s)
+    # model masses (O 15.999, H 1.008) on the waters, a few ligand particles fixed
+    m = np.full(x.shape[0], 12.011)
+    for r in range(nrep):
+        base = r * s.n
+        m[base + w[:, 0]] = 15.999
+        m[base + w[:, 1]] = m[base + w[:, 2]] = 1.008
+    im = 1.0 / m
+    for r in range(nrep):
+        im[r * s.n + s.n - 5:r * s.n + s.n] = 0.0
+    h.set_rigid_waters(0, w, d_oh, d_hh)
+    return s, h, x, v, im, fext, dev, (w, d_oh, d_hh)
+
+
+def _all_waters(s, w, nrep):
+    return np.concatenate([w + r * s.n for r in range(nrep)])
+
+
+def test_rigid_waters_step_matches_shake_oracle():
+    """T = 0 step with SETTLE on every water of two replicas against the
+    oracle's SHAKE iterated to convergence (the same constraint problem);
+    waters that straddle the box boundary included."""
+    import torch
+    s, h, x, v, im, fext, dev, (w, d_oh, d_hh) = _rigid_setup()
+    ws = _all_waters(s, w, 2)
+    # translate and wrap particle by particle (the physics is unchanged):
+    # waters cut by the box faces now straddle them
+    x = x + np.array([0.5, 0.37, 0.21]) * s.box
+    x = x - s.box * np.floor(x / s.box)
+    straddle = np.abs(x[ws[:, 1:]] - x[ws[:, :1]]).max(axis=(1, 2)) > 0.5 * s.box.min()
+    assert straddle.sum() > 10
+    _, F = h.evaluate(x)
+    h.set_langevin(DT, FRICTION, 0.0, seed=5)
+    xd, vd, imd, fd = dev(x), dev(v), dev(im), dev(fext)
+    rd = torch.zeros((h.nrep, capi.NRESULTS), dtype=torch.float64, device="cuda")
+    h.langevin_step(xd.data_ptr(), vd.data_ptr(), imd.data_ptr(), rd.data_ptr(), 1, fd.data_ptr())
+    torch.cuda.synchronize()
+    xo, vo = oracle.langevin_update(x, v, im, F + fext, DT, FRICTION, 0.0, waters=ws, d_oh=d_oh, d_hh=d_hh,
+                                    box=s.box)
+    xg, vg = xd.cpu().numpy(), vd.cpu().numpy()
+    assert np.abs(xg - xo).max() < 1e-11
+    assert np.abs(vg - vo).max() < 1e-7
+    others = np.setdiff1d(np.arange(x.shape[0]), ws.reshape(-1))
+    assert np.array_equal(xg[others], xo[others]) and np.array_equal(vg[others], vo[others])
+    assert h.check_status() == 0
+
+
+def test_rigid_waters_stay_rigid_over_steps():
+    import torch
+    s, h, x, v, im, fext, dev, (w, d_oh, d_hh) = _rigid_setup()
+    h.set_langevin(DT, FRICTION, 300.0, seed=3)
+    xd, vd, imd = dev(x), dev(v * 0.0), dev(im)
+    rd = torch.zeros((h.nrep, capi.NRESULTS), dtype=torch.float64, device="cuda")
+    h.langevin_step(xd.data_ptr(), vd.data_ptr(), imd.data_ptr(), rd.data_ptr(), 20)
+    torch.cuda.synchronize()
+    xg = xd.cpu().numpy()
+    ws = _all_waters(s, w, 2)
+
+    def dist(i, j):
+        d = xg[ws[:, i]] - xg[ws[:, j]]
+        d -= s.box * np.round(d / s.box)
+        return np.linalg.norm(d, axis=1)
+    assert np.abs(dist(0, 1) - d_oh).max() < 1e-10
+    assert np.abs(dist(0, 2) - d_oh).max() < 1e-10
+    assert np.abs(dist(1, 2) - d_hh).max() < 1e-10
+    assert np.isfinite(rd.cpu().numpy()[:, :14]).all() and h.check_status() == 0
+
+
+def test_rigid_water_input_checks():
+    s, h, *_ = _setup(nrep=1)
+    w, d_oh, d_hh = S.rigid_waters(s)
+    for bad in ((np.array([[0, 1, s.n]]), d_oh, d_hh), (np.array([[0, 1, 2], [2, 3, 4]]), d_oh, d_hh),
+                (w, d_oh, 2.5 * d_oh), (w, -d_oh, d_hh)):
+        with pytest.raises(capi.SdmError):
+            h.set_rigid_waters(0, *bad)
+    h.set_rigid_waters(0, w, d_oh, d_hh)
+    h.set_rigid_waters(0, None)   # removes them
