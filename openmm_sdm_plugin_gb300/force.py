@@ -276,7 +276,9 @@ class LangevinIntegratorSDM(SDMForce):
     per step the two-state evaluation and the stochastic-dynamics update
     (``sdm_langevin_step``, one CUDA graph per step, no host synchronisation).
     Masses come from ``setParticleMass`` (0 holds a particle fixed, as a zero
-    mass does in the reference); constraints are not applied."""
+    mass does in the reference).  Constraints: rigid 3-site waters
+    (``setRigidWaters``, SETTLE on the device); other constraints are not
+    applied."""
 
     def __init__(self, temperature: float, frictionCoeff: float, stepSize: float, nParticles: int = 0):
         self._mass = []
@@ -288,6 +290,8 @@ class LangevinIntegratorSDM(SDMForce):
         self._lv_dirty = True
         self._step_count = 0
         self._x = self._v = self._im = self._res = None
+        self._waters = None          # rigid waters: ((W, 3) O H H, d_oh, d_hh)
+        self._waters_dirty = False
 
     def addParticle(self, charge: float, sigma: float, epsilon: float, mass: float = 1.0) -> int:
         k = super().addParticle(charge, sigma, epsilon)
@@ -309,6 +313,26 @@ class LangevinIntegratorSDM(SDMForce):
     def getStepSize(self): return self._step_size
     def setRandomNumberSeed(self, seed): self._seed = int(seed); self._lv_dirty = True
     def getRandomNumberSeed(self): return self._seed
+
+    def setRigidWaters(self, waters, d_oh: float, d_hh: float):
+        """Holds the (O, H, H) waters rigid in step() (the reference context's
+        constraints on them; SETTLE on the device).  waters: (W, 3) indices or
+        None to remove."""
+        self._waters = None if waters is None else (np.asarray(waters, np.int32).reshape(-1, 3), float(d_oh),
+                                                     float(d_hh))
+        self._waters_dirty = True
+
+    def _sync(self, device: int = 0):
+        rebuilt = self._topology_dirty or self._handle is None
+        super()._sync(device)
+        if rebuilt:
+            self._waters_dirty = self._waters is not None
+        if self._waters_dirty:
+            if self._waters is None:
+                self._handle.set_rigid_waters(0, None)
+            else:
+                self._handle.set_rigid_waters(0, *self._waters)
+            self._waters_dirty = False
 
     def setState(self, positions, velocities=None, device: int = 0):
         """Uploads positions (and velocities, default zero), FP64 (N, 3)."""

@@ -65,3 +65,13 @@ def test_oracle_restraint_terms_closed_forms():
     al = S.Restraints(use_alignment=True, liga_ref=(0, 1, 2), ligb_ref=(3, 4, 5), kf_displ=4.0,
                       k_theta=3.0, k_psi=2.0, align_offset=(0.1, 0.0, 0.0))
     assert oracle.restraint_energy(x, al) == pytest.approx(0.5 * 4.0 * 0.2 ** 2)   # aligned: no theta/psi
+
+
+def test_integrator_mirror_records_rigid_waters():
+    f = LangevinIntegratorSDM(300.0, 1.0, 0.002, nParticles=6)
+    f.setRigidWaters([[0, 1, 2], [3, 4, 5]], 0.09572, 0.1514)
+    w, d_oh, d_hh = f._waters
+    assert w.tolist() == [[0, 1, 2], [3, 4, 5]] and d_oh == 0.09572 and d_hh == 0.1514
+    assert f._waters_dirty
+    f.setRigidWaters(None, 0.0, 0.0)
+    assert f._waters is None and f._waters_dirty
