@@ -224,3 +224,48 @@ def test_rigid_water_input_checks():
             h.set_rigid_waters(0, *bad)
     h.set_rigid_waters(0, w, d_oh, d_hh)
     h.set_rigid_waters(0, None)   # removes them
+
+
+def test_integrator_mirror_rigid_waters():
+    """LangevinIntegratorSDM.setRigidWaters: a T = 0 step of the mirror equals
+    the oracle's update with SHAKE on the same waters, and the waters stay
+    rigid over noisy steps."""
+    from openmm_sdm_plugin_gb300.force import LangevinIntegratorSDM, force_from_system
+    s = S.config2(nrep=1)
+    w, d_oh, d_hh = S.rigid_waters(s)
+    m = np.full(s.n, 12.011)
+    m[w[:, 0]] = 15.999
+    m[w[:, 1]] = m[w[:, 2]] = 1.008
+    ref = force_from_system(s)
+    integ = LangevinIntegratorSDM(0.0, FRICTION, DT)
+    for k, (q, sg, ep) in enumerate(zip(s.charge, s.sigma, s.epsilon)):
+        integ.addParticle(q, sg, ep, mass=m[k])
+    for i, j in s.exclusions:
+        integ.addExclusion(int(i), int(j))
+    integ.setCutoffDistance(s.cutoff)
+    integ.setReactionFieldDielectric(s.eps_rf)
+    integ.setPeriodicBoxVectors((s.box[0], 0, 0), (0, s.box[1], 0), (0, 0, s.box[2]))
+    for i in np.nonzero(np.any(s.displacement != 0, axis=1))[0]:
+        integ.setDisplacement(int(i), *s.displacement[i])
+    integ._p = ref._p
+    integ.setRigidWaters(w, d_oh, d_hh)
+    x = s.positions[0].copy()
+    v = np.random.default_rng(4).normal(scale=0.3, size=x.shape)
+    integ.setState(x, v)
+    integ.step(1)
+    xg, vg = integ.getState()
+    _, F = ref.evaluate(x)
+    xo, vo = oracle.langevin_update(x, v, 1.0 / m, F, DT, FRICTION, 0.0, waters=w, d_oh=d_oh, d_hh=d_hh,
+                                    box=s.box)
+    assert np.abs(xg - xo).max() < 1e-11
+    assert np.abs(vg - vo).max() < 1e-7
+    integ.setTemperature(300.0)
+    integ.step(10)
+    xg, _ = integ.getState()
+    for a, b, d0 in ((0, 1, d_oh), (0, 2, d_oh), (1, 2, d_hh)):
+        d = xg[w[:, a]] - xg[w[:, b]]
+        d -= s.box * np.round(d / s.box)
+        assert np.abs(np.linalg.norm(d, axis=1) - d0).max() < 1e-10
+    assert np.isfinite(integ.getBindE()) and np.isfinite(integ.getPotEnergy())
+    integ.close()
+    ref.close()
