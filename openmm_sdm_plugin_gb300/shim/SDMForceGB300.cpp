@@ -1,0 +1,221 @@
+/*
+ * SDMForceGB300.cpp -- the OpenMM force plugin over libsdm_gb300.so.
+ *
+ * SDMForce copies what the reference reads from the group-2 NonbondedForce
+ * (the particles and exceptions that example/desmonddmsfile75.py:772-850
+ * puts there, the cutoff and the electrostatics of :418-426).  SDMForceImpl
+ * owns one sdm_handle per context: initialize() is the reference kernel's
+ * initialize (platforms/reference/src/ReferenceSDMKernels.cpp:144-159), and
+ * computeForce() is one step's two group-2 evaluations, the state save,
+ * displace and restore (LangevinIntegratorSDM.cpp:158-173) and the combine
+ * of ReferenceSDMKernels.cpp:231-318, in one sdm_evaluate call.
+ */
+#include "SDMForceGB300.h"
+
+#include "openmm/Context.h"
+#include "openmm/OpenMMException.h"
+#include "openmm/internal/ContextImpl.h"
+#include "openmm/internal/CustomCPPForceImpl.h"
+
+#include <cmath>
+#include <string>
+
+namespace SDMPluginGB300 {
+
+using OpenMM::OpenMMException;
+using OpenMM::Vec3;
+
+namespace {
+
+void check(sdm_status st, const sdm_handle* h, const char* what) {
+    if (st != SDM_OK)
+        throw OpenMMException(std::string("SDMForce: ") + what + ": " + sdm_last_error(h));
+}
+
+}  // namespace
+
+SDMForce::SDMForce(const OpenMM::NonbondedForce& nb, int device) : device_(device) {
+    using OpenMM::NonbondedForce;
+    const int n = nb.getNumParticles();
+    charge_.resize(n);
+    sigma_.resize(n);
+    epsilon_.resize(n);
+    for (int i = 0; i < n; ++i) nb.getParticleParameters(i, charge_[i], sigma_[i], epsilon_[i]);
+    displ_.assign(3 * (size_t)n, 0.0);
+    // every exception is an excluded pair; the ones with a charge product or
+    // a well depth interact with their own parameters (the 1-4 pairs)
+    for (int e = 0; e < nb.getNumExceptions(); ++e) {
+        int i, j;
+        double qq, sg, ep;
+        nb.getExceptionParameters(e, i, j, qq, sg, ep);
+        exclusions_.push_back(i);
+        exclusions_.push_back(j);
+        if (qq != 0.0 || ep != 0.0) {
+            exception_pairs_.push_back(i);
+            exception_pairs_.push_back(j);
+            exception_params_.push_back(qq);
+            exception_params_.push_back(sg);
+            exception_params_.push_back(ep);
+        }
+    }
+    cutoff_ = nb.getCutoffDistance();
+    eps_rf_ = nb.getReactionFieldDielectric();
+    ewald_tol_ = nb.getEwaldErrorTolerance();
+    pme_grid_[0] = pme_grid_[1] = pme_grid_[2] = 0;
+    switch (nb.getNonbondedMethod()) {
+        case NonbondedForce::CutoffPeriodic: method_ = SDM_NB_REACTION_FIELD; break;
+        case NonbondedForce::PME: {
+            method_ = SDM_NB_PME;
+            double alpha;
+            int nx, ny, nz;
+            nb.getPMEParameters(alpha, nx, ny, nz);
+            // the library derives the splitting parameter from the tolerance
+            // (OpenMM's rule); an explicit alpha would be a different model
+            if (alpha != 0.0)
+                throw OpenMMException("SDMForce: explicit PME parameters are not supported; "
+                                      "set the Ewald error tolerance instead");
+            break;
+        }
+        default:
+            throw OpenMMException("SDMForce: the NonbondedForce must use CutoffPeriodic (reaction field) or PME");
+    }
+    if (nb.getUseDispersionCorrection())
+        throw OpenMMException("SDMForce: the NonbondedForce must have setUseDispersionCorrection(false)");
+    if (nb.getUseSwitchingFunction())
+        throw OpenMMException("SDMForce: switching functions are not supported");
+    // reference integrator defaults (LangevinIntegratorSDM.cpp:56-75)
+    for (double& v : p_) v = 0.0;
+    p_[SDM_P_BIAS_METHOD] = LinearMethod;
+    p_[SDM_P_SOFTCORE_METHOD] = NoSoftCoreMethod;
+    p_[SDM_P_LAMBDA] = 1.0;
+    p_[SDM_P_WB] = 1.0;
+    p_[SDM_P_LAMBDA1] = 1.0;
+    p_[SDM_P_LAMBDA2] = 1.0;
+    p_[SDM_P_ALPHA] = 1.0;
+    p_[SDM_P_UMAX] = 200.0;
+    p_[SDM_P_ACORE] = 0.25;
+    setForceGroup(2);
+}
+
+void SDMForce::setDisplacement(int atom, double dx, double dy, double dz) {
+    if (atom < 0 || atom >= getNumParticles()) throw OpenMMException("SDMForce: particle index out of range");
+    displ_[3 * (size_t)atom + 0] = dx;
+    displ_[3 * (size_t)atom + 1] = dy;
+    displ_[3 * (size_t)atom + 2] = dz;
+}
+
+Vec3 SDMForce::getDisplacement(int atom) const {
+    if (atom < 0 || atom >= getNumParticles()) throw OpenMMException("SDMForce: particle index out of range");
+    const double* d = &displ_[3 * (size_t)atom];
+    return Vec3(d[0], d[1], d[2]);
+}
+
+sdm_system_desc SDMForce::describe(const double box[3]) const {
+    sdm_system_desc d = {};
+    d.num_particles = getNumParticles();
+    d.charge = charge_.data();
+    d.sigma = sigma_.data();
+    d.epsilon = epsilon_.data();
+    d.num_exclusions = (int)(exclusions_.size() / 2);
+    d.exclusions = exclusions_.data();
+    d.displacement = displ_.data();
+    for (int k = 0; k < 3; ++k) d.box[k] = box[k];
+    d.cutoff = cutoff_;
+    d.reaction_field_dielectric = eps_rf_;
+    d.num_replicas = 1;
+    d.num_exceptions = (int)(exception_params_.size() / 3);
+    d.exception_pairs = exception_pairs_.data();
+    d.exception_params = exception_params_.data();
+    d.nonbonded_method = method_;
+    d.ewald_tolerance = ewald_tol_;
+    for (int k = 0; k < 3; ++k) d.pme_grid[k] = pme_grid_[k];
+    return d;
+}
+
+/* One sdm_handle per context.  The box is fixed at handle creation; a
+ * context whose box changes (a barostat) gets a new handle. */
+class SDMForceImpl : public OpenMM::CustomCPPForceImpl {
+public:
+    explicit SDMForceImpl(const SDMForce& owner) : OpenMM::CustomCPPForceImpl(owner), owner_(owner) {
+        for (double& v : res_) v = 0.0;
+    }
+    ~SDMForceImpl() override { sdm_destroy(h_); }
+
+    void initialize(OpenMM::ContextImpl& context) override {
+        OpenMM::CustomCPPForceImpl::initialize(context);
+        if (context.getSystem().getNumParticles() != owner_.getNumParticles())
+            throw OpenMMException("SDMForce: particle count differs from the System's");
+        for (int k = 0; k < SDM_NPARAMS; ++k) p_[k] = owner_.p_[k];
+        displ_ = owner_.displ_;
+        create(context);
+    }
+
+    double computeForce(OpenMM::ContextImpl& context, const std::vector<Vec3>& positions,
+                        std::vector<Vec3>& forces) override {
+        double box[3];
+        box_of(context, box);
+        if (box[0] != box_[0] || box[1] != box_[1] || box[2] != box_[2]) create(context);
+        const size_t n = positions.size();
+        x_.resize(3 * n);
+        f_.resize(3 * n);
+        for (size_t i = 0; i < n; ++i) {
+            x_[3 * i + 0] = positions[i][0];
+            x_[3 * i + 1] = positions[i][1];
+            x_[3 * i + 2] = positions[i][2];
+        }
+        check(sdm_evaluate(h_, x_.data(), res_, f_.data()), h_, "evaluation failed");
+        forces.resize(n);
+        for (size_t i = 0; i < n; ++i) forces[i] = Vec3(f_[3 * i + 0], f_[3 * i + 1], f_[3 * i + 2]);
+        return res_[SDM_R_EPOT];
+    }
+
+    void updateParametersInContext(const SDMForce& f) {
+        check(sdm_set_params(h_, 0, f.p_), h_, "invalid SDM parameters");
+        check(sdm_set_displacement(h_, 0, f.displ_.data()), h_, "invalid displacement");
+        for (int k = 0; k < SDM_NPARAMS; ++k) p_[k] = f.p_[k];
+        displ_ = f.displ_;
+    }
+
+    const double* results() const { return res_; }
+
+private:
+    static void box_of(OpenMM::ContextImpl& context, double box[3]) {
+        Vec3 a, b, c;
+        context.getPeriodicBoxVectors(a, b, c);
+        if (a[1] != 0.0 || a[2] != 0.0 || b[0] != 0.0 || b[2] != 0.0 || c[0] != 0.0 || c[1] != 0.0)
+            throw OpenMMException("SDMForce: the periodic box must be rectangular");
+        box[0] = a[0];
+        box[1] = b[1];
+        box[2] = c[2];
+    }
+
+    void create(OpenMM::ContextImpl& context) {
+        box_of(context, box_);
+        sdm_destroy(h_);
+        h_ = nullptr;
+        sdm_system_desc d = owner_.describe(box_);
+        d.displacement = displ_.data();
+        check(sdm_create(&d, 1, owner_.device_, &h_), nullptr, "sdm_create failed");
+        check(sdm_set_params(h_, 0, p_), h_, "invalid SDM parameters");
+    }
+
+    const SDMForce& owner_;
+    sdm_handle* h_ = nullptr;
+    double box_[3] = {0.0, 0.0, 0.0};
+    double p_[SDM_NPARAMS];
+    double res_[SDM_NRESULTS];
+    std::vector<double> displ_, x_, f_;
+};
+
+OpenMM::ForceImpl* SDMForce::createImpl() const { return new SDMForceImpl(*this); }
+
+void SDMForce::updateParametersInContext(OpenMM::Context& context) {
+    dynamic_cast<SDMForceImpl&>(getImplInContext(context)).updateParametersInContext(*this);
+}
+
+std::vector<double> SDMForce::getResults(OpenMM::Context& context) {
+    const double* r = dynamic_cast<SDMForceImpl&>(getImplInContext(context)).results();
+    return std::vector<double>(r, r + SDM_NRESULTS);
+}
+
+}  // namespace SDMPluginGB300

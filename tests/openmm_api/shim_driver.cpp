@@ -1,0 +1,148 @@
+// Test driver of the GB300 force plugin through the OpenMM API subset.
+//
+//   shim_driver describe <input> <output>   SDMForce::describe() of the input system
+//   shim_driver evaluate <input> <output>   a Context holding the force: energy, forces and
+//                                           results; then lambda1 += 0.1 through
+//                                           updateParametersInContext and again
+//
+// Input (little-endian): int32 n, n_exceptions, method (OpenMM NonbondedMethod),
+// dispersion_correction; float64 box[3], cutoff, eps_rf, ewald_tol,
+// params[SDM_NPARAMS], charge[n], sigma[n], epsilon[n], displacement[3n],
+// positions[3n], exceptions[n_exceptions][5] (i, j, charge product, sigma, epsilon).
+// An OpenMMException prints its message on stderr and exits with status 3.
+#include "SDMForceGB300.h"
+#include "openmm/Context.h"
+#include "openmm/System.h"
+
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+using namespace OpenMM;
+
+namespace {
+
+struct Reader {
+    FILE* f;
+    template <class T> T one() {
+        T v;
+        if (fread(&v, sizeof(T), 1, f) != 1) throw std::runtime_error("short input");
+        return v;
+    }
+    std::vector<double> many(size_t k) {
+        std::vector<double> v(k);
+        if (k && fread(v.data(), sizeof(double), k, f) != k) throw std::runtime_error("short input");
+        return v;
+    }
+};
+
+template <class T> void put(FILE* f, const T* p, size_t k) { fwrite(p, sizeof(T), k, f); }
+
+int run(const std::string& mode, const char* in_path, const char* out_path) {
+    FILE* fi = fopen(in_path, "rb");
+    if (!fi) throw std::runtime_error("cannot open input");
+    Reader r{fi};
+    const int n = r.one<int>(), nx = r.one<int>(), method = r.one<int>(), disp = r.one<int>();
+    std::vector<double> box = r.many(3);
+    const double cutoff = r.one<double>(), eps_rf = r.one<double>(), tol = r.one<double>();
+    std::vector<double> params = r.many(SDM_NPARAMS), q = r.many(n), sig = r.many(n), eps = r.many(n);
+    std::vector<double> d = r.many(3 * (size_t)n), x = r.many(3 * (size_t)n), ex = r.many(5 * (size_t)nx);
+    fclose(fi);
+
+    NonbondedForce nb;
+    for (int i = 0; i < n; ++i) nb.addParticle(q[i], sig[i], eps[i]);
+    for (int e = 0; e < nx; ++e)
+        nb.addException((int)ex[5 * e], (int)ex[5 * e + 1], ex[5 * e + 2], ex[5 * e + 3], ex[5 * e + 4]);
+    nb.setNonbondedMethod((NonbondedForce::NonbondedMethod)method);
+    nb.setCutoffDistance(cutoff);
+    nb.setReactionFieldDielectric(eps_rf);
+    nb.setEwaldErrorTolerance(tol);
+    nb.setUseDispersionCorrection(disp != 0);
+
+    auto* force = new SDMPluginGB300::SDMForce(nb);
+    force->setBiasMethod((int)params[SDM_P_BIAS_METHOD]);
+    force->setSoftCoreMethod((int)params[SDM_P_SOFTCORE_METHOD]);
+    force->setLambda(params[SDM_P_LAMBDA]);
+    force->setLambda1(params[SDM_P_LAMBDA1]);
+    force->setLambda2(params[SDM_P_LAMBDA2]);
+    force->setAlpha(params[SDM_P_ALPHA]);
+    force->setU0(params[SDM_P_U0]);
+    force->setW0coeff(params[SDM_P_W0]);
+    force->setGamma(params[SDM_P_GAMMA]);
+    force->setWBcoeff(params[SDM_P_WB]);
+    force->setUmax(params[SDM_P_UMAX]);
+    force->setAcore(params[SDM_P_ACORE]);
+    force->setUbcore(params[SDM_P_UBCORE]);
+    force->setNonEquilibrium((int)params[SDM_P_NONEQ]);
+    force->setlambda1Slope(params[SDM_P_M_LAMBDA1]);
+    force->setlambda2Slope(params[SDM_P_M_LAMBDA2]);
+    force->setu0Slope(params[SDM_P_M_U0]);
+    force->setw0Slope(params[SDM_P_M_W0]);
+    force->setlambda1intercept(params[SDM_P_B_LAMBDA1]);
+    force->setlambda2intercept(params[SDM_P_B_LAMBDA2]);
+    force->setu0intercept(params[SDM_P_B_U0]);
+    force->setw0intercept(params[SDM_P_B_W0]);
+    for (int i = 0; i < n; ++i)
+        if (d[3 * i] != 0.0 || d[3 * i + 1] != 0.0 || d[3 * i + 2] != 0.0)
+            force->setDisplacement(i, d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+
+    FILE* fo = fopen(out_path, "wb");
+    if (!fo) throw std::runtime_error("cannot open output");
+    if (mode == "describe") {
+        sdm_system_desc s = force->describe(box.data());
+        int counts[4] = {s.num_exclusions, s.num_exceptions, s.nonbonded_method, force->getForceGroup()};
+        put(fo, counts, 4);
+        put(fo, s.exclusions, 2 * (size_t)s.num_exclusions);
+        put(fo, s.exception_pairs, 2 * (size_t)s.num_exceptions);
+        put(fo, s.exception_params, 3 * (size_t)s.num_exceptions);
+        put(fo, s.displacement, 3 * (size_t)n);
+        const double scal[4] = {s.cutoff, s.reaction_field_dielectric, s.ewald_tolerance, s.box[0] + s.box[1] + s.box[2]};
+        put(fo, scal, 4);
+        put(fo, force->getParameterBlock(), SDM_NPARAMS);
+        fclose(fo);
+        delete force;
+        return 0;
+    }
+    System system;
+    for (int i = 0; i < n; ++i) system.addParticle(12.0);
+    system.setDefaultPeriodicBoxVectors(Vec3(box[0], 0, 0), Vec3(0, box[1], 0), Vec3(0, 0, box[2]));
+    system.addForce(force);
+    std::vector<Vec3> pos(n);
+    for (int i = 0; i < n; ++i) pos[i] = Vec3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+    Context context(system);
+    context.setPositions(pos);
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {
+            force->setLambda1(force->getLambda1() + 0.1);
+            force->updateParametersInContext(context);
+        }
+        State st = context.getState(State::Energy | State::Forces, false, 1 << 2);
+        const double e = st.getPotentialEnergy();
+        std::vector<double> res = force->getResults(context);
+        put(fo, &e, 1);
+        put(fo, res.data(), res.size());
+        for (const Vec3& f : st.getForces()) {
+            const double v[3] = {f[0], f[1], f[2]};
+            put(fo, v, 3);
+        }
+    }
+    fclose(fo);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc != 4) {
+        fprintf(stderr, "usage: shim_driver describe|evaluate <input> <output>\n");
+        return 2;
+    }
+    try {
+        return run(argv[1], argv[2], argv[3]);
+    } catch (const OpenMMException& e) {
+        fprintf(stderr, "%s\n", e.what());
+        return 3;
+    }
+}

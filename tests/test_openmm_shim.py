@@ -1,0 +1,174 @@
+"""The OpenMM force plugin (openmm_sdm_plugin_gb300/shim, SDMPluginGB300::
+SDMForce) compiled against the OpenMM API subset of tests/openmm_api and
+linked with libsdm_gb300.so.
+
+CPU: what the plugin reads from a NonbondedForce (exclusions from every
+exception, interacting exceptions with their parameters, method, cutoff,
+reaction-field dielectric, Ewald tolerance; the reference integrator's
+parameter defaults), the models it refuses, and a clean OpenMMException
+when no GPU is present.  GPU: energy, forces and results through a Context
+equal the C ABI's evaluation of the same system bit for bit, before and
+after updateParametersInContext."""
+import dataclasses
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from openmm_sdm_plugin_gb300 import capi, systems as S
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+API = os.path.join(ROOT, "tests", "openmm_api")
+SHIM = os.path.join(ROOT, "openmm_sdm_plugin_gb300", "shim")
+METHODS = {"rf": 2, "pme": 4}   # OpenMM NonbondedForce::CutoffPeriodic, ::PME
+P_LAMBDA1 = 3                   # SDM_P_LAMBDA1
+
+
+@pytest.fixture(scope="module")
+def driver(built_lib, tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("shim") / "shim_driver")
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-Wno-unused-parameter",
+           "-I", API, "-I", os.path.join(ROOT, "include"), "-I", SHIM,
+           os.path.join(SHIM, "SDMForceGB300.cpp"), os.path.join(API, "ApiSubset.cpp"),
+           os.path.join(API, "shim_driver.cpp"), "-o", exe, built_lib,
+           "-Wl,-rpath," + os.path.dirname(built_lib)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def openmm_exceptions(s):
+    """The exception list of the NonbondedForce the reference builds for s:
+    every excluded pair once, with its own parameters where it interacts
+    (zero charge product and well depth otherwise)."""
+    own = {}
+    if s.exceptions is not None:
+        for (i, j), prm in zip(np.asarray(s.exceptions).reshape(-1, 2), np.asarray(s.exception_params).reshape(-1, 3)):
+            own[(min(i, j), max(i, j))] = prm
+    ex = []
+    for i, j in np.asarray(s.exclusions).reshape(-1, 2):
+        qq, sg, ep = own.get((min(i, j), max(i, j)), (0.0, 1.0, 0.0))
+        ex.append((i, j, qq, sg, ep))
+    return np.array(ex, np.float64).reshape(-1, 5)
+
+
+def write_input(path, s, p, x, method=None, dispersion=False):
+    ex = openmm_exceptions(s)
+    m = METHODS[s.nonbonded_method] if method is None else method
+    with open(path, "wb") as f:
+        np.array([s.n, ex.shape[0], m, int(dispersion)], np.int32).tofile(f)
+        np.array([*s.box, s.cutoff, s.eps_rf, s.ewald_tolerance], np.float64).tofile(f)
+        for a in (p.as_array(), s.charge, s.sigma, s.epsilon, s.displacement, x, ex):
+            np.ascontiguousarray(a, np.float64).reshape(-1).tofile(f)
+
+
+def run(driver, mode, tmp_path, s, p, x, **kw):
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    write_input(inp, s, p, x, **kw)
+    r = subprocess.run([driver, mode, inp, out], capture_output=True, text=True, timeout=300)
+    return r, out
+
+
+def _dms_system():
+    from openmm_sdm_plugin_gb300 import dms
+    p = S.SDMParams(bias_method=S.ILOGISTIC, softcore_method=S.RATIONAL_SOFTCORE, lambda1=0.3, lambda2=0.6,
+                    alpha=0.05, u0=10.0, w0=1.0, umax=50.0, acore=0.25, ubcore=10.0)
+    return dms.load_compact(os.path.join(ROOT, "tests", "golden", "temoa_g1_g4.npz"),
+                            displacement={2: (2.2, 2.2, 2.2), 3: (-2.2, -2.2, -2.2)}, params=[p])
+
+
+def test_describe_copies_the_nonbonded_force(driver, tmp_path):
+    s = _dms_system()
+    p = s.params[0]
+    r, out = run(driver, "describe", tmp_path, s, p, s.positions[0])
+    assert r.returncode == 0, r.stderr
+    b = open(out, "rb").read()
+    ne, nx, method, group = np.frombuffer(b[:16], np.int32)
+    o = 16
+    excl = np.frombuffer(b[o:o + 8 * ne], np.int32).reshape(-1, 2); o += 8 * ne
+    pairs = np.frombuffer(b[o:o + 8 * nx], np.int32).reshape(-1, 2); o += 8 * nx
+    rest = np.frombuffer(b[o:], np.float64)
+    prm, rest = rest[:3 * nx].reshape(-1, 3), rest[3 * nx:]
+    displ, rest = rest[:3 * s.n].reshape(-1, 3), rest[3 * s.n:]
+    cutoff, eps_rf, tol, boxsum = rest[:4]
+    params = rest[4:]
+    assert group == 2 and method == capi.NB_REACTION_FIELD
+    assert np.array_equal(excl, s.exclusions)
+    ex = openmm_exceptions(s)
+    live = (ex[:, 2] != 0) | (ex[:, 4] != 0)
+    assert nx == live.sum() == len(s.exceptions)
+    assert np.array_equal(pairs, ex[live, :2].astype(np.int32))
+    assert np.array_equal(prm, ex[live, 2:])
+    assert np.array_equal(displ, s.displacement)
+    assert (cutoff, eps_rf, tol, boxsum) == (s.cutoff, s.eps_rf, s.ewald_tolerance, s.box.sum())
+    assert np.array_equal(params, p.as_array())
+
+
+def test_defaults_are_the_reference_integrators(driver, tmp_path):
+    """Parameters left unset keep LangevinIntegratorSDM's constructor defaults
+    (LangevinIntegratorSDM.cpp:56-75): the driver sets every one, so a system
+    written with the defaults must read back unchanged."""
+    s = S.config0(variant="b")
+    p = S.SDMParams(bias_method=S.LINEAR, softcore_method=S.NO_SOFTCORE, lambdac=1.0, lambda1=1.0, lambda2=1.0,
+                    alpha=1.0, u0=0.0, w0=0.0, gamma=0.0, wb=1.0, umax=200.0, acore=0.25, ubcore=0.0)
+    r, out = run(driver, "describe", tmp_path, s, p, s.positions[0])
+    assert r.returncode == 0, r.stderr
+    params = np.frombuffer(open(out, "rb").read(), np.float64)[-capi.NPARAMS:]
+    assert np.array_equal(params, p.as_array())
+
+
+@pytest.mark.parametrize("kw,msg", [(dict(method=0), "CutoffPeriodic"), (dict(method=3), "CutoffPeriodic"),
+                                    (dict(dispersion=True), "DispersionCorrection")])
+def test_refuses_other_models(driver, tmp_path, kw, msg):
+    s = S.config0(variant="b")
+    r, _ = run(driver, "describe", tmp_path, s, s.params[0], s.positions[0], **kw)
+    assert r.returncode == 3 and msg in r.stderr, r.stderr
+
+
+def test_no_gpu_raises_openmm_exception(driver, tmp_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    s = S.config0(variant="b")
+    r, _ = run(driver, "evaluate", tmp_path, s, s.params[0], s.positions[0])
+    assert r.returncode == 3 and "sdm_create failed" in r.stderr, r.stderr
+
+
+def _reference_order(s):
+    """s with its exceptions in the plugin's order (exclusion order), so that
+    the C ABI sums the exception terms in the same order."""
+    ex = openmm_exceptions(s)
+    live = (ex[:, 2] != 0) | (ex[:, 4] != 0)
+    if not live.any():
+        return s
+    return dataclasses.replace(s, exceptions=ex[live, :2].astype(np.int32), exception_params=ex[live, 2:].copy())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which", ["config0", "temoa", "config0_pme"])
+def test_context_evaluation_equals_the_c_abi(driver, tmp_path, which):
+    if which == "temoa":
+        s = _dms_system()
+    else:
+        s = S.config0(variant="b").replica(0)
+        if which == "config0_pme":
+            s = dataclasses.replace(s, nonbonded_method="pme", ewald_tolerance=5e-4)
+    p = s.params[0]
+    x = s.positions[0]
+    r, out = run(driver, "evaluate", tmp_path, s, p, x)
+    assert r.returncode == 0, r.stderr
+    got = np.frombuffer(open(out, "rb").read(), np.float64).reshape(2, -1)
+    ref = _reference_order(s)
+    h = capi.Handle([ref])
+    for k, lam1_shift in enumerate((0.0, 0.1)):
+        a = p.as_array().copy()
+        a[P_LAMBDA1] += lam1_shift
+        h.set_params(0, a)
+        res, F = h.evaluate(x)
+        e, rr, ff = got[k, 0], got[k, 1:1 + capi.NRESULTS], got[k, 1 + capi.NRESULTS:].reshape(-1, 3)
+        assert e == res[0, capi.R_EPOT]
+        assert np.array_equal(rr, res[0])
+        assert np.array_equal(ff, F.reshape(-1, 3))
+    assert got[1, 1 + capi.R_L1] != got[0, 1 + capi.R_L1]
+    h.close()
