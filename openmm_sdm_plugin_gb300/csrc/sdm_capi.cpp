@@ -1144,6 +1144,10 @@ static sdm_status upload_restraints(sdm_handle* h) {
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
     if (h->rs_buf) { cudaFree(h->rs_buf); h->rs_buf = nullptr; }
+    // no kernel may see the freed buffer if the allocation below fails
+    h->args.rs_prm = h->args.rs_w = nullptr;
+    h->args.rs_idx = nullptr;
+    h->args.rs_any = 0;
     const size_t nd = prm.size() + w.size();
     SDM_CUDA(h, cudaMalloc(&h->rs_buf, nd * sizeof(double) + idx.size() * sizeof(int) + 16));
     double* dp = static_cast<double*>(h->rs_buf);
@@ -1275,6 +1279,10 @@ static sdm_status upload_rigid_waters(sdm_handle* h) {
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
     if (h->st_buf) { cudaFree(h->st_buf); h->st_buf = nullptr; }
+    // no kernel may see the freed buffer if the allocation below fails
+    h->args.lv_xp = nullptr;
+    h->args.st_idx = h->args.st_flag = nullptr;
+    h->args.st_any = h->args.st_max = 0;
     const size_t nxp = 3 * (size_t)h->total_particles;
     SDM_CUDA(h, cudaMalloc(&h->st_buf, nxp * sizeof(double) + (idx.size() + flag.size()) * sizeof(int) + 16));
     double* xp = static_cast<double*>(h->st_buf);
