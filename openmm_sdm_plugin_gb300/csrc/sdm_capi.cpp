@@ -164,6 +164,8 @@ struct sdm_handle {
     std::vector<long long> pme_grid_off, pme_spec_off;
 };
 
+static sdm_status sdm_reserve_lists(sdm_handle* h, int cap);
+
 namespace {
 
 const char* const kKernelNames[] = {"k_cells", "k_scan", "k_bucket", "k_cellsort", "k_clusters",
@@ -670,6 +672,10 @@ sdm_status flush_langevin(sdm_handle* h, cudaStream_t st) {
 
 sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStream_t st, int mode,
                bool allow_graph, const LvBind* lv = nullptr) {
+    if (!h->jl_buf) {   // a failed regrow left no lists: allocate the last capacity again
+        sdm_status s0 = sdm_reserve_lists(h, h->jl_cap);
+        if (s0) return s0;
+    }
     SdmArgs a = h->args;
     a.x = x;
     a.results = res;
@@ -749,7 +755,12 @@ static sdm_status sdm_reserve_lists(sdm_handle* h, int cap) {
     if (h->jl_buf) { cudaFree(h->jl_buf); h->jl_buf = nullptr; }
     const size_t bytes = (size_t)h->jl_clusters * (size_t)cap * sizeof(int4);
     cudaError_t ce = cudaMalloc(&h->jl_buf, bytes);
-    if (ce != cudaSuccess) { h->jl_buf = nullptr; return cuda_fail(h, ce, "cudaMalloc(cluster-pair lists)"); }
+    if (ce != cudaSuccess) {
+        // jl_cap keeps the last capacity that was allocated; run() retries it
+        h->jl_buf = nullptr;
+        h->args.jl = nullptr;
+        return cuda_fail(h, ce, "cudaMalloc(cluster-pair lists)");
+    }
     h->jl_cap = cap;
     h->args.jl = h->jl_buf;
     h->args.jl_cap = cap;
