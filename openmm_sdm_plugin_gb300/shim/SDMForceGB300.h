@@ -119,6 +119,15 @@ public:
     double getBindE(OpenMM::Context& context) { return getResults(context)[SDM_R_BINDE]; }
     /* U0 + W: the reference's getPotEnergy() without the group-1 energy. */
     double getPotEnergy(OpenMM::Context& context) { return getResults(context)[SDM_R_EPOT]; }
+    /* u, U0, U1, W and W' of the context's last evaluation. */
+    void getPerturbationEnergy(OpenMM::Context& context, double& u, double& u0, double& u1, double& w, double& dw) {
+        const std::vector<double> r = getResults(context);
+        u = r[SDM_R_U];
+        u0 = r[SDM_R_U0];
+        u1 = r[SDM_R_U1];
+        w = r[SDM_R_W];
+        dw = r[SDM_R_DW];
+    }
 
     /* The system descriptor handed to sdm_create for a box (a, b, c diagonal);
      * the pointers stay valid while this force lives and is not modified. */
