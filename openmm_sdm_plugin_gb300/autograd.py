@@ -20,13 +20,12 @@ is the exact derivative of the integrated logistic bias.
 from __future__ import annotations
 
 import math
-from typing import Optional
 
 import numpy as np
 import torch
 
 from . import capi
-from .systems import ILOGISTIC, LINEAR, QUADRATIC, SDMParams, SDMSystem
+from .systems import ILOGISTIC, QUADRATIC, SDMParams, SDMSystem
 
 
 def bias_partials(p: SDMParams, be: float) -> dict:

@@ -10,7 +10,6 @@ coordinates.  Each call is one evaluation of all replicas (device buffers).
 from __future__ import annotations
 
 import argparse
-import ctypes as C
 import dataclasses
 
 import numpy as np

@@ -7,8 +7,6 @@ array shared by every call, so this test calls it twice in a row and checks
 both results against sdm_evaluate on the same inputs, with the tolerances of
 the other parity tests.  This file is collected last on purpose.
 """
-import ctypes as C
-
 import numpy as np
 import pytest
 
