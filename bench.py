@@ -138,6 +138,21 @@ def cpu_baseline_port(sysm, nthreads: int, budget_s: float = 10.0):
     return n / dt, n, dt
 
 
+def cpu_baselines(sysm, budget_s: float = 10.0, budget_small_s: float = 2.0):
+    """The cpu_baseline object: the FP64 oracle on one host core, on whole
+    lambda states of one 22,580-particle replica of the workload (`value`),
+    with the 930-site system timed beside it (`per_config`)."""
+    from openmm_sdm_plugin_gb300 import systems as S
+    v1, n1, dt1 = cpu_baseline_port(sysm.replica(0), nthreads=1, budget_s=budget_s)
+    s0 = S.config0(variant="b")
+    v0, n0, dt0 = cpu_baseline_port(s0, nthreads=1, budget_s=budget_small_s)
+    return {"value": v1, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n1} FP64 lambda-state evaluations of one 22,580-particle replica in {dt1:.1f} s",
+            "per_config": {
+                "config1_22580": {"value": v1, "unit": UNIT, "sample": f"{n1} states in {dt1:.1f} s"},
+                "config0_930": {"value": v0, "unit": UNIT, "sample": f"{n0} states of {s0.n} sites in {dt0:.1f} s"}}}
+
+
 def run_reference(args):
     """--impl reference: the reference path's CPU implementation on the host cores.
 
@@ -478,9 +493,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v1, nst, dt = cpu_baseline_port(sysm.replica(0), nthreads=1, budget_s=10.0)
-        cpu = {"value": v1, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{nst} FP64 lambda-state evaluations of one 22,580-particle replica in {dt:.1f} s"}
+        cpu = cpu_baselines(sysm)
 
     h2d = xh.nbytes
     d2h = xh.nbytes + NREP * capi.NRESULTS * 8

@@ -60,3 +60,15 @@ def test_two_gloo_ranks_replicas_only():
     assert d0[2] == pytest.approx(3 * world / d0[1])
     # the ranks evaluated different replicas (independent work)
     assert d0[3] != d1[3]
+
+
+def test_cpu_baselines_object(oracle_lib):
+    """The bench line's cpu_baseline object: one host core, the oracle port,
+    a value per config, samples named."""
+    import bench
+    from openmm_sdm_plugin_gb300 import systems as S
+    c = bench.cpu_baselines(S.config2(2), budget_s=0.01, budget_small_s=0.01)
+    assert c["kind"] == "port" and c["cores"] == 1 and c["unit"] == bench.UNIT
+    assert c["value"] > 0 and c["value"] == c["per_config"]["config1_22580"]["value"]
+    assert c["per_config"]["config0_930"]["value"] > c["value"]
+    assert "930 sites" in c["per_config"]["config0_930"]["sample"]
