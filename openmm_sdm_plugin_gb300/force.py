@@ -289,6 +289,7 @@ class LangevinIntegratorSDM(SDMForce):
         self._seed = 0
         self._lv_dirty = True
         self._step_count = 0
+        self._time = 0.0             # ps, the context time of the reference integrator
         self._x = self._v = self._im = self._res = None
         self._waters = None          # rigid waters: ((W, 3) O H H, d_oh, d_hh)
         self._waters_dirty = False
@@ -313,6 +314,8 @@ class LangevinIntegratorSDM(SDMForce):
     def getStepSize(self): return self._step_size
     def setRandomNumberSeed(self, seed): self._seed = int(seed); self._lv_dirty = True
     def getRandomNumberSeed(self): return self._seed
+    def setTime(self, t): self._time = float(t)
+    def getTime(self): return self._time
 
     def setRigidWaters(self, waters, d_oh: float, d_hh: float):
         """Holds the (O, H, H) waters rigid in step() (the reference context's
@@ -352,9 +355,29 @@ class LangevinIntegratorSDM(SDMForce):
         return self._x.cpu().numpy(), self._v.cpu().numpy()
 
     def step(self, steps: int = 1):
-        import torch
+        """Advances `steps` steps.  With setNonEquilibrium(1) each step is one
+        call, as in the reference kernel (ReferenceSDMKernels.cpp:229-245,
+        289-302): lambda = t / Ntmax at the start of the step, lambda1,
+        lambda2, u0 and w0 of the schedule written back, and the work value
+        raised by (dt / Ntmax) dW/dlambda."""
         if self._x is None:
             raise RuntimeError("setState first")
+        if int(self._p.noneq) != 1:
+            self._advance(int(steps))
+            return
+        if not self._ntmax > 0.0:
+            raise ValueError("non-equilibrium steps need setNoneqtmax(t) with t > 0")
+        for _ in range(int(steps)):
+            self._p.lambdac = self._time / self._ntmax
+            self._params_dirty = True
+            r = self._advance(1)
+            self._p.lambda1, self._p.lambda2 = float(r[capi.R_L1]), float(r[capi.R_L2])
+            self._p.u0, self._p.w0 = float(r[capi.R_U0P]), float(r[capi.R_W0P])
+            self._work += self._step_size / self._ntmax * float(r[capi.R_DWDL])
+
+    def _advance(self, steps: int):
+        """`steps` fused steps on the device; returns the results of the last."""
+        import torch
         self._sync(self._x.device.index or 0)
         if self._im is None:
             m = np.asarray(self._mass[:len(self._q)], np.float64)
@@ -368,10 +391,12 @@ class LangevinIntegratorSDM(SDMForce):
                                    self._res.data_ptr(), int(steps),
                                    stream=torch.cuda.current_stream(self._x.device).cuda_stream)
         self._step_count += int(steps)
+        self._time += int(steps) * self._step_size
         r = self._res[0].cpu().numpy()
         self._last = r
         self._bind_e = float(r[capi.R_BINDE])
         self._pot_e = float(r[capi.R_EPOT])
+        return r
 
 
 class SDMUtils:
