@@ -146,6 +146,7 @@ public:
         if (context.getSystem().getNumParticles() != owner_.getNumParticles())
             throw OpenMMException("SDMForce: particle count differs from the System's");
         for (int k = 0; k < SDM_NPARAMS; ++k) p_[k] = owner_.p_[k];
+        ntmax_ = owner_.ntmax_;
         displ_ = owner_.displ_;
         create(context);
     }
@@ -155,6 +156,18 @@ public:
         double box[3];
         box_of(context, box);
         if (box[0] != box_[0] || box[1] != box_[1] || box[2] != box_[2]) create(context);
+        const bool noneq = p_[SDM_P_NONEQ] == 1.0 && ntmax_ > 0.0;
+        const double t = context.getTime();
+        if (noneq) {
+            // the step from the last evaluation's time to t is complete: its
+            // work increment uses dW/dlambda at that step's start
+            if (have_last_ && t != t_last_) work_ += (t - t_last_) / ntmax_ * dwdl_last_;
+            const double lam = t / ntmax_;
+            if (lam != p_[SDM_P_LAMBDA]) {
+                p_[SDM_P_LAMBDA] = lam;
+                check(sdm_set_params(h_, 0, p_), h_, "invalid SDM parameters");
+            }
+        }
         const size_t n = positions.size();
         x_.resize(3 * n);
         f_.resize(3 * n);
@@ -164,6 +177,11 @@ public:
             x_[3 * i + 2] = positions[i][2];
         }
         check(sdm_evaluate(h_, x_.data(), res_, f_.data()), h_, "evaluation failed");
+        if (noneq) {
+            have_last_ = true;
+            t_last_ = t;
+            dwdl_last_ = res_[SDM_R_DWDLAMBDA];
+        }
         forces.resize(n);
         for (size_t i = 0; i < n; ++i) forces[i] = Vec3(f_[3 * i + 0], f_[3 * i + 1], f_[3 * i + 2]);
         return res_[SDM_R_EPOT];
@@ -173,10 +191,20 @@ public:
         check(sdm_set_params(h_, 0, f.p_), h_, "invalid SDM parameters");
         check(sdm_set_displacement(h_, 0, f.displ_.data()), h_, "invalid displacement");
         for (int k = 0; k < SDM_NPARAMS; ++k) p_[k] = f.p_[k];
+        ntmax_ = f.ntmax_;
         displ_ = f.displ_;
     }
 
     const double* results() const { return res_; }
+
+    /* The accumulated work plus the increment of the step that ends at the
+     * context's current time (its force evaluation at the step start is the
+     * last one seen). */
+    double work(const OpenMM::ContextImpl& context) const {
+        if (!have_last_ || !(ntmax_ > 0.0)) return work_;
+        return work_ + (context.getTime() - t_last_) / ntmax_ * dwdl_last_;
+    }
+    void set_work(const OpenMM::ContextImpl& context, double w) { work_ += w - work(context); }
 
 private:
     static void box_of(OpenMM::ContextImpl& context, double box[3]) {
@@ -205,12 +233,24 @@ private:
     double p_[SDM_NPARAMS];
     double res_[SDM_NRESULTS];
     std::vector<double> displ_, x_, f_;
+    // non-equilibrium work: the sum over completed steps, and the time and
+    // dW/dlambda of the last evaluation
+    double ntmax_ = 0.0, work_ = 0.0, t_last_ = 0.0, dwdl_last_ = 0.0;
+    bool have_last_ = false;
 };
 
 OpenMM::ForceImpl* SDMForce::createImpl() const { return new SDMForceImpl(*this); }
 
 void SDMForce::updateParametersInContext(OpenMM::Context& context) {
     dynamic_cast<SDMForceImpl&>(getImplInContext(context)).updateParametersInContext(*this);
+}
+
+double SDMForce::getNoneqWorkvalue(OpenMM::Context& context) {
+    return dynamic_cast<SDMForceImpl&>(getImplInContext(context)).work(getContextImpl(context));
+}
+
+void SDMForce::setNoneqWorkvalue(OpenMM::Context& context, double work) {
+    dynamic_cast<SDMForceImpl&>(getImplInContext(context)).set_work(getContextImpl(context), work);
 }
 
 std::vector<double> SDMForce::getResults(OpenMM::Context& context) {

@@ -87,6 +87,14 @@ public:
     double getUbcore() const { return p_[SDM_P_UBCORE]; }
     void setNonEquilibrium(int v) { p_[SDM_P_NONEQ] = v; }
     int getNonEquilibrium() const { return (int)p_[SDM_P_NONEQ]; }
+    /* Non-equilibrium protocol (ReferenceSDMKernels.cpp:229-245, 289-302):
+     * with setNonEquilibrium(1) and Ntmax > 0 every evaluation uses
+     * lambda = t / Ntmax, t the context time, and the context accumulates
+     * the work sum over steps of (dt / Ntmax) dW/dlambda at the step start. */
+    void setNoneqtmax(double t) { ntmax_ = t; }
+    double getNoneqtmax() const { return ntmax_; }
+    double getNoneqWorkvalue(OpenMM::Context& context);
+    void setNoneqWorkvalue(OpenMM::Context& context, double work);
     void setlambda1Slope(double v) { p_[SDM_P_M_LAMBDA1] = v; }
     double getlambda1Slope() const { return p_[SDM_P_M_LAMBDA1]; }
     void setlambda2Slope(double v) { p_[SDM_P_M_LAMBDA2] = v; }
@@ -148,6 +156,7 @@ private:
     double cutoff_, eps_rf_, ewald_tol_;
     int method_;
     int pme_grid_[3];
+    double ntmax_ = 0.0;
 };
 
 }  // namespace SDMPluginGB300

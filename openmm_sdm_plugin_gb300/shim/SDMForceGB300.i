@@ -46,6 +46,10 @@ public:
     double getUbcore() const;
     void setNonEquilibrium(int v);
     int getNonEquilibrium() const;
+    void setNoneqtmax(double t);
+    double getNoneqtmax() const;
+    double getNoneqWorkvalue(OpenMM::Context& context);
+    void setNoneqWorkvalue(OpenMM::Context& context, double work);
     void setlambda1Slope(double v);
     double getlambda1Slope() const;
     void setlambda2Slope(double v);

@@ -1,0 +1,61 @@
+// Stand-in of the C ABI (include/sdm_capi.h) for CPU tests of the force
+// plugin's host logic: the entry points the plugin calls, with results that
+// follow from the parameters alone (no force evaluation).
+//   results[SDM_R_EPOT]       = 100 lambda
+//   results[SDM_R_DWDLAMBDA]  = 3 + 2 lambda
+//   results[SDM_R_RESERVED]   = number of sdm_set_params calls so far
+// Forces are zero.
+#include "sdm_capi.h"
+
+#include <cstring>
+#include <new>
+
+struct sdm_handle {
+    int n = 0;
+    int set_params_calls = 0;
+    double p[SDM_NPARAMS] = {};
+};
+
+extern "C" {
+
+sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int, sdm_handle** out) {
+    if (!out || !systems || num_systems != 1) return SDM_ERR_INVALID_ARGUMENT;
+    sdm_handle* h = new (std::nothrow) sdm_handle();
+    if (!h) return SDM_ERR_INVALID_ARGUMENT;
+    h->n = systems[0].num_particles;
+    *out = h;
+    return SDM_OK;
+}
+
+sdm_status sdm_destroy(sdm_handle* h) {
+    delete h;
+    return SDM_OK;
+}
+
+const char* sdm_last_error(const sdm_handle*) { return "fake"; }
+
+sdm_status sdm_set_params(sdm_handle* h, int replica, const double* params) {
+    if (!h || replica != 0 || !params) return SDM_ERR_INVALID_ARGUMENT;
+    std::memcpy(h->p, params, sizeof(h->p));
+    h->set_params_calls++;
+    return SDM_OK;
+}
+
+sdm_status sdm_set_displacement(sdm_handle* h, int system, const double* d) {
+    return (h && system == 0 && d) ? SDM_OK : SDM_ERR_INVALID_ARGUMENT;
+}
+
+sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double* forces) {
+    if (!h || !x) return SDM_ERR_INVALID_ARGUMENT;
+    const double lam = h->p[SDM_P_LAMBDA];
+    if (results) {
+        for (int k = 0; k < SDM_NRESULTS; ++k) results[k] = 0.0;
+        results[SDM_R_EPOT] = 100.0 * lam;
+        results[SDM_R_DWDLAMBDA] = 3.0 + 2.0 * lam;
+        results[SDM_R_RESERVED] = h->set_params_calls;
+    }
+    if (forces) std::memset(forces, 0, 3 * (size_t)h->n * sizeof(double));
+    return SDM_OK;
+}
+
+}  // extern "C"

@@ -173,6 +173,8 @@ public:
     void setPositions(const std::vector<Vec3>& p) { positions = p; }
     void getPeriodicBoxVectors(Vec3& a, Vec3& b, Vec3& c) { a = box[0]; b = box[1]; c = box[2]; }
     void setPeriodicBoxVectors(const Vec3& a, const Vec3& b, const Vec3& c) { box[0] = a; box[1] = b; box[2] = c; }
+    double getTime() const { return time; }
+    void setTime(double t) { time = t; }
     std::vector<ForceImpl*>& getForceImpls() { return forceImpls; }
     double calcForcesAndEnergy(bool includeForces, bool includeEnergy, int groups = 0xFFFFFFFF);
     std::vector<Vec3>& getForceAccumulator() { return forces; }
@@ -183,6 +185,7 @@ private:
     std::vector<ForceImpl*> forceImpls;
     std::vector<Vec3> positions, forces;
     Vec3 box[3];
+    double time = 0.0;
 };
 
 /* A context without an integrator: enough to evaluate forces and energies. */
@@ -192,6 +195,7 @@ public:
     ~Context();
     void setPositions(const std::vector<Vec3>& positions) { impl->setPositions(positions); }
     void setPeriodicBoxVectors(const Vec3& a, const Vec3& b, const Vec3& c) { impl->setPeriodicBoxVectors(a, b, c); }
+    void setTime(double time) { impl->setTime(time); }
     State getState(int types, bool enforcePeriodicBox = false, int groups = 0xFFFFFFFF);
 
 private:

@@ -4,11 +4,18 @@
 //   shim_driver evaluate <input> <output>   a Context holding the force: energy, forces and
 //                                           results; then lambda1 += 0.1 through
 //                                           updateParametersInContext and again
+//   shim_driver noneq <input> <output>      the non-equilibrium protocol over nsteps steps of
+//                                           dt (context time advanced by hand, two
+//                                           evaluations per step time): per step the energy and
+//                                           results[SDM_R_RESERVED]; then the work value, the
+//                                           work after setNoneqWorkvalue(1.5), and after one
+//                                           more step
 //
 // Input (little-endian): int32 n, n_exceptions, method (OpenMM NonbondedMethod),
 // dispersion_correction; float64 box[3], cutoff, eps_rf, ewald_tol,
 // params[SDM_NPARAMS], charge[n], sigma[n], epsilon[n], displacement[3n],
-// positions[3n], exceptions[n_exceptions][5] (i, j, charge product, sigma, epsilon).
+// positions[3n], exceptions[n_exceptions][5] (i, j, charge product, sigma, epsilon);
+// mode noneq only: float64 ntmax, dt; int32 nsteps.
 // An OpenMMException prints its message on stderr and exits with status 3.
 #include "SDMForceGB300.h"
 #include "openmm/Context.h"
@@ -49,6 +56,13 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
     const double cutoff = r.one<double>(), eps_rf = r.one<double>(), tol = r.one<double>();
     std::vector<double> params = r.many(SDM_NPARAMS), q = r.many(n), sig = r.many(n), eps = r.many(n);
     std::vector<double> d = r.many(3 * (size_t)n), x = r.many(3 * (size_t)n), ex = r.many(5 * (size_t)nx);
+    double ntmax = 0.0, dt = 0.0;
+    int nsteps = 0;
+    if (mode == "noneq") {
+        ntmax = r.one<double>();
+        dt = r.one<double>();
+        nsteps = r.one<int>();
+    }
     fclose(fi);
 
     NonbondedForce nb;
@@ -113,6 +127,35 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
     for (int i = 0; i < n; ++i) pos[i] = Vec3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
     Context context(system);
     context.setPositions(pos);
+    if (mode == "noneq") {
+        force->setNonEquilibrium(1);
+        force->setNoneqtmax(ntmax);
+        force->updateParametersInContext(context);
+        double t = 0.0;
+        auto step = [&]() {
+            context.setTime(t);
+            double e = 0.0, calls = 0.0;
+            for (int rep = 0; rep < 2; ++rep) {   // a second evaluation at the same time adds no work
+                e = context.getState(State::Energy, false, 1 << 2).getPotentialEnergy();
+                calls = force->getResults(context)[SDM_R_RESERVED];
+            }
+            put(fo, &e, 1);
+            put(fo, &calls, 1);
+            t += dt;
+        };
+        for (int k = 0; k < nsteps; ++k) step();
+        context.setTime(t);
+        const double w1 = force->getNoneqWorkvalue(context);
+        force->setNoneqWorkvalue(context, 1.5);
+        const double w2 = force->getNoneqWorkvalue(context);
+        step();
+        context.setTime(t);
+        const double w3 = force->getNoneqWorkvalue(context);
+        const double ws[3] = {w1, w2, w3};
+        put(fo, ws, 3);
+        fclose(fo);
+        return 0;
+    }
     for (int pass = 0; pass < 2; ++pass) {
         if (pass == 1) {
             force->setLambda1(force->getLambda1() + 0.1);
@@ -136,7 +179,7 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
 
 int main(int argc, char** argv) {
     if (argc != 4) {
-        fprintf(stderr, "usage: shim_driver describe|evaluate <input> <output>\n");
+        fprintf(stderr, "usage: shim_driver describe|evaluate|noneq <input> <output>\n");
         return 2;
     }
     try {

@@ -172,3 +172,47 @@ def test_context_evaluation_equals_the_c_abi(driver, tmp_path, which):
         assert np.array_equal(ff, F.reshape(-1, 3))
     assert got[1, 1 + capi.R_L1] != got[0, 1 + capi.R_L1]
     h.close()
+
+
+@pytest.fixture(scope="module")
+def fake_driver(tmp_path_factory):
+    """The same driver linked against the C-ABI stand-in of
+    tests/openmm_api/fake_sdm.cpp (results follow from the parameters)."""
+    exe = str(tmp_path_factory.mktemp("shim_fake") / "shim_driver")
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-Wno-unused-parameter",
+           "-I", API, "-I", os.path.join(ROOT, "include"), "-I", SHIM,
+           os.path.join(SHIM, "SDMForceGB300.cpp"), os.path.join(API, "ApiSubset.cpp"),
+           os.path.join(API, "shim_driver.cpp"), os.path.join(API, "fake_sdm.cpp"), "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_non_equilibrium_protocol_on_context_time(fake_driver, tmp_path):
+    """lambda = t / Ntmax at every evaluation (parameters pushed once per
+    new time), and the work the reference integrator accumulates,
+    sum_k (dt / Ntmax) dW/dlambda(t_k), read after each step; a second
+    evaluation at the same time adds nothing; setNoneqWorkvalue restarts
+    the sum (ReferenceSDMKernels.cpp:229-245, 289-302)."""
+    s = S.config0(variant="b")
+    T, dt, nsteps = 0.02, 0.002, 7
+    inp, out = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    write_input(inp, s, s.params[0], s.positions[0])
+    with open(inp, "ab") as f:
+        np.array([T, dt], np.float64).tofile(f)
+        np.array([nsteps], np.int32).tofile(f)
+    r = subprocess.run([fake_driver, "noneq", inp, out], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    v = np.frombuffer(open(out, "rb").read(), np.float64)
+    per_step, (w1, w2, w3) = v[:-3].reshape(-1, 2), v[-3:]
+    assert per_step.shape[0] == nsteps + 1
+    t, work, lams = 0.0, 0.0, []
+    for _ in range(nsteps):
+        lams.append(t / T)
+        work += dt / T * (3.0 + 2.0 * (t / T))   # the stand-in's dW/dlambda
+        t += dt
+    assert np.array_equal(per_step[:nsteps, 0], 100.0 * np.array(lams))
+    assert np.all(np.diff(per_step[:, 1]) == 1.0)      # one parameter push per new time
+    assert w1 == pytest.approx(work, rel=1e-14)
+    assert w2 == 1.5
+    assert w3 == pytest.approx(1.5 + dt / T * (3.0 + 2.0 * (t / T)), rel=1e-14)
