@@ -3,15 +3,20 @@
 // follow from the parameters alone (no force evaluation).
 //   results[SDM_R_EPOT]       = 100 lambda
 //   results[SDM_R_DWDLAMBDA]  = 3 + 2 lambda
-//   results[SDM_R_RESERVED]   = number of sdm_set_params calls so far
+//   results[SDM_R_RESERVED]   = number of sdm_set_params calls on this handle
+//   results[SDM_R_U0]         = the handle's box edge x
+//   results[SDM_R_U1]         = number of sdm_create calls in the process
 // Forces are zero.
 #include "sdm_capi.h"
 
 #include <cstring>
 #include <new>
 
+static int g_creates = 0;
+
 struct sdm_handle {
     int n = 0;
+    double box0 = 0.0;
     int set_params_calls = 0;
     double p[SDM_NPARAMS] = {};
 };
@@ -23,6 +28,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int, sdm_
     sdm_handle* h = new (std::nothrow) sdm_handle();
     if (!h) return SDM_ERR_INVALID_ARGUMENT;
     h->n = systems[0].num_particles;
+    h->box0 = systems[0].box[0];
+    ++g_creates;
     *out = h;
     return SDM_OK;
 }
@@ -53,6 +60,8 @@ sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double*
         results[SDM_R_EPOT] = 100.0 * lam;
         results[SDM_R_DWDLAMBDA] = 3.0 + 2.0 * lam;
         results[SDM_R_RESERVED] = h->set_params_calls;
+        results[SDM_R_U0] = h->box0;
+        results[SDM_R_U1] = g_creates;
     }
     if (forces) std::memset(forces, 0, 3 * (size_t)h->n * sizeof(double));
     return SDM_OK;

@@ -10,6 +10,10 @@
 //                                           results[SDM_R_RESERVED]; then the work value, the
 //                                           work after setNoneqWorkvalue(1.5), and after one
 //                                           more step
+//   shim_driver rebox <input> <output>      evaluate, evaluate again, change the box and
+//                                           evaluate: results[SDM_R_RESERVED], [SDM_R_U0] and
+//                                           [SDM_R_U1] after each; then a triclinic box (an
+//                                           OpenMMException)
 //
 // Input (little-endian): int32 n, n_exceptions, method (OpenMM NonbondedMethod),
 // dispersion_correction; float64 box[3], cutoff, eps_rf, ewald_tol,
@@ -127,6 +131,19 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
     for (int i = 0; i < n; ++i) pos[i] = Vec3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
     Context context(system);
     context.setPositions(pos);
+    if (mode == "rebox") {
+        for (int k = 0; k < 3; ++k) {
+            if (k == 2) context.setPeriodicBoxVectors(Vec3(box[0] + 0.1, 0, 0), Vec3(0, box[1], 0), Vec3(0, 0, box[2]));
+            context.getState(State::Energy, false, 1 << 2);
+            const std::vector<double> res = force->getResults(context);
+            const double v[3] = {res[SDM_R_RESERVED], res[SDM_R_U0], res[SDM_R_U1]};
+            put(fo, v, 3);
+        }
+        fclose(fo);
+        context.setPeriodicBoxVectors(Vec3(box[0], 0, 0), Vec3(0.5, box[1], 0), Vec3(0, 0, box[2]));
+        context.getState(State::Energy, false, 1 << 2);   // throws: the box must be rectangular
+        return 0;
+    }
     if (mode == "noneq") {
         force->setNonEquilibrium(1);
         force->setNoneqtmax(ntmax);
@@ -179,7 +196,7 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
 
 int main(int argc, char** argv) {
     if (argc != 4) {
-        fprintf(stderr, "usage: shim_driver describe|evaluate|noneq <input> <output>\n");
+        fprintf(stderr, "usage: shim_driver describe|evaluate|noneq|rebox <input> <output>\n");
         return 2;
     }
     try {

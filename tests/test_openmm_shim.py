@@ -216,3 +216,18 @@ def test_non_equilibrium_protocol_on_context_time(fake_driver, tmp_path):
     assert w1 == pytest.approx(work, rel=1e-14)
     assert w2 == 1.5
     assert w3 == pytest.approx(1.5 + dt / T * (3.0 + 2.0 * (t / T)), rel=1e-14)
+
+
+def test_box_change_rebuilds_the_handle(fake_driver, tmp_path):
+    """A context whose box changes (a barostat) gets a new handle, made with
+    the new box and the context's parameters; a triclinic box is refused."""
+    s = S.config0(variant="b")
+    r, out = run(fake_driver, "rebox", tmp_path, s, s.params[0], s.positions[0])
+    assert r.returncode == 3 and "rectangular" in r.stderr, r.stderr
+    v = np.frombuffer(open(out, "rb").read(), np.float64).reshape(3, 3)
+    pushes, box_x, creates = v[:, 0], v[:, 1], v[:, 2]
+    # the same box keeps the handle; the new box makes a new one, created
+    # with that box and given the parameters once
+    assert list(box_x) == [s.box[0], s.box[0], s.box[0] + 0.1]
+    assert creates[1] == creates[0] and creates[2] == creates[0] + 1
+    assert list(pushes) == [1.0, 1.0, 1.0]
