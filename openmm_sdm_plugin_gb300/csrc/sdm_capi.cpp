@@ -233,8 +233,9 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
     s.q.resize(n); s.hs.resize(n); s.se.resize(n); s.grp.assign(n, 0); s.d.assign(3 * (size_t)n, 0.0);
     const double sk = std::sqrt(kCoulomb);
     for (int i = 0; i < n; ++i) {
-        if (!(d.sigma[i] >= 0.0) || !(d.epsilon[i] >= 0.0) || !std::isfinite(d.charge[i]))
-            return "sigma/epsilon must be >= 0 and charges finite";
+        if (!(d.sigma[i] >= 0.0) || !(d.epsilon[i] >= 0.0) || !std::isfinite(d.sigma[i]) ||
+            !std::isfinite(d.epsilon[i]) || !std::isfinite(d.charge[i]))
+            return "sigma/epsilon must be finite and >= 0, charges finite";
         s.q[i] = (float)(d.charge[i] * sk);
         s.hs[i] = (float)(0.5 * d.sigma[i]);
         s.se[i] = (float)(2.0 * std::sqrt(d.epsilon[i]));
@@ -788,6 +789,17 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
         sdm_destroy(h);
         return s;
     };
+    // host-side setup and validation of every system first (no device call),
+    // so that a bad descriptor is reported as such with or without a GPU
+    h->sys.resize(num_systems);
+    for (int s = 0; s < num_systems; ++s) {
+        std::string e = setup_system(systems[s], h->sys[s]);
+        if (!e.empty()) {
+            delete h;
+            return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "system " + std::to_string(s) + ": " + e);
+        }
+        setup_displacement(h->sys[s], systems[s].displacement);
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         delete h;
@@ -806,15 +818,6 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     if (prop.major < 10) {
         delete h;
         return fail(nullptr, SDM_ERR_NO_DEVICE, "the library is built for sm_103a (Blackwell Ultra)");
-    }
-    h->sys.resize(num_systems);
-    for (int s = 0; s < num_systems; ++s) {
-        std::string e = setup_system(systems[s], h->sys[s]);
-        if (!e.empty()) {
-            delete h;
-            return fail(nullptr, SDM_ERR_INVALID_ARGUMENT, "system " + std::to_string(s) + ": " + e);
-        }
-        setup_displacement(h->sys[s], systems[s].displacement);
     }
     h->pme = h->sys[0].dev.pme != 0;
     for (int s = 1; s < num_systems; ++s)
@@ -1522,8 +1525,9 @@ sdm_status sdm_set_particle_params(sdm_handle* h, int system, int n, const int* 
     for (int k = 0; k < n; ++k) {
         const int i = index[k];
         if (i < 0 || i >= S.n) return fail(h, SDM_ERR_INVALID_ARGUMENT, "particle index out of range");
-        if (!(sigma[k] >= 0.0) || !(epsilon[k] >= 0.0) || !std::isfinite(charge[k]))
-            return fail(h, SDM_ERR_INVALID_ARGUMENT, "sigma/epsilon must be >= 0 and charges finite");
+        if (!(sigma[k] >= 0.0) || !(epsilon[k] >= 0.0) || !std::isfinite(sigma[k]) || !std::isfinite(epsilon[k]) ||
+            !std::isfinite(charge[k]))
+            return fail(h, SDM_ERR_INVALID_ARGUMENT, "sigma/epsilon must be finite and >= 0, charges finite");
     }
     cudaSetDevice(h->device);
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));

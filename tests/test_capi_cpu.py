@@ -4,6 +4,7 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -88,3 +89,38 @@ def test_force_api_mirrors_reference_setters():
     f.setDisplacement(1, 1.0, 2.0, 3.0)
     assert f.getDisplacement(1) == (1.0, 2.0, 3.0)
     assert f.getDisplacement(0) == (0.0, 0.0, 0.0)
+
+
+def _bad(s, **kw):
+    import dataclasses
+    return dataclasses.replace(s, **kw)
+
+
+def _with(a, i, v):
+    a = np.array(a, dtype=float)
+    a[i] = v
+    return a
+
+
+def test_descriptor_errors_are_reported_before_any_device_query(built_lib):
+    """Every system descriptor is validated on the host before the library
+    looks for a device, so these errors read the same with or without a GPU."""
+    from openmm_sdm_plugin_gb300 import capi, systems
+    s = systems.config0(variant="b")
+    ex = np.asarray(s.exclusions).copy()
+    ex[0, 1] = s.n
+    cases = [
+        (_bad(s, sigma=_with(s.sigma, 0, np.inf)), "sigma/epsilon must be finite"),
+        (_bad(s, epsilon=_with(s.epsilon, 3, -1.0)), "sigma/epsilon must be finite"),
+        (_bad(s, charge=_with(s.charge, 5, np.nan)), "charges finite"),
+        (_bad(s, cutoff=0.6 * float(s.box.min())), "below half the box edge"),
+        (_bad(s, box=np.array([s.box[0], 0.0, s.box[2]])), "box edges must be finite"),
+        (_bad(s, eps_rf=0.0), "reaction_field_dielectric"),
+        (_bad(s, exclusions=ex), "exclusion index out of range"),
+        (_bad(s, nonbonded_method="pme", ewald_tolerance=0.7), "ewald_tolerance"),
+    ]
+    for bad, msg in cases:
+        with pytest.raises(capi.SdmError) as e:
+            capi.Handle([s, bad])
+        assert e.value.status == capi.SDM_ERR_INVALID_ARGUMENT, (msg, e.value)
+        assert "system 1" in str(e.value) and msg in str(e.value), str(e.value)
