@@ -1361,9 +1361,10 @@ sdm_status sdm_get_restraint_energies(sdm_handle* h, double* energies) {
 sdm_status sdm_set_params(sdm_handle* h, int replica, const double* params) {
     if (!h || !params) return SDM_ERR_INVALID_ARGUMENT;
     if (replica < 0 || replica >= h->nrep) return fail(h, SDM_ERR_INVALID_ARGUMENT, "replica index out of range");
-    const int bm = (int)params[SDM_P_BIAS_METHOD], sm = (int)params[SDM_P_SOFTCORE_METHOD];
-    if (bm < 0 || bm > 2 || bm != params[SDM_P_BIAS_METHOD]) return fail(h, SDM_ERR_UNKNOWN_METHOD, "Unknown bias method");
-    if (sm < 0 || sm > 2 || sm != params[SDM_P_SOFTCORE_METHOD]) return fail(h, SDM_ERR_UNKNOWN_METHOD, "Unknown soft core method");
+    // compared as doubles: a cast of NaN or of a huge value to int is undefined
+    const double bm = params[SDM_P_BIAS_METHOD], sm = params[SDM_P_SOFTCORE_METHOD];
+    if (!(bm == 0.0 || bm == 1.0 || bm == 2.0)) return fail(h, SDM_ERR_UNKNOWN_METHOD, "Unknown bias method");
+    if (!(sm == 0.0 || sm == 1.0 || sm == 2.0)) return fail(h, SDM_ERR_UNKNOWN_METHOD, "Unknown soft core method");
     std::memcpy(&h->params[(size_t)replica * SDM_NPARAMS], params, sizeof(double) * SDM_NPARAMS);
     h->params_dirty = true;
     return SDM_OK;

@@ -56,3 +56,23 @@ def test_shared_displacement_gives_zero_u_and_equal_state_forces():
     assert res[0, capi.R_U] == 0.0 and res[0, capi.R_U1] == res[0, capi.R_U0]
     assert np.array_equal(F0, F1)
     assert np.array_equal(F, F0)
+
+
+def test_unknown_method_ids_are_rejected():
+    """Bias and soft-core ids other than 0, 1, 2 (including NaN, fractions and
+    values beyond int range) are SDM_ERR_UNKNOWN_METHOD, as the reference
+    throws "Unknown soft core method" (LangevinIntegratorSDM.cpp:147); the
+    replica keeps its last valid parameters."""
+    s = _tiny(20, 2.5)
+    h = capi.Handle([s])
+    good = s.params[0].as_array()
+    h.set_params(0, good)
+    for k in (0, 1):   # SDM_P_BIAS_METHOD, SDM_P_SOFTCORE_METHOD
+        for v in (3.0, -1.0, 1.5, np.nan, np.inf, 1e300):
+            p = good.copy()
+            p[k] = v
+            with pytest.raises(capi.SdmError) as e:
+                h.set_params(0, p)
+            assert e.value.status == capi.SDM_ERR_UNKNOWN_METHOD
+    res, _ = h.evaluate(s.positions[0])
+    assert res[0, capi.R_STATUS] == 0 and np.isfinite(res[0, :capi.R_STATUS]).all()
