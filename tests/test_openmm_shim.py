@@ -231,3 +231,34 @@ def test_box_change_rebuilds_the_handle(fake_driver, tmp_path):
     assert list(box_x) == [s.box[0], s.box[0], s.box[0] + 0.1]
     assert creates[1] == creates[0] and creates[2] == creates[0] + 1
     assert list(pushes) == [1.0, 1.0, 1.0]
+
+
+def test_makefile_builds_the_plugin_library(driver, tmp_path):
+    """The maintainer's recipe (openmm_sdm_plugin_gb300/shim/Makefile) against
+    an OPENMM_DIR made of the API subset (headers, and a libOpenMM.so of its
+    bodies): it builds libSDMPluginGB300.so, and a program linked with that
+    library reads a NonbondedForce as the statically built driver does."""
+    root = tmp_path / "openmm"
+    (root / "lib").mkdir(parents=True)
+    os.symlink(API, root / "include")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-I", API,
+                        os.path.join(API, "ApiSubset.cpp"), "-o", str(root / "lib" / "libOpenMM.so")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    plugin = str(tmp_path / "libSDMPluginGB300.so")
+    r = subprocess.run(["make", "-s", "-C", SHIM, f"OPENMM_DIR={root}", f"OUT={plugin}"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    exe = str(tmp_path / "linked_driver")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", API, "-I", os.path.join(ROOT, "include"), "-I", SHIM,
+                        os.path.join(API, "shim_driver.cpp"), "-o", exe, plugin, str(root / "lib" / "libOpenMM.so"),
+                        "-Wl,-rpath," + str(tmp_path) + ":" + str(root / "lib")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    s = _dms_system()
+    (tmp_path / "a").mkdir()
+    (tmp_path / "b").mkdir()
+    ra, out_a = run(exe, "describe", tmp_path / "a", s, s.params[0], s.positions[0])
+    rb, out_b = run(driver, "describe", tmp_path / "b", s, s.params[0], s.positions[0])
+    assert ra.returncode == 0 and rb.returncode == 0, ra.stderr + rb.stderr
+    assert open(out_a, "rb").read() == open(out_b, "rb").read()
