@@ -4,6 +4,11 @@ TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
 and the CPU-baseline leg of ``bench.py``, where it is the checker or the timed
 CPU baseline -- never the product path.  See ``sdm_oracle.c`` for the
 reference files each routine restates.
+
+PARITY UNPINNED: the reference has no tests, golden vectors or fixtures for
+this path and cannot be built here (it needs OpenMM), so the restatements are
+cross-checked against independent implementations, closed forms and
+invariances rather than against the reference's outputs.
 """
 from __future__ import annotations
 

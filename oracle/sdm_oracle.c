@@ -26,8 +26,14 @@
  *     E = K qi qj (1/r + krf r^2 - crf),
  *     krf = (eps_rf-1)/((2 eps_rf+1) rc^3),  crf = 3 eps_rf/((2 eps_rf+1) rc),
  * minimum image in an orthorhombic box, excluded pairs contribute nothing,
- * no dispersion correction.  Parity of this part is UNPINNED: the reference
- * ships no golden vectors and cannot be built here (it needs OpenMM).
+ * no dispersion correction.
+ *
+ * PARITY UNPINNED.  The reference ships no tests, golden vectors or fixtures
+ * for this path, and it cannot be built here (every source needs OpenMM).  So
+ * neither the pair arithmetic nor the combine above is pinned against the
+ * reference's own outputs.  The restatement is cross-checked instead against
+ * an independent dense numpy implementation, analytic two-particle cases,
+ * invariances and an independent Python restatement of the combine.
  *
  * Besides the FP64 physics ("fp64 rule": a pair interacts iff its FP64
  * minimum-image distance is below rc) the file restates the pair-inclusion
