@@ -12,7 +12,7 @@ Public surface:
 """
 from . import systems  # noqa: F401
 from .capi import Handle, SdmError, load_library  # noqa: F401
-from .force import LangevinIntegratorSDM, SDMForce, SDMUtils, force_from_system  # noqa: F401
+from .force import LangevinIntegratorSDM, SDMForce, SDMUtils, force_from_system, integrator_from_system  # noqa: F401
 
 __all__ = ["systems", "Handle", "SdmError", "load_library", "SDMForce", "LangevinIntegratorSDM", "SDMUtils",
-           "force_from_system"]
+           "force_from_system", "integrator_from_system"]

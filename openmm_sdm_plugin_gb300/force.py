@@ -36,12 +36,19 @@ class SDMForce:
     NoSoftCoreMethod = 0
     TanhMethod = 1
     RationalMethod = 2
+    # nonbonded method ids of OpenMM's NonbondedForce that the path supports
+    CutoffPeriodic = 2
+    PME = 4
 
     def __init__(self, nParticles: int = 0):
         self._q: List[float] = []
         self._sig: List[float] = []
         self._eps: List[float] = []
         self._excl: List[tuple] = []
+        self._exc: List[tuple] = []      # (i, j, charge product, sigma, epsilon)
+        self._method = SDMForce.CutoffPeriodic
+        self._ewald_tol = 5e-4
+        self._pme_grid = None            # explicit PME grid (None: from the tolerance)
         self._displ = np.zeros((nParticles, 3))
         for _ in range(nParticles):
             self.addParticle(0.0, 0.0, 0.0)
@@ -92,6 +99,47 @@ class SDMForce:
 
     def getNumExclusions(self) -> int:
         return len(self._excl)
+
+    def addException(self, particle1: int, particle2: int, chargeProd: float, sigma: float, epsilon: float,
+                     replace: bool = False) -> int:
+        """OpenMM NonbondedForce.addException: the pair is excluded from the
+        nonbonded sum; with a charge product or a well depth it interacts
+        with these parameters instead (the 1-4 pairs of
+        example/desmonddmsfile75.py:813-848)."""
+        i, j = int(particle1), int(particle2)
+        key = (min(i, j), max(i, j))
+        for k, e in enumerate(self._exc):
+            if (min(e[0], e[1]), max(e[0], e[1])) == key:
+                if not replace:
+                    raise ValueError(f"there is already an exception for particles {i} and {j}")
+                self._exc[k] = (i, j, float(chargeProd), float(sigma), float(epsilon))
+                self._topology_dirty = True
+                return k
+        self._exc.append((i, j, float(chargeProd), float(sigma), float(epsilon)))
+        self._topology_dirty = True
+        return len(self._exc) - 1
+
+    def getNumExceptions(self) -> int:
+        return len(self._exc)
+
+    def getExceptionParameters(self, index: int):
+        return self._exc[index]
+
+    def setNonbondedMethod(self, method: int):
+        if int(method) not in (SDMForce.CutoffPeriodic, SDMForce.PME):
+            raise ValueError("the nonbonded method must be CutoffPeriodic (reaction field) or PME")
+        self._method = int(method)
+        self._topology_dirty = True
+
+    def getNonbondedMethod(self) -> int:
+        return self._method
+
+    def setEwaldErrorTolerance(self, tol: float):
+        self._ewald_tol = float(tol)
+        self._topology_dirty = True
+
+    def getEwaldErrorTolerance(self) -> float:
+        return self._ewald_tol
 
     def setCutoffDistance(self, rc: float):
         self._cutoff = float(rc)
@@ -222,10 +270,23 @@ class SDMForce:
     # -- evaluation -------------------------------------------------------
     def _system(self) -> SDMSystem:
         n = len(self._q)
-        ex = np.array(self._excl, np.int32).reshape(-1, 2) if self._excl else np.zeros((0, 2), np.int32)
+        # exclusions: addExclusion pairs and every exception pair, each once
+        seen, pairs = set(), []
+        for i, j in list(self._excl) + [(e[0], e[1]) for e in self._exc]:
+            key = (min(i, j), max(i, j))
+            if key not in seen:
+                seen.add(key)
+                pairs.append((i, j))
+        ex = np.array(pairs, np.int32).reshape(-1, 2)
+        live = [e for e in self._exc if e[2] != 0.0 or e[4] != 0.0]
+        xp = np.array([e[:2] for e in live], np.int32).reshape(-1, 2) if live else None
+        xprm = np.array([e[2:] for e in live], np.float64).reshape(-1, 3) if live else None
         return SDMSystem("SDMForce", self._box.copy(), np.array(self._q), np.array(self._sig),
                          np.array(self._eps), ex, self._displ[:n].copy(), np.zeros((1, n, 3)),
-                         [self._p], cutoff=self._cutoff, eps_rf=self._eps_rf)
+                         [self._p], cutoff=self._cutoff, eps_rf=self._eps_rf, exceptions=xp,
+                         exception_params=xprm,
+                         nonbonded_method="pme" if self._method == SDMForce.PME else "rf",
+                         ewald_tolerance=self._ewald_tol, pme_grid=self._pme_grid)
 
     def _sync(self, device: int = 0):
         if self._topology_dirty or self._handle is None:
@@ -477,19 +538,45 @@ class SDMUtils:
         self._push()
 
 
-def force_from_system(s: SDMSystem, replica: int = 0) -> SDMForce:
-    """Builds an SDMForce from a synthetic system (parameters of `replica`)."""
-    f = SDMForce()
-    for q, sg, ep in zip(s.charge, s.sigma, s.epsilon):
-        f.addParticle(q, sg, ep)
+def _fill_from_system(f: SDMForce, s: SDMSystem, replica: int, masses=None) -> SDMForce:
+    for k, (q, sg, ep) in enumerate(zip(s.charge, s.sigma, s.epsilon)):
+        if masses is None:
+            f.addParticle(q, sg, ep)
+        else:
+            f.addParticle(q, sg, ep, mass=float(masses[k]))
     for i, j in np.asarray(s.exclusions).reshape(-1, 2):
         f.addExclusion(int(i), int(j))
+    if s.exceptions is not None:
+        for (i, j), (qq, sg, ep) in zip(np.asarray(s.exceptions).reshape(-1, 2),
+                                        np.asarray(s.exception_params).reshape(-1, 3)):
+            f.addException(int(i), int(j), float(qq), float(sg), float(ep))
+    f.setNonbondedMethod(SDMForce.PME if s.nonbonded_method == "pme" else SDMForce.CutoffPeriodic)
+    f.setEwaldErrorTolerance(s.ewald_tolerance)
+    f._pme_grid = None if s.pme_grid is None else tuple(int(v) for v in s.pme_grid)
     f.setCutoffDistance(s.cutoff)
     f.setReactionFieldDielectric(s.eps_rf)
     f.setPeriodicBoxVectors((s.box[0], 0, 0), (0, s.box[1], 0), (0, 0, s.box[2]))
     for i in np.nonzero(np.any(s.displacement != 0, axis=1))[0]:
         f.setDisplacement(int(i), *s.displacement[i])
-    p = s.params[replica]
-    f._p = dataclasses.replace(p)
+    f._p = dataclasses.replace(s.params[replica])
     f._params_dirty = True
     return f
+
+
+def force_from_system(s: SDMSystem, replica: int = 0) -> SDMForce:
+    """Builds an SDMForce from a system (synthetic or read by dms.read_dms):
+    particles, exclusions, exceptions, electrostatics, box, displacement and
+    the SDM parameters of `replica`."""
+    return _fill_from_system(SDMForce(), s, replica)
+
+
+def integrator_from_system(s: SDMSystem, temperature: float, frictionCoeff: float, stepSize: float,
+                           replica: int = 0) -> "LangevinIntegratorSDM":
+    """A LangevinIntegratorSDM mirror for a system, as the reference's example
+    builds LangevinIntegratorSDM(temperature, friction, step size, N) and sets
+    its SDM parameters and displacements (example/test.py:172-188).  Masses
+    come from s.masses (required)."""
+    if s.masses is None:
+        raise ValueError("the system has no masses (SDMSystem.masses)")
+    return _fill_from_system(LangevinIntegratorSDM(temperature, frictionCoeff, stepSize), s, replica,
+                             masses=np.asarray(s.masses, np.float64))

@@ -175,3 +175,67 @@ def test_temoa_dms_system_parity():
     a = oracle.OracleSystem(s).f32rule(x, h.grid(0))
     assert int(c[0, 0]) == a["P0"] and int(c[0, 1]) == a["P1delta"]
     assert res[0, capi.R_STATUS] == 0
+
+
+def test_mirror_from_a_dms_system_carries_its_nonbonded_force():
+    """force_from_system / integrator_from_system on the TEMOA system: the
+    mirror's system descriptor holds the same exclusions (each once, in the
+    same order), the 1-4 exceptions with their parameters, the electrostatics
+    and the masses (OpenMM NonbondedForce.addException semantics: every
+    exception excluded, the interacting ones with their own terms)."""
+    from openmm_sdm_plugin_gb300 import force_from_system, integrator_from_system
+    s = temoa_system()
+    f = force_from_system(s)
+    d = f._system()
+    assert np.array_equal(d.exclusions, s.exclusions)
+    assert np.array_equal(d.exceptions, s.exceptions)
+    assert np.array_equal(d.exception_params, s.exception_params)
+    assert d.nonbonded_method == "rf" and d.cutoff == s.cutoff and d.eps_rf == s.eps_rf
+    assert np.array_equal(d.displacement, s.displacement)
+    assert np.array_equal(d.params[0].as_array(), s.params[0].as_array())
+    integ = integrator_from_system(s, 300.0, 1.0, 0.002)
+    assert np.array_equal(integ._system().exceptions, s.exceptions)
+    assert [integ.getParticleMass(i) for i in range(s.n)] == list(s.masses)
+    with pytest.raises(ValueError, match="masses"):
+        integrator_from_system(dataclasses.replace(s, masses=None), 300.0, 1.0, 0.002)
+    pme = force_from_system(dataclasses.replace(s, nonbonded_method="pme", ewald_tolerance=2e-4))._system()
+    assert pme.nonbonded_method == "pme" and pme.ewald_tolerance == 2e-4
+
+
+def test_mirror_exception_rules():
+    from openmm_sdm_plugin_gb300 import SDMForce
+    f = SDMForce()
+    for _ in range(4):
+        f.addParticle(0.1, 0.3, 0.5)
+    f.setPeriodicBoxVectors((3, 0, 0), (0, 3, 0), (0, 0, 3))
+    f.addExclusion(0, 1)
+    f.addException(1, 0, 0.0, 1.0, 0.0)          # excluded, no own term (already excluded: once)
+    f.addException(2, 3, -0.05, 0.3, 0.2)        # a 1-4 pair
+    with pytest.raises(ValueError, match="already an exception"):
+        f.addException(3, 2, 0.0, 1.0, 0.0)
+    assert f.addException(3, 2, -0.07, 0.31, 0.25, replace=True) == 1
+    assert f.getNumExceptions() == 2 and f.getExceptionParameters(1) == (3, 2, -0.07, 0.31, 0.25)
+    d = f._system()
+    assert d.exclusions.tolist() == [[0, 1], [3, 2]]    # the pair as the replacing call gave it
+    assert d.exceptions.tolist() == [[3, 2]] and d.exception_params.tolist() == [[-0.07, 0.31, 0.25]]
+    with pytest.raises(ValueError, match="CutoffPeriodic"):
+        f.setNonbondedMethod(3)                   # Ewald
+    f.setNonbondedMethod(SDMForce.PME)
+    assert f._system().nonbonded_method == "pme"
+
+
+@pytest.mark.gpu
+def test_mirror_evaluates_a_dms_system_like_the_c_abi():
+    """The mirror built from the TEMOA system (1-4 exceptions included)
+    evaluates exactly as the C ABI on the same system."""
+    from openmm_sdm_plugin_gb300 import force_from_system
+    s = temoa_system()
+    f = force_from_system(s)
+    e, F = f.evaluate(s.positions[0])
+    h = capi.Handle([s])
+    h.set_params(0, s.params[0].as_array())
+    res, Fh = h.evaluate(s.positions[0])
+    assert e == res[0, capi.R_EPOT] and f.getBindE() == res[0, capi.R_BINDE]
+    assert np.array_equal(F, Fh)
+    f.close()
+    h.close()
