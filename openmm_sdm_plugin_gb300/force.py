@@ -141,6 +141,22 @@ class SDMForce:
     def getEwaldErrorTolerance(self) -> float:
         return self._ewald_tol
 
+    # the model of the path has neither (the reference's loader turns the
+    # dispersion correction off, example/desmonddmsfile75.py:427-428)
+    def setUseDispersionCorrection(self, use: bool):
+        if use:
+            raise ValueError("the dispersion correction is not supported")
+
+    def getUseDispersionCorrection(self) -> bool:
+        return False
+
+    def setUseSwitchingFunction(self, use: bool):
+        if use:
+            raise ValueError("switching functions are not supported")
+
+    def getUseSwitchingFunction(self) -> bool:
+        return False
+
     def setCutoffDistance(self, rc: float):
         self._cutoff = float(rc)
         self._topology_dirty = True

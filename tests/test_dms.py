@@ -222,6 +222,11 @@ def test_mirror_exception_rules():
         f.setNonbondedMethod(3)                   # Ewald
     f.setNonbondedMethod(SDMForce.PME)
     assert f._system().nonbonded_method == "pme"
+    f.setUseDispersionCorrection(False)
+    f.setUseSwitchingFunction(False)
+    for setter in (f.setUseDispersionCorrection, f.setUseSwitchingFunction):
+        with pytest.raises(ValueError, match="not supported"):
+            setter(True)
 
 
 @pytest.mark.gpu
