@@ -405,8 +405,9 @@ class LangevinIntegratorSDM(SDMForce):
     def _sync(self, device: int = 0):
         rebuilt = self._topology_dirty or self._handle is None
         super()._sync(device)
-        if rebuilt:
+        if rebuilt:   # a new handle holds neither the waters nor the Langevin parameters
             self._waters_dirty = self._waters is not None
+            self._lv_dirty = True
         if self._waters_dirty:
             if self._waters is None:
                 self._handle.set_rigid_waters(0, None)

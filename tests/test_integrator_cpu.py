@@ -104,3 +104,40 @@ def test_equilibrium_steps_go_in_one_call():
     integ._advance = lambda steps: calls.append(steps)
     integ.step(7)
     assert calls == [7] and integ.getNoneqWorkvalue() == 0.0
+
+
+class _FakeHandle:
+    """Records the configuration calls a mirror makes on its handle."""
+    made = []
+
+    def __init__(self, systems, device=0):
+        self.calls = []
+        _FakeHandle.made.append(self)
+
+    def __getattr__(self, name):
+        def call(*args, **kw):
+            self.calls.append(name)
+        return call
+
+
+def test_a_rebuilt_handle_gets_the_langevin_parameters_and_waters_again(monkeypatch):
+    """A topology change after stepping makes a new handle; the integrator
+    mirror sends it the rigid waters at once and the Langevin parameters
+    before its next step."""
+    from openmm_sdm_plugin_gb300 import force as F
+    monkeypatch.setattr(F.capi, "Handle", _FakeHandle)
+    _FakeHandle.made = []
+    integ = F.LangevinIntegratorSDM(300.0, 1.0, 0.002)
+    for _ in range(6):
+        integ.addParticle(0.0, 0.3, 0.5, mass=16.0)
+    integ.setPeriodicBoxVectors((3, 0, 0), (0, 3, 0), (0, 0, 3))
+    integ.setRigidWaters([[0, 1, 2], [3, 4, 5]], 0.09572, 0.15139)
+    integ._sync()
+    integ._lv_dirty = False          # as after the first step's set_langevin
+    integ._sync()                    # nothing changed: same handle, nothing re-sent
+    assert len(_FakeHandle.made) == 1 and not integ._lv_dirty
+    integ.setCutoffDistance(1.2)     # topology change: a new handle
+    integ._sync()
+    assert len(_FakeHandle.made) == 2
+    assert "set_rigid_waters" in _FakeHandle.made[1].calls and "set_params" in _FakeHandle.made[1].calls
+    assert integ._lv_dirty
