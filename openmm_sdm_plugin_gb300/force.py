@@ -420,6 +420,9 @@ class LangevinIntegratorSDM(SDMForce):
         import torch
         x = np.ascontiguousarray(np.asarray(positions, np.float64).reshape(-1, 3))
         v = np.zeros_like(x) if velocities is None else np.asarray(velocities, np.float64).reshape(-1, 3)
+        n = len(self._q)
+        if x.shape[0] != n or v.shape != x.shape:
+            raise ValueError(f"positions and velocities must be ({n}, 3)")
         dev = torch.device("cuda", device)
         self._x = torch.from_numpy(x.copy()).to(dev)
         self._v = torch.from_numpy(np.ascontiguousarray(v)).to(dev)
@@ -456,6 +459,11 @@ class LangevinIntegratorSDM(SDMForce):
     def _advance(self, steps: int):
         """`steps` fused steps on the device; returns the results of the last."""
         import torch
+        # the kernels take raw pointers: the resident buffers must match the
+        # particle count (a particle added after setState would not)
+        n = len(self._q)
+        if self._x.shape[0] != n or self._v.shape[0] != n:
+            raise ValueError(f"the state holds {self._x.shape[0]} particles, the system {n}: call setState")
         self._sync(self._x.device.index or 0)
         if self._im is None:
             m = np.asarray(self._mass[:len(self._q)], np.float64)

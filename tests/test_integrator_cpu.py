@@ -141,3 +141,19 @@ def test_a_rebuilt_handle_gets_the_langevin_parameters_and_waters_again(monkeypa
     assert len(_FakeHandle.made) == 2
     assert "set_rigid_waters" in _FakeHandle.made[1].calls and "set_params" in _FakeHandle.made[1].calls
     assert integ._lv_dirty
+
+
+def test_state_must_match_the_particle_count():
+    """The fused step takes raw device pointers, so the mirror refuses a state
+    whose size differs from the system's before any device call."""
+    integ = LangevinIntegratorSDM(300.0, 1.0, 0.002)
+    for _ in range(4):
+        integ.addParticle(0.0, 0.3, 0.5, mass=16.0)
+    with pytest.raises(ValueError, match=r"\(4, 3\)"):
+        integ.setState(np.zeros((3, 3)))
+    with pytest.raises(ValueError, match=r"\(4, 3\)"):
+        integ.setState(np.zeros((4, 3)), np.zeros((5, 3)))
+    integ._x = integ._v = np.zeros((4, 3))   # a state of 4 particles ...
+    integ.addParticle(0.0, 0.3, 0.5)         # ... then a fifth particle
+    with pytest.raises(ValueError, match="setState"):
+        integ.step(1)
