@@ -179,6 +179,13 @@ def restraint_desc(rs, keep):
     return d
 
 
+def n_displaced(d) -> int:
+    """Particles with a nonzero displacement vector (d: (N, 3), flat, or None)."""
+    if d is None:
+        return 0
+    return int(np.count_nonzero(np.any(np.asarray(d, np.float64).reshape(-1, 3) != 0.0, axis=1)))
+
+
 class Handle:
     """Owning wrapper of one ``sdm_handle``.
 
@@ -241,6 +248,9 @@ class Handle:
             self.rep_sys += [k] * r
             self.rep_n += [int(s.charge.shape[0])] * r
         self.total_particles = int(sum(self.rep_n))
+        # displaced particles per system (the library's rule: a nonzero
+        # displacement vector); sizes the adjoint output
+        self.sys_nD = [n_displaced(getattr(s, "displacement", None)) for s in self.systems]
         for k, s in enumerate(self.systems):
             if getattr(s, "restraints", None) is not None:
                 self.set_restraints(k, s.restraints)
@@ -292,6 +302,7 @@ class Handle:
     def set_displacement(self, system: int, d):
         dd = np.ascontiguousarray(np.asarray(d, np.float64).reshape(-1))
         self._check(self.lib.sdm_set_displacement(self.h, int(system), dd.ctypes.data))
+        self.sys_nD[int(system)] = n_displaced(dd)
 
     def set_option(self, opt: int, value: int):
         self._check(self.lib.sdm_set_option(self.h, int(opt), int(value)))
@@ -315,9 +326,14 @@ class Handle:
         self._check(self.lib.sdm_set_particle_params(self.h, int(system), int(idx.size), idx.ctypes.data,
                                                      q.ctypes.data, sg.ctypes.data, ep.ctypes.data))
 
-    def adjoint(self, n_displaced):
-        """Adjoint sums of the last evaluation: (sum over replicas of nD, 2 states, 3)."""
-        out = np.zeros(6 * int(n_displaced))
+    def adjoint(self, n_displaced=None):
+        """Adjoint sums of the last evaluation: (sum over replicas of nD, 2 states, 3).
+        The output is sized from the handle's own displaced-particle count;
+        n_displaced, when given, must equal it."""
+        total = sum(self.sys_nD[k] for k in self.rep_sys)
+        if n_displaced is not None and int(n_displaced) != total:
+            raise ValueError(f"the replicas hold {total} displaced particles, not {int(n_displaced)}")
+        out = np.zeros(6 * total)
         self._check(self.lib.sdm_adjoint(self.h, out.ctypes.data))
         return out.reshape(-1, 2, 3)
 

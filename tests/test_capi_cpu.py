@@ -124,3 +124,15 @@ def test_descriptor_errors_are_reported_before_any_device_query(built_lib):
             capi.Handle([s, bad])
         assert e.value.status == capi.SDM_ERR_INVALID_ARGUMENT, (msg, e.value)
         assert "system 1" in str(e.value) and msg in str(e.value), str(e.value)
+
+
+def test_displaced_count_follows_the_library_rule():
+    """Handle.adjoint sizes its output from this count (the library writes six
+    doubles per displaced particle and replica): a particle is displaced iff
+    its displacement vector is nonzero; -0.0 counts as zero."""
+    from openmm_sdm_plugin_gb300 import capi
+    d = np.zeros((5, 3))
+    d[1] = [0.0, 0.0, 1e-300]
+    d[3] = [-0.0, -0.0, -0.0]
+    d[4] = [2.0, 0.0, 0.0]
+    assert capi.n_displaced(d) == 2 and capi.n_displaced(d.reshape(-1)) == 2 and capi.n_displaced(None) == 0
