@@ -7,8 +7,9 @@ names, argument meanings, defaults (openmmapi/src/LangevinIntegratorSDM.cpp:48-8
 and error behaviour (an unknown soft-core method raises, as
 LangevinIntegratorSDM.cpp:147 throws).  On top of that it holds what the
 reference takes from OpenMM's NonbondedForce in force group 2: per-particle
-charge/sigma/epsilon, exclusions, cutoff, reaction-field dielectric and the
-periodic box.
+charge/sigma/epsilon, exclusions and exceptions (the 1-4 pairs), the
+electrostatics (CutoffPeriodic reaction field or PME with its Ewald
+tolerance), cutoff, reaction-field dielectric and the periodic box.
 
 ``evaluate`` does what one reference step does to the nonbonded group
 (LangevinIntegratorSDM.cpp:158-176 plus ReferenceSDMKernels.cpp:202-318 without
