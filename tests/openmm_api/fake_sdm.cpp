@@ -6,6 +6,7 @@
 //   results[SDM_R_RESERVED]   = number of sdm_set_params calls on this handle
 //   results[SDM_R_U0]         = the handle's box edge x
 //   results[SDM_R_U1]         = number of sdm_create calls in the process
+//   results[SDM_R_U], [SDM_R_W], [SDM_R_DW] = 7, 11, 13
 // Forces are zero.
 #include "sdm_capi.h"
 
@@ -62,6 +63,9 @@ sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double*
         results[SDM_R_RESERVED] = h->set_params_calls;
         results[SDM_R_U0] = h->box0;
         results[SDM_R_U1] = g_creates;
+        results[SDM_R_U] = 7.0;
+        results[SDM_R_W] = 11.0;
+        results[SDM_R_DW] = 13.0;
     }
     if (forces) std::memset(forces, 0, 3 * (size_t)h->n * sizeof(double));
     return SDM_OK;

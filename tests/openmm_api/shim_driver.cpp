@@ -12,8 +12,8 @@
 //                                           more step
 //   shim_driver rebox <input> <output>      evaluate, evaluate again, change the box and
 //                                           evaluate: results[SDM_R_RESERVED], [SDM_R_U0] and
-//                                           [SDM_R_U1] after each; then a triclinic box (an
-//                                           OpenMMException)
+//                                           [SDM_R_U1] after each, getPerturbationEnergy; then a
+//                                           triclinic box (an OpenMMException)
 //
 // Input (little-endian): int32 n, n_exceptions, method (OpenMM NonbondedMethod),
 // dispersion_correction; float64 box[3], cutoff, eps_rf, ewald_tol,
@@ -139,6 +139,9 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
             const double v[3] = {res[SDM_R_RESERVED], res[SDM_R_U0], res[SDM_R_U1]};
             put(fo, v, 3);
         }
+        double pe[5];
+        force->getPerturbationEnergy(context, pe[0], pe[1], pe[2], pe[3], pe[4]);
+        put(fo, pe, 5);
         fclose(fo);
         context.setPeriodicBoxVectors(Vec3(box[0], 0, 0), Vec3(0.5, box[1], 0), Vec3(0, 0, box[2]));
         context.getState(State::Energy, false, 1 << 2);   // throws: the box must be rectangular

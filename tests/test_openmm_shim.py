@@ -224,8 +224,11 @@ def test_box_change_rebuilds_the_handle(fake_driver, tmp_path):
     s = S.config0(variant="b")
     r, out = run(fake_driver, "rebox", tmp_path, s, s.params[0], s.positions[0])
     assert r.returncode == 3 and "rectangular" in r.stderr, r.stderr
-    v = np.frombuffer(open(out, "rb").read(), np.float64).reshape(3, 3)
+    raw = np.frombuffer(open(out, "rb").read(), np.float64)
+    v, pe = raw[:9].reshape(3, 3), raw[9:]
     pushes, box_x, creates = v[:, 0], v[:, 1], v[:, 2]
+    # getPerturbationEnergy: (u, U0, U1, W, W') from the results' own slots
+    assert list(pe) == [7.0, s.box[0] + 0.1, creates[2], 11.0, 13.0]
     # the same box keeps the handle; the new box makes a new one, created
     # with that box and given the parameters once
     assert list(box_x) == [s.box[0], s.box[0], s.box[0] + 0.1]
