@@ -368,8 +368,20 @@ sdm_status sdm_set_particle_params(sdm_handle* h, int system, int n, const int* 
  * D_r = displaced particles of the replicas before r.  Host pointer;
  * synchronises.  The parameter gradient of U_lambda = U0 + W is
  * (1-s) dU_0 + s dU_1 with s = results[SDM_R_S]; the displacement gradient
- * is -s F1 (sdm_get_state_forces). */
+ * is -s F1 (sdm_get_state_forces).  `out` holds 6 * sdm_get_num_perturbed
+ * doubles. */
 sdm_status sdm_adjoint(sdm_handle* h, double* out);
+
+/* The same sums into a device buffer of 6 * sdm_get_num_perturbed doubles,
+ * asynchronous on `stream` (a cudaStream_t, NULL = the handle's own stream).
+ * The stream must be the one of the last evaluation, or ordered after it.
+ * No counterpart in the reference (see sdm_adjoint). */
+sdm_status sdm_adjoint_device(sdm_handle* h, double* out, void* stream);
+
+/* Number of (replica, displaced particle) entries of the adjoint output: the
+ * sum over replicas of their system's particles with a nonzero displacement
+ * under the current displacement maps.  No counterpart in the reference. */
+sdm_status sdm_get_num_perturbed(const sdm_handle* h, int* count);
 
 /* Diagnostic export of the clustering and neighbour lists of replica
  * `replica` for coordinates x (host pointer, that replica's 3*num_particles):

@@ -42,7 +42,7 @@ EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_get_state_forces", "sdm_check_status", "sdm_set_option", "sdm_get_option",
             "sdm_get_kernel_times", "sdm_autotune", "sdm_count_pairs", "sdm_get_grid",
             "sdm_export_lists", "sdm_evaluate_noalloc", "sdm_set_particle_params",
-            "sdm_adjoint", "sdm_set_langevin", "sdm_langevin_step", "sdm_set_restraints",
+            "sdm_adjoint", "sdm_adjoint_device", "sdm_get_num_perturbed", "sdm_set_langevin", "sdm_langevin_step", "sdm_set_restraints",
             "sdm_set_restraint_control", "sdm_get_restraint_energies", "sdm_set_rigid_waters")
 
 NB_REACTION_FIELD, NB_PME = 0, 1
@@ -114,6 +114,8 @@ def load_library(path: str = LIB_PATH):
                                            C.c_double, vp, vp, vp, vp]
         L.sdm_set_particle_params.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp]
         L.sdm_adjoint.argtypes = [vp, vp]
+        L.sdm_adjoint_device.argtypes = [vp, vp, vp]
+        L.sdm_get_num_perturbed.argtypes = [vp, ip]
         L.sdm_set_langevin.argtypes = [vp, C.POINTER(LangevinParams), C.c_ulonglong]
         L.sdm_langevin_step.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int, vp]
         L.sdm_set_restraints.argtypes = [vp, C.c_int, C.POINTER(RestraintDesc)]
@@ -179,13 +181,6 @@ def restraint_desc(rs, keep):
     return d
 
 
-def n_displaced(d) -> int:
-    """Particles with a nonzero displacement vector (d: (N, 3), flat, or None)."""
-    if d is None:
-        return 0
-    return int(np.count_nonzero(np.any(np.asarray(d, np.float64).reshape(-1, 3) != 0.0, axis=1)))
-
-
 class Handle:
     """Owning wrapper of one ``sdm_handle``.
 
@@ -248,9 +243,6 @@ class Handle:
             self.rep_sys += [k] * r
             self.rep_n += [int(s.charge.shape[0])] * r
         self.total_particles = int(sum(self.rep_n))
-        # displaced particles per system (the library's rule: a nonzero
-        # displacement vector); sizes the adjoint output
-        self.sys_nD = [n_displaced(getattr(s, "displacement", None)) for s in self.systems]
         for k, s in enumerate(self.systems):
             if getattr(s, "restraints", None) is not None:
                 self.set_restraints(k, s.restraints)
@@ -302,7 +294,6 @@ class Handle:
     def set_displacement(self, system: int, d):
         dd = np.ascontiguousarray(np.asarray(d, np.float64).reshape(-1))
         self._check(self.lib.sdm_set_displacement(self.h, int(system), dd.ctypes.data))
-        self.sys_nD[int(system)] = n_displaced(dd)
 
     def set_option(self, opt: int, value: int):
         self._check(self.lib.sdm_set_option(self.h, int(opt), int(value)))
@@ -326,16 +317,28 @@ class Handle:
         self._check(self.lib.sdm_set_particle_params(self.h, int(system), int(idx.size), idx.ctypes.data,
                                                      q.ctypes.data, sg.ctypes.data, ep.ctypes.data))
 
+    def num_perturbed(self) -> int:
+        """(replica, displaced particle) entries of the adjoint output, as the
+        library counts them."""
+        v = C.c_int(0)
+        self._check(self.lib.sdm_get_num_perturbed(self.h, C.byref(v)))
+        return v.value
+
     def adjoint(self, n_displaced=None):
         """Adjoint sums of the last evaluation: (sum over replicas of nD, 2 states, 3).
-        The output is sized from the handle's own displaced-particle count;
+        The output is sized from the library's own displaced-particle count;
         n_displaced, when given, must equal it."""
-        total = sum(self.sys_nD[k] for k in self.rep_sys)
+        total = self.num_perturbed()
         if n_displaced is not None and int(n_displaced) != total:
             raise ValueError(f"the replicas hold {total} displaced particles, not {int(n_displaced)}")
         out = np.zeros(6 * total)
         self._check(self.lib.sdm_adjoint(self.h, out.ctypes.data))
         return out.reshape(-1, 2, 3)
+
+    def adjoint_device(self, out_ptr: int, stream: int = 0):
+        """sdm_adjoint_device: the sums into a device buffer of 6 * num_perturbed()
+        doubles, asynchronous on ``stream``."""
+        self._check(self.lib.sdm_adjoint_device(self.h, C.c_void_p(out_ptr), C.c_void_p(stream) if stream else None))
 
     def set_langevin(self, step_size: float, friction: float, temperature: float, seed: int = 0,
                      step: int = 0):

@@ -240,6 +240,11 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
         s.hs[i] = (float)(0.5 * d.sigma[i]);
         s.se[i] = (float)(2.0 * std::sqrt(d.epsilon[i]));
     }
+    // the same rule as sdm_set_displacement: a NaN would break the ordering of
+    // the displacement-group map and reach the kernels as displaced coordinates
+    if (d.displacement)
+        for (size_t k = 0; k < 3 * (size_t)n; ++k)
+            if (!std::isfinite(d.displacement[k])) return "non-finite displacement";
     // exclusions: symmetric CSR, sorted, de-duplicated
     std::vector<std::vector<int>> adj(n);
     for (int e = 0; e < d.num_exclusions; ++e) {
@@ -1552,6 +1557,24 @@ sdm_status sdm_adjoint(sdm_handle* h, double* out) {
     const size_t n = 3 * (size_t)h->args.total_pert;
     if (n) SDM_CUDA(h, cudaMemcpyAsync(out, h->args.adj, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SDM_OK;
+}
+
+sdm_status sdm_adjoint_device(sdm_handle* h, double* out, void* stream) {
+    if (!h || !out) return SDM_ERR_INVALID_ARGUMENT;
+    if (h->pme) return fail(h, SDM_ERR_INVALID_ARGUMENT, "parameter derivatives are reaction-field only");
+    if (!h->have_eval) return fail(h, SDM_ERR_INVALID_ARGUMENT, "no evaluation yet");
+    cudaSetDevice(h->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+    SDM_CUDA(h, sdm_launch_adjoint(h->args, st));
+    const size_t n = 3 * (size_t)h->args.total_pert;
+    if (n) SDM_CUDA(h, cudaMemcpyAsync(out, h->args.adj, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    return SDM_OK;
+}
+
+sdm_status sdm_get_num_perturbed(const sdm_handle* h, int* count) {
+    if (!h || !count) return SDM_ERR_INVALID_ARGUMENT;
+    *count = h->args.total_pert / 2;
     return SDM_OK;
 }
 

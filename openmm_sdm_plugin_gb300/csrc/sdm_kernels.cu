@@ -1920,11 +1920,20 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     double fp;
     const double be = softcore(u, (int)p[SDM_P_SOFTCORE_METHOD], p[SDM_P_UMAX], p[SDM_P_ACORE],
                                p[SDM_P_UBCORE], &fp);
+    // dW/dlambda sees the reference's function-scope lambda1, lambda2, alpha, u0
+    // (ReferenceSDMKernels.cpp:214-217, 289-297): the scheduled values of its
+    // non-equilibrium block are block-local (:236-239) and only the
+    // integrated-logistic branch reloads them (:255-260).  For linear and
+    // quadratic bias that is lambda1 = lambda2 (only their difference, 0,
+    // enters), alpha = 1, u0 = 0 (the OpenCL platform does the same,
+    // OpenCLSDMKernels.cpp:156-185,256-265).
+    const bool ilog = method == SDM_ILOGISTIC;
+    const double dl1 = ilog ? l1 : lambdac, dl2 = ilog ? l2 : lambdac, du0 = ilog ? u0 : 0.0;
     // e^(-alpha (u' - u0)) and log(1 + e^...), shared by the integrated-logistic
     // bias and dW/dlambda (one thread: the FP64 transcendentals are serial)
     double ex = 0.0, ee = 1.0, lee = 0.0;
-    if (method == SDM_ILOGISTIC || noneq == 1) {
-        ex = exp(-alpha * (be - u0));
+    if (ilog || noneq == 1) {
+        ex = exp(-alpha * (be - du0));
         ee = 1.0 + ex;
         lee = log(ee);
     }
@@ -1944,7 +1953,7 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     double dwdl = 0.0;
     if (noneq == 1) {
         dwdl = (-lee / alpha) * p[SDM_P_M_LAMBDA1] + (be + lee / alpha) * p[SDM_P_M_LAMBDA2] +
-               ((l2 - l1) * ex / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
+               ((dl2 - dl1) * ex / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
     }
     int st = *(volatile int*)a.status;
     if (!isfinite(U0) || !isfinite(u)) { st |= SDM_DEV_ENERGY_NONFINITE; atomicOr(a.status, SDM_DEV_ENERGY_NONFINITE); }
@@ -2614,9 +2623,12 @@ __device__ void na_combine(const double* p, double U0, double u, int st, double*
     }
     double dwdl = 0.0;
     if (noneq == 1) {
-        const double ee = 1.0 + exp(-alpha * (be - u0));
+        // linear and quadratic bias: lambda1 = lambda2, alpha = 1, u0 = 0, as in k_finalize
+        const bool ilog = method == SDM_ILOGISTIC;
+        const double dl1 = ilog ? l1 : lambdac, dl2 = ilog ? l2 : lambdac, du0 = ilog ? u0 : 0.0;
+        const double ee = 1.0 + exp(-alpha * (be - du0));
         dwdl = (-log(ee) / alpha) * p[SDM_P_M_LAMBDA1] + (be + log(ee) / alpha) * p[SDM_P_M_LAMBDA2] +
-               ((l2 - l1) * exp(-alpha * (be - u0)) / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
+               ((dl2 - dl1) * exp(-alpha * (be - du0)) / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
     }
     if (!isfinite(U0) || !isfinite(u)) st |= SDM_DEV_ENERGY_NONFINITE;
     o[SDM_R_U0] = U0;

@@ -187,9 +187,21 @@ public:
         return res_[SDM_R_EPOT];
     }
 
+    /* All or nothing: on any error the handle and this object keep the
+     * parameters and displacements of the last successful update, so a later
+     * re-creation (box change) applies consistent values. */
     void updateParametersInContext(const SDMForce& f) {
+        if (f.displ_.size() != displ_.size())
+            throw OpenMMException("SDMForce: the displacement map must keep the particle count");
+        for (double v : f.displ_)
+            if (!std::isfinite(v)) throw OpenMMException("SDMForce: invalid displacement: non-finite value");
         check(sdm_set_params(h_, 0, f.p_), h_, "invalid SDM parameters");
-        check(sdm_set_displacement(h_, 0, f.displ_.data()), h_, "invalid displacement");
+        const sdm_status st = sdm_set_displacement(h_, 0, f.displ_.data());
+        if (st != SDM_OK) {
+            const std::string msg = std::string("invalid displacement: ") + sdm_last_error(h_);
+            sdm_set_params(h_, 0, p_);   // back to the parameters that this object still holds
+            throw OpenMMException("SDMForce: " + msg);
+        }
         for (int k = 0; k < SDM_NPARAMS; ++k) p_[k] = f.p_[k];
         ntmax_ = f.ntmax_;
         displ_ = f.displ_;

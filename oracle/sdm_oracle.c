@@ -366,10 +366,25 @@ void orc_combine(const double* p, double U0, double U1, double* out) {
     }
     double dwdl = 0.0;
     if ((int)p[P_NONEQ] == 1) {
-        double ee = 1.0 + exp(-alpha * (be - u0));
-        double dwdl1 = -log(ee) / alpha;
-        double dwdl2 = be + log(ee) / alpha;
-        double dwdu0 = (l2 - l1) * exp(-alpha * (be - u0)) / ee;
+        /* ReferenceSDMKernels.cpp:289-297 reads the function-scope lambda1,
+         * lambda2, alpha, u0 (:214-217).  The scheduled values of the
+         * non-equilibrium block are block-local declarations (:236-239), and
+         * only the integrated-logistic branch (:255-260) reloads the outer
+         * ones.  For linear and quadratic bias the derivative therefore sees
+         * lambda1 = lambda2 (the lambda before the step), alpha = 1 and
+         * u0 = 0; the lambda value itself only enters as lambda2 - lambda1 = 0.
+         * OpenCLSDMKernels.cpp:156-185,256-265 behaves the same. */
+        double dl1 = l1, dl2 = l2, da = alpha, du0 = u0;
+        if (method != 2) {
+            dl1 = lambdac;
+            dl2 = lambdac;
+            da = 1.0;
+            du0 = 0.0;
+        }
+        double ee = 1.0 + exp(-da * (be - du0));
+        double dwdl1 = -log(ee) / da;
+        double dwdl2 = be + log(ee) / da;
+        double dwdu0 = (dl2 - dl1) * exp(-da * (be - du0)) / ee;
         dwdl = dwdl1 * p[P_ML1] + dwdl2 * p[P_ML2] + dwdu0 * p[P_MU0] + 1.0 * p[P_MW0];
     }
     out[0] = u;

@@ -3,7 +3,7 @@ example/temoa-g1-g4.dms (TEMOA host, guests G1 and G4, 6,734 waters, ions;
 20,446 particles) through the package's own DMS reader, so that the GPU
 parity test runs on a real system where the reference tree is absent.
 
-    python tests/golden/make_dms_fixture.py /root/reference/example/temoa-g1-g4.dms
+    python tests/golden/make_dms_fixture.py <reference>/example/temoa-g1-g4.dms
 
 Positions, charges and masses are stored as float32 (the fixture defines the
 test input); LJ parameters by type; exclusions and 1-4 exceptions as read.

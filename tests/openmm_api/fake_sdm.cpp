@@ -49,8 +49,13 @@ sdm_status sdm_set_params(sdm_handle* h, int replica, const double* params) {
     return SDM_OK;
 }
 
+// refuses displacement components beyond 1e6 nm (a library-side refusal
+// for the plugin's all-or-nothing update test)
 sdm_status sdm_set_displacement(sdm_handle* h, int system, const double* d) {
-    return (h && system == 0 && d) ? SDM_OK : SDM_ERR_INVALID_ARGUMENT;
+    if (!h || system != 0 || !d) return SDM_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < 3 * h->n; ++k)
+        if (d[k] > 1.0e6) return SDM_ERR_INVALID_ARGUMENT;
+    return SDM_OK;
 }
 
 sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double* forces) {

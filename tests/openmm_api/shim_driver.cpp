@@ -25,6 +25,7 @@
 #include "openmm/Context.h"
 #include "openmm/System.h"
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
@@ -147,6 +148,30 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
         context.getState(State::Energy, false, 1 << 2);   // throws: the box must be rectangular
         return 0;
     }
+    if (mode == "atomic") {
+        // a failed updateParametersInContext leaves the context's parameters
+        // and displacements as they were, also for a handle re-created later
+        auto energy = [&]() { return context.getState(State::Energy, false, 1 << 2).getPotentialEnergy(); };
+        double v[6];
+        v[0] = energy();
+        const double lam = force->getLambda();
+        int threw = 0;
+        force->setLambda(lam + 0.1);
+        force->setDisplacement(0, std::nan(""), 0.0, 0.0);   // refused by the force before any push
+        try { force->updateParametersInContext(context); } catch (const OpenMMException&) { threw |= 1; }
+        v[1] = energy();
+        force->setDisplacement(0, 2.0e6, 0.0, 0.0);          // refused by the library after the parameters
+        force->setLambda(lam + 0.2);
+        try { force->updateParametersInContext(context); } catch (const OpenMMException&) { threw |= 2; }
+        v[2] = energy();
+        context.setPeriodicBoxVectors(Vec3(box[0] + 0.1, 0, 0), Vec3(0, box[1], 0), Vec3(0, 0, box[2]));
+        v[3] = energy();   // a new handle, made from what the context holds
+        v[4] = force->getResults(context)[SDM_R_U1];
+        v[5] = threw;
+        put(fo, v, 6);
+        fclose(fo);
+        return 0;
+    }
     if (mode == "noneq") {
         force->setNonEquilibrium(1);
         force->setNoneqtmax(ntmax);
@@ -199,7 +224,7 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
 
 int main(int argc, char** argv) {
     if (argc != 4) {
-        fprintf(stderr, "usage: shim_driver describe|evaluate|noneq|rebox <input> <output>\n");
+        fprintf(stderr, "usage: shim_driver describe|evaluate|noneq|rebox|atomic <input> <output>\n");
         return 2;
     }
     try {

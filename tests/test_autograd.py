@@ -187,3 +187,38 @@ def test_ti_dudlambda_chain_rule():
     fd = (float(U_of(0.37 + h)[0]) - float(U_of(0.37 - h)[0])) / (2 * h)
     eng.close()
     assert float(lam.grad) == pytest.approx(fd, rel=1e-6, abs=1e-6)
+
+
+@pytest.mark.gpu
+def test_num_perturbed_follows_the_displacement_rule_and_device_adjoint_matches():
+    """The adjoint output holds 6 doubles per (replica, displaced particle);
+    the library's count is the one callers size their buffers from.  A
+    particle is displaced iff its displacement vector is nonzero (-0.0 counts
+    as zero).  The device variant writes the same sums as the host one."""
+    from openmm_sdm_plugin_gb300 import capi
+    s = S.config2(nrep=2)
+    h = capi.Handle([s])
+    for r in range(2):
+        h.set_params(r, s.params[r].as_array())
+    nd = int(np.count_nonzero(np.any(s.displacement != 0, axis=1)))
+    assert h.num_perturbed() == 2 * nd
+    d = s.displacement.copy()
+    lig = np.nonzero(np.any(d != 0, axis=1))[0]
+    d[lig[0]] = [-0.0, -0.0, -0.0]
+    d[0] = [0.0, 0.0, 1e-300]
+    h.set_displacement(0, d)
+    assert h.num_perturbed() == 2 * nd
+    d[lig[1]] = 0.0
+    h.set_displacement(0, d)
+    assert h.num_perturbed() == 2 * (nd - 1)
+    x = np.ascontiguousarray(s.positions.reshape(-1, 3))
+    h.evaluate(x)
+    G = h.adjoint()
+    out = torch.full((6 * h.num_perturbed(),), float("nan"), dtype=torch.float64, device="cuda")
+    st = torch.cuda.Stream()
+    h.adjoint_device(out.data_ptr(), st.cuda_stream)
+    st.synchronize()
+    assert np.array_equal(out.cpu().numpy(), G.reshape(-1))
+    with pytest.raises(ValueError):
+        h.adjoint(n_displaced=nd)
+    h.close()

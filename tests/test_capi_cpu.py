@@ -118,21 +118,11 @@ def test_descriptor_errors_are_reported_before_any_device_query(built_lib):
         (_bad(s, eps_rf=0.0), "reaction_field_dielectric"),
         (_bad(s, exclusions=ex), "exclusion index out of range"),
         (_bad(s, nonbonded_method="pme", ewald_tolerance=0.7), "ewald_tolerance"),
+        (_bad(s, displacement=_with(s.displacement, (7, 1), np.nan)), "non-finite displacement"),
+        (_bad(s, displacement=_with(s.displacement, (2, 0), -np.inf)), "non-finite displacement"),
     ]
     for bad, msg in cases:
         with pytest.raises(capi.SdmError) as e:
             capi.Handle([s, bad])
         assert e.value.status == capi.SDM_ERR_INVALID_ARGUMENT, (msg, e.value)
         assert "system 1" in str(e.value) and msg in str(e.value), str(e.value)
-
-
-def test_displaced_count_follows_the_library_rule():
-    """Handle.adjoint sizes its output from this count (the library writes six
-    doubles per displaced particle and replica): a particle is displaced iff
-    its displacement vector is nonzero; -0.0 counts as zero."""
-    from openmm_sdm_plugin_gb300 import capi
-    d = np.zeros((5, 3))
-    d[1] = [0.0, 0.0, 1e-300]
-    d[3] = [-0.0, -0.0, -0.0]
-    d[4] = [2.0, 0.0, 0.0]
-    assert capi.n_displaced(d) == 2 and capi.n_displaced(d.reshape(-1)) == 2 and capi.n_displaced(None) == 0

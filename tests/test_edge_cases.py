@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from openmm_sdm_plugin_gb300 import capi, systems as S
-from test_gpu_parity import _check_replica
+from helpers import check_replica
 
 pytestmark = pytest.mark.gpu
 
@@ -43,7 +43,7 @@ def test_tiny_systems_one_cell_per_axis(n, L):
     x = s.positions[0]
     res, F = h.evaluate(x)
     F0, F1 = h.state_forces()
-    _check_replica(s, x, res[0], F, F0, F1, M)
+    check_replica(s, x, res[0], F, F0, F1, M)
     assert res[0, capi.R_STATUS] == 0
 
 

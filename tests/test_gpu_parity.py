@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import FORCE_RMS_REL_TOL, U_ABS_TOL, energy_tol, rms_rel
+from helpers import FORCE_RMS_REL_TOL, U_ABS_TOL, check_replica, energy_tol, rms_rel
 from openmm_sdm_plugin_gb300 import capi, systems as S
 
 pytestmark = pytest.mark.gpu
@@ -30,44 +30,13 @@ def _handle(sysms):
     return h
 
 
-def _check_replica(s, x, res, F, F0, F1, M, strict_u=True):
-    o = oracle.OracleSystem(s)
-    a = o.f32rule(x, M)
-    b = o.states(x)
-    n0 = max(a["P0"], 1)
-    assert abs(res[capi.R_U0] - a["U0"]) < energy_tol(a["U0"], n0), (res[capi.R_U0], a["U0"])
-    assert abs(res[capi.R_U0] - b["U0"]) < energy_tol(b["U0"], n0) + 0.05
-    assert rms_rel(F0, a["F0"]) < 1e-5
-    assert rms_rel(F0, b["F0"]) < FORCE_RMS_REL_TOL
-    assert rms_rel(F1, a["F0"] + a["dF"]) < 1e-5
-    assert rms_rel(F1, b["F1"]) < FORCE_RMS_REL_TOL
-    u_ref = b["u_direct"]
-    tol = U_ABS_TOL if strict_u else max(U_ABS_TOL, 1e-6 * abs(u_ref))
-    assert abs(res[capi.R_U] - a["u"]) < tol, (res[capi.R_U], a["u"])
-    assert abs(res[capi.R_U] - u_ref) < tol, (res[capi.R_U], u_ref)
-    assert res[capi.R_U1] == pytest.approx(res[capi.R_U0] + res[capi.R_U], rel=1e-15)
-    # combine on the GPU's own energies matches the restated reference combine
-    p = s.params[0].as_array()
-    comb = oracle.combine(p, res[capi.R_U0], res[capi.R_U1])
-    assert res[capi.R_BINDE] == pytest.approx(comb[1], rel=1e-9, abs=1e-9)
-    assert res[capi.R_W] == pytest.approx(comb[3], rel=1e-9, abs=1e-9)
-    assert res[capi.R_DW] == pytest.approx(comb[4], rel=1e-9, abs=1e-12)
-    assert res[capi.R_S] == pytest.approx(comb[5], rel=1e-9, abs=1e-12)
-    assert res[capi.R_EPOT] == pytest.approx(comb[6], rel=1e-12)
-    # mixed force
-    sw = res[capi.R_S]
-    Fref = sw * b["F1"] + (1 - sw) * b["F0"]
-    assert rms_rel(F, Fref) < FORCE_RMS_REL_TOL
-    return a, b
-
-
 def test_config0_parity():
     s = S.config0(variant="b")
     h = _handle([s])
     x = s.positions[0]
     res, F = h.evaluate(x)
     F0, F1 = h.state_forces()
-    _check_replica(s, x, res[0], F, F0, F1, h.grid(0))
+    check_replica(s, x, res[0], F, F0, F1, h.grid(0))
     assert res[0, capi.R_STATUS] == 0
 
 
@@ -126,7 +95,7 @@ def test_config1_parity():
     x = s.positions[0]
     res, F = h.evaluate(x)
     F0, F1 = h.state_forces()
-    a, b = _check_replica(s, x, res[0], F, F0, F1, h.grid(0))
+    a, b = check_replica(s, x, res[0], F, F0, F1, h.grid(0))
     print("config1 U0", res[0, capi.R_U0], "u", res[0, capi.R_U], "oracle u", b["u_direct"])
 
 
@@ -136,7 +105,7 @@ def test_config1b_logistic_term():
     x = s.positions[0]
     res, F = h.evaluate(x)
     F0, F1 = h.state_forces()
-    _check_replica(s, x, res[0], F, F0, F1, h.grid(0))
+    check_replica(s, x, res[0], F, F0, F1, h.grid(0))
 
 
 def test_pair_counts_exact():
@@ -180,7 +149,7 @@ def test_batched_replicas_match_single():
     for r in range(4):
         sr = s.replica(r)
         sl = slice(r * n, (r + 1) * n)
-        _check_replica(sr, s.positions[r], res[r], F[sl], F0[sl], F1[sl], M)
+        check_replica(sr, s.positions[r], res[r], F[sl], F0[sl], F1[sl], M)
 
 
 def test_uneven_multisystem_batch():
@@ -197,7 +166,7 @@ def test_uneven_multisystem_batch():
         for q in range(s.replicas):
             sr = s.replica(q)
             sl = slice(off, off + s.n)
-            _check_replica(sr, s.positions[q], res[r], F[sl], F0[sl], F1[sl], M)
+            check_replica(sr, s.positions[q], res[r], F[sl], F0[sl], F1[sl], M)
             off += s.n
             r += 1
 
@@ -226,16 +195,22 @@ def test_bias_and_softcore_methods(bias, soft):
         assert res[0, idx] == pytest.approx(comb[k], rel=1e-9, abs=1e-12)
 
 
-def test_nonequilibrium_dwdlambda():
+@pytest.mark.parametrize("bias", [0, 1, 2])
+def test_nonequilibrium_dwdlambda(bias):
+    # linear and quadratic bias: the reference's dW/dlambda sees alpha = 1 and
+    # u0 = 0 (ReferenceSDMKernels.cpp:214-217,236-239,289-297); the oracle's CPU
+    # tests pin that scoping, this compares the device with the oracle
     s = S.config0(variant="b")
-    s.params = [S.SDMParams(bias_method=2, softcore_method=2, alpha=0.1, noneq=1, lambdac=0.3,
+    s.params = [S.SDMParams(bias_method=bias, softcore_method=2, alpha=0.1, noneq=1, lambdac=0.3,
                             m_lambda1=0.8, m_lambda2=1.0, m_u0=20.0, m_w0=2.0, b_lambda1=0.05,
-                            b_u0=100.0, umax=200, acore=1 / 16, ubcore=100)]
+                            b_u0=100.0, gamma=0.01, wb=0.4, umax=200, acore=1 / 16, ubcore=100)]
     h = _handle([s])
     res, _ = h.evaluate(s.positions[0])
     comb = oracle.combine(s.params[0].as_array(), res[0, capi.R_U0], res[0, capi.R_U1])
     assert res[0, capi.R_DWDL] == pytest.approx(comb[7], rel=1e-9)
+    assert res[0, capi.R_W] == pytest.approx(comb[3], rel=1e-9, abs=1e-12)
     assert res[0, capi.R_L1] == pytest.approx(0.8 * 0.3 + 0.05)
+    assert res[0, capi.R_U0P] == pytest.approx(20 * 0.3 + 100)
 
 
 def test_device_api_and_graph_replay():
@@ -328,7 +303,7 @@ def test_nonclique_exclusions_parity():
     x = s.positions[0]
     res, F = h.evaluate(x)
     F0, F1 = h.state_forces()
-    _check_replica(s, x, res[0], F, F0, F1, h.grid(0))
+    check_replica(s, x, res[0], F, F0, F1, h.grid(0))
     c = h.count_pairs(x)
     a = oracle.OracleSystem(s).f32rule(x, h.grid(0))
     assert int(c[0, 0]) == a["P0"]

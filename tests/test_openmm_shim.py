@@ -236,6 +236,22 @@ def test_box_change_rebuilds_the_handle(fake_driver, tmp_path):
     assert list(pushes) == [1.0, 1.0, 1.0]
 
 
+def test_failed_parameter_update_changes_nothing(fake_driver, tmp_path):
+    """updateParametersInContext is all or nothing: a non-finite displacement
+    is refused before anything is pushed, a displacement the library refuses
+    brings the handle back to the parameters it had, and a handle re-created
+    later (box change) gets the last good parameters."""
+    s = S.config0(variant="b")
+    p = dataclasses.replace(s.params[0], bias_method=0, lambdac=0.3)
+    r, out = run(fake_driver, "atomic", tmp_path, s, p, s.positions[0])
+    assert r.returncode == 0, r.stderr
+    e0, e1, e2, e3, creates, threw = np.frombuffer(open(out, "rb").read(), np.float64)
+    assert threw == 3.0
+    # the fake's energy is 100 lambda: every evaluation still sees lambda = 0.3
+    assert e0 == pytest.approx(30.0) and e1 == e0 and e2 == e0 and e3 == e0
+    assert creates == 2.0
+
+
 def test_makefile_builds_the_plugin_library(driver, tmp_path):
     """The maintainer's recipe (openmm_sdm_plugin_gb300/shim/Makefile) against
     an OPENMM_DIR made of the API subset (headers, and a libOpenMM.so of its

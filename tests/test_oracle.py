@@ -241,6 +241,54 @@ def test_noneq_dwdlambda_fd():
     assert out[10] == pytest.approx(20 * 0.3 + 100)
 
 
+def _noneq_dwdl_reference_scoping(p, U0, U1, lambda_before):
+    """ReferenceSDMKernels.cpp:202-302 for NonEquilibrium = 1, written with the
+    reference's variable scopes: the function-scope lambda1/lambda2/alpha/u0
+    (:214-217) start from the lambda before the step, 1 and 0; the scheduled
+    values of the non-equilibrium block (:236-239) are block-local and go only
+    to the integrator's setters; the integrated-logistic branch (:255-260)
+    reloads them from the integrator.  dW/dlambda (:289-297) reads the
+    function-scope names."""
+    lambda1 = lambda2 = lambda_before
+    alpha, u0 = 1.0, 0.0
+    lambdac = p.lambdac                      # t / Ntmax, assigned to the outer name (:233)
+    set_l1 = p.m_lambda1 * lambdac + p.b_lambda1
+    set_l2 = p.m_lambda2 * lambdac + p.b_lambda2
+    set_u0 = p.m_u0 * lambdac + p.b_u0
+    if p.bias_method == 2:
+        lambda1, lambda2, alpha, u0 = set_l1, set_l2, p.alpha, set_u0
+    be, _ = ref_softcore(U1 - U0, int(p.softcore_method), p.umax, p.acore, p.ubcore)
+    ee = 1.0 + math.exp(-alpha * (be - u0))
+    dwdl1 = -math.log(ee) / alpha
+    dwdl2 = be + math.log(ee) / alpha
+    dwdu0 = (lambda2 - lambda1) * math.exp(-alpha * (be - u0)) / ee
+    return dwdl1 * p.m_lambda1 + dwdl2 * p.m_lambda2 + dwdu0 * p.m_u0 + 1.0 * p.m_w0
+
+
+@pytest.mark.parametrize("bias", [0, 1, 2])
+@pytest.mark.parametrize("soft", [0, 2])
+def test_noneq_dwdlambda_reference_scoping(bias, soft):
+    p = S.SDMParams(bias_method=bias, softcore_method=soft, alpha=0.1, noneq=1, lambdac=0.3,
+                    m_lambda1=0.8, m_lambda2=1.0, m_u0=20.0, m_w0=2.0, b_lambda1=0.05,
+                    b_lambda2=0.0, b_u0=100.0, b_w0=-1.0, gamma=0.01, wb=0.4, umax=200,
+                    acore=1 / 16, ubcore=100)
+    for U0, U1 in [(-500.0, -380.0), (10.0, 5.0), (0.0, 30.0)]:
+        out = oracle.combine(p.as_array(), U0, U1)
+        # the lambda before the step only enters as lambda2 - lambda1 = 0
+        for lam_before in (0.0, 0.29, 0.7):
+            ref = _noneq_dwdl_reference_scoping(p, U0, U1, lam_before)
+            assert out[7] == pytest.approx(ref, rel=1e-13, abs=1e-13)
+        # the integrator receives the scheduled parameters for every method
+        assert out[8] == pytest.approx(0.8 * 0.3 + 0.05)
+        assert out[10] == pytest.approx(20 * 0.3 + 100)
+    if bias != 2:
+        # differs from the derivative of W along the schedule: alpha = 1 and u0 = 0
+        be, _ = ref_softcore(120.0, soft, 200.0, 1 / 16, 100.0)
+        l1e = math.log(1.0 + math.exp(-be))
+        assert oracle.combine(p.as_array(), -500.0, -380.0)[7] == pytest.approx(
+            -l1e * 0.8 + (be + l1e) * 1.0 + 2.0, rel=1e-13)
+
+
 def test_mixed_force_eval_state():
     s = S.config0(variant="b")
     o = oracle.OracleSystem(s)

@@ -7,14 +7,20 @@
 - 22 lambda states on one coordinate set give the same U0, U1, u, F0 and F1,
   and the mixed forces differ only by (s_r - s_q) dF.
 - Two calls give the same bits.
+- Every replica of the batch against both oracle rules (the parity test of
+  the benchmark input itself; oracle calls on a thread pool).
 
 Tolerances are far below any real error. The terms are the same, and the
 fixed-point force sums do not depend on order, so agreement is expected to
 the last bit; the margin only covers summation orders.  Named to run after
 the other parity files."""
+import os
+from concurrent.futures import ThreadPoolExecutor
+
 import numpy as np
 import pytest
 
+from helpers import check_replica, oracle_replica
 from openmm_sdm_plugin_gb300 import capi, systems as S
 
 pytestmark = pytest.mark.gpu
@@ -92,3 +98,18 @@ def test_two_calls_give_the_same_bits(full):
     res2, F2 = h.evaluate(s.positions.reshape(-1, 3))
     assert np.array_equal(res2[:, :capi.R_STATUS], res[:, :capi.R_STATUS])
     assert np.array_equal(F2, F)
+
+
+def test_every_replica_against_the_oracle(full):
+    """All 22 replicas of the benchmark batch against the FP64 and FP32-rule
+    oracles, with the tolerances of every other parity test (u 5e-3 kJ/mol,
+    forces 1e-4 rms relative against the FP64 rule)."""
+    s, h, res, F, F0, F1 = full
+    n = s.n
+    M = h.grid(0)
+    # the oracle's C calls release the GIL, so threads run them in parallel
+    with ThreadPoolExecutor(max_workers=min(NREP, os.cpu_count() or 1)) as ex:
+        outs = list(ex.map(lambda r: oracle_replica(s.replica(r), s.positions[r], M), range(NREP)))
+    for r in range(NREP):
+        sl = slice(r * n, (r + 1) * n)
+        check_replica(s.replica(r), s.positions[r], res[r], F[sl], F0[sl], F1[sl], M, ab=outs[r])
