@@ -40,7 +40,13 @@ FLOP_PER_PAIR = 52  # FP32 flops per pair per state (FMA = 2, rsqrt = 1)
 # k_jlist k_pair k_pert_prep k_perturb k_finalize k_mix
 KERNELS_PER_STEP = 11
 NREP = 22
+WORKLOAD = ("config2: 22 replicas x 22,580 particles (7,500 waters + 2x40 ligand), 6.2 nm box, "
+            "rc 1.0 nm reaction field, one batched call per step")
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_pair launch on this
+# workload: a stored figure from the ncu capture summarised in
+# profiles/k_pair_config2x22.md (cold cache between replay passes)
 K_PAIR_DRAM_BYTES_PER_LAUNCH = 122.466560e6 + 6.279680e6
+K_PAIR_TRAFFIC_SOURCE = "stored: ncu capture of the same workload (profiles/k_pair_config2x22.md)"
 
 
 def _peaks():
@@ -192,7 +198,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": "config2: 22 replicas x 22,580 particles, rc 1.0 nm RF, 6.2 nm box",
+        "config": {"workload": WORKLOAD,
                    "sample": f"{per_step} lambda states per step (round robin over the 22)"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
                          "sample": f"{per_step} full FP64 lambda-state evaluations per step"},
@@ -428,6 +434,73 @@ def main():
                              "states x 20,446 particles, the stored coordinates, guests displaced +-2.2 nm/axis"}
         ht.close()
 
+    # ---- the uneven multi-system batch: 64 host-guest systems x 16 lambda
+    # states (1,024 replicas, 2,010-54,820 particles each) in one call ----
+    ms3, c3 = [], None
+    s3 = S.config3()
+    h3 = capi.Handle(s3, device=local)
+    r = 0
+    for sy in s3:
+        for p in sy.params:
+            h3.set_params(r, p.as_array())
+            r += 1
+    x3h = np.ascontiguousarray(np.concatenate([sy.positions.reshape(-1, 3) for sy in s3]))
+    cnt3 = h3.count_pairs(x3h)
+    x3 = torch.from_numpy(x3h).to(dev)
+    r3 = torch.zeros((h3.nrep, capi.NRESULTS), dtype=torch.float64, device=dev)
+    f3 = torch.zeros_like(x3)
+    h3.set_option(capi.OPT_PROFILE, 2)
+    n3 = min(args.steps, 20)
+    ms3, pk3 = timed(lambda: h3.evaluate_device(x3.data_ptr(), r3.data_ptr(), f3.data_ptr(), sptr), n3, warm,
+                     per_kernel=h3.kernel_times)
+    tot3 = max_over_ranks(sum(ms3) / 1e3, dist, dev)
+    pair3 = sum(d["k_pair"] for d in pk3) / len(pk3)
+    flop3 = FLOP_PER_PAIR * int(cnt3.sum())
+    config3 = {"value": whole_job_rate(h3.nrep * n3, world, tot3), "unit": UNIT, "ms_per_call": sum(ms3) / n3,
+               "steps": n3, "device_status": h3.check_status(), "replicas": h3.nrep,
+               "particles": int(sum(sy.n * sy.replicas for sy in s3)),
+               "pair_kernel_ms": pair3, "pair_frac": None,
+               "flop_per_launch": flop3,
+               "workload": "config3: 64 host-guest systems (2,010-54,820 particles, log-uniform, seed 3) x 16 "
+                           "lambda states, every replica its own coordinates, one batched call per step"}
+    h3.close()
+    del x3, r3, f3
+
+    # ---- backward: the 22-state batch through the autograd Function, forward
+    # (evaluation, state-1 forces, adjoint sums) and backward (gradients for
+    # positions, ligand charge/sigma/epsilon, displacement map, lambda1,
+    # lambda2, alpha, u0, w0), all device-resident on one stream ----
+    from openmm_sdm_plugin_gb300.autograd import SDMEngine, sdm_potential
+    eng = SDMEngine(sysm, device=local)
+    Dl = eng.D
+    f64 = dict(dtype=torch.float64, device=dev)
+    xg = xd.view(NREP, n, 3).clone().requires_grad_(True)
+    qD = torch.tensor(sysm.charge[Dl], **f64).requires_grad_(True)
+    sD = torch.tensor(sysm.sigma[Dl], **f64).requires_grad_(True)
+    eD = torch.tensor(sysm.epsilon[Dl], **f64).requires_grad_(True)
+    dg = torch.tensor(sysm.displacement, **f64).requires_grad_(True)
+    vec = lambda k: torch.tensor([getattr(p, k) for p in sysm.params], **f64).requires_grad_(True)
+    lams = [vec(k) for k in ("lambda1", "lambda2", "alpha", "u0", "w0")]
+    leaves = [xg, qD, sD, eD, dg] + lams
+
+    def bwd_step():
+        for t in leaves:
+            t.grad = None
+        with torch.cuda.stream(stream):
+            U = sdm_potential(eng, xg, qD, sD, eD, dg, *lams)
+            U.sum().backward()
+
+    nb = min(args.steps, 100)
+    ms_bw, _ = timed(bwd_step, nb, warm)
+    tot_bw = max_over_ranks(sum(ms_bw) / 1e3, dist, dev)
+    backward = {"value": whole_job_rate(NREP * nb, world, tot_bw),
+                "unit": "lambda-state evals with full gradients/s", "ms_per_step": sum(ms_bw) / nb, "steps": nb,
+                "device_status": eng.h.check_status(),
+                "workload": "config4: forward + backward of the 22-state config2 batch through the "
+                            "torch.autograd.Function (dU/dx, dU/dq, dU/dsigma, dU/depsilon of the 80 ligand "
+                            "particles, dU/dd, dU/dlambda1, dU/dlambda2, dU/dalpha, dU/du0, dU/dw0), device timed"}
+    eng.close()
+
     # ---- e2e through the host C ABI: pinned host inputs/outputs ----
     h.set_option(capi.OPT_PROFILE, 0)
     xpin = torch.from_numpy(xh.copy()).pin_memory()
@@ -475,21 +548,20 @@ def main():
     fmax = float(peaks.get("sm_max_mhz", 2070.0))
     peak_tf = nsm * 128 * 2 * fmax * 1e6 / 1e12
     achieved_tf = flop_per_launch / (pair_avg * 1e-3) / 1e12
+    config3["pair_frac"] = flop3 / (config3["pair_kernel_ms"] * 1e-3) / 1e12 / peak_tf
     f_run = clocks.get("sm_mhz")
+    jl_avg = sum(jlist_ms) / len(jlist_ms)
+    pt_avg = sum(pert_ms) / len(pert_ms)
     roof = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
-            "frac": achieved_tf / peak_tf, "traffic": None,
+            "frac": achieved_tf / peak_tf, "traffic": K_PAIR_DRAM_BYTES_PER_LAUNCH,
+            "traffic_source": K_PAIR_TRAFFIC_SOURCE,
             "kernel": "k_pair (main pass, all 22 replicas)",
             "peak_source": f"{nsm} SMs x 128 FP32 lanes x 2 x {fmax:.0f} MHz ({src} sm_max_mhz)",
             "frac_at_run_clock": (achieved_tf / (nsm * 256 * f_run * 1e6 / 1e12)) if f_run else None,
-            "pair_kernel_ms": pair_avg, "perturb_kernel_ms": sum(pert_ms) / len(pert_ms),
-            "jlist_kernel_ms": sum(jlist_ms) / len(jlist_ms),
-            "frac_pair_path": (flop_per_launch / ((pair_avg + sum(jlist_ms) / len(jlist_ms)
-                                                   + sum(pert_ms) / len(pert_ms)) * 1e-3) / 1e12) / peak_tf,
+            "pair_kernel_ms": pair_avg, "perturb_kernel_ms": pt_avg, "jlist_kernel_ms": jl_avg,
+            "frac_pair_path": (flop_per_launch / ((pair_avg + jl_avg + pt_avg) * 1e-3) / 1e12) / peak_tf,
+            "frac_whole_call": (flop_per_launch / (sum(ms_b) / len(ms_b) * 1e-3) / 1e12) / peak_tf,
             "flop_per_launch": flop_per_launch, "P0": P0, "P1delta": P1}
-    # dram__bytes_read.sum + dram__bytes_write.sum of one k_pair launch on this
-    # workload (ncu --set full, cold cache): profiles/k_pair_k_jlist_k_perturb_config2x22.md
-    roof["traffic"] = K_PAIR_DRAM_BYTES_PER_LAUNCH
-    roof["traffic_note"] = "ncu capture of the same workload, cold cache between replay passes"
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -497,37 +569,42 @@ def main():
 
     h2d = xh.nbytes
     d2h = xh.nbytes + NREP * capi.NRESULTS * 8
+    plain_obj = {"value": plain, "unit": UNIT, "ms_per_call": sum(ms_p) / len(ms_p),
+                 "workload": "config1: one 22,580-particle replica per call (CUDA graph)"}
+    # secondary fields first, the headline keys last (a reader of the line's
+    # tail sees value, e2e, roofline, plain and batched_over_plain)
     line = {
+        "kernel_ms": breakdown,
+        "langevin": langevin,
+        "dms_temoa": temoa,
+        "pme": pme,
+        "adjoint": adjoint,
+        "config3": config3,
+        "backward": backward,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "device_status": status,
+        "wall_s_timed_region": t_wall,
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warm, "ms_per_step": sum(ms_b) / len(ms_b), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32 pairs, int64 fixed-point forces, f64 energies",
         "data": "synthetic (seeded)",
-        "config": {"workload": "config2: 22 replicas x 22,580 particles (7,500 waters + 2x40 ligand), "
-                               "6.2 nm box, rc 1.0 nm reaction field, one batched call per step as a CUDA graph",
+        "config": {"workload": WORKLOAD,
                    "replicas_per_gpu": NREP, "particles": n, "l2": "flushed (256 MB write) before every timed step",
                    "parallelism": f"replicas only, {world} independent rank(s)",
                    "schedule": {"split": h.get_option(capi.OPT_SPLIT), "ctas_per_sm": h.get_option(capi.OPT_CTAS_PER_SM),
                                 "ctas_resident": h.get_option(capi.OPT_PAIR_RESIDENT),
+                                "pair_variant": h.get_option(capi.OPT_PAIR_VARIANT),
                                 "autotuned": tuned is not None}},
-        "plain": {"value": plain, "unit": UNIT, "ms_per_call": sum(ms_p) / len(ms_p),
-                  "workload": "config1: one 22,580-particle replica per call (CUDA graph)"},
-        "batched_over_plain": value / world / plain,
+        "gpu_launches": KERNELS_PER_STEP * args.steps,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": sum(e2e_ms) / len(e2e_ms),
                 "path": "sdm_evaluate (host C ABI) on page-locked host buffers, cudaMemcpyAsync in and out",
                 "coords_in_place": {"value": e2e_zc, "ms_per_step": sum(e2e_ms_zc) / len(e2e_ms_zc),
                                     "path": "same call, SDM_OPT_ZERO_COPY=1: k_cells reads the host coordinates"}},
-        "langevin": langevin,
-        "dms_temoa": temoa,
-        "pme": pme,
-        "adjoint": adjoint,
         "roofline": roof,
-        "kernel_ms": breakdown,
-        "cpu_baseline": cpu,
-        "clocks": clocks,
-        "gpu_launches": KERNELS_PER_STEP * args.steps,
-        "device_status": status,
-        "wall_s_timed_region": t_wall,
+        "plain": plain_obj,
+        "batched_over_plain": value / world / plain,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -200,6 +200,13 @@ sdm_status sdm_evaluate_device(sdm_handle* h, const double* x, double* results, 
  * selected by `on_device`): F0 and F1 = F0 + dF, [sum 3*num_particles] each. */
 sdm_status sdm_get_state_forces(sdm_handle* h, double* F0, double* F1, int on_device);
 
+/* The same per-state forces into device buffers, asynchronous on `stream`
+ * (NULL = the handle's own stream), which must be the stream of the last
+ * evaluation or ordered after it.  Either pointer may be NULL.  The
+ * reference's counterparts are its saved state forces (SaveState1/SaveState2,
+ * platforms/reference/src/ReferenceSDMKernels.cpp:161-190). */
+sdm_status sdm_get_state_forces_device(sdm_handle* h, double* F0, double* F1, void* stream);
+
 /* Langevin dynamics on the SDM force (the caller side of the path).  One
  * sdm_langevin_step step = the two-state evaluation of every replica, then the
  * stochastic-dynamics update of platforms/reference/src/
@@ -324,10 +331,14 @@ enum {
     SDM_OPT_VERIFY = 4,       /* 1 = sdm_evaluate checks the device status word after each call */
     SDM_OPT_PAIR_RESIDENT = 5, /* read only: pair-kernel CTAs per SM that are resident for the
                                   current SDM_OPT_CTAS_PER_SM (occupancy calculator) */
-    SDM_OPT_ZERO_COPY = 6     /* 1 = sdm_evaluate reads page-locked coordinates (cudaHostAlloc /
+    SDM_OPT_ZERO_COPY = 6,    /* 1 = sdm_evaluate reads page-locked coordinates (cudaHostAlloc /
                                  cudaHostRegister) in place instead of staging them through a
                                  device copy; results and forces are always copied out (default 0:
                                  on GB300 the two measured on par) */
+    SDM_OPT_PAIR_VARIANT = 7  /* main-pass implementation: 0 = candidates staged through shared
+                                 memory by cp.async, masks in every tile (default); 1 = candidates
+                                 loaded into registers one step ahead, partial-mask candidates in
+                                 a ring of their own.  Same pair sets and terms. */
 };
 sdm_status sdm_set_option(sdm_handle* h, int option, int value);
 sdm_status sdm_get_option(const sdm_handle* h, int option, int* value);
@@ -436,6 +447,55 @@ sdm_status sdm_evaluate_noalloc(int num_particles, const double* x, const double
                                 const double* displacement, const double* box, double cutoff,
                                 double reaction_field_dielectric, const double* params,
                                 double* results, double* forces, void* stream);
+
+/* Interop with an engine that keeps its particles in its own order on the
+ * device (OpenMM's CUDA platform: posq, atom index and the 64-bit
+ * fixed-point force buffer; the reference's CUDA/OpenCL kernels read and
+ * write those arrays directly, platforms/opencl/src/OpenCLSDMKernels.cpp:86-97
+ * and platforms/cuda/src/kernels/langevin.cu:10,19-21).  Both calls are
+ * asynchronous on `stream` (a cudaStream_t, NULL = the legacy default
+ * stream) and take device pointers; errors in the arguments are reported
+ * through sdm_last_error(NULL).
+ *
+ * sdm_gather_positions: for k < n, x[3*index[k] + c] = posq[k].c (+
+ * posq_correction[k].c when not NULL, the FP32 remainder of mixed
+ * precision), c = 0..2; posq and the correction are float4, or double4 when
+ * double_precision is nonzero.  x is [3n] in the ABI's particle order. */
+sdm_status sdm_gather_positions(const void* posq, const void* posq_correction, int double_precision,
+                                const int* index, int n, double* x, void* stream);
+
+/* sdm_scatter_forces_fixed: for k < n and c = 0..2,
+ * buffer[c*padded_n + k] += round(forces[3*index[k] + c] * 2^32), with forces
+ * in kJ/mol/nm in the ABI's order and buffer the engine's component-major
+ * fixed-point accumulator. */
+sdm_status sdm_scatter_forces_fixed(const double* forces, const int* index, int n, int padded_n,
+                                    long long* buffer, void* stream);
+
+/* One evaluation of a handle of one replica, fed from and into an engine's
+ * device arrays in the engine's particle order: the positions are gathered
+ * as by sdm_gather_positions (n = the handle's particle count), the call
+ * evaluates as sdm_evaluate_device does into the handle's own buffers (a
+ * captured graph), and the mixed force is added into `force_buffer` as by
+ * sdm_scatter_forces_fixed (skipped when it is NULL).  This replaces the
+ * reference kernel's Save/Make/Restore state copies and its force mix on the
+ * engine's arrays (platforms/opencl/src/OpenCLSDMKernels.cpp:104-146,
+ * 271-276; platforms/cuda/src/kernels/langevin.cu:10,19-21).
+ *
+ * results NULL: asynchronous on `stream`; a device status error (a list
+ * overflow among them) stays in the status word for the next synchronous
+ * call or sdm_check_status, and the forces added since then are incomplete.
+ * results given (host, SDM_NRESULTS doubles): the call synchronises, a list
+ * overflow regrows the lists and evaluates again before any force is added,
+ * and another status error fails the call (SDM_OPT_VERIFY) with nothing
+ * added.  No counterpart in the reference as one call. */
+sdm_status sdm_evaluate_engine(sdm_handle* h, const void* posq, const void* posq_correction, int double_precision,
+                               const int* index, int padded_n, long long* force_buffer, double* results,
+                               void* stream);
+
+/* Results of the last evaluation (host, SDM_NRESULTS doubles per replica);
+ * synchronises the device.  The reference integrator's getters read its last
+ * step the same way (openmmapi/include/LangevinIntegratorSDM.h:301-324). */
+sdm_status sdm_get_last_results(sdm_handle* h, double* results);
 
 /* Device status bits (sdm_check_status, SDM_R_STATUS). */
 enum {

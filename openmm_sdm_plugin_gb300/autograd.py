@@ -56,16 +56,43 @@ def bias_partials(p: SDMParams, be: float) -> dict:
     return out
 
 
+def bias_partials_device(methods, be, l1, l2, alpha, u0):
+    """bias_partials for every replica at once, on the device: (R,) tensors
+    d W / d {lambda1, lambda2, alpha, u0, w0} at fixed u' = be.  methods: (R,)
+    bias method ids."""
+    zero = torch.zeros_like(be)
+    ilog = methods == ILOGISTIC
+    pos = ilog & (alpha > 0)
+    a = torch.where(pos, alpha, torch.ones_like(alpha))
+    x = -a * (be - u0)
+    e = torch.where(pos, torch.exp(x), zero)
+    ee = 1.0 + e
+    L = torch.log(ee)
+    dl = l2 - l1
+    d_l1 = torch.where(pos, -L / a, zero)
+    d_l2 = torch.where(pos, L / a + be, torch.where(ilog, be, zero))
+    d_u0 = torch.where(pos, dl * e / ee, zero)
+    d_al = torch.where(pos, dl * (-L / (a * a) - (be - u0) * e / (a * ee)), zero)
+    d_w0 = torch.where(ilog | (methods == QUADRATIC), torch.ones_like(be), zero)
+    return d_l1, d_l2, d_al, d_u0, d_w0
+
+
 class SDMEngine:
     """One system with R replicas on the GPU, prepared for differentiation.
 
     The displaced set D (particles with a nonzero displacement at creation)
     is fixed; its charges/sigmas/epsilons and the displacement values are
-    the differentiable inputs."""
+    the differentiable inputs.  Everything after the parameter pushes stays
+    on the device and on the caller's current CUDA stream: the evaluation
+    (a captured graph), the state-1 forces, the adjoint sums and the
+    backward contractions.  Parameters are pushed to the library (a host
+    call that synchronises) only when an input tensor changed: a different
+    tensor object or a new in-place version."""
 
     def __init__(self, system: SDMSystem, device: int = 0):
         self.system = system
         self.h = capi.Handle([system], device=device)
+        self.dev = torch.device("cuda", device)
         self.R = system.replicas
         self.n = system.n
         d = np.asarray(system.displacement, np.float64).reshape(-1, 3)
@@ -75,35 +102,66 @@ class SDMEngine:
         self._s = np.asarray(system.sigma, np.float64).copy()
         self._e = np.asarray(system.epsilon, np.float64).copy()
         self._d = d.copy()
+        f64 = dict(dtype=torch.float64, device=self.dev)
+        self.methods = torch.tensor([p.bias_method for p in self.base], dtype=torch.int64, device=self.dev)
+        # persistent device buffers: the captured evaluation graph keys on their addresses
+        self.x = torch.zeros((self.R * self.n, 3), **f64)
+        self.res = torch.zeros((self.R, capi.NRESULTS), **f64)
+        self.F = torch.zeros((self.R * self.n, 3), **f64)
+        self.F1 = torch.zeros((self.R * self.n, 3), **f64)
+        self.G = torch.zeros((6 * self.h.num_perturbed(),), **f64)
+        self._seen = {}
 
     def close(self):
         self.h.close()
 
+    def _changed(self, name, t) -> bool:
+        last = self._seen.get(name)
+        if last is not None and last[0] is t and last[1] == t._version:
+            return False
+        self._seen[name] = (t, t._version)
+        return True
+
+    def _push(self, qD, sD, eD, d, lam1, lam2, alpha, u0, w0):
+        host = lambda t: t.detach().to("cpu", torch.float64).numpy()
+        if self._changed("qD", qD) | self._changed("sD", sD) | self._changed("eD", eD):
+            q, sg, ep = host(qD), host(sD), host(eD)
+            if not (np.array_equal(q, self._q[self.D]) and np.array_equal(sg, self._s[self.D])
+                    and np.array_equal(ep, self._e[self.D])):
+                self._q[self.D], self._s[self.D], self._e[self.D] = q, sg, ep
+                self.h.set_particle_params(0, self.D, q, sg, ep)
+        if self._changed("d", d):
+            dd = host(d).reshape(-1, 3)
+            if not np.array_equal(dd, self._d):
+                nz = np.nonzero(np.any(dd != 0.0, axis=1))[0]
+                if not np.array_equal(nz, self.D):
+                    raise ValueError("the set of displaced particles must not change")
+                self._d = dd.copy()
+                self.h.set_displacement(0, dd)
+        names = ("lambda1", "lambda2", "alpha", "u0", "w0")
+        vals = (lam1, lam2, alpha, u0, w0)
+        if any([self._changed(k, v) for k, v in zip(names, vals)]):
+            hv = [host(v).reshape(-1) for v in vals]
+            for r in range(self.R):
+                p = dataclass_copy(self.base[r])
+                p.lambda1, p.lambda2, p.alpha, p.u0, p.w0 = (float(v[r]) for v in hv)
+                p.noneq = 0
+                self.h.set_params(r, p.as_array())
+
     def run(self, x, qD, sD, eD, d, lam1, lam2, alpha, u0, w0):
-        """Forward + everything the backward needs (FP64 numpy arrays)."""
-        if not (np.array_equal(qD, self._q[self.D]) and np.array_equal(sD, self._s[self.D])
-                and np.array_equal(eD, self._e[self.D])):
-            self._q[self.D], self._s[self.D], self._e[self.D] = qD, sD, eD
-            self.h.set_particle_params(0, self.D, qD, sD, eD)
-        d = np.asarray(d, np.float64).reshape(-1, 3)
-        if not np.array_equal(d, self._d):
-            nz = np.nonzero(np.any(d != 0.0, axis=1))[0]
-            if not np.array_equal(nz, self.D):
-                raise ValueError("the set of displaced particles must not change")
-            self._d = d.copy()
-            self.h.set_displacement(0, d)
-        params = []
-        for r in range(self.R):
-            p = dataclass_copy(self.base[r])
-            p.lambda1, p.lambda2, p.alpha, p.u0, p.w0 = (float(lam1[r]), float(lam2[r]), float(alpha[r]),
-                                                        float(u0[r]), float(w0[r]))
-            p.noneq = 0
-            self.h.set_params(r, p.as_array())
-            params.append(p)
-        res, F = self.h.evaluate(np.asarray(x, np.float64).reshape(-1, 3))
-        F0, F1 = self.h.state_forces()
-        G = self.h.adjoint(self.R * len(self.D)).reshape(self.R, len(self.D), 2, 3)
-        return res, F.reshape(self.R, self.n, 3), F1.reshape(self.R, self.n, 3), G, params
+        """Forward on the device: (U, s, F, F1, G, partials) as device tensors
+        (views of the engine's buffers: copy what must outlive the next call)."""
+        self._push(qD, sD, eD, d, lam1, lam2, alpha, u0, w0)
+        stream = torch.cuda.current_stream(self.dev).cuda_stream
+        self.x.copy_(x.detach().reshape(-1, 3))
+        self.h.evaluate_device(self.x.data_ptr(), self.res.data_ptr(), self.F.data_ptr(), stream)
+        self.h.state_forces_device(0, self.F1.data_ptr(), stream)
+        self.h.adjoint_device(self.G.data_ptr(), stream)
+        res = self.res
+        on = lambda t: t.detach().to(self.dev, torch.float64).reshape(-1)
+        part = bias_partials_device(self.methods, res[:, capi.R_BINDE], on(lam1), on(lam2), on(alpha), on(u0))
+        return (res[:, capi.R_EPOT], res[:, capi.R_S], self.F.view(self.R, self.n, 3),
+                self.F1.view(self.R, self.n, 3), self.G.view(self.R, -1, 2, 3), part)
 
 
 def dataclass_copy(p):
@@ -114,26 +172,23 @@ def dataclass_copy(p):
 class SDMPotential(torch.autograd.Function):
     """U (R,) = SDMPotential.apply(engine, x, qD, sD, eD, d, lambda1, lambda2, alpha, u0, w0)
 
-    x: (R, N, 3); qD, sD, eD: (nD,); d: (N, 3); lambda1..w0: (R,).  All FP64.
+    x: (R, N, 3); qD, sD, eD: (nD,); d: (N, 3); lambda1..w0: (R,).  All FP64,
+    on any device (the result and the gradients come back on x's device).
     Differentiable in every tensor input."""
 
     @staticmethod
     def forward(ctx, engine: SDMEngine, x, qD, sD, eD, d, lam1, lam2, alpha, u0, w0):
-        cpu = lambda t: t.detach().to("cpu", torch.float64).numpy()
-        res, F, F1, G, params = engine.run(cpu(x), cpu(qD), cpu(sD), cpu(eD), cpu(d), cpu(lam1), cpu(lam2),
-                                           cpu(alpha), cpu(u0), cpu(w0))
-        s = res[:, capi.R_S]
-        part = [bias_partials(p, res[r, capi.R_BINDE]) for r, p in enumerate(params)]
-        ctx.save_for_backward(*(torch.from_numpy(np.ascontiguousarray(v)) for v in
-                                (s, F, F1, G, cpu(eD))))
-        ctx.partials = part
-        ctx.dev = x.device
-        return torch.from_numpy(res[:, capi.R_EPOT].copy()).to(x.device)
+        U, s, F, F1, G, part = engine.run(x, qD, sD, eD, d, lam1, lam2, alpha, u0, w0)
+        ctx.save_for_backward(s.clone(), F.clone(), F1.clone(), G.clone(),
+                              eD.detach().to(engine.dev, torch.float64), *part)
+        ctx.devs = (x.device, qD.device, d.device, lam1.device)
+        return U.clone().to(x.device)
 
     @staticmethod
     def backward(ctx, gU):
-        s, F, F1, G, eD = ctx.saved_tensors
-        g = gU.detach().to("cpu", torch.float64)
+        s, F, F1, G, eD, d_l1, d_l2, d_al, d_u0, d_w0 = ctx.saved_tensors
+        xdev, pdev, ddev, ldev = ctx.devs
+        g = gU.detach().to(s.device, torch.float64)
         w = torch.stack([(1.0 - s), s], dim=1)                   # (R, 2) state weights
         gD = torch.einsum("r,rs,rksc->kc", g, w, G)              # (nD, 3)
         grad_q = gD[:, 0]
@@ -141,11 +196,9 @@ class SDMPotential(torch.autograd.Function):
         grad_e = torch.where(eD > 0, gD[:, 2] / (2.0 * eD.clamp_min(1e-300)), torch.zeros_like(eD))
         grad_d = -torch.einsum("r,r,rnc->nc", g, s, F1)
         grad_x = -g[:, None, None] * F
-        pl = lambda key: g * torch.tensor([p[key] for p in ctx.partials], dtype=torch.float64)
-        dev = ctx.dev
-        to = lambda t: t.to(dev)
-        return (None, to(grad_x), to(grad_q), to(grad_s), to(grad_e), to(grad_d), to(pl("lambda1")),
-                to(pl("lambda2")), to(pl("alpha")), to(pl("u0")), to(pl("w0")))
+        return (None, grad_x.to(xdev), grad_q.to(pdev), grad_s.to(pdev), grad_e.to(pdev), grad_d.to(ddev),
+                (g * d_l1).to(ldev), (g * d_l2).to(ldev), (g * d_al).to(ldev), (g * d_u0).to(ldev),
+                (g * d_w0).to(ldev))
 
 
 def sdm_potential(engine: SDMEngine, x, qD, sD, eD, d, lam1, lam2, alpha, u0, w0):

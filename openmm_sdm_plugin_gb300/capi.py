@@ -35,15 +35,17 @@ RESULT_FIELDS = ("U0", "U1", "u", "BindE", "fp", "W", "dW", "s", "E_pot", "dWdla
 (R_U0, R_U1, R_U, R_BINDE, R_FP, R_W, R_DW, R_S, R_EPOT, R_DWDL, R_L1, R_L2, R_U0P, R_W0P,
  R_STATUS, R_NCL) = range(16)
 
-OPT_GRAPH, OPT_PROFILE, OPT_SPLIT, OPT_CTAS_PER_SM, OPT_VERIFY, OPT_PAIR_RESIDENT, OPT_ZERO_COPY = range(7)
+(OPT_GRAPH, OPT_PROFILE, OPT_SPLIT, OPT_CTAS_PER_SM, OPT_VERIFY, OPT_PAIR_RESIDENT, OPT_ZERO_COPY,
+ OPT_PAIR_VARIANT) = range(8)
 
 EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_set_displacement", "sdm_set_params", "sdm_evaluate", "sdm_evaluate_device",
-            "sdm_get_state_forces", "sdm_check_status", "sdm_set_option", "sdm_get_option",
+            "sdm_get_state_forces", "sdm_get_state_forces_device", "sdm_check_status", "sdm_set_option", "sdm_get_option",
             "sdm_get_kernel_times", "sdm_autotune", "sdm_count_pairs", "sdm_get_grid",
             "sdm_export_lists", "sdm_evaluate_noalloc", "sdm_set_particle_params",
             "sdm_adjoint", "sdm_adjoint_device", "sdm_get_num_perturbed", "sdm_set_langevin", "sdm_langevin_step", "sdm_set_restraints",
-            "sdm_set_restraint_control", "sdm_get_restraint_energies", "sdm_set_rigid_waters")
+            "sdm_set_restraint_control", "sdm_get_restraint_energies", "sdm_set_rigid_waters",
+            "sdm_gather_positions", "sdm_scatter_forces_fixed", "sdm_evaluate_engine", "sdm_get_last_results")
 
 NB_REACTION_FIELD, NB_PME = 0, 1
 NOALLOC_MAX_PARTICLES = 8192
@@ -102,6 +104,11 @@ def load_library(path: str = LIB_PATH):
         L.sdm_evaluate.argtypes = [vp, vp, vp, vp]
         L.sdm_evaluate_device.argtypes = [vp, vp, vp, vp, vp]
         L.sdm_get_state_forces.argtypes = [vp, vp, vp, C.c_int]
+        L.sdm_get_state_forces_device.argtypes = [vp, vp, vp, vp]
+        L.sdm_gather_positions.argtypes = [vp, vp, C.c_int, vp, C.c_int, vp, vp]
+        L.sdm_scatter_forces_fixed.argtypes = [vp, vp, C.c_int, C.c_int, vp, vp]
+        L.sdm_evaluate_engine.argtypes = [vp, vp, vp, C.c_int, vp, C.c_int, vp, vp, vp]
+        L.sdm_get_last_results.argtypes = [vp, vp]
         L.sdm_check_status.argtypes = [vp, ip]
         L.sdm_set_option.argtypes = [vp, C.c_int, C.c_int]
         L.sdm_get_option.argtypes = [vp, C.c_int, ip]
@@ -380,6 +387,13 @@ class Handle:
         F1 = np.zeros(3 * self.total_particles)
         self._check(self.lib.sdm_get_state_forces(self.h, F0.ctypes.data, F1.ctypes.data, 0))
         return F0.reshape(-1, 3), F1.reshape(-1, 3)
+
+    def state_forces_device(self, F0_ptr: int = 0, F1_ptr: int = 0, stream: int = 0):
+        """sdm_get_state_forces_device: F0 and/or F1 of the last evaluation into
+        device buffers, asynchronous on ``stream``."""
+        self._check(self.lib.sdm_get_state_forces_device(self.h, C.c_void_p(F0_ptr) if F0_ptr else None,
+                                                         C.c_void_p(F1_ptr) if F1_ptr else None,
+                                                         C.c_void_p(stream) if stream else None))
 
     def check_status(self) -> int:
         v = C.c_int(0)

@@ -25,9 +25,9 @@ cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* cl_prefix, 
 cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_t st);
 cudaError_t sdm_pair_prepare();
 #define SDM_MAX_CTAS 4  // pair-kernel CTAs per SM with a built register bound
-int sdm_pair_resident(int ctas_per_sm);
+int sdm_pair_resident(int ctas_per_sm, int variant);
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
-                            int resident, bool pme, cudaStream_t st);
+                            int resident, bool pme, int variant, cudaStream_t st);
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
 cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_pme(const SdmArgs& a, const cufftHandle* r2c, const cufftHandle* c2r, const long long* grid_off,
@@ -36,6 +36,10 @@ cudaError_t sdm_pme_prepare(int smem_bytes);
 cudaError_t sdm_launch_restraints(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st);
+cudaError_t sdm_launch_gather_positions(const void* posq, const void* corr, int double_precision,
+                                        const int* index, int n, double* x, cudaStream_t st);
+cudaError_t sdm_launch_scatter_forces(const double* f, const int* index, int n, int padded, long long* buf,
+                                      cudaStream_t st);
 cudaError_t sdm_launch_adjoint(const SdmArgs& a, cudaStream_t st);
 
 namespace {
@@ -149,7 +153,8 @@ struct sdm_handle {
     bool lv_set = false, lv_dirty = false;
     // options
     int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 4, opt_verify = 1, opt_zero_copy = 0;
-    int pair_res[SDM_MAX_CTAS + 1] = {};  // resident pair-kernel CTAs per SM by request
+    int opt_pair_variant = 0;
+    int pair_res[2][SDM_MAX_CTAS + 1] = {};  // resident pair-kernel CTAs per SM by variant and request
     // graphs
     std::map<GraphKey, cudaGraphExec_t> graphs;
     // profiling
@@ -641,7 +646,8 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->cl_prefix, h->done, st, ev, 6, fl));
     SDM_CUDA(h, sdm_launch_jlist(a, h->cl_prefix, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[6], st, fl));
-    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[h->opt_ctas], h->pme, st));
+    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[h->opt_pair_variant][h->opt_ctas],
+                                h->pme, h->opt_pair_variant, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
     if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
     if (mode == 0) SDM_CUDA(h, sdm_launch_exceptions(a, st));
@@ -716,7 +722,7 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
         return SDM_OK;
     }
     const bool gprof = h->opt_profile == 2;
-    GraphKey key{x, res, f, st, a.split, h->opt_ctas + (gprof ? 100 : 0)};
+    GraphKey key{x, res, f, st, a.split, h->opt_ctas + (gprof ? 100 : 0) + 1000 * h->opt_pair_variant};
     if (lv) { key.v = lv->v; key.invm = lv->invm; key.fext = lv->fext; }
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
@@ -817,7 +823,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     h->device = device;
     if (cudaSetDevice(device) != cudaSuccess) { delete h; return fail(nullptr, SDM_ERR_CUDA, "cudaSetDevice failed"); }
     if (sdm_pair_prepare() != cudaSuccess) { delete h; return fail(nullptr, SDM_ERR_CUDA, "pair kernel setup failed"); }
-    for (int c = 1; c <= SDM_MAX_CTAS; ++c) h->pair_res[c] = sdm_pair_resident(c);
+    for (int v = 0; v < 2; ++v)
+        for (int c = 1; c <= SDM_MAX_CTAS; ++c) h->pair_res[v][c] = sdm_pair_resident(c, v);
     cudaDeviceProp prop{};
     cudaGetDeviceProperties(&prop, device);
     if (prop.major < 10) {
@@ -1447,6 +1454,54 @@ sdm_status sdm_evaluate_device(sdm_handle* h, const double* x, double* results, 
     return run(h, x, results, forces, st, 0, true);
 }
 
+sdm_status sdm_evaluate_engine(sdm_handle* h, const void* posq, const void* posq_correction, int double_precision,
+                               const int* index, int padded_n, long long* force_buffer, double* results,
+                               void* stream) {
+    if (!h || !posq || !index) return SDM_ERR_INVALID_ARGUMENT;
+    const int n = (int)h->total_particles;
+    if (padded_n < n) return fail(h, SDM_ERR_INVALID_ARGUMENT, "padded_n is below the particle count");
+    cudaSetDevice(h->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+    SDM_CUDA(h, sdm_launch_gather_positions(posq, posq_correction, double_precision, index, n, h->x_in, st));
+    sdm_status s = run(h, h->x_in, h->res_in, force_buffer ? h->f_in : nullptr, st, 0, true);
+    if (s) return s;
+    if (results) {
+        // the synchronous form validates before the forces go out: a list
+        // overflow regrows the lists and evaluates again
+        for (int attempt = 0;; ++attempt) {
+            SDM_CUDA(h, cudaMemcpyAsync(results, h->res_in, sizeof(double) * SDM_NRESULTS * h->nrep,
+                                        cudaMemcpyDeviceToHost, st));
+            SDM_CUDA(h, cudaStreamSynchronize(st));
+            int v = 0;
+            for (int r = 0; r < h->nrep; ++r) v |= (int)results[(size_t)r * SDM_NRESULTS + SDM_R_STATUS];
+            if (!(v & SDM_DEV_LIST_OVERFLOW)) {
+                if (v) {
+                    SDM_CUDA(h, cudaMemset(h->args.status, 0, sizeof(int)));
+                    if (h->opt_verify) return fail(h, SDM_ERR_OVERFLOW, "device status error (see SDM_R_STATUS)");
+                }
+                break;
+            }
+            SDM_CUDA(h, cudaMemset(h->args.status, 0, sizeof(int)));
+            if (attempt >= 8) return fail(h, SDM_ERR_CAPACITY, "cluster-pair lists keep overflowing");
+            s = regrow_lists(h);
+            if (s) return s;
+            s = run(h, h->x_in, h->res_in, force_buffer ? h->f_in : nullptr, st, 0, true);
+            if (s) return s;
+        }
+    }
+    if (force_buffer) SDM_CUDA(h, sdm_launch_scatter_forces(h->f_in, index, n, padded_n, force_buffer, st));
+    return SDM_OK;
+}
+
+sdm_status sdm_get_last_results(sdm_handle* h, double* results) {
+    if (!h || !results) return SDM_ERR_INVALID_ARGUMENT;
+    if (!h->have_eval) return fail(h, SDM_ERR_INVALID_ARGUMENT, "no evaluation yet");
+    cudaSetDevice(h->device);
+    SDM_CUDA(h, cudaDeviceSynchronize());
+    SDM_CUDA(h, cudaMemcpy(results, h->res_in, sizeof(double) * SDM_NRESULTS * h->nrep, cudaMemcpyDeviceToHost));
+    return SDM_OK;
+}
+
 sdm_status sdm_set_langevin(sdm_handle* h, const sdm_langevin_params* p, unsigned long long step) {
     if (!h || !p) return SDM_ERR_INVALID_ARGUMENT;
     if (!(p->step_size > 0.0) || !std::isfinite(p->step_size))
@@ -1519,6 +1574,50 @@ sdm_status sdm_get_state_forces(sdm_handle* h, double* F0, double* F1, int on_de
         }
     }
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SDM_OK;
+}
+
+sdm_status sdm_get_state_forces_device(sdm_handle* h, double* F0, double* F1, void* stream) {
+    if (!h) return SDM_ERR_INVALID_ARGUMENT;
+    if (!h->have_eval) return fail(h, SDM_ERR_INVALID_ARGUMENT, "no evaluation yet");
+    if (!F0 && !F1) return SDM_OK;
+    cudaSetDevice(h->device);
+    SdmArgs a = h->args;
+    a.forces = nullptr;
+    a.F0out = F0;
+    a.F1out = F1;
+    SDM_CUDA(h, sdm_launch_mix(a, stream ? (cudaStream_t)stream : h->stream));
+    return SDM_OK;
+}
+
+sdm_status sdm_gather_positions(const void* posq, const void* posq_correction, int double_precision,
+                                const int* index, int n, double* x, void* stream) {
+    if (!posq || !index || !x || n < 0) {
+        sdm_set_thread_error("sdm_gather_positions: NULL array or negative count");
+        return SDM_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return SDM_OK;
+    const cudaError_t e = sdm_launch_gather_positions(posq, posq_correction, double_precision, index, n, x,
+                                                      (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        sdm_set_thread_error(cudaGetErrorString(e));
+        return SDM_ERR_CUDA;
+    }
+    return SDM_OK;
+}
+
+sdm_status sdm_scatter_forces_fixed(const double* forces, const int* index, int n, int padded_n,
+                                    long long* buffer, void* stream) {
+    if (!forces || !index || !buffer || n < 0 || padded_n < n) {
+        sdm_set_thread_error("sdm_scatter_forces_fixed: NULL array or bad sizes");
+        return SDM_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return SDM_OK;
+    const cudaError_t e = sdm_launch_scatter_forces(forces, index, n, padded_n, buffer, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        sdm_set_thread_error(cudaGetErrorString(e));
+        return SDM_ERR_CUDA;
+    }
     return SDM_OK;
 }
 
@@ -1613,6 +1712,10 @@ sdm_status sdm_set_option(sdm_handle* h, int option, int value) {
             break;
         case SDM_OPT_VERIFY: h->opt_verify = value ? 1 : 0; break;
         case SDM_OPT_ZERO_COPY: h->opt_zero_copy = value ? 1 : 0; break;
+        case SDM_OPT_PAIR_VARIANT:
+            if (value != 0 && value != 1) return fail(h, SDM_ERR_INVALID_ARGUMENT, "pair variant must be 0 or 1");
+            h->opt_pair_variant = value;
+            break;
         default: return fail(h, SDM_ERR_INVALID_ARGUMENT, "unknown option");
     }
     return SDM_OK;
@@ -1626,7 +1729,8 @@ sdm_status sdm_get_option(const sdm_handle* h, int option, int* value) {
         case SDM_OPT_SPLIT: *value = h->opt_split; break;
         case SDM_OPT_CTAS_PER_SM: *value = h->opt_ctas; break;
         case SDM_OPT_VERIFY: *value = h->opt_verify; break;
-        case SDM_OPT_PAIR_RESIDENT: *value = h->pair_res[h->opt_ctas]; break;
+        case SDM_OPT_PAIR_RESIDENT: *value = h->pair_res[h->opt_pair_variant][h->opt_ctas]; break;
+        case SDM_OPT_PAIR_VARIANT: *value = h->opt_pair_variant; break;
         case SDM_OPT_ZERO_COPY: *value = h->opt_zero_copy; break;
         default: return SDM_ERR_INVALID_ARGUMENT;
     }

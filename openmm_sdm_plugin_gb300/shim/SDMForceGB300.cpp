@@ -11,6 +11,7 @@
  * of ReferenceSDMKernels.cpp:231-318, in one sdm_evaluate call.
  */
 #include "SDMForceGB300.h"
+#include "SDMKernels.h"
 
 #include "openmm/Context.h"
 #include "openmm/OpenMMException.h"
@@ -132,42 +133,134 @@ sdm_system_desc SDMForce::describe(const double box[3]) const {
     return d;
 }
 
+// ---------------------------------------------------------------------------
+// SDMContextState: one context's handle, parameters and work bookkeeping
+// ---------------------------------------------------------------------------
+SDMContextState::SDMContextState(const SDMForce& owner) : owner_(owner) {
+    for (double& v : res_) v = 0.0;
+    for (double& v : p_) v = 0.0;
+}
+
+SDMContextState::~SDMContextState() { sdm_destroy(h_); }
+
+void SDMContextState::boxOf(OpenMM::ContextImpl& context, double box[3]) {
+    Vec3 a, b, c;
+    context.getPeriodicBoxVectors(a, b, c);
+    if (a[1] != 0.0 || a[2] != 0.0 || b[0] != 0.0 || b[2] != 0.0 || c[0] != 0.0 || c[1] != 0.0)
+        throw OpenMMException("SDMForce: the periodic box must be rectangular");
+    box[0] = a[0];
+    box[1] = b[1];
+    box[2] = c[2];
+}
+
+void SDMContextState::initialize(const OpenMM::System& system) {
+    if (system.getNumParticles() != owner_.getNumParticles())
+        throw OpenMMException("SDMForce: particle count differs from the System's");
+    for (int k = 0; k < SDM_NPARAMS; ++k) p_[k] = owner_.p_[k];
+    ntmax_ = owner_.ntmax_;
+    displ_ = owner_.displ_;
+}
+
 /* One sdm_handle per context.  The box is fixed at handle creation; a
  * context whose box changes (a barostat) gets a new handle. */
+void SDMContextState::create(OpenMM::ContextImpl& context) {
+    boxOf(context, box_);
+    sdm_destroy(h_);
+    h_ = nullptr;
+    sdm_system_desc d = owner_.describe(box_);
+    d.displacement = displ_.data();
+    check(sdm_create(&d, 1, device_ >= 0 ? device_ : owner_.device_, &h_), nullptr, "sdm_create failed");
+    check(sdm_set_params(h_, 0, p_), h_, "invalid SDM parameters");
+}
+
+sdm_handle* SDMContextState::prepare(OpenMM::ContextImpl& context) {
+    double box[3];
+    boxOf(context, box);
+    if (!h_ || box[0] != box_[0] || box[1] != box_[1] || box[2] != box_[2]) create(context);
+    if (nonEquilibrium()) {
+        const double t = context.getTime();
+        // the step from the last evaluation's time to t is complete: its
+        // work increment uses dW/dlambda at that step's start
+        if (have_last_ && t != t_last_) work_ += (t - t_last_) / ntmax_ * dwdl_last_;
+        const double lam = t / ntmax_;
+        if (lam != p_[SDM_P_LAMBDA]) {
+            p_[SDM_P_LAMBDA] = lam;
+            check(sdm_set_params(h_, 0, p_), h_, "invalid SDM parameters");
+        }
+    }
+    return h_;
+}
+
+void SDMContextState::finish(OpenMM::ContextImpl& context) {
+    if (!nonEquilibrium()) return;
+    have_last_ = true;
+    t_last_ = context.getTime();
+    dwdl_last_ = res_[SDM_R_DWDLAMBDA];
+}
+
+/* All or nothing: on any error the handle and this object keep the
+ * parameters and displacements of the last successful update, so a later
+ * re-creation (box change) applies consistent values. */
+void SDMContextState::update(const SDMForce& f) {
+    if (f.displ_.size() != displ_.size())
+        throw OpenMMException("SDMForce: the displacement map must keep the particle count");
+    for (double v : f.displ_)
+        if (!std::isfinite(v)) throw OpenMMException("SDMForce: invalid displacement: non-finite value");
+    check(sdm_set_params(h_, 0, f.p_), h_, "invalid SDM parameters");
+    const sdm_status st = sdm_set_displacement(h_, 0, f.displ_.data());
+    if (st != SDM_OK) {
+        const std::string msg = std::string("invalid displacement: ") + sdm_last_error(h_);
+        sdm_set_params(h_, 0, p_);   // back to the parameters that this object still holds
+        throw OpenMMException("SDMForce: " + msg);
+    }
+    for (int k = 0; k < SDM_NPARAMS; ++k) p_[k] = f.p_[k];
+    ntmax_ = f.ntmax_;
+    displ_ = f.displ_;
+}
+
+/* The accumulated work plus the increment of the step that ends at the
+ * context's current time (its force evaluation at the step start is the
+ * last one seen). */
+double SDMContextState::work(const OpenMM::ContextImpl& context) const {
+    if (!have_last_ || !(ntmax_ > 0.0)) return work_;
+    return work_ + (context.getTime() - t_last_) / ntmax_ * dwdl_last_;
+}
+
+void SDMContextState::setWork(const OpenMM::ContextImpl& context, double w) { work_ += w - work(context); }
+
+// ---------------------------------------------------------------------------
+// SDMForceImpl: the platform kernel where a factory provides one (OpenMM's
+// CUDA platform with this plugin's kernels registered), else the host path
+// ---------------------------------------------------------------------------
 class SDMForceImpl : public OpenMM::CustomCPPForceImpl {
 public:
-    explicit SDMForceImpl(const SDMForce& owner) : OpenMM::CustomCPPForceImpl(owner), owner_(owner) {
-        for (double& v : res_) v = 0.0;
-    }
-    ~SDMForceImpl() override { sdm_destroy(h_); }
+    explicit SDMForceImpl(const SDMForce& owner) : OpenMM::CustomCPPForceImpl(owner), owner_(owner), st_(owner) {}
 
     void initialize(OpenMM::ContextImpl& context) override {
+        OpenMM::Platform& platform = context.getPlatform();
+        if (platform.supportsKernels({CalcSDMForceKernel::Name()})) {
+            kernel_ = platform.createKernel(CalcSDMForceKernel::Name(), context);
+            kernel_.getAs<CalcSDMForceKernel>().initialize(context.getSystem(), owner_);
+            have_kernel_ = true;
+            return;
+        }
         OpenMM::CustomCPPForceImpl::initialize(context);
-        if (context.getSystem().getNumParticles() != owner_.getNumParticles())
-            throw OpenMMException("SDMForce: particle count differs from the System's");
-        for (int k = 0; k < SDM_NPARAMS; ++k) p_[k] = owner_.p_[k];
-        ntmax_ = owner_.ntmax_;
-        displ_ = owner_.displ_;
-        create(context);
+        st_.initialize(context.getSystem());
+        st_.prepare(context);   // the handle now: a bad descriptor fails the context's creation
+    }
+
+    bool usesKernel() const { return have_kernel_; }
+
+    double calcForcesAndEnergy(OpenMM::ContextImpl& context, bool includeForces, bool includeEnergy,
+                               int groups) override {
+        if (!usesKernel()) return OpenMM::CustomCPPForceImpl::calcForcesAndEnergy(context, includeForces, includeEnergy, groups);
+        if ((groups & (1 << owner_.getForceGroup())) == 0) return 0.0;
+        return kernel_.getAs<CalcSDMForceKernel>().execute(context, includeForces, includeEnergy);
     }
 
     double computeForce(OpenMM::ContextImpl& context, const std::vector<Vec3>& positions,
                         std::vector<Vec3>& forces) override {
-        double box[3];
-        box_of(context, box);
-        if (box[0] != box_[0] || box[1] != box_[1] || box[2] != box_[2]) create(context);
-        const bool noneq = p_[SDM_P_NONEQ] == 1.0 && ntmax_ > 0.0;
-        const double t = context.getTime();
-        if (noneq) {
-            // the step from the last evaluation's time to t is complete: its
-            // work increment uses dW/dlambda at that step's start
-            if (have_last_ && t != t_last_) work_ += (t - t_last_) / ntmax_ * dwdl_last_;
-            const double lam = t / ntmax_;
-            if (lam != p_[SDM_P_LAMBDA]) {
-                p_[SDM_P_LAMBDA] = lam;
-                check(sdm_set_params(h_, 0, p_), h_, "invalid SDM parameters");
-            }
-        }
+        sdm_handle* h = st_.prepare(context);
         const size_t n = positions.size();
         x_.resize(3 * n);
         f_.resize(3 * n);
@@ -176,85 +269,42 @@ public:
             x_[3 * i + 1] = positions[i][1];
             x_[3 * i + 2] = positions[i][2];
         }
-        check(sdm_evaluate(h_, x_.data(), res_, f_.data()), h_, "evaluation failed");
-        if (noneq) {
-            have_last_ = true;
-            t_last_ = t;
-            dwdl_last_ = res_[SDM_R_DWDLAMBDA];
-        }
+        double* res = st_.results();
+        check(sdm_evaluate(h, x_.data(), res, f_.data()), h, "evaluation failed");
+        st_.finish(context);
         forces.resize(n);
         for (size_t i = 0; i < n; ++i) forces[i] = Vec3(f_[3 * i + 0], f_[3 * i + 1], f_[3 * i + 2]);
-        return res_[SDM_R_EPOT];
+        return res[SDM_R_EPOT];
     }
 
-    /* All or nothing: on any error the handle and this object keep the
-     * parameters and displacements of the last successful update, so a later
-     * re-creation (box change) applies consistent values. */
-    void updateParametersInContext(const SDMForce& f) {
-        if (f.displ_.size() != displ_.size())
-            throw OpenMMException("SDMForce: the displacement map must keep the particle count");
-        for (double v : f.displ_)
-            if (!std::isfinite(v)) throw OpenMMException("SDMForce: invalid displacement: non-finite value");
-        check(sdm_set_params(h_, 0, f.p_), h_, "invalid SDM parameters");
-        const sdm_status st = sdm_set_displacement(h_, 0, f.displ_.data());
-        if (st != SDM_OK) {
-            const std::string msg = std::string("invalid displacement: ") + sdm_last_error(h_);
-            sdm_set_params(h_, 0, p_);   // back to the parameters that this object still holds
-            throw OpenMMException("SDMForce: " + msg);
-        }
-        for (int k = 0; k < SDM_NPARAMS; ++k) p_[k] = f.p_[k];
-        ntmax_ = f.ntmax_;
-        displ_ = f.displ_;
+    void updateParametersInContext(OpenMM::ContextImpl& context, const SDMForce& f) {
+        if (usesKernel()) kernel_.getAs<CalcSDMForceKernel>().copyParametersToContext(context, f);
+        else st_.update(f);
     }
 
-    const double* results() const { return res_; }
-
-    /* The accumulated work plus the increment of the step that ends at the
-     * context's current time (its force evaluation at the step start is the
-     * last one seen). */
-    double work(const OpenMM::ContextImpl& context) const {
-        if (!have_last_ || !(ntmax_ > 0.0)) return work_;
-        return work_ + (context.getTime() - t_last_) / ntmax_ * dwdl_last_;
+    const double* results() {
+        return usesKernel() ? kernel_.getAs<CalcSDMForceKernel>().getResults() : st_.results();
     }
-    void set_work(const OpenMM::ContextImpl& context, double w) { work_ += w - work(context); }
+    double work(const OpenMM::ContextImpl& context) {
+        return usesKernel() ? kernel_.getAs<CalcSDMForceKernel>().getNoneqWorkvalue(context) : st_.work(context);
+    }
+    void setWork(const OpenMM::ContextImpl& context, double w) {
+        if (usesKernel()) kernel_.getAs<CalcSDMForceKernel>().setNoneqWorkvalue(context, w);
+        else st_.setWork(context, w);
+    }
 
 private:
-    static void box_of(OpenMM::ContextImpl& context, double box[3]) {
-        Vec3 a, b, c;
-        context.getPeriodicBoxVectors(a, b, c);
-        if (a[1] != 0.0 || a[2] != 0.0 || b[0] != 0.0 || b[2] != 0.0 || c[0] != 0.0 || c[1] != 0.0)
-            throw OpenMMException("SDMForce: the periodic box must be rectangular");
-        box[0] = a[0];
-        box[1] = b[1];
-        box[2] = c[2];
-    }
-
-    void create(OpenMM::ContextImpl& context) {
-        box_of(context, box_);
-        sdm_destroy(h_);
-        h_ = nullptr;
-        sdm_system_desc d = owner_.describe(box_);
-        d.displacement = displ_.data();
-        check(sdm_create(&d, 1, owner_.device_, &h_), nullptr, "sdm_create failed");
-        check(sdm_set_params(h_, 0, p_), h_, "invalid SDM parameters");
-    }
-
     const SDMForce& owner_;
-    sdm_handle* h_ = nullptr;
-    double box_[3] = {0.0, 0.0, 0.0};
-    double p_[SDM_NPARAMS];
-    double res_[SDM_NRESULTS];
-    std::vector<double> displ_, x_, f_;
-    // non-equilibrium work: the sum over completed steps, and the time and
-    // dW/dlambda of the last evaluation
-    double ntmax_ = 0.0, work_ = 0.0, t_last_ = 0.0, dwdl_last_ = 0.0;
-    bool have_last_ = false;
+    SDMContextState st_;     // the host path's state (the kernel keeps its own)
+    OpenMM::Kernel kernel_;
+    bool have_kernel_ = false;
+    std::vector<double> x_, f_;
 };
 
 OpenMM::ForceImpl* SDMForce::createImpl() const { return new SDMForceImpl(*this); }
 
 void SDMForce::updateParametersInContext(OpenMM::Context& context) {
-    dynamic_cast<SDMForceImpl&>(getImplInContext(context)).updateParametersInContext(*this);
+    dynamic_cast<SDMForceImpl&>(getImplInContext(context)).updateParametersInContext(getContextImpl(context), *this);
 }
 
 double SDMForce::getNoneqWorkvalue(OpenMM::Context& context) {
@@ -262,7 +312,7 @@ double SDMForce::getNoneqWorkvalue(OpenMM::Context& context) {
 }
 
 void SDMForce::setNoneqWorkvalue(OpenMM::Context& context, double work) {
-    dynamic_cast<SDMForceImpl&>(getImplInContext(context)).set_work(getContextImpl(context), work);
+    dynamic_cast<SDMForceImpl&>(getImplInContext(context)).setWork(getContextImpl(context), work);
 }
 
 std::vector<double> SDMForce::getResults(OpenMM::Context& context) {

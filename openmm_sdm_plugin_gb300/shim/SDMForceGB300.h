@@ -148,6 +148,7 @@ protected:
 
 private:
     friend class SDMForceImpl;
+    friend class SDMContextState;
     int device_;
     double p_[SDM_NPARAMS];
     std::vector<double> charge_, sigma_, epsilon_, displ_;

@@ -81,24 +81,104 @@ System::~System() {
     for (Force* f : forces) delete f;
 }
 
-ContextImpl::ContextImpl(Context& owner, const System& system) : owner(owner), system(system) {
+void Kernel::release() {
+    if (refs && --*refs == 0) {
+        delete impl;
+        delete refs;
+    }
+    impl = nullptr;
+    refs = nullptr;
+}
+
+Kernel& Kernel::operator=(const Kernel& o) {
+    if (this != &o) {
+        release();
+        impl = o.impl;
+        refs = o.refs;
+        if (refs) ++*refs;
+    }
+    return *this;
+}
+
+namespace {
+std::vector<Platform*>& platforms() {
+    static std::vector<Platform*> list;
+    return list;
+}
+}  // namespace
+
+Platform::~Platform() {
+    for (auto& kv : factories) {
+        bool seen = false;   // one factory may serve several names
+        for (auto& kv2 : factories) {
+            if (&kv2 == &kv) break;
+            if (kv2.second == kv.second) seen = true;
+        }
+        if (!seen) delete kv.second;
+    }
+}
+
+void Platform::registerKernelFactory(const std::string& name, KernelFactory* factory) { factories[name] = factory; }
+
+bool Platform::supportsKernels(const std::vector<std::string>& kernelNames) const {
+    for (const std::string& n : kernelNames)
+        if (factories.find(n) == factories.end()) return false;
+    return true;
+}
+
+Kernel Platform::createKernel(const std::string& name, ContextImpl& context) const {
+    auto it = factories.find(name);
+    if (it == factories.end())
+        throw OpenMMException("Called createKernel() on a Platform which does not support the requested kernel");
+    return Kernel(it->second->createKernelImpl(name, *this, context));
+}
+
+void Platform::registerPlatform(Platform* platform) { platforms().push_back(platform); }
+int Platform::getNumPlatforms() { return (int)platforms().size(); }
+Platform& Platform::getPlatform(int index) { return *platforms().at(index); }
+
+Platform& Platform::getPlatformByName(const std::string& name) {
+    for (Platform* p : platforms())
+        if (p->getName() == name) return *p;
+    throw OpenMMException("There is no registered Platform called \"" + name + "\"");
+}
+
+const std::string& ReferencePlatform::getName() const {
+    static const std::string name = "Reference";
+    return name;
+}
+
+namespace {
+// the default platform, registered when the library loads
+struct RegisterReference {
+    RegisterReference() { Platform::registerPlatform(new ReferencePlatform()); }
+} registerReference;
+}  // namespace
+
+ContextImpl::ContextImpl(Context& owner, const System& system, Platform& platform)
+    : owner(owner), system(system), platform(platform) {
     system.getDefaultPeriodicBoxVectors(box[0], box[1], box[2]);
     positions.assign(system.getNumParticles(), Vec3());
+    platform.contextCreated(*this);
     for (int i = 0; i < system.getNumForces(); ++i) forceImpls.push_back(system.getForce(i).createImpl());
 }
 
 ContextImpl::~ContextImpl() {
     for (ForceImpl* f : forceImpls) delete f;
+    platform.contextDestroyed(*this);
 }
 
 double ContextImpl::calcForcesAndEnergy(bool includeForces, bool includeEnergy, int groups) {
     forces.assign(system.getNumParticles(), Vec3());
+    platform.beginForces(*this);
     double energy = 0.0;
     for (ForceImpl* f : forceImpls) energy += f->calcForcesAndEnergy(*this, includeForces, includeEnergy, groups);
+    platform.endForces(*this);
     return energy;
 }
 
-Context::Context(const System& system) : impl(new ContextImpl(*this, system)) {
+void Context::create(const System& system, Platform& platform) {
+    impl = new ContextImpl(*this, system, platform);
     try {
         for (ForceImpl* f : impl->getForceImpls()) f->initialize(*impl);
     } catch (...) {
@@ -106,6 +186,10 @@ Context::Context(const System& system) : impl(new ContextImpl(*this, system)) {
         throw;
     }
 }
+
+Context::Context(const System& system) : impl(nullptr) { create(system, Platform::getPlatformByName("Reference")); }
+
+Context::Context(const System& system, Platform& platform) : impl(nullptr) { create(system, platform); }
 
 Context::~Context() { delete impl; }
 

@@ -14,6 +14,10 @@
 #include <string>
 #include <vector>
 
+#ifndef OPENMM_EXPORT
+#define OPENMM_EXPORT __attribute__((visibility("default")))
+#endif
+
 namespace OpenMM {
 
 class Vec3 {
@@ -40,6 +44,73 @@ private:
 class Context;
 class ContextImpl;
 class ForceImpl;
+class Platform;
+
+class KernelImpl {
+public:
+    KernelImpl(std::string name, const Platform& platform) : name(name), platform(&platform) {}
+    virtual ~KernelImpl() {}
+    std::string getName() const { return name; }
+    const Platform& getPlatform() { return *platform; }
+
+private:
+    std::string name;
+    const Platform* platform;
+};
+
+/* A shared handle of a KernelImpl (the last copy deletes it). */
+class Kernel {
+public:
+    Kernel() : impl(nullptr), refs(nullptr) {}
+    explicit Kernel(KernelImpl* impl) : impl(impl), refs(new int(1)) {}
+    Kernel(const Kernel& o) : impl(o.impl), refs(o.refs) { if (refs) ++*refs; }
+    Kernel& operator=(const Kernel& o);
+    ~Kernel() { release(); }
+    std::string getName() const { return impl->getName(); }
+    const KernelImpl& getImpl() const { return *impl; }
+    KernelImpl& getImpl() { return *impl; }
+    template <class T> T& getAs() { return dynamic_cast<T&>(*impl); }
+
+private:
+    void release();
+    KernelImpl* impl;
+    int* refs;
+};
+
+class KernelFactory {
+public:
+    virtual ~KernelFactory() {}
+    virtual KernelImpl* createKernelImpl(std::string name, const Platform& platform, ContextImpl& context) const = 0;
+};
+
+class Platform {
+public:
+    virtual ~Platform();
+    virtual const std::string& getName() const = 0;
+    void registerKernelFactory(const std::string& name, KernelFactory* factory);
+    bool supportsKernels(const std::vector<std::string>& kernelNames) const;
+    Kernel createKernel(const std::string& name, ContextImpl& context) const;
+    static void registerPlatform(Platform* platform);
+    static int getNumPlatforms();
+    static Platform& getPlatform(int index);
+    static Platform& getPlatformByName(const std::string& name);
+    // stand-in hooks (not OpenMM API): platform data of a new context, and
+    // the moves of positions and forces between the host and the platform
+    virtual void contextCreated(ContextImpl& context) const {}
+    virtual void contextDestroyed(ContextImpl& context) const {}
+    virtual void positionsChanged(ContextImpl& context) const {}
+    virtual void beginForces(ContextImpl& context) const {}
+    virtual void endForces(ContextImpl& context) const {}
+
+private:
+    std::map<std::string, KernelFactory*> factories;
+};
+
+/* The default platform of this subset: host positions, host forces. */
+class ReferencePlatform : public Platform {
+public:
+    const std::string& getName() const override;
+};
 
 class Force {
 public:
@@ -165,16 +236,19 @@ private:
 
 class ContextImpl {
 public:
-    ContextImpl(Context& owner, const System& system);
+    ContextImpl(Context& owner, const System& system, Platform& platform);
     ~ContextImpl();
     const System& getSystem() const { return system; }
     Context& getOwner() { return owner; }
     void getPositions(std::vector<Vec3>& out) { out = positions; }
-    void setPositions(const std::vector<Vec3>& p) { positions = p; }
+    void setPositions(const std::vector<Vec3>& p) { positions = p; platform.positionsChanged(*this); }
     void getPeriodicBoxVectors(Vec3& a, Vec3& b, Vec3& c) { a = box[0]; b = box[1]; c = box[2]; }
     void setPeriodicBoxVectors(const Vec3& a, const Vec3& b, const Vec3& c) { box[0] = a; box[1] = b; box[2] = c; }
     double getTime() const { return time; }
     void setTime(double t) { time = t; }
+    Platform& getPlatform() { return platform; }
+    void* getPlatformData() { return platformData; }
+    void setPlatformData(void* data) { platformData = data; }
     std::vector<ForceImpl*>& getForceImpls() { return forceImpls; }
     double calcForcesAndEnergy(bool includeForces, bool includeEnergy, int groups = 0xFFFFFFFF);
     std::vector<Vec3>& getForceAccumulator() { return forces; }
@@ -182,6 +256,8 @@ public:
 private:
     Context& owner;
     const System& system;
+    Platform& platform;
+    void* platformData = nullptr;
     std::vector<ForceImpl*> forceImpls;
     std::vector<Vec3> positions, forces;
     Vec3 box[3];
@@ -192,7 +268,10 @@ private:
 class Context {
 public:
     explicit Context(const System& system);
+    Context(const System& system, Platform& platform);
     ~Context();
+    // stand-in accessor (not OpenMM API) for tests of kernel factories
+    ContextImpl& getImplForTests() { return *impl; }
     void setPositions(const std::vector<Vec3>& positions) { impl->setPositions(positions); }
     void setPeriodicBoxVectors(const Vec3& a, const Vec3& b, const Vec3& c) { impl->setPeriodicBoxVectors(a, b, c); }
     void setTime(double time) { impl->setTime(time); }
@@ -200,6 +279,7 @@ public:
 
 private:
     friend class Force;
+    void create(const System& system, Platform& platform);
     ContextImpl* impl;
 };
 

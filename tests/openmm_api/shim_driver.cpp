@@ -14,6 +14,16 @@
 //                                           evaluate: results[SDM_R_RESERVED], [SDM_R_U0] and
 //                                           [SDM_R_U1] after each, getPerturbationEnergy; then a
 //                                           triclinic box (an OpenMMException)
+//   shim_driver atomic <input> <output>     failed updateParametersInContext calls change nothing
+//
+// Built with SDM_TEST_CUDA_PLATFORM (and SDMCudaKernels.cpp, CudaSubset.cpp):
+//   shim_driver factory - <output>          registerKernelFactories on a CUDA platform: which
+//                                           platforms support CalcSDMForce, the kernel created
+//                                           by name, an unknown name refused (no GPU needed)
+//   shim_driver cuda-mixed|cuda-double <input> <output>
+//                                           the evaluate sequence on the CUDA platform (the
+//                                           CalcSDMForce kernel on shuffled device arrays), then
+//                                           forces without energy and the results read after it
 //
 // Input (little-endian): int32 n, n_exceptions, method (OpenMM NonbondedMethod),
 // dispersion_correction; float64 box[3], cutoff, eps_rf, ewald_tol,
@@ -24,6 +34,10 @@
 #include "SDMForceGB300.h"
 #include "openmm/Context.h"
 #include "openmm/System.h"
+#ifdef SDM_TEST_CUDA_PLATFORM
+#include "openmm/cuda/CudaPlatform.h"
+extern "C" void registerKernelFactories();
+#endif
 
 #include <cmath>
 #include <cstdio>
@@ -52,7 +66,45 @@ struct Reader {
 
 template <class T> void put(FILE* f, const T* p, size_t k) { fwrite(p, sizeof(T), k, f); }
 
+#ifdef SDM_TEST_CUDA_PLATFORM
+CudaPlatform* cuda_platform(const std::string& precision) {
+    static CudaPlatform* cp = nullptr;
+    if (!cp) {
+        cp = new CudaPlatform(precision);
+        Platform::registerPlatform(cp);
+        registerKernelFactories();
+    }
+    return cp;
+}
+
+int factory(const char* out_path) {
+    CudaPlatform* cp = cuda_platform("mixed");
+    FILE* fo = fopen(out_path, "w");
+    if (!fo) throw std::runtime_error("cannot open output");
+    for (int i = 0; i < Platform::getNumPlatforms(); ++i) {
+        Platform& p = Platform::getPlatform(i);
+        fprintf(fo, "platform %s supports %d\n", p.getName().c_str(), (int)p.supportsKernels({"CalcSDMForce"}));
+    }
+    System system;
+    system.addParticle(1.0);
+    Context context(system, *cp);
+    Kernel k = cp->createKernel("CalcSDMForce", context.getImplForTests());
+    fprintf(fo, "kernel %s\n", k.getName().c_str());
+    try {
+        cp->createKernel("NoSuchKernel", context.getImplForTests());
+        fprintf(fo, "unknown accepted\n");
+    } catch (const OpenMMException& e) {
+        fprintf(fo, "unknown refused: %s\n", e.what());
+    }
+    fclose(fo);
+    return 0;
+}
+#endif
+
 int run(const std::string& mode, const char* in_path, const char* out_path) {
+#ifdef SDM_TEST_CUDA_PLATFORM
+    if (mode == "factory") return factory(out_path);
+#endif
     FILE* fi = fopen(in_path, "rb");
     if (!fi) throw std::runtime_error("cannot open input");
     Reader r{fi};
@@ -130,7 +182,14 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
     system.addForce(force);
     std::vector<Vec3> pos(n);
     for (int i = 0; i < n; ++i) pos[i] = Vec3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+#ifdef SDM_TEST_CUDA_PLATFORM
+    const bool on_cuda = mode == "cuda-mixed" || mode == "cuda-double";
+    Context context = on_cuda ? Context(system, *cuda_platform(mode == "cuda-double" ? "double" : "mixed"))
+                              : Context(system);
+#else
+    const bool on_cuda = false;
     Context context(system);
+#endif
     context.setPositions(pos);
     if (mode == "rebox") {
         for (int k = 0; k < 3; ++k) {
@@ -201,6 +260,17 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
         fclose(fo);
         return 0;
     }
+    if (on_cuda) {
+        // forces without the energy (the kernel's asynchronous form), then the
+        // results of that evaluation read afterwards
+        State st = context.getState(State::Forces, false, 1 << 2);
+        for (const Vec3& f : st.getForces()) {
+            const double v[3] = {f[0], f[1], f[2]};
+            put(fo, v, 3);
+        }
+        std::vector<double> res = force->getResults(context);
+        put(fo, res.data(), res.size());
+    }
     for (int pass = 0; pass < 2; ++pass) {
         if (pass == 1) {
             force->setLambda1(force->getLambda1() + 0.1);
@@ -224,7 +294,8 @@ int run(const std::string& mode, const char* in_path, const char* out_path) {
 
 int main(int argc, char** argv) {
     if (argc != 4) {
-        fprintf(stderr, "usage: shim_driver describe|evaluate|noneq|rebox|atomic <input> <output>\n");
+        fprintf(stderr, "usage: shim_driver describe|evaluate|noneq|rebox|atomic|factory|cuda-mixed|cuda-double "
+                        "<input> <output>\n");
         return 2;
     }
     try {

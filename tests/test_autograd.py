@@ -67,6 +67,26 @@ def test_bias_partials_fd(be):
         assert d[key] == pytest.approx((Wp - Wm) / (2 * h), rel=1e-6, abs=1e-8), key
 
 
+@pytest.mark.parametrize("method", [0, 1, 2])
+def test_bias_partials_batched_matches_scalar(method):
+    """The batched partials used on the device equal the scalar ones, per
+    replica, for every bias method (alpha = 0 included)."""
+    from openmm_sdm_plugin_gb300.autograd import bias_partials_device
+    rng = np.random.default_rng(method)
+    R = 7
+    be = rng.uniform(-50, 250, R)
+    l1, l2 = rng.uniform(0, 1, R), rng.uniform(0, 1, R)
+    al = np.where(np.arange(R) % 3 == 0, 0.0, rng.uniform(0.01, 0.3, R))
+    u0 = rng.uniform(50, 150, R)
+    t = lambda a: torch.tensor(a, dtype=torch.float64)
+    out = bias_partials_device(torch.full((R,), method), t(be), t(l1), t(l2), t(al), t(u0))
+    for r in range(R):
+        p = S.SDMParams(bias_method=method, lambda1=l1[r], lambda2=l2[r], alpha=al[r], u0=u0[r])
+        ref = bias_partials(p, be[r])
+        for k, key in enumerate(("lambda1", "lambda2", "alpha", "u0", "w0")):
+            assert float(out[k][r]) == pytest.approx(ref[key], rel=1e-13, abs=1e-13), (r, key)
+
+
 def _gpu_grads(s):
     from openmm_sdm_plugin_gb300.autograd import SDMEngine, sdm_potential
     eng = SDMEngine(s)

@@ -5,10 +5,12 @@ linked with libsdm_gb300.so.
 CPU: what the plugin reads from a NonbondedForce (exclusions from every
 exception, interacting exceptions with their parameters, method, cutoff,
 reaction-field dielectric, Ewald tolerance; the reference integrator's
-parameter defaults), the models it refuses, and a clean OpenMMException
-when no GPU is present.  GPU: energy, forces and results through a Context
-equal the C ABI's evaluation of the same system bit for bit, before and
-after updateParametersInContext."""
+parameter defaults), the models it refuses, a clean OpenMMException when no
+GPU is present, and the kernel factory that registerKernelFactories puts on
+the CUDA platform.  GPU: energy, forces and results through a Context equal
+the C ABI's evaluation of the same system bit for bit, before and after
+updateParametersInContext, on the host path and through the CalcSDMForce
+kernel on a stand-in of OpenMM's CUDA platform (tests/openmm_api/CudaSubset.cpp)."""
 import dataclasses
 import os
 import subprocess
@@ -174,6 +176,88 @@ def test_context_evaluation_equals_the_c_abi(driver, tmp_path, which):
     h.close()
 
 
+def _cuda_home():
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.exists(os.path.join(c, "include", "cuda.h")):
+            return c
+    pytest.skip("CUDA toolkit headers not found")
+
+
+@pytest.fixture(scope="module")
+def cuda_driver(built_lib, tmp_path_factory):
+    """The driver with the CUDA-platform stand-in (tests/openmm_api/CudaSubset.cpp)
+    and the plugin's platform kernel (shim/SDMCudaKernels.cpp)."""
+    cuda = _cuda_home()
+    exe = str(tmp_path_factory.mktemp("shim_cuda") / "shim_driver")
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-Wno-unused-parameter",
+           "-DSDM_TEST_CUDA_PLATFORM", "-I", API, "-I", os.path.join(ROOT, "include"), "-I", SHIM,
+           "-I", os.path.join(cuda, "include"),
+           os.path.join(SHIM, "SDMForceGB300.cpp"), os.path.join(SHIM, "SDMCudaKernels.cpp"),
+           os.path.join(API, "ApiSubset.cpp"), os.path.join(API, "CudaSubset.cpp"),
+           os.path.join(API, "shim_driver.cpp"), "-o", exe, built_lib,
+           "-L", os.path.join(cuda, "lib64"), "-lcudart",
+           "-Wl,-rpath," + os.path.dirname(built_lib) + ":" + os.path.join(cuda, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_kernel_factory_registers_on_the_cuda_platform(cuda_driver, tmp_path):
+    """registerKernelFactories (the plugin entry OpenMM calls on loading)
+    registers CalcSDMForce with the CUDA platform only; the kernel is created
+    by name through the platform, an unknown name is refused.  No GPU needed:
+    the kernel touches the device only when it first executes."""
+    out = str(tmp_path / "factory.txt")
+    r = subprocess.run([cuda_driver, "factory", "-", out], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    lines = open(out).read().splitlines()
+    assert "platform Reference supports 0" in lines
+    assert "platform CUDA supports 1" in lines
+    assert "kernel CalcSDMForce" in lines
+    assert any(ln.startswith("unknown refused:") for ln in lines)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["mixed", "double"])
+@pytest.mark.parametrize("which", ["config0", "temoa"])
+def test_cuda_platform_kernel_equals_the_c_abi(cuda_driver, tmp_path, precision, which):
+    """SDMForce on the CUDA platform runs the CalcSDMForce kernel: positions
+    gathered from the platform's shuffled posq (with the mixed-precision
+    correction), forces added into its 2^32 fixed-point buffer.  The energy,
+    the results and the forces equal the C ABI's on the same coordinates, bit
+    for bit (forces at the buffer's 2^-32 resolution); also for forces without
+    the energy (results read afterwards) and after updateParametersInContext."""
+    s = _dms_system() if which == "temoa" else S.config0(variant="b").replica(0)
+    p = s.params[0]
+    x = np.ascontiguousarray(s.positions[0], np.float64)
+    r, out = run(cuda_driver, "cuda-" + precision, tmp_path, s, p, x)
+    assert r.returncode == 0, r.stderr
+    raw = np.frombuffer(open(out, "rb").read(), np.float64)
+    n3 = 3 * s.n
+    f_async, res_async = raw[:n3].reshape(-1, 3), raw[n3:n3 + capi.NRESULTS]
+    got = raw[n3 + capi.NRESULTS:].reshape(2, -1)
+    if precision == "mixed":
+        # the positions the kernel sees: float(x) + float(x - float(x))
+        hi = x.astype(np.float32).astype(np.float64)
+        x = hi + (x - hi).astype(np.float32).astype(np.float64)
+    fix = lambda F: np.rint(np.asarray(F) * 2.0 ** 32) / 2.0 ** 32
+    ref = _reference_order(s)
+    h = capi.Handle([ref])
+    for k, lam1_shift in enumerate((0.0, 0.1)):
+        a = p.as_array().copy()
+        a[P_LAMBDA1] += lam1_shift
+        h.set_params(0, a)
+        res, F = h.evaluate(x)
+        e, rr, ff = got[k, 0], got[k, 1:1 + capi.NRESULTS], got[k, 1 + capi.NRESULTS:].reshape(-1, 3)
+        assert e == res[0, capi.R_EPOT]
+        assert np.array_equal(rr[:capi.R_STATUS], res[0, :capi.R_STATUS])
+        assert np.array_equal(ff, fix(F.reshape(-1, 3)))
+        if k == 0:
+            assert np.array_equal(f_async, ff)
+            assert np.array_equal(res_async[:capi.R_STATUS], res[0, :capi.R_STATUS])
+    h.close()
+
+
 @pytest.fixture(scope="module")
 def fake_driver(tmp_path_factory):
     """The same driver linked against the C-ABI stand-in of
@@ -281,3 +365,18 @@ def test_makefile_builds_the_plugin_library(driver, tmp_path):
     rb, out_b = run(driver, "describe", tmp_path / "b", s, s.params[0], s.positions[0])
     assert ra.returncode == 0 and rb.returncode == 0, ra.stderr + rb.stderr
     assert open(out_a, "rb").read() == open(out_b, "rb").read()
+    # the CUDA platform library, against a libOpenMMCUDA.so of the CUDA stand-in:
+    # it exports the plugin entry points OpenMM calls
+    cuda = _cuda_home()
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-I", API, "-I", os.path.join(cuda, "include"),
+                        os.path.join(API, "CudaSubset.cpp"), "-o", str(root / "lib" / "libOpenMMCUDA.so"),
+                        str(root / "lib" / "libOpenMM.so"), "-L", os.path.join(cuda, "lib64"), "-lcudart"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    plugin_cuda = str(tmp_path / "libSDMPluginGB300CUDA.so")
+    r = subprocess.run(["make", "-s", "-C", SHIM, "cuda", f"OPENMM_DIR={root}", f"OUT={plugin}",
+                        f"OUT_CUDA={plugin_cuda}", f"CUDA_HOME={cuda}"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    syms = subprocess.run(["nm", "-D", "--defined-only", plugin_cuda], capture_output=True, text=True).stdout
+    for name in ("registerKernelFactories", "registerPlatforms"):
+        assert f" T {name}" in syms, name
