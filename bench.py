@@ -552,6 +552,7 @@ def main():
     f_run = clocks.get("sm_mhz")
     jl_avg = sum(jlist_ms) / len(jlist_ms)
     pt_avg = sum(pert_ms) / len(pert_ms)
+
     roof = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
             "frac": achieved_tf / peak_tf, "traffic": K_PAIR_DRAM_BYTES_PER_LAUNCH,
             "traffic_source": K_PAIR_TRAFFIC_SOURCE,
@@ -594,7 +595,7 @@ def main():
                    "parallelism": f"replicas only, {world} independent rank(s)",
                    "schedule": {"split": h.get_option(capi.OPT_SPLIT), "ctas_per_sm": h.get_option(capi.OPT_CTAS_PER_SM),
                                 "ctas_resident": h.get_option(capi.OPT_PAIR_RESIDENT),
-                                "pair_variant": h.get_option(capi.OPT_PAIR_VARIANT),
+                                "stage_chunk": h.get_option(capi.OPT_STAGE_CHUNK),
                                 "autotuned": tuned is not None}},
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -335,10 +335,9 @@ enum {
                                  cudaHostRegister) in place instead of staging them through a
                                  device copy; results and forces are always copied out (default 0:
                                  on GB300 the two measured on par) */
-    SDM_OPT_PAIR_VARIANT = 7  /* main-pass implementation: 0 = candidates staged through shared
-                                 memory by cp.async, masks in every tile (default); 1 = candidates
-                                 loaded into registers one step ahead, partial-mask candidates in
-                                 a ring of their own.  Same pair sets and terms. */
+    SDM_OPT_STAGE_CHUNK = 7   /* cluster-pair list entries the main pass stages per chunk
+                                 (cp.async into shared memory, two chunks ahead): 8, 12 (default)
+                                 or 16.  Same pair sets and terms; the autotuner's tile-staging axis. */
 };
 sdm_status sdm_set_option(sdm_handle* h, int option, int value);
 sdm_status sdm_get_option(const sdm_handle* h, int option, int* value);
@@ -347,8 +346,34 @@ sdm_status sdm_get_option(const sdm_handle* h, int option, int* value);
  * and ms[i] for i < *count (in: capacity, out: entries). */
 sdm_status sdm_get_kernel_times(const sdm_handle* h, const char** names, float* ms, int* count);
 
-/* Tries every schedule candidate (split x CTAs per SM) on coordinates x
- * (device pointer) and keeps the fastest; writes the choice to split/ctas. */
+/* The main-pass choice of the autotuner. */
+typedef struct {
+    int stage_chunk;    /* SDM_OPT_STAGE_CHUNK */
+    int ctas_per_sm;    /* SDM_OPT_CTAS_PER_SM */
+    int split;          /* SDM_OPT_SPLIT */
+    float ms;           /* median time of one whole evaluation (graph replay) with this choice */
+    int from_cache;     /* 1: read from the cache file, nothing timed */
+} sdm_tune_result;
+
+/* Autotuner (no counterpart in the reference, which has one fixed OpenCL
+ * schedule).  Times every staging chunk (8, 12, 16 list entries) x CTAs per
+ * SM (3, 4) x split (1, 2) on coordinates x (device pointer): each candidate is a whole
+ * evaluation replayed as a CUDA graph, 5 timed replays after 2 warm-up ones,
+ * median.  The fastest becomes the handle's setting.  With cache_path, the
+ * choice is stored in that text file under the workload key of
+ * sdm_tune_key, and a later call with the same key (another handle, another
+ * process) takes it from there without timing.  Synchronises.  Returns
+ * SDM_ERR_CAPACITY if the lists overflowed on x (evaluate once, then tune). */
+sdm_status sdm_autotune_cached(sdm_handle* h, const double* x_device, const char* cache_path,
+                               sdm_tune_result* out);
+
+/* The cache key of a workload: mean particles per replica, mean density
+ * (1/nm^3, one decimal), cutoff, replicas, systems, electrostatics and the
+ * device's SM count.  Host only (no device needed). */
+sdm_status sdm_tune_key(const sdm_system_desc* systems, int num_systems, int num_sms, char* key, int capacity);
+
+/* sdm_autotune_cached without a cache file; writes the chosen split and CTAs
+ * per SM. */
 sdm_status sdm_autotune(sdm_handle* h, const double* x_device, int* split, int* ctas_per_sm);
 
 /* Interaction counts of coordinates x (host pointer) under the kernels' own

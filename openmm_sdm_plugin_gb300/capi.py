@@ -36,12 +36,13 @@ RESULT_FIELDS = ("U0", "U1", "u", "BindE", "fp", "W", "dW", "s", "E_pot", "dWdla
  R_STATUS, R_NCL) = range(16)
 
 (OPT_GRAPH, OPT_PROFILE, OPT_SPLIT, OPT_CTAS_PER_SM, OPT_VERIFY, OPT_PAIR_RESIDENT, OPT_ZERO_COPY,
- OPT_PAIR_VARIANT) = range(8)
+ OPT_STAGE_CHUNK) = range(8)
 
 EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_set_displacement", "sdm_set_params", "sdm_evaluate", "sdm_evaluate_device",
             "sdm_get_state_forces", "sdm_get_state_forces_device", "sdm_check_status", "sdm_set_option", "sdm_get_option",
-            "sdm_get_kernel_times", "sdm_autotune", "sdm_count_pairs", "sdm_get_grid",
+            "sdm_get_kernel_times", "sdm_autotune", "sdm_autotune_cached", "sdm_tune_key",
+            "sdm_count_pairs", "sdm_get_grid",
             "sdm_export_lists", "sdm_evaluate_noalloc", "sdm_set_particle_params",
             "sdm_adjoint", "sdm_adjoint_device", "sdm_get_num_perturbed", "sdm_set_langevin", "sdm_langevin_step", "sdm_set_restraints",
             "sdm_set_restraint_control", "sdm_get_restraint_energies", "sdm_set_rigid_waters",
@@ -56,6 +57,11 @@ class SdmError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"sdm status {status}: {message}")
         self.status = status
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("stage_chunk", C.c_int), ("ctas_per_sm", C.c_int), ("split", C.c_int), ("ms", C.c_float),
+                ("from_cache", C.c_int)]
 
 
 class SystemDesc(C.Structure):
@@ -114,6 +120,8 @@ def load_library(path: str = LIB_PATH):
         L.sdm_get_option.argtypes = [vp, C.c_int, ip]
         L.sdm_get_kernel_times.argtypes = [vp, C.POINTER(C.c_char_p), C.POINTER(C.c_float), ip]
         L.sdm_autotune.argtypes = [vp, vp, ip, ip]
+        L.sdm_autotune_cached.argtypes = [vp, vp, C.c_char_p, C.POINTER(TuneResult)]
+        L.sdm_tune_key.argtypes = [C.POINTER(SystemDesc), C.c_int, C.c_int, C.c_char_p, C.c_int]
         L.sdm_count_pairs.argtypes = [vp, vp, vp]
         L.sdm_get_grid.argtypes = [vp, C.c_int, ip]
         L.sdm_export_lists.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, ip, vp, vp, vp]
@@ -188,6 +196,48 @@ def restraint_desc(rs, keep):
     return d
 
 
+def system_descs(systems, keep):
+    """sdm_system_desc array of systems; the arrays it points to are appended
+    to `keep` (they must outlive the array)."""
+    descs = (SystemDesc * len(systems))()
+    for k, s in enumerate(systems):
+        q = np.ascontiguousarray(s.charge, np.float64)
+        sg = np.ascontiguousarray(s.sigma, np.float64)
+        ep = np.ascontiguousarray(s.epsilon, np.float64)
+        ex = np.ascontiguousarray(np.asarray(s.exclusions, np.int32).reshape(-1))
+        dd = np.ascontiguousarray(np.asarray(s.displacement, np.float64).reshape(-1))
+        keep += [q, sg, ep, ex, dd]
+        d = descs[k]
+        d.num_particles = int(q.shape[0])
+        d.charge = q.ctypes.data_as(C.POINTER(C.c_double))
+        d.sigma = sg.ctypes.data_as(C.POINTER(C.c_double))
+        d.epsilon = ep.ctypes.data_as(C.POINTER(C.c_double))
+        d.num_exclusions = int(ex.shape[0] // 2)
+        d.exclusions = ex.ctypes.data_as(C.POINTER(C.c_int)) if ex.size else None
+        d.displacement = dd.ctypes.data_as(C.POINTER(C.c_double))
+        d.box[:] = [float(v) for v in s.box]
+        d.cutoff = float(s.cutoff)
+        d.reaction_field_dielectric = float(s.eps_rf)
+        d.num_replicas = int(s.positions.shape[0]) if getattr(s, "positions", None) is not None else 1
+        if getattr(s, "nonbonded_method", "rf") == "pme":
+            d.nonbonded_method = NB_PME
+            d.ewald_tolerance = float(getattr(s, "ewald_tolerance", 5e-4))
+            g = getattr(s, "pme_grid", None)
+            if g is not None:
+                d.pme_grid[:] = [int(v) for v in g]
+        xp = getattr(s, "exceptions", None)
+        if xp is not None and len(xp):
+            xpi = np.ascontiguousarray(np.asarray(xp, np.int32).reshape(-1))
+            xpp = np.ascontiguousarray(np.asarray(s.exception_params, np.float64).reshape(-1))
+            if xpp.size != 3 * (xpi.size // 2):
+                raise ValueError("exception_params needs (charge product, sigma, epsilon) per pair")
+            keep += [xpi, xpp]
+            d.num_exceptions = int(xpi.size // 2)
+            d.exception_pairs = xpi.ctypes.data_as(C.POINTER(C.c_int))
+            d.exception_params = xpp.ctypes.data_as(C.POINTER(C.c_double))
+    return descs
+
+
 class Handle:
     """Owning wrapper of one ``sdm_handle``.
 
@@ -199,42 +249,7 @@ class Handle:
         self.lib = load_library()
         self.systems = list(systems)
         self._keep = []
-        descs = (SystemDesc * len(self.systems))()
-        for k, s in enumerate(self.systems):
-            q = np.ascontiguousarray(s.charge, np.float64)
-            sg = np.ascontiguousarray(s.sigma, np.float64)
-            ep = np.ascontiguousarray(s.epsilon, np.float64)
-            ex = np.ascontiguousarray(np.asarray(s.exclusions, np.int32).reshape(-1))
-            dd = np.ascontiguousarray(np.asarray(s.displacement, np.float64).reshape(-1))
-            self._keep += [q, sg, ep, ex, dd]
-            d = descs[k]
-            d.num_particles = int(q.shape[0])
-            d.charge = q.ctypes.data_as(C.POINTER(C.c_double))
-            d.sigma = sg.ctypes.data_as(C.POINTER(C.c_double))
-            d.epsilon = ep.ctypes.data_as(C.POINTER(C.c_double))
-            d.num_exclusions = int(ex.shape[0] // 2)
-            d.exclusions = ex.ctypes.data_as(C.POINTER(C.c_int)) if ex.size else None
-            d.displacement = dd.ctypes.data_as(C.POINTER(C.c_double))
-            d.box[:] = [float(v) for v in s.box]
-            d.cutoff = float(s.cutoff)
-            d.reaction_field_dielectric = float(s.eps_rf)
-            d.num_replicas = int(s.positions.shape[0]) if getattr(s, "positions", None) is not None else 1
-            if getattr(s, "nonbonded_method", "rf") == "pme":
-                d.nonbonded_method = NB_PME
-                d.ewald_tolerance = float(getattr(s, "ewald_tolerance", 5e-4))
-                g = getattr(s, "pme_grid", None)
-                if g is not None:
-                    d.pme_grid[:] = [int(v) for v in g]
-            xp = getattr(s, "exceptions", None)
-            if xp is not None and len(xp):
-                xpi = np.ascontiguousarray(np.asarray(xp, np.int32).reshape(-1))
-                xpp = np.ascontiguousarray(np.asarray(s.exception_params, np.float64).reshape(-1))
-                if xpp.size != 3 * (xpi.size // 2):
-                    raise ValueError("exception_params needs (charge product, sigma, epsilon) per pair")
-                self._keep += [xpi, xpp]
-                d.num_exceptions = int(xpi.size // 2)
-                d.exception_pairs = xpi.ctypes.data_as(C.POINTER(C.c_int))
-                d.exception_params = xpp.ctypes.data_as(C.POINTER(C.c_double))
+        descs = system_descs(self.systems, self._keep)
         h = C.c_void_p()
         st = self.lib.sdm_create(descs, len(self.systems), int(device), C.byref(h))
         if st != SDM_OK:
@@ -407,10 +422,14 @@ class Handle:
         self._check(self.lib.sdm_get_kernel_times(self.h, names, ms, C.byref(n)))
         return {names[k].decode(): float(ms[k]) for k in range(n.value)}
 
-    def autotune(self, x_ptr: int):
-        sp, ct = C.c_int(0), C.c_int(0)
-        self._check(self.lib.sdm_autotune(self.h, C.c_void_p(x_ptr), C.byref(sp), C.byref(ct)))
-        return sp.value, ct.value
+    def autotune(self, x_ptr: int, cache_path=None):
+        """sdm_autotune_cached on device coordinates: dict of the chosen
+        stage_chunk, ctas_per_sm, split, the median ms and from_cache."""
+        r = TuneResult()
+        self._check(self.lib.sdm_autotune_cached(self.h, C.c_void_p(x_ptr),
+                                                 cache_path.encode() if cache_path else None, C.byref(r)))
+        return dict(stage_chunk=r.stage_chunk, ctas_per_sm=r.ctas_per_sm, split=r.split, ms=r.ms,
+                    from_cache=bool(r.from_cache))
 
     def count_pairs(self, x):
         x = np.ascontiguousarray(np.asarray(x, np.float64).reshape(-1))
@@ -452,3 +471,15 @@ def evaluate_noalloc(n, x_ptr, q_ptr, sig_ptr, eps_ptr, eoff_ptr, eidx_ptr, d_pt
                                 C.c_void_p(stream) if stream else None)
     if st != SDM_OK:
         raise SdmError(st, L.sdm_last_error(None).decode())
+
+
+def tune_key(systems, num_sms: int) -> str:
+    """The autotuner's cache key of a workload (sdm_tune_key; no device needed)."""
+    L = load_library()
+    keep = []
+    descs = system_descs(list(systems), keep)
+    buf = C.create_string_buffer(256)
+    st = L.sdm_tune_key(descs, len(systems), int(num_sms), buf, 256)
+    if st != SDM_OK:
+        raise SdmError(st, "sdm_tune_key failed")
+    return buf.value.decode()

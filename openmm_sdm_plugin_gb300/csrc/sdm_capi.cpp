@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <new>
@@ -25,9 +26,9 @@ cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* cl_prefix, 
 cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_t st);
 cudaError_t sdm_pair_prepare();
 #define SDM_MAX_CTAS 4  // pair-kernel CTAs per SM with a built register bound
-int sdm_pair_resident(int ctas_per_sm, int variant);
+int sdm_pair_resident(int ctas_per_sm, int chunk);
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
-                            int resident, bool pme, int variant, cudaStream_t st);
+                            int resident, bool pme, int chunk, cudaStream_t st);
 cudaError_t sdm_launch_perturb(const SdmArgs& a, int mode, cudaStream_t st);
 cudaError_t sdm_launch_exceptions(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_pme(const SdmArgs& a, const cufftHandle* r2c, const cufftHandle* c2r, const long long* grid_off,
@@ -153,8 +154,8 @@ struct sdm_handle {
     bool lv_set = false, lv_dirty = false;
     // options
     int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 4, opt_verify = 1, opt_zero_copy = 0;
-    int opt_pair_variant = 0;
-    int pair_res[2][SDM_MAX_CTAS + 1] = {};  // resident pair-kernel CTAs per SM by variant and request
+    int opt_chunk = 12;                   // list entries per staged chunk of the main pass (8, 12, 16)
+    int pair_res[3][SDM_MAX_CTAS + 1] = {};  // resident pair-kernel CTAs per SM by chunk (8, 12, 16) and request
     // graphs
     std::map<GraphKey, cudaGraphExec_t> graphs;
     // profiling
@@ -172,6 +173,9 @@ struct sdm_handle {
 static sdm_status sdm_reserve_lists(sdm_handle* h, int cap);
 
 namespace {
+
+// index of a staging chunk size (8, 12, 16) in the per-chunk tables
+inline int chunk_index(int chunk) { return chunk == 8 ? 0 : chunk == 16 ? 2 : 1; }
 
 const char* const kKernelNames[] = {"k_cells", "k_scan", "k_bucket", "k_cellsort", "k_clusters",
                                     "k_jlist", "k_pair", "k_pert_prep+k_perturb", "k_finalize+k_mix"};
@@ -646,8 +650,8 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->cl_prefix, h->done, st, ev, 6, fl));
     SDM_CUDA(h, sdm_launch_jlist(a, h->cl_prefix, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[6], st, fl));
-    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[h->opt_pair_variant][h->opt_ctas],
-                                h->pme, h->opt_pair_variant, st));
+    SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[chunk_index(h->opt_chunk)][h->opt_ctas],
+                                h->pme, h->opt_chunk, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
     if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
     if (mode == 0) SDM_CUDA(h, sdm_launch_exceptions(a, st));
@@ -722,7 +726,7 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
         return SDM_OK;
     }
     const bool gprof = h->opt_profile == 2;
-    GraphKey key{x, res, f, st, a.split, h->opt_ctas + (gprof ? 100 : 0) + 1000 * h->opt_pair_variant};
+    GraphKey key{x, res, f, st, a.split, h->opt_ctas + (gprof ? 100 : 0) + 1000 * h->opt_chunk};
     if (lv) { key.v = lv->v; key.invm = lv->invm; key.fext = lv->fext; }
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
@@ -823,8 +827,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     h->device = device;
     if (cudaSetDevice(device) != cudaSuccess) { delete h; return fail(nullptr, SDM_ERR_CUDA, "cudaSetDevice failed"); }
     if (sdm_pair_prepare() != cudaSuccess) { delete h; return fail(nullptr, SDM_ERR_CUDA, "pair kernel setup failed"); }
-    for (int v = 0; v < 2; ++v)
-        for (int c = 1; c <= SDM_MAX_CTAS; ++c) h->pair_res[v][c] = sdm_pair_resident(c, v);
+    for (int k = 0; k < 3; ++k)
+        for (int c = 1; c <= SDM_MAX_CTAS; ++c) h->pair_res[k][c] = sdm_pair_resident(c, 8 + 4 * k);
     cudaDeviceProp prop{};
     cudaGetDeviceProperties(&prop, device);
     if (prop.major < 10) {
@@ -1712,9 +1716,10 @@ sdm_status sdm_set_option(sdm_handle* h, int option, int value) {
             break;
         case SDM_OPT_VERIFY: h->opt_verify = value ? 1 : 0; break;
         case SDM_OPT_ZERO_COPY: h->opt_zero_copy = value ? 1 : 0; break;
-        case SDM_OPT_PAIR_VARIANT:
-            if (value != 0 && value != 1) return fail(h, SDM_ERR_INVALID_ARGUMENT, "pair variant must be 0 or 1");
-            h->opt_pair_variant = value;
+        case SDM_OPT_STAGE_CHUNK:
+            if (value != 8 && value != 12 && value != 16)
+                return fail(h, SDM_ERR_INVALID_ARGUMENT, "stage chunk must be 8, 12 or 16");
+            h->opt_chunk = value;
             break;
         default: return fail(h, SDM_ERR_INVALID_ARGUMENT, "unknown option");
     }
@@ -1729,8 +1734,8 @@ sdm_status sdm_get_option(const sdm_handle* h, int option, int* value) {
         case SDM_OPT_SPLIT: *value = h->opt_split; break;
         case SDM_OPT_CTAS_PER_SM: *value = h->opt_ctas; break;
         case SDM_OPT_VERIFY: *value = h->opt_verify; break;
-        case SDM_OPT_PAIR_RESIDENT: *value = h->pair_res[h->opt_pair_variant][h->opt_ctas]; break;
-        case SDM_OPT_PAIR_VARIANT: *value = h->opt_pair_variant; break;
+        case SDM_OPT_PAIR_RESIDENT: *value = h->pair_res[chunk_index(h->opt_chunk)][h->opt_ctas]; break;
+        case SDM_OPT_STAGE_CHUNK: *value = h->opt_chunk; break;
         case SDM_OPT_ZERO_COPY: *value = h->opt_zero_copy; break;
         default: return SDM_ERR_INVALID_ARGUMENT;
     }
@@ -1756,32 +1761,183 @@ sdm_status sdm_get_kernel_times(const sdm_handle* hc, const char** names, float*
     return SDM_OK;
 }
 
-sdm_status sdm_autotune(sdm_handle* h, const double* x_device, int* split, int* ctas_per_sm) {
+// ---------------------------------------------------------------------------
+// autotuner: main-pass implementation x CTAs per SM x split, each timed on
+// the production path (the captured graph of a whole evaluation), the choice
+// kept in a text cache keyed by the workload
+// ---------------------------------------------------------------------------
+namespace {
+
+// workload key: mean particles per replica, mean density, cutoff, replicas,
+// systems, electrostatics and the SM count of the device
+std::string tune_key_of(long long particles, int replicas, double volume_weighted, double rc, int systems, bool pme,
+                        int sms) {
+    const double rho = volume_weighted > 0.0 ? (double)particles / volume_weighted : 0.0;
+    char buf[256];
+    snprintf(buf, sizeof buf, "sdm-tune-v1 n=%lld rho=%.1f rc=%.3f replicas=%d systems=%d method=%s sms=%d",
+             replicas > 0 ? (particles + replicas / 2) / replicas : 0LL, rho, rc, replicas, systems,
+             pme ? "pme" : "rf", sms);
+    return buf;
+}
+
+bool tune_cache_read(const char* path, const std::string& key, sdm_tune_result* r) {
+    if (!path) return false;
+    FILE* f = fopen(path, "r");
+    if (!f) return false;
+    char line[512];
+    bool found = false;
+    while (fgets(line, sizeof line, f)) {
+        const char* bar = strchr(line, '|');
+        if (!bar || std::string(line, bar - line) != key) continue;
+        sdm_tune_result t = {};
+        if (sscanf(bar + 1, "%d %d %d %f", &t.stage_chunk, &t.ctas_per_sm, &t.split, &t.ms) == 4) {
+            *r = t;
+            found = true;   // the last line of a key wins
+        }
+    }
+    fclose(f);
+    return found;
+}
+
+bool tune_cache_write(const char* path, const std::string& key, const sdm_tune_result& r) {
+    if (!path) return true;
+    std::vector<std::string> keep;
+    if (FILE* f = fopen(path, "r")) {
+        char line[512];
+        while (fgets(line, sizeof line, f)) {
+            const char* bar = strchr(line, '|');
+            if (bar && std::string(line, bar - line) == key) continue;
+            keep.emplace_back(line);
+        }
+        fclose(f);
+    }
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE* f = fopen(tmp.c_str(), "w");
+    if (!f) return false;
+    for (const std::string& l : keep) fputs(l.c_str(), f);
+    fprintf(f, "%s|%d %d %d %.6f\n", key.c_str(), r.stage_chunk, r.ctas_per_sm, r.split, r.ms);
+    const bool ok = fclose(f) == 0;
+    return ok && rename(tmp.c_str(), path) == 0;
+}
+
+std::string tune_key_handle(const sdm_handle* h) {
+    long long particles = 0;
+    double vol = 0.0, rc = 0.0;
+    for (const SysHost& s : h->sys) {
+        particles += (long long)s.n * s.replicas;
+        vol += s.dev.box[0] * s.dev.box[1] * s.dev.box[2] * s.replicas;
+        rc = std::max(rc, s.dev.rc);
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    return tune_key_of(particles, h->nrep, vol, rc, (int)h->sys.size(), h->pme, sms);
+}
+
+}  // namespace
+
+sdm_status sdm_tune_key(const sdm_system_desc* systems, int num_systems, int num_sms, char* key, int capacity) {
+    if (!systems || num_systems < 1 || !key || capacity < 1) return SDM_ERR_INVALID_ARGUMENT;
+    long long particles = 0;
+    int replicas = 0;
+    double vol = 0.0, rc = 0.0;
+    bool pme = false;
+    for (int k = 0; k < num_systems; ++k) {
+        const sdm_system_desc& d = systems[k];
+        particles += (long long)d.num_particles * d.num_replicas;
+        replicas += d.num_replicas;
+        vol += d.box[0] * d.box[1] * d.box[2] * d.num_replicas;
+        rc = std::max(rc, d.cutoff);
+        pme = pme || d.nonbonded_method == SDM_NB_PME;
+    }
+    const std::string s = tune_key_of(particles, replicas, vol, rc, num_systems, pme, num_sms);
+    if ((int)s.size() + 1 > capacity) return SDM_ERR_CAPACITY;
+    memcpy(key, s.c_str(), s.size() + 1);
+    return SDM_OK;
+}
+
+sdm_status sdm_autotune_cached(sdm_handle* h, const double* x_device, const char* cache_path,
+                               sdm_tune_result* out) {
     if (!h || !x_device) return SDM_ERR_INVALID_ARGUMENT;
     cudaSetDevice(h->device);
-    const int osplit = h->opt_split, octas = h->opt_ctas, oprof = h->opt_profile;
-    h->opt_profile = 1;
-    float best = 1e30f;
-    int bs = osplit, bc = octas;
-    const int splits[] = {1, 2, 4};
-    const int ctas[] = {3, 4};
-    for (int sp : splits)
-        for (int c : ctas) {
-            h->opt_split = sp;
-            h->opt_ctas = c;
-            float t = 0.f;
-            for (int rep = 0; rep < 4; ++rep) {
-                sdm_status s = run(h, x_device, h->res_in, h->f_in, h->stream, 0, false);
-                if (s) { h->opt_split = osplit; h->opt_ctas = octas; h->opt_profile = oprof; return s; }
-                if (rep > 0) t += h->last_ms[5] + h->last_ms[6] + h->last_ms[7];
+    const std::string key = tune_key_handle(h);
+    sdm_tune_result best = {};
+    if (tune_cache_read(cache_path, key, &best) &&
+        (best.stage_chunk == 8 || best.stage_chunk == 12 || best.stage_chunk == 16) &&
+        best.ctas_per_sm >= 1 && best.ctas_per_sm <= SDM_MAX_CTAS &&
+        (best.split == 1 || best.split == 2 || best.split == 4) &&
+        h->pair_res[chunk_index(best.stage_chunk)][best.ctas_per_sm] > 0) {
+        h->opt_chunk = best.stage_chunk;
+        h->opt_ctas = best.ctas_per_sm;
+        h->opt_split = best.split;
+        best.from_cache = 1;
+        if (out) *out = best;
+        return SDM_OK;
+    }
+    const int ochunk = h->opt_chunk, octas = h->opt_ctas, osplit = h->opt_split, oprof = h->opt_profile;
+    auto restore = [&]() {
+        h->opt_chunk = ochunk; h->opt_ctas = octas; h->opt_split = osplit; h->opt_profile = oprof;
+    };
+    h->opt_profile = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        restore();
+        return fail(h, SDM_ERR_CUDA, "cudaEventCreate");
+    }
+    best.ms = 1e30f;
+    sdm_status st = SDM_OK;
+    for (int ch : {8, 12, 16})
+        for (int c = 3; c <= SDM_MAX_CTAS && st == SDM_OK; ++c)
+            for (int sp : {1, 2}) {
+                if (st != SDM_OK || h->pair_res[chunk_index(ch)][c] < 1) continue;
+                h->opt_chunk = ch;
+                h->opt_ctas = c;
+                h->opt_split = sp;
+                std::vector<float> ms;
+                for (int rep = 0; rep < 7; ++rep) {
+                    if (rep >= 2) cudaEventRecord(e0, h->stream);
+                    st = run(h, x_device, h->res_in, h->f_in, h->stream, 0, true);
+                    if (st) break;
+                    if (rep >= 2) {
+                        cudaEventRecord(e1, h->stream);
+                        cudaEventSynchronize(e1);
+                        float t = 0.f;
+                        cudaEventElapsedTime(&t, e0, e1);
+                        ms.push_back(t);
+                    }
+                }
+                if (st) break;
+                std::sort(ms.begin(), ms.end());
+                const float med = ms[ms.size() / 2];
+                if (med < best.ms) best = sdm_tune_result{ch, c, sp, med, 0};
             }
-            if (t < best) { best = t; bs = sp; bc = c; }
-        }
-    h->opt_split = bs;
-    h->opt_ctas = bc;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) { restore(); return st; }
+    // the timed calls ran on the caller's coordinates: their lists may have
+    // overflowed, which the status word reports (and the next call regrows)
+    int v = 0;
+    st = check_dev_status(h, &v, false);
+    if (st) { restore(); return st; }
+    if (v & SDM_DEV_LIST_OVERFLOW) {
+        restore();
+        return fail(h, SDM_ERR_CAPACITY, "lists overflowed while tuning: evaluate once, then tune again");
+    }
+    h->opt_chunk = best.stage_chunk;
+    h->opt_ctas = best.ctas_per_sm;
+    h->opt_split = best.split;
     h->opt_profile = oprof;
-    if (split) *split = bs;
-    if (ctas_per_sm) *ctas_per_sm = bc;
+    if (!tune_cache_write(cache_path, key, best)) return fail(h, SDM_ERR_INVALID_ARGUMENT, "cannot write the tuning cache");
+    if (out) *out = best;
+    return SDM_OK;
+}
+
+sdm_status sdm_autotune(sdm_handle* h, const double* x_device, int* split, int* ctas_per_sm) {
+    sdm_tune_result r = {};
+    sdm_status s = sdm_autotune_cached(h, x_device, nullptr, &r);
+    if (s) return s;
+    if (split) *split = r.split;
+    if (ctas_per_sm) *ctas_per_sm = r.ctas_per_sm;
     return SDM_OK;
 }
 

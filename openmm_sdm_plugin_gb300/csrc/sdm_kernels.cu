@@ -513,27 +513,27 @@ struct Ring {                   // one tile ring: 64 prepared j entries
     float4 b[SDM_RING];         // (hs, se, mask bits, slot bits)
 };
 
-#define SDM_CH 12               // cluster-pair list entries per staged chunk
+// cluster-pair list entries per staged chunk (SDM_OPT_STAGE_CHUNK): 8, 12 (default) or 16
+#define SDM_CH_DEFAULT 12
 
 // Two-level cp.async pipeline: list entries two chunks ahead, the candidate
 // particles (8 per entry) one chunk ahead of the chunk being filtered.
-// i-cluster data of particles (2u, 2u+1), read as broadcasts: qh[u] = (q, q',
-// sigma/2, sigma'/2), se[u] = (2 sqrt(eps), 2 sqrt(eps')), nx/ny/nz[u] the
-// negated coordinates (d = x_j + (-x_i) rounds like x_j - x_i)
-struct IParams {
-    float4 qh[4];
-    float2 se[4];
-    float2 nx[4], ny[4], nz[4];
+// i-cluster data of particles (2u, 2u+1) in three 16-byte words per u, read
+// as shared-memory broadcasts: (q, q', sigma/2, sigma'/2),
+// (2 sqrt(eps), 2 sqrt(eps'), -x, -x'), (-y, -y', -z, -z')
+struct IPar3 {
+    float4 a[4], b[4], c[4];
 };
 
+template <int CH>
 struct EvalSmem {
     Ring lj;                    // j with epsilon != 0
     Ring co;                    // j with epsilon == 0 (Coulomb only)
-    int4 je[3][SDM_CH];         // list entries of chunks c, c+1, c+2
-    float4 sx[2][SDM_CH * 8];   // staged cluster-local coordinates + charge of candidates
-    float2 sp[2][SDM_CH * 8];   // staged (sigma/2, 2 sqrt(eps)) of candidates
-    int sm_[2][SDM_CH * 8];     // staged molecule ids of candidates
-    IParams ip;                 // i-cluster parameters by particle pair, read as broadcasts
+    int4 je[3][CH];             // list entries of chunks c, c+1, c+2
+    float4 sx[2][CH * 8];       // staged cluster-local coordinates + charge of candidates
+    float2 sp[2][CH * 8];       // staged (sigma/2, 2 sqrt(eps)) of candidates
+    int sm_[2][CH * 8];         // staged molecule ids of candidates
+    IPar3 ip;                   // i-cluster parameters by particle pair, read as broadcasts
     int im[8];                  // i-cluster molecule ids
     float4 ib[2];               // i-cluster box centre and half extents (w: list cutoff squared)
 };
@@ -761,23 +761,22 @@ __global__ void __launch_bounds__(256, 4) k_jlist(SdmArgs a, const int* cl_prefi
 // K6b: main pass                                                            //
 // ------------------------------------------------------------------------- //
 
-// One tile: every lane owns one j of the ring window [head, head+count) and
-// sweeps the 8 i-particles of the cluster (warp-uniform i).  LJ = false is the
-// ring of j with epsilon = 0: Lennard-Jones vanishes for every i, Coulomb only.
-template <int MODE, bool IMG, bool LJ, bool PME>
-__device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
-                                          const Ring& rg, const IParams& ip, unsigned head, int count,
-                                          ICluster& ic, float& ef, long long& npair) {
-    const int lane = lane_id();
-    const unsigned idx = (head + lane) & (SDM_RING - 1);
-    const bool active = lane < count;
-    // inactive lanes use zeros, never stale ring contents
-    const float4 A = active ? rg.a[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 B = active ? rg.b[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const unsigned m = active ? __float_as_uint(B.z) : 0u;
+// One tile of 32 j (one per lane) against the 8 i of the cluster (warp-
+// uniform i, packed FP32x2 over i pairs).  MASKED: the lane's allowed-i bits
+// m apply; otherwise every i is allowed.  Out-of-range pairs are removed by
+// one select of r^2 to +inf per pair (rsqrt gives 0, and every force and
+// Lennard-Jones term carries a factor 1/r^2) and one select of the charge
+// product for the reaction-field or Ewald energy; the pair rule is the FP32
+// r^2 of these roundings below the FP32 cutoff square.  LJ = false: the j
+// have epsilon = 0 (Coulomb only).  Inactive lanes add no j force or energy.
+template <int MODE, bool IMG, bool PME, bool MASKED, bool LJ = true>
+__device__ __forceinline__ void pair_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R, const IPar3& ip,
+                                           const float4& A, float hj_s, float ej_s, unsigned m, bool active,
+                                           int slot, ICluster& ic, float& ef, long long& npair) {
     const float2 xs = make_float2(A.x, A.x), ys = make_float2(A.y, A.y), zs = make_float2(A.z, A.z);
-    const float2 qj = make_float2(A.w, A.w), hj = make_float2(B.x, B.x), ej = make_float2(B.y, B.y);
+    const float2 qj = make_float2(A.w, A.w), hj = make_float2(hj_s, hj_s), ej = make_float2(ej_s, ej_s);
     const float rc2 = S.rc2f;
+    const float inf = __int_as_float(0x7f800000);
     const float2 krf = make_float2(S.krf, S.krf), ncrf = make_float2(-S.crf, -S.crf);
     const float2 krf2 = make_float2(-2.0f * S.krf, -2.0f * S.krf);
     const float2 one_n = make_float2(-1.0f, -1.0f), c12 = make_float2(12.0f, 12.0f),
@@ -786,53 +785,50 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
     int cnt = 0;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        float2 dx = __fadd2_rn(xs, ip.nx[u]);
-        float2 dy = __fadd2_rn(ys, ip.ny[u]);
-        float2 dz = __fadd2_rn(zs, ip.nz[u]);
+        const float4 pa = ip.a[u], pb = ip.b[u], pc = ip.c[u];
+        float2 dx = __fadd2_rn(xs, make_float2(pb.z, pb.w));
+        float2 dy = __fadd2_rn(ys, make_float2(pc.x, pc.y));
+        float2 dz = __fadd2_rn(zs, make_float2(pc.z, pc.w));
         if (IMG) {
             dx = make_float2(img32(dx.x, S.Lf[0], S.invLf[0]), img32(dx.y, S.Lf[0], S.invLf[0]));
             dy = make_float2(img32(dy.x, S.Lf[1], S.invLf[1]), img32(dy.y, S.Lf[1], S.invLf[1]));
             dz = make_float2(img32(dz.x, S.Lf[2], S.invLf[2]), img32(dz.y, S.Lf[2], S.invLf[2]));
         }
-        // same roundings as r2_chain: dz*dz + (dy*dy + dx*dx)
         const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-        const bool ok0 = (r2.x < rc2) && ((m >> (2 * u)) & 1u);
-        const bool ok1 = (r2.y < rc2) && ((m >> (2 * u + 1)) & 1u);
+        bool ok0 = r2.x < rc2, ok1 = r2.y < rc2;
+        if (MASKED) {
+            ok0 = ok0 && ((m >> (2 * u)) & 1u);
+            ok1 = ok1 && ((m >> (2 * u + 1)) & 1u);
+        }
         if (MODE == MODE_COUNT) {
             cnt += (ok0 ? 1 : 0) + (ok1 ? 1 : 0);
             continue;
         }
-        const float2 r2s = make_float2(ok0 ? r2.x : 1.0f, ok1 ? r2.y : 1.0f);
-        const float2 ir = make_float2(fast_rsqrt(r2s.x), fast_rsqrt(r2s.y));
+        const float2 ir = make_float2(fast_rsqrt(ok0 ? r2.x : inf), fast_rsqrt(ok1 ? r2.y : inf));
         const float2 ir2 = __fmul2_rn(ir, ir);
-        const float4 qh = ip.qh[u];   // same address in every lane: one broadcast
-        float2 qq = __fmul2_rn(make_float2(qh.x, qh.y), qj);
-        qq = make_float2(ok0 ? qq.x : 0.0f, ok1 ? qq.y : 0.0f);
-        float2 fs;
+        const float2 qq = __fmul2_rn(make_float2(pa.x, pa.y), qj);
+        const float2 qqe = make_float2(ok0 ? qq.x : 0.0f, ok1 ? qq.y : 0.0f);
         float2 fc;
         if (PME) {
-            // Ewald direct space: qq erfc(beta r)/r, force qq (erfc/r + 2beta/sqrt(pi) e^{-beta^2 r^2}) / r^2
-            const float2 xb = __fmul2_rn(__fmul2_rn(r2s, ir), make_float2(S.beta_f, S.beta_f));
+            const float2 xb = __fmul2_rn(__fmul2_rn(r2, ir), make_float2(S.beta_f, S.beta_f));
             const float2 gx = make_float2(__expf(-xb.x * xb.x), __expf(-xb.y * xb.y));
             const float2 eci = __fmul2_rn(__fmul2_rn(erfc_scaled2(xb), gx), ir);
             fc = __fmul2_rn(qq, __ffma2_rn(make_float2(S.c2_f, S.c2_f), gx, eci));
-            e = __ffma2_rn(qq, eci, e);
+            e = __ffma2_rn(qqe, eci, e);
         } else {
-            fc = __fmul2_rn(qq, __ffma2_rn(krf2, r2s, ir));
+            fc = __fmul2_rn(qq, __ffma2_rn(krf2, r2, ir));
+            e = __ffma2_rn(qqe, __ffma2_rn(krf, r2, __fadd2_rn(ir, ncrf)), e);
         }
+        float2 fs;
         if (LJ) {
-            const float2 sg = __fadd2_rn(make_float2(qh.z, qh.w), hj);
+            const float2 sg = __fadd2_rn(make_float2(pa.z, pa.w), hj);
             const float2 s2 = __fmul2_rn(__fmul2_rn(sg, sg), ir2);
             const float2 s6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
-            float2 epsm = __fmul2_rn(ip.se[u], ej);
-            epsm = make_float2(ok0 ? epsm.x : 0.0f, ok1 ? epsm.y : 0.0f);
-            const float2 t6 = __fmul2_rn(epsm, s6);
+            const float2 t6 = __fmul2_rn(__fmul2_rn(make_float2(pb.x, pb.y), ej), s6);
             e = __ffma2_rn(t6, __fadd2_rn(s6, one_n), e);
-            if (!PME) e = __ffma2_rn(qq, __ffma2_rn(krf, r2s, __fadd2_rn(ir, ncrf)), e);
             fs = __fmul2_rn(__ffma2_rn(t6, __ffma2_rn(c12, s6, c6n), fc), ir2);
         } else {
-            if (!PME) e = __ffma2_rn(qq, __ffma2_rn(krf, r2s, __fadd2_rn(ir, ncrf)), e);
-            fs = __fmul2_rn(fc, ir2);
+            fs = __fmul2_rn(fc, ir2);   // j with epsilon = 0: Coulomb only
         }
         fjx = __ffma2_rn(fs, dx, fjx);
         fjy = __ffma2_rn(fs, dy, fjy);
@@ -845,7 +841,6 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
         npair += cnt;
     } else if (active) {
         const float gx = __fadd_rn(fjx.x, fjx.y), gy = __fadd_rn(fjy.x, fjy.y), gz = __fadd_rn(fjz.x, fjz.y);
-        const int slot = __float_as_int(B.w);
         const size_t gsl = (size_t)R.slot_win + slot;
         if (!(fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) < 1.0e9f)) atomicOr(a.status, SDM_DEV_FORCE_OVERFLOW);
         atomicAdd(a.F0x + gsl, fix64(gx));
@@ -853,6 +848,23 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
         atomicAdd(a.F0z + gsl, fix64(gz));
         ef += __fadd_rn(e.x, e.y);
     }
+}
+
+// One tile of a ring: every lane owns one j of the ring window [head,
+// head+count) and sweeps the 8 i-particles of the cluster.  LJ = false is the
+// ring of j with epsilon = 0: Lennard-Jones vanishes for every i, Coulomb only.
+template <int MODE, bool IMG, bool LJ, bool PME>
+__device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
+                                          const Ring& rg, const IPar3& ip, unsigned head, int count,
+                                          ICluster& ic, float& ef, long long& npair) {
+    const int lane = lane_id();
+    const unsigned idx = (head + lane) & (SDM_RING - 1);
+    const bool active = lane < count;
+    // inactive lanes use zeros, never stale ring contents, and allow no i
+    const float4 A = active ? rg.a[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 B = active ? rg.b[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned m = active ? __float_as_uint(B.z) : 0u;
+    pair_tile<MODE, IMG, PME, true, LJ>(a, S, R, ip, A, B.x, B.y, m, active, __float_as_int(B.w), ic, ef, npair);
 }
 
 // Computes the allowed-i mask of candidate slot j (cluster J) against
@@ -934,8 +946,8 @@ __device__ __forceinline__ void reduce_i_forces(const SdmArgs& a, const ICluster
     }
 }
 
-template <int MODE, bool IMG, bool PME>
-__device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSmem& sm) {
+template <int MODE, bool IMG, bool PME, int SDM_CH>
+__device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSmem<SDM_CH>& sm) {
     const int lane = lane_id();
     const SdmRep R = a.rep[r];
     const SdmSys S = a.sys[R.sys];
@@ -949,10 +961,13 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         if (lane < 8) { xi4 = a.clX[slot0 + lane]; pi2 = a.clP[slot0 + lane]; }
         __syncwarp();
         if (lane < 8) {
-            float* qh = reinterpret_cast<float*>(&sm.ip.qh[lane >> 1]);
-            qh[lane & 1] = xi4.w;
-            qh[2 + (lane & 1)] = pi2.x;
-            reinterpret_cast<float*>(&sm.ip.se[lane >> 1])[lane & 1] = pi2.y;
+            const int u = lane >> 1, h = lane & 1;
+            reinterpret_cast<float*>(&sm.ip.a[u])[h] = xi4.w;
+            reinterpret_cast<float*>(&sm.ip.a[u])[2 + h] = pi2.x;
+            reinterpret_cast<float*>(&sm.ip.b[u])[h] = pi2.y;
+            reinterpret_cast<float*>(&sm.ip.b[u])[2 + h] = -xi4.x;
+            reinterpret_cast<float*>(&sm.ip.c[u])[h] = -xi4.y;
+            reinterpret_cast<float*>(&sm.ip.c[u])[2 + h] = -xi4.z;
             sm.im[lane] = a.clM[slot0 + lane];
         }
         if (lane == 0) {
@@ -963,11 +978,6 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            if (lane < 8 && (lane >> 1) == u) {
-                reinterpret_cast<float*>(&sm.ip.nx[u])[lane & 1] = -xi4.x;
-                reinterpret_cast<float*>(&sm.ip.ny[u])[lane & 1] = -xi4.y;
-                reinterpret_cast<float*>(&sm.ip.nz[u])[lane & 1] = -xi4.z;
-            }
             ic.ax[u] = make_float2(0.f, 0.f); ic.ay[u] = ic.ax[u]; ic.az[u] = ic.ax[u];
         }
         __syncwarp();
@@ -1136,359 +1146,14 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
     if (lane == 0) a.e_part[(size_t)cw * a.split + part] = ed;
 }
 
-// ------------------------------------------------------------------------- //
-// K6b (v2): main pass with register-prefetched candidates                   //
-// ------------------------------------------------------------------------- //
-//
-// Same work as process_cluster, organised for fewer instructions per
-// candidate: the cluster-pair list arrives in 32-entry chunks (one 16-byte
-// cp.async per lane), each step's 32 candidates (4 entries x 8 slots) are
-// loaded straight into registers one step ahead, and candidates whose
-// allowed-i mask is partial (the own cluster, exclusion partners) go to a
-// ring of their own, so the tiles of the two main rings carry no mask logic
-// (outside image mode, padding i particles sit at 1e6 nm and fail the cutoff
-// by themselves).  Out-of-range pairs are removed by one select of r^2 to
-// +inf per pair (rsqrt gives 0, and every force and Lennard-Jones term
-// carries a factor 1/r^2) and one select of the charge product for the
-// reaction-field energy.  The pair rule is unchanged: FP32 r^2 of the same
-// roundings below the FP32 cutoff square.
-
-#define SDM_CH2 32              // list entries per staged chunk (one per lane)
-
-struct Eval2Smem {
-    Ring lj;                    // j with epsilon != 0, every i allowed
-    Ring co;                    // j with epsilon == 0, every i allowed
-    Ring mk;                    // j with a partial allowed-i mask (any epsilon)
-    int4 je[2][SDM_CH2];        // list entries, chunks c and c+1
-    IParams ip;
-    int im[8];
-};
-
-// One tile of ring `rg`.  MASKED: each lane's allowed-i bits come from the
-// ring (inactive lanes: none); otherwise every i is allowed and inactive
-// lanes hold far-away coordinates (image mode always uses masks).
-template <int MODE, bool IMG, bool LJ, bool PME, bool MASKED>
-__device__ __forceinline__ void eval_tile2(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
-                                           const Ring& rg, const IParams& ip, unsigned head, int count,
-                                           ICluster& ic, float& ef, long long& npair) {
-    const int lane = lane_id();
-    const unsigned idx = (head + lane) & (SDM_RING - 1);
-    const bool active = lane < count;
-    // inactive lanes sit at -1e6 nm: far from every particle, padding i
-    // particles (at +1e6 nm) included
-    const float far = -SDM_INVALID_COORD;
-    const float4 A = active ? rg.a[idx] : make_float4(far, far, far, 0.f);
-    const float4 B = active ? rg.b[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const unsigned m = MASKED ? (active ? __float_as_uint(B.z) : 0u) : 0xffu;
-    const float2 xs = make_float2(A.x, A.x), ys = make_float2(A.y, A.y), zs = make_float2(A.z, A.z);
-    const float2 qj = make_float2(A.w, A.w), hj = make_float2(B.x, B.x), ej = make_float2(B.y, B.y);
-    const float rc2 = S.rc2f;
-    const float inf = __int_as_float(0x7f800000);
-    const float2 krf = make_float2(S.krf, S.krf), ncrf = make_float2(-S.crf, -S.crf);
-    const float2 krf2 = make_float2(-2.0f * S.krf, -2.0f * S.krf);
-    const float2 one_n = make_float2(-1.0f, -1.0f), c12 = make_float2(12.0f, 12.0f),
-                 c6n = make_float2(-6.0f, -6.0f);
-    float2 fjx = make_float2(0.f, 0.f), fjy = fjx, fjz = fjx, e = fjx;
-    int cnt = 0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        float2 dx = __fadd2_rn(xs, ip.nx[u]);
-        float2 dy = __fadd2_rn(ys, ip.ny[u]);
-        float2 dz = __fadd2_rn(zs, ip.nz[u]);
-        if (IMG) {
-            dx = make_float2(img32(dx.x, S.Lf[0], S.invLf[0]), img32(dx.y, S.Lf[0], S.invLf[0]));
-            dy = make_float2(img32(dy.x, S.Lf[1], S.invLf[1]), img32(dy.y, S.Lf[1], S.invLf[1]));
-            dz = make_float2(img32(dz.x, S.Lf[2], S.invLf[2]), img32(dz.y, S.Lf[2], S.invLf[2]));
-        }
-        const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-        bool ok0 = r2.x < rc2, ok1 = r2.y < rc2;
-        if (MASKED) {
-            ok0 = ok0 && ((m >> (2 * u)) & 1u);
-            ok1 = ok1 && ((m >> (2 * u + 1)) & 1u);
-        }
-        if (MODE == MODE_COUNT) {
-            cnt += (ok0 ? 1 : 0) + (ok1 ? 1 : 0);
-            continue;
-        }
-        const float2 ir = make_float2(fast_rsqrt(ok0 ? r2.x : inf), fast_rsqrt(ok1 ? r2.y : inf));
-        const float2 ir2 = __fmul2_rn(ir, ir);
-        const float4 qh = ip.qh[u];
-        const float2 qq = __fmul2_rn(make_float2(qh.x, qh.y), qj);
-        const float2 qqe = make_float2(ok0 ? qq.x : 0.0f, ok1 ? qq.y : 0.0f);
-        float2 fc;
-        if (PME) {
-            // r^2 (finite) times 1/r: beta r in range, 0 outside (its terms then carry 1/r or 1/r^2 = 0)
-            const float2 xb = __fmul2_rn(__fmul2_rn(r2, ir), make_float2(S.beta_f, S.beta_f));
-            const float2 gx = make_float2(__expf(-xb.x * xb.x), __expf(-xb.y * xb.y));
-            const float2 eci = __fmul2_rn(__fmul2_rn(erfc_scaled2(xb), gx), ir);
-            fc = __fmul2_rn(qq, __ffma2_rn(make_float2(S.c2_f, S.c2_f), gx, eci));
-            e = __ffma2_rn(qqe, eci, e);
-        } else {
-            fc = __fmul2_rn(qq, __ffma2_rn(krf2, r2, ir));
-            e = __ffma2_rn(qqe, __ffma2_rn(krf, r2, __fadd2_rn(ir, ncrf)), e);
-        }
-        float2 fs;
-        if (LJ) {
-            const float2 sg = __fadd2_rn(make_float2(qh.z, qh.w), hj);
-            const float2 s2 = __fmul2_rn(__fmul2_rn(sg, sg), ir2);
-            const float2 s6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
-            const float2 t6 = __fmul2_rn(__fmul2_rn(ip.se[u], ej), s6);
-            e = __ffma2_rn(t6, __fadd2_rn(s6, one_n), e);
-            fs = __fmul2_rn(__ffma2_rn(t6, __ffma2_rn(c12, s6, c6n), fc), ir2);
-        } else {
-            fs = __fmul2_rn(fc, ir2);
-        }
-        fjx = __ffma2_rn(fs, dx, fjx);
-        fjy = __ffma2_rn(fs, dy, fjy);
-        fjz = __ffma2_rn(fs, dz, fjz);
-        ic.ax[u] = __ffma2_rn(fs, dx, ic.ax[u]);
-        ic.ay[u] = __ffma2_rn(fs, dy, ic.ay[u]);
-        ic.az[u] = __ffma2_rn(fs, dz, ic.az[u]);
-    }
-    if (MODE == MODE_COUNT) {
-        npair += cnt;
-    } else if (active) {
-        const float gx = __fadd_rn(fjx.x, fjx.y), gy = __fadd_rn(fjy.x, fjy.y), gz = __fadd_rn(fjz.x, fjz.y);
-        const size_t gsl = (size_t)R.slot_win + __float_as_int(B.w);
-        if (!(fmaxf(fabsf(gx), fmaxf(fabsf(gy), fabsf(gz))) < 1.0e9f)) atomicOr(a.status, SDM_DEV_FORCE_OVERFLOW);
-        atomicAdd(a.F0x + gsl, fix64(gx));
-        atomicAdd(a.F0y + gsl, fix64(gy));
-        atomicAdd(a.F0z + gsl, fix64(gz));
-        ef += __fadd_rn(e.x, e.y);
-    }
-}
-
-// appends the lanes with `take` to ring `rg` at tail t (ring counters are warp-uniform)
-__device__ __forceinline__ void ring_put(Ring& rg, unsigned& t, bool take, const float4& A, const float4& B) {
-    const unsigned bal = __ballot_sync(0xffffffffu, take);
-    if (take) {
-        const unsigned idx = (t + __popc(bal & ((1u << lane_id()) - 1u))) & (SDM_RING - 1);
-        rg.a[idx] = A;
-        rg.b[idx] = B;
-    }
-    t += __popc(bal);
-}
-
-template <int MODE, bool IMG, bool PME>
-__device__ void process_cluster2(const SdmArgs& a, int r, int I, int part, Eval2Smem& sm) {
-    const int lane = lane_id();
-    const SdmRep R = a.rep[r];
-    const SdmSys S = a.sys[R.sys];
-    const int cw = R.cl_win + I;
-    const int slot0 = R.slot_win + 8 * I;
-    ICluster ic;
-    {
-        float4 xi4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        float2 pi2 = make_float2(0.f, 0.f);
-        if (lane < 8) { xi4 = a.clX[slot0 + lane]; pi2 = a.clP[slot0 + lane]; }
-        __syncwarp();
-        if (lane < 8) {
-            float* qh = reinterpret_cast<float*>(&sm.ip.qh[lane >> 1]);
-            qh[lane & 1] = xi4.w;
-            qh[2 + (lane & 1)] = pi2.x;
-            reinterpret_cast<float*>(&sm.ip.se[lane >> 1])[lane & 1] = pi2.y;
-            reinterpret_cast<float*>(&sm.ip.nx[lane >> 1])[lane & 1] = -xi4.x;
-            reinterpret_cast<float*>(&sm.ip.ny[lane >> 1])[lane & 1] = -xi4.y;
-            reinterpret_cast<float*>(&sm.ip.nz[lane >> 1])[lane & 1] = -xi4.z;
-            sm.im[lane] = a.clM[slot0 + lane];
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            ic.ax[u] = make_float2(0.f, 0.f); ic.ay[u] = ic.ax[u]; ic.az[u] = ic.ax[u];
-        }
-    }
-    const float4 bc = a.cl_bbc[cw], bh = a.cl_bbh[cw];
-    const float rcl2 = S.rcl2f;
-    const unsigned vmask = __ballot_sync(0xffffffffu, lane < 8 && a.perm[slot0 + (lane & 7)] >= 0) & 0xffu;
-    // allowed-i bits before exclusions: outside image mode the padding i
-    // particles fail the cutoff by their coordinates, except for the list export
-    const unsigned base = (IMG || MODE == MODE_EMIT) ? vmask : 0xffu;
-    const int njl = min(a.jl_cnt[cw], a.jl_cap);
-    const int ebeg = (njl * part) / a.split, eend = (njl * (part + 1)) / a.split;
-    const int nent = eend - ebeg;
-    const int4* jl = a.jl + (size_t)cw * a.jl_cap + ebeg;
-    const float4* clX = a.clX + R.slot_win;
-    const float2* clP = a.clP + R.slot_win;
-    const int* clM = a.clM + R.slot_win;
-    const bool clique = S.excl_clique != 0;
-
-    unsigned hl = 0, tl = 0, hc = 0, tc = 0, hm = 0, tm = 0;   // ring counters (uniform)
-    float ef = 0.0f;
-    long long npair = 0;
-    int emit_n = 0;
-    const int t = lane & 7, q = lane >> 3;
-    const int nsteps = (nent + 3) >> 2;
-    const int nchunk = (nent + SDM_CH2 - 1) / SDM_CH2;
-    auto issue_chunk = [&](int c) {
-        if (c < nchunk && c * SDM_CH2 + lane < nent) cp_async16(&sm.je[c & 1][lane], jl + c * SDM_CH2 + lane);
-        cp_async_commit();
-    };
-    // candidate of step k for this lane: entry 4k + q (the last entry when past the end)
-    auto fetch = [&](int k, int4& en, float4& X, float2& P, int& M) {
-        const int e = min(4 * k + q, nent - 1);
-        en = sm.je[(e / SDM_CH2) & 1][e % SDM_CH2];
-        const int sj = 8 * (en.x & 0x7fffffff) + t;
-        X = __ldg(clX + sj);
-        P = __ldg(clP + sj);
-        M = clique ? __ldg(clM + sj) : 0;
-    };
-    int4 en;
-    float4 X;
-    float2 P;
-    int M = 0;
-    if (nsteps > 0) {
-        issue_chunk(0);
-        issue_chunk(1);
-        cp_async_wait<1>();
-        __syncwarp();
-        fetch(0, en, X, P, M);
-    }
-    for (int k = 0; k < nsteps; ++k) {
-        // the next step's candidate, loaded while this one is processed
-        int4 en1 = en;
-        float4 X1 = X;
-        float2 P1 = P;
-        int M1 = M;
-        if (k + 1 < nsteps) {
-            if (((k + 1) & 7) == 0) {
-                // first step of chunk c = (k+1)/8: wait for it, then refill the
-                // buffer of chunk c-1 (no longer read) with chunk c+1
-                cp_async_wait<0>();
-                __syncwarp();
-            }
-            fetch(k + 1, en1, X1, P1, M1);
-            if (((k + 1) & 7) == 0) issue_chunk(((k + 1) >> 3) + 1);
-        }
-        const bool valid = 4 * k + q < nent;
-        const int J = en.x & 0x7fffffff;
-        const bool nm = en.x < 0;
-        const float xs = __fadd_rn(X.x, __int_as_float(en.y));
-        const float ys = __fadd_rn(X.y, __int_as_float(en.z));
-        const float zs = __fadd_rn(X.z, __int_as_float(en.w));
-        bool pass;
-        {
-            float tx = __fsub_rn(xs, bc.x), ty = __fsub_rn(ys, bc.y), tz = __fsub_rn(zs, bc.z);
-            if (IMG) {
-                tx = img32(tx, S.Lf[0], S.invLf[0]);
-                ty = img32(ty, S.Lf[1], S.invLf[1]);
-                tz = img32(tz, S.Lf[2], S.invLf[2]);
-            }
-            const float ex = fmaxf(__fsub_rn(fabsf(tx), bh.x), 0.0f);
-            const float ey = fmaxf(__fsub_rn(fabsf(ty), bh.y), 0.0f);
-            const float ez = fmaxf(__fsub_rn(fabsf(tz), bh.z), 0.0f);
-            // padding slots carry 1e6 coordinates: they fail the box test
-            // unless image mode wraps them back, hence the explicit test there
-            pass = valid && r2_chain(ex, ey, ez) < rcl2;
-            if (IMG) pass = pass && (X.x < 1.0e5f);
-        }
-        unsigned m = base;
-        if (J == I) m &= (1u << t) - 1u;    // own cluster: i < j only (uniform per entry)
-        if (clique) {
-            // excluded <=> same molecule: compare with the 8 i ids (uniform branch)
-            if (__any_sync(0xffffffffu, pass && nm)) {
-                unsigned mm = m;
-#pragma unroll
-                for (int u = 0; u < 8; ++u) mm = (sm.im[u] == M) ? (mm & ~(1u << u)) : mm;
-                m = nm ? mm : m;
-            }
-        } else if (pass && nm) {
-            m &= j_mask(a, S, R, I, J, 8 * J + t, 0xffu, true);
-        }
-        pass = pass && m != 0u;
-        if (MODE == MODE_EMIT) {
-            const unsigned bal = __ballot_sync(0xffffffffu, pass);
-            const int pos = __popc(bal & ((1u << lane) - 1u));
-            if (pass && emit_n + pos < a.ex_cap) {
-                const size_t o = (size_t)I * a.ex_cap + emit_n + pos;
-                a.ex_slot[o] = 8 * J + t;
-                a.ex_mask[o] = (unsigned char)m;
-            }
-            emit_n += __popc(bal);
-            __syncwarp();
-        } else {
-            const float4 A4 = make_float4(xs, ys, zs, X.w);
-            const float4 B4 = make_float4(P.x, P.y, __uint_as_float(m), __int_as_float(8 * J + t));
-            if (IMG) {
-                // image mode: every tile applies its lanes' masks
-                ring_put(sm.lj, tl, pass && P.y != 0.0f, A4, B4);
-                ring_put(sm.co, tc, pass && P.y == 0.0f, A4, B4);
-            } else {
-                const bool full = m == 0xffu;
-                ring_put(sm.lj, tl, pass && full && P.y != 0.0f, A4, B4);
-                ring_put(sm.co, tc, pass && full && P.y == 0.0f, A4, B4);
-                ring_put(sm.mk, tm, pass && !full, A4, B4);
-            }
-            __syncwarp();
-            if (tl - hl >= 32u) {
-                eval_tile2<MODE, IMG, true, PME, IMG>(a, S, R, sm.lj, sm.ip, hl, 32, ic, ef, npair);
-                hl += 32u;
-            }
-            if (tc - hc >= 32u) {
-                eval_tile2<MODE, IMG, false, PME, IMG>(a, S, R, sm.co, sm.ip, hc, 32, ic, ef, npair);
-                hc += 32u;
-            }
-            if (!IMG && tm - hm >= 32u) {
-                eval_tile2<MODE, IMG, true, PME, true>(a, S, R, sm.mk, sm.ip, hm, 32, ic, ef, npair);
-                hm += 32u;
-            }
-            __syncwarp();
-        }
-        en = en1;
-        X = X1;
-        P = P1;
-        M = M1;
-    }
-    cp_async_wait<0>();
-    __syncwarp();
-    if (MODE == MODE_EMIT) {
-        if (lane == 0 && part == 0) {
-            a.ex_cnt[I] = emit_n;
-            if (emit_n > a.ex_cap) atomicOr(a.status, 1 << 16);
-        }
-        return;
-    }
-    if (tl != hl) eval_tile2<MODE, IMG, true, PME, IMG>(a, S, R, sm.lj, sm.ip, hl, (int)(tl - hl), ic, ef, npair);
-    if (tc != hc) eval_tile2<MODE, IMG, false, PME, IMG>(a, S, R, sm.co, sm.ip, hc, (int)(tc - hc), ic, ef, npair);
-    if (!IMG && tm != hm)
-        eval_tile2<MODE, IMG, true, PME, true>(a, S, R, sm.mk, sm.ip, hm, (int)(tm - hm), ic, ef, npair);
-    if (MODE == MODE_COUNT) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) npair += __shfl_xor_sync(0xffffffffu, npair, o);
-        if (lane == 0) atomicAdd((unsigned long long*)&a.counts[2 * r], (unsigned long long)npair);
-        return;
-    }
-    reduce_i_forces(a, ic, vmask, slot0);
-    double ed = (double)ef;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) ed += __shfl_xor_sync(0xffffffffu, ed, o);
-    if (lane == 0) a.e_part[(size_t)cw * a.split + part] = ed;
-}
-
-template <int MODE, int MINB, int NW, bool PME = false>
-__global__ void __launch_bounds__(NW * 32) __maxnreg__((65536 / (MINB * NW * 32)) & ~7)
-k_pair2(SdmArgs a, const int* item_prefix) {
-    extern __shared__ __align__(16) unsigned char pair_smem[];
-    Eval2Smem& sm = reinterpret_cast<Eval2Smem*>(pair_smem)[threadIdx.x >> 5];
-    const int total = item_prefix[a.nrep];
-    const int W = gridDim.x * NW;
-    for (int item = blockIdx.x * NW + (threadIdx.x >> 5); item < total; item += W) {
-        const int r = rep_by_item(item_prefix, a.nrep, item);
-        const int local = item - item_prefix[r];
-        const int I = local / a.split, part = local - I * a.split;
-        if (MODE == MODE_EMIT && r != a.ex_rep) continue;
-        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) process_cluster2<MODE, true, PME>(a, r, I, part, sm);
-        else process_cluster2<MODE, false, PME>(a, r, I, part, sm);
-    }
-}
-
 // NW warps per CTA, each with its own EvalSmem in dynamic shared memory;
 // MINB CTAs per SM fit the register file: registers per thread are capped at
 // 65536 / (MINB * NW * 32), rounded down to the allocation unit of 8
-template <int MODE, int MINB, int NW, bool PME = false>
+template <int MODE, int MINB, int NW, bool PME = false, int CH = SDM_CH_DEFAULT>
 __global__ void __launch_bounds__(NW * 32) __maxnreg__((65536 / (MINB * NW * 32)) & ~7)
 k_pair(SdmArgs a, const int* item_prefix) {
     extern __shared__ __align__(16) unsigned char pair_smem[];
-    EvalSmem& sm = reinterpret_cast<EvalSmem*>(pair_smem)[threadIdx.x >> 5];
+    EvalSmem<CH>& sm = reinterpret_cast<EvalSmem<CH>*>(pair_smem)[threadIdx.x >> 5];
     const int total = item_prefix[a.nrep];
     const int W = gridDim.x * NW;
     // static schedule: warp w takes items w, w+W, ...
@@ -1497,8 +1162,8 @@ k_pair(SdmArgs a, const int* item_prefix) {
         const int local = item - item_prefix[r];
         const int I = local / a.split, part = local - I * a.split;
         if (MODE == MODE_EMIT && r != a.ex_rep) continue;
-        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) process_cluster<MODE, true, PME>(a, r, I, part, sm);
-        else process_cluster<MODE, false, PME>(a, r, I, part, sm);
+        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) process_cluster<MODE, true, PME, CH>(a, r, I, part, sm);
+        else process_cluster<MODE, false, PME, CH>(a, r, I, part, sm);
     }
 }
 
@@ -2611,23 +2276,23 @@ cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_
 // the kernel spills).
 #define SDM_PAIR_SHAPES(X) X(4, 3) X(4, 4)
 
-template <int MODE, int MINB, int NW, bool PME = false>
+template <int MODE, int MINB, int NW, bool PME = false, int CH = SDM_CH_DEFAULT>
 static cudaError_t pair_attr() {
-    cudaError_t e = cudaFuncSetAttribute(k_pair<MODE, MINB, NW, PME>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(NW * sizeof(EvalSmem)));
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_pair2<MODE, MINB, NW, PME>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(NW * sizeof(Eval2Smem)));
-    return e;
+    return cudaFuncSetAttribute(k_pair<MODE, MINB, NW, PME, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(NW * sizeof(EvalSmem<CH>)));
 }
 
 // Raises the dynamic shared memory limit of every pair-kernel shape on the
 // current device (called once per handle, outside any stream capture).
 cudaError_t sdm_pair_prepare() {
     cudaError_t e = cudaSuccess;
-#define SDM_ATTR(NW, MB) \
-    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW>(); \
-    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW, true>();
+#define SDM_ATTR(NW, MB)                                                                   \
+    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW, false, 8>();                    \
+    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW, false, 12>();                   \
+    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW, false, 16>();                   \
+    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW, true, 8>();                     \
+    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW, true, 12>();                    \
+    if (e == cudaSuccess) e = pair_attr<MODE_EVAL, MB, NW, true, 16>();
     SDM_PAIR_SHAPES(SDM_ATTR)
 #undef SDM_ATTR
     if (e == cudaSuccess) e = pair_attr<MODE_COUNT, 3, 4>();
@@ -2647,21 +2312,27 @@ static int pair_minb(int ctas_per_sm) {
 }
 
 // CTAs of pair-kernel shape (NW, MB) the occupancy calculator places on one SM
-template <int MODE, int MINB, int NW>
-static int pair_resident(int variant) {
+template <int MODE, int MINB, int NW, int CH>
+static int pair_resident() {
     int n = 0;
-    const cudaError_t e = variant == 1
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pair2<MODE, MINB, NW>, NW * 32, NW * sizeof(Eval2Smem))
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pair<MODE, MINB, NW>, NW * 32, NW * sizeof(EvalSmem));
-    return e == cudaSuccess ? n : 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pair<MODE, MINB, NW, false, CH>, NW * 32,
+                                                      NW * sizeof(EvalSmem<CH>)) != cudaSuccess)
+        return 0;
+    return n;
 }
 
-// CTAs per SM that are resident when ctas_per_sm are requested (current device);
-// 0 when no pair kernel is built for the request
-int sdm_pair_resident(int ctas_per_sm, int variant) {
+// CTAs per SM that are resident when ctas_per_sm are requested with a staging
+// chunk of `chunk` list entries (current device); 0 when no pair kernel is
+// built for the request
+int sdm_pair_resident(int ctas_per_sm, int chunk) {
     const int mb = pair_minb(ctas_per_sm);
-#define SDM_RES(NW, MB) \
-    if (mb == MB) return std::min(ctas_per_sm, pair_resident<MODE_EVAL, MB, NW>(variant));
+#define SDM_RES(NW, MB)                                                                         \
+    if (mb == MB) {                                                                             \
+        const int n = chunk == 8 ? pair_resident<MODE_EVAL, MB, NW, 8>()                        \
+                      : chunk == 16 ? pair_resident<MODE_EVAL, MB, NW, 16>()                    \
+                                    : pair_resident<MODE_EVAL, MB, NW, 12>();                   \
+        return std::min(ctas_per_sm, n);                                                        \
+    }
     SDM_PAIR_SHAPES(SDM_RES)
 #undef SDM_RES
     return 0;
@@ -2669,32 +2340,32 @@ int sdm_pair_resident(int ctas_per_sm, int variant) {
 
 // resident = CTAs per SM that fit (sdm_pair_resident): the persistent static
 // schedule covers every item with any grid, so the grid never exceeds one wave
+template <int MB, int NW, int CH>
+static void launch_pair_eval(const SdmArgs& a, const int* item_prefix, int grid, bool pme, cudaStream_t st) {
+    const size_t smem = NW * sizeof(EvalSmem<CH>);
+    if (pme) k_pair<MODE_EVAL, MB, NW, true, CH><<<grid, NW * 32, smem, st>>>(a, item_prefix);
+    else k_pair<MODE_EVAL, MB, NW, false, CH><<<grid, NW * 32, smem, st>>>(a, item_prefix);
+}
+
 cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, int ctas_per_sm,
-                            int resident, bool pme, int variant, cudaStream_t st) {
+                            int resident, bool pme, int chunk, cudaStream_t st) {
     const int grid = num_sms() * std::max(1, std::min(ctas_per_sm, resident));
-    const size_t sm1 = sizeof(EvalSmem), sm2 = sizeof(Eval2Smem);
     if (mode == MODE_EVAL) {
         const int mb = pair_minb(ctas_per_sm);
-#define SDM_GO(NW, MB)                                                                                         \
-        if (mb == MB) {                                                                                     \
-            if (variant == 1) {                                                                             \
-                if (pme) k_pair2<MODE_EVAL, MB, NW, true><<<grid, NW * 32, NW * sm2, st>>>(a, item_prefix); \
-                else k_pair2<MODE_EVAL, MB, NW><<<grid, NW * 32, NW * sm2, st>>>(a, item_prefix);          \
-            } else {                                                                                        \
-                if (pme) k_pair<MODE_EVAL, MB, NW, true><<<grid, NW * 32, NW * sm1, st>>>(a, item_prefix);  \
-                else k_pair<MODE_EVAL, MB, NW><<<grid, NW * 32, NW * sm1, st>>>(a, item_prefix);           \
-            }                                                                                               \
-            return cudaGetLastError();                                                                      \
+#define SDM_GO(NW, MB)                                                                    \
+        if (mb == MB) {                                                                \
+            if (chunk == 8) launch_pair_eval<MB, NW, 8>(a, item_prefix, grid, pme, st);  \
+            else if (chunk == 16) launch_pair_eval<MB, NW, 16>(a, item_prefix, grid, pme, st); \
+            else launch_pair_eval<MB, NW, 12>(a, item_prefix, grid, pme, st);            \
+            return cudaGetLastError();                                                 \
         }
         SDM_PAIR_SHAPES(SDM_GO)
 #undef SDM_GO
         return cudaErrorInvalidValue;
     } else if (mode == MODE_COUNT) {
-        if (variant == 1) k_pair2<MODE_COUNT, 3, 4><<<num_sms() * 3, 4 * 32, 4 * sm2, st>>>(a, item_prefix);
-        else k_pair<MODE_COUNT, 3, 4><<<num_sms() * 3, 4 * 32, 4 * sm1, st>>>(a, item_prefix);
+        k_pair<MODE_COUNT, 3, 4><<<num_sms() * 3, 4 * 32, 4 * sizeof(EvalSmem<SDM_CH_DEFAULT>), st>>>(a, item_prefix);
     } else {
-        if (variant == 1) k_pair2<MODE_EMIT, 3, 4><<<num_sms() * 3, 4 * 32, 4 * sm2, st>>>(a, item_prefix);
-        else k_pair<MODE_EMIT, 3, 4><<<num_sms() * 3, 4 * 32, 4 * sm1, st>>>(a, item_prefix);
+        k_pair<MODE_EMIT, 3, 4><<<num_sms() * 3, 4 * 32, 4 * sizeof(EvalSmem<SDM_CH_DEFAULT>), st>>>(a, item_prefix);
     }
     return cudaGetLastError();
 }

@@ -1,7 +1,7 @@
 """Runs a fixed synthetic SDM workload a few times (for profilers).
 
   python -m openmm_sdm_plugin_gb300.profile_workload [--replicas 22] [--calls 3] [--eager] [--pme]
-      [--variant 0|1] [--ctas 3|4]
+      [--chunk 8|12|16] [--ctas 3|4]
 
 The workload is the batched relative-binding system used by the benchmark:
 `--replicas` copies of the 22,580-particle system with independent seeded
@@ -26,7 +26,7 @@ def main():
     ap.add_argument("--eager", action="store_true", help="no CUDA graph")
     ap.add_argument("--config", default="config2", choices=["config2", "config0"])
     ap.add_argument("--pme", action="store_true", help="PME electrostatics instead of reaction field")
-    ap.add_argument("--variant", type=int, default=None, help="main-pass implementation (SDM_OPT_PAIR_VARIANT)")
+    ap.add_argument("--chunk", type=int, default=None, help="list entries per staged chunk (SDM_OPT_STAGE_CHUNK)")
     ap.add_argument("--ctas", type=int, default=None, help="pair-kernel CTAs per SM")
     a = ap.parse_args()
     _build.build()
@@ -39,8 +39,8 @@ def main():
         h.set_params(r, s.params[r].as_array())
     if a.eager:
         h.set_option(capi.OPT_GRAPH, 0)
-    if a.variant is not None:
-        h.set_option(capi.OPT_PAIR_VARIANT, a.variant)
+    if a.chunk is not None:
+        h.set_option(capi.OPT_STAGE_CHUNK, a.chunk)
     if a.ctas is not None:
         h.set_option(capi.OPT_CTAS_PER_SM, a.ctas)
     x = torch.from_numpy(np.ascontiguousarray(s.positions.reshape(-1, 3))).cuda()

@@ -126,3 +126,24 @@ def test_descriptor_errors_are_reported_before_any_device_query(built_lib):
             capi.Handle([s, bad])
         assert e.value.status == capi.SDM_ERR_INVALID_ARGUMENT, (msg, e.value)
         assert "system 1" in str(e.value) and msg in str(e.value), str(e.value)
+
+
+def test_tune_key_names_the_workload(built_lib):
+    """The autotuner's cache key: mean particles per replica, density,
+    cutoff, replicas, systems, electrostatics, SM count; the coordinates do
+    not enter it.  Computed on the host (no device)."""
+    import dataclasses
+    from openmm_sdm_plugin_gb300 import capi, systems
+    s = systems.config2(nrep=3)
+    k = capi.tune_key([s], 152)
+    rho = s.n / float(np.prod(s.box))
+    assert k == (f"sdm-tune-v1 n={s.n} rho={rho:.1f} rc={s.cutoff:.3f} replicas=3 systems=1 "
+                 f"method=rf sms=152"), k
+    moved = dataclasses.replace(s, positions=s.positions + 0.01)
+    assert capi.tune_key([moved], 152) == k
+    assert capi.tune_key([s], 148) != k
+    assert capi.tune_key([systems.config2(nrep=2)], 152) != k
+    assert capi.tune_key([dataclasses.replace(s, nonbonded_method="pme")], 152) != k
+    assert capi.tune_key([dataclasses.replace(s, cutoff=1.1)], 152) != k
+    two = capi.tune_key([s, systems.config0(variant="b")], 152)
+    assert "systems=2" in two and "replicas=4" in two
