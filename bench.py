@@ -37,16 +37,17 @@ METRIC = "SDM lambda-state force evals/s at 23k atoms x 22 lambda, batched vs pl
 UNIT = "lambda-state evals/s"
 FLOP_PER_PAIR = 52  # FP32 flops per pair per state (FMA = 2, rsqrt = 1)
 # kernels of one batched evaluation: k_cells k_scan k_bucket k_cellsort k_clusters
-# k_jlist k_pair k_pert_prep k_perturb k_finalize k_mix
-KERNELS_PER_STEP = 11
+# k_jlist k_pair k_pert_prep k_perturb k_finalize_mix
+KERNELS_PER_STEP = 10
 NREP = 22
 WORKLOAD = ("config2: 22 replicas x 22,580 particles (7,500 waters + 2x40 ligand), 6.2 nm box, "
             "rc 1.0 nm reaction field, one batched call per step")
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_pair launch on this
-# workload: a stored figure from the ncu capture summarised in
-# profiles/k_pair_config2x22.md (cold cache between replay passes)
-K_PAIR_DRAM_BYTES_PER_LAUNCH = 122.466560e6 + 6.279680e6
-K_PAIR_TRAFFIC_SOURCE = "stored: ncu capture of the same workload (profiles/k_pair_config2x22.md)"
+# workload: a stored figure, the 4-replica ncu capture summarised in
+# profiles/k_pair_config2x4.md scaled by 22/4 (cold cache between replay passes)
+K_PAIR_DRAM_BYTES_PER_LAUNCH = (22.318336e6 + 0.0) * 22 / 4
+K_PAIR_TRAFFIC_SOURCE = ("stored: ncu capture of 4 replicas of the same workload x 22/4 "
+                         "(profiles/k_pair_config2x4.md)")
 
 
 def _peaks():
@@ -215,7 +216,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the library's default schedule instead of the autotuner's choice")
+    ap.add_argument("--tune-cache", default=None,
+                    help="autotuner cache file (default: sdm_tune_cache.txt in the system temp directory)")
     ap.add_argument("--ctas", type=int, default=0, help="pair-kernel CTAs per SM (0 = library default)")
     ap.add_argument("--split", type=int, default=0, help="work items per i-cluster (0 = default)")
     args = ap.parse_args()
@@ -267,8 +271,14 @@ def main():
         if args.split:
             hh.set_option(capi.OPT_SPLIT, args.split)
     tuned = None
-    if args.autotune:
-        tuned = h.autotune(xd.data_ptr())
+    if not args.no_autotune and not (args.ctas or args.split):
+        import tempfile
+        cache = args.tune_cache or os.path.join(tempfile.gettempdir(), "sdm_tune_cache.txt")
+        # the lists are sized by a first evaluation, then every schedule is timed
+        h.evaluate_device(xd.data_ptr(), rd.data_ptr(), fd.data_ptr(), sptr)
+        torch.cuda.synchronize()
+        h.check_status()
+        tuned = h.autotune(xd.data_ptr(), cache)
     l2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
 
     def flush():
@@ -286,6 +296,12 @@ def main():
     x1 = xd[:n].contiguous()
     r1 = torch.zeros((1, capi.NRESULTS), dtype=torch.float64, device=dev)
     f1 = torch.zeros_like(x1)
+    tuned1 = None
+    if tuned is not None:
+        h1.evaluate_device(x1.data_ptr(), r1.data_ptr(), f1.data_ptr(), sptr)
+        torch.cuda.synchronize()
+        h1.check_status()
+        tuned1 = h1.autotune(x1.data_ptr(), cache)
 
     def timed(fn, steps, warmup, per_kernel=None, pre=None):
         for _ in range(warmup):
@@ -449,6 +465,12 @@ def main():
     x3 = torch.from_numpy(x3h).to(dev)
     r3 = torch.zeros((h3.nrep, capi.NRESULTS), dtype=torch.float64, device=dev)
     f3 = torch.zeros_like(x3)
+    tuned3 = None
+    if tuned is not None:
+        h3.evaluate_device(x3.data_ptr(), r3.data_ptr(), f3.data_ptr(), sptr)
+        torch.cuda.synchronize()
+        h3.check_status()
+        tuned3 = h3.autotune(x3.data_ptr(), cache)
     h3.set_option(capi.OPT_PROFILE, 2)
     n3 = min(args.steps, 20)
     ms3, pk3 = timed(lambda: h3.evaluate_device(x3.data_ptr(), r3.data_ptr(), f3.data_ptr(), sptr), n3, warm,
@@ -459,7 +481,7 @@ def main():
     config3 = {"value": whole_job_rate(h3.nrep * n3, world, tot3), "unit": UNIT, "ms_per_call": sum(ms3) / n3,
                "steps": n3, "device_status": h3.check_status(), "replicas": h3.nrep,
                "particles": int(sum(sy.n * sy.replicas for sy in s3)),
-               "pair_kernel_ms": pair3, "pair_frac": None,
+               "pair_kernel_ms": pair3, "pair_frac": None, "tuning": tuned3,
                "flop_per_launch": flop3,
                "workload": "config3: 64 host-guest systems (2,010-54,820 particles, log-uniform, seed 3) x 16 "
                            "lambda states, every replica its own coordinates, one batched call per step"}
@@ -570,7 +592,7 @@ def main():
 
     h2d = xh.nbytes
     d2h = xh.nbytes + NREP * capi.NRESULTS * 8
-    plain_obj = {"value": plain, "unit": UNIT, "ms_per_call": sum(ms_p) / len(ms_p),
+    plain_obj = {"value": plain, "unit": UNIT, "ms_per_call": sum(ms_p) / len(ms_p), "tuning": tuned1,
                  "workload": "config1: one 22,580-particle replica per call (CUDA graph)"}
     # secondary fields first, the headline keys last (a reader of the line's
     # tail sees value, e2e, roofline, plain and batched_over_plain)
@@ -596,7 +618,8 @@ def main():
                    "schedule": {"split": h.get_option(capi.OPT_SPLIT), "ctas_per_sm": h.get_option(capi.OPT_CTAS_PER_SM),
                                 "ctas_resident": h.get_option(capi.OPT_PAIR_RESIDENT),
                                 "stage_chunk": h.get_option(capi.OPT_STAGE_CHUNK),
-                                "autotuned": tuned is not None}},
+                                "autotuned": tuned is not None,
+                                "tuning": tuned}},
         "gpu_launches": KERNELS_PER_STEP * args.steps,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": sum(e2e_ms) / len(e2e_ms),

@@ -1045,6 +1045,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.jl_cnt = at<int>(B, o_jc);
     h->done = at<int>(B, o_done);
     a.total_atoms = (int)A;
+    a.max_rep_atoms = 0;
+    for (auto& r : h->rep) a.max_rep_atoms = std::max(a.max_rep_atoms, r.n);
     a.total_cols = (int)Ccol;
     a.total_cells = (int)Ccel;
     a.pme_charge = a.topo_q;

@@ -1889,9 +1889,10 @@ __device__ double softcore(double u, int method, double umax, double a, double u
     return (umax - ub) * (za - 1.0) / (za + 1.0) + ub;
 }
 
-__global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
-    __shared__ double red[256];
-    const int r = blockIdx.x;
+// energies of replica r (fixed-order block reductions) and the combine; thread
+// 0 leaves the mixing weight in *s_out and, when `write`, the results, the
+// weight for the Langevin step and the status bits
+__device__ void finalize_replica(const SdmArgs& a, int r, double* red, double* s_out, bool write) {
     const SdmRep& R = a.rep[r];
     const SdmSys& S = a.sys[R.sys];
     const int ncl = a.ncl[r];
@@ -1971,6 +1972,8 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
         dwdl = (-lee / alpha) * p[SDM_P_M_LAMBDA1] + (be + lee / alpha) * p[SDM_P_M_LAMBDA2] +
                ((dl2 - dl1) * ex / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
     }
+    *s_out = bfp * fp;
+    if (!write) return;
     int st = *(volatile int*)a.status;
     if (!isfinite(U0) || !isfinite(u)) { st |= SDM_DEV_ENERGY_NONFINITE; atomicOr(a.status, SDM_DEV_ENERGY_NONFINITE); }
     double* o = a.results + (size_t)r * SDM_NRESULTS;
@@ -1991,6 +1994,12 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
     o[SDM_R_W0PARAM] = w0;
     o[SDM_R_STATUS] = (double)st;
     o[SDM_R_RESERVED] = (double)ncl;
+}
+
+__global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
+    __shared__ double red[256];
+    __shared__ double s;
+    finalize_replica(a, blockIdx.x, red, &s, true);
 }
 
 // ------------------------------------------------------------------------- //
@@ -2018,6 +2027,38 @@ __global__ void k_mix(SdmArgs a) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             if (a.forces) a.forces[o + k] = __fma_rn(s, df[k], f0[k]);
+            if (a.F0out) a.F0out[o + k] = f0[k];
+            if (a.F1out) a.F1out[o + k] = f0[k] + df[k];
+        }
+    }
+}
+
+// Finalize and mix in one launch (the evaluation without a Langevin step):
+// blockIdx.y = replica, blockIdx.x = a slice of kMixSlice particles.  Every
+// block of a replica repeats the replica's energy reductions and combine (the
+// same fixed order, so the same bits), block 0 writes the results, and each
+// block mixes its slice with the weight it computed: no second launch waits
+// for the weights.
+constexpr int kMixSlice = 2048;
+__global__ void __launch_bounds__(256) k_finalize_mix(SdmArgs a) {
+    __shared__ double red[256];
+    __shared__ double s;
+    const int r = blockIdx.y;
+    const SdmRep& R = a.rep[r];
+    const int i0 = blockIdx.x * kMixSlice;
+    if (blockIdx.x > 0 && i0 >= R.n) return;   // uniform per block
+    finalize_replica(a, r, red, &s, blockIdx.x == 0);
+    __syncthreads();
+    const double sw = a.forces ? s : 0.0;
+    const int i1 = min(R.n, i0 + kMixSlice);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const size_t gsl = (size_t)R.slot_win + a.inv[R.atom_win + i];
+        const double f0[3] = {fix_to_double(a.F0x[gsl]), fix_to_double(a.F0y[gsl]), fix_to_double(a.F0z[gsl])};
+        const double df[3] = {fix_to_double(a.dFx[gsl]), fix_to_double(a.dFy[gsl]), fix_to_double(a.dFz[gsl])};
+        const size_t o = 3 * (size_t)(R.x_off + i);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (a.forces) a.forces[o + k] = __fma_rn(sw, df[k], f0[k]);
             if (a.F0out) a.F0out[o + k] = f0[k];
             if (a.F1out) a.F1out[o + k] = f0[k] + df[k];
         }
@@ -2453,13 +2494,13 @@ cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st) {
 }
 
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st) {
-    k_finalize<<<a.nrep, 256, 0, st>>>(a);
     if (a.lv_x) {   // Langevin step: the mixed force feeds the update directly
+        k_finalize<<<a.nrep, 256, 0, st>>>(a);
         k_langevin<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
         if (a.st_any) k_settle<<<dim3((a.st_max + 127) / 128, a.nrep), 128, 0, st>>>(a);
         k_lv_tick<<<1, 1, 0, st>>>(a.lv_prm);
     } else {
-        k_mix<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
+        k_finalize_mix<<<dim3((a.max_rep_atoms + kMixSlice - 1) / kMixSlice, a.nrep), 256, 0, st>>>(a);
     }
     return cudaGetLastError();
 }

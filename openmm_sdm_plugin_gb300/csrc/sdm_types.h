@@ -258,6 +258,7 @@ struct SdmArgs {
     int ex_rep;
     // totals
     int total_atoms;     // sum of n over replicas
+    int max_rep_atoms;   // largest n of a replica
     int total_cols;      // sum of ncol over replicas
     int total_cells;     // sum of ncol*M[2]+1 over replicas
     int total_slots;     // sum of slot_cap over replicas
