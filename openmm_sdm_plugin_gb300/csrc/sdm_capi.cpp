@@ -21,9 +21,9 @@
 #include "../../include/sdm_capi.h"
 #include "sdm_types.h"
 
-cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* cl_prefix, int* done, cudaStream_t st,
+cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* grp_prefix, int* done, cudaStream_t st,
                             cudaEvent_t* ev, int nev, unsigned ev_flags);
-cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_t st);
+cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* grp_prefix, cudaStream_t st);
 cudaError_t sdm_pair_prepare();
 #define SDM_MAX_CTAS 4  // pair-kernel CTAs per SM with a built register bound
 int sdm_pair_resident(int ctas_per_sm, int chunk);
@@ -133,7 +133,7 @@ struct sdm_handle {
     cudaStream_t stream = nullptr;
     SdmArgs args{};
     int* item_prefix = nullptr;
-    int* cl_prefix = nullptr;
+    int* grp_prefix = nullptr;   // list-building groups over replicas (k_jlist items)
     int* done = nullptr;
     // cluster-pair lists (own allocation: regrown on overflow)
     int4* jl_buf = nullptr;
@@ -647,8 +647,8 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     const unsigned fl = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     SDM_CUDA(h, cudaMemsetAsync(h->counters, 0, h->counters_bytes, st));
     cudaEvent_t* ev = profile ? h->ev : nullptr;
-    SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->cl_prefix, h->done, st, ev, 6, fl));
-    SDM_CUDA(h, sdm_launch_jlist(a, h->cl_prefix, st));
+    SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->grp_prefix, h->done, st, ev, 6, fl));
+    SDM_CUDA(h, sdm_launch_jlist(a, h->grp_prefix, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[6], st, fl));
     SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[chunk_index(h->opt_chunk)][h->opt_ctas],
                                 h->pme, h->opt_chunk, st));
@@ -961,6 +961,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_counts = ar.take<long long>(2 * nrep), o_ip = ar.take<int>(nrep + 1);
     const size_t o_cp = ar.take<int>(nrep + 1), o_jc = ar.take<int>(Cl);
     const size_t o_done = ar.take<int>(4);
+    const size_t o_ngrp = ar.take<int>(nrep), o_lgrp = ar.take<int2>(Cl);
     h->arena_bytes = ar.off + 256;
     cudaError_t ce = cudaMalloc(&h->arena, h->arena_bytes);
     if (ce != cudaSuccess) { h->arena = nullptr; cuda_fail(h, ce, "cudaMalloc(arena)"); return bail(SDM_ERR_CUDA); }
@@ -1038,10 +1039,12 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.pert_pos = at<SdmPertPos>(B, o_ppos);
     a.adj = at<double>(B, o_adj);
     a.ncl = at<int>(B, o_ncl);
+    a.ngrp = at<int>(B, o_ngrp);
+    a.cl_grp = at<int2>(B, o_lgrp);
     a.status = at<int>(B, o_st);
     a.counts = at<long long>(B, o_counts);
     h->item_prefix = at<int>(B, o_ip);
-    h->cl_prefix = at<int>(B, o_cp);
+    h->grp_prefix = at<int>(B, o_cp);
     a.jl_cnt = at<int>(B, o_jc);
     h->done = at<int>(B, o_done);
     a.total_atoms = (int)A;

@@ -208,18 +208,23 @@ __global__ void k_cells(SdmArgs a) {
 // ------------------------------------------------------------------------- //
 // K2: column prefix sums; the last block builds the work-item prefix        //
 // ------------------------------------------------------------------------- //
-__device__ __forceinline__ int2 warp_incl_scan2(int2 v) {
+__device__ __forceinline__ int4 warp_incl_scan3(int4 v) {
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int x = __shfl_up_sync(0xffffffffu, v.x, o);
-        int y = __shfl_up_sync(0xffffffffu, v.y, o);
-        if (lane_id() >= o) { v.x += x; v.y += y; }
+        const int x = __shfl_up_sync(0xffffffffu, v.x, o);
+        const int y = __shfl_up_sync(0xffffffffu, v.y, o);
+        const int z = __shfl_up_sync(0xffffffffu, v.z, o);
+        if (lane_id() >= o) { v.x += x; v.y += y; v.z += z; }
     }
     return v;
 }
 
-__global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int* cl_prefix, int* done) {
-    __shared__ int2 wsum[32];
+// Column prefixes of particles, clusters and list-building groups (SDM_JG
+// z-consecutive clusters of one column); the group table (first cluster,
+// clusters) of every group.  The last block builds the work-item prefix of
+// the main pass and the group prefix of the list builder over replicas.
+__global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int* grp_prefix, int* done) {
+    __shared__ int4 wsum[32];
     __shared__ int last;
     const int r = blockIdx.x;
     const SdmRep& R = a.rep[r];
@@ -230,44 +235,50 @@ __global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int*
     int* cnt = a.col_cnt + R.col_win;
     int* aoff = a.col_aoff + R.col_win;
     int* cl = a.col_cl + R.col_win;
+    int2* grp = a.cl_grp + R.cl_win;
     const int per = (ncol + blockDim.x - 1) / blockDim.x;
     const int beg = min(ncol, (int)threadIdx.x * per);
     const int end = min(ncol, beg + per);
-    int2 s = make_int2(0, 0);
+    int4 s = make_int4(0, 0, 0, 0);
     for (int c = beg; c < end; ++c) {
         int n = 0;
         for (int z = 0; z < mz; ++z) n += ccnt[c * mz + z];
         cnt[c] = n;
+        const int nc = (n + 7) >> 3;
         s.x += n;
-        s.y += (n + 7) >> 3;
+        s.y += nc;
+        s.z += (nc + SDM_JG - 1) / SDM_JG;
     }
-    int2 inc = warp_incl_scan2(s);
+    int4 inc = warp_incl_scan3(s);
     const int wid = threadIdx.x >> 5;
     if (lane_id() == 31) wsum[wid] = inc;
     __syncthreads();
     if (wid == 0) {
-        int2 v = (lane_id() < (int)(blockDim.x >> 5)) ? wsum[lane_id()] : make_int2(0, 0);
-        v = warp_incl_scan2(v);
+        int4 v = (lane_id() < (int)(blockDim.x >> 5)) ? wsum[lane_id()] : make_int4(0, 0, 0, 0);
+        v = warp_incl_scan3(v);
         wsum[lane_id()] = v;
     }
     __syncthreads();
-    int2 base = make_int2(inc.x - s.x, inc.y - s.y);
-    if (wid > 0) { base.x += wsum[wid - 1].x; base.y += wsum[wid - 1].y; }
+    int4 base = make_int4(inc.x - s.x, inc.y - s.y, inc.z - s.z, 0);
+    if (wid > 0) { base.x += wsum[wid - 1].x; base.y += wsum[wid - 1].y; base.z += wsum[wid - 1].z; }
     for (int c = beg; c < end; ++c) {
         aoff[c] = base.x;
         cl[c] = base.y;
         int o = base.x;
         for (int z = 0; z < mz; ++z) { coff[c * mz + z] = o; o += ccnt[c * mz + z]; }
+        const int nc = (cnt[c] + 7) >> 3;
+        for (int k = 0; k < nc; k += SDM_JG) grp[base.z++] = make_int2(base.y + k, min(SDM_JG, nc - k));
         base.x += cnt[c];
-        base.y += (cnt[c] + 7) >> 3;
+        base.y += nc;
     }
     if (threadIdx.x == blockDim.x - 1) {
         aoff[ncol] = base.x;
         cl[ncol] = base.y;
         coff[ncol * mz] = base.x;
         a.ncl[r] = base.y;
+        a.ngrp[r] = base.z;
     }
-    // last block computes the item prefix over replicas (no waiting involved)
+    // last block computes the prefixes over replicas (no waiting involved)
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last = (atomicAdd(done, 1) == (int)gridDim.x - 1);
@@ -279,25 +290,30 @@ __global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int*
         const int per2 = (nrep + blockDim.x - 1) / blockDim.x;
         const int b2 = min(nrep, (int)threadIdx.x * per2);
         const int e2 = min(nrep, b2 + per2);
-        int2 t = make_int2(0, 0);
-        for (int q = b2; q < e2; ++q) t.x += ((volatile int*)a.ncl)[q] * a.split;
-        int2 inc2 = warp_incl_scan2(t);
+        int4 t = make_int4(0, 0, 0, 0);
+        for (int q = b2; q < e2; ++q) {
+            t.x += ((volatile int*)a.ncl)[q] * a.split;
+            t.y += ((volatile int*)a.ngrp)[q];
+        }
+        int4 inc2 = warp_incl_scan3(t);
         __syncthreads();
         if (lane_id() == 31) wsum[wid] = inc2;
         __syncthreads();
         if (wid == 0) {
-            int2 v = (lane_id() < (int)(blockDim.x >> 5)) ? wsum[lane_id()] : make_int2(0, 0);
-            v = warp_incl_scan2(v);
+            int4 v = (lane_id() < (int)(blockDim.x >> 5)) ? wsum[lane_id()] : make_int4(0, 0, 0, 0);
+            v = warp_incl_scan3(v);
             wsum[lane_id()] = v;
         }
         __syncthreads();
         int b = inc2.x - t.x + (wid > 0 ? wsum[wid - 1].x : 0);
+        int bg = inc2.y - t.y + (wid > 0 ? wsum[wid - 1].y : 0);
         for (int q = b2; q < e2; ++q) {
             item_prefix[q] = b;
-            cl_prefix[q] = b / a.split;
+            grp_prefix[q] = bg;
             b += ((volatile int*)a.ncl)[q] * a.split;
+            bg += ((volatile int*)a.ngrp)[q];
         }
-        if (threadIdx.x == blockDim.x - 1) { item_prefix[nrep] = b; cl_prefix[nrep] = b / a.split; }
+        if (threadIdx.x == blockDim.x - 1) { item_prefix[nrep] = b; grp_prefix[nrep] = bg; }
         if (threadIdx.x == 0) *done = 0;
     }
 }
@@ -605,18 +621,36 @@ __device__ __forceinline__ int upper_zlo(const float2* zb, int lo, int hi, float
     return lo;
 }
 
+// Per-warp scratch of the list builder: candidate ranges of one stencil round
+// and the group's clusters (box centre with the reference z cell in w, half
+// extents, exclusion-linked clusters).
+struct JlSmem {
+    int4 rng[64];               // (Jbegin | own column << 31, prefix, Sx bits, Sy bits)
+    float4 bc[SDM_JG];
+    float4 bh[SDM_JG];
+    int4 lk[SDM_JG][2];
+};
+
+// The lists of the nI <= SDM_JG z-consecutive clusters I0.. of one column.
+// The column searches run once over the union of the members' z windows and
+// each candidate's box is loaded once; every member then applies its own
+// box test (the rule of a list built for that cluster alone) and appends to
+// its own list in candidate order.
 template <bool IMG>
-__device__ void build_jlist(const SdmArgs& a, int r, int I, int4* rng) {
+__device__ void build_jlist(const SdmArgs& a, int r, int g, JlSmem& js) {
     const int lane = lane_id();
     const SdmRep R = a.rep[r];
     const SdmSys S = a.sys[R.sys];
-    const int cw = R.cl_win + I;
-    const float4 bc = a.cl_bbc[cw];
-    const float4 bh = a.cl_bbh[cw];
-    const int4 ref = a.cl_ref[cw];
-    // clusters sharing an exclusion with I: the relation is symmetric, so I's
-    // own (complete unless -2) partner list decides every candidate J
-    const int4 lkA = a.cl_link[2 * (size_t)cw], lkB = a.cl_link[2 * (size_t)cw + 1];
+    const int2 gi = a.cl_grp[R.cl_win + g];
+    const int I0 = gi.x, nI = gi.y;
+    const int cw0 = R.cl_win + I0;
+    const int4 ref = a.cl_ref[cw0];   // column (x, y, id): the same for every member
+    if (lane < nI) {
+        js.bc[lane] = a.cl_bbc[cw0 + lane];
+        js.bh[lane] = a.cl_bbh[cw0 + lane];
+    }
+    if (lane < 2 * nI) js.lk[lane >> 1][lane & 1] = a.cl_link[2 * (size_t)cw0 + lane];
+    __syncwarp();
     const float rclc = S.rcl + 2.0e-4f;
     const float rclc2 = rclc * rclc;
     const float* tabx = a.shift_tab + S.shift_base;
@@ -624,40 +658,48 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I, int4* rng) {
     const float* tabz = taby + 2 * S.M[1] + 1;
     const int* colcl = a.col_cl + R.col_win;
     const float2* zb = a.cl_zb + R.cl_win;
-    // z window of I (absolute, conservative) and its pieces inside [0, Lz)
-    const float z0 = tabz[ref.z + S.M[2]] + bc.z;
-    const float ZA = z0 - bh.z - rclc - 1.0e-4f, ZB = z0 + bh.z + rclc + 1.0e-4f;
+    // union over the members: z window (absolute, conservative) and xy box
+    float ZA = 3.0e38f, ZB = -3.0e38f, ulx = 3.0e38f, uhx = -3.0e38f, uly = 3.0e38f, uhy = -3.0e38f;
+    for (int b = 0; b < nI; ++b) {
+        const float4 bc = js.bc[b], bh = js.bh[b];
+        const float z0 = tabz[__float_as_int(bc.w) + S.M[2]] + bc.z;
+        ZA = fminf(ZA, z0 - bh.z - rclc - 1.0e-4f);
+        ZB = fmaxf(ZB, z0 + bh.z + rclc + 1.0e-4f);
+        ulx = fminf(ulx, bc.x - bh.x); uhx = fmaxf(uhx, bc.x + bh.x);
+        uly = fminf(uly, bc.y - bh.y); uhy = fmaxf(uhy, bc.y + bh.y);
+    }
     const float Lz = S.Lf[2];
     const bool wholez = IMG || (ZB - ZA >= Lz);
     float za1 = fmaxf(ZA, 0.0f), zb1 = fminf(ZB, Lz), za2 = 1.0f, zb2 = 0.0f;  // empty 2nd piece
     if (ZA < 0.0f) { za2 = ZA + Lz; zb2 = Lz; }
     else if (ZB > Lz) { za2 = 0.0f; zb2 = ZB - Lz; }
-    int4* out = a.jl + (size_t)cw * a.jl_cap;
-    int cnt = 0;
+    int mycnt = 0;   // lane b < nI: entries of member b so far
     for (int k0 = 0; k0 < S.hst_count; k0 += 32) {
         const int k = k0 + lane;
         int jb1 = 0, c1 = 0, jb2 = 0, c2 = 0;
         float Sx = 0.f, Sy = 0.f;
+        bool own = false;
         if (k < S.hst_count) {
             const int2 off = a.stencil[S.hst_base + k];
             const int ccx = wrap_add(ref.x, off.x, S.M[0]);
             const int ccy = wrap_add(ref.y, off.y, S.M[1]);
             const int colid = ccx * S.M[1] + ccy;
+            own = colid == ref.w;
             bool ok = S.half_geo ? true : (colid >= ref.w);
             Sx = tabx[wrap_cell(ccx - ref.x, S.M[0]) + S.M[0]];
             Sy = taby[wrap_cell(ccy - ref.y, S.M[1]) + S.M[1]];
             if (!IMG && ok) {
-                // conservative xy gap between the i box and the column's slab
+                // conservative xy gap between the members' union box and the column's slab
                 const float lox = Sx - 1.0e-4f, hix = Sx + S.gf[0] + 1.0e-4f;
                 const float loy = Sy - 1.0e-4f, hiy = Sy + S.gf[1] + 1.0e-4f;
-                const float gx = fmaxf(0.0f, fmaxf(lox - (bc.x + bh.x), (bc.x - bh.x) - hix));
-                const float gy = fmaxf(0.0f, fmaxf(loy - (bc.y + bh.y), (bc.y - bh.y) - hiy));
+                const float gx = fmaxf(0.0f, fmaxf(lox - uhx, ulx - hix));
+                const float gy = fmaxf(0.0f, fmaxf(loy - uhy, uly - hiy));
                 ok = gx * gx + gy * gy < rclc2;
             }
             if (ok) {
                 int lo = colcl[colid];
                 const int hi = colcl[colid + 1];
-                if (colid == ref.w) lo = I;  // own column: clusters J >= I only
+                if (own) lo = I0;  // own column: clusters J >= I0 (each member: J >= its own index)
                 if (wholez) {
                     jb1 = lo;
                     c1 = hi - lo;
@@ -679,7 +721,7 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I, int4* rng) {
             }
         }
         // the columns' candidate ranges (up to two per lane) in lane order, then
-        // the candidates flattened over all lanes: every lane tests one per round
+        // the candidates flattened over all lanes: every lane takes one per round
         const bool h1 = c1 > 0, h2 = c2 > 0;
         const unsigned hb1 = __ballot_sync(0xffffffffu, h1), hb2 = __ballot_sync(0xffffffffu, h2);
         int incl = c1 + c2;
@@ -692,68 +734,90 @@ __device__ void build_jlist(const SdmArgs& a, int r, int I, int4* rng) {
         {
             const unsigned lt = (1u << lane) - 1u;
             const int ri = __popc(hb1 & lt) + __popc(hb2 & lt);
-            if (h1) rng[ri] = make_int4(jb1, incl - c1 - c2, __float_as_int(Sx), __float_as_int(Sy));
-            if (h2) rng[ri + (h1 ? 1 : 0)] = make_int4(jb2, incl - c2, __float_as_int(Sx), __float_as_int(Sy));
+            const int ob = own ? (int)0x80000000 : 0;
+            if (h1) js.rng[ri] = make_int4(jb1 | ob, incl - c1 - c2, __float_as_int(Sx), __float_as_int(Sy));
+            if (h2) js.rng[ri + (h1 ? 1 : 0)] = make_int4(jb2 | ob, incl - c2, __float_as_int(Sx), __float_as_int(Sy));
         }
         const int nr = __popc(hb1) + __popc(hb2);
         __syncwarp();
         for (int e0 = 0; e0 < total; e0 += 32) {
             const int e = e0 + lane;
-            bool pass = false;
-            int4 en = make_int4(0, 0, 0, 0);
+            int J = 0, czj = 0;
+            bool inr = false, ownc = false;
+            float cSx = 0.f, cSy = 0.f;
+            float4 cj = make_float4(0.f, 0.f, 0.f, 0.f), hjb = cj;
             if (e < total) {
                 int lo = 0, hi = nr - 1;
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
-                    if (rng[mid].y <= e) lo = mid; else hi = mid - 1;
+                    if (js.rng[mid].y <= e) lo = mid; else hi = mid - 1;
                 }
-                const int4 rg = rng[lo];
-                const int J = rg.x + (e - rg.y);
-                const float cSx = __int_as_float(rg.z), cSy = __int_as_float(rg.w);
+                const int4 rg = js.rng[lo];
+                J = (rg.x & 0x7fffffff) + (e - rg.y);
+                ownc = rg.x < 0;
+                cSx = __int_as_float(rg.z);
+                cSy = __int_as_float(rg.w);
                 const int jw = R.cl_win + J;
-                const float4 cj = a.cl_bbc[jw], hjb = a.cl_bbh[jw];
-                const float sz = tabz[wrap_cell(__float_as_int(cj.w) - ref.z, S.M[2]) + S.M[2]];
-                float dx = cj.x + cSx - bc.x, dy = cj.y + cSy - bc.y, dz = cj.z + sz - bc.z;
-                if (IMG) {
-                    dx = img32(dx, S.Lf[0], S.invLf[0]);
-                    dy = img32(dy, S.Lf[1], S.invLf[1]);
-                    dz = img32(dz, S.Lf[2], S.invLf[2]);
+                cj = a.cl_bbc[jw];
+                hjb = a.cl_bbh[jw];
+                czj = __float_as_int(cj.w);
+                inr = true;
+            }
+#pragma unroll 1
+            for (int b = 0; b < nI; ++b) {
+                const int I = I0 + b;
+                const float4 bc = js.bc[b], bh = js.bh[b];
+                bool pass = false;
+                int4 en = make_int4(0, 0, 0, 0);
+                if (inr && (!ownc || J >= I)) {
+                    const float sz = tabz[wrap_cell(czj - __float_as_int(bc.w), S.M[2]) + S.M[2]];
+                    float dx = cj.x + cSx - bc.x, dy = cj.y + cSy - bc.y, dz = cj.z + sz - bc.z;
+                    if (IMG) {
+                        dx = img32(dx, S.Lf[0], S.invLf[0]);
+                        dy = img32(dy, S.Lf[1], S.invLf[1]);
+                        dz = img32(dz, S.Lf[2], S.invLf[2]);
+                    }
+                    const float gx = fmaxf(fabsf(dx) - bh.x - hjb.x, 0.0f);
+                    const float gy = fmaxf(fabsf(dy) - bh.y - hjb.y, 0.0f);
+                    const float gz = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
+                    pass = gx * gx + gy * gy + gz * gz < rclc2;
+                    const int4 lkA = js.lk[b][0], lkB = js.lk[b][1];
+                    // clusters sharing an exclusion with I: the relation is symmetric,
+                    // so I's own (complete unless -2) partner list decides every J
+                    const bool nm = (J == I) || lkA.x == -2 || lkA.x == J || lkA.y == J || lkA.z == J ||
+                                    lkA.w == J || lkB.x == J || lkB.y == J || lkB.z == J || lkB.w == J;
+                    en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(cSx), __float_as_int(cSy),
+                                   __float_as_int(sz));
                 }
-                const float gx = fmaxf(fabsf(dx) - bh.x - hjb.x, 0.0f);
-                const float gy = fmaxf(fabsf(dy) - bh.y - hjb.y, 0.0f);
-                const float gz = fmaxf(fabsf(dz) - bh.z - hjb.z, 0.0f);
-                pass = gx * gx + gy * gy + gz * gz < rclc2;
-                const bool nm = (J == I) || lkA.x == -2 || lkA.x == J || lkA.y == J || lkA.z == J ||
-                                lkA.w == J || lkB.x == J || lkB.y == J || lkB.z == J || lkB.w == J;
-                en = make_int4(J | (nm ? (int)0x80000000 : 0), __float_as_int(cSx), __float_as_int(cSy),
-                               __float_as_int(sz));
+                const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                const int base = __shfl_sync(0xffffffffu, mycnt, b);
+                if (pass) {
+                    const int pos = base + __popc(bal & ((1u << lane) - 1u));
+                    if (pos < a.jl_cap) a.jl[(size_t)(cw0 + b) * a.jl_cap + pos] = en;
+                }
+                if (lane == b) mycnt += __popc(bal);
             }
-            const unsigned bal = __ballot_sync(0xffffffffu, pass);
-            if (pass) {
-                const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
-                if (pos < a.jl_cap) out[pos] = en;
-            }
-            cnt += __popc(bal);
         }
         __syncwarp();   // rng is rewritten by the next stencil round
     }
-    if (lane == 0) {
-        a.jl_cnt[cw] = cnt;
-        if (cnt > a.jl_cap) atomicOr(a.status, SDM_DEV_LIST_OVERFLOW);
+    if (lane < nI) {
+        a.jl_cnt[cw0 + lane] = mycnt;
+        if (mycnt > a.jl_cap) atomicOr(a.status, SDM_DEV_LIST_OVERFLOW);
     }
+    __syncwarp();   // js is rewritten by the warp's next group
 }
 
-// static schedule: warp w takes items w, w+W, w+2W, ...
-__global__ void __launch_bounds__(256, 4) k_jlist(SdmArgs a, const int* cl_prefix) {
-    __shared__ int4 rng_all[8][64];   // per warp: candidate ranges of one stencil round
-    int4* rng = rng_all[threadIdx.x >> 5];
-    const int total = cl_prefix[a.nrep];
+// static schedule: warp w takes groups w, w+W, w+2W, ...
+__global__ void __launch_bounds__(256, 4) k_jlist(SdmArgs a, const int* grp_prefix) {
+    __shared__ JlSmem js_all[8];
+    JlSmem& js = js_all[threadIdx.x >> 5];
+    const int total = grp_prefix[a.nrep];
     const int W = gridDim.x * (blockDim.x >> 5);
     for (int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < total; item += W) {
-        const int r = rep_by_item(cl_prefix, a.nrep, item);
-        const int I = item - cl_prefix[r];
-        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) build_jlist<true>(a, r, I, rng);
-        else build_jlist<false>(a, r, I, rng);
+        const int r = rep_by_item(grp_prefix, a.nrep, item);
+        const int g = item - grp_prefix[r];
+        if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) build_jlist<true>(a, r, g, js);
+        else build_jlist<false>(a, r, g, js);
     }
 }
 
@@ -2287,14 +2351,14 @@ static int grid_for(long long n, int block) {
 
 extern "C++" {
 
-cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* cl_prefix, int* done, cudaStream_t st,
+cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* grp_prefix, int* done, cudaStream_t st,
                             cudaEvent_t* ev, int nev, unsigned ev_flags) {
     int e = 0;
     auto mark = [&]() { if (ev && e < nev) cudaEventRecordWithFlags(ev[e++], st, ev_flags); };
     mark();
     k_cells<<<grid_for(a.total_atoms > a.total_slots ? a.total_atoms : a.total_slots, 256), 256, 0, st>>>(a);
     mark();
-    k_scan<<<a.nrep, 1024, 0, st>>>(a, item_prefix, cl_prefix, done);
+    k_scan<<<a.nrep, 1024, 0, st>>>(a, item_prefix, grp_prefix, done);
     mark();
     k_bucket<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
     mark();
@@ -2305,8 +2369,8 @@ cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* cl_prefix, 
     return cudaGetLastError();
 }
 
-cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* cl_prefix, cudaStream_t st) {
-    k_jlist<<<num_sms() * 8, 256, 0, st>>>(a, cl_prefix);
+cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* grp_prefix, cudaStream_t st) {
+    k_jlist<<<num_sms() * 8, 256, 0, st>>>(a, grp_prefix);
     return cudaGetLastError();
 }
 

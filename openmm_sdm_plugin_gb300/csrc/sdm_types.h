@@ -29,6 +29,7 @@
 //     F0x/F0y/F0z, dFx/dFy/dFz   int64 fixed point 2^32
 //   per replica, cluster-indexed (window = slot_cap/8)
 //     jl       int4[jl_cap]  cluster-pair list of the i-cluster, jl_cnt entries
+//     cl_grp   int2    list-building groups: SDM_JG z-consecutive clusters of a column
 //     cl_ref   int4    reference cell (cx, cy, cz) and column id
 //     cl_bbc   float4  bounding-box centre (cluster frame)
 //     cl_bbh   float4  bounding-box half extents
@@ -42,6 +43,7 @@
 #define SDM_FIX_SCALE 4294967296.0 // 2^32 fixed point for forces
 #define SDM_LIST_MARGIN 1.0e-4   // nm added to the cutoff in the list filter
 #define SDM_MAX_SPLIT 4
+#define SDM_JG 4                 // i-clusters per list-building group (one column, z-consecutive)
 
 // Langevin parameter block (doubles; seed and step are stored as integer bits)
 #define SDM_LV_DT 0
@@ -246,6 +248,8 @@ struct SdmArgs {
     int st_any;             // 1 when some system has rigid waters
     int st_max;             // largest water count of a system
     int* ncl;            // clusters per replica
+    int* ngrp;           // list-building groups per replica
+    int2* cl_grp;        // per group (cluster window): first cluster, clusters (1..SDM_JG)
     unsigned* extz;      // per replica max cluster z extent (float bits)
     int* work_counter;   // [0] main pass, [1] perturbation pass
     int* status;         // device status word
