@@ -953,7 +953,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_ref = ar.take<int4>(Cl), o_bbc = ar.take<float4>(Cl), o_bbh = ar.take<float4>(Cl);
     const size_t o_lnk = ar.take<int4>(2 * Cl), o_ep = ar.take<double>(Cl * SDM_MAX_SPLIT);
     const size_t o_zb = ar.take<float2>(Cl);
-    const size_t o_pp = ar.take<double>(std::max(Pp, 1LL) * 4);   // SDM_PERT_PARTS partials per item
+    const size_t o_pp = ar.take<double>(std::max(Pp, 1LL) * SDM_PERT_PARTS);   // partials per item
     const size_t o_ppos = ar.take<SdmPertPos>(std::max(Pp, 1LL));
     const size_t o_adj = ar.take<double>(3 * std::max(Pp, 1LL));
     const size_t o_ncl = ar.take<int>(nrep), o_st = ar.take<int>(4), o_srep = ar.take<double>(nrep);

@@ -35,7 +35,6 @@
 
 #define SDM_WARPS 4
 #define SDM_JL_CAP 256
-#define SDM_PERT_PARTS 4         // warps per perturbation item (stencil columns split between them)
 #define SDM_RING 64
 #define SDM_INVALID_COORD 1.0e6f
 

@@ -44,6 +44,7 @@
 #define SDM_LIST_MARGIN 1.0e-4   // nm added to the cutoff in the list filter
 #define SDM_MAX_SPLIT 4
 #define SDM_JG 4                 // i-clusters per list-building group (one column, z-consecutive)
+#define SDM_PERT_PARTS 4         // warps per perturbation item (stencil columns split between them)
 
 // Langevin parameter block (doubles; seed and step are stored as integer bits)
 #define SDM_LV_DT 0
