@@ -36,7 +36,7 @@ RESULT_FIELDS = ("U0", "U1", "u", "BindE", "fp", "W", "dW", "s", "E_pot", "dWdla
  R_STATUS, R_NCL) = range(16)
 
 (OPT_GRAPH, OPT_PROFILE, OPT_SPLIT, OPT_CTAS_PER_SM, OPT_VERIFY, OPT_PAIR_RESIDENT, OPT_ZERO_COPY,
- OPT_STAGE_CHUNK) = range(8)
+ OPT_STAGE_CHUNK, OPT_OVERLAP, OPT_LIST_GROUP) = range(10)
 
 EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_set_displacement", "sdm_set_params", "sdm_evaluate", "sdm_evaluate_device",

@@ -131,6 +131,8 @@ struct sdm_handle {
     void* rs_buf = nullptr;   // restraint data of every system (sdm_set_restraints)
     void* st_buf = nullptr;   // rigid-water data and the unconstrained-position scratch
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;          // second branch of an evaluation (perturbation pass)
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     SdmArgs args{};
     int* item_prefix = nullptr;
     int* grp_prefix = nullptr;   // list-building groups over replicas (k_jlist items)
@@ -155,6 +157,9 @@ struct sdm_handle {
     // options
     int opt_graph = 1, opt_profile = 0, opt_split = 1, opt_ctas = 4, opt_verify = 1, opt_zero_copy = 0;
     int opt_chunk = 12;                   // list entries per staged chunk of the main pass (8, 12, 16)
+    int opt_overlap = 2;                  // second graph branch (SDM_OPT_OVERLAP)
+    int opt_list_group = 0;               // clusters per list-building group (SDM_OPT_LIST_GROUP; 0 automatic)
+    int auto_list_group = 4;              // the automatic choice, set at creation
     int pair_res[3][SDM_MAX_CTAS + 1] = {};  // resident pair-kernel CTAs per SM by chunk (8, 12, 16) and request
     // graphs
     std::map<GraphKey, cudaGraphExec_t> graphs;
@@ -648,15 +653,37 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     SDM_CUDA(h, cudaMemsetAsync(h->counters, 0, h->counters_bytes, st));
     cudaEvent_t* ev = profile ? h->ev : nullptr;
     SDM_CUDA(h, sdm_launch_prep(a, h->item_prefix, h->grp_prefix, h->done, st, ev, 6, fl));
+    // The perturbation pass reads only what the preparation kernels wrote and
+    // adds into its own accumulators (dF, its energy partials), and the PME
+    // reciprocal space reads positions and cell data and adds forces by
+    // integer atomics: they run on a second branch of the graph beside the
+    // list build.  SDM_OPT_OVERLAP 1 joins it before the main pass, 2 after it
+    // (with PME on the branch: the main pass takes clusters from a counter, so
+    // CTAs that start late take fewer).  Timed evaluations keep one branch so
+    // that the events bracket single kernels.
+    const int ov = profile || mode == 2 ? 0 : h->opt_overlap;
+    const bool pme_side = ov == 2 && mode == 0 && h->pme;
+    const bool fork = ov != 0 && (a.total_pert > 0 || pme_side);
+    if (fork) {
+        SDM_CUDA(h, cudaEventRecord(h->fork_ev, st));
+        SDM_CUDA(h, cudaStreamWaitEvent(h->side, h->fork_ev, 0));
+        SDM_CUDA(h, sdm_launch_perturb(a, mode, h->side));
+        if (pme_side)
+            SDM_CUDA(h, sdm_launch_pme(a, h->pme_r2c.data(), h->pme_c2r.data(), h->pme_grid_off.data(),
+                                       h->pme_spec_off.data(), (int)h->sys.size(), a.pme_conv_blocks, h->side));
+        SDM_CUDA(h, cudaEventRecord(h->join_ev, h->side));
+    }
     SDM_CUDA(h, sdm_launch_jlist(a, h->grp_prefix, st));
+    if (fork && ov == 1) SDM_CUDA(h, cudaStreamWaitEvent(st, h->join_ev, 0));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[6], st, fl));
     SDM_CUDA(h, sdm_launch_pair(a, h->item_prefix, mode, h->opt_ctas, h->pair_res[chunk_index(h->opt_chunk)][h->opt_ctas],
                                 h->pme, h->opt_chunk, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
-    if (mode != 2) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
+    if (fork && ov == 2) SDM_CUDA(h, cudaStreamWaitEvent(st, h->join_ev, 0));
+    if (mode != 2 && !fork) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
     if (mode == 0) SDM_CUDA(h, sdm_launch_exceptions(a, st));
     if (mode == 0) SDM_CUDA(h, sdm_launch_restraints(a, st));
-    if (mode == 0 && h->pme)
+    if (mode == 0 && h->pme && !pme_side)
         SDM_CUDA(h, sdm_launch_pme(a, h->pme_r2c.data(), h->pme_c2r.data(), h->pme_grid_off.data(),
                                    h->pme_spec_off.data(), (int)h->sys.size(), a.pme_conv_blocks, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[8], st, fl));
@@ -697,6 +724,7 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
     a.results = res;
     a.forces = f;
     a.F0out = nullptr;
+    a.jg = h->opt_list_group ? h->opt_list_group : h->auto_list_group;
     a.lv_x = lv ? lv->x : nullptr;
     a.lv_v = lv ? lv->v : nullptr;
     a.lv_invm = lv ? lv->invm : nullptr;
@@ -726,7 +754,7 @@ sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStrea
         return SDM_OK;
     }
     const bool gprof = h->opt_profile == 2;
-    GraphKey key{x, res, f, st, a.split, h->opt_ctas + (gprof ? 100 : 0) + 1000 * h->opt_chunk};
+    GraphKey key{x, res, f, st, a.split, h->opt_ctas + (gprof ? 100 : 0) + 1000 * h->opt_chunk + 100000 * h->opt_overlap + 1000000 * h->opt_list_group};
     if (lv) { key.v = lv->v; key.invm = lv->invm; key.fext = lv->fext; }
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
@@ -967,6 +995,10 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     if (ce != cudaSuccess) { h->arena = nullptr; cuda_fail(h, ce, "cudaMalloc(arena)"); return bail(SDM_ERR_CUDA); }
     ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) { cuda_fail(h, ce, "cudaStreamCreate"); return bail(SDM_ERR_CUDA); }
+    ce = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming);
+    if (ce != cudaSuccess) { cuda_fail(h, ce, "cudaStreamCreate(side)"); return bail(SDM_ERR_CUDA); }
     ce = cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
     if (ce != cudaSuccess) { cuda_fail(h, ce, "cudaMemset(arena)"); return bail(SDM_ERR_CUDA); }
     for (int k = 0; k < 12; ++k) cudaEventCreate(&h->ev[k]);
@@ -1088,6 +1120,12 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
         }
     }
     a.total_slots = (int)Sl;
+    // list-building groups of four clusters, also for a single replica: with
+    // the perturbation pass running beside the list build, the fewer, longer
+    // list-building warps leave it room (1-replica call 0.115 ms against
+    // 0.120 ms with groups of 1 or 2)
+    h->auto_list_group = SDM_JG;
+    a.jg = h->auto_list_group;
     a.split = 1;
     a.ex_cap = 0;
     a.ex_rep = -1;
@@ -1127,6 +1165,9 @@ sdm_status sdm_destroy(sdm_handle* h) {
     for (auto p : h->pme_r2c) cufftDestroy(p);
     for (auto p : h->pme_c2r) cufftDestroy(p);
     if (h->stream) { cudaStreamSynchronize(h->stream); cudaStreamDestroy(h->stream); }
+    if (h->side) { cudaStreamSynchronize(h->side); cudaStreamDestroy(h->side); }
+    if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+    if (h->join_ev) cudaEventDestroy(h->join_ev);
     if (h->arena) cudaFree(h->arena);
     if (h->params_pinned) cudaFreeHost(h->params_pinned);
     delete h;
@@ -1726,6 +1767,15 @@ sdm_status sdm_set_option(sdm_handle* h, int option, int value) {
                 return fail(h, SDM_ERR_INVALID_ARGUMENT, "stage chunk must be 8, 12 or 16");
             h->opt_chunk = value;
             break;
+        case SDM_OPT_OVERLAP:
+            if (value < 0 || value > 2) return fail(h, SDM_ERR_INVALID_ARGUMENT, "overlap must be 0, 1 or 2");
+            h->opt_overlap = value;
+            break;
+        case SDM_OPT_LIST_GROUP:
+            if (value != 0 && value != 1 && value != 2 && value != SDM_JG)
+                return fail(h, SDM_ERR_INVALID_ARGUMENT, "list group must be 0 (automatic), 1, 2 or 4");
+            h->opt_list_group = value;
+            break;
         default: return fail(h, SDM_ERR_INVALID_ARGUMENT, "unknown option");
     }
     return SDM_OK;
@@ -1742,6 +1792,8 @@ sdm_status sdm_get_option(const sdm_handle* h, int option, int* value) {
         case SDM_OPT_PAIR_RESIDENT: *value = h->pair_res[chunk_index(h->opt_chunk)][h->opt_ctas]; break;
         case SDM_OPT_STAGE_CHUNK: *value = h->opt_chunk; break;
         case SDM_OPT_ZERO_COPY: *value = h->opt_zero_copy; break;
+        case SDM_OPT_OVERLAP: *value = h->opt_overlap; break;
+        case SDM_OPT_LIST_GROUP: *value = h->opt_list_group; break;
         default: return SDM_ERR_INVALID_ARGUMENT;
     }
     return SDM_OK;

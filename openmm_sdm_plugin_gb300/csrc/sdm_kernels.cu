@@ -218,8 +218,8 @@ __device__ __forceinline__ int4 warp_incl_scan3(int4 v) {
     return v;
 }
 
-// Column prefixes of particles, clusters and list-building groups (SDM_JG
-// z-consecutive clusters of one column); the group table (first cluster,
+// Column prefixes of particles, clusters and list-building groups (a.jg <=
+// SDM_JG z-consecutive clusters of one column); the group table (first cluster,
 // clusters) of every group.  The last block builds the work-item prefix of
 // the main pass and the group prefix of the list builder over replicas.
 __global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int* grp_prefix, int* done) {
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int*
         const int nc = (n + 7) >> 3;
         s.x += n;
         s.y += nc;
-        s.z += (nc + SDM_JG - 1) / SDM_JG;
+        s.z += (nc + a.jg - 1) / a.jg;
     }
     int4 inc = warp_incl_scan3(s);
     const int wid = threadIdx.x >> 5;
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(1024) k_scan(SdmArgs a, int* item_prefix, int*
         int o = base.x;
         for (int z = 0; z < mz; ++z) { coff[c * mz + z] = o; o += ccnt[c * mz + z]; }
         const int nc = (cnt[c] + 7) >> 3;
-        for (int k = 0; k < nc; k += SDM_JG) grp[base.z++] = make_int2(base.y + k, min(SDM_JG, nc - k));
+        for (int k = 0; k < nc; k += a.jg) grp[base.z++] = make_int2(base.y + k, min(a.jg, nc - k));
         base.x += cnt[c];
         base.y += nc;
     }
@@ -630,7 +630,7 @@ struct JlSmem {
     int4 lk[SDM_JG][2];
 };
 
-// The lists of the nI <= SDM_JG z-consecutive clusters I0.. of one column.
+// The lists of the nI <= a.jg <= SDM_JG z-consecutive clusters I0.. of one column.
 // The column searches run once over the union of the members' z windows and
 // each candidate's box is loaded once; every member then applies its own
 // box test (the rule of a list built for that cluster alone) and appends to
@@ -1218,9 +1218,14 @@ k_pair(SdmArgs a, const int* item_prefix) {
     extern __shared__ __align__(16) unsigned char pair_smem[];
     EvalSmem<CH>& sm = reinterpret_cast<EvalSmem<CH>*>(pair_smem)[threadIdx.x >> 5];
     const int total = item_prefix[a.nrep];
-    const int W = gridDim.x * NW;
-    // static schedule: warp w takes items w, w+W, ...
-    for (int item = blockIdx.x * NW + (threadIdx.x >> 5); item < total; item += W) {
+    // dynamic schedule: each warp takes the next item from a counter (zeroed
+    // at the start of every evaluation), so CTAs that become resident late
+    // (other branches of the graph still running) just take fewer items
+    for (;;) {
+        int item = 0;
+        if (lane_id() == 0) item = atomicAdd(&a.work_counter[2], 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
         const int r = rep_by_item(item_prefix, a.nrep, item);
         const int local = item - item_prefix[r];
         const int I = local / a.split, part = local - I * a.split;

@@ -43,7 +43,7 @@
 #define SDM_FIX_SCALE 4294967296.0 // 2^32 fixed point for forces
 #define SDM_LIST_MARGIN 1.0e-4   // nm added to the cutoff in the list filter
 #define SDM_MAX_SPLIT 4
-#define SDM_JG 4                 // i-clusters per list-building group (one column, z-consecutive)
+#define SDM_JG 4                 // largest list-building group (i-clusters of one column, z-consecutive)
 #define SDM_PERT_PARTS 4         // warps per perturbation item (stencil columns split between them)
 
 // Langevin parameter block (doubles; seed and step are stored as integer bits)
@@ -250,6 +250,7 @@ struct SdmArgs {
     int st_max;             // largest water count of a system
     int* ncl;            // clusters per replica
     int* ngrp;           // list-building groups per replica
+    int jg;              // clusters per list-building group (1, 2 or SDM_JG)
     int2* cl_grp;        // per group (cluster window): first cluster, clusters (1..SDM_JG)
     unsigned* extz;      // per replica max cluster z extent (float bits)
     int* work_counter;   // [0] main pass, [1] perturbation pass

@@ -138,6 +138,32 @@ def test_clusters_and_lists_bit_exact(which):
         assert np.array_equal(gm[order], ol["mask"][I, :k])
 
 
+def test_list_groups_give_the_same_lists():
+    """Lists built for groups of 1, 2 and 4 z-consecutive clusters (and the
+    automatic choice) hold the same entries per i-cluster; the evaluations
+    agree to FP32 summation order (tile composition may differ)."""
+    s = S.config1()
+    h = _handle([s])
+    x = s.positions[0]
+    assert h.get_option(capi.OPT_LIST_GROUP) == 0
+    ref = None
+    for g in (0, 1, 2, 4):
+        h.set_option(capi.OPT_LIST_GROUP, g)
+        L = h.export_lists(0, x)
+        res, F = h.evaluate(x)
+        ent = [sorted(zip(L["slot"][I, :L["cnt"][I]].tolist(), L["mask"][I, :L["cnt"][I]].tolist()))
+               for I in range(L["ncl"])]
+        if ref is None:
+            ref = (ent, res, F)
+            continue
+        assert ent == ref[0], g
+        for k in (capi.R_U0, capi.R_U1, capi.R_U):
+            assert abs(res[0, k] - ref[1][0, k]) <= 1e-6 * max(1.0, abs(ref[1][0, k])), (g, k)
+        assert np.abs(F - ref[2]).max() < 1e-3, g
+    with pytest.raises(capi.SdmError):
+        h.set_option(capi.OPT_LIST_GROUP, 3)
+
+
 def test_batched_replicas_match_single():
     s = S.config2(nrep=4)
     h = _handle([s])
@@ -179,6 +205,28 @@ def test_deterministic_bitwise():
     r2, F2 = h.evaluate(x)
     assert np.array_equal(r1, r2)
     assert np.array_equal(F1, F2)
+
+
+def test_overlapped_perturbation_pass_same_bits():
+    """The perturbation pass on a second stream branch joined after (default)
+    or before the main pass, against one stream, captured and eager: the same
+    results and forces bit for bit, state forces included."""
+    s = S.config2(nrep=3)
+    h = _handle([s])
+    x = s.positions.reshape(-1, 3)
+    assert h.get_option(capi.OPT_OVERLAP) == 2
+    out = {}
+    for overlap in (2, 1, 0):
+        for graph in (1, 0):
+            h.set_option(capi.OPT_OVERLAP, overlap)
+            h.set_option(capi.OPT_GRAPH, graph)
+            r, F = h.evaluate(x)
+            out[overlap, graph] = (r, F) + h.state_forces()
+    ref = out[2, 1]
+    assert np.all(ref[0][:, capi.R_STATUS] == 0)
+    for k, v in out.items():
+        for a, b in zip(v, ref):
+            assert np.array_equal(a, b), k
 
 
 @pytest.mark.parametrize("bias", [0, 1, 2])

@@ -143,3 +143,23 @@ def test_pme_rejects_mixed_methods_and_adjoint():
     h.evaluate(s.positions[0])
     with pytest.raises(capi.SdmError):
         h.adjoint(30)
+
+
+def test_pme_reciprocal_space_on_the_second_branch():
+    """SDM_OPT_OVERLAP 2 runs the reciprocal space on the graph's second
+    branch beside the list build and the main pass: the same bits as one
+    stream and as the default branch joined before the main pass."""
+    s = _pme(S.host_guest(1500, seed=5, nstates=3))
+    h = capi.Handle([s])
+    for r, p in enumerate(s.params):
+        h.set_params(r, p.as_array())
+    x = np.ascontiguousarray(s.positions.reshape(-1, 3))
+    out = {}
+    for ov in (0, 1, 2):
+        h.set_option(capi.OPT_OVERLAP, ov)
+        r, F = h.evaluate(x)
+        out[ov] = (r, F) + h.state_forces()
+    assert np.all(out[0][0][:, capi.R_STATUS] == 0)
+    for ov in (1, 2):
+        for a, b in zip(out[ov], out[0]):
+            assert np.array_equal(a, b), ov
