@@ -148,7 +148,7 @@ def test_pme_rejects_mixed_methods_and_adjoint():
 def test_pme_reciprocal_space_on_the_second_branch():
     """SDM_OPT_OVERLAP 2 runs the reciprocal space on the graph's second
     branch beside the list build and the main pass: the same bits as one
-    stream and as the default branch joined before the main pass."""
+    stream and as the branch joined before the main pass."""
     s = _pme(S.host_guest(1500, seed=5, nstates=3))
     h = capi.Handle([s])
     for r, p in enumerate(s.params):
@@ -159,7 +159,8 @@ def test_pme_reciprocal_space_on_the_second_branch():
         h.set_option(capi.OPT_OVERLAP, ov)
         r, F = h.evaluate(x)
         out[ov] = (r, F) + h.state_forces()
-    assert np.all(out[0][0][:, capi.R_STATUS] == 0)
-    for ov in (1, 2):
-        for a, b in zip(out[ov], out[0]):
-            assert np.array_equal(a, b), ov
+    ref = out[0]
+    assert np.all(ref[0][:, capi.R_STATUS] == 0)
+    for k, v in out.items():
+        for a, b in zip(v, ref):
+            assert np.array_equal(a, b), k
