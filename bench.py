@@ -632,6 +632,8 @@ def main():
                    "schedule": {"split": h.get_option(capi.OPT_SPLIT), "ctas_per_sm": h.get_option(capi.OPT_CTAS_PER_SM),
                                 "ctas_resident": h.get_option(capi.OPT_PAIR_RESIDENT),
                                 "stage_chunk": h.get_option(capi.OPT_STAGE_CHUNK),
+                                "list_group": h.get_option(capi.OPT_LIST_GROUP) or 4,
+                                "overlap": h.get_option(capi.OPT_OVERLAP),
                                 "autotuned": tuned is not None,
                                 "tuning": tuned}},
         "gpu_launches": KERNELS_PER_STEP * args.steps,

@@ -354,20 +354,24 @@ sdm_status sdm_get_option(const sdm_handle* h, int option, int* value);
  * and ms[i] for i < *count (in: capacity, out: entries). */
 sdm_status sdm_get_kernel_times(const sdm_handle* h, const char** names, float* ms, int* count);
 
-/* The main-pass choice of the autotuner. */
+/* The schedule chosen by the autotuner. */
 typedef struct {
     int stage_chunk;    /* SDM_OPT_STAGE_CHUNK */
     int ctas_per_sm;    /* SDM_OPT_CTAS_PER_SM */
     int split;          /* SDM_OPT_SPLIT */
     float ms;           /* median time of one whole evaluation (graph replay) with this choice */
     int from_cache;     /* 1: read from the cache file, nothing timed */
+    int list_group;     /* SDM_OPT_LIST_GROUP (1, 2 or 4) */
+    int overlap;        /* SDM_OPT_OVERLAP (0, 1 or 2) */
 } sdm_tune_result;
 
 /* Autotuner (no counterpart in the reference, which has one fixed OpenCL
  * schedule).  Times every staging chunk (8, 12, 16 list entries) x CTAs per
- * SM (3, 4) x split (1, 2) on coordinates x (device pointer): each candidate is a whole
- * evaluation replayed as a CUDA graph, 5 timed replays after 2 warm-up ones,
- * median.  The fastest becomes the handle's setting.  With cache_path, the
+ * SM (3, 4) x split (1, 2) on coordinates x (device pointer), then, on the
+ * fastest of those, the list-building group (1, 2, 4) and the graph's second
+ * branch (SDM_OPT_OVERLAP 0, 1, 2): each candidate is a whole evaluation
+ * replayed as a CUDA graph, 5 timed replays after 2 warm-up ones, median.
+ * The fastest becomes the handle's setting.  With cache_path, the
  * choice is stored in that text file under the workload key of
  * sdm_tune_key, and a later call with the same key (another handle, another
  * process) takes it from there without timing.  Synchronises.  Returns

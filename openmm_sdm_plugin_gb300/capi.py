@@ -61,7 +61,7 @@ class SdmError(RuntimeError):
 
 class TuneResult(C.Structure):
     _fields_ = [("stage_chunk", C.c_int), ("ctas_per_sm", C.c_int), ("split", C.c_int), ("ms", C.c_float),
-                ("from_cache", C.c_int)]
+                ("from_cache", C.c_int), ("list_group", C.c_int), ("overlap", C.c_int)]
 
 
 class SystemDesc(C.Structure):
@@ -424,12 +424,13 @@ class Handle:
 
     def autotune(self, x_ptr: int, cache_path=None):
         """sdm_autotune_cached on device coordinates: dict of the chosen
-        stage_chunk, ctas_per_sm, split, the median ms and from_cache."""
+        stage_chunk, ctas_per_sm, split, list_group, overlap, the median ms
+        and from_cache."""
         r = TuneResult()
         self._check(self.lib.sdm_autotune_cached(self.h, C.c_void_p(x_ptr),
                                                  cache_path.encode() if cache_path else None, C.byref(r)))
         return dict(stage_chunk=r.stage_chunk, ctas_per_sm=r.ctas_per_sm, split=r.split, ms=r.ms,
-                    from_cache=bool(r.from_cache))
+                    from_cache=bool(r.from_cache), list_group=r.list_group, overlap=r.overlap)
 
     def count_pairs(self, x):
         x = np.ascontiguousarray(np.asarray(x, np.float64).reshape(-1))

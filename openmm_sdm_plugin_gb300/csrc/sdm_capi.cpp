@@ -1847,7 +1847,12 @@ bool tune_cache_read(const char* path, const std::string& key, sdm_tune_result* 
         const char* bar = strchr(line, '|');
         if (!bar || std::string(line, bar - line) != key) continue;
         sdm_tune_result t = {};
-        if (sscanf(bar + 1, "%d %d %d %f", &t.stage_chunk, &t.ctas_per_sm, &t.split, &t.ms) == 4) {
+        t.list_group = SDM_JG;
+        t.overlap = 2;
+        // chunk, CTAs, split, ms [, list group, overlap]: lines without the last
+        // two (an older cache) take the defaults
+        if (sscanf(bar + 1, "%d %d %d %f %d %d", &t.stage_chunk, &t.ctas_per_sm, &t.split, &t.ms, &t.list_group,
+                   &t.overlap) >= 4) {
             *r = t;
             found = true;   // the last line of a key wins
         }
@@ -1872,7 +1877,8 @@ bool tune_cache_write(const char* path, const std::string& key, const sdm_tune_r
     FILE* f = fopen(tmp.c_str(), "w");
     if (!f) return false;
     for (const std::string& l : keep) fputs(l.c_str(), f);
-    fprintf(f, "%s|%d %d %d %.6f\n", key.c_str(), r.stage_chunk, r.ctas_per_sm, r.split, r.ms);
+    fprintf(f, "%s|%d %d %d %.6f %d %d\n", key.c_str(), r.stage_chunk, r.ctas_per_sm, r.split, r.ms, r.list_group,
+            r.overlap);
     const bool ok = fclose(f) == 0;
     return ok && rename(tmp.c_str(), path) == 0;
 }
@@ -1922,17 +1928,23 @@ sdm_status sdm_autotune_cached(sdm_handle* h, const double* x_device, const char
         (best.stage_chunk == 8 || best.stage_chunk == 12 || best.stage_chunk == 16) &&
         best.ctas_per_sm >= 1 && best.ctas_per_sm <= SDM_MAX_CTAS &&
         (best.split == 1 || best.split == 2 || best.split == 4) &&
+        (best.list_group == 1 || best.list_group == 2 || best.list_group == SDM_JG) &&
+        best.overlap >= 0 && best.overlap <= 2 &&
         h->pair_res[chunk_index(best.stage_chunk)][best.ctas_per_sm] > 0) {
         h->opt_chunk = best.stage_chunk;
         h->opt_ctas = best.ctas_per_sm;
         h->opt_split = best.split;
+        h->opt_list_group = best.list_group;
+        h->opt_overlap = best.overlap;
         best.from_cache = 1;
         if (out) *out = best;
         return SDM_OK;
     }
     const int ochunk = h->opt_chunk, octas = h->opt_ctas, osplit = h->opt_split, oprof = h->opt_profile;
+    const int ogroup = h->opt_list_group, oover = h->opt_overlap;
     auto restore = [&]() {
         h->opt_chunk = ochunk; h->opt_ctas = octas; h->opt_split = osplit; h->opt_profile = oprof;
+        h->opt_list_group = ogroup; h->opt_overlap = oover;
     };
     h->opt_profile = 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1943,6 +1955,28 @@ sdm_status sdm_autotune_cached(sdm_handle* h, const double* x_device, const char
     }
     best.ms = 1e30f;
     sdm_status st = SDM_OK;
+    // median of 5 timed graph replays (after 2 untimed) of the current setting
+    auto time_setting = [&](float* med) -> sdm_status {
+        std::vector<float> ms;
+        for (int rep = 0; rep < 7; ++rep) {
+            if (rep >= 2) cudaEventRecord(e0, h->stream);
+            sdm_status s2 = run(h, x_device, h->res_in, h->f_in, h->stream, 0, true);
+            if (s2) return s2;
+            if (rep >= 2) {
+                cudaEventRecord(e1, h->stream);
+                cudaEventSynchronize(e1);
+                float t = 0.f;
+                cudaEventElapsedTime(&t, e0, e1);
+                ms.push_back(t);
+            }
+        }
+        std::sort(ms.begin(), ms.end());
+        *med = ms[ms.size() / 2];
+        return SDM_OK;
+    };
+    // pass 1: staging chunk x CTAs per SM x split, with the handle's list
+    // group and branch settings
+    const int group0 = h->opt_list_group ? h->opt_list_group : h->auto_list_group;
     for (int ch : {8, 12, 16})
         for (int c = 3; c <= SDM_MAX_CTAS && st == SDM_OK; ++c)
             for (int sp : {1, 2}) {
@@ -1950,24 +1984,35 @@ sdm_status sdm_autotune_cached(sdm_handle* h, const double* x_device, const char
                 h->opt_chunk = ch;
                 h->opt_ctas = c;
                 h->opt_split = sp;
-                std::vector<float> ms;
-                for (int rep = 0; rep < 7; ++rep) {
-                    if (rep >= 2) cudaEventRecord(e0, h->stream);
-                    st = run(h, x_device, h->res_in, h->f_in, h->stream, 0, true);
-                    if (st) break;
-                    if (rep >= 2) {
-                        cudaEventRecord(e1, h->stream);
-                        cudaEventSynchronize(e1);
-                        float t = 0.f;
-                        cudaEventElapsedTime(&t, e0, e1);
-                        ms.push_back(t);
-                    }
-                }
+                float med = 0.f;
+                st = time_setting(&med);
                 if (st) break;
-                std::sort(ms.begin(), ms.end());
-                const float med = ms[ms.size() / 2];
-                if (med < best.ms) best = sdm_tune_result{ch, c, sp, med, 0};
+                if (med < best.ms) best = sdm_tune_result{ch, c, sp, med, 0, group0, h->opt_overlap};
             }
+    // pass 2: on that schedule, the list-building group, then the second branch
+    if (st == SDM_OK) {
+        h->opt_chunk = best.stage_chunk;
+        h->opt_ctas = best.ctas_per_sm;
+        h->opt_split = best.split;
+        for (int g : {1, 2, SDM_JG}) {
+            if (g == best.list_group) continue;
+            h->opt_list_group = g;
+            h->opt_overlap = best.overlap;
+            float med = 0.f;
+            st = time_setting(&med);
+            if (st) break;
+            if (med < best.ms) { best.ms = med; best.list_group = g; }
+        }
+        for (int ov : {0, 1, 2}) {
+            if (st != SDM_OK || ov == best.overlap) continue;
+            h->opt_list_group = best.list_group;
+            h->opt_overlap = ov;
+            float med = 0.f;
+            st = time_setting(&med);
+            if (st) break;
+            if (med < best.ms) { best.ms = med; best.overlap = ov; }
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st) { restore(); return st; }
@@ -1983,6 +2028,8 @@ sdm_status sdm_autotune_cached(sdm_handle* h, const double* x_device, const char
     h->opt_chunk = best.stage_chunk;
     h->opt_ctas = best.ctas_per_sm;
     h->opt_split = best.split;
+    h->opt_list_group = best.list_group;
+    h->opt_overlap = best.overlap;
     h->opt_profile = oprof;
     if (!tune_cache_write(cache_path, key, best)) return fail(h, SDM_ERR_INVALID_ARGUMENT, "cannot write the tuning cache");
     if (out) *out = best;

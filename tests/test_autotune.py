@@ -1,7 +1,9 @@
 """The autotuner (sdm_autotune_cached): every staging chunk and schedule of
-the main pass timed on the production path, the fastest kept, the choice cached
-under the workload key and read back by a second handle; the chosen setting
-gives the same results as the default one within the parity tolerances."""
+the main pass timed on the production path, then the list-building group and
+the graph's second branch on the fastest of them; the choice cached under the
+workload key and read back by a second handle (an older cache line without
+the last two fields reads with their defaults); the chosen setting gives the
+same results as the default one within the parity tolerances."""
 import os
 
 import numpy as np
@@ -34,6 +36,9 @@ def test_autotune_chooses_caches_and_keeps_results(tmp_path):
     assert h.get_option(capi.OPT_STAGE_CHUNK) == r1["stage_chunk"]
     assert h.get_option(capi.OPT_CTAS_PER_SM) == r1["ctas_per_sm"]
     assert h.get_option(capi.OPT_SPLIT) == r1["split"]
+    assert r1["list_group"] in (1, 2, 4) and r1["overlap"] in (0, 1, 2)
+    assert h.get_option(capi.OPT_LIST_GROUP) == r1["list_group"]
+    assert h.get_option(capi.OPT_OVERLAP) == r1["overlap"]
     res, F = h.evaluate(x)
     for r in range(4):
         assert abs(res[r, capi.R_U] - ref_res[r, capi.R_U]) < U_ABS_TOL
@@ -47,7 +52,19 @@ def test_autotune_chooses_caches_and_keeps_results(tmp_path):
     h2 = _handle(S.config2(nrep=4))
     r2 = h2.autotune(xd.data_ptr(), cache)
     assert r2["from_cache"]
-    assert (r2["stage_chunk"], r2["ctas_per_sm"], r2["split"]) == (r1["stage_chunk"], r1["ctas_per_sm"], r1["split"])
+    fields = ("stage_chunk", "ctas_per_sm", "split", "list_group", "overlap")
+    assert all(r2[k] == r1[k] for k in fields)
     assert h2.get_option(capi.OPT_STAGE_CHUNK) == r1["stage_chunk"]
+    assert h2.get_option(capi.OPT_LIST_GROUP) == r1["list_group"]
     h2.close()
     assert os.path.exists(cache)
+    # a line written before the last two fields existed: list group 4, branch 2
+    with open(cache, "w") as f:
+        f.write(f"{key}|{r1['stage_chunk']} {r1['ctas_per_sm']} {r1['split']} 0.5\n")
+    h3 = _handle(S.config2(nrep=4))
+    h3.set_option(capi.OPT_LIST_GROUP, 1)
+    h3.set_option(capi.OPT_OVERLAP, 0)
+    r3 = h3.autotune(xd.data_ptr(), cache)
+    assert r3["from_cache"] and r3["list_group"] == 4 and r3["overlap"] == 2
+    assert h3.get_option(capi.OPT_LIST_GROUP) == 4 and h3.get_option(capi.OPT_OVERLAP) == 2
+    h3.close()
