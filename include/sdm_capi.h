@@ -426,6 +426,29 @@ sdm_status sdm_adjoint(sdm_handle* h, double* out);
  * No counterpart in the reference (see sdm_adjoint). */
 sdm_status sdm_adjoint_device(sdm_handle* h, double* out, void* stream);
 
+/* Backward of the differentiable potential U_r = U0 + W(u') of every replica
+ * (no counterpart in the reference), one launch on `stream`, device pointers.
+ * Inputs: grad_u [nrep] = dL/dU_r; results [nrep * SDM_NRESULTS], forces
+ * (mixed F) and forces1 (F1, sdm_get_state_forces_device) [3 * particles of
+ * all replicas] and adjoint [6 * sdm_get_num_perturbed] (sdm_adjoint_device)
+ * of the evaluation being differentiated; eps_displaced [sum over systems
+ * of their displaced particles] their FP64 epsilon (NULL: the third
+ * parameter gradient stays 2 eps dL/deps); bias_params [4 * nrep] rows of
+ * lambda1, lambda2, alpha, u0 used by that evaluation (NULL: the handle's
+ * current parameters).  Outputs (any may be NULL):
+ *   grad_x    [3 * particles of all replicas]  -grad_u[r] F
+ *   grad_d    [3 * particles of all systems]   -sum_r grad_u[r] s_r F1 over the system's replicas
+ *   grad_p    [3 * displaced of all systems]   charge, sigma, epsilon: sum_r grad_u[r]
+ *                                              ((1 - s_r) dU_0 + s_r dU_1)
+ *   grad_bias [5 * nrep] rows: dL/dlambda1, dL/dlambda2, dL/dalpha, dL/du0, dL/dw0
+ *             (partial derivatives of W at fixed u' = results[SDM_R_BINDE])
+ * Sums over replicas run in index order (deterministic).  grad_p needs
+ * reaction field (sdm_adjoint). */
+sdm_status sdm_backward_device(sdm_handle* h, const double* grad_u, const double* results, const double* forces,
+                               const double* forces1, const double* adjoint, const double* eps_displaced,
+                               const double* bias_params, double* grad_x, double* grad_d, double* grad_p,
+                               double* grad_bias, void* stream);
+
 /* Number of (replica, displaced particle) entries of the adjoint output: the
  * sum over replicas of their system's particles with a nonzero displacement
  * under the current displacement maps.  No counterpart in the reference. */

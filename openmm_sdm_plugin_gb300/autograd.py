@@ -10,8 +10,12 @@ With s = W'(u') du'/du:
 * d U / d d_i = -s F1_i for the displacement map (F1: forces at x + d);
 * d U / d x_i = -F_i (the mixed force);
 * d U / d {lambda1, lambda2, alpha, u0, w0} = partial derivatives of W at
-  fixed u' (FP64, below), from which dU/dlambda of a thermodynamic-
-  integration schedule follows by the chain rule.
+  fixed u' (FP64), from which dU/dlambda of a thermodynamic-integration
+  schedule follows by the chain rule.
+
+The backward is one library call (sdm_backward_device: one kernel, fixed-
+order FP64 sums); ``bias_partials`` and ``bias_partials_device`` below are
+the same partial derivatives in plain Python and torch, kept as references.
 
 The reference's only derivative is the non-equilibrium dW/dlambda
 (ReferenceSDMKernels.cpp:289-302, which sets dW/dalpha to 0); here dW/dalpha
@@ -149,7 +153,7 @@ class SDMEngine:
                 self.h.set_params(r, p.as_array())
 
     def run(self, x, qD, sD, eD, d, lam1, lam2, alpha, u0, w0):
-        """Forward on the device: (U, s, F, F1, G, partials) as device tensors
+        """Forward on the device: (U, s, F, F1, G, results) as device tensors
         (views of the engine's buffers: copy what must outlive the next call)."""
         self._push(qD, sD, eD, d, lam1, lam2, alpha, u0, w0)
         stream = torch.cuda.current_stream(self.dev).cuda_stream
@@ -158,10 +162,25 @@ class SDMEngine:
         self.h.state_forces_device(0, self.F1.data_ptr(), stream)
         self.h.adjoint_device(self.G.data_ptr(), stream)
         res = self.res
-        on = lambda t: t.detach().to(self.dev, torch.float64).reshape(-1)
-        part = bias_partials_device(self.methods, res[:, capi.R_BINDE], on(lam1), on(lam2), on(alpha), on(u0))
         return (res[:, capi.R_EPOT], res[:, capi.R_S], self.F.view(self.R, self.n, 3),
-                self.F1.view(self.R, self.n, 3), self.G.view(self.R, -1, 2, 3), part)
+                self.F1.view(self.R, self.n, 3), self.G.view(self.R, -1, 2, 3), res)
+
+    def backward(self, g, res, F, F1, G, eD, prm, need):
+        """All gradients from dL/dU = g (R,) in one library call
+        (sdm_backward_device) on the current stream: grad_x (R, N, 3),
+        grad_d (N, 3), grad_p (nD, 3: charge, sigma, epsilon) and the bias
+        rows (5, R: lambda1, lambda2, alpha, u0, w0).  `need` = which of
+        (x, parameters, displacement, bias) to compute; the others are None."""
+        f64 = dict(dtype=torch.float64, device=self.dev)
+        gx = torch.empty((self.R, self.n, 3), **f64) if need[0] else None
+        gp = torch.empty((len(self.D), 3), **f64) if need[1] else None
+        gd = torch.empty((self.n, 3), **f64) if need[2] else None
+        gb = torch.empty((5, self.R), **f64) if need[3] else None
+        ptr = lambda t: t.data_ptr() if t is not None else 0
+        self.h.backward_device(g.data_ptr(), res.data_ptr(), F.data_ptr(), F1.data_ptr(), G.data_ptr(),
+                               eD.data_ptr(), prm.data_ptr(), ptr(gx), ptr(gd), ptr(gp), ptr(gb),
+                               torch.cuda.current_stream(self.dev).cuda_stream)
+        return gx, gp, gd, gb
 
 
 def dataclass_copy(p):
@@ -178,27 +197,28 @@ class SDMPotential(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, engine: SDMEngine, x, qD, sD, eD, d, lam1, lam2, alpha, u0, w0):
-        U, s, F, F1, G, part = engine.run(x, qD, sD, eD, d, lam1, lam2, alpha, u0, w0)
-        ctx.save_for_backward(s.clone(), F.clone(), F1.clone(), G.clone(),
-                              eD.detach().to(engine.dev, torch.float64), *part)
+        U, s, F, F1, G, res = engine.run(x, qD, sD, eD, d, lam1, lam2, alpha, u0, w0)
+        on = lambda t: t.detach().to(engine.dev, torch.float64).reshape(-1)
+        prm = torch.stack([on(lam1), on(lam2), on(alpha), on(u0)])   # (4, R) of this evaluation
+        ctx.save_for_backward(res.clone(), F.clone(), F1.clone(), G.clone(),
+                              on(eD).contiguous(), prm)
+        ctx.engine = engine
         ctx.devs = (x.device, qD.device, d.device, lam1.device)
         return U.clone().to(x.device)
 
     @staticmethod
     def backward(ctx, gU):
-        s, F, F1, G, eD, d_l1, d_l2, d_al, d_u0, d_w0 = ctx.saved_tensors
+        res, F, F1, G, eD, prm = ctx.saved_tensors
         xdev, pdev, ddev, ldev = ctx.devs
-        g = gU.detach().to(s.device, torch.float64)
-        w = torch.stack([(1.0 - s), s], dim=1)                   # (R, 2) state weights
-        gD = torch.einsum("r,rs,rksc->kc", g, w, G)              # (nD, 3)
-        grad_q = gD[:, 0]
-        grad_s = gD[:, 1]
-        grad_e = torch.where(eD > 0, gD[:, 2] / (2.0 * eD.clamp_min(1e-300)), torch.zeros_like(eD))
-        grad_d = -torch.einsum("r,r,rnc->nc", g, s, F1)
-        grad_x = -g[:, None, None] * F
-        return (None, grad_x.to(xdev), grad_q.to(pdev), grad_s.to(pdev), grad_e.to(pdev), grad_d.to(ddev),
-                (g * d_l1).to(ldev), (g * d_l2).to(ldev), (g * d_al).to(ldev), (g * d_u0).to(ldev),
-                (g * d_w0).to(ldev))
+        n = ctx.needs_input_grad
+        need = (n[1], n[2] or n[3] or n[4], n[5], any(n[6:]))
+        g = gU.detach().to(res.device, torch.float64).contiguous()
+        gx, gp, gd, gb = ctx.engine.backward(g, res, F, F1, G, eD, prm, need)
+        col = lambda t, k, dev: t[:, k].to(dev) if t is not None else None
+        row = lambda k: gb[k].to(ldev) if gb is not None else None
+        return (None, gx.to(xdev) if gx is not None else None, col(gp, 0, pdev), col(gp, 1, pdev),
+                col(gp, 2, pdev), gd.to(ddev) if gd is not None else None,
+                row(0), row(1), row(2), row(3), row(4))
 
 
 def sdm_potential(engine: SDMEngine, x, qD, sD, eD, d, lam1, lam2, alpha, u0, w0):

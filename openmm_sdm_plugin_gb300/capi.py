@@ -44,7 +44,7 @@ EXPORTED = ("sdm_create", "sdm_destroy", "sdm_last_error", "sdm_num_replicas",
             "sdm_get_kernel_times", "sdm_autotune", "sdm_autotune_cached", "sdm_tune_key",
             "sdm_count_pairs", "sdm_get_grid",
             "sdm_export_lists", "sdm_evaluate_noalloc", "sdm_set_particle_params",
-            "sdm_adjoint", "sdm_adjoint_device", "sdm_get_num_perturbed", "sdm_set_langevin", "sdm_langevin_step", "sdm_set_restraints",
+            "sdm_adjoint", "sdm_adjoint_device", "sdm_backward_device", "sdm_get_num_perturbed", "sdm_set_langevin", "sdm_langevin_step", "sdm_set_restraints",
             "sdm_set_restraint_control", "sdm_get_restraint_energies", "sdm_set_rigid_waters",
             "sdm_gather_positions", "sdm_scatter_forces_fixed", "sdm_evaluate_engine", "sdm_get_last_results")
 
@@ -361,6 +361,16 @@ class Handle:
         """sdm_adjoint_device: the sums into a device buffer of 6 * num_perturbed()
         doubles, asynchronous on ``stream``."""
         self._check(self.lib.sdm_adjoint_device(self.h, C.c_void_p(out_ptr), C.c_void_p(stream) if stream else None))
+
+    def backward_device(self, grad_u: int, results: int, forces: int = 0, forces1: int = 0, adjoint: int = 0,
+                        eps_displaced: int = 0, bias_params: int = 0, grad_x: int = 0, grad_d: int = 0,
+                        grad_p: int = 0, grad_bias: int = 0, stream: int = 0):
+        """sdm_backward_device: gradients of the replicas' potentials from
+        dL/dU (device pointers; 0 = NULL), asynchronous on ``stream``."""
+        v = lambda p: C.c_void_p(p) if p else None
+        self._check(self.lib.sdm_backward_device(self.h, v(grad_u), v(results), v(forces), v(forces1), v(adjoint),
+                                                 v(eps_displaced), v(bias_params), v(grad_x), v(grad_d),
+                                                 v(grad_p), v(grad_bias), v(stream)))
 
     def set_langevin(self, step_size: float, friction: float, temperature: float, seed: int = 0,
                      step: int = 0):

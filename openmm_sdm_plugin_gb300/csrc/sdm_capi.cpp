@@ -24,6 +24,7 @@
 cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* grp_prefix, int* done, cudaStream_t st,
                             cudaEvent_t* ev, int nev, unsigned ev_flags);
 cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* grp_prefix, cudaStream_t st);
+cudaError_t sdm_launch_backward(const SdmArgs& a, const BwdArgs& b, cudaStream_t st);
 cudaError_t sdm_pair_prepare();
 #define SDM_MAX_CTAS 4  // pair-kernel CTAs per SM with a built register bound
 int sdm_pair_resident(int ctas_per_sm, int chunk);
@@ -872,6 +873,10 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     // replica windows
     long long xo = 0, pg = 0, ps = 0;
     int aw = 0, cw = 0, sw = 0, zw = 0;
+    for (int s = 0, r0 = 0; s < num_systems; r0 += h->sys[s].replicas, ++s) {
+        h->sys[s].dev.rep0 = r0;
+        h->sys[s].dev.nrep = h->sys[s].replicas;
+    }
     for (int s = 0; s < num_systems; ++s) {
         const SysHost& S = h->sys[s];
         const long long kp = S.dev.pme ? (long long)S.dev.pme_grid[0] * S.dev.pme_grid[1] * S.dev.pme_grid[2] : 0;
@@ -1706,6 +1711,40 @@ sdm_status sdm_adjoint(sdm_handle* h, double* out) {
     const size_t n = 3 * (size_t)h->args.total_pert;
     if (n) SDM_CUDA(h, cudaMemcpyAsync(out, h->args.adj, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     SDM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return SDM_OK;
+}
+
+sdm_status sdm_backward_device(sdm_handle* h, const double* grad_u, const double* results, const double* forces,
+                               const double* forces1, const double* adjoint, const double* eps_displaced,
+                               const double* bias_params, double* grad_x, double* grad_d, double* grad_p,
+                               double* grad_bias, void* stream) {
+    if (!h || !grad_u || !results) return SDM_ERR_INVALID_ARGUMENT;
+    if ((grad_x && !forces) || ((grad_d || grad_p) && !results) || (grad_d && !forces1) || (grad_p && !adjoint))
+        return fail(h, SDM_ERR_INVALID_ARGUMENT, "sdm_backward_device: an output lacks its input");
+    if (grad_p && h->pme) return fail(h, SDM_ERR_INVALID_ARGUMENT, "parameter derivatives are reaction-field only");
+    cudaSetDevice(h->device);
+    long long atoms = 0, nd = 0;
+    for (const SysHost& s : h->sys) {
+        atoms += s.n;
+        nd += (long long)s.D.size();
+    }
+    BwdArgs b{};
+    b.g = grad_u;
+    b.res = results;
+    b.F = forces;
+    b.F1 = forces1;
+    b.G = adjoint;
+    b.eps = eps_displaced;
+    b.prm = bias_params;
+    b.gx = grad_x;
+    b.gd = grad_d;
+    b.gp = grad_p;
+    b.gb = grad_bias;
+    b.n_x = grad_x ? 3 * (long long)h->total_particles : 0;
+    b.n_d = grad_d ? 3 * atoms : 0;
+    b.n_p = grad_p ? 3 * nd : 0;
+    b.n_b = grad_bias ? 5LL * h->nrep : 0;
+    SDM_CUDA(h, sdm_launch_backward(h->args, b, stream ? (cudaStream_t)stream : h->stream));
     return SDM_OK;
 }
 

@@ -1773,6 +1773,100 @@ __global__ void __launch_bounds__(SDM_WARPS * 32) k_adjoint(SdmArgs a) {
 }
 
 // ------------------------------------------------------------------------- //
+// Backward of U_r = U0 + W (the differentiable potential), one launch        //
+// ------------------------------------------------------------------------- //
+// Given g_r = dL/dU_r: dL/dx = -g_r F (mixed force); dL/dd_i = -sum_r g_r s_r
+// F1_ri over the replicas of i's system; the displaced particles' parameter
+// gradients sum_r g_r ((1 - s_r) G_r0 + s_r G_r1) over the adjoint sums G;
+// and g_r times the partial derivatives of W at fixed u' with respect to
+// lambda1, lambda2, alpha, u0, w0 (integrated logistic; w0 also quadratic).
+// Sums run over replicas in index order (fixed order, FP64).
+__device__ __forceinline__ int sys_by_atom(const SdmArgs& a, int i) {
+    int lo = 0, hi = a.nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.sys[mid].atom_base <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int sys_by_d(const SdmArgs& a, int k) {
+    int lo = 0, hi = a.nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.sys[mid].D_base <= k) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_backward(SdmArgs a, BwdArgs b) {
+    const long long total = b.n_x + b.n_d + b.n_p + b.n_b;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += stride) {
+        long long q = t;
+        if (q < b.n_x) {
+            const int r = rep_by_atom(a.rep, a.nrep, (int)(q / 3));
+            b.gx[q] = -b.g[r] * b.F[q];
+            continue;
+        }
+        q -= b.n_x;
+        if (q < b.n_d) {
+            const int ia = (int)(q / 3), c = (int)(q - 3LL * ia);
+            const SdmSys& S = a.sys[sys_by_atom(a, ia)];
+            const int i = ia - S.atom_base;
+            double acc = 0.0;
+            for (int r = S.rep0; r < S.rep0 + S.nrep; ++r)
+                acc = __fma_rn(b.g[r] * b.res[(size_t)r * SDM_NRESULTS + SDM_R_S],
+                               b.F1[3 * (size_t)(a.rep[r].x_off + i) + c], acc);
+            b.gd[q] = -acc;
+            continue;
+        }
+        q -= b.n_d;
+        if (q < b.n_p) {
+            const int kd = (int)(q / 3), c = (int)(q - 3LL * kd);
+            const SdmSys& S = a.sys[sys_by_d(a, kd)];
+            const int k = kd - S.D_base;
+            double acc = 0.0;
+            for (int r = S.rep0; r < S.rep0 + S.nrep; ++r) {
+                const double sw = b.res[(size_t)r * SDM_NRESULTS + SDM_R_S];
+                const size_t e = ((size_t)(a.rep[r].pert_win / 2 + k) * 2) * 3 + c;
+                acc = __fma_rn(b.g[r], __fma_rn(sw, b.G[e + 3], (1.0 - sw) * b.G[e]), acc);
+            }
+            // the third sum is 2 eps dU/deps: divided by 2 eps when eps is given
+            if (c == 2 && b.eps) acc = b.eps[kd] > 0.0 ? acc / (2.0 * b.eps[kd]) : 0.0;
+            b.gp[q] = acc;
+            continue;
+        }
+        q -= b.n_p;
+        {
+            const int k = (int)(q / a.nrep), r = (int)(q - (long long)k * a.nrep);
+            const double* p = a.params + (size_t)r * SDM_NPARAMS;
+            const int method = (int)p[SDM_P_BIAS_METHOD];
+            // lambda1, lambda2, alpha, u0 of the forward (rows of b.prm) or the handle's
+            const double l1 = b.prm ? b.prm[r] : p[SDM_P_LAMBDA1];
+            const double l2 = b.prm ? b.prm[a.nrep + r] : p[SDM_P_LAMBDA2];
+            const double al = b.prm ? b.prm[2 * a.nrep + r] : p[SDM_P_ALPHA];
+            const double u0 = b.prm ? b.prm[3 * a.nrep + r] : p[SDM_P_U0];
+            const double be = b.res[(size_t)r * SDM_NRESULTS + SDM_R_BINDE];
+            const bool ilog = method == SDM_ILOGISTIC, pos = ilog && al > 0.0;
+            double d = 0.0;
+            if (k == 4) {
+                d = (ilog || method == SDM_QUADRATIC) ? 1.0 : 0.0;
+            } else if (pos) {
+                const double e = exp(-al * (be - u0)), ee = 1.0 + e, L = log(ee);
+                const double dl = l2 - l1;
+                d = k == 0 ? -L / al
+                    : k == 1 ? L / al + be
+                    : k == 2 ? dl * (-L / (al * al) - (be - u0) * e / (al * ee))
+                             : dl * e / ee;
+            } else if (k == 1 && ilog) {
+                d = be;
+            }
+            b.gb[q] = b.g[r] * d;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------- //
 // K8: energies, soft core, bias (FP64)                                      //
 // ------------------------------------------------------------------------- //
 // ------------------------------------------------------------------------- //
@@ -2476,6 +2570,13 @@ cudaError_t sdm_launch_pair(const SdmArgs& a, const int* item_prefix, int mode, 
     } else {
         k_pair<MODE_EMIT, 3, 4><<<num_sms() * 3, 4 * 32, 4 * sizeof(EvalSmem<SDM_CH_DEFAULT>), st>>>(a, item_prefix);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t sdm_launch_backward(const SdmArgs& a, const BwdArgs& b, cudaStream_t st) {
+    const long long total = b.n_x + b.n_d + b.n_p + b.n_b;
+    if (total == 0) return cudaSuccess;
+    k_backward<<<grid_for(total, 256), 256, 0, st>>>(a, b);
     return cudaGetLastError();
 }
 

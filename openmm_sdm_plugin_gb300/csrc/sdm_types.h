@@ -78,6 +78,7 @@ struct SdmSys {
     int shift_base;   // offset into shift_tab: 3 tables of 2*Mk+1 floats (index n+Mk)
     int org_base;     // offset into cell_org: 3 tables of Mk doubles, c * g[k]
     int cx_base;      // offset into cx_off/cx_idx (changed-pair exclusions per displaced particle)
+    int rep0, nrep;   // the system's replicas: rep0 .. rep0+nrep-1 (replicas are numbered system by system)
     int half_geo;     // 1: pairs of columns are owned through the forward half stencil
                       // (offset ox>0, or ox==0 and oy>0; own column J>=I); 0: by lower column id
     int excl_clique;  // 1: every exclusion component is a clique (excluded <=> same molecule id)
@@ -272,4 +273,21 @@ struct SdmArgs {
     int total_ex;        // sum of ex_count over replicas
     int total_xc;        // sum of xc_count over replicas
     int split;           // work items per i-cluster
+};
+
+// Backward of the differentiable potential (k_backward): inputs of the
+// forward, the upstream gradient and the outputs wanted (n_* = 0: skipped)
+struct BwdArgs {
+    const double* g;        // [nrep] dL/dU_r
+    const double* res;      // [nrep * SDM_NRESULTS] results of the forward
+    const double* F;        // mixed forces [3 * total particles]
+    const double* F1;       // state-1 forces [3 * total particles]
+    const double* G;        // adjoint sums [6 * perturbed]
+    const double* eps;      // FP64 epsilon of the displaced particles [sum nD], or null
+    const double* prm;      // [4 * nrep] lambda1, lambda2, alpha, u0 rows, or null (the handle's)
+    double* gx;             // [3 * total particles]
+    double* gd;             // [3 * sum of the systems' particles]
+    double* gp;             // [3 * sum nD]: charge, sigma, epsilon
+    double* gb;             // [5 * nrep]: lambda1, lambda2, alpha, u0, w0 rows
+    long long n_x, n_d, n_p, n_b;
 };

@@ -15,6 +15,7 @@ import torch
 import oracle
 from dense_sdm import candidate_pairs, potential
 from openmm_sdm_plugin_gb300 import systems as S
+from openmm_sdm_plugin_gb300 import capi
 from openmm_sdm_plugin_gb300.autograd import bias_partials
 
 GRAD_REL_TOL = 2e-4   # gradient vs FP64 reference: FP32 pair terms, FP64 sums
@@ -242,3 +243,45 @@ def test_num_perturbed_follows_the_displacement_rule_and_device_adjoint_matches(
     with pytest.raises(ValueError):
         h.adjoint(n_displaced=nd)
     h.close()
+
+
+@pytest.mark.gpu
+def test_library_backward_matches_torch_formulas():
+    """sdm_backward_device (one kernel) against the same gradients written as
+    torch operations on the forward's outputs: three lambda states (every
+    bias method), random upstream gradients, all outputs at 1e-12; outputs
+    that are not wanted are skipped."""
+    from openmm_sdm_plugin_gb300.autograd import SDMEngine, bias_partials_device
+    s = S.host_guest(1500, seed=5, nstates=3)
+    for r, m in enumerate((0, 1, 2)):
+        s.params[r] = dataclasses.replace(s.params[r], bias_method=m, alpha=0.05 * (r + 1), u0=20.0 * r)
+    eng = SDMEngine(s)
+    dev = eng.dev
+    f64 = dict(dtype=torch.float64, device=dev)
+    D = eng.D
+    x = torch.tensor(s.positions, **f64)
+    vec = lambda k: torch.tensor([getattr(p, k) for p in s.params], **f64)
+    lam = [vec(k) for k in ("lambda1", "lambda2", "alpha", "u0", "w0")]
+    qD, sD, eD = (torch.tensor(a[D], **f64) for a in (s.charge, s.sigma, s.epsilon))
+    d = torch.tensor(s.displacement, **f64)
+    U, sw, F, F1, G, res = eng.run(x, qD, sD, eD, d, *lam)
+    res, F, F1, G = res.clone(), F.clone(), F1.clone(), G.clone()
+    prm = torch.stack(lam[:4])
+    g = torch.randn(eng.R, **f64)
+    gx, gp, gd, gb = eng.backward(g, res, F, F1, G, eD, prm, (True, True, True, True))
+    torch.cuda.synchronize()
+    s_ = res[:, capi.R_S]
+    w = torch.stack([(1.0 - s_), s_], dim=1)
+    gD = torch.einsum("r,rs,rksc->kc", g, w, G)
+    ref_e = torch.where(eD > 0, gD[:, 2] / (2.0 * eD), torch.zeros_like(eD))
+    part = bias_partials_device(eng.methods, res[:, capi.R_BINDE], *lam[:4])
+    close = lambda a, b: torch.allclose(a, b, rtol=1e-12, atol=1e-12 * float(b.abs().max() + 1e-300))
+    assert close(gx, -g[:, None, None] * F)
+    assert close(gd, -torch.einsum("r,r,rnc->nc", g, s_, F1))
+    assert close(gp[:, 0], gD[:, 0]) and close(gp[:, 1], gD[:, 1]) and close(gp[:, 2], ref_e)
+    for k in range(5):
+        assert close(gb[k], g * part[k]), k
+    # nothing requested but the bias rows
+    gx2, gp2, gd2, gb2 = eng.backward(g, res, F, F1, G, eD, prm, (False, False, False, True))
+    assert gx2 is None and gp2 is None and gd2 is None and torch.equal(gb2, gb)
+    eng.close()
