@@ -192,7 +192,11 @@ sdm_status sdm_evaluate(sdm_handle* h, const double* x, double* results, double*
  * the handle's own stream).  x/results/forces are device pointers with the
  * sizes of sdm_evaluate.  With graph mode on (default), the launch sequence is
  * captured once per distinct (x, results, forces, stream) tuple and replayed
- * as a CUDA graph. */
+ * as a CUDA graph.  The default streams (cudaStreamLegacy, cudaStreamPerThread)
+ * cannot be captured: given one of them, the call runs on the handle's own
+ * stream, ordered after the caller's earlier work on it and before its later
+ * work (two event edges); the same holds for every entry point below that
+ * takes a stream and evaluates (sdm_langevin_step, sdm_evaluate_engine). */
 sdm_status sdm_evaluate_device(sdm_handle* h, const double* x, double* results, double* forces,
                                void* stream);
 

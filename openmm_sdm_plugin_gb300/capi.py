@@ -90,6 +90,14 @@ _lock = threading.Lock()
 _lib = None
 
 
+def _stream(stream: int):
+    """A torch ``cuda_stream`` value as the ABI's stream argument: torch's
+    default stream has the handle 0, which is CUDA's legacy default stream
+    (cudaStreamLegacy), not the ABI's NULL (the handle's own stream, which is
+    not ordered with the caller's default-stream work)."""
+    return C.c_void_p(stream if stream else 1)
+
+
 def load_library(path: str = LIB_PATH):
     """Loads (once) and returns the CDLL with argument types declared."""
     global _lib
@@ -360,7 +368,7 @@ class Handle:
     def adjoint_device(self, out_ptr: int, stream: int = 0):
         """sdm_adjoint_device: the sums into a device buffer of 6 * num_perturbed()
         doubles, asynchronous on ``stream``."""
-        self._check(self.lib.sdm_adjoint_device(self.h, C.c_void_p(out_ptr), C.c_void_p(stream) if stream else None))
+        self._check(self.lib.sdm_adjoint_device(self.h, C.c_void_p(out_ptr), _stream(stream)))
 
     def backward_device(self, grad_u: int, results: int, forces: int = 0, forces1: int = 0, adjoint: int = 0,
                         eps_displaced: int = 0, bias_params: int = 0, grad_x: int = 0, grad_d: int = 0,
@@ -370,7 +378,7 @@ class Handle:
         v = lambda p: C.c_void_p(p) if p else None
         self._check(self.lib.sdm_backward_device(self.h, v(grad_u), v(results), v(forces), v(forces1), v(adjoint),
                                                  v(eps_displaced), v(bias_params), v(grad_x), v(grad_d),
-                                                 v(grad_p), v(grad_bias), v(stream)))
+                                                 v(grad_p), v(grad_bias), _stream(stream)))
 
     def set_langevin(self, step_size: float, friction: float, temperature: float, seed: int = 0,
                      step: int = 0):
@@ -384,7 +392,7 @@ class Handle:
                                                C.c_void_p(inv_mass_ptr),
                                                C.c_void_p(f_extra_ptr) if f_extra_ptr else None,
                                                C.c_void_p(res_ptr), int(nsteps),
-                                               C.c_void_p(stream) if stream else None))
+                                               _stream(stream)))
 
     def evaluate(self, x, forces: bool = True):
         """Host evaluation of all replicas. x: (total_particles, 3) float64."""
@@ -405,7 +413,7 @@ class Handle:
     def evaluate_device(self, x_ptr: int, res_ptr: int, f_ptr: int = 0, stream: int = 0):
         self._check(self.lib.sdm_evaluate_device(self.h, C.c_void_p(x_ptr), C.c_void_p(res_ptr),
                                                  C.c_void_p(f_ptr) if f_ptr else None,
-                                                 C.c_void_p(stream) if stream else None))
+                                                 _stream(stream)))
 
     def state_forces(self):
         F0 = np.zeros(3 * self.total_particles)
@@ -418,7 +426,7 @@ class Handle:
         device buffers, asynchronous on ``stream``."""
         self._check(self.lib.sdm_get_state_forces_device(self.h, C.c_void_p(F0_ptr) if F0_ptr else None,
                                                          C.c_void_p(F1_ptr) if F1_ptr else None,
-                                                         C.c_void_p(stream) if stream else None))
+                                                         _stream(stream)))
 
     def check_status(self) -> int:
         v = C.c_int(0)
@@ -479,7 +487,7 @@ def evaluate_noalloc(n, x_ptr, q_ptr, sig_ptr, eps_ptr, eoff_ptr, eidx_ptr, d_pt
                                 C.c_void_p(d_ptr) if d_ptr else None, b.ctypes.data,
                                 float(cutoff), float(eps_rf), p.ctypes.data, C.c_void_p(res_ptr),
                                 C.c_void_p(f_ptr) if f_ptr else None,
-                                C.c_void_p(stream) if stream else None)
+                                _stream(stream))
     if st != SDM_OK:
         raise SdmError(st, L.sdm_last_error(None).decode())
 

@@ -134,6 +134,7 @@ struct sdm_handle {
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;          // second branch of an evaluation (perturbation pass)
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaEvent_t bridge_ev[2] = {};         // special caller streams: into and out of the handle's stream
     SdmArgs args{};
     int* item_prefix = nullptr;
     int* grp_prefix = nullptr;   // list-building groups over replicas (k_jlist items)
@@ -716,6 +717,17 @@ sdm_status flush_langevin(sdm_handle* h, cudaStream_t st) {
 
 sdm_status run(sdm_handle* h, const double* x, double* res, double* f, cudaStream_t st, int mode,
                bool allow_graph, const LvBind* lv = nullptr) {
+    if (st == cudaStreamLegacy || st == cudaStreamPerThread) {
+        // the default streams cannot be captured into a graph: the call runs
+        // on the handle's stream, after the caller's earlier work on `st` and
+        // before its later work
+        SDM_CUDA(h, cudaEventRecord(h->bridge_ev[0], st));
+        SDM_CUDA(h, cudaStreamWaitEvent(h->stream, h->bridge_ev[0], 0));
+        const sdm_status s = run(h, x, res, f, h->stream, mode, allow_graph, lv);
+        SDM_CUDA(h, cudaEventRecord(h->bridge_ev[1], h->stream));
+        SDM_CUDA(h, cudaStreamWaitEvent(st, h->bridge_ev[1], 0));
+        return s;
+    }
     if (!h->jl_buf) {   // a failed regrow left no lists: allocate the last capacity again
         sdm_status s0 = sdm_reserve_lists(h, h->jl_cap);
         if (s0) return s0;
@@ -1003,6 +1015,8 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     ce = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming);
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->bridge_ev[0], cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->bridge_ev[1], cudaEventDisableTiming);
     if (ce != cudaSuccess) { cuda_fail(h, ce, "cudaStreamCreate(side)"); return bail(SDM_ERR_CUDA); }
     ce = cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
     if (ce != cudaSuccess) { cuda_fail(h, ce, "cudaMemset(arena)"); return bail(SDM_ERR_CUDA); }
@@ -1173,6 +1187,7 @@ sdm_status sdm_destroy(sdm_handle* h) {
     if (h->side) { cudaStreamSynchronize(h->side); cudaStreamDestroy(h->side); }
     if (h->fork_ev) cudaEventDestroy(h->fork_ev);
     if (h->join_ev) cudaEventDestroy(h->join_ev);
+    for (cudaEvent_t e : h->bridge_ev) if (e) cudaEventDestroy(e);
     if (h->arena) cudaFree(h->arena);
     if (h->params_pinned) cudaFreeHost(h->params_pinned);
     delete h;

@@ -1569,6 +1569,8 @@ __device__ __forceinline__ bool adj_excluded(const AdjSmem& sm, const SdmArgs& a
     return e;
 }
 
+// One adjoint item (replica, displaced particle, state) per warp: every
+// partner of the particle in that state
 template <bool IMG>
 __device__ void process_adjoint(const SdmArgs& a, int r, int local, AdjSmem& sm) {
     const int lane = lane_id();
@@ -1577,17 +1579,12 @@ __device__ void process_adjoint(const SdmArgs& a, int r, int local, AdjSmem& sm)
     const int pidx = local >> 1, st = local & 1;
     const int p = a.D_idx[S.D_base + pidx];
     const int tp = S.atom_base + p;
-    double y[3];
-    int cy[3];
-    float o[3];
-    const double* wp = a.w + 3 * (size_t)(R.atom_win + p);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const double v = st ? __dadd_rn(wp[k], a.topo_d[3 * (size_t)tp + k]) : wp[k];
-        y[k] = wrap1(v, S.box[k], S.invL[k]);
-        cy[k] = cell_of(y[k], S.invg[k], S.M[k]);
-        o[k] = __double2float_rn(__dsub_rn(y[k], __dmul_rn((double)cy[k], S.g[k])));
-    }
+    // the particle's position in this state, as the evaluation's k_pert_prep
+    // computed it (the adjoint differentiates that evaluation)
+    const SdmPertPos pp = a.pert_pos[R.pert_win + local];
+    const double y[3] = {pp.y[0], pp.y[1], pp.y[2]};
+    const int cy[3] = {pp.cy[0], pp.cy[1], pp.cy[2]};
+    const float o[3] = {pp.o[0], pp.o[1], pp.o[2]};
     const float hp = a.topo_hs[tp], sp_ = a.topo_se[tp];
     const int eb = a.excl_off[tp], ne = a.excl_off[tp + 1] - eb;
     __syncwarp();
@@ -1600,6 +1597,16 @@ __device__ void process_adjoint(const SdmArgs& a, int r, int local, AdjSmem& sm)
     const float* tabz = taby + 2 * S.M[1] + 1;
     const int nst = S.fst_count;
     const int* colcl = a.col_cl + R.col_win;
+    // z window of the point (absolute, conservative) and its pieces inside
+    // [0, Lz): the clusters of a column outside it are beyond the cutoff
+    const float2* zb = a.cl_zb + R.cl_win;
+    const float zq = __double2float_rn(y[2]);
+    const float ZA = zq - rclc - 1.0e-4f, ZB = zq + rclc + 1.0e-4f;
+    const float Lz = S.Lf[2];
+    const bool wholez = IMG || (ZB - ZA >= Lz);
+    float za1 = fmaxf(ZA, 0.0f), zb1 = fminf(ZB, Lz), za2 = 1.0f, zb2 = 0.0f;  // empty 2nd piece
+    if (ZA < 0.0f) { za2 = ZA + Lz; zb2 = Lz; }
+    else if (ZB > Lz) { za2 = 0.0f; zb2 = ZB - Lz; }
     const float sqrtK = 11.787089759563214f;
     double gq = 0.0, gs = 0.0, ge = 0.0;
     int jl_n = 0;
@@ -1646,7 +1653,7 @@ __device__ void process_adjoint(const SdmArgs& a, int r, int local, AdjSmem& sm)
 
     for (int k0 = 0; k0 < nst; k0 += 32) {
         const int k = k0 + lane;
-        int cntJ = 0, Jb = 0;
+        int cntJ = 0, Jb = 0, cnt2 = 0, Jb2 = 0;
         float Sx = 0.f, Sy = 0.f;
         if (k < nst) {
             const int2 off = a.stencil[S.fst_base + k];
@@ -1664,24 +1671,44 @@ __device__ void process_adjoint(const SdmArgs& a, int r, int local, AdjSmem& sm)
                 ok = gx * gx + gy * gy < rclc2;
             }
             if (ok) {
-                Jb = colcl[colid];
-                cntJ = max(colcl[colid + 1] - Jb, 0);
+                const int lo = colcl[colid], hi = colcl[colid + 1];
+                if (wholez) {
+                    Jb = lo;
+                    cntJ = hi - lo;
+                } else {
+                    Jb = lower_zhi(zb, lo, hi, za1);
+                    cntJ = upper_zlo(zb, Jb, hi, zb1) - Jb;
+                    if (za2 <= zb2) {
+                        Jb2 = lower_zhi(zb, lo, hi, za2);
+                        cnt2 = upper_zlo(zb, Jb2, hi, zb2) - Jb2;
+                        // the two pieces are disjoint in z; clusters are counted once
+                        if (cnt2 > 0 && cntJ > 0 && Jb2 < Jb + cntJ && Jb2 + cnt2 > Jb) {
+                            const int u0 = min(Jb, Jb2), u1 = max(Jb + cntJ, Jb2 + cnt2);
+                            Jb = u0; cntJ = u1 - u0; cnt2 = 0;
+                        }
+                    }
+                }
+                cntJ = max(cntJ, 0);
+                cnt2 = max(cnt2, 0);
             }
         }
-        const bool has = cntJ > 0;
-        const unsigned hb = __ballot_sync(0xffffffffu, has);
-        int incl = cntJ;
+        // up to two cluster ranges per column, in lane order
+        const bool h1 = cntJ > 0, h2 = cnt2 > 0;
+        const unsigned hb1 = __ballot_sync(0xffffffffu, h1), hb2 = __ballot_sync(0xffffffffu, h2);
+        int incl = cntJ + cnt2;
 #pragma unroll
         for (int oo = 1; oo < 32; oo <<= 1) {
             const int v = __shfl_up_sync(0xffffffffu, incl, oo);
             if (lane >= oo) incl += v;
         }
         const int total = __shfl_sync(0xffffffffu, incl, 31);
-        if (has) {
-            const int ri = __popc(hb & ((1u << lane) - 1u));
-            sm.rng[ri] = make_int4(Jb, incl - cntJ, __float_as_int(Sx), __float_as_int(Sy));
+        {
+            const unsigned lt = (1u << lane) - 1u;
+            const int ri = __popc(hb1 & lt) + __popc(hb2 & lt);
+            if (h1) sm.rng[ri] = make_int4(Jb, incl - cntJ - cnt2, __float_as_int(Sx), __float_as_int(Sy));
+            if (h2) sm.rng[ri + (h1 ? 1 : 0)] = make_int4(Jb2, incl - cnt2, __float_as_int(Sx), __float_as_int(Sy));
         }
-        const int nr = __popc(hb);
+        const int nr = __popc(hb1) + __popc(hb2);
         __syncwarp();
         for (int e0 = 0; e0 < total; e0 += 32) {
             const int e = e0 + lane;
@@ -1728,12 +1755,11 @@ __device__ void process_adjoint(const SdmArgs& a, int r, int local, AdjSmem& sm)
             const int qa = a.D_idx[S.D_base + qi];
             if (qa != p) {
                 const int tq = S.atom_base + qa;
-                const double* wq = a.w + 3 * (size_t)(R.atom_win + qa);
+                const SdmPertPos& pq = a.pert_pos[R.pert_win + 2 * qi + st];
                 float d[3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    const double vq = st ? __dadd_rn(wq[k], a.topo_d[3 * (size_t)tq + k]) : wq[k];
-                    const double yq = wrap1(vq, S.box[k], S.invL[k]);
+                    const double yq = pq.y[k];
                     double v = __dsub_rn(yq, y[k]);
                     const double tt = rint(__dmul_rn(v, S.invL[k]));
                     v = __dsub_rn(v, __dmul_rn(tt, S.box[k]));
@@ -2651,7 +2677,7 @@ cudaError_t sdm_launch_scatter_forces(const double* f, const int* index, int n, 
 cudaError_t sdm_launch_adjoint(const SdmArgs& a, cudaStream_t st) {
     if (a.total_pert == 0) return cudaSuccess;
     int grid = (a.total_pert + SDM_WARPS - 1) / SDM_WARPS;
-    const int cap = num_sms() * 4;
+    const int cap = num_sms() * 8;
     if (grid > cap) grid = cap;
     k_adjoint<<<grid, SDM_WARPS * 32, 0, st>>>(a);
     return cudaGetLastError();

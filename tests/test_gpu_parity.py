@@ -390,3 +390,29 @@ def test_pair_schedule_options():
     for bad in (0, 5):
         with pytest.raises(capi.SdmError):
             h.set_option(capi.OPT_CTAS_PER_SM, bad)
+
+
+def test_default_stream_calls_are_ordered_with_torch():
+    """On torch's default stream (cuda_stream 0, CUDA's legacy stream) the
+    device calls are ordered with the caller's work: coordinates written by a
+    torch copy just before the call are the ones evaluated, and results read
+    by torch just after are the call's (the call bridges to the handle's
+    stream with two event edges; no explicit synchronisation here)."""
+    import torch
+    s = S.config2(nrep=3)
+    h = _handle([s])
+    x = np.ascontiguousarray(s.positions.reshape(-1, 3))
+    ref_res, ref_F = h.evaluate(x)
+    xh = torch.from_numpy(x).pin_memory()
+    xd = torch.zeros_like(xh, device="cuda")
+    rd = torch.zeros((h.nrep, capi.NRESULTS), dtype=torch.float64, device="cuda")
+    fd = torch.zeros_like(xd)
+    assert torch.cuda.current_stream().cuda_stream == 0
+    for k in range(6):
+        xd.zero_()
+        rd.zero_()
+        xd.copy_(xh, non_blocking=True)           # default stream
+        h.evaluate_device(xd.data_ptr(), rd.data_ptr(), fd.data_ptr(), 0)
+        got = rd.cpu().numpy()                     # default stream, then host
+        assert np.array_equal(got[:, :capi.R_STATUS], ref_res[:, :capi.R_STATUS]), k
+        assert np.array_equal(fd.cpu().numpy(), ref_F), k
