@@ -285,3 +285,79 @@ def test_library_backward_matches_torch_formulas():
     gx2, gp2, gd2, gb2 = eng.backward(g, res, F, F1, G, eD, prm, (False, False, False, True))
     assert gx2 is None and gp2 is None and gd2 is None and torch.equal(gb2, gb)
     eng.close()
+
+
+@pytest.mark.gpu
+def test_backward_device_two_systems_against_numpy():
+    """sdm_backward_device on a handle of two systems (3 and 2 lambda states,
+    different sizes and ligands): every output against the same sums in
+    numpy from the evaluation's results, forces, state forces and adjoint
+    sums; per-system displacement and parameter gradients over that system's
+    replicas only."""
+    from openmm_sdm_plugin_gb300.autograd import bias_partials
+    sysms = [S.host_guest(1500, seed=5, nstates=3), S.host_guest(2200, seed=7, nstates=2)]
+    h = capi.Handle(sysms)
+    r = 0
+    for s_ in sysms:
+        for p in s_.params:
+            h.set_params(r, p.as_array())
+            r += 1
+    R = h.nrep
+    f64 = dict(dtype=torch.float64, device="cuda")
+    x = torch.from_numpy(np.concatenate([s_.positions.reshape(-1, 3) for s_ in sysms])).to(**f64)
+    res = torch.zeros((R, capi.NRESULTS), **f64)
+    F = torch.zeros_like(x)
+    F1 = torch.zeros_like(x)
+    npert = h.num_perturbed()
+    G = torch.zeros(6 * npert, **f64)
+    st = torch.cuda.Stream()
+    s0 = st.cuda_stream
+    h.evaluate_device(x.data_ptr(), res.data_ptr(), F.data_ptr(), s0)
+    h.state_forces_device(0, F1.data_ptr(), s0)
+    h.adjoint_device(G.data_ptr(), s0)
+    Ds = [np.nonzero(np.any(np.asarray(s_.displacement).reshape(-1, 3) != 0, axis=1))[0] for s_ in sysms]
+    eps = torch.from_numpy(np.concatenate([s_.epsilon[D] for s_, D in zip(sysms, Ds)])).to(**f64)
+    g = torch.randn(R, **f64)
+    natoms = sum(s_.n for s_ in sysms)
+    gx = torch.empty_like(x)
+    gd = torch.empty((natoms, 3), **f64)
+    gp = torch.empty((eps.numel(), 3), **f64)
+    gb = torch.empty((5, R), **f64)
+    h.backward_device(g.data_ptr(), res.data_ptr(), F.data_ptr(), F1.data_ptr(), G.data_ptr(), eps.data_ptr(), 0,
+                      gx.data_ptr(), gd.data_ptr(), gp.data_ptr(), gb.data_ptr(), s0)
+    torch.cuda.synchronize()
+    res_, F_, F1_, G_, g_ = (t.cpu().numpy() for t in (res, F, F1, G, g))
+    gx_, gd_, gp_, gb_ = (t.cpu().numpy() for t in (gx, gd, gp, gb))
+    sw = res_[:, capi.R_S]
+    close = lambda a, b: np.allclose(a, b, rtol=1e-12, atol=1e-12 * (np.abs(b).max() + 1e-300))
+    # rows of every replica, replicas numbered system by system
+    row, r, rep_rows, rep_sys = 0, 0, [], []
+    for k, s_ in enumerate(sysms):
+        for q in range(s_.replicas):
+            rep_rows.append(slice(row, row + s_.n))
+            rep_sys.append(k)
+            row += s_.n
+    for q in range(R):
+        assert close(gx_[rep_rows[q]], -g_[q] * F_[rep_rows[q]])
+    Gq = G_.reshape(-1, 2, 3)
+    d0, a0, p0 = 0, 0, 0
+    for k, (s_, D) in enumerate(zip(sysms, Ds)):
+        reps = [q for q in range(R) if rep_sys[q] == k]
+        ref_d = -sum(g_[q] * sw[q] * F1_[rep_rows[q]] for q in reps)
+        assert close(gd_[a0:a0 + s_.n], ref_d), k
+        ref_p = np.zeros((len(D), 3))
+        for q in reps:
+            off = sum(len(Ds[rep_sys[qq]]) for qq in range(q))
+            ref_p += g_[q] * ((1 - sw[q]) * Gq[off:off + len(D), 0] + sw[q] * Gq[off:off + len(D), 1])
+        ref_p[:, 2] = np.where(s_.epsilon[D] > 0, ref_p[:, 2] / (2 * s_.epsilon[D]), 0.0)
+        assert close(gp_[p0:p0 + len(D)], ref_p), k
+        a0 += s_.n
+        p0 += len(D)
+    q = 0
+    for s_ in sysms:
+        for p in s_.params:
+            ref = bias_partials(p, res_[q, capi.R_BINDE])
+            for kk, key in enumerate(("lambda1", "lambda2", "alpha", "u0", "w0")):
+                assert gb_[kk, q] == pytest.approx(g_[q] * ref[key], rel=1e-12, abs=1e-12), (q, key)
+            q += 1
+    h.close()
