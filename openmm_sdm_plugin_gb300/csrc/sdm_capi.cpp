@@ -65,7 +65,7 @@ struct SysHost {
     std::vector<int> cx_idx;
     std::vector<int2> hst, fst;  // owner / full column stencils
     std::vector<int2> ex_pair;   // exceptions (local indices)
-    std::vector<double4> ex_prm; // (K qq, sigma, 4 eps, 0)
+    std::vector<double4_16a> ex_prm; // (K qq, sigma, 4 eps, 0)
     std::vector<int2> xc_pair;   // PME: excluded pairs i < j and K q_i q_j
     std::vector<float> xc_qq;
     std::vector<float> theta;    // PME: Ewald kernel x B-spline moduli, half spectrum
@@ -315,7 +315,7 @@ std::string setup_system(const sdm_system_desc& d, SysHost& s) {
         if (!std::isfinite(qq) || !std::isfinite(sg) || !std::isfinite(ep) || ep < 0.0)
             return "invalid exception parameters";
         s.ex_pair.push_back(make_int2(a, b));
-        s.ex_prm.push_back(make_double4(kCoulomb * qq, sg, 4.0 * ep, 0.0));
+        s.ex_prm.push_back(make_double4_16a(kCoulomb * qq, sg, 4.0 * ep, 0.0));
     }
     // grid
     SdmSys& g = s.dev;
@@ -529,7 +529,7 @@ sdm_status upload_topology(sdm_handle* h) {
     std::vector<float> tab;
     std::vector<int4> ex4;
     std::vector<int2> sten, exp_, xcp;
-    std::vector<double4> exq;
+    std::vector<double4_16a> exq;
     std::vector<float> xcq, th;
     std::vector<SdmSys> sd;
     int atom = 0, excl = 0, dbase = 0, cxbase = 0, tabbase = 0, orgbase = 0;
@@ -619,7 +619,7 @@ sdm_status upload_topology(sdm_handle* h) {
     if ((st = put(a.stencil, sten.data(), sten.size() * sizeof(int2)))) return st;
     if (!exp_.empty()) {
         if ((st = put(a.ex_pair, exp_.data(), exp_.size() * sizeof(int2)))) return st;
-        if ((st = put(a.ex_prm, exq.data(), exq.size() * sizeof(double4)))) return st;
+        if ((st = put(a.ex_prm, exq.data(), exq.size() * sizeof(double4_16a)))) return st;
     }
     if (!xcp.empty()) {
         if ((st = put(a.xc_pair, xcp.data(), xcp.size() * sizeof(int2)))) return st;
@@ -956,7 +956,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_grp = ar.take<int>(tot_n), o_d = ar.take<double>(3LL * tot_n);
     const size_t o_mol = ar.take<int>(tot_n), o_ex4t = ar.take<int4>(tot_n);
     const size_t o_org = ar.take<double>(std::max(tot_org, 1));
-    const size_t o_exp = ar.take<int2>(std::max(tot_expair, 1)), o_exq = ar.take<double4>(std::max(tot_expair, 1));
+    const size_t o_exp = ar.take<int2>(std::max(tot_expair, 1)), o_exq = ar.take<double4_16a>(std::max(tot_expair, 1));
     const size_t o_exe = ar.take<double>(std::max(tot_exitem, 1LL)), o_exu = ar.take<double>(std::max(tot_exitem, 1LL));
     const size_t o_xcp = ar.take<int2>(std::max(tot_xcpair, 1LL)), o_xcq = ar.take<float>(std::max(tot_xcpair, 1LL));
     int max_xc = 0;
@@ -1034,7 +1034,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.topo_ex4 = at<int4>(B, o_ex4t);
     a.cell_org = at<double>(B, o_org);
     a.ex_pair = at<int2>(B, o_exp);
-    a.ex_prm = at<double4>(B, o_exq);
+    a.ex_prm = at<double4_16a>(B, o_exq);
     a.ex_e0 = at<double>(B, o_exe);
     a.ex_du = at<double>(B, o_exu);
     a.xc_pair = at<int2>(B, o_xcp);

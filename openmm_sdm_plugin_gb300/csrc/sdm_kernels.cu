@@ -1902,7 +1902,7 @@ __global__ void k_backward(SdmArgs a, BwdArgs b) {
 // coordinates (no cutoff, no reaction field, no periodic image), FP64; both
 // states when the two displacements differ.  One thread per (replica,
 // exception); forces enter the fixed-point F0 / dF of the two slots.
-__device__ __forceinline__ void ex_terms(const double4 p, double dx, double dy, double dz, double& e, double& fs) {
+__device__ __forceinline__ void ex_terms(const double4_16a p, double dx, double dy, double dz, double& e, double& fs) {
     const double r2 = dx * dx + dy * dy + dz * dz;
     const double ir2 = 1.0 / r2, ir = sqrt(ir2);
     const double s2 = p.y * p.y * ir2, s6 = s2 * s2 * s2, s12 = s6 * s6;
@@ -1927,7 +1927,7 @@ __global__ void k_except(SdmArgs a) {
     const SdmSys& S = a.sys[R.sys];
     const int e = item - R.ex_win;
     const int2 pr = a.ex_pair[S.ex_base + e];
-    const double4 prm = a.ex_prm[S.ex_base + e];
+    const double4_16a prm = a.ex_prm[S.ex_base + e];
     const double* xi = a.x + 3 * (R.x_off + pr.x);
     const double* xj = a.x + 3 * (R.x_off + pr.y);
     const double* di = a.topo_d + 3 * (size_t)(S.atom_base + pr.x);
@@ -2662,7 +2662,7 @@ cudaError_t sdm_launch_gather_positions(const void* posq, const void* corr, int 
                                         const int* index, int n, double* x, cudaStream_t st) {
     const int grid = grid_for(n, 256);
     if (double_precision)
-        k_gather_posq<double4><<<grid, 256, 0, st>>>((const double4*)posq, (const double4*)corr, index, n, x);
+        k_gather_posq<double4_16a><<<grid, 256, 0, st>>>((const double4_16a*)posq, (const double4_16a*)corr, index, n, x);
     else
         k_gather_posq<float4><<<grid, 256, 0, st>>>((const float4*)posq, (const float4*)corr, index, n, x);
     return cudaGetLastError();

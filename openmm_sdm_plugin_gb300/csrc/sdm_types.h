@@ -158,7 +158,7 @@ struct SdmArgs {
     const int4* topo_ex4; // up to 4 exclusion partners (system-local; -1 none, -2 more than 4)
     const double* topo_d;
     const int2* ex_pair;    // exceptions (system-local particle indices)
-    const double4* ex_prm;  // (K qq, sigma, 4 eps, 0)
+    const double4_16a* ex_prm;  // (K qq, sigma, 4 eps, 0)
     const int2* xc_pair;    // PME: excluded pairs (i < j, system-local) ...
     const float* xc_qq;     // ... and their K q_i q_j
     const int* excl_off;
