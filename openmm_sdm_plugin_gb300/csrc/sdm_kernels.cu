@@ -2196,9 +2196,21 @@ __global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
 // fixed point 2^32 -> double: one conversion, the scale applied to the
 // exponent field (exact: every nonzero value is >= 1 before scaling)
 __device__ __forceinline__ double fix_to_double(unsigned long long v) {
-    const double d = (double)(long long)v;
+    // the conversion (double)(long long)v / 2^32 in integer arithmetic (the
+    // integer-to-FP64 conversion runs on GB300's narrow FP64 pipe): the
+    // magnitude normalised by its leading zeros, 52 mantissa bits rounded to
+    // nearest, ties to even, as the conversion rounds; the exponent field
+    // carries the 2^-32 scale (every nonzero value stays normal)
     if (v == 0ull) return 0.0;
-    return __hiloint2double(__double2hiint(d) - (32 << 20), __double2loint(d));
+    const unsigned long long sign = v & 0x8000000000000000ull;
+    unsigned long long m = sign ? (0ull - v) : v;        // |v| (2^63 for the most negative value)
+    const int lz = __clzll((long long)m);
+    m <<= lz;                                             // leading one at bit 63
+    const unsigned long long mant = (m >> 11) & 0x000FFFFFFFFFFFFFull;
+    const unsigned long long rest = m & 0x7FFull;         // the 11 bits below the mantissa
+    unsigned long long bits = ((unsigned long long)(63 - lz + 1023 - 32) << 52) | mant;
+    if (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) bits += 1ull;   // a carry moves into the exponent
+    return __longlong_as_double((long long)(sign | bits));
 }
 
 __global__ void k_mix(SdmArgs a) {
