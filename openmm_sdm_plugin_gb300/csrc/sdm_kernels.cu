@@ -14,8 +14,10 @@
 //   k_pert_prep the displaced particles' positions in both states
 //   k_perturb   perturbation pass: only pairs whose displacements differ, at
 //               both states -> u (FP64) and dF = F1 - F0 (fixed point)
-//   k_finalize  deterministic energy reductions, soft core, bias, weight s
-//   k_mix       F = F0 + s dF in original particle order
+//   k_finalize_mix  deterministic energy reductions, soft core, bias,
+//               weight s, then F = F0 + s dF in original particle order
+//               (k_langevin: the same reductions and combine, then the
+//               stochastic-dynamics update; k_mix: the state forces)
 //
 // Reference correspondence: the two nonbonded evaluations of
 // openmmapi/src/LangevinIntegratorSDM.cpp:158-176 (OpenMM NonbondedForce at x
@@ -2184,11 +2186,6 @@ __device__ void finalize_replica(const SdmArgs& a, int r, double* red, double* s
     o[SDM_R_RESERVED] = (double)ncl;
 }
 
-__global__ void __launch_bounds__(256) k_finalize(SdmArgs a) {
-    __shared__ double red[256];
-    __shared__ double s;
-    finalize_replica(a, blockIdx.x, red, &s, true);
-}
 
 // ------------------------------------------------------------------------- //
 // K9: mix                                                                   //
@@ -2298,27 +2295,39 @@ __device__ __forceinline__ float2 lv_normals(unsigned long long seed, unsigned l
     return make_float2(r * cs, r * sn);
 }
 
-__global__ void k_langevin(SdmArgs a) {
-    const int stride = gridDim.x * blockDim.x;
+// Finalize and the stochastic-dynamics update in one launch, as
+// k_finalize_mix does for the mix: blockIdx.y = replica, blockIdx.x = a slice
+// of kMixSlice particles; every block of a replica repeats its reductions and
+// combine in the same order (the same s), block 0 writes the results and
+// s_rep.
+__global__ void __launch_bounds__(256) k_langevin(SdmArgs a) {
+    __shared__ double red[256];
+    __shared__ double s_sh;
+    const int r = blockIdx.y;
+    const SdmRep& R = a.rep[r];
+    const int i0 = blockIdx.x * kMixSlice;
+    if (blockIdx.x > 0 && i0 >= R.n) return;   // uniform per block
+    finalize_replica(a, r, red, &s_sh, blockIdx.x == 0);
+    __syncthreads();
+    const double s = s_sh;
     const double* prm = a.lv_prm;
     const double dt = prm[SDM_LV_DT], vscale = prm[SDM_LV_VSCALE], fscale = prm[SDM_LV_FSCALE];
     const double noise = prm[SDM_LV_NOISE], invdt = prm[SDM_LV_INVDT];
     const unsigned long long seed = (unsigned long long)__double_as_longlong(prm[SDM_LV_SEED]);
     const unsigned long long step = (unsigned long long)__double_as_longlong(prm[SDM_LV_STEP]);
-    for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < a.total_atoms; gi += stride) {
-        const int r = rep_by_atom(a.rep, a.nrep, gi);
-        const SdmRep& R = a.rep[r];
-        const size_t pi = (size_t)R.x_off + (gi - R.atom_win);   // particle in the concatenated order
+    const int i1 = min(R.n, i0 + kMixSlice);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int gi = R.atom_win + i;
+        const size_t pi = (size_t)R.x_off + i;   // particle in the concatenated order
         const double im = a.lv_invm[pi];
         // rigid-water particles leave x' in lv_xp; k_settle constrains and sets x and v
-        const bool cons = a.st_any && a.st_flag[a.sys[R.sys].atom_base + (gi - R.atom_win)];
+        const bool cons = a.st_any && a.st_flag[a.sys[R.sys].atom_base + i];
         if (im == 0.0) {
             if (cons)
                 for (int k = 0; k < 3; ++k) a.lv_xp[3 * pi + k] = a.lv_x[3 * pi + k];
             continue;
         }
         const size_t gsl = (size_t)R.slot_win + a.inv[gi];
-        const double s = a.s_rep[r];
         const double f0[3] = {fix_to_double(a.F0x[gsl]), fix_to_double(a.F0y[gsl]), fix_to_double(a.F0z[gsl])};
         const double df[3] = {fix_to_double(a.dFx[gsl]), fix_to_double(a.dFy[gsl]), fix_to_double(a.dFz[gsl])};
         const float2 n01 = lv_normals(seed, step, 2 * pi), n2x = lv_normals(seed, step, 2 * pi + 1);
@@ -2702,8 +2711,7 @@ cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st) {
 
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st) {
     if (a.lv_x) {   // Langevin step: the mixed force feeds the update directly
-        k_finalize<<<a.nrep, 256, 0, st>>>(a);
-        k_langevin<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
+        k_langevin<<<dim3((a.max_rep_atoms + kMixSlice - 1) / kMixSlice, a.nrep), 256, 0, st>>>(a);
         if (a.st_any) k_settle<<<dim3((a.st_max + 127) / 128, a.nrep), 128, 0, st>>>(a);
         k_lv_tick<<<1, 1, 0, st>>>(a.lv_prm);
     } else {
@@ -2956,7 +2964,7 @@ __device__ void na_combine(const double* p, double U0, double u, int st, double*
     }
     double dwdl = 0.0;
     if (noneq == 1) {
-        // linear and quadratic bias: lambda1 = lambda2, alpha = 1, u0 = 0, as in k_finalize
+        // linear and quadratic bias: lambda1 = lambda2, alpha = 1, u0 = 0, as in finalize_replica
         const bool ilog = method == SDM_ILOGISTIC;
         const double dl1 = ilog ? l1 : lambdac, dl2 = ilog ? l2 : lambdac, du0 = ilog ? u0 : 0.0;
         const double ee = 1.0 + exp(-alpha * (be - du0));
