@@ -269,3 +269,25 @@ def test_integrator_mirror_rigid_waters():
     assert np.isfinite(integ.getBindE()) and np.isfinite(integ.getPotEnergy())
     integ.close()
     ref.close()
+
+
+def test_langevin_steps_equal_in_every_branch_mode():
+    """Three steps at 300 K with the graph's second branch joined after the
+    main pass (default), before it, and with one stream: the same positions,
+    velocities and results bit for bit (same seed and step counter)."""
+    import torch
+    s, h, x, v, im, fext, dev = _setup()
+    imd, fd = dev(im), dev(fext)
+    out = {}
+    for ov in (2, 1, 0):
+        h.set_option(capi.OPT_OVERLAP, ov)
+        h.set_langevin(DT, FRICTION, 300.0, seed=3, step=7)
+        xa, va = dev(x), dev(v)
+        rd = torch.zeros((h.nrep, capi.NRESULTS), dtype=torch.float64, device="cuda")
+        h.langevin_step(xa.data_ptr(), va.data_ptr(), imd.data_ptr(), rd.data_ptr(), 3, fd.data_ptr())
+        torch.cuda.synchronize()
+        out[ov] = (xa.cpu().numpy(), va.cpu().numpy(), rd.cpu().numpy())
+    for ov in (1, 0):
+        for a, b in zip(out[ov], out[2]):
+            assert np.array_equal(a, b), ov
+    assert h.check_status() == 0
