@@ -36,6 +36,7 @@ cudaError_t sdm_launch_pme(const SdmArgs& a, const cufftHandle* r2c, const cufft
                            const long long* spec_off, int nsys, int conv_blocks, cudaStream_t st);
 cudaError_t sdm_pme_prepare(int smem_bytes);
 cudaError_t sdm_launch_restraints(const SdmArgs& a, cudaStream_t st);
+cudaError_t sdm_launch_combine(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st);
 cudaError_t sdm_launch_gather_positions(const void* posq, const void* corr, int double_precision,
@@ -663,16 +664,27 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     // (with PME on the branch: the main pass takes clusters from a counter, so
     // CTAs that start late take fewer).  Timed evaluations keep one branch so
     // that the events bracket single kernels.
+    //
+    // The combine (u, soft core, bias, the mixing weight s) needs every part
+    // of u (perturbation pass, exceptions, excluded-pair corrections,
+    // reciprocal space) and nothing of the main pass, so with a branch the
+    // exceptions and the combine run there too; the finalize then reads s and
+    // only reduces U0.  The exceptions add forces by integer atomics, in any
+    // order beside the main pass's.
     const int ov = profile || mode == 2 ? 0 : h->opt_overlap;
     const bool pme_side = ov == 2 && mode == 0 && h->pme;
     const bool fork = ov != 0 && (a.total_pert > 0 || pme_side);
+    const bool ex_side = fork && mode == 0;
+    const bool cmb_side = ex_side && (!h->pme || pme_side);
     if (fork) {
         SDM_CUDA(h, cudaEventRecord(h->fork_ev, st));
         SDM_CUDA(h, cudaStreamWaitEvent(h->side, h->fork_ev, 0));
         SDM_CUDA(h, sdm_launch_perturb(a, mode, h->side));
+        if (ex_side) SDM_CUDA(h, sdm_launch_exceptions(a, h->side));
         if (pme_side)
             SDM_CUDA(h, sdm_launch_pme(a, h->pme_r2c.data(), h->pme_c2r.data(), h->pme_grid_off.data(),
                                        h->pme_spec_off.data(), (int)h->sys.size(), a.pme_conv_blocks, h->side));
+        if (cmb_side) SDM_CUDA(h, sdm_launch_combine(a, h->side));
         SDM_CUDA(h, cudaEventRecord(h->join_ev, h->side));
     }
     SDM_CUDA(h, sdm_launch_jlist(a, h->grp_prefix, st));
@@ -683,12 +695,13 @@ sdm_status enqueue(sdm_handle* h, const SdmArgs& a, int mode, cudaStream_t st, b
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[7], st, fl));
     if (fork && ov == 2) SDM_CUDA(h, cudaStreamWaitEvent(st, h->join_ev, 0));
     if (mode != 2 && !fork) SDM_CUDA(h, sdm_launch_perturb(a, mode, st));
-    if (mode == 0) SDM_CUDA(h, sdm_launch_exceptions(a, st));
+    if (mode == 0 && !ex_side) SDM_CUDA(h, sdm_launch_exceptions(a, st));
     if (mode == 0) SDM_CUDA(h, sdm_launch_restraints(a, st));
     if (mode == 0 && h->pme && !pme_side)
         SDM_CUDA(h, sdm_launch_pme(a, h->pme_r2c.data(), h->pme_c2r.data(), h->pme_grid_off.data(),
                                    h->pme_spec_off.data(), (int)h->sys.size(), a.pme_conv_blocks, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[8], st, fl));
+    if (mode == 0 && !cmb_side) SDM_CUDA(h, sdm_launch_combine(a, st));
     if (mode == 0) SDM_CUDA(h, sdm_launch_finalize(a, st));
     if (profile) SDM_CUDA(h, cudaEventRecordWithFlags(h->ev[9], st, fl));
     return SDM_OK;
@@ -1002,6 +1015,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     const size_t o_ppos = ar.take<SdmPertPos>(std::max(Pp, 1LL));
     const size_t o_adj = ar.take<double>(3 * std::max(Pp, 1LL));
     const size_t o_ncl = ar.take<int>(nrep), o_st = ar.take<int>(4), o_srep = ar.take<double>(nrep);
+    const size_t o_cmb = ar.take<double>((size_t)nrep * SDM_CMB_FIELDS);
     const size_t o_lv = ar.take<double>(SDM_LV_COUNT);
     const size_t o_counts = ar.take<long long>(2 * nrep), o_ip = ar.take<int>(nrep + 1);
     const size_t o_cp = ar.take<int>(nrep + 1), o_jc = ar.take<int>(Cl);
@@ -1087,6 +1101,7 @@ sdm_status sdm_create(const sdm_system_desc* systems, int num_systems, int devic
     a.e_part = at<double>(B, o_ep);
     a.p_part = at<double>(B, o_pp);
     a.s_rep = at<double>(B, o_srep);
+    a.cmb = at<double>(B, o_cmb);
     a.pert_pos = at<SdmPertPos>(B, o_ppos);
     a.adj = at<double>(B, o_adj);
     a.ncl = at<int>(B, o_ncl);

@@ -14,10 +14,12 @@
 //   k_pert_prep the displaced particles' positions in both states
 //   k_perturb   perturbation pass: only pairs whose displacements differ, at
 //               both states -> u (FP64) and dF = F1 - F0 (fixed point)
-//   k_finalize_mix  deterministic energy reductions, soft core, bias,
-//               weight s, then F = F0 + s dF in original particle order
-//               (k_langevin: the same reductions and combine, then the
-//               stochastic-dynamics update; k_mix: the state forces)
+//   k_combine   deterministic reduction of u, soft core, bias, weight s
+//               (needs no main-pass result: runs beside it)
+//   k_finalize_mix  F = F0 + s dF in original particle order; one more block
+//               per replica reduces U0 and writes the results
+//               (k_langevin: the same layout with the stochastic-dynamics
+//               update; k_mix: the state forces)
 //
 // Reference correspondence: the two nonbonded evaluations of
 // openmmapi/src/LangevinIntegratorSDM.cpp:158-176 (OpenMM NonbondedForce at x
@@ -2079,22 +2081,22 @@ __device__ double softcore(double u, int method, double umax, double a, double u
     return (umax - ub) * (za - 1.0) / (za + 1.0) + ub;
 }
 
-// energies of replica r (fixed-order block reductions) and the combine; thread
-// 0 leaves the mixing weight in *s_out and, when `write`, the results, the
-// weight for the Langevin step and the status bits
-__device__ void finalize_replica(const SdmArgs& a, int r, double* red, double* s_out, bool write) {
+// Combine record of a replica, written by k_combine, read by the finalize
+enum { CMB_U, CMB_BE, CMB_FP, CMB_W, CMB_DW, CMB_DWDL, CMB_L1, CMB_L2, CMB_U0, CMB_W0 };
+static_assert(CMB_W0 + 1 == SDM_CMB_FIELDS, "combine record size");
+
+// The perturbation energy u of replica r (a fixed-order block reduction of
+// the perturbation pass's, exceptions', excluded-pair corrections' and
+// reciprocal space's parts) and the combine of
+// platforms/reference/src/ReferenceSDMKernels.cpp:202-302: soft core, bias
+// W, its derivative, dW/dlambda, and the mixing weight s of
+// ReferenceSDMKernels.cpp:309-318.  None of it depends on the main pass.
+// One block per replica.
+__global__ void __launch_bounds__(256) k_combine(SdmArgs a) {
+    __shared__ double red[256];
+    const int r = blockIdx.x;
     const SdmRep& R = a.rep[r];
     const SdmSys& S = a.sys[R.sys];
-    const int ncl = a.ncl[r];
-    double e0 = 0.0;
-    const double* ep = a.e_part + (size_t)R.cl_win * a.split;
-    for (int k = threadIdx.x; k < ncl * a.split; k += blockDim.x) e0 += ep[k];
-    for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) e0 += a.ex_e0[R.ex_win + k];
-    if (a.total_xc)
-        for (int k = threadIdx.x; k < a.xc_blocks; k += blockDim.x) e0 += a.xc_e0[(size_t)r * a.xc_blocks + k];
-    if (S.pme)
-        for (int k = threadIdx.x; k < a.pme_conv_blocks; k += blockDim.x) e0 += a.pme_epart[(size_t)r * a.pme_conv_blocks + k];
-    const double U0 = block_sum(e0, red) + S.e_const;
     double eu = 0.0;
     for (int k = threadIdx.x; k < 2 * S.nD * SDM_PERT_PARTS; k += blockDim.x)
         eu += a.p_part[(size_t)R.pert_win * SDM_PERT_PARTS + k];
@@ -2162,26 +2164,57 @@ __device__ void finalize_replica(const SdmArgs& a, int r, double* red, double* s
         dwdl = (-lee / alpha) * p[SDM_P_M_LAMBDA1] + (be + lee / alpha) * p[SDM_P_M_LAMBDA2] +
                ((dl2 - dl1) * ex / ee) * p[SDM_P_M_U0] + p[SDM_P_M_W0];
     }
-    *s_out = bfp * fp;
-    if (!write) return;
+    double* c = a.cmb + (size_t)r * SDM_CMB_FIELDS;
+    c[CMB_U] = u;
+    c[CMB_BE] = be;
+    c[CMB_FP] = fp;
+    c[CMB_W] = ebias;
+    c[CMB_DW] = bfp;
+    c[CMB_DWDL] = dwdl;
+    c[CMB_L1] = l1;
+    c[CMB_L2] = l2;
+    c[CMB_U0] = u0;
+    c[CMB_W0] = w0;
+    a.s_rep[r] = bfp * fp;
+}
+
+// U0 of replica r (fixed-order block reduction of the main pass's,
+// exceptions', excluded-pair corrections' and reciprocal space's parts) and
+// the replica's results, with the combine record of k_combine.  Thread 0
+// writes.
+__device__ void finalize_results(const SdmArgs& a, int r, double* red) {
+    const SdmRep& R = a.rep[r];
+    const SdmSys& S = a.sys[R.sys];
+    const int ncl = a.ncl[r];
+    double e0 = 0.0;
+    const double* ep = a.e_part + (size_t)R.cl_win * a.split;
+    for (int k = threadIdx.x; k < ncl * a.split; k += blockDim.x) e0 += ep[k];
+    for (int k = threadIdx.x; k < S.ex_count; k += blockDim.x) e0 += a.ex_e0[R.ex_win + k];
+    if (a.total_xc)
+        for (int k = threadIdx.x; k < a.xc_blocks; k += blockDim.x) e0 += a.xc_e0[(size_t)r * a.xc_blocks + k];
+    if (S.pme)
+        for (int k = threadIdx.x; k < a.pme_conv_blocks; k += blockDim.x) e0 += a.pme_epart[(size_t)r * a.pme_conv_blocks + k];
+    const double U0 = block_sum(e0, red) + S.e_const;
+    if (threadIdx.x != 0) return;
+    const double* c = a.cmb + (size_t)r * SDM_CMB_FIELDS;
+    const double u = c[CMB_U];
     int st = *(volatile int*)a.status;
     if (!isfinite(U0) || !isfinite(u)) { st |= SDM_DEV_ENERGY_NONFINITE; atomicOr(a.status, SDM_DEV_ENERGY_NONFINITE); }
     double* o = a.results + (size_t)r * SDM_NRESULTS;
     o[SDM_R_U0] = U0;
     o[SDM_R_U1] = U0 + u;
     o[SDM_R_U] = u;
-    o[SDM_R_BINDE] = be;
-    o[SDM_R_FP] = fp;
-    o[SDM_R_W] = ebias;
-    o[SDM_R_DW] = bfp;
-    o[SDM_R_S] = bfp * fp;
-    a.s_rep[r] = bfp * fp;
-    o[SDM_R_EPOT] = U0 + ebias + (a.rs_any ? a.rs_e[r] : 0.0);   // + group-1 restraints
-    o[SDM_R_DWDLAMBDA] = dwdl;
-    o[SDM_R_LAMBDA1] = l1;
-    o[SDM_R_LAMBDA2] = l2;
-    o[SDM_R_U0PARAM] = u0;
-    o[SDM_R_W0PARAM] = w0;
+    o[SDM_R_BINDE] = c[CMB_BE];
+    o[SDM_R_FP] = c[CMB_FP];
+    o[SDM_R_W] = c[CMB_W];
+    o[SDM_R_DW] = c[CMB_DW];
+    o[SDM_R_S] = c[CMB_DW] * c[CMB_FP];
+    o[SDM_R_EPOT] = U0 + c[CMB_W] + (a.rs_any ? a.rs_e[r] : 0.0);   // + group-1 restraints
+    o[SDM_R_DWDLAMBDA] = c[CMB_DWDL];
+    o[SDM_R_LAMBDA1] = c[CMB_L1];
+    o[SDM_R_LAMBDA2] = c[CMB_L2];
+    o[SDM_R_U0PARAM] = c[CMB_U0];
+    o[SDM_R_W0PARAM] = c[CMB_W0];
     o[SDM_R_STATUS] = (double)st;
     o[SDM_R_RESERVED] = (double)ncl;
 }
@@ -2231,22 +2264,21 @@ __global__ void k_mix(SdmArgs a) {
 }
 
 // Finalize and mix in one launch (the evaluation without a Langevin step):
-// blockIdx.y = replica, blockIdx.x = a slice of kMixSlice particles.  Every
-// block of a replica repeats the replica's energy reductions and combine (the
-// same fixed order, so the same bits), block 0 writes the results, and each
-// block mixes its slice with the weight it computed: no second launch waits
-// for the weights.
+// blockIdx.y = replica; blockIdx.x < gridDim.x - 1 mixes a slice of
+// kMixSlice particles with the weight s of k_combine, the last block reduces
+// U0 and writes the replica's results beside them.
 constexpr int kMixSlice = 2048;
 __global__ void __launch_bounds__(256) k_finalize_mix(SdmArgs a) {
     __shared__ double red[256];
-    __shared__ double s;
     const int r = blockIdx.y;
     const SdmRep& R = a.rep[r];
+    if (blockIdx.x == gridDim.x - 1) {   // uniform per block
+        finalize_results(a, r, red);
+        return;
+    }
     const int i0 = blockIdx.x * kMixSlice;
-    if (blockIdx.x > 0 && i0 >= R.n) return;   // uniform per block
-    finalize_replica(a, r, red, &s, blockIdx.x == 0);
-    __syncthreads();
-    const double sw = a.forces ? s : 0.0;
+    if (i0 >= R.n) return;
+    const double sw = a.forces ? a.s_rep[r] : 0.0;
     const int i1 = min(R.n, i0 + kMixSlice);
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const size_t gsl = (size_t)R.slot_win + a.inv[R.atom_win + i];
@@ -2295,21 +2327,21 @@ __device__ __forceinline__ float2 lv_normals(unsigned long long seed, unsigned l
     return make_float2(r * cs, r * sn);
 }
 
-// Finalize and the stochastic-dynamics update in one launch, as
-// k_finalize_mix does for the mix: blockIdx.y = replica, blockIdx.x = a slice
-// of kMixSlice particles; every block of a replica repeats its reductions and
-// combine in the same order (the same s), block 0 writes the results and
-// s_rep.
+// The stochastic-dynamics update in the finalize's launch, laid out as
+// k_finalize_mix: blockIdx.y = replica; blockIdx.x < gridDim.x - 1 updates a
+// slice of kMixSlice particles with the weight s of k_combine, the last block
+// writes the replica's results.
 __global__ void __launch_bounds__(256) k_langevin(SdmArgs a) {
     __shared__ double red[256];
-    __shared__ double s_sh;
     const int r = blockIdx.y;
     const SdmRep& R = a.rep[r];
+    if (blockIdx.x == gridDim.x - 1) {   // uniform per block
+        finalize_results(a, r, red);
+        return;
+    }
     const int i0 = blockIdx.x * kMixSlice;
-    if (blockIdx.x > 0 && i0 >= R.n) return;   // uniform per block
-    finalize_replica(a, r, red, &s_sh, blockIdx.x == 0);
-    __syncthreads();
-    const double s = s_sh;
+    if (i0 >= R.n) return;
+    const double s = a.s_rep[r];
     const double* prm = a.lv_prm;
     const double dt = prm[SDM_LV_DT], vscale = prm[SDM_LV_VSCALE], fscale = prm[SDM_LV_FSCALE];
     const double noise = prm[SDM_LV_NOISE], invdt = prm[SDM_LV_INVDT];
@@ -2711,12 +2743,17 @@ cudaError_t sdm_launch_mix(const SdmArgs& a, cudaStream_t st) {
 
 cudaError_t sdm_launch_finalize(const SdmArgs& a, cudaStream_t st) {
     if (a.lv_x) {   // Langevin step: the mixed force feeds the update directly
-        k_langevin<<<dim3((a.max_rep_atoms + kMixSlice - 1) / kMixSlice, a.nrep), 256, 0, st>>>(a);
+        k_langevin<<<dim3((a.max_rep_atoms + kMixSlice - 1) / kMixSlice + 1, a.nrep), 256, 0, st>>>(a);
         if (a.st_any) k_settle<<<dim3((a.st_max + 127) / 128, a.nrep), 128, 0, st>>>(a);
         k_lv_tick<<<1, 1, 0, st>>>(a.lv_prm);
     } else {
-        k_finalize_mix<<<dim3((a.max_rep_atoms + kMixSlice - 1) / kMixSlice, a.nrep), 256, 0, st>>>(a);
+        k_finalize_mix<<<dim3((a.max_rep_atoms + kMixSlice - 1) / kMixSlice + 1, a.nrep), 256, 0, st>>>(a);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t sdm_launch_combine(const SdmArgs& a, cudaStream_t st) {
+    k_combine<<<a.nrep, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -2964,7 +3001,7 @@ __device__ void na_combine(const double* p, double U0, double u, int st, double*
     }
     double dwdl = 0.0;
     if (noneq == 1) {
-        // linear and quadratic bias: lambda1 = lambda2, alpha = 1, u0 = 0, as in finalize_replica
+        // linear and quadratic bias: lambda1 = lambda2, alpha = 1, u0 = 0, as in k_combine
         const bool ilog = method == SDM_ILOGISTIC;
         const double dl1 = ilog ? l1 : lambdac, dl2 = ilog ? l2 : lambdac, du0 = ilog ? u0 : 0.0;
         const double ee = 1.0 + exp(-alpha * (be - du0));

@@ -45,6 +45,8 @@
 #define SDM_MAX_SPLIT 4
 #define SDM_JG 4                 // largest list-building group (i-clusters of one column, z-consecutive)
 #define SDM_PERT_PARTS 4         // warps per perturbation item (stencil columns split between them)
+// per-replica record of the combine (perturbation energy u, soft core, bias)
+#define SDM_CMB_FIELDS 10
 
 // Langevin parameter block (doubles; seed and step are stored as integer bits)
 #define SDM_LV_DT 0
@@ -172,7 +174,8 @@ struct SdmArgs {
     // input / output
     const double* x;      // concatenated coordinates
     double* results;      // nrep * SDM_NRESULTS (device or mapped host memory)
-    double* s_rep;        // nrep: mixing weight s of the last finalize (device)
+    double* s_rep;        // nrep: mixing weight s of the last combine (device)
+    double* cmb;          // nrep * SDM_CMB_FIELDS: u and the combine terms of the last evaluation
     // Langevin step (sdm_langevin_step): positions lv_x are also the evaluation's x
     double* lv_x;         // [3 * total particles] updated in place
     double* lv_v;         // [3 * total particles] updated in place
