@@ -37,8 +37,25 @@ METRIC = "SDM lambda-state force evals/s at 23k atoms x 22 lambda, batched vs pl
 UNIT = "lambda-state evals/s"
 FLOP_PER_PAIR = 52  # FP32 flops per pair per state (FMA = 2, rsqrt = 1)
 # kernels of one batched evaluation: k_cells k_scan k_bucket k_cellsort k_clusters
-# k_jlist k_pair k_pert_prep k_perturb k_finalize_mix
-KERNELS_PER_STEP = 10
+# k_jlist k_pair k_pert_prep k_perturb k_combine k_finalize_mix
+KERNELS_PER_STEP = 11
+# Algorithmic bytes of the O(N) kernels, each datum read or written once
+# (per particle, per cluster slot, per cell): k_cells reads x (24 B) and
+# writes the wrapped copy (24 B), the cell pair (8 B) and a histogram count
+# (4 B), and zeroes the six fixed-point force words of every slot (48 B);
+# k_bucket reads the cell pair and offset and writes the count and the
+# bucket entry (20 B); k_cellsort reads the bucket entry, cell pair, cell
+# bounds, z, column offsets and writes perm, inv and the cluster's reference
+# cell (46 B); k_clusters reads perm, position, five per-particle
+# parameters, the exclusion partners and their slots (80 B) and writes the
+# cluster-ordered coordinates, parameters, group, molecule and exclusion
+# slots (48 B) and, per cluster of 8 slots, reads its reference cell and
+# origin (40 B) and writes z bounds, box and links (72 B); the finalize
+# reads inv and the six force words and writes the three mixed components
+# (76 B); k_scan reads the cell counts and writes the cell offsets (8 B per
+# cell, the column tables 12 B per column).
+ON_BYTES = {"k_cells": (60, 48, 0, 0), "k_bucket": (20, 0, 0, 0), "k_cellsort": (46, 0, 0, 0),
+            "k_clusters": (0, 142, 0, 0), "k_finalize+k_mix": (76, 0, 0, 0), "k_scan": (0, 0, 8, 12)}
 NREP = 22
 WORKLOAD = ("config2: 22 replicas x 22,580 particles (7,500 waters + 2x40 ligand), 6.2 nm box, "
             "rc 1.0 nm reaction field, one batched call per step")
@@ -342,6 +359,7 @@ def main():
     clocks = sampler.stop()
     tot_b = max_over_ranks(sum(ms_b) / 1e3, dist, dev)
     value = whole_job_rate(NREP * args.steps, world, tot_b)
+    ncl_tot = int(rd[:, capi.R_NCL].sum().item())   # clusters of all replicas (headline call)
     # per-kernel times: a second timed region of the same call with CUDA events
     # recorded between the kernels inside the graph (the event nodes add to the
     # call, so the headline region above runs without them)
@@ -602,6 +620,21 @@ def main():
             "frac_whole_call": (flop_per_launch / (sum(ms_b) / len(ms_b) * 1e-3) / 1e12) / peak_tf,
             "flop_per_launch": flop_per_launch, "P0": P0, "P1delta": P1}
 
+    # O(N) kernels against the measured HBM bandwidth: algorithmic bytes per
+    # launch (ON_BYTES x particles, slots, cells, columns) over the in-graph
+    # event times of the profiled region
+    Mg = h.grid(0)
+    units = (NREP * n, 8 * ncl_tot, NREP * int(Mg[0] * Mg[1] * Mg[2]), NREP * int(Mg[0] * Mg[1]))
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    on_kernels = {}
+    for k, per in ON_BYTES.items():
+        if k not in breakdown:
+            continue
+        b = float(sum(pu * u for pu, u in zip(per, units)))
+        gbs = b / (breakdown[k] * 1e-3) / 1e9
+        on_kernels[k] = {"ms": breakdown[k], "bytes": b, "gbs": gbs, "frac_hbm": gbs / hbm}
+    on_kernels["peak_gbs"] = hbm
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baselines(sysm)
@@ -614,6 +647,7 @@ def main():
     # tail sees value, e2e, roofline, plain and batched_over_plain)
     line = {
         "kernel_ms": breakdown,
+        "on_kernels": on_kernels,
         "kernel_timing": {"steps": n_prof, "ms_per_step_instrumented": sum(ms_prof) / len(ms_prof),
                           "how": "CUDA events between the kernels inside the replayed graph, over a second "
                                  "timed region of the headline call; the headline region runs the graph "

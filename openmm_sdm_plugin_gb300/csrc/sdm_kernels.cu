@@ -810,13 +810,25 @@ __device__ void build_jlist(const SdmArgs& a, int r, int g, JlSmem& js) {
     __syncwarp();   // js is rewritten by the warp's next group
 }
 
-// static schedule: warp w takes groups w, w+W, w+2W, ...
+// DYN: every warp takes groups from a per-call counter until none is left
+// (warps that finish early take more; the launch ends with the last group,
+// not the last of a fixed share).  Otherwise warp w builds groups w, w + W,
+// ... (no counter round trip; the host picks this form when there are about
+// as many groups as warps).  Both build the same lists.
+__device__ __forceinline__ int next_group(const SdmArgs& a) {
+    int g = 0;
+    if (lane_id() == 0) g = atomicAdd(&a.work_counter[0], 1);
+    return __shfl_sync(0xffffffffu, g, 0);
+}
+
+template <bool DYN>
 __global__ void __launch_bounds__(256, 4) k_jlist(SdmArgs a, const int* grp_prefix) {
     __shared__ JlSmem js_all[8];
     JlSmem& js = js_all[threadIdx.x >> 5];
     const int total = grp_prefix[a.nrep];
-    const int W = gridDim.x * (blockDim.x >> 5);
-    for (int item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < total; item += W) {
+    const int W = DYN ? 0 : gridDim.x * (blockDim.x >> 5);
+    for (int item = DYN ? next_group(a) : blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); item < total;
+         item = DYN ? next_group(a) : item + W) {
         const int r = rep_by_item(grp_prefix, a.nrep, item);
         const int g = item - grp_prefix[r];
         if (replica_image_mode(a, a.sys[a.rep[r].sys], r)) build_jlist<true>(a, r, g, js);
@@ -2280,16 +2292,30 @@ __global__ void __launch_bounds__(256) k_finalize_mix(SdmArgs a) {
     if (i0 >= R.n) return;
     const double sw = a.forces ? a.s_rep[r] : 0.0;
     const int i1 = min(R.n, i0 + kMixSlice);
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        const size_t gsl = (size_t)R.slot_win + a.inv[R.atom_win + i];
-        const double f0[3] = {fix_to_double(a.F0x[gsl]), fix_to_double(a.F0y[gsl]), fix_to_double(a.F0z[gsl])};
-        const double df[3] = {fix_to_double(a.dFx[gsl]), fix_to_double(a.dFy[gsl]), fix_to_double(a.dFz[gsl])};
-        const size_t o = 3 * (size_t)(R.x_off + i);
+    // kMixBatch particles per thread and round: every gather of the round is
+    // issued before the first conversion (the slot gathers are L2 latency)
+    constexpr int kMixBatch = 4;
+    for (int ib = i0 + threadIdx.x; ib < i1; ib += kMixBatch * blockDim.x) {
+        unsigned long long v[kMixBatch][6];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            if (a.forces) a.forces[o + k] = __fma_rn(sw, df[k], f0[k]);
-            if (a.F0out) a.F0out[o + k] = f0[k];
-            if (a.F1out) a.F1out[o + k] = f0[k] + df[k];
+        for (int q = 0; q < kMixBatch; ++q) {
+            const int i = ib + q * (int)blockDim.x;
+            const size_t gsl = (size_t)R.slot_win + a.inv[R.atom_win + (i < i1 ? i : ib)];
+            v[q][0] = a.F0x[gsl]; v[q][1] = a.F0y[gsl]; v[q][2] = a.F0z[gsl];
+            v[q][3] = a.dFx[gsl]; v[q][4] = a.dFy[gsl]; v[q][5] = a.dFz[gsl];
+        }
+#pragma unroll
+        for (int q = 0; q < kMixBatch; ++q) {
+            const int i = ib + q * (int)blockDim.x;
+            if (i >= i1) break;
+            const size_t o = 3 * (size_t)(R.x_off + i);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double f0 = fix_to_double(v[q][k]), df = fix_to_double(v[q][3 + k]);
+                if (a.forces) a.forces[o + k] = __fma_rn(sw, df, f0);
+                if (a.F0out) a.F0out[o + k] = f0;
+                if (a.F1out) a.F1out[o + k] = f0 + df;
+            }
         }
     }
 }
@@ -2547,7 +2573,11 @@ cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* grp_prefix,
 }
 
 cudaError_t sdm_launch_jlist(const SdmArgs& a, const int* grp_prefix, cudaStream_t st) {
-    k_jlist<<<num_sms() * 8, 256, 0, st>>>(a, grp_prefix);
+    // one wave (the launch bounds give 4 CTAs per SM); the counter pays off
+    // once the groups (at least particles / (8 jg)) outnumber the warps
+    const int grid = num_sms() * 4;
+    if ((long long)a.total_atoms > 8LL * a.jg * grid * 8) k_jlist<true><<<grid, 256, 0, st>>>(a, grp_prefix);
+    else k_jlist<false><<<grid, 256, 0, st>>>(a, grp_prefix);
     return cudaGetLastError();
 }
 

@@ -257,7 +257,7 @@ struct SdmArgs {
     int jg;              // clusters per list-building group (1, 2 or SDM_JG)
     int2* cl_grp;        // per group (cluster window): first cluster, clusters (1..SDM_JG)
     unsigned* extz;      // per replica max cluster z extent (float bits)
-    int* work_counter;   // [0] main pass, [1] perturbation pass
+    int* work_counter;   // [0] list build, [1] perturbation pass, [2] main pass (zeroed every call)
     int* status;         // device status word
     long long* counts;   // optional: per replica P0, P1delta (count mode)
     // list export (diagnostic)
