@@ -177,6 +177,30 @@ def test_temoa_dms_system_parity():
     assert res[0, capi.R_STATUS] == 0
 
 
+@pytest.mark.gpu
+def test_exceptions_on_the_second_branch_same_bits():
+    """With a second graph branch the 1-4 exceptions and the combine run
+    there, beside the main pass (their forces are integer atomics into the
+    same accumulators); one stream runs them after it.  Every branch mode,
+    captured and eager, gives the same results and forces bit for bit."""
+    s = temoa_system()
+    h = capi.Handle([s])
+    h.set_params(0, s.params[0].as_array())
+    x = s.positions[0]
+    out = {}
+    for overlap in (2, 1, 0):
+        for graph in (1, 0):
+            h.set_option(capi.OPT_OVERLAP, overlap)
+            h.set_option(capi.OPT_GRAPH, graph)
+            r, F = h.evaluate(x)
+            out[overlap, graph] = (r, F) + h.state_forces()
+    ref = out[2, 1]
+    assert ref[0][0, capi.R_STATUS] == 0
+    for k, v in out.items():
+        for a, b in zip(v, ref):
+            assert np.array_equal(a, b), k
+
+
 def test_mirror_from_a_dms_system_carries_its_nonbonded_force():
     """force_from_system / integrator_from_system on the TEMOA system: the
     mirror's system descriptor holds the same exclusions (each once, in the
