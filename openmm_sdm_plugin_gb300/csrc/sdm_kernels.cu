@@ -202,10 +202,6 @@ __global__ void k_cells(SdmArgs a) {
         a.cellinfo[gi] = make_int2(col, c[2]);
         atomicAdd(&a.cel_cnt[R.cel_win + col * S.M[2] + c[2]], 1);
     }
-    for (int gs = blockIdx.x * blockDim.x + threadIdx.x; gs < a.total_slots; gs += stride) {
-        a.F0x[gs] = 0ull; a.F0y[gs] = 0ull; a.F0z[gs] = 0ull;
-        a.dFx[gs] = 0ull; a.dFy[gs] = 0ull; a.dFz[gs] = 0ull;
-    }
 }
 
 // ------------------------------------------------------------------------- //
@@ -434,6 +430,11 @@ __global__ void k_clusters(SdmArgs a) {
             q4 = make_float4(X[0], X[1], X[2], 0.0f);
             p2 = make_float2(0.0f, 0.0f);
         }
+        // the slot's fixed-point force accumulators start the call at zero
+        // (every later force goes in by integer atomics; slots past the
+        // replica's clusters are read by nobody)
+        a.F0x[gs] = 0ull; a.F0y[gs] = 0ull; a.F0z[gs] = 0ull;
+        a.dFx[gs] = 0ull; a.dFy[gs] = 0ull; a.dFz[gs] = 0ull;
         a.clX[gs] = q4;
         a.clP[gs] = p2;
         a.grp[gs] = g;
@@ -946,6 +947,25 @@ __device__ __forceinline__ void eval_tile(const SdmArgs& a, const SdmSys& S, con
     pair_tile<MODE, IMG, PME, true, LJ>(a, S, R, ip, A, B.x, B.y, m, active, __float_as_int(B.w), ic, ef, npair);
 }
 
+// The remainders of both rings at the end of an i-cluster in one tile when
+// they fit: lanes < nl take the LJ ring's entries, the next nc the Coulomb
+// ring's, all through the Lennard-Jones tile (epsilon = 0 makes its LJ terms
+// add exactly zero, so those pairs' forces are the Coulomb tile's bits).
+template <int MODE, bool IMG, bool PME, int CH>
+__device__ __forceinline__ void eval_tile_both(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
+                                               const EvalSmem<CH>& sm, unsigned hl, int nl, unsigned hc, int nc,
+                                               ICluster& ic, float& ef, long long& npair) {
+    const int lane = lane_id();
+    const bool fromlj = lane < nl;
+    const Ring& rg = fromlj ? sm.lj : sm.co;
+    const unsigned idx = (fromlj ? hl + lane : hc + (lane - nl)) & (SDM_RING - 1);
+    const bool active = lane < nl + nc;
+    const float4 A = active ? rg.a[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 B = active ? rg.b[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned m = active ? __float_as_uint(B.z) : 0u;
+    pair_tile<MODE, IMG, PME, true, true>(a, S, R, sm.ip, A, B.x, B.y, m, active, __float_as_int(B.w), ic, ef, npair);
+}
+
 // Computes the allowed-i mask of candidate slot j (cluster J) against
 // i-cluster I (valid-i bits vmask).
 __device__ __forceinline__ unsigned j_mask(const SdmArgs& a, const SdmSys& S, const SdmRep& R,
@@ -1210,8 +1230,13 @@ __device__ void process_cluster(const SdmArgs& a, int r, int I, int part, EvalSm
         }
         return;
     }
-    if (tl != hl) eval_tile<MODE, IMG, true, PME>(a, S, R, sm.lj, sm.ip, hl, (int)(tl - hl), ic, ef, npair);
-    if (tc != hc) eval_tile<MODE, IMG, false, PME>(a, S, R, sm.co, sm.ip, hc, (int)(tc - hc), ic, ef, npair);
+    const int nl = (int)(tl - hl), nc = (int)(tc - hc);
+    if (nl > 0 && nc > 0 && nl + nc <= 32) {
+        eval_tile_both<MODE, IMG, PME>(a, S, R, sm, hl, nl, hc, nc, ic, ef, npair);
+    } else {
+        if (nl > 0) eval_tile<MODE, IMG, true, PME>(a, S, R, sm.lj, sm.ip, hl, nl, ic, ef, npair);
+        if (nc > 0) eval_tile<MODE, IMG, false, PME>(a, S, R, sm.co, sm.ip, hc, nc, ic, ef, npair);
+    }
     if (MODE == MODE_COUNT) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) npair += __shfl_xor_sync(0xffffffffu, npair, o);
@@ -2559,7 +2584,7 @@ cudaError_t sdm_launch_prep(const SdmArgs& a, int* item_prefix, int* grp_prefix,
     int e = 0;
     auto mark = [&]() { if (ev && e < nev) cudaEventRecordWithFlags(ev[e++], st, ev_flags); };
     mark();
-    k_cells<<<grid_for(a.total_atoms > a.total_slots ? a.total_atoms : a.total_slots, 256), 256, 0, st>>>(a);
+    k_cells<<<grid_for(a.total_atoms, 256), 256, 0, st>>>(a);
     mark();
     k_scan<<<a.nrep, 1024, 0, st>>>(a, item_prefix, grp_prefix, done);
     mark();
