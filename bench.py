@@ -42,20 +42,21 @@ KERNELS_PER_STEP = 11
 # Algorithmic bytes of the O(N) kernels, each datum read or written once
 # (per particle, per cluster slot, per cell): k_cells reads x (24 B) and
 # writes the wrapped copy (24 B), the cell pair (8 B) and a histogram count
-# (4 B), and zeroes the six fixed-point force words of every slot (48 B);
+# (4 B);
 # k_bucket reads the cell pair and offset and writes the count and the
 # bucket entry (20 B); k_cellsort reads the bucket entry, cell pair, cell
 # bounds, z, column offsets and writes perm, inv and the cluster's reference
 # cell (46 B); k_clusters reads perm, position, five per-particle
 # parameters, the exclusion partners and their slots (80 B) and writes the
 # cluster-ordered coordinates, parameters, group, molecule and exclusion
-# slots (48 B) and, per cluster of 8 slots, reads its reference cell and
-# origin (40 B) and writes z bounds, box and links (72 B); the finalize
+# slots (48 B), zeroes the slot's six fixed-point force words (48 B) and, per
+# cluster of 8 slots, reads its reference cell and origin (40 B) and writes
+# z bounds, box and links (72 B); the finalize
 # reads inv and the six force words and writes the three mixed components
 # (76 B); k_scan reads the cell counts and writes the cell offsets (8 B per
 # cell, the column tables 12 B per column).
-ON_BYTES = {"k_cells": (60, 48, 0, 0), "k_bucket": (20, 0, 0, 0), "k_cellsort": (46, 0, 0, 0),
-            "k_clusters": (0, 142, 0, 0), "k_finalize+k_mix": (76, 0, 0, 0), "k_scan": (0, 0, 8, 12)}
+ON_BYTES = {"k_cells": (60, 0, 0, 0), "k_bucket": (20, 0, 0, 0), "k_cellsort": (46, 0, 0, 0),
+            "k_clusters": (0, 190, 0, 0), "k_finalize+k_mix": (76, 0, 0, 0), "k_scan": (0, 0, 8, 12)}
 NREP = 22
 WORKLOAD = ("config2: 22 replicas x 22,580 particles (7,500 waters + 2x40 ligand), 6.2 nm box, "
             "rc 1.0 nm reaction field, one batched call per step")
