@@ -1410,8 +1410,7 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, Wa
     };
 
     // z window of the point (absolute, conservative) and its pieces inside [0, Lz):
-    // clusters of a column outside it are farther than the cutoff in z
-    const float2* zb = a.cl_zb + R.cl_win;
+    // particles of a column outside it are farther than the cutoff in z
     const float zq = __double2float_rn(y[2]);
     const float ZA = zq - rclc - 1.0e-4f, ZB = zq + rclc + 1.0e-4f;
     const float Lz = S.Lf[2];
@@ -1446,11 +1445,23 @@ __device__ void process_perturb(const SdmArgs& a, int r, int local, int part, Wa
                     Jb = lo;
                     cntJ = hi - lo;
                 } else {
-                    Jb = lower_zhi(zb, lo, hi, za1);
-                    cntJ = upper_zlo(zb, Jb, hi, zb1) - Jb;
+                    // the clusters holding the column's particles of the z cells
+                    // that overlap the window (particles outside those cells are
+                    // farther than the cutoff in z): cell offsets instead of
+                    // binary searches over the cluster z bounds
+                    const int* coff = a.cel_off + R.cel_win + colid * S.M[2];
+                    const int a0 = a.col_aoff[R.col_win + colid];
+                    const float ig = (float)S.invg[2];
+                    auto crange = [&](float z0, float z1, int& jb, int& n) {
+                        const int c0 = min(max(__float2int_rd((z0 - 1.0e-3f) * ig), 0), S.M[2] - 1);
+                        const int c1 = min(max(__float2int_rd((z1 + 1.0e-3f) * ig), 0), S.M[2] - 1);
+                        const int p0 = coff[c0] - a0, p1 = coff[c1 + 1] - a0;
+                        jb = lo + (p0 >> 3);
+                        n = p1 > p0 ? ((p1 + 7) >> 3) - (p0 >> 3) : 0;
+                    };
+                    crange(za1, zb1, Jb, cntJ);
                     if (za2 <= zb2) {
-                        Jb2 = lower_zhi(zb, lo, hi, za2);
-                        cnt2 = upper_zlo(zb, Jb2, hi, zb2) - Jb2;
+                        crange(za2, zb2, Jb2, cnt2);
                         // the two pieces are disjoint in z; clusters are counted once
                         if (cnt2 > 0 && cntJ > 0 && Jb2 < Jb + cntJ && Jb2 + cnt2 > Jb) {
                             const int u0 = min(Jb, Jb2), u1 = max(Jb + cntJ, Jb2 + cnt2);
