@@ -56,7 +56,7 @@ KERNELS_PER_STEP = 11
 # (76 B); k_scan reads the cell counts and writes the cell offsets (8 B per
 # cell, the column tables 12 B per column).
 ON_BYTES = {"k_cells": (60, 0, 0, 0), "k_bucket": (20, 0, 0, 0), "k_cellsort": (46, 0, 0, 0),
-            "k_clusters": (0, 190, 0, 0), "k_finalize+k_mix": (76, 0, 0, 0), "k_scan": (0, 0, 8, 12)}
+            "k_clusters": (0, 190, 0, 0), "k_combine+k_finalize_mix": (76, 0, 0, 0), "k_scan": (0, 0, 8, 12)}
 NREP = 22
 WORKLOAD = ("config2: 22 replicas x 22,580 particles (7,500 waters + 2x40 ligand), 6.2 nm box, "
             "rc 1.0 nm reaction field, one batched call per step")

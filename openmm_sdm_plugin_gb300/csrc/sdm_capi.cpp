@@ -186,7 +186,7 @@ namespace {
 inline int chunk_index(int chunk) { return chunk == 8 ? 0 : chunk == 16 ? 2 : 1; }
 
 const char* const kKernelNames[] = {"k_cells", "k_scan", "k_bucket", "k_cellsort", "k_clusters",
-                                    "k_jlist", "k_pair", "k_pert_prep+k_perturb", "k_finalize+k_mix"};
+                                    "k_jlist", "k_pair", "k_pert_prep+k_perturb", "k_combine+k_finalize_mix"};
 const int kNumTimed = 9;
 
 sdm_status fail(sdm_handle* h, sdm_status code, const std::string& msg) {
