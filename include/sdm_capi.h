@@ -342,11 +342,13 @@ enum {
     SDM_OPT_STAGE_CHUNK = 7,  /* cluster-pair list entries the main pass stages per chunk
                                  (cp.async into shared memory, two chunks ahead): 8, 12 (default)
                                  or 16.  Same pair sets and terms; the autotuner's tile-staging axis. */
-    SDM_OPT_OVERLAP = 8,      /* 2 = the perturbation pass (changed pairs of the displaced particles)
-                                 and the PME reciprocal space run on a second stream branch beside the
+    SDM_OPT_OVERLAP = 8,      /* 2 = the perturbation pass (changed pairs of the displaced particles),
+                                 the exceptions, the PME reciprocal space and the combine (u, soft
+                                 core, bias, mixing weight) run on a second stream branch beside the
                                  list build and the main pass, joined before the finalize (default);
-                                 1 = the branch holds the perturbation pass only and joins before the
-                                 main pass; 0 = one stream.  Identical results. */
+                                 1 = the branch (without the reciprocal space; the combine then
+                                 follows it on the main stream when the system has PME) joins
+                                 before the main pass; 0 = one stream.  Identical results. */
     SDM_OPT_LIST_GROUP = 9    /* z-consecutive i-clusters of a column whose lists one warp of the list
                                  builder builds together (column searches and candidate boxes shared):
                                  1, 2, 4, or 0 = automatic (default: 4).  Identical lists. */
