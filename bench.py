@@ -63,7 +63,7 @@ WORKLOAD = ("config2: 22 replicas x 22,580 particles (7,500 waters + 2x40 ligand
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_pair launch on this
 # workload: a stored figure, the 4-replica ncu capture summarised in
 # profiles/k_pair_config2x4.md scaled by 22/4 (cold cache between replay passes)
-K_PAIR_DRAM_BYTES_PER_LAUNCH = (22.319872e6 + 256.0) * 22 / 4
+K_PAIR_DRAM_BYTES_PER_LAUNCH = (22.318080e6 + 0.0) * 22 / 4
 K_PAIR_TRAFFIC_SOURCE = ("stored: ncu capture of 4 replicas of the same workload x 22/4 "
                          "(profiles/k_pair_config2x4.md)")
 
