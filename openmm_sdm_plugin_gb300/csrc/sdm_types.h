@@ -44,7 +44,7 @@
 #define SDM_LIST_MARGIN 1.0e-4   // nm added to the cutoff in the list filter
 #define SDM_MAX_SPLIT 4
 #define SDM_JG 4                 // largest list-building group (i-clusters of one column, z-consecutive)
-#define SDM_PERT_PARTS 4         // warps per perturbation item (stencil columns split between them)
+#define SDM_PERT_PARTS 2         // warps per perturbation item (stencil columns split between them)
 // per-replica record of the combine (perturbation energy u, soft core, bias)
 #define SDM_CMB_FIELDS 10
 
